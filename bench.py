@@ -1,0 +1,457 @@
+#!/usr/bin/env python
+"""Benchmark of the msplat training step on GB300.
+
+Workload (the headline configuration): one training step of a single view --
+1,000,000 Gaussians with SH degree 3, one 1600x1060 camera (focal 1150 px,
+radius 5), forward RGB + depth + normal (7 channels), loss L1 + 0.2 * L2
+against a fixed random target, backward to every Gaussian parameter and to
+the camera extrinsic (6-DoF quaternion + translation) and intrinsics.  Data
+are seeded synthetic tensors with the stated distributions.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+Prints one JSON line.  ``value`` is training iterations per second with the
+scene resident in HBM (device-timed with CUDA events); ``e2e`` is the same
+metric through the ``MsplatRender`` plug-in with the per-step camera and
+target image copied in from pinned host memory and the loss read back every
+step.  ``--impl reference`` times the CPU float64 rendition of the same step
+(the oracle: the reference operator backend itself is absent) on a bounded
+sample of tiles, on all host cores.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import torch  # noqa: E402
+
+METRIC = "train iters/s & Mpix/s at 1M Gaussians SH3; serve p50/p99 ms vs plain path"
+WORKLOAD = ("single-view training step: 1,000,000 Gaussians SH3, 1600x1060, RGB+depth+normal "
+            "(7 ch), L1+0.2*L2, grads to all Gaussian params + camera extrinsic/intrinsics")
+PEAKS_FALLBACK = {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--n", type=int, default=1_000_000, help="Gaussians (workload default 1M)")
+    ap.add_argument("--cpu-tile-stride", type=int, default=0,
+                    help="CPU sample: blend every k-th tile (0 = choose for ~10-30 s of CPU work)")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+# ----------------------------------------------------------------- dist ---
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def dist_init(world, backend):
+    if world > 1 and not torch.distributed.is_initialized():
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        torch.distributed.init_process_group(backend)
+
+
+def barrier(world):
+    if world > 1:
+        torch.distributed.barrier()
+
+
+def max_over_ranks(x, world, device):
+    if world == 1:
+        return x
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+# --------------------------------------------------------------- clocks ---
+class ClockSampler:
+    """Samples nvidia-smi clocks and throttle reasons while running."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+        return False
+
+    def summary(self):
+        if not self.path or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        rows = []
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                rows.append((float(parts[1]), float(parts[2]), parts[5:9]))
+            except ValueError:
+                continue
+        os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for _, _, flags in rows for i, f in enumerate(flags) if f == "Active"})
+        return {"sm_mhz": statistics.median(r[0] for r in rows), "sm_max_mhz": max(r[1] for r in rows),
+                "reasons": reasons, "samples": len(rows)}
+
+
+# ------------------------------------------------------------- workload ---
+def quat_to_rot(q):
+    q = q / q.norm()
+    w, x, y, z = q.unbind()
+    return torch.stack([
+        torch.stack([1 - 2 * (y * y + z * z), 2 * (x * y - w * z), 2 * (x * z + w * y)]),
+        torch.stack([2 * (x * y + w * z), 1 - 2 * (x * x + z * z), 2 * (y * z - w * x)]),
+        torch.stack([2 * (x * z - w * y), 2 * (y * z + w * x), 1 - 2 * (x * x + y * y)])])
+
+
+def rot_to_quat(R):
+    R = R.double()
+    w = torch.sqrt(torch.clamp(1 + R[0, 0] + R[1, 1] + R[2, 2], min=1e-12)) / 2
+    x = (R[2, 1] - R[1, 2]) / (4 * w)
+    y = (R[0, 2] - R[2, 0]) / (4 * w)
+    z = (R[1, 0] - R[0, 1]) / (4 * w)
+    return torch.stack([w, x, y, z]).float()
+
+
+class CameraParams:
+    """Differentiable camera: wxyz quaternion + translation (6-DoF) and
+    intrinsics, assembled into the world->camera matrix each step."""
+
+    def __init__(self, cam, device, grad=True):
+        self.W, self.H = cam.W, cam.H
+        self.q = rot_to_quat(cam.extr[:3, :3]).to(device).requires_grad_(grad)
+        self.t = cam.extr[:3, 3].clone().to(device).requires_grad_(grad)
+        self.intr = cam.intr.clone().to(device).requires_grad_(grad)
+
+    def extrinsic(self):
+        R = quat_to_rot(self.q)
+        top = torch.cat([R, self.t[:, None]], 1)
+        return torch.cat([top, torch.tensor([[0.0, 0, 0, 1]], device=top.device)], 0)
+
+    def center(self):
+        R = quat_to_rot(self.q)
+        return -(R.T @ self.t)
+
+    def leaves(self):
+        return [self.q, self.t, self.intr]
+
+
+def training_step(renderer, scene, camp, target, WL):
+    pos, sc, q, op, shs = scene.activated()
+    normal = WL.normals_from_scene(sc, q)
+    out = renderer.render_iter(camp.H, camp.W, camp.extrinsic(), camp.intr, camp.center(),
+                               pos, op, sc, q, shs, extra_features={"normal": normal})
+    f = out["rendered_features_split"]
+    img = torch.cat([f["rgb"], f["depth"], f["normal"]], 0)
+    diff = img - target
+    loss = diff.abs().mean() + 0.2 * (diff * diff).mean()
+    loss.backward()
+    return loss
+
+
+def zero_grads(tensors):
+    for t in tensors:
+        t.grad = None
+
+
+# ----------------------------------------------- algorithmic bytes/unit ---
+def blend_fwd_bytes(n, C, K, T, W, H):
+    """Inputs and outputs of one alpha_blending forward, each once: per
+    Gaussian uv 8 + conic 12 + opacity 4 + C features; per list entry a 4 B
+    id; per tile an 8 B range; per pixel C outputs + final T + n_contrib."""
+    return n * (24 + 4 * C) + 4 * K + 8 * T + W * H * (4 * C + 8)
+
+
+def blend_bwd_bytes(n, C, K, T, W, H):
+    """The forward's record (read) and the gradient outputs per Gaussian, ids,
+    ranges, and per pixel dL/dout + final T + n_contrib."""
+    rec = 4 * (16 if C <= 10 else 32)
+    return n * (rec + 24 + 4 * C) + 4 * K + 8 * T + W * H * (4 * C + 8)
+
+
+def sort_bytes(n, K, T):
+    """Depth sort of N (key,value) pairs in four 8-bit passes, emission of K
+    pairs, tile sort in ceil(log2 T / 8) passes, range pass."""
+    passes = 1 if T <= 256 else 2
+    return n * (12 + 4 * 16) + n * 28 + K * 8 + passes * K * 16 + K * 4 + T * 8
+
+
+def load_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            d = json.load(f)
+        return d, "measured"
+    except Exception:
+        return PEAKS_FALLBACK, "fallback"
+
+
+# ------------------------------------------------------ CPU (the oracle) ---
+def cpu_step_time(scene, cam, target, tile_stride, threads):
+    """One float64 CPU training step of the oracle: the per-Gaussian operators
+    and their backward on all N Gaussians, the sort, and blending forward +
+    backward on every ``tile_stride``-th tile, the blending time scaled to all
+    tiles.  Returns (seconds per full step, details)."""
+    from oracle import msplat_cpu as O
+    from pointrix_gb300 import workloads as WL
+
+    torch.set_num_threads(threads)
+    dt = torch.float64
+    leaves = [t.detach().to(dt).requires_grad_(True) for t in
+              (scene.position, scene.log_scale, scene.quat_raw, scene.opacity_logit, scene.shs)]
+    intr = cam.intr.to(dt).requires_grad_(True)
+    extr = cam.extr[:3].to(dt).requires_grad_(True)
+    center = cam.center.to(dt)
+    W, H = cam.W, cam.H
+    gx, gy = O.tile_grid(W, H)
+    T = gx * gy
+    tiles = list(range(0, T, tile_stride))
+    t0 = time.perf_counter()
+    pos, logs, qr, opl, shs = leaves
+    sc = torch.exp(logs)
+    q = qr / qr.norm(dim=1, keepdim=True)
+    op = torch.sigmoid(opl)
+    d = pos - center[None]
+    d = d / d.norm(dim=1, keepdim=True)
+    rgb = (O.compute_sh(shs.permute(0, 2, 1), d) + 0.5).clamp(min=0)
+    uv, depth = O.project_point(pos, intr, extr, W, H, nearest=0.2)
+    vis = depth != 0
+    cov = O.compute_cov3d(sc, q, vis)
+    conic, radius, ntiles = O.ewa_project(pos, cov, intr, extr, uv, W, H, vis)
+    normal = WL.normals_from_scene(sc, q)
+    feat = torch.cat([rgb, depth, normal], 1)
+    t1 = time.perf_counter()
+    ids, rng = O.sort_gaussian(uv.detach(), depth.detach(), W, H, radius, ntiles)
+    t2 = time.perf_counter()
+    bl = [uv, conic, op, feat]
+    bl_in = [x.detach().requires_grad_(True) for x in bl]
+    img = O.alpha_blending(*bl_in, ids, rng, 0.0, W, H, tiles=tiles)
+    diff = img - target.to(dt)
+    loss = diff.abs().mean() + 0.2 * (diff * diff).mean()
+    t3 = time.perf_counter()
+    grads = torch.autograd.grad(loss, bl_in)
+    t4 = time.perf_counter()
+    torch.autograd.backward(bl, grads)
+    t5 = time.perf_counter()
+    blend = (t3 - t2) + (t4 - t3)
+    full = (t1 - t0) + (t2 - t1) + blend * (T / len(tiles)) + (t5 - t4)
+    return full, {"preprocess_fwd_s": t1 - t0, "sort_s": t2 - t1, "blend_sample_s": blend,
+                  "preprocess_bwd_s": t5 - t4, "tiles_sampled": len(tiles), "tiles": T,
+                  "K": int(ids.numel())}
+
+
+def choose_stride(T):
+    # about 1/48 of the tiles keeps one CPU step near 10-20 s on 8-16 cores
+    return max(1, T // 140)
+
+
+def run_reference(args):
+    world, rank, _ = dist_env()
+    if rank != 0:
+        return
+    from pointrix_gb300 import workloads as WL
+
+    scene, cam = WL.scene_train_view(1, n=args.n)
+    g = torch.Generator().manual_seed(7)
+    target = torch.rand(7, cam.H, cam.W, generator=g)
+    T = ((cam.W + 15) // 16) * ((cam.H + 15) // 16)
+    stride = args.cpu_tile_stride or choose_stride(T)
+    threads = len(os.sched_getaffinity(0))
+    for _ in range(args.warmup):
+        cpu_step_time(scene, cam, target, stride, threads)
+    times = []
+    for _ in range(args.steps):
+        s, det = cpu_step_time(scene, cam, target, stride, threads)
+        times.append(s)
+    sec = statistics.mean(times)
+    value = 1.0 / sec
+    sample = (f"float64 oracle step: all {args.n} Gaussians through the per-Gaussian operators and the sort; "
+              f"blending fwd+bwd on every {stride}-th tile ({det['tiles_sampled']} of {det['tiles']}), "
+              f"blending time scaled to all tiles")
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "iters/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": sec * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+        "config": {"workload": WORKLOAD, "gaussians": args.n, "width": cam.W, "height": cam.H,
+                   "channels": 7, "sh_degree": 3, "parallelism": "cpu, host cores"},
+        "cpu_baseline": {"value": value, "unit": "iters/s", "cores": threads, "kind": "port",
+                         "sample": sample, "detail": det},
+        "e2e": {"value": value, "unit": "iters/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }), flush=True)
+
+
+# ------------------------------------------------------------- GPU arm ---
+def run_gb300(args):
+    world, rank, local = dist_env()
+    dist_init(world, "nccl")
+    device = torch.device("cuda", local)
+    torch.cuda.set_device(device)
+    from pointrix_gb300 import ops
+    from pointrix_gb300 import workloads as WL
+    from pointrix_gb300.renderer import MsplatRender
+
+    scene_cpu, cam = WL.scene_train_view(1, n=args.n)
+    scene = scene_cpu.to(device).leaves()
+    camp = CameraParams(cam, device)
+    g = torch.Generator().manual_seed(7)
+    target_cpu = torch.rand(7, cam.H, cam.W, generator=g)
+    target = target_cpu.to(device)
+    renderer = MsplatRender(MsplatRender.Config(render_depth=True, max_sh_degree=3), device=device)
+    renderer.sh_degree = 3
+    params = [scene.position, scene.log_scale, scene.quat_raw, scene.opacity_logit, scene.shs] + camp.leaves()
+    W, H = cam.W, cam.H
+    stream = torch.cuda.current_stream(device)
+
+    for _ in range(max(3, args.warmup)):
+        zero_grads(params)
+        training_step(renderer, scene, camp, target, WL)
+    torch.cuda.synchronize(device)
+
+    # -- device-resident timed region
+    with ClockSampler(device.index) as clocks:
+        barrier(world)
+        torch.cuda.synchronize(device)
+        start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with ops.kernel_timing() as kt:
+            start.record(stream)
+            for _ in range(args.steps):
+                zero_grads(params)
+                training_step(renderer, scene, camp, target, WL)
+            end.record(stream)
+            torch.cuda.synchronize(device)
+        barrier(world)
+    ms = start.elapsed_time(end) / args.steps
+    ms = max_over_ranks(ms, world, device)
+    value = world / (ms / 1e3)
+    ops.check_device_status(device)
+
+    # -- end to end through the plug-in, host buffers
+    target_host = target_cpu.pin_memory()
+    cam_host = [t.detach().cpu().pin_memory() for t in camp.leaves()]
+    loss_host = torch.empty((), dtype=torch.float32).pin_memory()
+    h2d = target_host.numel() * 4 + sum(t.numel() * 4 for t in cam_host)
+    barrier(world)
+    torch.cuda.synchronize(device)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        zero_grads(params)
+        with torch.no_grad():
+            target.copy_(target_host, non_blocking=True)
+            for dst, src in zip(camp.leaves(), cam_host):
+                dst.copy_(src, non_blocking=True)
+        loss = training_step(renderer, scene, camp, target, WL)
+        loss_host.copy_(loss.detach(), non_blocking=True)
+        stream.synchronize()
+    e2e_s = (time.perf_counter() - t0) / args.steps
+    e2e_s = max_over_ranks(e2e_s, world, device)
+    barrier(world)
+
+    # -- dominant kernel and its roofline (live CUDA-event durations)
+    per_op = {name: statistics.mean(kt.ms(name)) for name in kt.names()}
+    calls = {name: len(kt.ms(name)) // args.steps for name in kt.names()}
+    dom = max(per_op, key=lambda k: per_op[k] * calls[k])
+    with torch.no_grad():
+        pos, sc, q, op, shs = scene.activated()
+        uv, depth = ops.project_point(pos, camp.intr, camp.extrinsic()[:3], W, H)
+        vis = depth != 0
+        cov = ops.compute_cov3d(sc, q, vis)
+        conic, radius, tiles = ops.ewa_project(pos, cov, camp.intr, camp.extrinsic()[:3], uv, W, H, vis)
+        K = int(tiles[radius > 0].sum())
+    T = ((W + 15) // 16) * ((H + 15) // 16)
+    n = args.n
+    algo = {"alpha_blending_fwd": blend_fwd_bytes(n, 7, K, T, W, H),
+            "alpha_blending_bwd": blend_bwd_bytes(n, 7, K, T, W, H),
+            "sort_finish": sort_bytes(n, K, T)}
+    peaks, peak_kind = load_peaks()
+    hbm_peak = float(peaks.get("hbm_gbs", PEAKS_FALLBACK["hbm_gbs"]))
+    dom_bytes = algo.get(dom)
+    achieved = dom_bytes / (per_op[dom] * 1e-3) / 1e9 if dom_bytes else None
+    roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                "frac": (achieved / hbm_peak) if achieved else None, "traffic": None,
+                "peak_source": peak_kind, "launch_ms": per_op[dom],
+                "algorithmic_bytes_per_launch": dom_bytes}
+
+    if rank == 0:
+        cpu = None
+        if world == 1 and not args.no_cpu_baseline:
+            stride = args.cpu_tile_stride or choose_stride(T)
+            threads = len(os.sched_getaffinity(0))
+            sec, det = cpu_step_time(scene_cpu, cam, target_cpu, stride, threads)
+            cpu = {"value": 1.0 / sec, "unit": "iters/s", "cores": threads, "kind": "port",
+                   "sample": (f"one float64 oracle step: all Gaussians through the per-Gaussian operators "
+                              f"and the sort; blending fwd+bwd on every {stride}-th tile "
+                              f"({det['tiles_sampled']} of {det['tiles']}), scaled to all tiles"),
+                   "detail": det}
+        line = {
+            "metric": METRIC, "value": value, "unit": "iters/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+            "config": {"workload": WORKLOAD, "gaussians": n, "width": W, "height": H, "channels": 7,
+                       "sh_degree": 3, "K_duplicates": K, "tiles": T,
+                       "l2": "inputs larger than L2 (0.31 GB of Gaussian parameters + 47 MB target per step)",
+                       "parallelism": "replicas" if world > 1 else "single GPU"},
+            "mpix_per_s": value * W * H / 1e6,
+            "e2e": {"value": world / e2e_s, "unit": "iters/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": 4},
+            "roofline": roofline,
+            "per_op_ms": {k: round(v, 4) for k, v in per_op.items()},
+            "gpu_launches": kt.total_launches(),
+            "clocks": clocks.summary(),
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    args = parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gb300(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,167 @@
+/*
+ * pointrix_gb300 -- C ABI of the GB300 (sm_103a) msplat operator kernels.
+ *
+ * Each entry point replaces one operator of the msplat CUDA extension that
+ * Pointrix's MsplatRender calls (pointrix/model/renderer/msplat.py:94-151;
+ * the same six calls in examples/supervise/renderer.py:42-85), split into a
+ * forward and a backward half so that any host language can bind it.  The
+ * Python binding (pointrix_gb300/ops.py) wraps each pair in a
+ * torch.autograd.Function with msplat's signature.
+ *
+ * Conventions for every call:
+ *  - all pointers are device pointers (unless stated), float32 unless typed
+ *    otherwise, densely packed row-major ([N,3] means 3 floats per row);
+ *  - `stream` is a cudaStream_t passed as void*; work is enqueued on it and
+ *    the call returns without synchronising (unless stated);
+ *  - nothing is allocated and no caller memory is freed: scratch is passed
+ *    in, sized by the matching *_scratch_bytes query;
+ *  - the return value is a PGB_* status; a non-zero value means nothing
+ *    useful was written.  Device-side faults that can only be seen after the
+ *    kernels ran are reported through the `info` words named below.
+ */
+#ifndef POINTRIX_GB300_H
+#define POINTRIX_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+  PGB_OK = 0,
+  PGB_ERR_INVALID = 1,   /* bad size, shape, pointer or scratch too small */
+  PGB_ERR_CUDA = 2,      /* a CUDA API call or kernel launch failed */
+  PGB_ERR_OVERFLOW = 3,  /* a device-side bound was exceeded */
+  PGB_ERR_TIMEOUT = 4,   /* a bounded device-side wait gave up */
+  PGB_ERR_MISMATCH = 5   /* tiles_touched disagrees with the uv/radius rectangles */
+};
+
+/* Human-readable name of a status code (static string). */
+const char* pgb_status_string(int status);
+/* ABI version of this library; bumped on any signature change. */
+int pgb_abi_version(void);
+
+/* ---------------------------------------------------------------------
+ * compute_sh -- replaces msplat.compute_sh
+ * (pointrix/model/renderer/msplat.py:104, examples/supervise/renderer.py:42)
+ * sh is [N,3,K] addressed through element strides (sn, sc, sk), so the
+ * permuted view that render_iter passes (strides 3K,1,3) is read in place;
+ * K in {1,4,9,16}.  dirs [N,3] unit view directions.  rgb [N,3] is the raw
+ * SH sum (no +0.5, no clamp).  The backward writes d_sh with the same
+ * strides as sh, and d_dirs [N,3].
+ * ------------------------------------------------------------------- */
+int pgb_compute_sh_forward(const float* sh, int64_t n, int k, int64_t sn, int64_t sc, int64_t sk,
+                           const float* dirs, float* rgb, void* stream);
+int pgb_compute_sh_backward(const float* sh, int64_t n, int k, int64_t sn, int64_t sc, int64_t sk,
+                            const float* dirs, const float* d_rgb, float* d_sh, float* d_dirs,
+                            void* stream);
+
+/* ---------------------------------------------------------------------
+ * project_point -- replaces msplat.project_point
+ * (pointrix/model/renderer/msplat.py:109-113)
+ * xyz [N,3]; intr [4] = fx,fy,cx,cy; extr [3,4] world->camera.
+ * uv [N,2], depth [N,1]; culled points (depth <= nearest, or centre outside
+ * `extent` times the half image) get uv = 0, depth = 0.
+ * The backward writes d_xyz [N,3], d_intr [4], d_extr [12]; it needs
+ * pgb_camera_grad_scratch_bytes() bytes of scratch.
+ * ------------------------------------------------------------------- */
+size_t pgb_camera_grad_scratch_bytes(void);
+int pgb_project_point_forward(const float* xyz, int64_t n, const float* intr, const float* extr,
+                              int width, int height, float nearest, float extent,
+                              float* uv, float* depth, void* stream);
+int pgb_project_point_backward(const float* xyz, int64_t n, const float* intr, const float* extr,
+                               int width, int height, float nearest, float extent,
+                               const float* d_uv, const float* d_depth,
+                               float* d_xyz, float* d_intr, float* d_extr,
+                               void* scratch, size_t scratch_bytes, void* stream);
+
+/* ---------------------------------------------------------------------
+ * compute_cov3d -- replaces msplat.compute_cov3d
+ * (pointrix/model/renderer/msplat.py:118)
+ * scales [N,3] (activated), uquats [N,4] unit wxyz, visible [N] bytes
+ * (0/1).  cov3d [N,6] = upper triangle xx,xy,xz,yy,yz,zz of R S S^T R^T.
+ * ------------------------------------------------------------------- */
+int pgb_compute_cov3d_forward(const float* scales, const float* uquats, const uint8_t* visible,
+                              int64_t n, float* cov3d, void* stream);
+int pgb_compute_cov3d_backward(const float* scales, const float* uquats, const uint8_t* visible,
+                               int64_t n, const float* d_cov3d, float* d_scales, float* d_uquats,
+                               void* stream);
+
+/* ---------------------------------------------------------------------
+ * ewa_project -- replaces msplat.ewa_project
+ * (pointrix/model/renderer/msplat.py:121-130)
+ * conic [N,3] (inverse 2D covariance a,b,c), radius [N] int32 (pixels),
+ * tiles_touched [N] int32 (16x16 tiles).  The backward takes the forward's
+ * radius (0 = culled) and writes d_xyz [N,3], d_cov3d [N,6], d_intr [4],
+ * d_extr [12]; scratch as for project_point.
+ * ------------------------------------------------------------------- */
+int pgb_ewa_project_forward(const float* xyz, const float* cov3d, const float* intr,
+                            const float* extr, const float* uv, const uint8_t* visible, int64_t n,
+                            int width, int height, float* conic, int32_t* radius,
+                            int32_t* tiles_touched, void* stream);
+int pgb_ewa_project_backward(const float* xyz, const float* cov3d, const float* intr,
+                             const float* extr, const int32_t* radius, int64_t n, int width,
+                             int height, const float* d_conic, float* d_xyz, float* d_cov3d,
+                             float* d_intr, float* d_extr, void* scratch, size_t scratch_bytes,
+                             void* stream);
+
+/* ---------------------------------------------------------------------
+ * sort_gaussian -- replaces msplat.sort_gaussian
+ * (pointrix/model/renderer/msplat.py:133-135)
+ * Two calls, because the output length K = sum(tiles_touched) is only known
+ * on the device:
+ *   1. pgb_sort_gaussian_begin writes info[0] = K and info[1] = 0 (int64
+ *      device words) and sorts the Gaussians by depth in scratch_n;
+ *   2. the caller reads K back, then pgb_sort_gaussian_finish writes
+ *      ids_out [K] int32 (Gaussian ids ordered by tile, then depth, then id)
+ *      and tile_range_out [T,2] int32 ([start,end) per 16x16 tile, [0,0] if
+ *      empty, T = ceil(W/16) * ceil(H/16)).
+ * After finish, info[1] holds a PGB_* status raised on the device
+ * (PGB_ERR_TIMEOUT, PGB_ERR_MISMATCH, PGB_ERR_OVERFLOW) or 0.
+ * Scratch: bytes_n for (n), bytes_k for (k); pass k = 0 to size bytes_n.
+ * ------------------------------------------------------------------- */
+int pgb_sort_scratch_bytes(int64_t n, int64_t k, int width, int height, size_t* bytes_n,
+                           size_t* bytes_k);
+int pgb_sort_gaussian_begin(const float* depth, const int32_t* radius,
+                            const int32_t* tiles_touched, int64_t n, int width, int height,
+                            void* scratch_n, size_t bytes_n, int64_t* info, void* stream);
+int pgb_sort_gaussian_finish(const float* uv, const int32_t* radius, const int32_t* tiles_touched,
+                             int64_t n, int width, int height, int64_t k, void* scratch_n,
+                             size_t bytes_n, void* scratch_k, size_t bytes_k, int64_t* info,
+                             int32_t* ids_out, int32_t* tile_range_out, void* stream);
+
+/* ---------------------------------------------------------------------
+ * alpha_blending -- replaces msplat.alpha_blending
+ * (pointrix/model/renderer/msplat.py:148-151)
+ * uv [N,2], conic [N,3], opacity [N,1], feature [N,C] (1 <= C <= 26),
+ * ids [K], tile_range [T,2] from sort_gaussian, bg added to every channel
+ * with the final transmittance.  The forward packs one record of
+ * pgb_blend_record_floats(C) floats per Gaussian into `records` (kept for
+ * the backward) and writes out [C,H,W], final_T [H,W] and n_contrib [H,W]
+ * (list entries up to the last contributor).  The backward writes d_uv
+ * [N,2] (also the gradient msplat routes to its `ndc` argument), d_conic
+ * [N,3], d_opacity [N,1], d_feature [N,C]; grad_records is scratch of the
+ * same size as records.  `info` is one device int64 word that the caller
+ * zeroes beforehand; a bounded device-side wait that expires writes
+ * PGB_ERR_TIMEOUT into it.
+ * ------------------------------------------------------------------- */
+int pgb_blend_record_floats(int channels);
+int pgb_alpha_blending_forward(const float* uv, const float* conic, const float* opacity,
+                               const float* feature, int64_t n, int channels, const int32_t* ids,
+                               int64_t k, const int32_t* tile_range, float bg, int width,
+                               int height, float* records, float* out, float* final_T,
+                               int32_t* n_contrib, int64_t* info, void* stream);
+int pgb_alpha_blending_backward(const float* records, int64_t n, int channels,
+                                const int32_t* ids, int64_t k, const int32_t* tile_range, float bg,
+                                int width, int height, const float* final_T,
+                                const int32_t* n_contrib, const float* d_out, float* grad_records,
+                                float* d_uv, float* d_conic, float* d_opacity, float* d_feature,
+                                int64_t* info, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* POINTRIX_GB300_H */

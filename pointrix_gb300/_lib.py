@@ -1,0 +1,71 @@
+"""ctypes binding of ``libpointrix_gb300.so`` (the C ABI in
+``include/pointrix_gb300.h``).
+
+The library is built in-tree by :mod:`pointrix_gb300.build`.  There is no
+fallback: if the library is missing or fails to load, every operator raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import threading
+
+from . import build as _build
+
+_lock = threading.Lock()
+_lib = None
+
+i32, i64, f32, szt = C.c_int, C.c_int64, C.c_float, C.c_size_t
+vp = C.c_void_p
+
+# name -> argtypes (restype int unless listed in _RESTYPES)
+SIGNATURES = {
+    "pgb_status_string": [i32],
+    "pgb_abi_version": [],
+    "pgb_compute_sh_forward": [vp, i64, i32, i64, i64, i64, vp, vp, vp],
+    "pgb_compute_sh_backward": [vp, i64, i32, i64, i64, i64, vp, vp, vp, vp, vp],
+    "pgb_camera_grad_scratch_bytes": [],
+    "pgb_project_point_forward": [vp, i64, vp, vp, i32, i32, f32, f32, vp, vp, vp],
+    "pgb_project_point_backward": [vp, i64, vp, vp, i32, i32, f32, f32, vp, vp, vp, vp, vp, vp, szt, vp],
+    "pgb_compute_cov3d_forward": [vp, vp, vp, i64, vp, vp],
+    "pgb_compute_cov3d_backward": [vp, vp, vp, i64, vp, vp, vp, vp],
+    "pgb_ewa_project_forward": [vp, vp, vp, vp, vp, vp, i64, i32, i32, vp, vp, vp, vp],
+    "pgb_ewa_project_backward": [vp, vp, vp, vp, vp, i64, i32, i32, vp, vp, vp, vp, vp, vp, szt, vp],
+    "pgb_sort_scratch_bytes": [i64, i64, i32, i32, C.POINTER(szt), C.POINTER(szt)],
+    "pgb_sort_gaussian_begin": [vp, vp, vp, i64, i32, i32, vp, szt, vp, vp],
+    "pgb_sort_gaussian_finish": [vp, vp, vp, i64, i32, i32, i64, vp, szt, vp, szt, vp, vp, vp, vp],
+    "pgb_blend_record_floats": [i32],
+    "pgb_alpha_blending_forward": [vp, vp, vp, vp, i64, i32, vp, i64, vp, f32, i32, i32, vp, vp, vp, vp, vp, vp],
+    "pgb_alpha_blending_backward": [vp, i64, i32, vp, i64, vp, f32, i32, i32, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp],
+}
+_RESTYPES = {"pgb_status_string": C.c_char_p, "pgb_camera_grad_scratch_bytes": szt}
+
+
+class PgbError(RuntimeError):
+    """A non-zero status from the GB300 kernel library."""
+
+
+def lib():
+    """The loaded library (built first if needed)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    with _lock:
+        if _lib is None:
+            path = _build.build()
+            handle = C.CDLL(str(path))
+            for name, args in SIGNATURES.items():
+                fn = getattr(handle, name)
+                fn.argtypes = args
+                fn.restype = _RESTYPES.get(name, i32)
+            _lib = handle
+    return _lib
+
+
+def check(status: int, what: str) -> None:
+    if status != 0:
+        msg = lib().pgb_status_string(status).decode()
+        raise PgbError(f"{what}: {msg} (status {status})")
+
+
+def call(name: str, *args) -> None:
+    check(getattr(lib(), name)(*args), name)

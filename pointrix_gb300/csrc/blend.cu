@@ -1,0 +1,544 @@
+// alpha_blending: per-tile front-to-back compositing of N-channel features,
+// forward and backward.
+//
+// Contract (pointrix/model/renderer/msplat.py:141-151, channel packing in
+// pointrix/model/renderer/utils/renderer_utils.py:30-71): for each pixel of
+// a 16x16 tile, walk the tile's depth-sorted Gaussians; alpha =
+// min(0.99, o exp(power)), power = -(a dx^2 + c dy^2)/2 - b dx dy with
+// d = uv - pixel (pixel centres on integer coordinates); skip power > 0 or
+// alpha < 1/255; stop before the Gaussian that would take the transmittance
+// T below 1e-4; out_c = sum f_c alpha T + T_final bg.  The backward is the
+// exact gradient of that function (including the background term and the
+// 0.99 clamp), replayed back to front from the stored final T and
+// last-contributor count.
+//
+// GB300 design:
+//  * pack: one pass writes a 64- or 128-byte record per Gaussian
+//    (u, v, a, b, c, o, f_0..f_{C-1}, zero padding) so that a splat is one
+//    16-byte aligned contiguous block;
+//  * forward/backward: one CTA of 256 threads per tile, one pixel per
+//    thread.  The tile's sorted ids are consumed in batches of 256; each
+//    thread issues a TMA bulk copy (cp.async.bulk, no multicast) of one
+//    record into a double-buffered shared-memory stage that completes on an
+//    mbarrier, so batch b+1 streams in while batch b is composited.  Every
+//    mbarrier wait is bounded; on expiry the CTA records PGB_ERR_TIMEOUT,
+//    drains its own copies (bounded again) and returns;
+//  * forward early exit per CTA (__syncthreads_count) and per warp;
+//  * backward: per-Gaussian gradients are summed across the warp with a
+//    reduce-scatter butterfly (16 shuffles for 16 values instead of 80),
+//    then across warps with shared-memory atomics, then flushed once per
+//    (tile, Gaussian) with 16-byte vector atomics into a gradient record.
+#include "pgb_common.cuh"
+
+namespace pgb {
+
+constexpr int kBlendThreads = 256;
+constexpr int kBatch = 256;
+constexpr uint32_t kWaitLimit = 1u << 22;
+
+// ---------------------------------------------------------------- PTX helpers
+__device__ inline uint32_t smem_addr(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ inline void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count)
+               : "memory");
+}
+__device__ inline void fence_mbar_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ inline void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)),
+               "r"(bytes)
+               : "memory");
+}
+__device__ inline bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_addr(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+__device__ inline bool mbar_wait_bounded(uint64_t* bar, uint32_t parity) {
+  for (uint32_t i = 0; i < kWaitLimit; ++i)
+    if (mbar_try_wait(bar, parity)) return true;
+  return false;
+}
+// Global -> shared bulk copy (TMA, non-tensor form): 16-byte aligned
+// addresses, size a multiple of 16; completion counted on `bar`.
+__device__ inline void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
+          "r"(smem_addr(dst)),
+      "l"(src), "r"(bytes), "r"(smem_addr(bar))
+      : "memory");
+}
+
+__device__ inline void set_info(int64_t* info, int code) {
+  if (info) atomicCAS(reinterpret_cast<unsigned long long*>(info), 0ull, (unsigned long long)code);
+}
+
+// Power and alpha of one (pixel, splat) pair, written with explicit
+// rounding intrinsics so that the forward and the backward take identical
+// skip/stop decisions whatever the compiler contracts elsewhere.
+__device__ __forceinline__ float splat_power(float a, float b, float c, float dx, float dy) {
+  const float q = __fmaf_rn(__fmul_rn(a, dx), dx, __fmul_rn(__fmul_rn(c, dy), dy));
+  const float bxy = __fmul_rn(__fmul_rn(b, dx), dy);
+  return __fmaf_rn(-0.5f, q, -bxy);
+}
+
+// Issue the bulk copies of one batch: thread t fetches the record of list
+// entry first + t (if below last) into stage slot t.  One arrive per warp
+// carries the warp's byte count (the barrier expects kBlendThreads/32
+// arrivals per phase).
+template <int RF>
+__device__ inline void issue_batch(const float* __restrict__ records,
+                                   const int32_t* __restrict__ ids, int64_t first, int64_t last,
+                                   float* stage, uint64_t* bar) {
+  const int lane = threadIdx.x & 31;
+  const int64_t e = first + threadIdx.x;
+  const bool valid = e < last;
+  const uint32_t ballot = __ballot_sync(0xffffffffu, valid);
+  if (lane == 0) mbar_arrive_expect_tx(bar, (uint32_t)__popc(ballot) * RF * 4u);
+  __syncwarp();
+  if (valid) {
+    const int32_t g = ids[e];
+    bulk_g2s(stage + threadIdx.x * RF, records + (int64_t)g * RF, RF * 4u, bar);
+  }
+}
+
+// ------------------------------------------------------------------ pack
+template <int RF>
+__global__ void pack_kernel(const float* __restrict__ uv, const float* __restrict__ conic,
+                            const float* __restrict__ opacity, const float* __restrict__ feature,
+                            int64_t n, int C, float* __restrict__ records) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    float r[RF];
+    r[0] = uv[2 * i];
+    r[1] = uv[2 * i + 1];
+    r[2] = conic[3 * i];
+    r[3] = conic[3 * i + 1];
+    r[4] = conic[3 * i + 2];
+    r[5] = opacity[i];
+#pragma unroll
+    for (int c = 0; c < RF - 6; ++c) r[6 + c] = c < C ? feature[i * C + c] : 0.f;
+    float4* o = reinterpret_cast<float4*>(records + i * RF);
+#pragma unroll
+    for (int q = 0; q < RF / 4; ++q) o[q] = make_float4(r[4 * q], r[4 * q + 1], r[4 * q + 2], r[4 * q + 3]);
+  }
+}
+
+// --------------------------------------------------------------- forward
+template <int NC, int RF>
+__global__ void __launch_bounds__(kBlendThreads) blend_fwd_kernel(
+    const float* __restrict__ records, const int32_t* __restrict__ ids,
+    const int2* __restrict__ ranges, float bg, int W, int H, int C, float* __restrict__ out,
+    float* __restrict__ final_T, int32_t* __restrict__ n_contrib, int64_t* __restrict__ info) {
+  extern __shared__ __align__(128) float smem[];
+  __shared__ __align__(8) uint64_t bars[2];
+
+  const int gx = grid_x(W);
+  const int tile = blockIdx.x;
+  const int px = (tile % gx) * kTile + (threadIdx.x & 15);
+  const int py = (tile / gx) * kTile + (threadIdx.x >> 4);
+  const bool inside = px < W && py < H;
+  const float pxf = (float)px, pyf = (float)py;
+
+  if (threadIdx.x == 0) {
+    mbar_init(&bars[0], kBlendThreads / 32);
+    mbar_init(&bars[1], kBlendThreads / 32);
+    fence_mbar_init();
+  }
+  __syncthreads();
+
+  const int2 rg = ranges[tile];
+  const int64_t start = rg.x, end = rg.y;
+  const int nb = end > start ? (int)((end - start + kBatch - 1) / kBatch) : 0;
+
+  float acc[NC];
+#pragma unroll
+  for (int c = 0; c < NC; ++c) acc[c] = 0.f;
+  float T = 1.f;
+  int last = 0;
+  bool done = !inside;
+  bool timed_out = false;
+
+  if (nb > 0) issue_batch<RF>(records, ids, start, end, smem, &bars[0]);
+  for (int b = 0; b < nb; ++b) {
+    const int buf = b & 1;
+    const int64_t first = start + (int64_t)b * kBatch;
+    if (b + 1 < nb) issue_batch<RF>(records, ids, first + kBatch, end, smem + (buf ^ 1) * kBatch * RF, &bars[buf ^ 1]);
+    // every thread observes the phase (that makes the TMA writes visible to
+    // it); the outcome is made block-uniform before any warp collective
+    timed_out = __syncthreads_or(!mbar_wait_bounded(&bars[buf], (b >> 1) & 1));
+    if (timed_out && threadIdx.x == 0) set_info(info, PGB_ERR_TIMEOUT);
+    const int cnt = (int)(end - first < kBatch ? end - first : kBatch);
+    const float* st = smem + buf * kBatch * RF;
+    if (!timed_out && !__all_sync(0xffffffffu, done)) {
+      if (!done) {
+        for (int j = 0; j < cnt; ++j) {
+          const float4 r0 = *reinterpret_cast<const float4*>(st + j * RF);
+          const float2 r1 = *reinterpret_cast<const float2*>(st + j * RF + 4);
+          const float dx = __fsub_rn(r0.x, pxf), dy = __fsub_rn(r0.y, pyf);
+          const float power = splat_power(r0.z, r0.w, r1.x, dx, dy);
+          if (power > 0.f) continue;
+          const float alpha = fminf(0.99f, __fmul_rn(r1.y, __expf(power)));
+          if (alpha < (1.0f / 255.0f)) continue;
+          const float test_T = __fmul_rn(T, __fsub_rn(1.0f, alpha));
+          if (test_T < 1e-4f) {
+            done = true;
+            break;
+          }
+          const float w = alpha * T;
+          const float* f = st + j * RF + 6;
+#pragma unroll
+          for (int c = 0; c < NC; ++c) acc[c] = fmaf(f[c], w, acc[c]);
+          T = test_T;
+          last = (int)(first - start) + j + 1;
+        }
+      }
+    }
+    const int ndone = __syncthreads_count(done || timed_out);
+    if (ndone == kBlendThreads || timed_out) {
+      if (b + 1 < nb && !mbar_wait_bounded(&bars[buf ^ 1], ((b + 1) >> 1) & 1))
+        set_info(info, PGB_ERR_TIMEOUT);
+      break;
+    }
+  }
+
+  if (inside) {
+    const int64_t pix = (int64_t)py * W + px;
+    const int64_t plane = (int64_t)W * H;
+#pragma unroll
+    for (int c = 0; c < NC; ++c)
+      if (c < C) out[c * plane + pix] = acc[c] + T * bg;
+    final_T[pix] = T;
+    n_contrib[pix] = last;
+  }
+}
+
+// ------------------------------------------------------------- backward
+// Warp reduce-scatter: on return lane L holds the warp sum of value
+// (GR == 32 ? L : (L >> 1) & 15) in v[0].
+template <int GR>
+__device__ __forceinline__ float warp_reduce_scatter(float (&v)[GR]) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int off = 16, m = GR / 2; m >= 1; off >>= 1, m >>= 1) {
+    const bool upper = (lane & off) != 0;
+#pragma unroll
+    for (int i = 0; i < m; ++i) {
+      const float send = upper ? v[i] : v[i + m];
+      const float keep = upper ? v[i + m] : v[i];
+      v[i] = keep + __shfl_xor_sync(0xffffffffu, send, off);
+    }
+  }
+  if constexpr (GR == 16) v[0] += __shfl_xor_sync(0xffffffffu, v[0], 1);
+  return v[0];
+}
+
+template <int NC, int RF>
+__global__ void __launch_bounds__(kBlendThreads) blend_bwd_kernel(
+    const float* __restrict__ records, const int32_t* __restrict__ ids,
+    const int2* __restrict__ ranges, float bg, int W, int H, int C,
+    const float* __restrict__ final_T, const int32_t* __restrict__ n_contrib,
+    const float* __restrict__ d_out, float* __restrict__ grad_records,
+    int64_t* __restrict__ info) {
+  static_assert(RF == 16 || RF == 32, "gradient records are 16 or 32 floats");
+  extern __shared__ __align__(128) float smem[];
+  __shared__ __align__(8) uint64_t bars[2];
+  __shared__ int s_max_nc;
+  __shared__ uint8_t s_touched[kBatch];
+  float* gacc = smem + 2 * kBatch * RF;  // [kBatch][RF]
+
+  const int gx = grid_x(W);
+  const int tile = blockIdx.x;
+  const int px = (tile % gx) * kTile + (threadIdx.x & 15);
+  const int py = (tile / gx) * kTile + (threadIdx.x >> 4);
+  const bool inside = px < W && py < H;
+  const float pxf = (float)px, pyf = (float)py;
+  const int lane = threadIdx.x & 31;
+
+  if (threadIdx.x == 0) {
+    mbar_init(&bars[0], kBlendThreads / 32);
+    mbar_init(&bars[1], kBlendThreads / 32);
+    fence_mbar_init();
+    s_max_nc = 0;
+  }
+  for (int i = threadIdx.x; i < kBatch * RF; i += kBlendThreads) gacc[i] = 0.f;
+  s_touched[threadIdx.x] = 0;
+  __syncthreads();
+
+  const int64_t pix = (int64_t)py * W + px;
+  const int64_t plane = (int64_t)W * H;
+  float T = 1.f;
+  int nc = 0;
+  float dout[NC], Bk[NC];
+#pragma unroll
+  for (int c = 0; c < NC; ++c) {
+    dout[c] = 0.f;
+    Bk[c] = bg;
+  }
+  if (inside) {
+    T = final_T[pix];
+    nc = n_contrib[pix];
+#pragma unroll
+    for (int c = 0; c < NC; ++c)
+      if (c < C) dout[c] = d_out[c * plane + pix];
+    atomicMax(&s_max_nc, nc);
+  }
+  __syncthreads();
+  const int2 rg = ranges[tile];
+  const int64_t start = rg.x;
+  const int max_nc = s_max_nc;
+  const int nb = (max_nc + kBatch - 1) / kBatch;
+
+  // batch b covers list positions [hi_b - kBatch, hi_b) with hi_b = max_nc - b*kBatch,
+  // clipped at 0; slot t holds position lo_b + t.
+  auto lo_of = [&](int b) { return max(0, max_nc - (b + 1) * kBatch); };
+  auto hi_of = [&](int b) { return max_nc - b * kBatch; };
+
+  bool timed_out = false;
+  if (nb > 0) issue_batch<RF>(records, ids, start + lo_of(0), start + hi_of(0), smem, &bars[0]);
+  for (int b = 0; b < nb; ++b) {
+    const int buf = b & 1;
+    const int lo = lo_of(b), hi = hi_of(b);
+    if (b + 1 < nb)
+      issue_batch<RF>(records, ids, start + lo_of(b + 1), start + hi_of(b + 1), smem + (buf ^ 1) * kBatch * RF,
+                      &bars[buf ^ 1]);
+    timed_out = __syncthreads_or(!mbar_wait_bounded(&bars[buf], (b >> 1) & 1));
+    if (timed_out && threadIdx.x == 0) set_info(info, PGB_ERR_TIMEOUT);
+    const float* st = smem + buf * kBatch * RF;
+    if (!timed_out) {
+      for (int j = hi - 1; j >= lo; --j) {
+        const int slot = j - lo;
+        float v[RF];
+#pragma unroll
+        for (int q = 0; q < RF; ++q) v[q] = 0.f;
+        bool contrib = false;
+        if (j < nc) {
+          const float4 r0 = *reinterpret_cast<const float4*>(st + slot * RF);
+          const float2 r1 = *reinterpret_cast<const float2*>(st + slot * RF + 4);
+          const float dx = __fsub_rn(r0.x, pxf), dy = __fsub_rn(r0.y, pyf);
+          const float power = splat_power(r0.z, r0.w, r1.x, dx, dy);
+          if (power <= 0.f) {
+            const float G = __expf(power);
+            const float araw = __fmul_rn(r1.y, G);
+            const float alpha = fminf(0.99f, araw);
+            if (alpha >= (1.0f / 255.0f)) {
+              contrib = true;
+              const float om = __fsub_rn(1.0f, alpha);
+              T = __fdividef(T, om);
+              const float* f = st + slot * RF + 6;
+              float dalpha = 0.f;
+              const float wT = alpha * T;
+#pragma unroll
+              for (int c = 0; c < NC; ++c) {
+                dalpha = fmaf(dout[c], f[c] - Bk[c], dalpha);
+                Bk[c] = fmaf(alpha, f[c], om * Bk[c]);
+                v[6 + c] = wT * dout[c];
+              }
+              dalpha *= T;
+              if (araw < 0.99f) {
+                const float dpow = alpha * dalpha;
+                v[5] = G * dalpha;
+                v[2] = -0.5f * dx * dx * dpow;
+                v[3] = -dx * dy * dpow;
+                v[4] = -0.5f * dy * dy * dpow;
+                v[0] = (-r0.z * dx - r0.w * dy) * dpow;
+                v[1] = (-r1.x * dy - r0.w * dx) * dpow;
+              }
+            }
+          }
+        }
+        if (__any_sync(0xffffffffu, contrib)) {
+          const float s = warp_reduce_scatter<RF>(v);
+          if (RF == 32) {
+            if (lane < 6 + NC) atomicAdd(&gacc[slot * RF + lane], s);
+          } else if ((lane & 1) == 0 && (lane >> 1) < 6 + NC) {
+            atomicAdd(&gacc[slot * RF + (lane >> 1)], s);
+          }
+          if (lane == 0) s_touched[slot] = 1;
+        }
+      }
+    }
+    __syncthreads();
+    // flush this batch's per-splat sums: one set of vector atomics per splat
+    const int t = threadIdx.x;
+    if (t < hi - lo && s_touched[t]) {
+      const int32_t g = ids[start + lo + t];
+      float4* dst = reinterpret_cast<float4*>(grad_records + (int64_t)g * RF);
+      float4* srcv = reinterpret_cast<float4*>(gacc + t * RF);
+#pragma unroll
+      for (int q = 0; q < (6 + NC + 3) / 4; ++q) {
+        atomicAdd(dst + q, srcv[q]);
+        srcv[q] = make_float4(0.f, 0.f, 0.f, 0.f);
+      }
+      s_touched[t] = 0;
+    }
+    __syncthreads();
+    if (timed_out) {
+      if (b + 1 < nb && !mbar_wait_bounded(&bars[buf ^ 1], ((b + 1) >> 1) & 1))
+        set_info(info, PGB_ERR_TIMEOUT);
+      break;
+    }
+  }
+}
+
+// ---------------------------------------------------------------- unpack
+template <int RF>
+__global__ void unpack_kernel(const float* __restrict__ g, int64_t n, int C,
+                              float* __restrict__ d_uv, float* __restrict__ d_conic,
+                              float* __restrict__ d_opacity, float* __restrict__ d_feature) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    float r[RF];
+    const float4* s = reinterpret_cast<const float4*>(g + i * RF);
+#pragma unroll
+    for (int q = 0; q < RF / 4; ++q) {
+      const float4 x = s[q];
+      r[4 * q] = x.x; r[4 * q + 1] = x.y; r[4 * q + 2] = x.z; r[4 * q + 3] = x.w;
+    }
+    reinterpret_cast<float2*>(d_uv)[i] = make_float2(r[0], r[1]);
+    d_conic[3 * i] = r[2];
+    d_conic[3 * i + 1] = r[3];
+    d_conic[3 * i + 2] = r[4];
+    d_opacity[i] = r[5];
+#pragma unroll
+    for (int c = 0; c < RF - 6; ++c)
+      if (c < C) d_feature[i * C + c] = r[6 + c];
+  }
+}
+
+// ------------------------------------------------------------- dispatch
+inline int record_floats(int C) { return C <= 10 ? 16 : 32; }
+
+template <int NC>
+static int launch_fwd_nc(const float* records, const int32_t* ids, const int2* ranges, float bg,
+                         int W, int H, int C, float* out, float* fT, int32_t* ncon,
+                         int64_t* info, cudaStream_t s) {
+  constexpr int RF = NC <= 10 ? 16 : 32;
+  const int tiles = grid_x(W) * grid_y(H);
+  const size_t smem = 2 * kBatch * RF * sizeof(float);
+  auto kern = blend_fwd_kernel<NC, RF>;
+  if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+      cudaSuccess)
+    return PGB_ERR_CUDA;
+  kern<<<tiles, kBlendThreads, smem, s>>>(records, ids, ranges, bg, W, H, C, out, fT, ncon, info);
+  return launch_status();
+}
+
+template <int NC>
+static int launch_bwd_nc(const float* records, const int32_t* ids, const int2* ranges, float bg,
+                         int W, int H, int C, const float* fT, const int32_t* ncon,
+                         const float* dout, float* grec, int64_t* info, cudaStream_t s) {
+  constexpr int RF = NC <= 10 ? 16 : 32;
+  const int tiles = grid_x(W) * grid_y(H);
+  const size_t smem = 3 * kBatch * RF * sizeof(float);
+  auto kern = blend_bwd_kernel<NC, RF>;
+  if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+      cudaSuccess)
+    return PGB_ERR_CUDA;
+  kern<<<tiles, kBlendThreads, smem, s>>>(records, ids, ranges, bg, W, H, C, fT, ncon, dout, grec,
+                                          info);
+  return launch_status();
+}
+
+// Channel counts with a compiled kernel; other counts round up (extra
+// channels are zero in the records and never written out).
+#define PGB_FOR_NC(X) X(1) X(3) X(4) X(7) X(8) X(10) X(16) X(26)
+
+inline int nc_bucket(int C) {
+  const int b[] = {1, 3, 4, 7, 8, 10, 16, 26};
+  for (int x : b)
+    if (C <= x) return x;
+  return -1;
+}
+
+}  // namespace pgb
+
+using namespace pgb;
+
+extern "C" {
+
+int pgb_blend_record_floats(int channels) {
+  if (channels < 1 || channels > 26) return -1;
+  return record_floats(channels);
+}
+
+int pgb_alpha_blending_forward(const float* uv, const float* conic, const float* opacity,
+                               const float* feature, int64_t n, int channels, const int32_t* ids,
+                               int64_t k, const int32_t* tile_range, float bg, int width,
+                               int height, float* records, float* out, float* final_T,
+                               int32_t* n_contrib, int64_t* info, void* stream) {
+  const int nc = nc_bucket(channels);
+  if (n < 0 || k < 0 || width <= 0 || height <= 0 || channels < 1 || nc < 0) return PGB_ERR_INVALID;
+  if (!tile_range || !out || !final_T || !n_contrib || (k > 0 && !ids)) return PGB_ERR_INVALID;
+  if (n > 0 && (!uv || !conic || !opacity || !feature || !records)) return PGB_ERR_INVALID;
+  cudaStream_t s = as_stream(stream);
+  const int RF = record_floats(channels);
+  if (n > 0) {
+    if (RF == 16)
+      pack_kernel<16><<<stream_grid(n), kStreamThreads, 0, s>>>(uv, conic, opacity, feature, n,
+                                                                channels, records);
+    else
+      pack_kernel<32><<<stream_grid(n), kStreamThreads, 0, s>>>(uv, conic, opacity, feature, n,
+                                                                channels, records);
+  }
+  const int2* rg = reinterpret_cast<const int2*>(tile_range);
+  switch (nc) {
+#define PGB_CASE(N) \
+  case N:           \
+    return launch_fwd_nc<N>(records, ids, rg, bg, width, height, channels, out, final_T, n_contrib, info, s);
+    PGB_FOR_NC(PGB_CASE)
+#undef PGB_CASE
+    default:
+      return PGB_ERR_INVALID;
+  }
+}
+
+int pgb_alpha_blending_backward(const float* records, int64_t n, int channels,
+                                const int32_t* ids, int64_t k, const int32_t* tile_range, float bg,
+                                int width, int height, const float* final_T,
+                                const int32_t* n_contrib, const float* d_out, float* grad_records,
+                                float* d_uv, float* d_conic, float* d_opacity, float* d_feature,
+                                int64_t* info, void* stream) {
+  const int nc = nc_bucket(channels);
+  if (n < 0 || k < 0 || width <= 0 || height <= 0 || channels < 1 || nc < 0) return PGB_ERR_INVALID;
+  if (!tile_range || !final_T || !n_contrib || !d_out || (k > 0 && !ids)) return PGB_ERR_INVALID;
+  if (n > 0 && (!records || !grad_records || !d_uv || !d_conic || !d_opacity || !d_feature))
+    return PGB_ERR_INVALID;
+  if (n == 0) return PGB_OK;
+  cudaStream_t s = as_stream(stream);
+  const int RF = record_floats(channels);
+  if (cudaMemsetAsync(grad_records, 0, (size_t)n * RF * sizeof(float), s) != cudaSuccess)
+    return PGB_ERR_CUDA;
+  const int2* rg = reinterpret_cast<const int2*>(tile_range);
+  int st = PGB_ERR_INVALID;
+  switch (nc) {
+#define PGB_CASE(N)                                                                          \
+  case N:                                                                                    \
+    st = launch_bwd_nc<N>(records, ids, rg, bg, width, height, channels, final_T, n_contrib, \
+                          d_out, grad_records, info, s);                                     \
+    break;
+    PGB_FOR_NC(PGB_CASE)
+#undef PGB_CASE
+    default:
+      break;
+  }
+  if (st != PGB_OK) return st;
+  if (RF == 16)
+    unpack_kernel<16><<<stream_grid(n), kStreamThreads, 0, s>>>(grad_records, n, channels, d_uv,
+                                                                d_conic, d_opacity, d_feature);
+  else
+    unpack_kernel<32><<<stream_grid(n), kStreamThreads, 0, s>>>(grad_records, n, channels, d_uv,
+                                                                d_conic, d_opacity, d_feature);
+  return launch_status();
+}
+
+}  // extern "C"

@@ -1,0 +1,294 @@
+// compute_sh: real spherical-harmonic colour, forward and backward.
+//
+// Contract: pointrix/model/renderer/msplat.py:99-105 passes the [N,3,K]
+// permuted view of get_shs' [N,K,3] storage (element strides 3K,1,3) and
+// unit view directions; the op returns the raw sum sum_k c_k Y_k(d) (the
+// caller adds 0.5 and clamps).  The basis is the real SH basis up to degree
+// 3 with the sign convention of the 3D Gaussian Splatting renderer; the
+// constants are the normalisation factors sqrt((2l+1)/(4 pi) ...) written
+// out to double precision.
+//
+// One thread per Gaussian.  For the two dense layouts ([N,K,3] storage seen
+// through the permute, or a contiguous [N,3,K]) the 3K coefficients of a
+// Gaussian are one contiguous, 16-byte aligned block and are moved with
+// float4 loads and stores; any other stride pattern takes a scalar path.
+#include "pgb_common.cuh"
+
+namespace pgb {
+
+constexpr float C0 = 0.28209479177387814f;
+constexpr float C1 = 0.4886025119029199f;
+constexpr float C2_0 = 1.0925484305920792f;
+constexpr float C2_1 = -1.0925484305920792f;
+constexpr float C2_2 = 0.31539156525252005f;
+constexpr float C2_3 = -1.0925484305920792f;
+constexpr float C2_4 = 0.5462742152960396f;
+constexpr float C3_0 = -0.5900435899266435f;
+constexpr float C3_1 = 2.890611442640554f;
+constexpr float C3_2 = -0.4570457994644658f;
+constexpr float C3_3 = 0.3731763325901154f;
+constexpr float C3_4 = -0.4570457994644658f;
+constexpr float C3_5 = 1.445305721320277f;
+constexpr float C3_6 = -0.5900435899266435f;
+
+template <int K>
+__device__ inline void sh_basis(float x, float y, float z, float (&Y)[K]) {
+  Y[0] = C0;
+  if constexpr (K > 1) {
+    Y[1] = -C1 * y;
+    Y[2] = C1 * z;
+    Y[3] = -C1 * x;
+  }
+  if constexpr (K > 4) {
+    const float xx = x * x, yy = y * y, zz = z * z;
+    Y[4] = C2_0 * (x * y);
+    Y[5] = C2_1 * (y * z);
+    Y[6] = C2_2 * (2.f * zz - xx - yy);
+    Y[7] = C2_3 * (x * z);
+    Y[8] = C2_4 * (xx - yy);
+    if constexpr (K > 9) {
+      Y[9] = C3_0 * y * (3.f * xx - yy);
+      Y[10] = C3_1 * (x * y) * z;
+      Y[11] = C3_2 * y * (4.f * zz - xx - yy);
+      Y[12] = C3_3 * z * (2.f * zz - 3.f * xx - 3.f * yy);
+      Y[13] = C3_4 * x * (4.f * zz - xx - yy);
+      Y[14] = C3_5 * z * (xx - yy);
+      Y[15] = C3_6 * x * (xx - 3.f * yy);
+    }
+  }
+}
+
+// d(sum_k G_k Y_k)/d(x,y,z) for given per-basis weights G.
+template <int K>
+__device__ inline void sh_basis_grad(float x, float y, float z, const float (&G)[K], float& gx,
+                                     float& gy, float& gz) {
+  gx = gy = gz = 0.f;
+  if constexpr (K > 1) {
+    gy += -C1 * G[1];
+    gz += C1 * G[2];
+    gx += -C1 * G[3];
+  }
+  if constexpr (K > 4) {
+    const float xx = x * x, yy = y * y, zz = z * z;
+    gx += C2_0 * y * G[4];
+    gy += C2_0 * x * G[4];
+    gy += C2_1 * z * G[5];
+    gz += C2_1 * y * G[5];
+    gx += -2.f * C2_2 * x * G[6];
+    gy += -2.f * C2_2 * y * G[6];
+    gz += 4.f * C2_2 * z * G[6];
+    gx += C2_3 * z * G[7];
+    gz += C2_3 * x * G[7];
+    gx += 2.f * C2_4 * x * G[8];
+    gy += -2.f * C2_4 * y * G[8];
+    if constexpr (K > 9) {
+      gx += 6.f * C3_0 * x * y * G[9];
+      gy += C3_0 * (3.f * xx - 3.f * yy) * G[9];
+      gx += C3_1 * y * z * G[10];
+      gy += C3_1 * x * z * G[10];
+      gz += C3_1 * x * y * G[10];
+      gx += -2.f * C3_2 * x * y * G[11];
+      gy += C3_2 * (4.f * zz - xx - 3.f * yy) * G[11];
+      gz += 8.f * C3_2 * y * z * G[11];
+      gx += -6.f * C3_3 * x * z * G[12];
+      gy += -6.f * C3_3 * y * z * G[12];
+      gz += C3_3 * (6.f * zz - 3.f * xx - 3.f * yy) * G[12];
+      gx += C3_4 * (4.f * zz - 3.f * xx - yy) * G[13];
+      gy += -2.f * C3_4 * x * y * G[13];
+      gz += 8.f * C3_4 * x * z * G[13];
+      gx += 2.f * C3_5 * x * z * G[14];
+      gy += -2.f * C3_5 * y * z * G[14];
+      gz += C3_5 * (xx - yy) * G[14];
+      gx += C3_6 * (3.f * xx - 3.f * yy) * G[15];
+      gy += -6.f * C3_6 * x * y * G[15];
+    }
+  }
+}
+
+// Layouts of the 3K coefficients of one Gaussian.
+enum Layout { kKC = 0, kCK = 1, kStrided = 2 };  // kKC: [K][3] block, kCK: [3][K] block
+
+template <int K, int L>
+__device__ inline void load_coeffs(const float* __restrict__ sh, int64_t i, int64_t sn, int64_t sc,
+                                   int64_t sk, float (&c)[3][K]) {
+  if constexpr (L == kStrided) {
+    const float* p = sh + i * sn;
+#pragma unroll
+    for (int ch = 0; ch < 3; ++ch)
+#pragma unroll
+      for (int k = 0; k < K; ++k) c[ch][k] = p[ch * sc + k * sk];
+  } else {
+    float buf[3 * K];
+    const float* p = sh + i * (3 * K);
+    if constexpr ((3 * K) % 4 == 0) {
+#pragma unroll
+      for (int j = 0; j < 3 * K / 4; ++j) {
+        const float4 v = reinterpret_cast<const float4*>(p)[j];
+        buf[4 * j] = v.x; buf[4 * j + 1] = v.y; buf[4 * j + 2] = v.z; buf[4 * j + 3] = v.w;
+      }
+    } else {
+#pragma unroll
+      for (int j = 0; j < 3 * K; ++j) buf[j] = p[j];
+    }
+#pragma unroll
+    for (int ch = 0; ch < 3; ++ch)
+#pragma unroll
+      for (int k = 0; k < K; ++k) c[ch][k] = (L == kKC) ? buf[k * 3 + ch] : buf[ch * K + k];
+  }
+}
+
+template <int K, int L>
+__device__ inline void store_coeffs(float* __restrict__ out, int64_t i, int64_t sn, int64_t sc,
+                                    int64_t sk, const float (&c)[3][K]) {
+  if constexpr (L == kStrided) {
+    float* p = out + i * sn;
+#pragma unroll
+    for (int ch = 0; ch < 3; ++ch)
+#pragma unroll
+      for (int k = 0; k < K; ++k) p[ch * sc + k * sk] = c[ch][k];
+  } else {
+    float buf[3 * K];
+#pragma unroll
+    for (int ch = 0; ch < 3; ++ch)
+#pragma unroll
+      for (int k = 0; k < K; ++k) buf[(L == kKC) ? (k * 3 + ch) : (ch * K + k)] = c[ch][k];
+    float* p = out + i * (3 * K);
+    if constexpr ((3 * K) % 4 == 0) {
+#pragma unroll
+      for (int j = 0; j < 3 * K / 4; ++j)
+        reinterpret_cast<float4*>(p)[j] =
+            make_float4(buf[4 * j], buf[4 * j + 1], buf[4 * j + 2], buf[4 * j + 3]);
+    } else {
+#pragma unroll
+      for (int j = 0; j < 3 * K; ++j) p[j] = buf[j];
+    }
+  }
+}
+
+template <int K, int L>
+__global__ void __launch_bounds__(kStreamThreads) sh_fwd_kernel(
+    const float* __restrict__ sh, int64_t n, int64_t sn, int64_t sc, int64_t sk,
+    const float* __restrict__ dirs, float* __restrict__ rgb) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    float c[3][K];
+    load_coeffs<K, L>(sh, i, sn, sc, sk, c);
+    float Y[K];
+    sh_basis<K>(dirs[3 * i], dirs[3 * i + 1], dirs[3 * i + 2], Y);
+#pragma unroll
+    for (int ch = 0; ch < 3; ++ch) {
+      float s = 0.f;
+#pragma unroll
+      for (int k = 0; k < K; ++k) s += c[ch][k] * Y[k];
+      rgb[3 * i + ch] = s;
+    }
+  }
+}
+
+template <int K, int L>
+__global__ void __launch_bounds__(kStreamThreads) sh_bwd_kernel(
+    const float* __restrict__ sh, int64_t n, int64_t sn, int64_t sc, int64_t sk,
+    const float* __restrict__ dirs, const float* __restrict__ d_rgb, float* __restrict__ d_sh,
+    float* __restrict__ d_dirs) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const float x = dirs[3 * i], y = dirs[3 * i + 1], z = dirs[3 * i + 2];
+    const float g[3] = {d_rgb[3 * i], d_rgb[3 * i + 1], d_rgb[3 * i + 2]};
+    float Y[K];
+    sh_basis<K>(x, y, z, Y);
+    float dc[3][K];
+#pragma unroll
+    for (int ch = 0; ch < 3; ++ch)
+#pragma unroll
+      for (int k = 0; k < K; ++k) dc[ch][k] = g[ch] * Y[k];
+    store_coeffs<K, L>(d_sh, i, sn, sc, sk, dc);
+    float gx = 0.f, gy = 0.f, gz = 0.f;
+    if constexpr (K > 1) {
+      float c[3][K];
+      load_coeffs<K, L>(sh, i, sn, sc, sk, c);
+      float G[K];
+#pragma unroll
+      for (int k = 0; k < K; ++k) G[k] = g[0] * c[0][k] + g[1] * c[1][k] + g[2] * c[2][k];
+      sh_basis_grad<K>(x, y, z, G, gx, gy, gz);
+    }
+    d_dirs[3 * i] = gx;
+    d_dirs[3 * i + 1] = gy;
+    d_dirs[3 * i + 2] = gz;
+  }
+}
+
+static int layout_of(int k, int64_t sn, int64_t sc, int64_t sk, const void* p, const void* q) {
+  const bool aligned = ((reinterpret_cast<uintptr_t>(p) | reinterpret_cast<uintptr_t>(q)) & 15) == 0;
+  if (sn == 3 * k && aligned) {
+    if (sc == 1 && sk == 3) return kKC;
+    if (sc == k && sk == 1) return kCK;
+  }
+  return kStrided;
+}
+
+template <int K>
+static void launch_fwd(int L, const float* sh, int64_t n, int64_t sn, int64_t sc, int64_t sk,
+                       const float* dirs, float* rgb, cudaStream_t s) {
+  const int grid = stream_grid(n);
+  if (L == kKC)
+    sh_fwd_kernel<K, kKC><<<grid, kStreamThreads, 0, s>>>(sh, n, sn, sc, sk, dirs, rgb);
+  else if (L == kCK)
+    sh_fwd_kernel<K, kCK><<<grid, kStreamThreads, 0, s>>>(sh, n, sn, sc, sk, dirs, rgb);
+  else
+    sh_fwd_kernel<K, kStrided><<<grid, kStreamThreads, 0, s>>>(sh, n, sn, sc, sk, dirs, rgb);
+}
+
+template <int K>
+static void launch_bwd(int L, const float* sh, int64_t n, int64_t sn, int64_t sc, int64_t sk,
+                       const float* dirs, const float* d_rgb, float* d_sh, float* d_dirs,
+                       cudaStream_t s) {
+  const int grid = stream_grid(n);
+  if (L == kKC)
+    sh_bwd_kernel<K, kKC><<<grid, kStreamThreads, 0, s>>>(sh, n, sn, sc, sk, dirs, d_rgb, d_sh, d_dirs);
+  else if (L == kCK)
+    sh_bwd_kernel<K, kCK><<<grid, kStreamThreads, 0, s>>>(sh, n, sn, sc, sk, dirs, d_rgb, d_sh, d_dirs);
+  else
+    sh_bwd_kernel<K, kStrided><<<grid, kStreamThreads, 0, s>>>(sh, n, sn, sc, sk, dirs, d_rgb, d_sh,
+                                                               d_dirs);
+}
+
+}  // namespace pgb
+
+using namespace pgb;
+
+extern "C" {
+
+int pgb_compute_sh_forward(const float* sh, int64_t n, int k, int64_t sn, int64_t sc, int64_t sk,
+                           const float* dirs, float* rgb, void* stream) {
+  if (n < 0 || !(k == 1 || k == 4 || k == 9 || k == 16)) return PGB_ERR_INVALID;
+  if (n == 0) return PGB_OK;
+  if (!sh || !dirs || !rgb) return PGB_ERR_INVALID;
+  const int L = layout_of(k, sn, sc, sk, sh, sh);
+  cudaStream_t s = as_stream(stream);
+  switch (k) {
+    case 1: launch_fwd<1>(L, sh, n, sn, sc, sk, dirs, rgb, s); break;
+    case 4: launch_fwd<4>(L, sh, n, sn, sc, sk, dirs, rgb, s); break;
+    case 9: launch_fwd<9>(L, sh, n, sn, sc, sk, dirs, rgb, s); break;
+    default: launch_fwd<16>(L, sh, n, sn, sc, sk, dirs, rgb, s); break;
+  }
+  return launch_status();
+}
+
+int pgb_compute_sh_backward(const float* sh, int64_t n, int k, int64_t sn, int64_t sc, int64_t sk,
+                            const float* dirs, const float* d_rgb, float* d_sh, float* d_dirs,
+                            void* stream) {
+  if (n < 0 || !(k == 1 || k == 4 || k == 9 || k == 16)) return PGB_ERR_INVALID;
+  if (n == 0) return PGB_OK;
+  if (!sh || !dirs || !d_rgb || !d_sh || !d_dirs) return PGB_ERR_INVALID;
+  const int L = layout_of(k, sn, sc, sk, sh, d_sh);
+  cudaStream_t s = as_stream(stream);
+  switch (k) {
+    case 1: launch_bwd<1>(L, sh, n, sn, sc, sk, dirs, d_rgb, d_sh, d_dirs, s); break;
+    case 4: launch_bwd<4>(L, sh, n, sn, sc, sk, dirs, d_rgb, d_sh, d_dirs, s); break;
+    case 9: launch_bwd<9>(L, sh, n, sn, sc, sk, dirs, d_rgb, d_sh, d_dirs, s); break;
+    default: launch_bwd<16>(L, sh, n, sn, sc, sk, dirs, d_rgb, d_sh, d_dirs, s); break;
+  }
+  return launch_status();
+}
+
+}  // extern "C"

@@ -1,0 +1,531 @@
+"""The msplat operators on GB300: torch.autograd.Functions over the C ABI.
+
+Each public function keeps the signature and argument meaning that Pointrix's
+``MsplatRender.render_iter`` relies on (``pointrix/model/renderer/msplat.py``
+lines 104-151; the same six calls in ``examples/supervise/renderer.py:42-85``),
+so ``import msplat`` can resolve to this module unchanged.  Inputs are CUDA
+float32 tensors (possibly strided views); outputs are new tensors on the same
+device; all work is enqueued on the current CUDA stream.  Errors raise
+``ValueError`` (bad arguments) or :class:`pointrix_gb300._lib.PgbError`
+(a status from the kernel library).  There is no CPU path.
+"""
+from __future__ import annotations
+
+import threading
+
+import torch
+
+from . import _lib
+from ._lib import PgbError, call
+
+__all__ = [
+    "compute_sh", "project_point", "compute_cov3d", "ewa_project", "sort_gaussian",
+    "alpha_blending", "alpha_blending_with_state", "check_device_status", "kernel_timing",
+    "NEAREST_DEFAULT", "EXTENT_DEFAULT",
+]
+
+NEAREST_DEFAULT = 0.2
+EXTENT_DEFAULT = 1.3
+TILE = 16
+
+
+def _ptr(t):
+    return None if t is None else t.data_ptr()
+
+
+def _c(t):
+    """Contiguous and 16-byte aligned (kernels use 8- and 16-byte vector
+    accesses on rows); copies only when the input is neither."""
+    t = t.contiguous()
+    if t.data_ptr() % 16:
+        t = t.clone()
+    return t
+
+
+def _stream(device) -> int:
+    return torch.cuda.current_stream(device).cuda_stream
+
+
+def _need(t, name, dtype=torch.float32, ndim=None, last=None):
+    if not isinstance(t, torch.Tensor):
+        raise ValueError(f"{name} must be a tensor")
+    if not t.is_cuda:
+        raise ValueError(f"{name} must be a CUDA tensor (pointrix_gb300 has no CPU path)")
+    if t.dtype != dtype:
+        raise ValueError(f"{name} must be {dtype}, got {t.dtype}")
+    if ndim is not None and t.dim() != ndim:
+        raise ValueError(f"{name} must have {ndim} dims, got shape {tuple(t.shape)}")
+    if last is not None and t.shape[-1] != last:
+        raise ValueError(f"{name} must have last dim {last}, got shape {tuple(t.shape)}")
+
+
+def _intr4(intr):
+    _need(intr, "intr")
+    if intr.numel() != 4:
+        raise ValueError(f"intr must hold 4 values (fx, fy, cx, cy), got shape {tuple(intr.shape)}")
+    return _c(intr.reshape(4))
+
+
+def _extr34(extr):
+    _need(extr, "extr")
+    if tuple(extr.shape) != (3, 4):
+        raise ValueError(f"extr must be [3,4], got {tuple(extr.shape)}")
+    return _c(extr)
+
+
+def _visible_bytes(visible, n):
+    if visible.numel() != n:
+        raise ValueError(f"visible must have {n} entries, got shape {tuple(visible.shape)}")
+    v = visible.reshape(-1)
+    if v.dtype != torch.bool:
+        v = v != 0
+    return _c(v).view(torch.uint8)
+
+
+# ---------------------------------------------------------------------------
+# optional per-operator CUDA-event timing and kernel-launch counting
+# ---------------------------------------------------------------------------
+class KernelTiming:
+    """Records a CUDA event pair around every library call on the calling
+    stream, and counts the kernels each call launches.  Enable with
+    ``with kernel_timing() as kt: ...``; read after a synchronize."""
+
+    def __init__(self):
+        self.events: dict[str, list] = {}
+        self.launches: dict[str, int] = {}
+
+    def total_launches(self) -> int:
+        return sum(self.launches.values())
+
+    def ms(self, name: str) -> list[float]:
+        return [a.elapsed_time(b) for a, b in self.events.get(name, [])]
+
+    def names(self):
+        return list(self.events)
+
+
+_timing: KernelTiming | None = None
+
+
+class kernel_timing:
+    def __enter__(self) -> KernelTiming:
+        global _timing
+        self.prev, _timing = _timing, KernelTiming()
+        return _timing
+
+    def __exit__(self, *exc):
+        global _timing
+        _timing = self.prev
+        return False
+
+
+class _timed:
+    __slots__ = ("name", "dev", "kernels", "ev")
+
+    def __init__(self, name, dev, kernels):
+        self.name, self.dev, self.kernels = name, dev, kernels
+
+    def __enter__(self):
+        if _timing is not None:
+            self.ev = torch.cuda.Event(enable_timing=True)
+            self.ev.record(torch.cuda.current_stream(self.dev))
+        return self
+
+    def __exit__(self, *exc):
+        t = _timing
+        if t is not None and exc[0] is None:
+            end = torch.cuda.Event(enable_timing=True)
+            end.record(torch.cuda.current_stream(self.dev))
+            t.events.setdefault(self.name, []).append((self.ev, end))
+            t.launches[self.name] = t.launches.get(self.name, 0) + self.kernels
+        return False
+
+
+# ---------------------------------------------------------------------------
+# device status words (blend kernels write a PGB status on a device-side
+# fault; sort_gaussian's finish step reports through its per-call info words)
+# ---------------------------------------------------------------------------
+_status_lock = threading.Lock()
+_dev_status: dict[int, torch.Tensor] = {}
+_pending: list[tuple[torch.cuda.Event, torch.Tensor, str]] = []
+
+
+def _status_word(device) -> torch.Tensor:
+    idx = device.index if device.index is not None else torch.cuda.current_device()
+    with _status_lock:
+        t = _dev_status.get(idx)
+        if t is None:
+            t = torch.zeros(4, dtype=torch.int64, device=device)
+            _dev_status[idx] = t
+    return t
+
+
+def _defer_check(word: torch.Tensor, what: str):
+    host = torch.empty(word.numel(), dtype=torch.int64, pin_memory=True)
+    host.copy_(word, non_blocking=True)
+    ev = torch.cuda.Event()
+    ev.record(torch.cuda.current_stream(word.device))
+    with _status_lock:
+        _pending.append((ev, host, what))
+
+
+def _drain_pending(block: bool):
+    with _status_lock:
+        items = list(_pending)
+        _pending.clear()
+    keep, err = [], None
+    for ev, host, what in items:
+        if block:
+            ev.synchronize()
+        elif not ev.query():
+            keep.append((ev, host, what))
+            continue
+        code = int(host.max())
+        if code and err is None:
+            err = (code, what)
+    if keep:
+        with _status_lock:
+            _pending.extend(keep)
+    if err:
+        _lib.check(err[0], err[1])
+
+
+def check_device_status(device=None) -> None:
+    """Synchronise ``device`` and raise if any kernel of this library
+    recorded a device-side fault (expired bounded wait, overflow, mismatch)."""
+    device = torch.device("cuda", torch.cuda.current_device()) if device is None else torch.device(device)
+    torch.cuda.synchronize(device)
+    _drain_pending(block=True)
+    w = _status_word(device)
+    code = int(w.max().item())
+    if code:
+        w.zero_()
+        _lib.check(code, "device status")
+
+
+# ---------------------------------------------------------------------------
+# compute_sh
+# ---------------------------------------------------------------------------
+def _dense_sh(sh):
+    if sh.is_contiguous() or sh.permute(0, 2, 1).is_contiguous():
+        return sh
+    return sh.contiguous()
+
+
+class _ComputeSH(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, sh, dirs):
+        n, K = sh.shape[0], sh.shape[2]
+        rgb = torch.empty(n, 3, dtype=torch.float32, device=sh.device)
+        sn, sc, sk = sh.stride()
+        with _timed("compute_sh_fwd", sh.device, 1 if n else 0):
+            call("pgb_compute_sh_forward", _ptr(sh), n, K, sn, sc, sk, _ptr(dirs), _ptr(rgb), _stream(sh.device))
+        ctx.save_for_backward(sh, dirs)
+        return rgb
+
+    @staticmethod
+    def backward(ctx, d_rgb):
+        sh, dirs = ctx.saved_tensors
+        n, K = sh.shape[0], sh.shape[2]
+        d_sh = torch.empty_like(sh)
+        d_dirs = torch.empty_like(dirs)
+        sn, sc, sk = sh.stride()
+        with _timed("compute_sh_bwd", sh.device, 1 if n else 0):
+            call("pgb_compute_sh_backward", _ptr(sh), n, K, sn, sc, sk, _ptr(dirs),
+                 _ptr(_c(d_rgb)), _ptr(d_sh), _ptr(d_dirs), _stream(sh.device))
+        return d_sh, d_dirs
+
+
+def compute_sh(shs, view_dirs):
+    """Raw real-SH colour ``sum_k shs[:, c, k] Y_k(view_dirs)`` -> [N,3].
+
+    ``shs`` is [N,3,K] with K in {1,4,9,16} (any strides; the permuted
+    ``get_shs`` view is read in place); ``view_dirs`` [N,3] unit vectors.
+    No +0.5 offset and no clamp (``msplat.py:103-105`` adds them).
+    """
+    _need(shs, "shs", ndim=3)
+    _need(view_dirs, "view_dirs", ndim=2, last=3)
+    if shs.shape[1] != 3 or shs.shape[2] not in (1, 4, 9, 16):
+        raise ValueError(f"shs must be [N,3,K] with K in (1,4,9,16), got {tuple(shs.shape)}")
+    if view_dirs.shape[0] != shs.shape[0]:
+        raise ValueError("shs and view_dirs disagree on N")
+    return _ComputeSH.apply(_dense_sh(shs), _c(view_dirs))
+
+
+# ---------------------------------------------------------------------------
+# project_point
+# ---------------------------------------------------------------------------
+class _ProjectPoint(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, xyz, intr, extr, W, H, nearest, extent, intr_shape):
+        n = xyz.shape[0]
+        uv = torch.empty(n, 2, dtype=torch.float32, device=xyz.device)
+        depth = torch.empty(n, 1, dtype=torch.float32, device=xyz.device)
+        with _timed("project_point_fwd", xyz.device, 1 if n else 0):
+            call("pgb_project_point_forward", _ptr(xyz), n, _ptr(intr), _ptr(extr), W, H,
+                 float(nearest), float(extent), _ptr(uv), _ptr(depth), _stream(xyz.device))
+        ctx.save_for_backward(xyz, intr, extr)
+        ctx.cfg = (W, H, float(nearest), float(extent), intr_shape)
+        return uv, depth
+
+    @staticmethod
+    def backward(ctx, d_uv, d_depth):
+        xyz, intr, extr = ctx.saved_tensors
+        W, H, nearest, extent, intr_shape = ctx.cfg
+        n = xyz.shape[0]
+        dev = xyz.device
+        d_uv = torch.zeros(n, 2, device=dev) if d_uv is None else _c(d_uv)
+        d_depth = torch.zeros(n, 1, device=dev) if d_depth is None else _c(d_depth)
+        d_xyz = torch.empty_like(xyz)
+        d_intr = torch.empty(4, dtype=torch.float32, device=dev)
+        d_extr = torch.empty(3, 4, dtype=torch.float32, device=dev)
+        nbytes = _lib.lib().pgb_camera_grad_scratch_bytes()
+        scratch = torch.empty(nbytes, dtype=torch.uint8, device=dev)
+        with _timed("project_point_bwd", dev, 2):
+            call("pgb_project_point_backward", _ptr(xyz), n, _ptr(intr), _ptr(extr), W, H, nearest,
+                 extent, _ptr(d_uv), _ptr(d_depth), _ptr(d_xyz), _ptr(d_intr), _ptr(d_extr),
+                 _ptr(scratch), nbytes, _stream(dev))
+        return d_xyz, d_intr, d_extr, None, None, None, None, None
+
+
+def project_point(xyz, intr, extr, W, H, nearest=NEAREST_DEFAULT, extent=EXTENT_DEFAULT):
+    """Pinhole projection: uv [N,2] = (fx x/z + cx, fy y/z + cy) of the
+    camera-space point, depth [N,1] = z.  Points with z <= ``nearest`` or a
+    centre outside ``extent`` x the half image get uv = 0 and depth = 0
+    (``visible = depth != 0`` at ``msplat.py:115``).  ``intr`` is [4] or
+    [1,4] (fx, fy, cx, cy); ``extr`` is the world->camera [3,4]."""
+    _need(xyz, "xyz", ndim=2, last=3)
+    shape = tuple(intr.shape) if isinstance(intr, torch.Tensor) else None
+    intr4, extr34 = _intr4(intr), _extr34(extr)
+    return _ProjectPoint.apply(_c(xyz), intr4, extr34, int(W), int(H), nearest, extent, shape)
+
+
+# ---------------------------------------------------------------------------
+# compute_cov3d
+# ---------------------------------------------------------------------------
+class _ComputeCov3d(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, scales, uquats, vis_u8):
+        n = scales.shape[0]
+        cov = torch.empty(n, 6, dtype=torch.float32, device=scales.device)
+        with _timed("compute_cov3d_fwd", scales.device, 1 if n else 0):
+            call("pgb_compute_cov3d_forward", _ptr(scales), _ptr(uquats), _ptr(vis_u8), n, _ptr(cov),
+                 _stream(scales.device))
+        ctx.save_for_backward(scales, uquats, vis_u8)
+        return cov
+
+    @staticmethod
+    def backward(ctx, d_cov):
+        scales, uquats, vis_u8 = ctx.saved_tensors
+        n = scales.shape[0]
+        d_s = torch.empty_like(scales)
+        d_q = torch.empty_like(uquats)
+        with _timed("compute_cov3d_bwd", scales.device, 1 if n else 0):
+            call("pgb_compute_cov3d_backward", _ptr(scales), _ptr(uquats), _ptr(vis_u8), n,
+                 _ptr(_c(d_cov)), _ptr(d_s), _ptr(d_q), _stream(scales.device))
+        return d_s, d_q, None
+
+
+def compute_cov3d(scales, uquats, visible):
+    """3D covariance ``(R S)(R S)^T`` as its upper triangle
+    (xx, xy, xz, yy, yz, zz) [N,6]; zero rows where ``visible`` is false.
+    ``uquats`` are unit wxyz quaternions, ``scales`` activated [N,3]."""
+    _need(scales, "scales", ndim=2, last=3)
+    _need(uquats, "uquats", ndim=2, last=4)
+    n = scales.shape[0]
+    if uquats.shape[0] != n:
+        raise ValueError("scales and uquats disagree on N")
+    return _ComputeCov3d.apply(_c(scales), _c(uquats), _visible_bytes(visible, n))
+
+
+# ---------------------------------------------------------------------------
+# ewa_project
+# ---------------------------------------------------------------------------
+class _EwaProject(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, xyz, cov3d, intr, extr, uv, W, H, vis_u8, intr_shape):
+        n = xyz.shape[0]
+        dev = xyz.device
+        conic = torch.empty(n, 3, dtype=torch.float32, device=dev)
+        radius = torch.empty(n, dtype=torch.int32, device=dev)
+        tiles = torch.empty(n, dtype=torch.int32, device=dev)
+        with _timed("ewa_project_fwd", dev, 1 if n else 0):
+            call("pgb_ewa_project_forward", _ptr(xyz), _ptr(cov3d), _ptr(intr), _ptr(extr), _ptr(uv),
+                 _ptr(vis_u8), n, W, H, _ptr(conic), _ptr(radius), _ptr(tiles), _stream(dev))
+        ctx.save_for_backward(xyz, cov3d, intr, extr, radius)
+        ctx.cfg = (W, H, intr_shape)
+        ctx.mark_non_differentiable(radius, tiles)
+        return conic, radius, tiles
+
+    @staticmethod
+    def backward(ctx, d_conic, _r, _t):
+        xyz, cov3d, intr, extr, radius = ctx.saved_tensors
+        W, H, intr_shape = ctx.cfg
+        n = xyz.shape[0]
+        dev = xyz.device
+        if d_conic is None:
+            d_conic = torch.zeros(n, 3, device=dev)
+        d_xyz = torch.empty_like(xyz)
+        d_cov = torch.empty_like(cov3d)
+        d_intr = torch.empty(4, dtype=torch.float32, device=dev)
+        d_extr = torch.empty(3, 4, dtype=torch.float32, device=dev)
+        nbytes = _lib.lib().pgb_camera_grad_scratch_bytes()
+        scratch = torch.empty(nbytes, dtype=torch.uint8, device=dev)
+        with _timed("ewa_project_bwd", dev, 2):
+            call("pgb_ewa_project_backward", _ptr(xyz), _ptr(cov3d), _ptr(intr), _ptr(extr),
+                 _ptr(radius), n, W, H, _ptr(_c(d_conic)), _ptr(d_xyz), _ptr(d_cov),
+                 _ptr(d_intr), _ptr(d_extr), _ptr(scratch), nbytes, _stream(dev))
+        return d_xyz, d_cov, d_intr, d_extr, None, None, None, None, None
+
+
+def ewa_project(xyz, cov3d, intr, extr, uv, W, H, visible):
+    """EWA projection of the 3D covariance into an image-space conic.
+
+    Returns conic [N,3] (inverse 2D covariance a, b, c), radius [N] int32
+    (pixels, 3 sigma of the dilated footprint) and tiles_touched [N] int32
+    (16x16 tiles of its rectangle); culled Gaussians get zeros.
+    Differentiable in xyz, cov3d, intr and extr.
+    """
+    _need(xyz, "xyz", ndim=2, last=3)
+    _need(cov3d, "cov3d", ndim=2, last=6)
+    _need(uv, "uv", ndim=2, last=2)
+    n = xyz.shape[0]
+    shape = tuple(intr.shape)
+    return _EwaProject.apply(_c(xyz), _c(cov3d), _intr4(intr), _extr34(extr),
+                             _c(uv.detach()), int(W), int(H), _visible_bytes(visible, n), shape)
+
+
+# ---------------------------------------------------------------------------
+# sort_gaussian
+# ---------------------------------------------------------------------------
+def _sort_scratch(n, k, W, H):
+    import ctypes as C
+    bn, bk = C.c_size_t(0), C.c_size_t(0)
+    call("pgb_sort_scratch_bytes", n, k, W, H, C.byref(bn), C.byref(bk))
+    return bn.value, bk.value
+
+
+def sort_gaussian(uv, depth, W, H, radius, tiles_touched):
+    """Tile binning: ``gaussian_ids_sorted`` [K] int32 (ids ordered by tile,
+    then depth, then id) and ``tile_range`` [T,2] int32 ([start, end) per
+    16x16 tile, [0,0] when empty), K = sum of ``tiles_touched`` over
+    Gaussians with ``radius > 0``.  Reads K back to the host (one sync)."""
+    _need(uv, "uv", ndim=2, last=2)
+    _need(depth, "depth")
+    _need(radius, "radius", dtype=torch.int32)
+    _need(tiles_touched, "tiles_touched", dtype=torch.int32)
+    W, H = int(W), int(H)
+    n = uv.shape[0]
+    if depth.numel() != n or radius.numel() != n or tiles_touched.numel() != n:
+        raise ValueError("sort_gaussian: uv, depth, radius and tiles_touched disagree on N")
+    dev = uv.device
+    st = _stream(dev)
+    uv, depth = _c(uv.detach()), _c(depth.detach().reshape(-1))
+    radius, tiles_touched = _c(radius.reshape(-1)), _c(tiles_touched.reshape(-1))
+    bn, _ = _sort_scratch(n, 0, W, H)
+    scratch_n = torch.empty(max(bn, 1), dtype=torch.uint8, device=dev)
+    info = torch.empty(2, dtype=torch.int64, device=dev)
+    with _timed("sort_begin", dev, 5 if n else 0):
+        call("pgb_sort_gaussian_begin", _ptr(depth), _ptr(radius), _ptr(tiles_touched), n, W, H,
+             _ptr(scratch_n), bn, _ptr(info), st)
+    host = torch.empty(2, dtype=torch.int64, pin_memory=True)
+    host.copy_(info, non_blocking=True)
+    torch.cuda.current_stream(dev).synchronize()
+    _drain_pending(block=False)
+    K, err = int(host[0]), int(host[1])
+    _lib.check(err, "sort_gaussian (depth passes)")
+    T = ((W + TILE - 1) // TILE) * ((H + TILE - 1) // TILE)
+    _, bk = _sort_scratch(n, K, W, H)
+    scratch_k = torch.empty(max(bk, 1), dtype=torch.uint8, device=dev)
+    ids = torch.empty(K, dtype=torch.int32, device=dev)
+    rng = torch.empty(T, 2, dtype=torch.int32, device=dev)
+    passes = 1 if T <= 256 else (2 if T <= 65536 else 3)
+    with _timed("sort_finish", dev, (2 + passes) if (K and n) else 0):
+        call("pgb_sort_gaussian_finish", _ptr(uv), _ptr(radius), _ptr(tiles_touched), n, W, H, K,
+             _ptr(scratch_n), bn, _ptr(scratch_k), bk, _ptr(info), _ptr(ids) if K else None,
+             _ptr(rng), st)
+    _defer_check(info[1:], "sort_gaussian (tile passes)")
+    return ids, rng
+
+
+# ---------------------------------------------------------------------------
+# alpha_blending
+# ---------------------------------------------------------------------------
+class _AlphaBlending(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, uv, conic, opacity, feature, ids, tile_range, bg, W, H, ndc):
+        n, C = feature.shape
+        dev = feature.device
+        rf = _lib.lib().pgb_blend_record_floats(C)
+        records = torch.empty(n, rf, dtype=torch.float32, device=dev)
+        out = torch.empty(C, H, W, dtype=torch.float32, device=dev)
+        final_T = torch.empty(H, W, dtype=torch.float32, device=dev)
+        ncon = torch.empty(H, W, dtype=torch.int32, device=dev)
+        status = _status_word(dev)
+        with _timed("alpha_blending_fwd", dev, 2 if n else 1):
+            call("pgb_alpha_blending_forward", _ptr(uv), _ptr(conic), _ptr(opacity), _ptr(feature), n, C,
+                 _ptr(ids), ids.numel(), _ptr(tile_range), float(bg), W, H, _ptr(records), _ptr(out),
+                 _ptr(final_T), _ptr(ncon), _ptr(status), _stream(dev))
+        ctx.save_for_backward(records, ids, tile_range, final_T, ncon)
+        ctx.cfg = (n, C, float(bg), W, H, ndc is not None)
+        ctx.mark_non_differentiable(final_T, ncon)
+        return out, final_T, ncon
+
+    @staticmethod
+    def backward(ctx, d_out, _dT, _dn):
+        records, ids, tile_range, final_T, ncon = ctx.saved_tensors
+        n, C, bg, W, H, has_ndc = ctx.cfg
+        dev = records.device
+        grec = torch.empty_like(records)
+        d_uv = torch.empty(n, 2, dtype=torch.float32, device=dev)
+        d_conic = torch.empty(n, 3, dtype=torch.float32, device=dev)
+        d_op = torch.empty(n, dtype=torch.float32, device=dev)
+        d_feat = torch.empty(n, C, dtype=torch.float32, device=dev)
+        status = _status_word(dev)
+        with _timed("alpha_blending_bwd", dev, 2 if n else 0):
+            call("pgb_alpha_blending_backward", _ptr(records), n, C, _ptr(ids), ids.numel(),
+                 _ptr(tile_range), bg, W, H, _ptr(final_T), _ptr(ncon), _ptr(_c(d_out)),
+                 _ptr(grec), _ptr(d_uv), _ptr(d_conic), _ptr(d_op), _ptr(d_feat), _ptr(status),
+                 _stream(dev))
+        d_ndc = d_uv.clone() if has_ndc else None
+        return d_uv, d_conic, d_op, d_feat, None, None, None, None, None, d_ndc
+
+
+def alpha_blending_with_state(uv, conic, opacity, feature, gaussian_ids_sorted, tile_range, bg, W, H,
+                              ndc=None):
+    """As :func:`alpha_blending`, also returning the final transmittance
+    [H,W] and the per-pixel count of list entries up to the last
+    contributor [H,W] (what the backward replays from)."""
+    _need(uv, "uv", ndim=2, last=2)
+    _need(conic, "conic", ndim=2, last=3)
+    _need(opacity, "opacity")
+    _need(feature, "feature", ndim=2)
+    _need(gaussian_ids_sorted, "gaussian_ids_sorted", dtype=torch.int32)
+    _need(tile_range, "tile_range", dtype=torch.int32, ndim=2, last=2)
+    n, C = feature.shape
+    if C < 1 or C > 26:
+        raise ValueError(f"alpha_blending supports 1..26 feature channels, got {C}")
+    if uv.shape[0] != n or conic.shape[0] != n or opacity.numel() != n:
+        raise ValueError("alpha_blending: uv, conic, opacity and feature disagree on N")
+    W, H = int(W), int(H)
+    T = ((W + TILE - 1) // TILE) * ((H + TILE - 1) // TILE)
+    if tile_range.shape[0] != T:
+        raise ValueError(f"tile_range has {tile_range.shape[0]} rows, the {W}x{H} image has {T} tiles")
+    if isinstance(bg, torch.Tensor):
+        bg = float(bg)
+    if ndc is not None and tuple(ndc.shape) != (n, 2):
+        raise ValueError(f"ndc must be [N,2], got {tuple(ndc.shape)}")
+    return _AlphaBlending.apply(_c(uv), _c(conic), _c(opacity.reshape(n)), _c(feature),
+                                _c(gaussian_ids_sorted), _c(tile_range), bg, W, H, ndc)
+
+
+def alpha_blending(uv, conic, opacity, feature, gaussian_ids_sorted, tile_range, bg, W, H, ndc=None):
+    """Front-to-back alpha compositing of ``feature`` [N,C] per 16x16 tile ->
+    [C,H,W], plus ``bg`` times the final transmittance in every channel.
+
+    Differentiable in uv, conic, opacity and feature; ``ndc`` ([N,2], the
+    zero leaf that ``msplat.py:141-145`` creates) receives d(loss)/d(uv) in
+    pixel units, which the densification controller reads as ``ndc.grad``.
+    """
+    return alpha_blending_with_state(uv, conic, opacity, feature, gaussian_ids_sorted, tile_range,
+                                     bg, W, H, ndc)[0]

@@ -1,0 +1,329 @@
+"""GPU parity of every operator against the CPU oracle, through the C ABI.
+
+Bars (stated per test):
+* integer outputs (radius, tiles_touched, sorted ids, tile ranges) and the
+  float outputs of the FMA-free projection kernels (uv, depth, cov3d, conic):
+  bit-exact against the float32 oracle;
+* images and SH colours: within 1e-5 abs of the float64 oracle on the same
+  inputs (depth channel: 1e-5 relative to the scene depth);
+* gradients: within 1e-4 of the float64 oracle's autograd gradient,
+  relative to the largest gradient entry of that tensor.
+"""
+import pytest
+import torch
+
+from oracle import msplat_cpu as O
+from pointrix_gb300 import ops
+from pointrix_gb300 import workloads as WL
+
+pytestmark = pytest.mark.gpu
+DEV = "cuda"
+IMG_ATOL = 1e-5
+GRAD_RTOL = 1e-4
+
+
+def scaled_err(a, b):
+    if b is None:                      # the reference has no dependence: expect zeros
+        return float(a.detach().abs().max())
+    a, b = a.detach().double().cpu(), b.detach().double().cpu()
+    den = b.abs().max().clamp(min=1e-30)
+    return float((a - b).abs().max() / den)
+
+
+def cpu(t, dt=None):
+    t = t.detach().cpu()
+    return t if dt is None else t.to(dt)
+
+
+class Prepared:
+    """GPU preprocessing of one scene + camera, with the inputs kept."""
+
+    def __init__(self, scene, cam, channels=("rgb", "depth"), sh_degree=None):
+        pos, sc, q, op, shs = (t.to(DEV) for t in scene.activated())
+        self.pos, self.sc, self.q, self.op, self.shs = pos, sc, q, op, shs
+        self.cam = cam
+        self.W, self.H = cam.W, cam.H
+        self.intr = cam.intr.to(DEV)
+        self.extr = cam.extr[:3].to(DEV).contiguous()
+        self.center = cam.center.to(DEV)
+        d = pos - self.center[None]
+        self.dirs = d / d.norm(dim=1, keepdim=True)
+        self.shc = shs.permute(0, 2, 1)
+        self.rgb_raw = ops.compute_sh(self.shc, self.dirs)
+        self.uv, self.depth = ops.project_point(pos, self.intr, self.extr, self.W, self.H, nearest=0.2)
+        self.vis = self.depth != 0
+        self.cov = ops.compute_cov3d(sc, q, self.vis)
+        self.conic, self.radius, self.tiles = ops.ewa_project(pos, self.cov, self.intr, self.extr, self.uv,
+                                                              self.W, self.H, self.vis)
+        self.ids, self.rng = ops.sort_gaussian(self.uv, self.depth, self.W, self.H, self.radius, self.tiles)
+        feats = [(self.rgb_raw + 0.5).clamp(min=0)]
+        if "depth" in channels:
+            feats.append(self.depth)
+        self.feat = torch.cat(feats, 1).contiguous()
+
+
+@pytest.fixture(scope="module")
+def small():
+    scene, cam = WL.scene_small(0)
+    return Prepared(scene, cam)
+
+
+# --------------------------------------------------------------- forward ---
+def test_project_point_bitexact(small):
+    p = small
+    uv_o, d_o = O.project_point(cpu(p.pos), cpu(p.intr), cpu(p.extr), p.W, p.H, nearest=0.2)
+    assert torch.equal(cpu(p.uv), uv_o)
+    assert torch.equal(cpu(p.depth), d_o)
+    uv64, d64 = O.project_point(cpu(p.pos, torch.float64), cpu(p.intr, torch.float64),
+                                cpu(p.extr, torch.float64), p.W, p.H, nearest=0.2)
+    assert (cpu(p.uv, torch.float64) - uv64).abs().max() < 1e-3   # float32 rounding of pixel coords
+    assert int(p.vis.sum()) > 0.9 * p.pos.shape[0]
+
+
+def test_cov3d_and_ewa_bitexact(small):
+    p = small
+    cov_o = O.compute_cov3d(cpu(p.sc), cpu(p.q), cpu(p.vis))
+    assert torch.equal(cpu(p.cov), cov_o)
+    conic_o, rad_o, tiles_o = O.ewa_project(cpu(p.pos), cpu(p.cov), cpu(p.intr), cpu(p.extr), cpu(p.uv),
+                                            p.W, p.H, cpu(p.vis))
+    assert torch.equal(cpu(p.radius), rad_o)
+    assert torch.equal(cpu(p.tiles), tiles_o)
+    assert torch.equal(cpu(p.conic), conic_o)
+    assert int((rad_o > 0).sum()) > 0
+
+
+def test_sort_bitexact(small):
+    p = small
+    ids_o, rng_o = O.sort_gaussian(cpu(p.uv), cpu(p.depth), p.W, p.H, cpu(p.radius), cpu(p.tiles))
+    assert p.ids.numel() == int(p.tiles.sum()) > 0
+    assert torch.equal(cpu(p.ids), ids_o)
+    assert torch.equal(cpu(p.rng), rng_o)
+    ops.check_device_status()
+
+
+def test_compute_sh_close(small):
+    p = small
+    ref = O.compute_sh(cpu(p.shc, torch.float64), cpu(p.dirs, torch.float64))
+    assert (cpu(p.rgb_raw, torch.float64) - ref).abs().max() < IMG_ATOL
+
+
+@pytest.mark.parametrize("K", [1, 4, 9, 16])
+@pytest.mark.parametrize("layout", ["permuted", "contiguous", "strided"])
+def test_compute_sh_layouts_and_grad(K, layout):
+    g = torch.Generator().manual_seed(K)
+    n = 3000
+    base = torch.randn(n, K, 3, generator=g)
+    if layout == "permuted":
+        sh = base.to(DEV).permute(0, 2, 1)
+    elif layout == "contiguous":
+        sh = base.permute(0, 2, 1).contiguous().to(DEV)
+    else:
+        sh = torch.randn(n, 3, 2 * K, generator=g).to(DEV)[:, :, ::2]
+    d = torch.randn(n, 3, generator=g)
+    d = (d / d.norm(dim=1, keepdim=True)).to(DEV)
+    sh = sh.detach().requires_grad_(True)
+    d = d.requires_grad_(True)
+    out = ops.compute_sh(sh, d)
+    up = torch.randn(n, 3, generator=g).to(DEV)
+    out.backward(up)
+    sh64 = cpu(sh, torch.float64).requires_grad_(True)
+    d64 = cpu(d, torch.float64).requires_grad_(True)
+    ref = O.compute_sh(sh64, d64)
+    ref.backward(cpu(up, torch.float64))
+    assert (cpu(out, torch.float64) - ref).abs().max() < 1e-5 * max(1.0, float(ref.abs().max()))
+    assert scaled_err(sh.grad, sh64.grad) < GRAD_RTOL
+    assert scaled_err(d.grad, d64.grad) < GRAD_RTOL
+
+
+def blend_inputs64(p):
+    return [cpu(t, torch.float64) for t in (p.uv, p.conic, p.op, p.feat)]
+
+
+def test_alpha_blending_forward_close(small):
+    p = small
+    img, fT, nc = ops.alpha_blending_with_state(p.uv, p.conic, p.op, p.feat, p.ids, p.rng, 0.0, p.W, p.H)
+    u, c, o, f = blend_inputs64(p)
+    ref, fT_o, nc_o = O.alpha_blending(u, c, o, f, cpu(p.ids), cpu(p.rng), 0.0, p.W, p.H, return_state=True)
+    img = cpu(img, torch.float64)
+    assert (img[:3] - ref[:3]).abs().max() < IMG_ATOL
+    depth_scale = float(p.depth.max())
+    assert (img[3] - ref[3]).abs().max() < IMG_ATOL * depth_scale
+    # skip/stop decisions taken in float32 vs float64 may differ on a handful of pixels at most
+    assert (cpu(nc) != nc_o).float().mean() < 1e-3
+    assert (cpu(fT, torch.float64) - fT_o).abs().max() < 1e-5
+
+
+def test_alpha_blending_background(small):
+    p = small
+    img0 = ops.alpha_blending(p.uv, p.conic, p.op, p.feat, p.ids, p.rng, 0.0, p.W, p.H)
+    img1, fT, _ = ops.alpha_blending_with_state(p.uv, p.conic, p.op, p.feat, p.ids, p.rng, 0.7, p.W, p.H)
+    assert torch.allclose(img1 - img0, 0.7 * fT[None].expand_as(img0), atol=1e-6)
+
+
+# -------------------------------------------------------------- backward ---
+def test_alpha_blending_backward(small):
+    p = small
+    leaves = [t.detach().clone().requires_grad_(True) for t in (p.uv, p.conic, p.op, p.feat)]
+    ndc = torch.zeros_like(p.uv, requires_grad=True)
+    img = ops.alpha_blending(*leaves, p.ids, p.rng, 0.25, p.W, p.H, ndc)
+    g = torch.Generator().manual_seed(7)
+    up = torch.randn(img.shape, generator=g)
+    img.backward(up.to(DEV))
+    ref_leaves = [t.requires_grad_(True) for t in blend_inputs64(p)]
+    ref = O.alpha_blending(*ref_leaves, cpu(p.ids), cpu(p.rng), 0.25, p.W, p.H)
+    ref.backward(up.double())
+    for name, a, b in zip(("uv", "conic", "opacity", "feature"), leaves, ref_leaves):
+        e = scaled_err(a.grad, b.grad)
+        assert e < GRAD_RTOL, (name, e)
+    assert torch.equal(ndc.grad, leaves[0].grad)   # ndc receives the uv gradient
+
+
+def test_projection_backward(small):
+    p = small
+    g = torch.Generator().manual_seed(11)
+    pos = p.pos.detach().clone().requires_grad_(True)
+    sc = p.sc.detach().clone().requires_grad_(True)
+    q = p.q.detach().clone().requires_grad_(True)
+    intr = p.intr.detach().clone().requires_grad_(True)
+    extr = p.extr.detach().clone().requires_grad_(True)
+    uv, depth = ops.project_point(pos, intr, extr, p.W, p.H, nearest=0.2)
+    vis = depth != 0
+    cov = ops.compute_cov3d(sc, q, vis)
+    conic, radius, tiles = ops.ewa_project(pos, cov, intr, extr, uv, p.W, p.H, vis)
+    ups = [torch.randn(t.shape, generator=g) for t in (uv, depth, conic)]
+    torch.autograd.backward([uv, depth, conic], [u.to(DEV) for u in ups])
+
+    r = [cpu(t, torch.float64).requires_grad_(True) for t in (p.pos, p.sc, p.q, p.intr, p.extr)]
+    uv_o, d_o = O.project_point(r[0], r[3], r[4], p.W, p.H, nearest=0.2)
+    vis_o = cpu(vis)
+    cov_o = O.compute_cov3d(r[1], r[2], vis_o)
+    conic_o = O.ewa_project(r[0], cov_o, r[3], r[4], cpu(uv), p.W, p.H, vis_o)[0]
+    # cull decisions of the float64 rendition must match the GPU's
+    keep = (cpu(radius) > 0)
+    conic_o = torch.where(keep[:, None], conic_o, torch.zeros_like(conic_o))
+    torch.autograd.backward([uv_o, d_o, conic_o], [u.double() for u in ups])
+    for name, a, b in zip(("xyz", "scale", "quat", "intr", "extr"), (pos, sc, q, intr, extr), r):
+        e = scaled_err(a.grad, b.grad)
+        assert e < GRAD_RTOL, (name, e)
+
+
+def _render_chain_gpu(p, leaves, bg=0.0):
+    pos, sc, q, op, shs, intr, extr = leaves
+    d = pos - p.center[None]
+    d = d / d.norm(dim=1, keepdim=True)
+    rgb = (ops.compute_sh(shs.permute(0, 2, 1), d) + 0.5).clamp(min=0)
+    uv, depth = ops.project_point(pos, intr, extr, p.W, p.H, nearest=0.2)
+    vis = depth != 0
+    cov = ops.compute_cov3d(sc, q, vis)
+    conic, radius, tiles = ops.ewa_project(pos, cov, intr, extr, uv, p.W, p.H, vis)
+    ids, rng = ops.sort_gaussian(uv, depth, p.W, p.H, radius, tiles)
+    feat = torch.cat([rgb, depth], 1)
+    ndc = torch.zeros_like(uv, requires_grad=True)
+    img = ops.alpha_blending(uv, conic, op, feat, ids, rng, bg, p.W, p.H, ndc)
+    return img, ids, rng, vis, radius, ndc
+
+
+def test_end_to_end_gradients_match_oracle(small):
+    """Full MsplatRender chain, L1 loss against a random target (the small
+    workload), gradients for every Gaussian parameter and the camera."""
+    p = small
+    g = torch.Generator().manual_seed(21)
+    target = torch.rand(4, p.H, p.W, generator=g)
+    leaves = [t.detach().clone().requires_grad_(True) for t in (p.pos, p.sc, p.q, p.op, p.shs, p.intr, p.extr)]
+    img, ids, rng, vis, radius, ndc = _render_chain_gpu(p, leaves)
+    loss = (img - target.to(DEV)).abs().mean()
+    loss.backward()
+
+    r = [cpu(t, torch.float64).requires_grad_(True) for t in (p.pos, p.sc, p.q, p.op, p.shs, p.intr, p.extr)]
+    pos, sc, q, op, shs, intr, extr = r
+    d = pos - cpu(p.center, torch.float64)[None]
+    d = d / d.norm(dim=1, keepdim=True)
+    rgb = (O.compute_sh(shs.permute(0, 2, 1), d) + 0.5).clamp(min=0)
+    uv, depth = O.project_point(pos, intr, extr, p.W, p.H, nearest=0.2)
+    vis_o = cpu(vis)
+    cov = O.compute_cov3d(sc, q, vis_o)
+    conic = O.ewa_project(pos, cov, intr, extr, uv.detach().float(), p.W, p.H, vis_o)[0]
+    feat = torch.cat([rgb, depth], 1)
+    img_o = O.alpha_blending(uv, conic, op, feat, cpu(ids), cpu(rng), 0.0, p.W, p.H)
+    loss_o = (img_o - target.double()).abs().mean()
+    loss_o.backward()
+    assert abs(float(loss) - float(loss_o)) < 1e-5
+    # A float32 and a float64 rendition may take a different skip/stop
+    # decision for a few (pixel, splat) pairs that sit on a threshold, or a
+    # different sign of |img - target| for a pixel within rounding of its
+    # target; those move a handful of entries.  The bar is therefore on the
+    # relative L2 error of each gradient tensor (1e-4), with a looser bound on
+    # the worst single entry.
+    for name, a, b in zip(("position", "scale", "rotation", "opacity", "shs", "intr", "extr"), leaves, r):
+        A, B = a.grad.detach().double().cpu(), b.grad.double()
+        rel_l2 = float((A - B).norm() / B.norm().clamp(min=1e-30))
+        e = scaled_err(a.grad, b.grad)
+        assert rel_l2 < GRAD_RTOL and e < 2e-2, (name, rel_l2, e)
+
+
+# ------------------------------------------------------------ edge cases ---
+@pytest.mark.parametrize("W,H", [(250, 130), (16, 16), (10, 7), (33, 17)])
+def test_odd_image_sizes(W, H):
+    scene, _ = WL.scene_small(3, n=3000)
+    g = torch.Generator().manual_seed(W * 1000 + H)
+    cam = WL.make_camera(g, W, H, float(max(W, H)), 4.0)
+    p = Prepared(scene, cam)
+    ids_o, rng_o = O.sort_gaussian(cpu(p.uv), cpu(p.depth), W, H, cpu(p.radius), cpu(p.tiles))
+    assert torch.equal(cpu(p.ids), ids_o) and torch.equal(cpu(p.rng), rng_o)
+    img = ops.alpha_blending(p.uv, p.conic, p.op, p.feat, p.ids, p.rng, 0.1, W, H)
+    ref = O.alpha_blending(*blend_inputs64(p), cpu(p.ids), cpu(p.rng), 0.1, W, H)
+    assert img.shape == (4, H, W)
+    assert (cpu(img, torch.float64)[:3] - ref[:3]).abs().max() < IMG_ATOL
+
+
+def test_everything_culled_gives_background():
+    scene, cam = WL.scene_small(4, n=500)
+    p_pos = scene.position + 100.0   # all far outside the frustum extent
+    scene = WL.Scene(p_pos, scene.log_scale, scene.quat_raw, scene.opacity_logit, scene.shs)
+    p = Prepared(scene, cam)
+    assert p.ids.numel() == 0 and int(p.rng.abs().sum()) == 0
+    img = ops.alpha_blending(p.uv, p.conic, p.op, p.feat, p.ids, p.rng, 0.3, p.W, p.H)
+    assert torch.all(img == 0.3)
+    leaves = [t.detach().clone().requires_grad_(True) for t in (p.uv, p.conic, p.op, p.feat)]
+    ops.alpha_blending(*leaves, p.ids, p.rng, 0.3, p.W, p.H).sum().backward()
+    assert all(float(t.grad.abs().max()) == 0 for t in leaves)
+
+
+@pytest.mark.parametrize("C", [1, 3, 7, 12, 26])
+def test_channel_counts(small, C):
+    p = small
+    g = torch.Generator().manual_seed(C)
+    feat = torch.rand(p.pos.shape[0], C, generator=g).to(DEV).requires_grad_(True)
+    img = ops.alpha_blending(p.uv, p.conic, p.op, feat, p.ids, p.rng, 0.0, p.W, p.H)
+    up = torch.randn(img.shape, generator=g)
+    img.backward(up.to(DEV))
+    u, c, o, _ = blend_inputs64(p)
+    f64 = cpu(feat, torch.float64).requires_grad_(True)
+    ref = O.alpha_blending(u, c, o, f64, cpu(p.ids), cpu(p.rng), 0.0, p.W, p.H)
+    ref.backward(up.double())
+    assert (cpu(img, torch.float64) - ref).abs().max() < IMG_ATOL
+    assert scaled_err(feat.grad, f64.grad) < GRAD_RTOL
+
+
+def test_side_stream_and_reuse(small):
+    p = small
+    ref = ops.alpha_blending(p.uv, p.conic, p.op, p.feat, p.ids, p.rng, 0.0, p.W, p.H)
+    s = torch.cuda.Stream()
+    with torch.cuda.stream(s):
+        ids, rng = ops.sort_gaussian(p.uv, p.depth, p.W, p.H, p.radius, p.tiles)
+        img = ops.alpha_blending(p.uv, p.conic, p.op, p.feat, ids, rng, 0.0, p.W, p.H)
+    s.synchronize()
+    assert torch.equal(ids, p.ids) and torch.equal(img, ref)
+    ops.check_device_status()
+
+
+def test_bad_arguments_raise(small):
+    p = small
+    with pytest.raises(ValueError):
+        ops.compute_sh(torch.zeros(p.dirs.shape[0], 3, 5, device=DEV), p.dirs)
+    with pytest.raises(ValueError):
+        ops.project_point(p.pos.cpu(), p.intr, p.extr, p.W, p.H)
+    with pytest.raises(ValueError):
+        ops.alpha_blending(p.uv, p.conic, p.op, p.feat, p.ids, p.rng[:-1], 0.0, p.W, p.H)
+    with pytest.raises(ValueError):
+        ops.sort_gaussian(p.uv, p.depth, p.W, p.H, p.radius.float(), p.tiles)
