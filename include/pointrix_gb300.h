@@ -142,12 +142,14 @@ int pgb_sort_gaussian_finish(const float* uv, const int32_t* radius, const int32
  * the backward) and writes out [C,H,W], final_T [H,W] and n_contrib [H,W]
  * (list entries up to the last contributor).  The backward writes d_uv
  * [N,2] (also the gradient msplat routes to its `ndc` argument), d_conic
- * [N,3], d_opacity [N,1], d_feature [N,C]; grad_records is scratch of the
- * same size as records.  `info` is one device int64 word that the caller
+ * [N,3], d_opacity [N,1], d_feature [N,C]; grad_records is scratch of
+ * N * pgb_blend_grad_record_floats(C) floats.  `info` is one device int64 word that the caller
  * zeroes beforehand; a bounded device-side wait that expires writes
  * PGB_ERR_TIMEOUT into it.
  * ------------------------------------------------------------------- */
 int pgb_blend_record_floats(int channels);
+/* Floats per Gaussian of the backward's gradient scratch (16 or 32). */
+int pgb_blend_grad_record_floats(int channels);
 int pgb_alpha_blending_forward(const float* uv, const float* conic, const float* opacity,
                                const float* feature, int64_t n, int channels, const int32_t* ids,
                                int64_t k, const int32_t* tile_range, float bg, int width,

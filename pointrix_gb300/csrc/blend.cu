@@ -112,6 +112,15 @@ __device__ inline void issue_batch(const float* __restrict__ records,
 }
 
 // ------------------------------------------------------------------ pack
+// Record of one splat: u, v, a, b, c, o, tau, f_0..f_{C-1}, zero padding to
+// a multiple of 4 floats.  tau bounds the splat's support: alpha >= 1/255
+// requires Q(d) = a dx^2 + 2 b dx dy + c dy^2 <= 2 ln(255 o); tau is that
+// level plus a small margin, -1 when o < 1/255 (the splat never passes the
+// alpha test) and +inf when the conic is not positive definite (no bound).
+constexpr int kRecFeat = 7;  // offset of the first feature in a record
+__host__ __device__ constexpr int rec_floats(int C) { return ((kRecFeat + C + 3) / 4) * 4; }
+__host__ __device__ constexpr int grad_floats(int C) { return 6 + C <= 16 ? 16 : 32; }
+
 template <int RF>
 __global__ void pack_kernel(const float* __restrict__ uv, const float* __restrict__ conic,
                             const float* __restrict__ opacity, const float* __restrict__ feature,
@@ -121,16 +130,88 @@ __global__ void pack_kernel(const float* __restrict__ uv, const float* __restric
     float r[RF];
     r[0] = uv[2 * i];
     r[1] = uv[2 * i + 1];
-    r[2] = conic[3 * i];
-    r[3] = conic[3 * i + 1];
-    r[4] = conic[3 * i + 2];
-    r[5] = opacity[i];
+    const float a = conic[3 * i], b = conic[3 * i + 1], c = conic[3 * i + 2];
+    const float o = opacity[i];
+    r[2] = a;
+    r[3] = b;
+    r[4] = c;
+    r[5] = o;
+    float tau;
+    if (!(isfinite(r[0]) && isfinite(r[1]) && isfinite(o)))
+      tau = __int_as_float(0x7f800000);  // keep whatever the per-pixel arithmetic does
+    else if (!(o >= 0.999f / 255.0f))
+      tau = -1.0f;
+    else if (a > 0.f && c > 0.f && a * c - b * b > 0.f && isfinite(a) && isfinite(b) && isfinite(c))
+      tau = 2.0f * logf(255.0f * o) * 1.0001f + 1e-3f;
+    else
+      tau = __int_as_float(0x7f800000);  // +inf: never culled
+    r[6] = tau;
 #pragma unroll
-    for (int c = 0; c < RF - 6; ++c) r[6 + c] = c < C ? feature[i * C + c] : 0.f;
-    float4* o = reinterpret_cast<float4*>(records + i * RF);
+    for (int k = 0; k < RF - kRecFeat; ++k) r[kRecFeat + k] = k < C ? feature[i * C + k] : 0.f;
+    float4* dst = reinterpret_cast<float4*>(records + i * RF);
 #pragma unroll
-    for (int q = 0; q < RF / 4; ++q) o[q] = make_float4(r[4 * q], r[4 * q + 1], r[4 * q + 2], r[4 * q + 3]);
+    for (int q = 0; q < RF / 4; ++q)
+      dst[q] = make_float4(r[4 * q], r[4 * q + 1], r[4 * q + 2], r[4 * q + 3]);
   }
+}
+
+// Pixel of thread t in a 16x16 tile: warp w covers the 8x4 box at
+// (8 (w % 2), 4 (w / 2)); lane l is pixel (l % 8, l / 8) of that box.
+__device__ __forceinline__ void tile_pixel(int tile, int gx, int& px, int& py, int& bx0, int& by0) {
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  bx0 = (tile % gx) * kTile + 8 * (w & 1);
+  by0 = (tile / gx) * kTile + 4 * (w >> 1);
+  px = bx0 + (l & 7);
+  py = by0 + (l >> 3);
+}
+
+// Conservative test: can the splat pass the alpha test at any pixel centre
+// of the box [x0, x0 + 7] x [y0, y0 + 3]?  Minimum of the (convex) quadratic
+// form over the box -- zero if the centre is inside, else the least of its
+// four edge minima -- compared with tau after subtracting a bound on the
+// rounding of the per-pixel float evaluation (1e-5 of the largest term
+// magnitude over the box, far above the ~2e-7 that evaluation can lose).
+__device__ __forceinline__ bool splat_may_touch_box(const float* rec, float x0, float y0) {
+  const float tau = rec[6];
+  if (!(tau < 3.0e38f)) return true;
+  const float u = rec[0], v = rec[1], a = rec[2], b = rec[3], c = rec[4];
+  const float dx0 = u - (x0 + 7.f), dx1 = u - x0;
+  const float dy0 = v - (y0 + 3.f), dy1 = v - y0;
+  if (dx0 <= 0.f && dx1 >= 0.f && dy0 <= 0.f && dy1 >= 0.f) return tau >= 0.f;
+  const float ia = 1.0f / a, ic = 1.0f / c;
+  float qmin = 3.0e38f;
+#pragma unroll
+  for (int e = 0; e < 2; ++e) {
+    const float dx = e ? dx1 : dx0;
+    const float dy = fminf(fmaxf(-b * dx * ic, dy0), dy1);
+    qmin = fminf(qmin, a * dx * dx + 2.f * b * dx * dy + c * dy * dy);
+    const float ey = e ? dy1 : dy0;
+    const float ex = fminf(fmaxf(-b * ey * ia, dx0), dx1);
+    qmin = fminf(qmin, a * ex * ex + 2.f * b * ex * ey + c * ey * ey);
+  }
+  const float mx = fmaxf(fabsf(dx0), fabsf(dx1)) + fmaxf(fabsf(dy0), fabsf(dy1));
+  const float slack = 1e-5f * (a + c + 2.f * fabsf(b)) * mx * mx + 1e-4f;
+  return qmin - slack <= tau;
+}
+
+// Builds this warp's list of batch slots (in increasing order) whose splat
+// may touch the warp's pixel box; slots >= cnt are ignored.  Returns the
+// list length.
+__device__ __forceinline__ int warp_cull(const float* stage, int RF, int cnt, float x0, float y0,
+                                         uint8_t* list) {
+  const int lane = threadIdx.x & 31;
+  const uint32_t lt = (1u << lane) - 1u;
+  int n = 0;
+#pragma unroll
+  for (int k = 0; k < kBatch / 32; ++k) {
+    const int j = k * 32 + lane;
+    const bool keep = j < cnt && splat_may_touch_box(stage + j * RF, x0, y0);
+    const uint32_t m = __ballot_sync(0xffffffffu, keep);
+    if (keep) list[n + __popc(m & lt)] = (uint8_t)j;
+    n += __popc(m);
+  }
+  __syncwarp();
+  return n;
 }
 
 // --------------------------------------------------------------- forward
@@ -142,12 +223,14 @@ __global__ void __launch_bounds__(kBlendThreads) blend_fwd_kernel(
   extern __shared__ __align__(128) float smem[];
   __shared__ __align__(8) uint64_t bars[2];
 
+  __shared__ uint8_t s_list[kBlendThreads / 32][kBatch];
   const int gx = grid_x(W);
   const int tile = blockIdx.x;
-  const int px = (tile % gx) * kTile + (threadIdx.x & 15);
-  const int py = (tile / gx) * kTile + (threadIdx.x >> 4);
+  int px, py, bx0, by0;
+  tile_pixel(tile, gx, px, py, bx0, by0);
   const bool inside = px < W && py < H;
   const float pxf = (float)px, pyf = (float)py;
+  uint8_t* my_list = s_list[threadIdx.x >> 5];
 
   if (threadIdx.x == 0) {
     mbar_init(&bars[0], kBlendThreads / 32);
@@ -180,8 +263,10 @@ __global__ void __launch_bounds__(kBlendThreads) blend_fwd_kernel(
     const int cnt = (int)(end - first < kBatch ? end - first : kBatch);
     const float* st = smem + buf * kBatch * RF;
     if (!timed_out && !__all_sync(0xffffffffu, done)) {
+      const int nl = warp_cull(st, RF, cnt, (float)bx0, (float)by0, my_list);
       if (!done) {
-        for (int j = 0; j < cnt; ++j) {
+        for (int t = 0; t < nl; ++t) {
+          const int j = my_list[t];
           const float4 r0 = *reinterpret_cast<const float4*>(st + j * RF);
           const float2 r1 = *reinterpret_cast<const float2*>(st + j * RF + 4);
           const float dx = __fsub_rn(r0.x, pxf), dy = __fsub_rn(r0.y, pyf);
@@ -195,13 +280,14 @@ __global__ void __launch_bounds__(kBlendThreads) blend_fwd_kernel(
             break;
           }
           const float w = alpha * T;
-          const float* f = st + j * RF + 6;
+          const float* f = st + j * RF + kRecFeat;
 #pragma unroll
           for (int c = 0; c < NC; ++c) acc[c] = fmaf(f[c], w, acc[c]);
           T = test_T;
           last = (int)(first - start) + j + 1;
         }
       }
+      __syncwarp();
     }
     const int ndone = __syncthreads_count(done || timed_out);
     if (ndone == kBlendThreads || timed_out) {
@@ -242,27 +328,29 @@ __device__ __forceinline__ float warp_reduce_scatter(float (&v)[GR]) {
   return v[0];
 }
 
-template <int NC, int RF>
+template <int NC, int RF, int GR>
 __global__ void __launch_bounds__(kBlendThreads) blend_bwd_kernel(
     const float* __restrict__ records, const int32_t* __restrict__ ids,
     const int2* __restrict__ ranges, float bg, int W, int H, int C,
     const float* __restrict__ final_T, const int32_t* __restrict__ n_contrib,
     const float* __restrict__ d_out, float* __restrict__ grad_records,
     int64_t* __restrict__ info) {
-  static_assert(RF == 16 || RF == 32, "gradient records are 16 or 32 floats");
+  static_assert(GR == 16 || GR == 32, "gradient records are 16 or 32 floats");
   extern __shared__ __align__(128) float smem[];
   __shared__ __align__(8) uint64_t bars[2];
   __shared__ int s_max_nc;
   __shared__ uint8_t s_touched[kBatch];
-  float* gacc = smem + 2 * kBatch * RF;  // [kBatch][RF]
+  __shared__ uint8_t s_list[kBlendThreads / 32][kBatch];
+  float* gacc = smem + 2 * kBatch * RF;  // [kBatch][GR]
 
   const int gx = grid_x(W);
   const int tile = blockIdx.x;
-  const int px = (tile % gx) * kTile + (threadIdx.x & 15);
-  const int py = (tile / gx) * kTile + (threadIdx.x >> 4);
+  int px, py, bx0, by0;
+  tile_pixel(tile, gx, px, py, bx0, by0);
   const bool inside = px < W && py < H;
   const float pxf = (float)px, pyf = (float)py;
   const int lane = threadIdx.x & 31;
+  uint8_t* my_list = s_list[threadIdx.x >> 5];
 
   if (threadIdx.x == 0) {
     mbar_init(&bars[0], kBlendThreads / 32);
@@ -270,7 +358,7 @@ __global__ void __launch_bounds__(kBlendThreads) blend_bwd_kernel(
     fence_mbar_init();
     s_max_nc = 0;
   }
-  for (int i = threadIdx.x; i < kBatch * RF; i += kBlendThreads) gacc[i] = 0.f;
+  for (int i = threadIdx.x; i < kBatch * GR; i += kBlendThreads) gacc[i] = 0.f;
   s_touched[threadIdx.x] = 0;
   __syncthreads();
 
@@ -296,6 +384,9 @@ __global__ void __launch_bounds__(kBlendThreads) blend_bwd_kernel(
   const int2 rg = ranges[tile];
   const int64_t start = rg.x;
   const int max_nc = s_max_nc;
+  int warp_nc = nc;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) warp_nc = max(warp_nc, __shfl_xor_sync(0xffffffffu, warp_nc, o));
   const int nb = (max_nc + kBatch - 1) / kBatch;
 
   // batch b covers list positions [hi_b - kBatch, hi_b) with hi_b = max_nc - b*kBatch,
@@ -315,11 +406,13 @@ __global__ void __launch_bounds__(kBlendThreads) blend_bwd_kernel(
     if (timed_out && threadIdx.x == 0) set_info(info, PGB_ERR_TIMEOUT);
     const float* st = smem + buf * kBatch * RF;
     if (!timed_out) {
-      for (int j = hi - 1; j >= lo; --j) {
-        const int slot = j - lo;
-        float v[RF];
+      const int nl = warp_cull(st, RF, min(hi, warp_nc) - lo, (float)bx0, (float)by0, my_list);
+      for (int t = nl - 1; t >= 0; --t) {
+        const int slot = my_list[t];
+        const int j = lo + slot;
+        float v[GR];
 #pragma unroll
-        for (int q = 0; q < RF; ++q) v[q] = 0.f;
+        for (int q = 0; q < GR; ++q) v[q] = 0.f;
         bool contrib = false;
         if (j < nc) {
           const float4 r0 = *reinterpret_cast<const float4*>(st + slot * RF);
@@ -334,7 +427,7 @@ __global__ void __launch_bounds__(kBlendThreads) blend_bwd_kernel(
               contrib = true;
               const float om = __fsub_rn(1.0f, alpha);
               T = __fdividef(T, om);
-              const float* f = st + slot * RF + 6;
+              const float* f = st + slot * RF + kRecFeat;
               float dalpha = 0.f;
               const float wT = alpha * T;
 #pragma unroll
@@ -357,23 +450,24 @@ __global__ void __launch_bounds__(kBlendThreads) blend_bwd_kernel(
           }
         }
         if (__any_sync(0xffffffffu, contrib)) {
-          const float s = warp_reduce_scatter<RF>(v);
-          if (RF == 32) {
-            if (lane < 6 + NC) atomicAdd(&gacc[slot * RF + lane], s);
+          const float s = warp_reduce_scatter<GR>(v);
+          if (GR == 32) {
+            if (lane < 6 + NC) atomicAdd(&gacc[slot * GR + lane], s);
           } else if ((lane & 1) == 0 && (lane >> 1) < 6 + NC) {
-            atomicAdd(&gacc[slot * RF + (lane >> 1)], s);
+            atomicAdd(&gacc[slot * GR + (lane >> 1)], s);
           }
           if (lane == 0) s_touched[slot] = 1;
         }
       }
+      __syncwarp();
     }
     __syncthreads();
     // flush this batch's per-splat sums: one set of vector atomics per splat
     const int t = threadIdx.x;
     if (t < hi - lo && s_touched[t]) {
       const int32_t g = ids[start + lo + t];
-      float4* dst = reinterpret_cast<float4*>(grad_records + (int64_t)g * RF);
-      float4* srcv = reinterpret_cast<float4*>(gacc + t * RF);
+      float4* dst = reinterpret_cast<float4*>(grad_records + (int64_t)g * GR);
+      float4* srcv = reinterpret_cast<float4*>(gacc + t * GR);
 #pragma unroll
       for (int q = 0; q < (6 + NC + 3) / 4; ++q) {
         atomicAdd(dst + q, srcv[q]);
@@ -416,13 +510,11 @@ __global__ void unpack_kernel(const float* __restrict__ g, int64_t n, int C,
 }
 
 // ------------------------------------------------------------- dispatch
-inline int record_floats(int C) { return C <= 10 ? 16 : 32; }
-
 template <int NC>
 static int launch_fwd_nc(const float* records, const int32_t* ids, const int2* ranges, float bg,
                          int W, int H, int C, float* out, float* fT, int32_t* ncon,
                          int64_t* info, cudaStream_t s) {
-  constexpr int RF = NC <= 10 ? 16 : 32;
+  constexpr int RF = rec_floats(NC);
   const int tiles = grid_x(W) * grid_y(H);
   const size_t smem = 2 * kBatch * RF * sizeof(float);
   auto kern = blend_fwd_kernel<NC, RF>;
@@ -437,10 +529,11 @@ template <int NC>
 static int launch_bwd_nc(const float* records, const int32_t* ids, const int2* ranges, float bg,
                          int W, int H, int C, const float* fT, const int32_t* ncon,
                          const float* dout, float* grec, int64_t* info, cudaStream_t s) {
-  constexpr int RF = NC <= 10 ? 16 : 32;
+  constexpr int RF = rec_floats(NC);
+  constexpr int GR = grad_floats(NC);
   const int tiles = grid_x(W) * grid_y(H);
-  const size_t smem = 3 * kBatch * RF * sizeof(float);
-  auto kern = blend_bwd_kernel<NC, RF>;
+  const size_t smem = (2 * RF + GR) * kBatch * sizeof(float);
+  auto kern = blend_bwd_kernel<NC, RF, GR>;
   if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
       cudaSuccess)
     return PGB_ERR_CUDA;
@@ -468,7 +561,12 @@ extern "C" {
 
 int pgb_blend_record_floats(int channels) {
   if (channels < 1 || channels > 26) return -1;
-  return record_floats(channels);
+  return rec_floats(nc_bucket(channels));
+}
+
+int pgb_blend_grad_record_floats(int channels) {
+  if (channels < 1 || channels > 26) return -1;
+  return grad_floats(nc_bucket(channels));
 }
 
 int pgb_alpha_blending_forward(const float* uv, const float* conic, const float* opacity,
@@ -481,19 +579,14 @@ int pgb_alpha_blending_forward(const float* uv, const float* conic, const float*
   if (!tile_range || !out || !final_T || !n_contrib || (k > 0 && !ids)) return PGB_ERR_INVALID;
   if (n > 0 && (!uv || !conic || !opacity || !feature || !records)) return PGB_ERR_INVALID;
   cudaStream_t s = as_stream(stream);
-  const int RF = record_floats(channels);
-  if (n > 0) {
-    if (RF == 16)
-      pack_kernel<16><<<stream_grid(n), kStreamThreads, 0, s>>>(uv, conic, opacity, feature, n,
-                                                                channels, records);
-    else
-      pack_kernel<32><<<stream_grid(n), kStreamThreads, 0, s>>>(uv, conic, opacity, feature, n,
-                                                                channels, records);
-  }
   const int2* rg = reinterpret_cast<const int2*>(tile_range);
   switch (nc) {
-#define PGB_CASE(N) \
-  case N:           \
+#define PGB_CASE(N)                                                                             \
+  case N:                                                                                       \
+    if (n > 0)                                                                                  \
+      pack_kernel<rec_floats(N)><<<stream_grid(n), kStreamThreads, 0, s>>>(uv, conic, opacity,  \
+                                                                           feature, n, channels, \
+                                                                           records);            \
     return launch_fwd_nc<N>(records, ids, rg, bg, width, height, channels, out, final_T, n_contrib, info, s);
     PGB_FOR_NC(PGB_CASE)
 #undef PGB_CASE
@@ -515,8 +608,8 @@ int pgb_alpha_blending_backward(const float* records, int64_t n, int channels,
     return PGB_ERR_INVALID;
   if (n == 0) return PGB_OK;
   cudaStream_t s = as_stream(stream);
-  const int RF = record_floats(channels);
-  if (cudaMemsetAsync(grad_records, 0, (size_t)n * RF * sizeof(float), s) != cudaSuccess)
+  const int GRf = grad_floats(nc);
+  if (cudaMemsetAsync(grad_records, 0, (size_t)n * GRf * sizeof(float), s) != cudaSuccess)
     return PGB_ERR_CUDA;
   const int2* rg = reinterpret_cast<const int2*>(tile_range);
   int st = PGB_ERR_INVALID;
@@ -532,7 +625,7 @@ int pgb_alpha_blending_backward(const float* records, int64_t n, int channels,
       break;
   }
   if (st != PGB_OK) return st;
-  if (RF == 16)
+  if (GRf == 16)
     unpack_kernel<16><<<stream_grid(n), kStreamThreads, 0, s>>>(grad_records, n, channels, d_uv,
                                                                 d_conic, d_opacity, d_feature);
   else

@@ -13,10 +13,11 @@
 //      and sums tiles_touched into K;
 //   2. four onesweep passes sort the N Gaussians by depth (stable, so equal
 //      depths stay in id order);
-//   3. scan_emit: a single-pass decoupled-look-back scan of tiles_touched in
-//      depth order gives each Gaussian its output offset, and the same
-//      thread writes its (tile id, Gaussian id) pairs, accumulating the tile
-//      digit histograms;
+//   3. scan_rect: a single-pass decoupled-look-back scan of tiles_touched in
+//      depth order gives each Gaussian its output offset and tile rectangle;
+//      emit then writes the (tile id, Gaussian id) pairs chunk by chunk of
+//      the output (load-balanced however unevenly the tiles are spread over
+//      Gaussians) and accumulates the tile digit histograms;
 //   4. ceil(log2(T)/8) stable onesweep passes (one for T <= 256, two up to
 //      65,536 tiles) sort the pairs by tile id;
 //   5. a range pass marks each tile's [start, end).
@@ -242,32 +243,51 @@ __global__ void __launch_bounds__(kSortThreads) onesweep_kernel(
 }
 
 // ---------------------------------------------------------------------------
-// 3. scan of tiles_touched in depth order + emission of (tile, id) pairs
+// 3a. scan of tiles_touched in depth order
+//
+// For depth-sorted position i (Gaussian g = order[i]) writes its output
+// offset offs[i], its tile rectangle rect[i] = (x0 | y0 << 16, w | h << 16),
+// and, for every emission chunk boundary b * kEmitChunk that falls inside
+// [offs[i], offs[i] + count), chunk_first[b] = i.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(kSortThreads) scan_emit_kernel(
+constexpr int kEmitChunk = 2048;
+constexpr int kEmitThreads = 256;
+
+__global__ void __launch_bounds__(kSortThreads) scan_rect_kernel(
     const uint32_t* __restrict__ order, int64_t n, const int32_t* __restrict__ tiles,
     const int32_t* __restrict__ radius, const float* __restrict__ uv, int W, int H, int64_t K,
-    int tile_passes, uint32_t* __restrict__ status, uint32_t* __restrict__ part_counter,
-    uint32_t* __restrict__ tkeys, uint32_t* __restrict__ tvals, uint32_t* __restrict__ tile_hist,
+    uint32_t* __restrict__ status, uint32_t* __restrict__ part_counter,
+    uint32_t* __restrict__ offs, uint2* __restrict__ rect, uint32_t* __restrict__ chunk_first,
     int64_t* __restrict__ info) {
-  __shared__ uint32_t s_hist[kMaxTilePasses][256];
   __shared__ uint32_t s_warp_tot[kSortThreads / 32];
   __shared__ uint32_t s_part, s_prior;
   if (threadIdx.x == 0) s_part = atomicAdd(part_counter, 1u);
-  for (int i = threadIdx.x; i < kMaxTilePasses * 256; i += blockDim.x) (&s_hist[0][0])[i] = 0;
   __syncthreads();
   const int part = (int)s_part;
   const int64_t base = (int64_t)part * kScanPart + (int64_t)threadIdx.x * kScanItems;
+  const int gx = grid_x(W), gy = grid_y(H);
 
-  uint32_t g[kScanItems];
   uint32_t cnt[kScanItems];
+  uint2 rc[kScanItems];
   uint32_t sum = 0;
 #pragma unroll
   for (int it = 0; it < kScanItems; ++it) {
     const int64_t e = base + it;
-    g[it] = e < n ? order[e] : 0u;
     cnt[it] = 0;
-    if (e < n && radius[g[it]] > 0) cnt[it] = (uint32_t)max(tiles[g[it]], 0);
+    rc[it] = make_uint2(0u, 0u);
+    if (e < n) {
+      const uint32_t g = order[e];
+      const int r = radius[g];
+      if (r > 0) {
+        cnt[it] = (uint32_t)max(tiles[g], 0);
+        const float2 p = reinterpret_cast<const float2*>(uv)[g];
+        int x0, x1, y0, y1;
+        tile_rect(p.x, p.y, (float)r, gx, gy, x0, x1, y0, y1);
+        if ((int64_t)(x1 - x0) * (y1 - y0) != (int64_t)cnt[it]) set_error(info, PGB_ERR_MISMATCH);
+        rc[it] = make_uint2((uint32_t)x0 | ((uint32_t)y0 << 16),
+                            (uint32_t)(x1 - x0) | ((uint32_t)(y1 - y0) << 16));
+      }
+    }
     sum += cnt[it];
   }
   uint32_t total;
@@ -286,39 +306,99 @@ __global__ void __launch_bounds__(kSortThreads) scan_emit_kernel(
   }
   __syncthreads();
   int64_t off = (int64_t)s_prior + excl;
-  const int gx = grid_x(W), gy = grid_y(H);
-#pragma unroll 1
+#pragma unroll
   for (int it = 0; it < kScanItems; ++it) {
-    const uint32_t c = cnt[it];
-    if (c == 0) continue;
-    const uint32_t gi = g[it];
-    const float2 p = reinterpret_cast<const float2*>(uv)[gi];
-    int x0, x1, y0, y1;
-    tile_rect(p.x, p.y, (float)radius[gi], gx, gy, x0, x1, y0, y1);
-    const int64_t rect = (int64_t)(x1 - x0) * (y1 - y0);
-    if (rect != (int64_t)c) set_error(info, PGB_ERR_MISMATCH);
-    if (off + (int64_t)c > K) {
-      set_error(info, PGB_ERR_OVERFLOW);
-      break;
-    }
-    uint32_t j = 0;
-    for (int ty = y0; ty < y1 && j < c; ++ty) {
-      for (int tx = x0; tx < x1 && j < c; ++tx, ++j) {
-        const uint32_t tid = (uint32_t)(ty * gx + tx);
-        tkeys[off + j] = tid;
-        tvals[off + j] = gi;
-        for (int p2 = 0; p2 < tile_passes; ++p2) atomicAdd(&s_hist[p2][(tid >> (8 * p2)) & 0xFF], 1u);
+    const int64_t e = base + it;
+    if (e < n) {
+      const int64_t end = off + cnt[it];
+      if (end > K) {
+        set_error(info, PGB_ERR_OVERFLOW);
+      } else {
+        offs[e] = (uint32_t)off;
+        rect[e] = rc[it];
+        // chunk boundaries owned by this Gaussian, and the owner of the
+        // last entry (stored after the last chunk's)
+        for (int64_t b = (off + kEmitChunk - 1) / kEmitChunk; b * kEmitChunk < end; ++b)
+          chunk_first[b] = (uint32_t)e;
+        if (off < K && K <= end) chunk_first[(K + kEmitChunk - 1) / kEmitChunk] = (uint32_t)e;
       }
+      off = end;
     }
-    for (; j < c; ++j) {  // only on a tiles_touched mismatch: keep the buffer well formed
-      tkeys[off + j] = 0;
-      tvals[off + j] = gi;
-      for (int p2 = 0; p2 < tile_passes; ++p2) atomicAdd(&s_hist[p2][0], 1u);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// 3b. emission of (tile id, Gaussian id) pairs over output chunks
+//
+// CTA b writes entries [b*kEmitChunk, min(K, (b+1)*kEmitChunk)): it stages
+// the offsets, rectangles and ids of the Gaussians that own them in shared
+// memory, and each thread finds the owner of its entries by binary search,
+// so every CTA does the same amount of work however unevenly the tiles are
+// spread over Gaussians.  Writes are coalesced.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kEmitThreads) emit_kernel(
+    const uint32_t* __restrict__ order, const uint32_t* __restrict__ offs,
+    const uint2* __restrict__ rect, const uint32_t* __restrict__ chunk_first, int64_t n_sorted,
+    int64_t K, int W, int tile_passes, uint32_t* __restrict__ tkeys, uint32_t* __restrict__ tvals,
+    uint32_t* __restrict__ tile_hist, int64_t* __restrict__ info) {
+  constexpr int CAP = kEmitChunk + 1;
+  __shared__ uint32_t s_off[CAP];
+  __shared__ uint2 s_rect[CAP];
+  __shared__ uint32_t s_g[CAP];
+  __shared__ uint32_t s_hist[kMaxTilePasses][256];
+  const int gx = grid_x(W);
+  const int64_t e0 = (int64_t)blockIdx.x * kEmitChunk;
+  const int64_t e1 = min(K, e0 + kEmitChunk);
+  const int64_t nchunks = (K + kEmitChunk - 1) / kEmitChunk;
+  // owners of this chunk's first entry and of the next chunk's first entry
+  // (for the last chunk: of entry K - 1)
+  const int64_t i0 = chunk_first[blockIdx.x];
+  const int64_t i1 = chunk_first[blockIdx.x + 1];
+  const int64_t m = i1 - i0 + 1;
+  (void)nchunks;
+  for (int i = threadIdx.x; i < kMaxTilePasses * 256; i += kEmitThreads) (&s_hist[0][0])[i] = 0;
+  const bool staged = m >= 1 && m <= CAP && i1 < n_sorted;
+  if (staged) {
+    for (int64_t i = threadIdx.x; i < m; i += kEmitThreads) {
+      s_off[i] = offs[i0 + i];
+      s_rect[i] = rect[i0 + i];
+      s_g[i] = order[i0 + i];
     }
-    off += c;
   }
   __syncthreads();
-  for (int i = threadIdx.x; i < tile_passes * 256; i += blockDim.x) {
+  const bool ok_range = i0 <= i1 && i1 < n_sorted;
+  if (!ok_range && threadIdx.x == 0) set_error(info, PGB_ERR_OVERFLOW);
+  const uint32_t lane = threadIdx.x & 31;
+  // fixed trip count: every lane reaches the warp collectives below
+  for (int k = 0; k < kEmitChunk / kEmitThreads; ++k) {
+    const int64_t e = e0 + (int64_t)k * kEmitThreads + threadIdx.x;
+    const bool valid = ok_range && e < e1;
+    uint32_t tid = 0;  // a tiles_touched/rectangle mismatch leaves tile 0 (reported)
+    if (valid) {
+      // owner: the last position p in [i0, i1] with offs[p] <= e
+      int64_t lo = 0, hi = i1 - i0;
+      while (lo < hi) {
+        const int64_t mid = (lo + hi + 1) >> 1;
+        const uint32_t o = staged ? s_off[mid] : offs[i0 + mid];
+        if ((int64_t)o <= e) lo = mid; else hi = mid - 1;
+      }
+      const uint32_t o = staged ? s_off[lo] : offs[i0 + lo];
+      const uint2 rc = staged ? s_rect[lo] : rect[i0 + lo];
+      const uint32_t g = staged ? s_g[lo] : order[i0 + lo];
+      const uint32_t j = (uint32_t)(e - o);
+      const uint32_t w = rc.y & 0xFFFFu, h = rc.y >> 16;
+      if (w > 0 && j < w * h) tid = ((rc.x >> 16) + j / w) * (uint32_t)gx + (rc.x & 0xFFFFu) + j % w;
+      tkeys[e] = tid;
+      tvals[e] = g;
+    }
+    for (int p = 0; p < tile_passes; ++p) {
+      const uint32_t d = (tid >> (8 * p)) & 0xFFu;
+      const uint32_t peers = __match_any_sync(0xffffffffu, valid ? d : 256u + lane);
+      if (valid && (peers & lanemask_lt()) == 0) atomicAdd(&s_hist[p][d], (uint32_t)__popc(peers));
+    }
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < tile_passes * 256; i += kEmitThreads) {
     const uint32_t v = (&s_hist[0][0])[i];
     if (v) atomicAdd(tile_hist + i, v);
   }
@@ -348,7 +428,7 @@ inline size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
 struct ScratchN {
   size_t counters, depth_hist, tile_hist, depth_status, scan_status, zero_bytes;
-  size_t dk0, dv0, dk1, dv1, total;
+  size_t dk0, dv0, dk1, dv1, offs, rect, total;
   int parts, scan_parts;
 };
 
@@ -368,13 +448,16 @@ inline ScratchN layout_n(int64_t n) {
   L.dv0 = o; o += nb;
   L.dk1 = o; o += nb;
   L.dv1 = o; o += nb;
+  L.offs = o; o += nb;
+  L.rect = o; o += align256((size_t)n * sizeof(uint2));
   L.total = o;
   return L;
 }
 
 struct ScratchK {
-  size_t tk0, tv0, tk1, tv1, status, total;
+  size_t tk0, tv0, tk1, tv1, status, chunk_first, total;
   int parts;
+  int64_t chunks;
 };
 
 inline ScratchK layout_k(int64_t k) {
@@ -387,6 +470,8 @@ inline ScratchK layout_k(int64_t k) {
   L.tk1 = o; o += kb;
   L.tv1 = o; o += kb;
   L.status = o; o += align256((size_t)kMaxTilePasses * L.parts * 256 * sizeof(uint32_t));
+  L.chunks = (k + kEmitChunk - 1) / kEmitChunk;
+  L.chunk_first = o; o += align256((size_t)(L.chunks + 2) * sizeof(uint32_t));
   L.total = o;
   return L;
 }
@@ -463,7 +548,8 @@ int pgb_sort_gaussian_finish(const float* uv, const int32_t* radius, const int32
   if (!scratch_n || bytes_n < LN.total) return PGB_ERR_INVALID;
   if (k > 0 && (!scratch_k || bytes_k < LK.total || !ids_out)) return PGB_ERR_INVALID;
   const uint32_t T = (uint32_t)grid_x(width) * (uint32_t)grid_y(height);
-  if (T > (1u << (8 * kMaxTilePasses))) return PGB_ERR_INVALID;
+  if (T > (1u << (8 * kMaxTilePasses)) || grid_x(width) > 65535 || grid_y(height) > 65535)
+    return PGB_ERR_INVALID;
   cudaStream_t s = as_stream(stream);
   if (cudaMemsetAsync(tile_range_out, 0, (size_t)T * 2 * sizeof(int32_t), s) != cudaSuccess)
     return PGB_ERR_CUDA;
@@ -478,9 +564,15 @@ int pgb_sort_gaussian_finish(const float* uv, const int32_t* radius, const int32
   uint32_t* bufk[2] = {at<uint32_t>(scratch_k, LK.tk0), at<uint32_t>(scratch_k, LK.tk1)};
   uint32_t* bufv[2] = {at<uint32_t>(scratch_k, LK.tv0), at<uint32_t>(scratch_k, LK.tv1)};
   uint32_t* status = at<uint32_t>(scratch_k, LK.status);
-  scan_emit_kernel<<<LN.scan_parts, kSortThreads, 0, s>>>(
-      order, n, tiles_touched, radius, uv, width, height, k, passes,
-      at<uint32_t>(scratch_n, LN.scan_status), counters + 4, bufk[0], bufv[0], thist, info);
+  uint32_t* offs = at<uint32_t>(scratch_n, LN.offs);
+  uint2* rect = at<uint2>(scratch_n, LN.rect);
+  uint32_t* chunk_first = at<uint32_t>(scratch_k, LK.chunk_first);
+  scan_rect_kernel<<<LN.scan_parts, kSortThreads, 0, s>>>(
+      order, n, tiles_touched, radius, uv, width, height, k,
+      at<uint32_t>(scratch_n, LN.scan_status), counters + 4, offs, rect, chunk_first, info);
+  emit_kernel<<<(unsigned)LK.chunks, kEmitThreads, 0, s>>>(order, offs, rect, chunk_first, n, k,
+                                                           width, passes, bufk[0], bufv[0], thist,
+                                                           info);
   int cur = 0;
   for (int p = 0; p < passes; ++p) {
     const bool last = p == passes - 1;

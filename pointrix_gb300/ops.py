@@ -476,7 +476,7 @@ class _AlphaBlending(torch.autograd.Function):
         records, ids, tile_range, final_T, ncon = ctx.saved_tensors
         n, C, bg, W, H, has_ndc = ctx.cfg
         dev = records.device
-        grec = torch.empty_like(records)
+        grec = torch.empty(n, _lib.lib().pgb_blend_grad_record_floats(C), dtype=torch.float32, device=dev)
         d_uv = torch.empty(n, 2, dtype=torch.float32, device=dev)
         d_conic = torch.empty(n, 3, dtype=torch.float32, device=dev)
         d_op = torch.empty(n, dtype=torch.float32, device=dev)

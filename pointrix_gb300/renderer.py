@@ -87,9 +87,14 @@ class MsplatRender:
         direction = direction / direction.norm(dim=1, keepdim=True)
 
         sh_coeff = shs.permute(0, 2, 1)
-        sh_mask = torch.zeros_like(sh_coeff)
-        sh_mask[..., : (self.sh_degree + 1) ** 2] = 1.0
-        rgb = ops.compute_sh(sh_coeff * sh_mask, direction)
+        active = (self.sh_degree + 1) ** 2
+        if active >= sh_coeff.shape[-1]:
+            # the warm-up mask is all ones: multiplying by it is the identity
+            rgb = ops.compute_sh(sh_coeff, direction)
+        else:
+            sh_mask = torch.zeros_like(sh_coeff)
+            sh_mask[..., :active] = 1.0
+            rgb = ops.compute_sh(sh_coeff * sh_mask, direction)
         rgb = (rgb + 0.5).clamp(min=0.0)
 
         extr = extrinsic_matrix[:3, :]

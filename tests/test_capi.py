@@ -37,7 +37,10 @@ def test_invalid_arguments_rejected_without_launch():
     assert lib.pgb_compute_sh_forward(None, 10, 5, 15, 1, 3, None, None, None) == 1
     assert lib.pgb_project_point_forward(None, 10, None, None, 0, 10, 0.2, 1.3, None, None, None) == 1
     assert lib.pgb_blend_record_floats(7) == 16
-    assert lib.pgb_blend_record_floats(26) == 32
+    assert lib.pgb_blend_record_floats(3) == 12
+    assert lib.pgb_blend_record_floats(26) == 36
+    assert lib.pgb_blend_grad_record_floats(7) == 16
+    assert lib.pgb_blend_grad_record_floats(26) == 32
     assert lib.pgb_blend_record_floats(27) == -1
     bn, bk = C.c_size_t(0), C.c_size_t(0)
     assert lib.pgb_sort_scratch_bytes(1000, 5000, 64, 64, C.byref(bn), C.byref(bk)) == 0
