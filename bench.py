@@ -403,12 +403,18 @@ def run_gb300(args):
     algo = {"alpha_blending_fwd": blend_fwd_bytes(n, 7, K, T, W, H),
             "alpha_blending_bwd": blend_bwd_bytes(n, 7, K, T, W, H),
             "sort_finish": sort_bytes(n, K, T)}
+    traffic = None
+    try:
+        with open(os.path.join(ROOT, "profiles", "dram_traffic.json")) as f:
+            traffic = json.load(f)["bytes_per_launch"]
+    except Exception:
+        traffic = {}
     peaks, peak_kind = load_peaks()
     hbm_peak = float(peaks.get("hbm_gbs", PEAKS_FALLBACK["hbm_gbs"]))
     dom_bytes = algo.get(dom)
     achieved = dom_bytes / (per_op[dom] * 1e-3) / 1e9 if dom_bytes else None
     roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-                "frac": (achieved / hbm_peak) if achieved else None, "traffic": None,
+                "frac": (achieved / hbm_peak) if achieved else None, "traffic": traffic.get(dom),
                 "peak_source": peak_kind, "launch_ms": per_op[dom],
                 "algorithmic_bytes_per_launch": dom_bytes}
 
