@@ -133,6 +133,34 @@ int pgb_sort_gaussian_finish(const float* uv, const int32_t* radius, const int32
                              int32_t* ids_out, int32_t* tile_range_out, void* stream);
 
 /* ---------------------------------------------------------------------
+ * pgb_sort_gaussian_noalloc -- no counterpart in the reference.
+ * The same result as pgb_sort_gaussian_begin + finish, for callers that
+ * cannot allocate device memory: code running inside a host application that
+ * owns the GPU memory budget, or that must not enter the CUDA allocator on
+ * its hot path (cudaMalloc synchronises the device and may fail under memory
+ * pressure).  Its scratch is a static device array of
+ * PGB_NOALLOC_SCRATCH_BYTES (24 MiB) that every GPU loading this library
+ * holds until the process exits; the call allocates nothing.
+ * Limits: n <= PGB_NOALLOC_MAX_GAUSSIANS (262,144), else PGB_ERR_INVALID
+ * before any GPU work; K (sum of tiles_touched) must fit the rest of the
+ * array (about 1.0 million entries at the largest n) and ids_capacity, else
+ * PGB_ERR_OVERFLOW with *k_out (host, may be NULL) set to the K needed.
+ * Synchronous: returns when the results are complete on `stream`; a
+ * device-side fault comes back as the return value.  The first call on a
+ * device looks up the array's device address (with that device current);
+ * make that first call before any stream capture.  All calls share the one
+ * array (each clears what must start at zero): calls that overlap on the GPU,
+ * e.g. from two streams or threads, race and must be serialised by the
+ * caller.
+ * ------------------------------------------------------------------- */
+#define PGB_NOALLOC_MAX_GAUSSIANS 262144
+#define PGB_NOALLOC_SCRATCH_BYTES (24u << 20)
+int pgb_sort_gaussian_noalloc(const float* uv, const float* depth, const int32_t* radius,
+                              const int32_t* tiles_touched, int64_t n, int width, int height,
+                              int32_t* ids_out, int64_t ids_capacity, int32_t* tile_range_out,
+                              int64_t* k_out, void* stream);
+
+/* ---------------------------------------------------------------------
  * alpha_blending -- replaces msplat.alpha_blending
  * (pointrix/model/renderer/msplat.py:148-151)
  * uv [N,2], conic [N,3], opacity [N,1], feature [N,C] (1 <= C <= 26),
