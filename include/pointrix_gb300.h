@@ -190,6 +190,28 @@ int pgb_alpha_blending_backward(const float* records, int64_t n, int channels,
                                 float* d_uv, float* d_conic, float* d_opacity, float* d_feature,
                                 int64_t* info, void* stream);
 
+/* ---------------------------------------------------------------------
+ * Adam step over several parameter tensors in one launch -- replaces the
+ * torch Adam update of the training step (pointrix/optimizer/optimizer.py:
+ * 128-140; apex FusedAdam hook pointrix/optimizer/__init__.py:56-59).
+ * Each segment is a dense float32 tensor with its gradient, both moment
+ * buffers, its learning rate and its bias corrections 1 - beta1^t and
+ * 1 - beta2^t for its own step count t; at most 32 segments.  Same update as
+ * torch.optim.Adam without weight decay or amsgrad.
+ * ------------------------------------------------------------------- */
+typedef struct {
+  float* param;
+  const float* grad;
+  float* exp_avg;
+  float* exp_avg_sq;
+  int64_t n;
+  float lr;
+  float bias_correction1;
+  float bias_correction2;
+} pgb_adam_segment;
+int pgb_adam_step(const pgb_adam_segment* segments, int nsegments, float beta1, float beta2,
+                  float eps, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -39,6 +39,14 @@ SIGNATURES = {
     "pgb_alpha_blending_forward": [vp, vp, vp, vp, i64, i32, vp, i64, vp, f32, i32, i32, vp, vp, vp, vp, vp, vp],
     "pgb_alpha_blending_backward": [vp, i64, i32, vp, i64, vp, f32, i32, i32, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp],
 }
+class AdamSegment(C.Structure):
+    """``pgb_adam_segment`` of include/pointrix_gb300.h."""
+    _fields_ = [("param", vp), ("grad", vp), ("exp_avg", vp), ("exp_avg_sq", vp),
+                ("n", i64), ("lr", f32), ("bias_correction1", f32), ("bias_correction2", f32)]
+
+
+SIGNATURES["pgb_adam_step"] = [C.POINTER(AdamSegment), i32, f32, f32, f32, vp]
+
 _RESTYPES = {"pgb_status_string": C.c_char_p, "pgb_camera_grad_scratch_bytes": szt}
 
 

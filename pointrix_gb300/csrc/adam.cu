@@ -1,0 +1,89 @@
+// Adam over the Gaussian (and camera) parameters in one launch.
+//
+// The training step of Pointrix updates every parameter group with torch's
+// Adam (pointrix/optimizer/optimizer.py:128-140; an apex FusedAdam hook at
+// pointrix/optimizer/__init__.py:56-59).  Here all groups are one segment
+// table and one launch; each element is read once (param, grad, both moments)
+// and written once (param, both moments): 28 bytes per element, an HBM
+// stream.  The update is torch.optim.Adam's (no weight decay, no amsgrad):
+//   m = b1 m + (1 - b1) g;  v = b2 v + (1 - b2) g^2
+//   p -= (lr / bc1) * m / (sqrt(v) / sqrt(bc2) + eps)
+// with the bias corrections bc1 = 1 - b1^t, bc2 = 1 - b2^t of each segment's
+// own step count t (a tensor skipped in a step keeps its count, as in torch).
+#include "pgb_common.cuh"
+
+namespace pgb {
+
+constexpr int kAdamThreads = 256;
+constexpr int kMaxAdamSegments = 32;
+
+struct AdamTable {
+  pgb_adam_segment seg[kMaxAdamSegments];
+  int64_t start4[kMaxAdamSegments + 1];  // prefix of ceil(n / 4) over segments
+  int nseg;
+};
+
+__device__ __forceinline__ void adam_one(float& p, float g, float& m, float& v, float b1, float b2,
+                                         float eps, float step_size, float inv_sqrt_bc2) {
+  m = b1 * m + (1.f - b1) * g;
+  v = b2 * v + (1.f - b2) * g * g;
+  p -= step_size * m / (sqrtf(v) * inv_sqrt_bc2 + eps);
+}
+
+__global__ void __launch_bounds__(kAdamThreads) adam_kernel(AdamTable t, float b1, float b2,
+                                                            float eps) {
+  const int64_t total = t.start4[t.nseg];
+  int s = 0;
+  for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < total;
+       q += (int64_t)gridDim.x * blockDim.x) {
+    while (q >= t.start4[s + 1]) ++s;  // q only grows for a thread
+    const pgb_adam_segment& sg = t.seg[s];
+    const int64_t i = (q - t.start4[s]) * 4;
+    const float step_size = sg.lr / sg.bias_correction1;
+    const float inv_sqrt_bc2 = 1.0f / sqrtf(sg.bias_correction2);
+    if (i + 4 <= sg.n && (((uintptr_t)sg.param | (uintptr_t)sg.grad | (uintptr_t)sg.exp_avg |
+                           (uintptr_t)sg.exp_avg_sq) & 15) == 0) {
+      float4 p = reinterpret_cast<float4*>(sg.param)[i / 4];
+      const float4 g = reinterpret_cast<const float4*>(sg.grad)[i / 4];
+      float4 m = reinterpret_cast<float4*>(sg.exp_avg)[i / 4];
+      float4 v = reinterpret_cast<float4*>(sg.exp_avg_sq)[i / 4];
+      adam_one(p.x, g.x, m.x, v.x, b1, b2, eps, step_size, inv_sqrt_bc2);
+      adam_one(p.y, g.y, m.y, v.y, b1, b2, eps, step_size, inv_sqrt_bc2);
+      adam_one(p.z, g.z, m.z, v.z, b1, b2, eps, step_size, inv_sqrt_bc2);
+      adam_one(p.w, g.w, m.w, v.w, b1, b2, eps, step_size, inv_sqrt_bc2);
+      reinterpret_cast<float4*>(sg.param)[i / 4] = p;
+      reinterpret_cast<float4*>(sg.exp_avg)[i / 4] = m;
+      reinterpret_cast<float4*>(sg.exp_avg_sq)[i / 4] = v;
+    } else {
+      for (int64_t j = i; j < i + 4 && j < sg.n; ++j)
+        adam_one(sg.param[j], sg.grad[j], sg.exp_avg[j], sg.exp_avg_sq[j], b1, b2, eps, step_size,
+                 inv_sqrt_bc2);
+    }
+  }
+}
+
+}  // namespace pgb
+
+using namespace pgb;
+
+extern "C" int pgb_adam_step(const pgb_adam_segment* segments, int nsegments, float beta1,
+                             float beta2, float eps, void* stream) {
+  if (nsegments < 0 || nsegments > kMaxAdamSegments || (nsegments > 0 && !segments))
+    return PGB_ERR_INVALID;
+  AdamTable t;
+  t.nseg = nsegments;
+  t.start4[0] = 0;
+  for (int i = 0; i < nsegments; ++i) {
+    const pgb_adam_segment& s = segments[i];
+    if (s.n < 0 || (s.n > 0 && (!s.param || !s.grad || !s.exp_avg || !s.exp_avg_sq)))
+      return PGB_ERR_INVALID;
+    if (!(s.bias_correction1 > 0.f) || !(s.bias_correction2 > 0.f)) return PGB_ERR_INVALID;
+    t.seg[i] = s;
+    t.start4[i + 1] = t.start4[i] + (s.n + 3) / 4;
+  }
+  const int64_t total = t.start4[nsegments];
+  if (total == 0) return PGB_OK;
+  adam_kernel<<<stream_grid(total, kAdamThreads, 8), kAdamThreads, 0, as_stream(stream)>>>(
+      t, beta1, beta2, eps);
+  return launch_status();
+}

@@ -148,15 +148,48 @@ def cameras_multiview(seed: int = 2, views: int = 16, radius: float = 5.0, f_sca
     return cams
 
 
+def _quat_pair_to_rot() -> torch.Tensor:
+    """[16, 9]: row-major rotation entries of a unit wxyz quaternion as linear
+    combinations of the products q_a q_b (index 4a + b), in the homogeneous
+    form of ``pointrix/utils/pose.py:40-84``."""
+    W_, X, Y, Z = 0, 1, 2, 3
+    terms = [
+        {(W_, W_): 1, (X, X): 1, (Y, Y): -1, (Z, Z): -1},   # R00
+        {(X, Y): 2, (W_, Z): -2},                            # R01
+        {(X, Z): 2, (W_, Y): 2},                             # R02
+        {(X, Y): 2, (W_, Z): 2},                             # R10
+        {(W_, W_): 1, (X, X): -1, (Y, Y): 1, (Z, Z): -1},   # R11
+        {(Y, Z): 2, (W_, X): -2},                            # R12
+        {(X, Z): 2, (W_, Y): -2},                            # R20
+        {(Y, Z): 2, (W_, X): 2},                             # R21
+        {(W_, W_): 1, (X, X): -1, (Y, Y): -1, (Z, Z): 1},   # R22
+    ]
+    A = torch.zeros(16, 9)
+    for j, t in enumerate(terms):
+        for (a, b), c in t.items():
+            A[4 * a + b, j] = c
+    return A
+
+
+_QQ_TO_R = _quat_pair_to_rot()
+_QQ_TO_R_ON: dict = {}
+
+
+def rotation_from_unit_quat(q: torch.Tensor) -> torch.Tensor:
+    """Rotation matrices [..., 3, 3] of unit wxyz quaternions [..., 4]: one
+    outer product and one small matmul (few kernels, also in backward)."""
+    key = (q.device, q.dtype)
+    A = _QQ_TO_R_ON.get(key)
+    if A is None:
+        A = _QQ_TO_R_ON[key] = _QQ_TO_R.to(q.device, q.dtype)
+    qq = (q[..., :, None] * q[..., None, :]).reshape(*q.shape[:-1], 16)
+    return (qq @ A).reshape(*q.shape[:-1], 3, 3)
+
+
 def normals_from_scene(scaling: torch.Tensor, rotation: torch.Tensor) -> torch.Tensor:
     """Shortest-axis normal, rotated into world space (the normal feature of
-    ``examples/supervise/model.py:50-62``)."""
+    ``examples/supervise/model.py:50-62``: column argmin(scale) of R(q))."""
     idx = torch.argmin(scaling.detach(), dim=-1)
-    w, x, y, z = rotation.unbind(-1)
-    cols = torch.stack([
-        torch.stack([1 - 2 * (y * y + z * z), 2 * (x * y + w * z), 2 * (x * z - w * y)], -1),
-        torch.stack([2 * (x * y - w * z), 1 - 2 * (x * x + z * z), 2 * (y * z + w * x)], -1),
-        torch.stack([2 * (x * z + w * y), 2 * (y * z - w * x), 1 - 2 * (x * x + y * y)], -1),
-    ], 1)                                              # [N, 3 (column), 3]
-    n = cols.gather(1, idx[:, None, None].expand(-1, 1, 3))[:, 0]
+    R = rotation_from_unit_quat(rotation)                     # [N, 3, 3]
+    n = R.gather(2, idx[:, None, None].expand(-1, 3, 1))[..., 0]
     return torch.nn.functional.normalize(n, dim=-1)
