@@ -78,6 +78,19 @@ __device__ inline void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint
       : "memory");
 }
 
+// 16-byte asynchronous global -> shared copy (cp.async, L1 bypass), and the
+// group commit / wait that orders it; the wait is a hardware wait for this
+// thread's own copies, it cannot spin.
+__device__ inline void cp_async16(void* dst, const void* src) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_addr(dst)), "l"(src)
+               : "memory");
+}
+__device__ inline void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ inline void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
 __device__ inline void set_info(int64_t* info, int code) {
   if (info) atomicCAS(reinterpret_cast<unsigned long long*>(info), 0ull, (unsigned long long)code);
 }
@@ -95,20 +108,57 @@ __device__ __forceinline__ float splat_power(float a, float b, float c, float dx
 // entry first + t (if below last) into stage slot t.  One arrive per warp
 // carries the warp's byte count (the barrier expects kBlendThreads/32
 // arrivals per phase).
-template <int RF>
+// Ids outside [0, n) (a corrupt list) are recorded in `info` and their
+// copies skipped; the byte count expected on the barrier counts only the
+// copies issued, so the phase still completes.
+template <int RF, int NT = kBatch>
 __device__ inline void issue_batch(const float* __restrict__ records,
                                    const int32_t* __restrict__ ids, int64_t first, int64_t last,
-                                   float* stage, uint64_t* bar) {
+                                   int64_t n, float* stage, uint64_t* bar, int64_t* info) {
+  constexpr int PER = kBatch / NT;  // slots per thread
   const int lane = threadIdx.x & 31;
-  const int64_t e = first + threadIdx.x;
-  const bool valid = e < last;
-  const uint32_t ballot = __ballot_sync(0xffffffffu, valid);
-  if (lane == 0) mbar_arrive_expect_tx(bar, (uint32_t)__popc(ballot) * RF * 4u);
-  __syncwarp();
-  if (valid) {
-    const int32_t g = ids[e];
-    bulk_g2s(stage + threadIdx.x * RF, records + (int64_t)g * RF, RF * 4u, bar);
+  int32_t g[PER];
+  bool ok[PER];
+  uint32_t nvalid = 0;
+#pragma unroll
+  for (int k = 0; k < PER; ++k) {
+    const int64_t e = first + threadIdx.x + k * NT;
+    g[k] = e < last ? ids[e] : -1;
+    ok[k] = e < last && g[k] >= 0 && (int64_t)g[k] < n;
+    if (e < last && !ok[k]) set_info(info, PGB_ERR_OVERFLOW);
+    nvalid += __popc(__ballot_sync(0xffffffffu, ok[k]));
   }
+  if (lane == 0) mbar_arrive_expect_tx(bar, nvalid * RF * 4u);
+  __syncwarp();
+#pragma unroll
+  for (int k = 0; k < PER; ++k)
+    if (ok[k])
+      bulk_g2s(stage + (threadIdx.x + k * NT) * RF, records + (int64_t)g[k] * RF, RF * 4u, bar);
+}
+
+// Stage one batch with cp.async: thread t copies the records of slots
+// t, t + NT, ... (16 bytes per instruction) and commits one group.
+template <int RF, int NT>
+__device__ inline void stage_batch(const float* __restrict__ records,
+                                   const int32_t* __restrict__ ids, int64_t first, int64_t last,
+                                   int64_t n, float* stage, int64_t* info) {
+#pragma unroll
+  for (int k = 0; k < kBatch / NT; ++k) {
+    const int slot = threadIdx.x + k * NT;
+    const int64_t e = first + slot;
+    if (e < last) {
+      const int32_t g = ids[e];
+      if (g < 0 || (int64_t)g >= n) {
+        set_info(info, PGB_ERR_OVERFLOW);
+        continue;
+      }
+      const float* src = records + (int64_t)g * RF;
+      float* dst = stage + slot * RF;
+#pragma unroll
+      for (int q = 0; q < RF / 4; ++q) cp_async16(dst + 4 * q, src + 4 * q);
+    }
+  }
+  cp_async_commit();
 }
 
 // ------------------------------------------------------------------ pack
@@ -166,17 +216,18 @@ __device__ __forceinline__ void tile_pixel(int tile, int gx, int& px, int& py, i
 }
 
 // Conservative test: can the splat pass the alpha test at any pixel centre
-// of the box [x0, x0 + 7] x [y0, y0 + 3]?  Minimum of the (convex) quadratic
+// of the box [x0, x0 + BW - 1] x [y0, y0 + BH - 1]?  Minimum of the (convex) quadratic
 // form over the box -- zero if the centre is inside, else the least of its
 // four edge minima -- compared with tau after subtracting a bound on the
 // rounding of the per-pixel float evaluation (1e-5 of the largest term
 // magnitude over the box, far above the ~2e-7 that evaluation can lose).
+template <int BW, int BH>
 __device__ __forceinline__ bool splat_may_touch_box(const float* rec, float x0, float y0) {
   const float tau = rec[6];
   if (!(tau < 3.0e38f)) return true;
   const float u = rec[0], v = rec[1], a = rec[2], b = rec[3], c = rec[4];
-  const float dx0 = u - (x0 + 7.f), dx1 = u - x0;
-  const float dy0 = v - (y0 + 3.f), dy1 = v - y0;
+  const float dx0 = u - (x0 + (float)(BW - 1)), dx1 = u - x0;
+  const float dy0 = v - (y0 + (float)(BH - 1)), dy1 = v - y0;
   if (dx0 <= 0.f && dx1 >= 0.f && dy0 <= 0.f && dy1 >= 0.f) return tau >= 0.f;
   const float ia = 1.0f / a, ic = 1.0f / c;
   float qmin = 3.0e38f;
@@ -197,6 +248,7 @@ __device__ __forceinline__ bool splat_may_touch_box(const float* rec, float x0, 
 // Builds this warp's list of batch slots (in increasing order) whose splat
 // may touch the warp's pixel box; slots >= cnt are ignored.  Returns the
 // list length.
+template <int BW, int BH>
 __device__ __forceinline__ int warp_cull(const float* stage, int RF, int cnt, float x0, float y0,
                                          uint8_t* list) {
   const int lane = threadIdx.x & 31;
@@ -205,7 +257,7 @@ __device__ __forceinline__ int warp_cull(const float* stage, int RF, int cnt, fl
 #pragma unroll
   for (int k = 0; k < kBatch / 32; ++k) {
     const int j = k * 32 + lane;
-    const bool keep = j < cnt && splat_may_touch_box(stage + j * RF, x0, y0);
+    const bool keep = j < cnt && splat_may_touch_box<BW, BH>(stage + j * RF, x0, y0);
     const uint32_t m = __ballot_sync(0xffffffffu, keep);
     if (keep) list[n + __popc(m & lt)] = (uint8_t)j;
     n += __popc(m);
@@ -218,8 +270,9 @@ __device__ __forceinline__ int warp_cull(const float* stage, int RF, int cnt, fl
 template <int NC, int RF>
 __global__ void __launch_bounds__(kBlendThreads) blend_fwd_kernel(
     const float* __restrict__ records, const int32_t* __restrict__ ids,
-    const int2* __restrict__ ranges, float bg, int W, int H, int C, float* __restrict__ out,
-    float* __restrict__ final_T, int32_t* __restrict__ n_contrib, int64_t* __restrict__ info) {
+    const int2* __restrict__ ranges, int64_t n, float bg, int W, int H, int C,
+    float* __restrict__ out, float* __restrict__ final_T, int32_t* __restrict__ n_contrib,
+    int64_t* __restrict__ info) {
   extern __shared__ __align__(128) float smem[];
   __shared__ __align__(8) uint64_t bars[2];
 
@@ -251,11 +304,13 @@ __global__ void __launch_bounds__(kBlendThreads) blend_fwd_kernel(
   bool done = !inside;
   bool timed_out = false;
 
-  if (nb > 0) issue_batch<RF>(records, ids, start, end, smem, &bars[0]);
+  if (nb > 0) issue_batch<RF>(records, ids, start, end, n, smem, &bars[0], info);
   for (int b = 0; b < nb; ++b) {
     const int buf = b & 1;
     const int64_t first = start + (int64_t)b * kBatch;
-    if (b + 1 < nb) issue_batch<RF>(records, ids, first + kBatch, end, smem + (buf ^ 1) * kBatch * RF, &bars[buf ^ 1]);
+    if (b + 1 < nb)
+      issue_batch<RF>(records, ids, first + kBatch, end, n, smem + (buf ^ 1) * kBatch * RF,
+                      &bars[buf ^ 1], info);
     // every thread observes the phase (that makes the TMA writes visible to
     // it); the outcome is made block-uniform before any warp collective
     timed_out = __syncthreads_or(!mbar_wait_bounded(&bars[buf], (b >> 1) & 1));
@@ -263,7 +318,7 @@ __global__ void __launch_bounds__(kBlendThreads) blend_fwd_kernel(
     const int cnt = (int)(end - first < kBatch ? end - first : kBatch);
     const float* st = smem + buf * kBatch * RF;
     if (!timed_out && !__all_sync(0xffffffffu, done)) {
-      const int nl = warp_cull(st, RF, cnt, (float)bx0, (float)by0, my_list);
+      const int nl = warp_cull<8, 4>(st, RF, cnt, (float)bx0, (float)by0, my_list);
       if (!done) {
         for (int t = 0; t < nl; ++t) {
           const int j = my_list[t];
@@ -328,65 +383,122 @@ __device__ __forceinline__ float warp_reduce_scatter(float (&v)[GR]) {
   return v[0];
 }
 
+// Backward: 128 threads per tile, two pixels per thread.  Warp w owns the
+// 8x8 box at (8 (w % 2), 8 (w / 2)); lane l owns pixels (l % 8, l / 8) and
+// (l % 8, l / 8 + 4) of it, so every per-splat warp reduction, record read
+// and culling test serves 64 pixels.
+constexpr int kBwdThreads = 128;
+constexpr int kBwdPix = 2;
+
+template <int NC>
+struct BwdPixel {
+  float T;
+  int nc;
+  float pxf, pyf;
+  float dout[NC], Bk[NC];
+};
+
+// Adds one pixel's contribution to the splat gradients v (u, v, a, b, c, o,
+// f...); replays the forward's skip decisions exactly.
+template <int NC, int GR>
+__device__ __forceinline__ bool bwd_pixel(BwdPixel<NC>& P, int j, const float* rec,
+                                          float (&v)[GR]) {
+  if (j >= P.nc) return false;
+  const float4 r0 = *reinterpret_cast<const float4*>(rec);
+  const float2 r1 = *reinterpret_cast<const float2*>(rec + 4);
+  const float dx = __fsub_rn(r0.x, P.pxf), dy = __fsub_rn(r0.y, P.pyf);
+  const float power = splat_power(r0.z, r0.w, r1.x, dx, dy);
+  if (power > 0.f) return false;
+  const float G = __expf(power);
+  const float araw = __fmul_rn(r1.y, G);
+  const float alpha = fminf(0.99f, araw);
+  if (alpha < (1.0f / 255.0f)) return false;
+  const float om = __fsub_rn(1.0f, alpha);
+  P.T = __fdividef(P.T, om);
+  const float* f = rec + kRecFeat;
+  float dalpha = 0.f;
+  const float wT = alpha * P.T;
+#pragma unroll
+  for (int c = 0; c < NC; ++c) {
+    dalpha = fmaf(P.dout[c], f[c] - P.Bk[c], dalpha);
+    P.Bk[c] = fmaf(alpha, f[c], om * P.Bk[c]);
+    v[6 + c] = fmaf(wT, P.dout[c], v[6 + c]);
+  }
+  dalpha *= P.T;
+  if (araw < 0.99f) {
+    const float dpow = alpha * dalpha;
+    v[5] = fmaf(G, dalpha, v[5]);
+    v[2] = fmaf(-0.5f * dx * dx, dpow, v[2]);
+    v[3] = fmaf(-dx * dy, dpow, v[3]);
+    v[4] = fmaf(-0.5f * dy * dy, dpow, v[4]);
+    v[0] = fmaf(-r0.z * dx - r0.w * dy, dpow, v[0]);
+    v[1] = fmaf(-r1.x * dy - r0.w * dx, dpow, v[1]);
+  }
+  return true;
+}
+
 template <int NC, int RF, int GR>
-__global__ void __launch_bounds__(kBlendThreads) blend_bwd_kernel(
+__global__ void __launch_bounds__(kBwdThreads) blend_bwd_kernel(
     const float* __restrict__ records, const int32_t* __restrict__ ids,
-    const int2* __restrict__ ranges, float bg, int W, int H, int C,
+    const int2* __restrict__ ranges, int64_t n, float bg, int W, int H, int C,
     const float* __restrict__ final_T, const int32_t* __restrict__ n_contrib,
     const float* __restrict__ d_out, float* __restrict__ grad_records,
     int64_t* __restrict__ info) {
   static_assert(GR == 16 || GR == 32, "gradient records are 16 or 32 floats");
   extern __shared__ __align__(128) float smem[];
-  __shared__ __align__(8) uint64_t bars[2];
   __shared__ int s_max_nc;
   __shared__ uint8_t s_touched[kBatch];
-  __shared__ uint8_t s_list[kBlendThreads / 32][kBatch];
+  __shared__ uint8_t s_list[kBwdThreads / 32][kBatch];
   float* gacc = smem + 2 * kBatch * RF;  // [kBatch][GR]
 
   const int gx = grid_x(W);
   const int tile = blockIdx.x;
-  int px, py, bx0, by0;
-  tile_pixel(tile, gx, px, py, bx0, by0);
-  const bool inside = px < W && py < H;
-  const float pxf = (float)px, pyf = (float)py;
-  const int lane = threadIdx.x & 31;
-  uint8_t* my_list = s_list[threadIdx.x >> 5];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int bx0 = (tile % gx) * kTile + 8 * (w & 1);
+  const int by0 = (tile / gx) * kTile + 8 * (w >> 1);
+  uint8_t* my_list = s_list[w];
 
-  if (threadIdx.x == 0) {
-    mbar_init(&bars[0], kBlendThreads / 32);
-    mbar_init(&bars[1], kBlendThreads / 32);
-    fence_mbar_init();
-    s_max_nc = 0;
-  }
-  for (int i = threadIdx.x; i < kBatch * GR; i += kBlendThreads) gacc[i] = 0.f;
-  s_touched[threadIdx.x] = 0;
+  if (threadIdx.x == 0) s_max_nc = 0;
+  for (int i = threadIdx.x; i < kBatch * GR; i += kBwdThreads) gacc[i] = 0.f;
+  for (int i = threadIdx.x; i < kBatch; i += kBwdThreads) s_touched[i] = 0;
   __syncthreads();
 
-  const int64_t pix = (int64_t)py * W + px;
   const int64_t plane = (int64_t)W * H;
-  float T = 1.f;
-  int nc = 0;
-  float dout[NC], Bk[NC];
+  BwdPixel<NC> P[kBwdPix];
+  int my_nc = 0;
 #pragma unroll
-  for (int c = 0; c < NC; ++c) {
-    dout[c] = 0.f;
-    Bk[c] = bg;
-  }
-  if (inside) {
-    T = final_T[pix];
-    nc = n_contrib[pix];
+  for (int q = 0; q < kBwdPix; ++q) {
+    const int px = bx0 + (lane & 7), py = by0 + (lane >> 3) + 4 * q;
+    P[q].pxf = (float)px;
+    P[q].pyf = (float)py;
+    P[q].T = 1.f;
+    P[q].nc = 0;
 #pragma unroll
-    for (int c = 0; c < NC; ++c)
-      if (c < C) dout[c] = d_out[c * plane + pix];
-    atomicMax(&s_max_nc, nc);
+    for (int c = 0; c < NC; ++c) {
+      P[q].dout[c] = 0.f;
+      P[q].Bk[c] = bg;
+    }
+    if (px < W && py < H) {
+      const int64_t pix = (int64_t)py * W + px;
+      P[q].T = final_T[pix];
+      P[q].nc = n_contrib[pix];
+#pragma unroll
+      for (int c = 0; c < NC; ++c)
+        if (c < C) P[q].dout[c] = d_out[c * plane + pix];
+    }
+    my_nc = max(my_nc, P[q].nc);
   }
+  int warp_nc = my_nc;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) warp_nc = max(warp_nc, __shfl_xor_sync(0xffffffffu, warp_nc, o));
+  if (lane == 0) atomicMax(&s_max_nc, warp_nc);
   __syncthreads();
   const int2 rg = ranges[tile];
   const int64_t start = rg.x;
-  const int max_nc = s_max_nc;
-  int warp_nc = nc;
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) warp_nc = max(warp_nc, __shfl_xor_sync(0xffffffffu, warp_nc, o));
+  // the replay never reads past the tile's list, whatever n_contrib holds
+  const int list_len = max(0, rg.y - rg.x);
+  if (s_max_nc > list_len && threadIdx.x == 0) set_info(info, PGB_ERR_OVERFLOW);
+  const int max_nc = min(s_max_nc, list_len);
   const int nb = (max_nc + kBatch - 1) / kBatch;
 
   // batch b covers list positions [hi_b - kBatch, hi_b) with hi_b = max_nc - b*kBatch,
@@ -394,67 +506,38 @@ __global__ void __launch_bounds__(kBlendThreads) blend_bwd_kernel(
   auto lo_of = [&](int b) { return max(0, max_nc - (b + 1) * kBatch); };
   auto hi_of = [&](int b) { return max_nc - b * kBatch; };
 
-  bool timed_out = false;
-  if (nb > 0) issue_batch<RF>(records, ids, start + lo_of(0), start + hi_of(0), smem, &bars[0]);
+  if (nb > 0)
+    stage_batch<RF, kBwdThreads>(records, ids, start + lo_of(0), start + hi_of(0), n, smem, info);
   for (int b = 0; b < nb; ++b) {
     const int buf = b & 1;
     const int lo = lo_of(b), hi = hi_of(b);
-    if (b + 1 < nb)
-      issue_batch<RF>(records, ids, start + lo_of(b + 1), start + hi_of(b + 1), smem + (buf ^ 1) * kBatch * RF,
-                      &bars[buf ^ 1]);
-    timed_out = __syncthreads_or(!mbar_wait_bounded(&bars[buf], (b >> 1) & 1));
-    if (timed_out && threadIdx.x == 0) set_info(info, PGB_ERR_TIMEOUT);
+    if (b + 1 < nb) {
+      stage_batch<RF, kBwdThreads>(records, ids, start + lo_of(b + 1), start + hi_of(b + 1), n,
+                                   smem + (buf ^ 1) * kBatch * RF, info);
+      cp_async_wait<1>();  // this thread's copies of batch b have landed
+    } else {
+      cp_async_wait<0>();
+    }
+    __syncthreads();  // ... and everyone's
     const float* st = smem + buf * kBatch * RF;
-    if (!timed_out) {
-      const int nl = warp_cull(st, RF, min(hi, warp_nc) - lo, (float)bx0, (float)by0, my_list);
+    {
+      const int nl = warp_cull<8, 8>(st, RF, min(hi, warp_nc) - lo, (float)bx0, (float)by0, my_list);
       for (int t = nl - 1; t >= 0; --t) {
         const int slot = my_list[t];
         const int j = lo + slot;
+        const float* rec = st + slot * RF;
         float v[GR];
 #pragma unroll
         for (int q = 0; q < GR; ++q) v[q] = 0.f;
         bool contrib = false;
-        if (j < nc) {
-          const float4 r0 = *reinterpret_cast<const float4*>(st + slot * RF);
-          const float2 r1 = *reinterpret_cast<const float2*>(st + slot * RF + 4);
-          const float dx = __fsub_rn(r0.x, pxf), dy = __fsub_rn(r0.y, pyf);
-          const float power = splat_power(r0.z, r0.w, r1.x, dx, dy);
-          if (power <= 0.f) {
-            const float G = __expf(power);
-            const float araw = __fmul_rn(r1.y, G);
-            const float alpha = fminf(0.99f, araw);
-            if (alpha >= (1.0f / 255.0f)) {
-              contrib = true;
-              const float om = __fsub_rn(1.0f, alpha);
-              T = __fdividef(T, om);
-              const float* f = st + slot * RF + kRecFeat;
-              float dalpha = 0.f;
-              const float wT = alpha * T;
 #pragma unroll
-              for (int c = 0; c < NC; ++c) {
-                dalpha = fmaf(dout[c], f[c] - Bk[c], dalpha);
-                Bk[c] = fmaf(alpha, f[c], om * Bk[c]);
-                v[6 + c] = wT * dout[c];
-              }
-              dalpha *= T;
-              if (araw < 0.99f) {
-                const float dpow = alpha * dalpha;
-                v[5] = G * dalpha;
-                v[2] = -0.5f * dx * dx * dpow;
-                v[3] = -dx * dy * dpow;
-                v[4] = -0.5f * dy * dy * dpow;
-                v[0] = (-r0.z * dx - r0.w * dy) * dpow;
-                v[1] = (-r1.x * dy - r0.w * dx) * dpow;
-              }
-            }
-          }
-        }
+        for (int q = 0; q < kBwdPix; ++q) contrib |= bwd_pixel<NC, GR>(P[q], j, rec, v);
         if (__any_sync(0xffffffffu, contrib)) {
-          const float s = warp_reduce_scatter<GR>(v);
+          const float sum = warp_reduce_scatter<GR>(v);
           if (GR == 32) {
-            if (lane < 6 + NC) atomicAdd(&gacc[slot * GR + lane], s);
+            if (lane < 6 + NC) atomicAdd(&gacc[slot * GR + lane], sum);
           } else if ((lane & 1) == 0 && (lane >> 1) < 6 + NC) {
-            atomicAdd(&gacc[slot * GR + (lane >> 1)], s);
+            atomicAdd(&gacc[slot * GR + (lane >> 1)], sum);
           }
           if (lane == 0) s_touched[slot] = 1;
         }
@@ -463,9 +546,13 @@ __global__ void __launch_bounds__(kBlendThreads) blend_bwd_kernel(
     }
     __syncthreads();
     // flush this batch's per-splat sums: one set of vector atomics per splat
-    const int t = threadIdx.x;
-    if (t < hi - lo && s_touched[t]) {
+    for (int t = threadIdx.x; t < hi - lo; t += kBwdThreads) {
+      if (!s_touched[t]) continue;
       const int32_t g = ids[start + lo + t];
+      if (g < 0 || (int64_t)g >= n) {
+        set_info(info, PGB_ERR_OVERFLOW);
+        continue;
+      }
       float4* dst = reinterpret_cast<float4*>(grad_records + (int64_t)g * GR);
       float4* srcv = reinterpret_cast<float4*>(gacc + t * GR);
 #pragma unroll
@@ -476,11 +563,6 @@ __global__ void __launch_bounds__(kBlendThreads) blend_bwd_kernel(
       s_touched[t] = 0;
     }
     __syncthreads();
-    if (timed_out) {
-      if (b + 1 < nb && !mbar_wait_bounded(&bars[buf ^ 1], ((b + 1) >> 1) & 1))
-        set_info(info, PGB_ERR_TIMEOUT);
-      break;
-    }
   }
 }
 
@@ -511,8 +593,8 @@ __global__ void unpack_kernel(const float* __restrict__ g, int64_t n, int C,
 
 // ------------------------------------------------------------- dispatch
 template <int NC>
-static int launch_fwd_nc(const float* records, const int32_t* ids, const int2* ranges, float bg,
-                         int W, int H, int C, float* out, float* fT, int32_t* ncon,
+static int launch_fwd_nc(const float* records, const int32_t* ids, const int2* ranges, int64_t n,
+                         float bg, int W, int H, int C, float* out, float* fT, int32_t* ncon,
                          int64_t* info, cudaStream_t s) {
   constexpr int RF = rec_floats(NC);
   const int tiles = grid_x(W) * grid_y(H);
@@ -521,13 +603,13 @@ static int launch_fwd_nc(const float* records, const int32_t* ids, const int2* r
   if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
       cudaSuccess)
     return PGB_ERR_CUDA;
-  kern<<<tiles, kBlendThreads, smem, s>>>(records, ids, ranges, bg, W, H, C, out, fT, ncon, info);
+  kern<<<tiles, kBlendThreads, smem, s>>>(records, ids, ranges, n, bg, W, H, C, out, fT, ncon, info);
   return launch_status();
 }
 
 template <int NC>
-static int launch_bwd_nc(const float* records, const int32_t* ids, const int2* ranges, float bg,
-                         int W, int H, int C, const float* fT, const int32_t* ncon,
+static int launch_bwd_nc(const float* records, const int32_t* ids, const int2* ranges, int64_t n,
+                         float bg, int W, int H, int C, const float* fT, const int32_t* ncon,
                          const float* dout, float* grec, int64_t* info, cudaStream_t s) {
   constexpr int RF = rec_floats(NC);
   constexpr int GR = grad_floats(NC);
@@ -537,8 +619,8 @@ static int launch_bwd_nc(const float* records, const int32_t* ids, const int2* r
   if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
       cudaSuccess)
     return PGB_ERR_CUDA;
-  kern<<<tiles, kBlendThreads, smem, s>>>(records, ids, ranges, bg, W, H, C, fT, ncon, dout, grec,
-                                          info);
+  kern<<<tiles, kBwdThreads, smem, s>>>(records, ids, ranges, n, bg, W, H, C, fT, ncon, dout,
+                                        grec, info);
   return launch_status();
 }
 
@@ -587,7 +669,8 @@ int pgb_alpha_blending_forward(const float* uv, const float* conic, const float*
       pack_kernel<rec_floats(N)><<<stream_grid(n), kStreamThreads, 0, s>>>(uv, conic, opacity,  \
                                                                            feature, n, channels, \
                                                                            records);            \
-    return launch_fwd_nc<N>(records, ids, rg, bg, width, height, channels, out, final_T, n_contrib, info, s);
+    return launch_fwd_nc<N>(records, ids, rg, n, bg, width, height, channels, out, final_T,       \
+                            n_contrib, info, s);
     PGB_FOR_NC(PGB_CASE)
 #undef PGB_CASE
     default:
@@ -616,8 +699,8 @@ int pgb_alpha_blending_backward(const float* records, int64_t n, int channels,
   switch (nc) {
 #define PGB_CASE(N)                                                                          \
   case N:                                                                                    \
-    st = launch_bwd_nc<N>(records, ids, rg, bg, width, height, channels, final_T, n_contrib, \
-                          d_out, grad_records, info, s);                                     \
+    st = launch_bwd_nc<N>(records, ids, rg, n, bg, width, height, channels, final_T,        \
+                          n_contrib, d_out, grad_records, info, s);                          \
     break;
     PGB_FOR_NC(PGB_CASE)
 #undef PGB_CASE

@@ -66,8 +66,10 @@ __device__ inline uint32_t lanemask_lt() {
   return m;
 }
 
-// Exclusive scan over the 256 threads of a CTA; `total` receives the sum.
+// Exclusive scan over the NT threads of a CTA; `total` receives the sum.
+template <int NT = kSortThreads>
 __device__ inline uint32_t block_excl_scan(uint32_t v, uint32_t& total, uint32_t* warp_tot) {
+  constexpr int NW = NT / 32;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   uint32_t x = v;
 #pragma unroll
@@ -78,40 +80,53 @@ __device__ inline uint32_t block_excl_scan(uint32_t v, uint32_t& total, uint32_t
   if (lane == 31) warp_tot[warp] = x;
   __syncthreads();
   if (warp == 0) {
-    uint32_t w = lane < kSortThreads / 32 ? warp_tot[lane] : 0u;
+    uint32_t w = lane < NW ? warp_tot[lane] : 0u;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
       const uint32_t y = __shfl_up_sync(0xffffffffu, w, o);
       if (lane >= o) w += y;
     }
-    if (lane < kSortThreads / 32) warp_tot[lane] = w;
+    if (lane < NW) warp_tot[lane] = w;
   }
   __syncthreads();
   const uint32_t prefix = warp > 0 ? warp_tot[warp - 1] : 0u;
-  total = warp_tot[kSortThreads / 32 - 1];
+  total = warp_tot[NW - 1];
   __syncthreads();
   return prefix + x - v;
 }
 
 // Sum of the counts published by partitions [0, part) for one digit (or the
 // scan's single value), walking back until an inclusive prefix is found.
+// The status words of the next kWindow predecessors are loaded together (a
+// walk over partitions still in flight would otherwise be a chain of
+// dependent L2 round trips) and consumed in order up to the first one not
+// yet published.
+constexpr int kWindow = 8;
+
 __device__ inline uint32_t look_back(const uint32_t* status, int part, int stride, int64_t* info) {
   uint32_t excl = 0, spins = 0;
   int p = part - 1;
   while (p >= 0) {
-    const uint32_t s = ld_volatile(status + (size_t)p * stride);
-    const uint32_t flag = s & ~kValMask;
-    if (flag == 0) {
+    uint32_t w[kWindow];
+#pragma unroll
+    for (int k = 0; k < kWindow; ++k)
+      w[k] = p - k >= 0 ? ld_volatile(status + (size_t)(p - k) * stride) : kFlagInc;
+    int k = 0;
+#pragma unroll
+    for (; k < kWindow; ++k) {
+      const uint32_t flag = w[k] & ~kValMask;
+      if (flag == 0) break;
+      excl += w[k] & kValMask;
+      if (flag == kFlagInc) return excl;
+    }
+    p -= k;
+    if (k == 0) {
       if (++spins > kSpinLimit) {
         set_error(info, PGB_ERR_TIMEOUT);
         break;
       }
       __nanosleep(32);
-      continue;
     }
-    excl += s & kValMask;
-    if (flag == kFlagInc) break;
-    --p;
   }
   return excl;
 }
@@ -151,19 +166,28 @@ __global__ void __launch_bounds__(kSortThreads) sort_prepare_kernel(
 
 // ---------------------------------------------------------------------------
 // 2/4. one stable LSD onesweep pass over 8 bits starting at `shift`
+//
+// 512 threads x 8 keys = one 4096-key partition per CTA; the first 256
+// threads also act as the 256 digits for the cross-warp prefix, the status
+// publication and the look-back.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(kSortThreads) onesweep_kernel(
+constexpr int kOsThreads = 512;
+constexpr int kOsItems = kPartKeys / kOsThreads;  // 8
+constexpr int kOsWarps = kOsThreads / 32;
+constexpr size_t kOsSmem = (size_t)kOsWarps * 256 * 4 + 2 * (size_t)kPartKeys * 4;
+
+__global__ void __launch_bounds__(kOsThreads) onesweep_kernel(
     const uint32_t* __restrict__ keys_in, const uint32_t* __restrict__ vals_in,
     uint32_t* __restrict__ keys_out, uint32_t* __restrict__ vals_out, int64_t n, int shift,
     const uint32_t* __restrict__ pass_hist, uint32_t* __restrict__ status,
     uint32_t* __restrict__ part_counter, int64_t* __restrict__ info) {
-  constexpr int NW = kSortThreads / 32;
-  __shared__ uint32_t warp_hist[NW][256];
-  __shared__ uint32_t s_keys[kPartKeys];
-  __shared__ uint32_t s_vals[kPartKeys];
+  extern __shared__ __align__(16) uint32_t os_smem[];
+  uint32_t (*warp_hist)[256] = reinterpret_cast<uint32_t (*)[256]>(os_smem);
+  uint32_t* s_keys = os_smem + kOsWarps * 256;
+  uint32_t* s_vals = s_keys + kPartKeys;
   __shared__ uint32_t s_block_excl[256];
   __shared__ uint32_t s_global_base[256];
-  __shared__ uint32_t s_warp_tot[NW];
+  __shared__ uint32_t s_warp_tot[kOsWarps];
   __shared__ uint32_t s_part;
 
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -171,16 +195,20 @@ __global__ void __launch_bounds__(kSortThreads) onesweep_kernel(
   for (int i = lane; i < 256; i += 32) warp_hist[warp][i] = 0;
   __syncthreads();
   const int part = (int)s_part;
-  const int64_t base = (int64_t)part * kPartKeys + (int64_t)warp * (32 * kSortItems);
+  const int64_t base = (int64_t)part * kPartKeys + (int64_t)warp * (32 * kOsItems);
 
-  uint32_t key[kSortItems], val[kSortItems], rank[kSortItems];
+  uint32_t key[kOsItems], val[kOsItems], rank[kOsItems];
   const uint32_t lt = lanemask_lt();
 #pragma unroll
-  for (int it = 0; it < kSortItems; ++it) {
+  for (int it = 0; it < kOsItems; ++it) {
     const int64_t e = base + it * 32 + lane;
     const bool valid = e < n;
     key[it] = valid ? keys_in[e] : 0u;
     val[it] = valid ? vals_in[e] : 0u;
+  }
+#pragma unroll
+  for (int it = 0; it < kOsItems; ++it) {
+    const bool valid = base + it * 32 + lane < n;
     const uint32_t d = (key[it] >> shift) & 0xFFu;  // 0 for invalid lanes
     const uint32_t peers = __match_any_sync(0xffffffffu, valid ? d : 256u);
     const uint32_t old = warp_hist[warp][d];
@@ -191,35 +219,40 @@ __global__ void __launch_bounds__(kSortThreads) onesweep_kernel(
   }
   __syncthreads();
 
-  // Per digit: exclusive offsets across warps, partition count, look-back.
-  const int t = threadIdx.x;  // digit
+  // Per digit (threads 0..255): exclusive offsets across warps, partition
+  // count, status publication, look-back.
+  const int t = threadIdx.x;
+  const bool is_digit = t < 256;
   uint32_t count = 0;
+  if (is_digit) {
 #pragma unroll
-  for (int w = 0; w < NW; ++w) {
-    const uint32_t c = warp_hist[w][t];
-    warp_hist[w][t] = count;
-    count += c;
+    for (int w = 0; w < kOsWarps; ++w) {
+      const uint32_t c = warp_hist[w][t];
+      warp_hist[w][t] = count;
+      count += c;
+    }
+    uint32_t* my_status = status + (size_t)part * 256 + t;
+    st_volatile(my_status, (part == 0 ? kFlagInc : kFlagAgg) | count);
   }
-  uint32_t* my_status = status + (size_t)part * 256 + t;
-  if (part == 0)
-    st_volatile(my_status, kFlagInc | count);
-  else
-    st_volatile(my_status, kFlagAgg | count);
   uint32_t unused;
-  const uint32_t digit_start = block_excl_scan(pass_hist[t], unused, s_warp_tot);
-  uint32_t prior = 0;
-  if (part > 0) {
-    prior = look_back(status + t, part, 256, info);
-    st_volatile(my_status, kFlagInc | ((prior + count) & kValMask));
+  const uint32_t digit_start =
+      block_excl_scan<kOsThreads>(is_digit ? pass_hist[t] : 0u, unused, s_warp_tot);
+  if (is_digit) {
+    uint32_t prior = 0;
+    if (part > 0) {
+      prior = look_back(status + t, part, 256, info);
+      st_volatile(status + (size_t)part * 256 + t, kFlagInc | ((prior + count) & kValMask));
+    }
+    s_global_base[t] = digit_start + prior;
   }
-  s_global_base[t] = digit_start + prior;
   uint32_t local_total;
-  s_block_excl[t] = block_excl_scan(count, local_total, s_warp_tot);
+  const uint32_t bex = block_excl_scan<kOsThreads>(is_digit ? count : 0u, local_total, s_warp_tot);
+  if (is_digit) s_block_excl[t] = bex;
   __syncthreads();
 
   // Stage in digit order.
 #pragma unroll
-  for (int it = 0; it < kSortItems; ++it) {
+  for (int it = 0; it < kOsItems; ++it) {
     const int64_t e = base + it * 32 + lane;
     if (e < n) {
       const uint32_t d = (key[it] >> shift) & 0xFFu;
@@ -229,7 +262,7 @@ __global__ void __launch_bounds__(kSortThreads) onesweep_kernel(
     }
   }
   __syncthreads();
-  for (uint32_t j = threadIdx.x; j < local_total; j += kSortThreads) {
+  for (uint32_t j = threadIdx.x; j < local_total; j += kOsThreads) {
     const uint32_t k = s_keys[j];
     const uint32_t d = (k >> shift) & 0xFFu;
     const uint32_t dst = s_global_base[d] + (j - s_block_excl[d]);
@@ -242,6 +275,13 @@ __global__ void __launch_bounds__(kSortThreads) onesweep_kernel(
   }
 }
 
+static int onesweep_attr() {
+  return cudaFuncSetAttribute(onesweep_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)kOsSmem) == cudaSuccess
+             ? PGB_OK
+             : PGB_ERR_CUDA;
+}
+
 // ---------------------------------------------------------------------------
 // 3a. scan of tiles_touched in depth order
 //
@@ -250,7 +290,7 @@ __global__ void __launch_bounds__(kSortThreads) onesweep_kernel(
 // and, for every emission chunk boundary b * kEmitChunk that falls inside
 // [offs[i], offs[i] + count), chunk_first[b] = i.
 // ---------------------------------------------------------------------------
-constexpr int kEmitChunk = 2048;
+constexpr int kEmitChunk = 1024;
 constexpr int kEmitThreads = 256;
 
 __global__ void __launch_bounds__(kSortThreads) scan_rect_kernel(
@@ -332,10 +372,13 @@ __global__ void __launch_bounds__(kSortThreads) scan_rect_kernel(
 //
 // CTA b writes entries [b*kEmitChunk, min(K, (b+1)*kEmitChunk)): it stages
 // the offsets, rectangles and ids of the Gaussians that own them in shared
-// memory, and each thread finds the owner of its entries by binary search,
-// so every CTA does the same amount of work however unevenly the tiles are
-// spread over Gaussians.  Writes are coalesced.
+// memory; each thread takes 8 consecutive entries, finds the owner of the
+// first by binary search and walks forward; the pairs are staged in shared
+// memory and written with 16-byte stores.  Every CTA does the same amount of
+// work however unevenly the tiles are spread over Gaussians.
 // ---------------------------------------------------------------------------
+constexpr int kEmitPer = kEmitChunk / kEmitThreads;  // 4
+
 __global__ void __launch_bounds__(kEmitThreads) emit_kernel(
     const uint32_t* __restrict__ order, const uint32_t* __restrict__ offs,
     const uint2* __restrict__ rect, const uint32_t* __restrict__ chunk_first, int64_t n_sorted,
@@ -345,19 +388,21 @@ __global__ void __launch_bounds__(kEmitThreads) emit_kernel(
   __shared__ uint32_t s_off[CAP];
   __shared__ uint2 s_rect[CAP];
   __shared__ uint32_t s_g[CAP];
+  __shared__ __align__(16) uint32_t s_key[kEmitChunk];
+  __shared__ __align__(16) uint32_t s_val[kEmitChunk];
   __shared__ uint32_t s_hist[kMaxTilePasses][256];
   const int gx = grid_x(W);
   const int64_t e0 = (int64_t)blockIdx.x * kEmitChunk;
   const int64_t e1 = min(K, e0 + kEmitChunk);
-  const int64_t nchunks = (K + kEmitChunk - 1) / kEmitChunk;
   // owners of this chunk's first entry and of the next chunk's first entry
   // (for the last chunk: of entry K - 1)
   const int64_t i0 = chunk_first[blockIdx.x];
   const int64_t i1 = chunk_first[blockIdx.x + 1];
   const int64_t m = i1 - i0 + 1;
-  (void)nchunks;
   for (int i = threadIdx.x; i < kMaxTilePasses * 256; i += kEmitThreads) (&s_hist[0][0])[i] = 0;
-  const bool staged = m >= 1 && m <= CAP && i1 < n_sorted;
+  const bool ok_range = i0 <= i1 && i1 < n_sorted;
+  if (!ok_range && threadIdx.x == 0) set_error(info, PGB_ERR_OVERFLOW);
+  const bool staged = ok_range && m <= CAP;
   if (staged) {
     for (int64_t i = threadIdx.x; i < m; i += kEmitThreads) {
       s_off[i] = offs[i0 + i];
@@ -366,31 +411,55 @@ __global__ void __launch_bounds__(kEmitThreads) emit_kernel(
     }
   }
   __syncthreads();
-  const bool ok_range = i0 <= i1 && i1 < n_sorted;
-  if (!ok_range && threadIdx.x == 0) set_error(info, PGB_ERR_OVERFLOW);
-  const uint32_t lane = threadIdx.x & 31;
-  // fixed trip count: every lane reaches the warp collectives below
-  for (int k = 0; k < kEmitChunk / kEmitThreads; ++k) {
-    const int64_t e = e0 + (int64_t)k * kEmitThreads + threadIdx.x;
-    const bool valid = ok_range && e < e1;
-    uint32_t tid = 0;  // a tiles_touched/rectangle mismatch leaves tile 0 (reported)
-    if (valid) {
-      // owner: the last position p in [i0, i1] with offs[p] <= e
-      int64_t lo = 0, hi = i1 - i0;
-      while (lo < hi) {
-        const int64_t mid = (lo + hi + 1) >> 1;
-        const uint32_t o = staged ? s_off[mid] : offs[i0 + mid];
-        if ((int64_t)o <= e) lo = mid; else hi = mid - 1;
-      }
-      const uint32_t o = staged ? s_off[lo] : offs[i0 + lo];
-      const uint2 rc = staged ? s_rect[lo] : rect[i0 + lo];
-      const uint32_t g = staged ? s_g[lo] : order[i0 + lo];
-      const uint32_t j = (uint32_t)(e - o);
-      const uint32_t w = rc.y & 0xFFFFu, h = rc.y >> 16;
-      if (w > 0 && j < w * h) tid = ((rc.x >> 16) + j / w) * (uint32_t)gx + (rc.x & 0xFFFFu) + j % w;
-      tkeys[e] = tid;
-      tvals[e] = g;
+  const int64_t ebeg = e0 + (int64_t)threadIdx.x * kEmitPer;
+  if (ok_range && ebeg < e1) {
+    auto off_at = [&](int64_t p) -> int64_t { return staged ? s_off[p] : offs[i0 + p]; };
+    // owner of ebeg: the last position p in [0, i1 - i0] with offs <= ebeg
+    int64_t lo = 0, hi = i1 - i0;
+    while (lo < hi) {
+      const int64_t mid = (lo + hi + 1) >> 1;
+      if (off_at(mid) <= ebeg) lo = mid; else hi = mid - 1;
     }
+    int64_t own = lo;
+    int64_t next_off = own < i1 - i0 ? off_at(own + 1) : INT64_MAX;
+    for (int j = 0; j < kEmitPer; ++j) {
+      const int64_t e = ebeg + j;
+      if (e >= e1) break;
+      while (e >= next_off) {  // walk to the owner of e (skips zero-count Gaussians)
+        ++own;
+        next_off = own < i1 - i0 ? off_at(own + 1) : INT64_MAX;
+      }
+      const uint32_t o = (uint32_t)off_at(own);
+      const uint2 rc = staged ? s_rect[own] : rect[i0 + own];
+      const uint32_t g = staged ? s_g[own] : order[i0 + own];
+      const uint32_t jj = (uint32_t)(e - o);
+      const uint32_t w = rc.y & 0xFFFFu, h = rc.y >> 16;
+      uint32_t tid = 0;  // a tiles_touched/rectangle mismatch leaves tile 0 (reported)
+      if (w > 0 && jj < w * h) tid = ((rc.x >> 16) + jj / w) * (uint32_t)gx + (rc.x & 0xFFFFu) + jj % w;
+      s_key[threadIdx.x * kEmitPer + j] = tid;
+      s_val[threadIdx.x * kEmitPer + j] = g;
+    }
+  }
+  __syncthreads();
+  // coalesced write-out and tile digit histograms (digits of consecutive
+  // keys read by consecutive lanes)
+  const int cnt = ok_range ? (int)(e1 - e0) : 0;
+  if (cnt == kEmitChunk) {
+    for (int q = threadIdx.x; q < kEmitChunk / 4; q += kEmitThreads) {
+      reinterpret_cast<uint4*>(tkeys + e0)[q] = reinterpret_cast<const uint4*>(s_key)[q];
+      reinterpret_cast<uint4*>(tvals + e0)[q] = reinterpret_cast<const uint4*>(s_val)[q];
+    }
+  } else {
+    for (int q = threadIdx.x; q < cnt; q += kEmitThreads) {
+      tkeys[e0 + q] = s_key[q];
+      tvals[e0 + q] = s_val[q];
+    }
+  }
+  const uint32_t lane = threadIdx.x & 31;
+  for (int q0 = 0; q0 < kEmitChunk; q0 += kEmitThreads) {
+    const int q = q0 + threadIdx.x;
+    const bool valid = q < cnt;
+    const uint32_t tid = valid ? s_key[q] : 0u;
     for (int p = 0; p < tile_passes; ++p) {
       const uint32_t d = (tid >> (8 * p)) & 0xFFu;
       const uint32_t peers = __match_any_sync(0xffffffffu, valid ? d : 256u + lane);
@@ -514,6 +583,7 @@ int pgb_sort_gaussian_begin(const float* depth, const int32_t* radius,
   if (cudaMemsetAsync(info, 0, 2 * sizeof(int64_t), s) != cudaSuccess) return PGB_ERR_CUDA;
   if (cudaMemsetAsync(scratch_n, 0, L.zero_bytes, s) != cudaSuccess) return PGB_ERR_CUDA;
   if (n == 0) return PGB_OK;
+  if (onesweep_attr() != PGB_OK) return PGB_ERR_CUDA;
   uint32_t* counters = at<uint32_t>(scratch_n, L.counters);
   uint32_t* hist = at<uint32_t>(scratch_n, L.depth_hist);
   uint32_t* status = at<uint32_t>(scratch_n, L.depth_status);
@@ -528,9 +598,9 @@ int pgb_sort_gaussian_begin(const float* depth, const int32_t* radius,
     const uint32_t* vi = (p & 1) ? v1 : v0;
     uint32_t* ko = (p & 1) ? k0 : k1;
     uint32_t* vo = (p & 1) ? v0 : v1;
-    onesweep_kernel<<<L.parts, kSortThreads, 0, s>>>(ki, vi, ko, vo, n, 8 * p, hist + 256 * p,
-                                                     status + (size_t)p * L.parts * 256,
-                                                     counters + p, info);
+    onesweep_kernel<<<L.parts, kOsThreads, kOsSmem, s>>>(ki, vi, ko, vo, n, 8 * p, hist + 256 * p,
+                                                         status + (size_t)p * L.parts * 256,
+                                                         counters + p, info);
   }
   // four passes: the depth order ends in (k0, v0)
   return launch_status();
@@ -558,6 +628,7 @@ int pgb_sort_gaussian_finish(const float* uv, const int32_t* radius, const int32
   if (cudaMemsetAsync(at<char>(scratch_k, LK.status), 0,
                       (size_t)kMaxTilePasses * LK.parts * 256 * sizeof(uint32_t), s) != cudaSuccess)
     return PGB_ERR_CUDA;
+  if (onesweep_attr() != PGB_OK) return PGB_ERR_CUDA;
   uint32_t* counters = at<uint32_t>(scratch_n, LN.counters);
   uint32_t* thist = at<uint32_t>(scratch_n, LN.tile_hist);
   const uint32_t* order = at<uint32_t>(scratch_n, LN.dv0);
@@ -577,7 +648,7 @@ int pgb_sort_gaussian_finish(const float* uv, const int32_t* radius, const int32
   for (int p = 0; p < passes; ++p) {
     const bool last = p == passes - 1;
     uint32_t* vo = last ? reinterpret_cast<uint32_t*>(ids_out) : bufv[cur ^ 1];
-    onesweep_kernel<<<LK.parts, kSortThreads, 0, s>>>(
+    onesweep_kernel<<<LK.parts, kOsThreads, kOsSmem, s>>>(
         bufk[cur], bufv[cur], bufk[cur ^ 1], vo, k, 8 * p, thist + 256 * p,
         status + (size_t)p * LK.parts * 256, counters + 5 + p, info);
     cur ^= 1;
