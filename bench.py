@@ -50,6 +50,7 @@ def parse_args():
     ap.add_argument("--cpu-tile-stride", type=int, default=0,
                     help="CPU sample: blend every k-th tile (0 = choose for ~10-30 s of CPU work)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-serve", action="store_true", help="skip the serving p50/p99 leg")
     return ap.parse_args()
 
 
@@ -337,6 +338,35 @@ def run_reference(args):
     }), flush=True)
 
 
+# --------------------------------------------------------------- serving ---
+SERVE_WORKLOAD = ("serving: 8 resident SH3 scenes, N log-uniform in [200k, 2M], forward RGB, "
+                  "Poisson arrivals, camera radius U[3,6], 512^2/800^2/1280x720/1920x1080")
+
+
+def serve_measure(device, rates=(100, 400, 1000), duration=1.5):
+    """p50/p99 latency and Mpix/s of the continuous-batching server against
+    the one-request-at-a-time plain path, per Poisson arrival rate."""
+    from pointrix_gb300 import serve
+
+    scenes = serve.serving_scenes(device=device)
+    for cls in (serve.PlainServer, serve.RenderServer):   # warm-up of both paths
+        srv = cls(scenes)
+        for r in serve.random_requests(16, len(scenes), seed=99):
+            srv.submit(r)
+        srv.close()
+    out = []
+    for rate in rates:
+        row = {"rate_req_per_s": rate}
+        for name, cls in (("plain", serve.PlainServer), ("continuous", serve.RenderServer)):
+            reqs = serve.random_requests(int(rate * duration), len(scenes), seed=rate, rate=rate)
+            srv = cls(scenes)
+            t0 = serve.drive(srv, reqs)
+            row[name] = {k: round(v, 3) if isinstance(v, float) else v
+                         for k, v in serve.summarize(srv.close(), t0).items()}
+        out.append(row)
+    return {"workload": SERVE_WORKLOAD, "duration_s": duration, "rates": out}
+
+
 # ------------------------------------------------------------- GPU arm ---
 def run_gb300(args):
     world, rank, local = dist_env()
@@ -433,6 +463,9 @@ def run_gb300(args):
                 "peak_source": peak_kind, "launch_ms": per_op[dom],
                 "algorithmic_bytes_per_launch": dom_bytes}
 
+    serving = None
+    if rank == 0 and not args.no_serve:
+        serving = serve_measure(device)
     if rank == 0:
         cpu = None
         if world == 1 and not args.no_cpu_baseline:
@@ -460,6 +493,7 @@ def run_gb300(args):
             "gpu_launches": kt.total_launches(),
             "clocks": clocks.summary(),
             "cpu_baseline": cpu,
+            "serve": serving,
         }
         print(json.dumps(line), flush=True)
     if world > 1:

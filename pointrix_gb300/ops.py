@@ -20,6 +20,7 @@ from ._lib import PgbError, call
 
 __all__ = [
     "compute_sh", "project_point", "compute_cov3d", "ewa_project", "sort_gaussian",
+    "sort_gaussian_begin", "SortHandle",
     "alpha_blending", "alpha_blending_with_state", "check_device_status", "kernel_timing",
     "NEAREST_DEFAULT", "EXTENT_DEFAULT",
 ]
@@ -405,11 +406,45 @@ def _sort_scratch(n, k, W, H):
     return bn.value, bk.value
 
 
-def sort_gaussian(uv, depth, W, H, radius, tiles_touched):
-    """Tile binning: ``gaussian_ids_sorted`` [K] int32 (ids ordered by tile,
-    then depth, then id) and ``tile_range`` [T,2] int32 ([start, end) per
-    16x16 tile, [0,0] when empty), K = sum of ``tiles_touched`` over
-    Gaussians with ``radius > 0``.  Reads K back to the host (one sync)."""
+class SortHandle:
+    """A sort between its two phases: the depth sort and the count K are
+    enqueued, K is being copied to pinned host memory.  ``ready()`` polls
+    without blocking; ``finish()`` allocates the K-sized outputs and enqueues
+    the tile passes (on the stream that was current at ``begin``)."""
+
+    __slots__ = ("uv", "depth", "radius", "tiles", "W", "H", "n", "dev", "stream", "scratch_n",
+                 "bn", "info", "host", "event")
+
+    def ready(self) -> bool:
+        return self.event.query()
+
+    def count(self) -> int:
+        """K, the number of (Gaussian, tile) entries (waits for phase one)."""
+        self.event.synchronize()
+        _lib.check(int(self.host[1]), "sort_gaussian (depth passes)")
+        return int(self.host[0])
+
+    def finish(self):
+        K = self.count()
+        W, H, n, dev = self.W, self.H, self.n, self.dev
+        T = ((W + TILE - 1) // TILE) * ((H + TILE - 1) // TILE)
+        with torch.cuda.stream(self.stream):
+            _, bk = _sort_scratch(n, K, W, H)
+            scratch_k = torch.empty(max(bk, 1), dtype=torch.uint8, device=dev)
+            ids = torch.empty(K, dtype=torch.int32, device=dev)
+            rng = torch.empty(T, 2, dtype=torch.int32, device=dev)
+            passes = 1 if T <= 256 else (2 if T <= 65536 else 3)
+            with _timed("sort_finish", dev, (2 + passes) if (K and n) else 0):
+                call("pgb_sort_gaussian_finish", _ptr(self.uv), _ptr(self.radius), _ptr(self.tiles),
+                     n, W, H, K, _ptr(self.scratch_n), self.bn, _ptr(scratch_k), bk, _ptr(self.info),
+                     _ptr(ids) if K else None, _ptr(rng), self.stream.cuda_stream)
+            _defer_check(self.info[1:], "sort_gaussian (tile passes)")
+        return ids, rng
+
+
+def sort_gaussian_begin(uv, depth, W, H, radius, tiles_touched) -> SortHandle:
+    """Phase one of :func:`sort_gaussian` without blocking the host: sorts the
+    Gaussians by depth and starts the read-back of K."""
     _need(uv, "uv", ndim=2, last=2)
     _need(depth, "depth")
     _need(radius, "radius", dtype=torch.int32)
@@ -418,34 +453,34 @@ def sort_gaussian(uv, depth, W, H, radius, tiles_touched):
     n = uv.shape[0]
     if depth.numel() != n or radius.numel() != n or tiles_touched.numel() != n:
         raise ValueError("sort_gaussian: uv, depth, radius and tiles_touched disagree on N")
-    dev = uv.device
-    st = _stream(dev)
-    uv, depth = _c(uv.detach()), _c(depth.detach().reshape(-1))
-    radius, tiles_touched = _c(radius.reshape(-1)), _c(tiles_touched.reshape(-1))
-    bn, _ = _sort_scratch(n, 0, W, H)
-    scratch_n = torch.empty(max(bn, 1), dtype=torch.uint8, device=dev)
-    info = torch.empty(2, dtype=torch.int64, device=dev)
-    with _timed("sort_begin", dev, 5 if n else 0):
-        call("pgb_sort_gaussian_begin", _ptr(depth), _ptr(radius), _ptr(tiles_touched), n, W, H,
-             _ptr(scratch_n), bn, _ptr(info), st)
-    host = torch.empty(2, dtype=torch.int64, pin_memory=True)
-    host.copy_(info, non_blocking=True)
-    torch.cuda.current_stream(dev).synchronize()
+    h = SortHandle()
+    h.dev = uv.device
+    h.stream = torch.cuda.current_stream(h.dev)
+    h.W, h.H, h.n = W, H, n
+    h.uv, h.depth = _c(uv.detach()), _c(depth.detach().reshape(-1))
+    h.radius, h.tiles = _c(radius.reshape(-1)), _c(tiles_touched.reshape(-1))
+    h.bn, _ = _sort_scratch(n, 0, W, H)
+    h.scratch_n = torch.empty(max(h.bn, 1), dtype=torch.uint8, device=h.dev)
+    h.info = torch.empty(2, dtype=torch.int64, device=h.dev)
+    with _timed("sort_begin", h.dev, 5 if n else 0):
+        call("pgb_sort_gaussian_begin", _ptr(h.depth), _ptr(h.radius), _ptr(h.tiles), n, W, H,
+             _ptr(h.scratch_n), h.bn, _ptr(h.info), h.stream.cuda_stream)
+    h.host = torch.empty(2, dtype=torch.int64, pin_memory=True)
+    h.host.copy_(h.info, non_blocking=True)
+    h.event = torch.cuda.Event()
+    h.event.record(h.stream)
+    return h
+
+
+def sort_gaussian(uv, depth, W, H, radius, tiles_touched):
+    """Tile binning: ``gaussian_ids_sorted`` [K] int32 (ids ordered by tile,
+    then depth, then id) and ``tile_range`` [T,2] int32 ([start, end) per
+    16x16 tile, [0,0] when empty), K = sum of ``tiles_touched`` over
+    Gaussians with ``radius > 0``.  Reads K back to the host (one sync)."""
+    h = sort_gaussian_begin(uv, depth, W, H, radius, tiles_touched)
+    h.count()
     _drain_pending(block=False)
-    K, err = int(host[0]), int(host[1])
-    _lib.check(err, "sort_gaussian (depth passes)")
-    T = ((W + TILE - 1) // TILE) * ((H + TILE - 1) // TILE)
-    _, bk = _sort_scratch(n, K, W, H)
-    scratch_k = torch.empty(max(bk, 1), dtype=torch.uint8, device=dev)
-    ids = torch.empty(K, dtype=torch.int32, device=dev)
-    rng = torch.empty(T, 2, dtype=torch.int32, device=dev)
-    passes = 1 if T <= 256 else (2 if T <= 65536 else 3)
-    with _timed("sort_finish", dev, (2 + passes) if (K and n) else 0):
-        call("pgb_sort_gaussian_finish", _ptr(uv), _ptr(radius), _ptr(tiles_touched), n, W, H, K,
-             _ptr(scratch_n), bn, _ptr(scratch_k), bk, _ptr(info), _ptr(ids) if K else None,
-             _ptr(rng), st)
-    _defer_check(info[1:], "sort_gaussian (tile passes)")
-    return ids, rng
+    return h.finish()
 
 
 # ---------------------------------------------------------------------------
