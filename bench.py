@@ -51,6 +51,8 @@ def parse_args():
                     help="CPU sample: blend every k-th tile (0 = choose for ~10-30 s of CPU work)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-serve", action="store_true", help="skip the serving p50/p99 leg")
+    ap.add_argument("--no-recompute", action="store_true",
+                    help="skip the 6M-Gaussian 4K stored-vs-recompute leg")
     return ap.parse_args()
 
 
@@ -338,6 +340,52 @@ def run_reference(args):
     }), flush=True)
 
 
+# -------------------------------------------------------- recompute mode ---
+RECOMPUTE_WORKLOAD = ("memory-bound differentiation: 6,000,000 Gaussians SH3, one 3840x2160 view, "
+                      "focal 2800, radius 5, RGB+depth, L1 loss, backward to all Gaussian params")
+
+
+def recompute_measure(device, n=6_000_000, steps=3):
+    """Stored vs recompute-in-backward: step time, peak HBM, memory held from
+    forward to backward, and gradient agreement between the two modes."""
+    from pointrix_gb300 import workloads as WL
+    from pointrix_gb300.renderer import MsplatRender
+
+    scene = WL.scene_sh3(4, n).to(device).leaves()
+    g = torch.Generator().manual_seed(44)
+    cam = WL.make_camera(g, 3840, 2160, 2800.0, 5.0).to(device)
+    target = torch.rand(4, cam.H, cam.W, generator=g).to(device)
+    res, grads = {}, {}
+    for mode in (False, True):
+        r = MsplatRender(MsplatRender.Config(render_depth=True, recompute_backward=mode), device=device)
+        r.sh_degree = 3
+        params = [scene.position, scene.log_scale, scene.quat_raw, scene.opacity_logit, scene.shs]
+        times, held = [], 0
+        for it in range(steps + 1):
+            zero_grads(params)
+            torch.cuda.synchronize(device)
+            torch.cuda.reset_peak_memory_stats(device)
+            base = torch.cuda.memory_allocated(device)
+            t0 = time.perf_counter()
+            pos, sc, q, op, shs = scene.activated()
+            out = r.render_iter(cam.H, cam.W, cam.extr, cam.intr, cam.center, pos, op, sc, q, shs)
+            f = out["rendered_features_split"]
+            loss = torch.nn.functional.l1_loss(torch.cat([f["rgb"], f["depth"]], 0), target)
+            torch.cuda.synchronize(device)
+            held = torch.cuda.memory_allocated(device) - base
+            loss.backward()
+            torch.cuda.synchronize(device)
+            if it > 0:
+                times.append(time.perf_counter() - t0)
+        peak = torch.cuda.max_memory_allocated(device) - base
+        grads[mode] = [p.grad.detach().clone() for p in params]
+        res["recompute" if mode else "stored"] = {
+            "ms_per_step": 1e3 * statistics.mean(times), "peak_gb": peak / 1e9,
+            "held_fwd_to_bwd_gb": held / 1e9}
+    rel = max(float((a - b).norm() / b.norm().clamp(min=1e-30)) for a, b in zip(grads[True], grads[False]))
+    return {"workload": RECOMPUTE_WORKLOAD, **res, "grad_rel_l2_max": rel}
+
+
 # --------------------------------------------------------------- serving ---
 SERVE_WORKLOAD = ("serving: 8 resident SH3 scenes, N log-uniform in [200k, 2M], forward RGB, "
                   "Poisson arrivals, camera radius U[3,6], 512^2/800^2/1280x720/1920x1080")
@@ -463,9 +511,11 @@ def run_gb300(args):
                 "peak_source": peak_kind, "launch_ms": per_op[dom],
                 "algorithmic_bytes_per_launch": dom_bytes}
 
-    serving = None
+    serving = recompute = None
     if rank == 0 and not args.no_serve:
         serving = serve_measure(device)
+    if rank == 0 and not args.no_recompute:
+        recompute = recompute_measure(device)
     if rank == 0:
         cpu = None
         if world == 1 and not args.no_cpu_baseline:
@@ -494,6 +544,7 @@ def run_gb300(args):
             "clocks": clocks.summary(),
             "cpu_baseline": cpu,
             "serve": serving,
+            "recompute": recompute,
         }
         print(json.dumps(line), flush=True)
     if world > 1:

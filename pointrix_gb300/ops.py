@@ -20,7 +20,7 @@ from ._lib import PgbError, call
 
 __all__ = [
     "compute_sh", "project_point", "compute_cov3d", "ewa_project", "sort_gaussian",
-    "sort_gaussian_begin", "SortHandle",
+    "sort_gaussian_begin", "SortHandle", "rasterize",
     "alpha_blending", "alpha_blending_with_state", "check_device_status", "kernel_timing",
     "NEAREST_DEFAULT", "EXTENT_DEFAULT",
 ]
@@ -486,21 +486,44 @@ def sort_gaussian(uv, depth, W, H, radius, tiles_touched):
 # ---------------------------------------------------------------------------
 # alpha_blending
 # ---------------------------------------------------------------------------
+def _blend_forward_raw(uv, conic, opacity, feature, ids, tile_range, bg, W, H):
+    n, C = feature.shape
+    dev = feature.device
+    rf = _lib.lib().pgb_blend_record_floats(C)
+    records = torch.empty(n, rf, dtype=torch.float32, device=dev)
+    out = torch.empty(C, H, W, dtype=torch.float32, device=dev)
+    final_T = torch.empty(H, W, dtype=torch.float32, device=dev)
+    ncon = torch.empty(H, W, dtype=torch.int32, device=dev)
+    status = _status_word(dev)
+    with _timed("alpha_blending_fwd", dev, 2 if n else 1):
+        call("pgb_alpha_blending_forward", _ptr(uv), _ptr(conic), _ptr(opacity), _ptr(feature), n, C,
+             _ptr(ids), ids.numel(), _ptr(tile_range), float(bg), W, H, _ptr(records), _ptr(out),
+             _ptr(final_T), _ptr(ncon), _ptr(status), _stream(dev))
+    return records, out, final_T, ncon
+
+
+def _blend_backward_raw(records, ids, tile_range, final_T, ncon, d_out, n, C, bg, W, H):
+    dev = records.device
+    grec = torch.empty(n, _lib.lib().pgb_blend_grad_record_floats(C), dtype=torch.float32, device=dev)
+    d_uv = torch.empty(n, 2, dtype=torch.float32, device=dev)
+    d_conic = torch.empty(n, 3, dtype=torch.float32, device=dev)
+    d_op = torch.empty(n, dtype=torch.float32, device=dev)
+    d_feat = torch.empty(n, C, dtype=torch.float32, device=dev)
+    status = _status_word(dev)
+    with _timed("alpha_blending_bwd", dev, 2 if n else 0):
+        call("pgb_alpha_blending_backward", _ptr(records), n, C, _ptr(ids), ids.numel(),
+             _ptr(tile_range), bg, W, H, _ptr(final_T), _ptr(ncon), _ptr(_c(d_out)),
+             _ptr(grec), _ptr(d_uv), _ptr(d_conic), _ptr(d_op), _ptr(d_feat), _ptr(status),
+             _stream(dev))
+    return d_uv, d_conic, d_op, d_feat
+
+
 class _AlphaBlending(torch.autograd.Function):
     @staticmethod
     def forward(ctx, uv, conic, opacity, feature, ids, tile_range, bg, W, H, ndc):
         n, C = feature.shape
-        dev = feature.device
-        rf = _lib.lib().pgb_blend_record_floats(C)
-        records = torch.empty(n, rf, dtype=torch.float32, device=dev)
-        out = torch.empty(C, H, W, dtype=torch.float32, device=dev)
-        final_T = torch.empty(H, W, dtype=torch.float32, device=dev)
-        ncon = torch.empty(H, W, dtype=torch.int32, device=dev)
-        status = _status_word(dev)
-        with _timed("alpha_blending_fwd", dev, 2 if n else 1):
-            call("pgb_alpha_blending_forward", _ptr(uv), _ptr(conic), _ptr(opacity), _ptr(feature), n, C,
-                 _ptr(ids), ids.numel(), _ptr(tile_range), float(bg), W, H, _ptr(records), _ptr(out),
-                 _ptr(final_T), _ptr(ncon), _ptr(status), _stream(dev))
+        records, out, final_T, ncon = _blend_forward_raw(uv, conic, opacity, feature, ids,
+                                                         tile_range, bg, W, H)
         ctx.save_for_backward(records, ids, tile_range, final_T, ncon)
         ctx.cfg = (n, C, float(bg), W, H, ndc is not None)
         ctx.mark_non_differentiable(final_T, ncon)
@@ -510,20 +533,59 @@ class _AlphaBlending(torch.autograd.Function):
     def backward(ctx, d_out, _dT, _dn):
         records, ids, tile_range, final_T, ncon = ctx.saved_tensors
         n, C, bg, W, H, has_ndc = ctx.cfg
-        dev = records.device
-        grec = torch.empty(n, _lib.lib().pgb_blend_grad_record_floats(C), dtype=torch.float32, device=dev)
-        d_uv = torch.empty(n, 2, dtype=torch.float32, device=dev)
-        d_conic = torch.empty(n, 3, dtype=torch.float32, device=dev)
-        d_op = torch.empty(n, dtype=torch.float32, device=dev)
-        d_feat = torch.empty(n, C, dtype=torch.float32, device=dev)
-        status = _status_word(dev)
-        with _timed("alpha_blending_bwd", dev, 2 if n else 0):
-            call("pgb_alpha_blending_backward", _ptr(records), n, C, _ptr(ids), ids.numel(),
-                 _ptr(tile_range), bg, W, H, _ptr(final_T), _ptr(ncon), _ptr(_c(d_out)),
-                 _ptr(grec), _ptr(d_uv), _ptr(d_conic), _ptr(d_op), _ptr(d_feat), _ptr(status),
-                 _stream(dev))
+        d_uv, d_conic, d_op, d_feat = _blend_backward_raw(records, ids, tile_range, final_T, ncon,
+                                                          d_out, n, C, bg, W, H)
         d_ndc = d_uv.clone() if has_ndc else None
         return d_uv, d_conic, d_op, d_feat, None, None, None, None, None, d_ndc
+
+
+class _RasterizeRecompute(torch.autograd.Function):
+    """Sort + blend whose backward recomputes the tile lists, the records and
+    the per-pixel final transmittance / last-contributor counts instead of
+    keeping them alive between forward and backward."""
+
+    @staticmethod
+    def forward(ctx, uv, conic, opacity, feature, depth, radius, tiles, bg, W, H, ndc):
+        ids, rng = sort_gaussian(uv, depth, W, H, radius, tiles)
+        _, out, _, _ = _blend_forward_raw(uv, conic, opacity, feature, ids, rng, bg, W, H)
+        ctx.save_for_backward(uv, conic, opacity, feature, depth, radius, tiles)
+        ctx.cfg = (float(bg), W, H, ndc is not None)
+        return out
+
+    @staticmethod
+    def backward(ctx, d_out):
+        uv, conic, opacity, feature, depth, radius, tiles = ctx.saved_tensors
+        bg, W, H, has_ndc = ctx.cfg
+        n, C = feature.shape
+        ids, rng = sort_gaussian(uv, depth, W, H, radius, tiles)
+        records, _, final_T, ncon = _blend_forward_raw(uv, conic, opacity, feature, ids, rng, bg, W, H)
+        d_uv, d_conic, d_op, d_feat = _blend_backward_raw(records, ids, rng, final_T, ncon, d_out,
+                                                          n, C, bg, W, H)
+        d_ndc = d_uv.clone() if has_ndc else None
+        return d_uv, d_conic, d_op, d_feat, None, None, None, None, None, None, d_ndc
+
+
+def rasterize(uv, conic, opacity, feature, depth, radius, tiles_touched, bg, W, H, ndc=None,
+              recompute=False):
+    """``sort_gaussian`` followed by ``alpha_blending`` -> [C,H,W].
+
+    With ``recompute=False`` this is exactly the two operators.  With
+    ``recompute=True`` the backward re-runs the sort and the blend forward
+    instead of keeping the tile lists, records and per-pixel state alive from
+    the forward: less memory held between forward and backward (what limits
+    4K views of millions of Gaussians), one more sort and blend forward per
+    step.  Gradients are the same in both modes."""
+    if not recompute:
+        ids, rng = sort_gaussian(uv, depth, W, H, radius, tiles_touched)
+        return alpha_blending(uv, conic, opacity, feature, ids, rng, bg, W, H, ndc)
+    _need(feature, "feature", ndim=2)
+    n, C = feature.shape
+    if C < 1 or C > 26:
+        raise ValueError(f"rasterize supports 1..26 feature channels, got {C}")
+    if isinstance(bg, torch.Tensor):
+        bg = float(bg)
+    return _RasterizeRecompute.apply(_c(uv), _c(conic), _c(opacity.reshape(n)), _c(feature),
+                                     depth, radius, tiles_touched, bg, int(W), int(H), ndc)
 
 
 def alpha_blending_with_state(uv, conic, opacity, feature, gaussian_ids_sorted, tile_range, bg, W, H,

@@ -61,6 +61,9 @@ class MsplatRender:
         update_sh_iter: int = 1000
         max_sh_degree: int = 3
         render_depth: bool = False
+        # recompute the sorted tile lists and per-pixel state in the backward
+        # instead of keeping them from the forward (memory for 4K views)
+        recompute_backward: bool = False
 
     def __init__(self, cfg: "MsplatRender.Config | dict | None" = None, white_bg: bool = False,
                  device="cuda", nearest: float = ops.NEAREST_DEFAULT):
@@ -104,8 +107,6 @@ class MsplatRender:
         cov3d = ops.compute_cov3d(scaling, rotation, visible)
         conic, radius, tiles_touched = ops.ewa_project(position, cov3d, intrinsic_params, extr, uv,
                                                        width, height, visible)
-        ids, tile_range = ops.sort_gaussian(uv, depth, width, height, radius, tiles_touched)
-
         feats = {"rgb": rgb}
         if self.cfg.render_depth:
             feats["depth"] = depth
@@ -118,8 +119,9 @@ class MsplatRender:
             ndc.retain_grad()
         except Exception as e:  # a leaf created under no_grad cannot retain
             raise ValueError("ndc does not have grad") from e
-        image = ops.alpha_blending(uv, conic, opacity, packed, ids, tile_range, self.bg_color,
-                                   width, height, ndc)
+        image = ops.rasterize(uv, conic, opacity, packed, depth, radius, tiles_touched,
+                              self.bg_color, width, height, ndc,
+                              recompute=self.cfg.recompute_backward)
         return {
             "rendered_features_split": render_features.split(image),
             "uv_points": ndc,

@@ -346,3 +346,22 @@ def test_bad_arguments_raise(small):
         ops.alpha_blending(p.uv, p.conic, p.op, p.feat, p.ids, p.rng[:-1], 0.0, p.W, p.H)
     with pytest.raises(ValueError):
         ops.sort_gaussian(p.uv, p.depth, p.W, p.H, p.radius.float(), p.tiles)
+
+
+def test_recompute_backward_matches_stored(small):
+    """rasterize(recompute=True) re-runs the sort and blend forward in the
+    backward; image and gradients equal the stored mode (1e-4 relative L2
+    for gradients: the backward's float atomics may add in another order)."""
+    p = small
+    outs = {}
+    for mode in (False, True):
+        leaves = [t.detach().clone().requires_grad_(True) for t in (p.uv, p.conic, p.op, p.feat)]
+        ndc = torch.zeros_like(p.uv, requires_grad=True)
+        img = ops.rasterize(*leaves, p.depth, p.radius, p.tiles, 0.2, p.W, p.H, ndc, recompute=mode)
+        g = torch.Generator().manual_seed(5)
+        img.backward(torch.randn(img.shape, generator=g).to(DEV))
+        outs[mode] = (img.detach(), [t.grad for t in leaves], ndc.grad)
+    assert torch.equal(outs[False][0], outs[True][0])
+    for a, b in zip(outs[False][1], outs[True][1]):
+        assert float((a - b).norm() / b.norm()) < 1e-4
+    assert torch.equal(outs[True][2], outs[True][1][0])
