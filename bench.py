@@ -51,6 +51,8 @@ def parse_args():
                     help="CPU sample: blend every k-th tile (0 = choose for ~10-30 s of CPU work)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-serve", action="store_true", help="skip the serving p50/p99 leg")
+    ap.add_argument("--no-multiview", action="store_true",
+                    help="skip the 16-view batched-vs-per-view leg")
     ap.add_argument("--no-recompute", action="store_true",
                     help="skip the 6M-Gaussian 4K stored-vs-recompute leg")
     return ap.parse_args()
@@ -340,6 +342,63 @@ def run_reference(args):
     }), flush=True)
 
 
+# ------------------------------------------------------ batched multi-view ---
+MULTIVIEW_WORKLOAD = ("batched multi-view: 3,000,000 Gaussians SH3, 16 views on a radius-5 sphere, "
+                      "resolutions from 640x480/1280x720/1600x1060/1920x1080, RGB+depth, L1 loss, "
+                      "forward+backward for all views")
+
+
+def multiview_measure(device, n=3_000_000, views=16, steps=3):
+    """Mpix/s of one batched forward+backward over all views against the
+    per-view loop of plain launches (MsplatRender.render_batch's order)."""
+    from pointrix_gb300 import multiview
+    from pointrix_gb300 import workloads as WL
+    from pointrix_gb300.renderer import MsplatRender
+
+    scene = WL.scene_sh3(3, n).to(device).leaves()
+    cams = [c.to(device) for c in WL.cameras_multiview(2, views)]
+    g = torch.Generator().manual_seed(33)
+    targets = [torch.rand(4, c.H, c.W, generator=g).to(device) for c in cams]
+    pix = sum(c.W * c.H for c in cams)
+    params = [scene.position, scene.log_scale, scene.quat_raw, scene.opacity_logit, scene.shs]
+    r = MsplatRender(MsplatRender.Config(render_depth=True), device=device)
+    r.sh_degree = 3
+    F = torch.nn.functional
+
+    def per_view():
+        pos, sc, q, op, shs = scene.activated()
+        loss = 0.0
+        for cam, tgt in zip(cams, targets):
+            out = r.render_iter(cam.H, cam.W, cam.extr, cam.intr, cam.center, pos, op, sc, q, shs)
+            f = out["rendered_features_split"]
+            loss = loss + F.l1_loss(torch.cat([f["rgb"], f["depth"]], 0), tgt)
+        loss.backward()
+
+    def batched():
+        pos, sc, q, op, shs = scene.activated()
+        imgs, _, _ = multiview.render_views(pos, sc, q, op, shs, cams)
+        loss = sum(F.l1_loss(img, tgt) for img, tgt in zip(imgs, targets))
+        loss.backward()
+
+    res = {}
+    for name, fn in (("per_view_loop", per_view), ("batched", batched)):
+        zero_grads(params)
+        fn()
+        torch.cuda.synchronize(device)
+        times = []
+        for _ in range(steps):
+            zero_grads(params)
+            torch.cuda.synchronize(device)
+            t0 = time.perf_counter()
+            fn()
+            torch.cuda.synchronize(device)
+            times.append(time.perf_counter() - t0)
+        ms = 1e3 * statistics.mean(times)
+        res[name] = {"ms_per_step": ms, "mpix_per_s": pix / (ms * 1e-3) / 1e6}
+    res["speedup"] = res["per_view_loop"]["ms_per_step"] / res["batched"]["ms_per_step"]
+    return {"workload": MULTIVIEW_WORKLOAD, "pixels_per_step": pix, **res}
+
+
 # -------------------------------------------------------- recompute mode ---
 RECOMPUTE_WORKLOAD = ("memory-bound differentiation: 6,000,000 Gaussians SH3, one 3840x2160 view, "
                       "focal 2800, radius 5, RGB+depth, L1 loss, backward to all Gaussian params")
@@ -516,6 +575,9 @@ def run_gb300(args):
         serving = serve_measure(device)
     if rank == 0 and not args.no_recompute:
         recompute = recompute_measure(device)
+    multi = None
+    if rank == 0 and not args.no_multiview:
+        multi = multiview_measure(device)
     if rank == 0:
         cpu = None
         if world == 1 and not args.no_cpu_baseline:
@@ -545,6 +607,7 @@ def run_gb300(args):
             "cpu_baseline": cpu,
             "serve": serving,
             "recompute": recompute,
+            "multiview": multi,
         }
         print(json.dumps(line), flush=True)
     if world > 1:

@@ -191,6 +191,39 @@ int pgb_alpha_blending_backward(const float* records, int64_t n, int channels,
                                 int64_t* info, void* stream);
 
 /* ---------------------------------------------------------------------
+ * Multi-view batches -- replace the per-view loop of MsplatRender.render_batch
+ * (pointrix/model/renderer/msplat.py:185-193): the sort and the blend of V
+ * views run as one launch sequence each.  Per-Gaussian arrays hold
+ * V * n_per_view elements, element g belonging to view g / n_per_view;
+ * `sizes` is a HOST array of V (width, height) pairs, 1 <= V <= 64.  The
+ * views own consecutive ranges of one 16x16 tile index space (T = sum of
+ * the views' tile counts <= 2^24, tile_range has T rows) and per-pixel
+ * arrays hold the views one after another (out: per-view [C,H,W] blocks;
+ * final_T, n_contrib: per-view [H,W] blocks).  Phase one of the sort is
+ * pgb_sort_gaussian_begin over all V * n_per_view elements (any view's size
+ * may be passed there).  Within a tile the order is depth, then element id,
+ * so each view's image equals rendering it alone.
+ * ------------------------------------------------------------------- */
+int pgb_sort_gaussian_finish_views(const float* uv, const int32_t* radius,
+                                   const int32_t* tiles_touched, int64_t n_per_view,
+                                   const int32_t* sizes, int nviews, int64_t k, void* scratch_n,
+                                   size_t bytes_n, void* scratch_k, size_t bytes_k, int64_t* info,
+                                   int32_t* ids_out, int32_t* tile_range_out, void* stream);
+int pgb_alpha_blending_forward_views(const float* uv, const float* conic, const float* opacity,
+                                     const float* feature, int64_t n_per_view, int channels,
+                                     const int32_t* ids, int64_t k, const int32_t* tile_range,
+                                     float bg, const int32_t* sizes, int nviews, float* records,
+                                     float* out, float* final_T, int32_t* n_contrib,
+                                     int64_t* info, void* stream);
+int pgb_alpha_blending_backward_views(const float* records, int64_t n_per_view, int channels,
+                                      const int32_t* ids, int64_t k, const int32_t* tile_range,
+                                      float bg, const int32_t* sizes, int nviews,
+                                      const float* final_T, const int32_t* n_contrib,
+                                      const float* d_out, float* grad_records, float* d_uv,
+                                      float* d_conic, float* d_opacity, float* d_feature,
+                                      int64_t* info, void* stream);
+
+/* ---------------------------------------------------------------------
  * Adam step over several parameter tensors in one launch -- replaces the
  * torch Adam update of the training step (pointrix/optimizer/optimizer.py:
  * 128-140; apex FusedAdam hook pointrix/optimizer/__init__.py:56-59).

@@ -270,17 +270,19 @@ __device__ __forceinline__ int warp_cull(const float* stage, int RF, int cnt, fl
 template <int NC, int RF>
 __global__ void __launch_bounds__(kBlendThreads) blend_fwd_kernel(
     const float* __restrict__ records, const int32_t* __restrict__ ids,
-    const int2* __restrict__ ranges, int64_t n, float bg, int W, int H, int C,
+    const int2* __restrict__ ranges, int64_t n, float bg, const ViewTable vt, int C,
     float* __restrict__ out, float* __restrict__ final_T, int32_t* __restrict__ n_contrib,
     int64_t* __restrict__ info) {
   extern __shared__ __align__(128) float smem[];
   __shared__ __align__(8) uint64_t bars[2];
 
   __shared__ uint8_t s_list[kBlendThreads / 32][kBatch];
-  const int gx = grid_x(W);
-  const int tile = blockIdx.x;
+  const int tile = blockIdx.x;  // global tile (of its view, for a batch)
+  int W, H, gx, ltile;
+  int64_t pbase;
+  tile_view(vt, tile, W, H, gx, ltile, pbase);
   int px, py, bx0, by0;
-  tile_pixel(tile, gx, px, py, bx0, by0);
+  tile_pixel(ltile, gx, px, py, bx0, by0);
   const bool inside = px < W && py < H;
   const float pxf = (float)px, pyf = (float)py;
   uint8_t* my_list = s_list[threadIdx.x >> 5];
@@ -357,9 +359,9 @@ __global__ void __launch_bounds__(kBlendThreads) blend_fwd_kernel(
     const int64_t plane = (int64_t)W * H;
 #pragma unroll
     for (int c = 0; c < NC; ++c)
-      if (c < C) out[c * plane + pix] = acc[c] + T * bg;
-    final_T[pix] = T;
-    n_contrib[pix] = last;
+      if (c < C) out[C * pbase + c * plane + pix] = acc[c] + T * bg;
+    final_T[pbase + pix] = T;
+    n_contrib[pbase + pix] = last;
   }
 }
 
@@ -440,7 +442,7 @@ __device__ __forceinline__ bool bwd_pixel(BwdPixel<NC>& P, int j, const float* r
 template <int NC, int RF, int GR>
 __global__ void __launch_bounds__(kBwdThreads) blend_bwd_kernel(
     const float* __restrict__ records, const int32_t* __restrict__ ids,
-    const int2* __restrict__ ranges, int64_t n, float bg, int W, int H, int C,
+    const int2* __restrict__ ranges, int64_t n, float bg, const ViewTable vt, int C,
     const float* __restrict__ final_T, const int32_t* __restrict__ n_contrib,
     const float* __restrict__ d_out, float* __restrict__ grad_records,
     int64_t* __restrict__ info) {
@@ -451,11 +453,13 @@ __global__ void __launch_bounds__(kBwdThreads) blend_bwd_kernel(
   __shared__ uint8_t s_list[kBwdThreads / 32][kBatch];
   float* gacc = smem + 2 * kBatch * RF;  // [kBatch][GR]
 
-  const int gx = grid_x(W);
-  const int tile = blockIdx.x;
+  const int tile = blockIdx.x;  // global tile (of its view, for a batch)
+  int W, H, gx, ltile;
+  int64_t pbase;
+  tile_view(vt, tile, W, H, gx, ltile, pbase);
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int bx0 = (tile % gx) * kTile + 8 * (w & 1);
-  const int by0 = (tile / gx) * kTile + 8 * (w >> 1);
+  const int bx0 = (ltile % gx) * kTile + 8 * (w & 1);
+  const int by0 = (ltile / gx) * kTile + 8 * (w >> 1);
   uint8_t* my_list = s_list[w];
 
   if (threadIdx.x == 0) s_max_nc = 0;
@@ -480,11 +484,11 @@ __global__ void __launch_bounds__(kBwdThreads) blend_bwd_kernel(
     }
     if (px < W && py < H) {
       const int64_t pix = (int64_t)py * W + px;
-      P[q].T = final_T[pix];
-      P[q].nc = n_contrib[pix];
+      P[q].T = final_T[pbase + pix];
+      P[q].nc = n_contrib[pbase + pix];
 #pragma unroll
       for (int c = 0; c < NC; ++c)
-        if (c < C) P[q].dout[c] = d_out[c * plane + pix];
+        if (c < C) P[q].dout[c] = d_out[C * pbase + c * plane + pix];
     }
     my_nc = max(my_nc, P[q].nc);
   }
@@ -594,33 +598,32 @@ __global__ void unpack_kernel(const float* __restrict__ g, int64_t n, int C,
 // ------------------------------------------------------------- dispatch
 template <int NC>
 static int launch_fwd_nc(const float* records, const int32_t* ids, const int2* ranges, int64_t n,
-                         float bg, int W, int H, int C, float* out, float* fT, int32_t* ncon,
-                         int64_t* info, cudaStream_t s) {
+                         float bg, const ViewTable& vt, int tiles, int C, float* out, float* fT,
+                         int32_t* ncon, int64_t* info, cudaStream_t s) {
   constexpr int RF = rec_floats(NC);
-  const int tiles = grid_x(W) * grid_y(H);
   const size_t smem = 2 * kBatch * RF * sizeof(float);
   auto kern = blend_fwd_kernel<NC, RF>;
   if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
       cudaSuccess)
     return PGB_ERR_CUDA;
-  kern<<<tiles, kBlendThreads, smem, s>>>(records, ids, ranges, n, bg, W, H, C, out, fT, ncon, info);
+  kern<<<tiles, kBlendThreads, smem, s>>>(records, ids, ranges, n, bg, vt, C, out, fT, ncon, info);
   return launch_status();
 }
 
 template <int NC>
 static int launch_bwd_nc(const float* records, const int32_t* ids, const int2* ranges, int64_t n,
-                         float bg, int W, int H, int C, const float* fT, const int32_t* ncon,
-                         const float* dout, float* grec, int64_t* info, cudaStream_t s) {
+                         float bg, const ViewTable& vt, int tiles, int C, const float* fT,
+                         const int32_t* ncon, const float* dout, float* grec, int64_t* info,
+                         cudaStream_t s) {
   constexpr int RF = rec_floats(NC);
   constexpr int GR = grad_floats(NC);
-  const int tiles = grid_x(W) * grid_y(H);
   const size_t smem = (2 * RF + GR) * kBatch * sizeof(float);
   auto kern = blend_bwd_kernel<NC, RF, GR>;
   if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
       cudaSuccess)
     return PGB_ERR_CUDA;
-  kern<<<tiles, kBwdThreads, smem, s>>>(records, ids, ranges, n, bg, W, H, C, fT, ncon, dout,
-                                        grec, info);
+  kern<<<tiles, kBwdThreads, smem, s>>>(records, ids, ranges, n, bg, vt, C, fT, ncon, dout, grec,
+                                        info);
   return launch_status();
 }
 
@@ -651,13 +654,15 @@ int pgb_blend_grad_record_floats(int channels) {
   return grad_floats(nc_bucket(channels));
 }
 
-int pgb_alpha_blending_forward(const float* uv, const float* conic, const float* opacity,
-                               const float* feature, int64_t n, int channels, const int32_t* ids,
-                               int64_t k, const int32_t* tile_range, float bg, int width,
-                               int height, float* records, float* out, float* final_T,
-                               int32_t* n_contrib, int64_t* info, void* stream) {
+}  // extern "C"
+
+static int blend_forward_impl(const float* uv, const float* conic, const float* opacity,
+                              const float* feature, int64_t n, int channels, const int32_t* ids,
+                              int64_t k, const int32_t* tile_range, float bg, const ViewTable& vt,
+                              int tiles, float* records, float* out, float* final_T,
+                              int32_t* n_contrib, int64_t* info, void* stream) {
   const int nc = nc_bucket(channels);
-  if (n < 0 || k < 0 || width <= 0 || height <= 0 || channels < 1 || nc < 0) return PGB_ERR_INVALID;
+  if (n < 0 || k < 0 || tiles <= 0 || channels < 1 || nc < 0) return PGB_ERR_INVALID;
   if (!tile_range || !out || !final_T || !n_contrib || (k > 0 && !ids)) return PGB_ERR_INVALID;
   if (n > 0 && (!uv || !conic || !opacity || !feature || !records)) return PGB_ERR_INVALID;
   cudaStream_t s = as_stream(stream);
@@ -669,7 +674,7 @@ int pgb_alpha_blending_forward(const float* uv, const float* conic, const float*
       pack_kernel<rec_floats(N)><<<stream_grid(n), kStreamThreads, 0, s>>>(uv, conic, opacity,  \
                                                                            feature, n, channels, \
                                                                            records);            \
-    return launch_fwd_nc<N>(records, ids, rg, n, bg, width, height, channels, out, final_T,       \
+    return launch_fwd_nc<N>(records, ids, rg, n, bg, vt, tiles, channels, out, final_T,          \
                             n_contrib, info, s);
     PGB_FOR_NC(PGB_CASE)
 #undef PGB_CASE
@@ -678,14 +683,14 @@ int pgb_alpha_blending_forward(const float* uv, const float* conic, const float*
   }
 }
 
-int pgb_alpha_blending_backward(const float* records, int64_t n, int channels,
-                                const int32_t* ids, int64_t k, const int32_t* tile_range, float bg,
-                                int width, int height, const float* final_T,
-                                const int32_t* n_contrib, const float* d_out, float* grad_records,
-                                float* d_uv, float* d_conic, float* d_opacity, float* d_feature,
-                                int64_t* info, void* stream) {
+static int blend_backward_impl(const float* records, int64_t n, int channels, const int32_t* ids,
+                               int64_t k, const int32_t* tile_range, float bg, const ViewTable& vt,
+                               int tiles, const float* final_T, const int32_t* n_contrib,
+                               const float* d_out, float* grad_records, float* d_uv,
+                               float* d_conic, float* d_opacity, float* d_feature, int64_t* info,
+                               void* stream) {
   const int nc = nc_bucket(channels);
-  if (n < 0 || k < 0 || width <= 0 || height <= 0 || channels < 1 || nc < 0) return PGB_ERR_INVALID;
+  if (n < 0 || k < 0 || tiles <= 0 || channels < 1 || nc < 0) return PGB_ERR_INVALID;
   if (!tile_range || !final_T || !n_contrib || !d_out || (k > 0 && !ids)) return PGB_ERR_INVALID;
   if (n > 0 && (!records || !grad_records || !d_uv || !d_conic || !d_opacity || !d_feature))
     return PGB_ERR_INVALID;
@@ -699,8 +704,8 @@ int pgb_alpha_blending_backward(const float* records, int64_t n, int channels,
   switch (nc) {
 #define PGB_CASE(N)                                                                          \
   case N:                                                                                    \
-    st = launch_bwd_nc<N>(records, ids, rg, n, bg, width, height, channels, final_T,        \
-                          n_contrib, d_out, grad_records, info, s);                          \
+    st = launch_bwd_nc<N>(records, ids, rg, n, bg, vt, tiles, channels, final_T, n_contrib,  \
+                          d_out, grad_records, info, s);                                     \
     break;
     PGB_FOR_NC(PGB_CASE)
 #undef PGB_CASE
@@ -715,6 +720,63 @@ int pgb_alpha_blending_backward(const float* records, int64_t n, int channels,
     unpack_kernel<32><<<stream_grid(n), kStreamThreads, 0, s>>>(grad_records, n, channels, d_uv,
                                                                 d_conic, d_opacity, d_feature);
   return launch_status();
+}
+
+extern "C" {
+
+int pgb_alpha_blending_forward(const float* uv, const float* conic, const float* opacity,
+                               const float* feature, int64_t n, int channels, const int32_t* ids,
+                               int64_t k, const int32_t* tile_range, float bg, int width,
+                               int height, float* records, float* out, float* final_T,
+                               int32_t* n_contrib, int64_t* info, void* stream) {
+  if (width <= 0 || height <= 0) return PGB_ERR_INVALID;
+  return blend_forward_impl(uv, conic, opacity, feature, n, channels, ids, k, tile_range, bg,
+                            single_view(width, height), grid_x(width) * grid_y(height), records,
+                            out, final_T, n_contrib, info, stream);
+}
+
+int pgb_alpha_blending_backward(const float* records, int64_t n, int channels,
+                                const int32_t* ids, int64_t k, const int32_t* tile_range, float bg,
+                                int width, int height, const float* final_T,
+                                const int32_t* n_contrib, const float* d_out, float* grad_records,
+                                float* d_uv, float* d_conic, float* d_opacity, float* d_feature,
+                                int64_t* info, void* stream) {
+  if (width <= 0 || height <= 0) return PGB_ERR_INVALID;
+  return blend_backward_impl(records, n, channels, ids, k, tile_range, bg,
+                             single_view(width, height), grid_x(width) * grid_y(height), final_T,
+                             n_contrib, d_out, grad_records, d_uv, d_conic, d_opacity, d_feature,
+                             info, stream);
+}
+
+int pgb_alpha_blending_forward_views(const float* uv, const float* conic, const float* opacity,
+                                     const float* feature, int64_t n_per_view, int channels,
+                                     const int32_t* ids, int64_t k, const int32_t* tile_range,
+                                     float bg, const int32_t* sizes, int nviews, float* records,
+                                     float* out, float* final_T, int32_t* n_contrib,
+                                     int64_t* info, void* stream) {
+  ViewTable vt;
+  uint32_t T = 0;
+  int64_t pixels = 0;
+  if (!make_views(sizes, nviews, n_per_view, vt, T, pixels)) return PGB_ERR_INVALID;
+  return blend_forward_impl(uv, conic, opacity, feature, n_per_view * nviews, channels, ids, k,
+                            tile_range, bg, vt, (int)T, records, out, final_T, n_contrib, info,
+                            stream);
+}
+
+int pgb_alpha_blending_backward_views(const float* records, int64_t n_per_view, int channels,
+                                      const int32_t* ids, int64_t k, const int32_t* tile_range,
+                                      float bg, const int32_t* sizes, int nviews,
+                                      const float* final_T, const int32_t* n_contrib,
+                                      const float* d_out, float* grad_records, float* d_uv,
+                                      float* d_conic, float* d_opacity, float* d_feature,
+                                      int64_t* info, void* stream) {
+  ViewTable vt;
+  uint32_t T = 0;
+  int64_t pixels = 0;
+  if (!make_views(sizes, nviews, n_per_view, vt, T, pixels)) return PGB_ERR_INVALID;
+  return blend_backward_impl(records, n_per_view * nviews, channels, ids, k, tile_range, bg, vt,
+                             (int)T, final_T, n_contrib, d_out, grad_records, d_uv, d_conic,
+                             d_opacity, d_feature, info, stream);
 }
 
 }  // extern "C"

@@ -45,6 +45,95 @@ __device__ inline void tile_rect(float u, float v, float r, int gx, int gy, int&
   ymax = (int)fminf((float)gy, fmaxf(0.0f, (v + r + c) / t));
 }
 
+// Where the tiles and pixels of a launch live, passed by value in kernel
+// parameters: one image (nviews == 0, size W x H) or a batch of up to
+// kMaxViews views.  In a batch the views own consecutive ranges of one global
+// 16x16 tile index space (view v's first tile is tile_base[v]), per-pixel
+// arrays hold the views one after another (view v's first pixel is
+// pixel_base[v]), and element g of the per-Gaussian arrays belongs to view
+// g / n_per_view.
+constexpr int kMaxViews = 64;
+
+struct ViewTable {
+  int nviews;
+  int W, H;
+  int64_t n_per_view;
+  int32_t w[kMaxViews], h[kMaxViews], tile_base[kMaxViews];
+  int64_t pixel_base[kMaxViews];
+};
+
+inline ViewTable single_view(int W, int H) {
+  ViewTable vt{};
+  vt.nviews = 0;
+  vt.W = W;
+  vt.H = H;
+  return vt;
+}
+
+// A batch from host (width, height) pairs; fills the bases and returns the
+// total tile and pixel counts, or false when a size is invalid.
+inline bool make_views(const int32_t* sizes, int nviews, int64_t n_per_view, ViewTable& vt,
+                       uint32_t& tiles, int64_t& pixels) {
+  if (!sizes || nviews < 1 || nviews > kMaxViews || n_per_view < 0) return false;
+  vt = ViewTable{};
+  vt.nviews = nviews;
+  vt.n_per_view = n_per_view;
+  uint64_t t = 0;
+  int64_t p = 0;
+  for (int v = 0; v < nviews; ++v) {
+    const int W = sizes[2 * v], H = sizes[2 * v + 1];
+    if (W <= 0 || H <= 0 || grid_x(W) > 65535 || grid_y(H) > 65535) return false;
+    vt.w[v] = W;
+    vt.h[v] = H;
+    vt.tile_base[v] = (int32_t)t;
+    vt.pixel_base[v] = p;
+    t += (uint64_t)grid_x(W) * grid_y(H);
+    p += (int64_t)W * H;
+    if (t > (1u << 24)) return false;
+  }
+  tiles = (uint32_t)t;
+  pixels = p;
+  return true;
+}
+
+// Tile grid and first global tile of the view that owns element g.
+__device__ inline void element_view(const ViewTable& vt, uint32_t g, int& gx, int& gy,
+                                    uint32_t& tile_base) {
+  if (vt.nviews == 0) {
+    gx = grid_x(vt.W);
+    gy = grid_y(vt.H);
+    tile_base = 0;
+    return;
+  }
+  int v = (int)((int64_t)g / vt.n_per_view);
+  v = v < vt.nviews - 1 ? v : vt.nviews - 1;
+  gx = grid_x(vt.w[v]);
+  gy = grid_y(vt.h[v]);
+  tile_base = (uint32_t)vt.tile_base[v];
+}
+
+// The view that owns global tile `tile`: its size, tile grid width, the tile's
+// index within the view and the view's first pixel in per-pixel arrays.
+__device__ inline void tile_view(const ViewTable& vt, int tile, int& W, int& H, int& gx,
+                                 int& local, int64_t& pixel_base) {
+  if (vt.nviews == 0) {
+    W = vt.W;
+    H = vt.H;
+    gx = grid_x(W);
+    local = tile;
+    pixel_base = 0;
+    return;
+  }
+  int v = 0;
+  for (int i = 1; i < vt.nviews; ++i)
+    if (vt.tile_base[i] <= tile) v = i;
+  W = vt.w[v];
+  H = vt.h[v];
+  gx = grid_x(W);
+  local = tile - vt.tile_base[v];
+  pixel_base = vt.pixel_base[v];
+}
+
 __device__ inline float warp_sum(float v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);

@@ -295,7 +295,7 @@ constexpr int kEmitThreads = 256;
 
 __global__ void __launch_bounds__(kSortThreads) scan_rect_kernel(
     const uint32_t* __restrict__ order, int64_t n, const int32_t* __restrict__ tiles,
-    const int32_t* __restrict__ radius, const float* __restrict__ uv, int W, int H, int64_t K,
+    const int32_t* __restrict__ radius, const float* __restrict__ uv, ViewTable vt, int64_t K,
     uint32_t* __restrict__ status, uint32_t* __restrict__ part_counter,
     uint32_t* __restrict__ offs, uint2* __restrict__ rect, uint32_t* __restrict__ chunk_first,
     int64_t* __restrict__ info) {
@@ -305,7 +305,6 @@ __global__ void __launch_bounds__(kSortThreads) scan_rect_kernel(
   __syncthreads();
   const int part = (int)s_part;
   const int64_t base = (int64_t)part * kScanPart + (int64_t)threadIdx.x * kScanItems;
-  const int gx = grid_x(W), gy = grid_y(H);
 
   uint32_t cnt[kScanItems];
   uint2 rc[kScanItems];
@@ -322,6 +321,9 @@ __global__ void __launch_bounds__(kSortThreads) scan_rect_kernel(
         cnt[it] = (uint32_t)max(tiles[g], 0);
         const float2 p = reinterpret_cast<const float2*>(uv)[g];
         int x0, x1, y0, y1;
+        int gx, gy;
+        uint32_t tile_base;
+        element_view(vt, g, gx, gy, tile_base);
         tile_rect(p.x, p.y, (float)r, gx, gy, x0, x1, y0, y1);
         if ((int64_t)(x1 - x0) * (y1 - y0) != (int64_t)cnt[it]) set_error(info, PGB_ERR_MISMATCH);
         rc[it] = make_uint2((uint32_t)x0 | ((uint32_t)y0 << 16),
@@ -382,7 +384,7 @@ constexpr int kEmitPer = kEmitChunk / kEmitThreads;  // 4
 __global__ void __launch_bounds__(kEmitThreads) emit_kernel(
     const uint32_t* __restrict__ order, const uint32_t* __restrict__ offs,
     const uint2* __restrict__ rect, const uint32_t* __restrict__ chunk_first, int64_t n_sorted,
-    int64_t K, int W, int tile_passes, uint32_t* __restrict__ tkeys, uint32_t* __restrict__ tvals,
+    int64_t K, ViewTable vt, int tile_passes, uint32_t* __restrict__ tkeys, uint32_t* __restrict__ tvals,
     uint32_t* __restrict__ tile_hist, int64_t* __restrict__ info) {
   constexpr int CAP = kEmitChunk + 1;
   __shared__ uint32_t s_off[CAP];
@@ -391,7 +393,6 @@ __global__ void __launch_bounds__(kEmitThreads) emit_kernel(
   __shared__ __align__(16) uint32_t s_key[kEmitChunk];
   __shared__ __align__(16) uint32_t s_val[kEmitChunk];
   __shared__ uint32_t s_hist[kMaxTilePasses][256];
-  const int gx = grid_x(W);
   const int64_t e0 = (int64_t)blockIdx.x * kEmitChunk;
   const int64_t e1 = min(K, e0 + kEmitChunk);
   // owners of this chunk's first entry and of the next chunk's first entry
@@ -434,8 +435,12 @@ __global__ void __launch_bounds__(kEmitThreads) emit_kernel(
       const uint32_t g = staged ? s_g[own] : order[i0 + own];
       const uint32_t jj = (uint32_t)(e - o);
       const uint32_t w = rc.y & 0xFFFFu, h = rc.y >> 16;
-      uint32_t tid = 0;  // a tiles_touched/rectangle mismatch leaves tile 0 (reported)
-      if (w > 0 && jj < w * h) tid = ((rc.x >> 16) + jj / w) * (uint32_t)gx + (rc.x & 0xFFFFu) + jj % w;
+      int gx, gy;
+      uint32_t tile_base;
+      element_view(vt, g, gx, gy, tile_base);
+      uint32_t tid = tile_base;  // a tiles_touched/rectangle mismatch leaves the view's first tile (reported)
+      if (w > 0 && jj < w * h)
+        tid = tile_base + ((rc.x >> 16) + jj / w) * (uint32_t)gx + (rc.x & 0xFFFFu) + jj % w;
       s_key[threadIdx.x * kEmitPer + j] = tid;
       s_val[threadIdx.x * kEmitPer + j] = g;
     }
@@ -606,20 +611,20 @@ int pgb_sort_gaussian_begin(const float* depth, const int32_t* radius,
   return launch_status();
 }
 
-int pgb_sort_gaussian_finish(const float* uv, const int32_t* radius, const int32_t* tiles_touched,
-                             int64_t n, int width, int height, int64_t k, void* scratch_n,
-                             size_t bytes_n, void* scratch_k, size_t bytes_k, int64_t* info,
-                             int32_t* ids_out, int32_t* tile_range_out, void* stream) {
-  if (n < 0 || k < 0 || width <= 0 || height <= 0 || !info || !tile_range_out)
-    return PGB_ERR_INVALID;
+}  // extern "C"
+
+// Phase two for one image or a batch of views (vt), over T global tiles.
+static int sort_finish_impl(const float* uv, const int32_t* radius, const int32_t* tiles_touched,
+                            int64_t n, const ViewTable& vt, uint32_t T, int64_t k, void* scratch_n,
+                            size_t bytes_n, void* scratch_k, size_t bytes_k, int64_t* info,
+                            int32_t* ids_out, int32_t* tile_range_out, void* stream) {
+  if (n < 0 || k < 0 || !info || !tile_range_out) return PGB_ERR_INVALID;
   if (k >= (int64_t)kValMask) return PGB_ERR_OVERFLOW;
   const ScratchN LN = layout_n(n);
   const ScratchK LK = layout_k(k);
   if (!scratch_n || bytes_n < LN.total) return PGB_ERR_INVALID;
   if (k > 0 && (!scratch_k || bytes_k < LK.total || !ids_out)) return PGB_ERR_INVALID;
-  const uint32_t T = (uint32_t)grid_x(width) * (uint32_t)grid_y(height);
-  if (T > (1u << (8 * kMaxTilePasses)) || grid_x(width) > 65535 || grid_y(height) > 65535)
-    return PGB_ERR_INVALID;
+  if (T == 0 || T > (1u << (8 * kMaxTilePasses))) return PGB_ERR_INVALID;
   cudaStream_t s = as_stream(stream);
   if (cudaMemsetAsync(tile_range_out, 0, (size_t)T * 2 * sizeof(int32_t), s) != cudaSuccess)
     return PGB_ERR_CUDA;
@@ -639,11 +644,10 @@ int pgb_sort_gaussian_finish(const float* uv, const int32_t* radius, const int32
   uint2* rect = at<uint2>(scratch_n, LN.rect);
   uint32_t* chunk_first = at<uint32_t>(scratch_k, LK.chunk_first);
   scan_rect_kernel<<<LN.scan_parts, kSortThreads, 0, s>>>(
-      order, n, tiles_touched, radius, uv, width, height, k,
-      at<uint32_t>(scratch_n, LN.scan_status), counters + 4, offs, rect, chunk_first, info);
-  emit_kernel<<<(unsigned)LK.chunks, kEmitThreads, 0, s>>>(order, offs, rect, chunk_first, n, k,
-                                                           width, passes, bufk[0], bufv[0], thist,
-                                                           info);
+      order, n, tiles_touched, radius, uv, vt, k, at<uint32_t>(scratch_n, LN.scan_status),
+      counters + 4, offs, rect, chunk_first, info);
+  emit_kernel<<<(unsigned)LK.chunks, kEmitThreads, 0, s>>>(order, offs, rect, chunk_first, n, k, vt,
+                                                           passes, bufk[0], bufv[0], thist, info);
   int cur = 0;
   for (int p = 0; p < passes; ++p) {
     const bool last = p == passes - 1;
@@ -656,6 +660,32 @@ int pgb_sort_gaussian_finish(const float* uv, const int32_t* radius, const int32
   tile_range_kernel<<<stream_grid(k), kStreamThreads, 0, s>>>(
       bufk[cur], k, T, reinterpret_cast<int2*>(tile_range_out), info);
   return launch_status();
+}
+
+extern "C" {
+
+int pgb_sort_gaussian_finish(const float* uv, const int32_t* radius, const int32_t* tiles_touched,
+                             int64_t n, int width, int height, int64_t k, void* scratch_n,
+                             size_t bytes_n, void* scratch_k, size_t bytes_k, int64_t* info,
+                             int32_t* ids_out, int32_t* tile_range_out, void* stream) {
+  if (width <= 0 || height <= 0 || grid_x(width) > 65535 || grid_y(height) > 65535)
+    return PGB_ERR_INVALID;
+  const uint32_t T = (uint32_t)grid_x(width) * (uint32_t)grid_y(height);
+  return sort_finish_impl(uv, radius, tiles_touched, n, single_view(width, height), T, k, scratch_n,
+                          bytes_n, scratch_k, bytes_k, info, ids_out, tile_range_out, stream);
+}
+
+int pgb_sort_gaussian_finish_views(const float* uv, const int32_t* radius,
+                                   const int32_t* tiles_touched, int64_t n_per_view,
+                                   const int32_t* sizes, int nviews, int64_t k, void* scratch_n,
+                                   size_t bytes_n, void* scratch_k, size_t bytes_k, int64_t* info,
+                                   int32_t* ids_out, int32_t* tile_range_out, void* stream) {
+  ViewTable vt;
+  uint32_t T = 0;
+  int64_t pixels = 0;
+  if (!make_views(sizes, nviews, n_per_view, vt, T, pixels)) return PGB_ERR_INVALID;
+  return sort_finish_impl(uv, radius, tiles_touched, n_per_view * nviews, vt, T, k, scratch_n,
+                          bytes_n, scratch_k, bytes_k, info, ids_out, tile_range_out, stream);
 }
 
 }  // extern "C"

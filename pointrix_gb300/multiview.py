@@ -1,0 +1,144 @@
+"""Batched multi-view rendering: V views, one sort and one blend launch.
+
+``MsplatRender.render_batch`` renders views one after another
+(``pointrix/model/renderer/msplat.py:185-213``): every view pays its own
+sort read-back (a host synchronisation), its own launches and, for small
+views, an under-filled GPU.  Here the per-Gaussian operators run per view
+(their inputs differ per camera) on one stream, and then all V x N
+(view, Gaussian) elements go through one sort -- one read-back for the
+batch -- and one blend launch forward and one backward over the tiles of
+every view.  Within any tile the order is depth, then element id, exactly
+as when the view is rendered alone, so each image equals the per-view
+result.  Differentiable in every Gaussian parameter and camera, like the
+per-view path.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import torch
+
+from . import _lib, ops
+from ._lib import call
+from .ops import _c, _ptr, _status_word, _stream, _timed
+
+TILE = 16
+MAX_VIEWS = 64
+
+
+def _sizes_array(sizes):
+    arr = (C.c_int32 * (2 * len(sizes)))()
+    for i, (W, H) in enumerate(sizes):
+        arr[2 * i], arr[2 * i + 1] = int(W), int(H)
+    return arr
+
+
+def _tiles(W, H):
+    return ((W + TILE - 1) // TILE) * ((H + TILE - 1) // TILE)
+
+
+def sort_views(uv, depth, radius, tiles_touched, sizes, n_per_view):
+    """Tile lists of V views at once: ids [K] (element ids v*N + g) and
+    tile_range [sum of tiles, 2] over the views' concatenated tile space."""
+    W0, H0 = sizes[0]
+    h = ops.sort_gaussian_begin(uv, depth, W0, H0, radius, tiles_touched)
+    K = h.count()
+    dev = uv.device
+    T = sum(_tiles(W, H) for W, H in sizes)
+    _, bk = ops._sort_scratch(h.n, K, W0, H0)
+    scratch_k = torch.empty(max(bk, 1), dtype=torch.uint8, device=dev)
+    ids = torch.empty(K, dtype=torch.int32, device=dev)
+    rng = torch.empty(T, 2, dtype=torch.int32, device=dev)
+    passes = 1 if T <= 256 else (2 if T <= 65536 else 3)
+    with _timed("sort_finish", dev, (2 + passes) if (K and h.n) else 0):
+        call("pgb_sort_gaussian_finish_views", _ptr(h.uv), _ptr(h.radius), _ptr(h.tiles),
+             n_per_view, _sizes_array(sizes), len(sizes), K, _ptr(h.scratch_n), h.bn,
+             _ptr(scratch_k), bk, _ptr(h.info), _ptr(ids) if K else None, _ptr(rng),
+             _stream(dev))
+    ops._defer_check(h.info[1:], "sort_views (tile passes)")
+    return ids, rng
+
+
+class _BlendViews(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, uv, conic, opacity, feature, ids, tile_range, bg, sizes, n_per_view):
+        n, Cc = feature.shape
+        dev = feature.device
+        P = sum(W * H for W, H in sizes)
+        records = torch.empty(n, _lib.lib().pgb_blend_record_floats(Cc), dtype=torch.float32, device=dev)
+        out = torch.empty(Cc * P, dtype=torch.float32, device=dev)
+        final_T = torch.empty(P, dtype=torch.float32, device=dev)
+        ncon = torch.empty(P, dtype=torch.int32, device=dev)
+        sz = _sizes_array(sizes)
+        with _timed("alpha_blending_fwd", dev, 2 if n else 1):
+            call("pgb_alpha_blending_forward_views", _ptr(uv), _ptr(conic), _ptr(opacity),
+                 _ptr(feature), n_per_view, Cc, _ptr(ids), ids.numel(), _ptr(tile_range), float(bg),
+                 sz, len(sizes), _ptr(records), _ptr(out), _ptr(final_T), _ptr(ncon),
+                 _ptr(_status_word(dev)), _stream(dev))
+        ctx.save_for_backward(records, ids, tile_range, final_T, ncon)
+        ctx.cfg = (n, Cc, float(bg), tuple(sizes), n_per_view)
+        return out
+
+    @staticmethod
+    def backward(ctx, d_out):
+        records, ids, tile_range, final_T, ncon = ctx.saved_tensors
+        n, Cc, bg, sizes, n_per_view = ctx.cfg
+        dev = records.device
+        grec = torch.empty(n, _lib.lib().pgb_blend_grad_record_floats(Cc), dtype=torch.float32,
+                           device=dev)
+        d_uv = torch.empty(n, 2, dtype=torch.float32, device=dev)
+        d_conic = torch.empty(n, 3, dtype=torch.float32, device=dev)
+        d_op = torch.empty(n, dtype=torch.float32, device=dev)
+        d_feat = torch.empty(n, Cc, dtype=torch.float32, device=dev)
+        with _timed("alpha_blending_bwd", dev, 2 if n else 0):
+            call("pgb_alpha_blending_backward_views", _ptr(records), n_per_view, Cc, _ptr(ids),
+                 ids.numel(), _ptr(tile_range), bg, _sizes_array(sizes), len(sizes), _ptr(final_T),
+                 _ptr(ncon), _ptr(_c(d_out)), _ptr(grec), _ptr(d_uv), _ptr(d_conic), _ptr(d_op),
+                 _ptr(d_feat), _ptr(_status_word(dev)), _stream(dev))
+        return d_uv, d_conic, d_op, d_feat, None, None, None, None, None
+
+
+def blend_views(uv, conic, opacity, feature, ids, tile_range, bg, sizes, n_per_view):
+    """Blends V views in one launch; returns the list of [C,H,W] images."""
+    n, Cc = feature.shape
+    if len(sizes) < 1 or len(sizes) > MAX_VIEWS:
+        raise ValueError(f"blend_views takes 1..{MAX_VIEWS} views, got {len(sizes)}")
+    if n != n_per_view * len(sizes):
+        raise ValueError("feature rows must be n_per_view * number of views")
+    flat = _BlendViews.apply(_c(uv), _c(conic), _c(opacity.reshape(n)), _c(feature), _c(ids),
+                             _c(tile_range), bg, [tuple(map(int, s)) for s in sizes], int(n_per_view))
+    out, o = [], 0
+    for W, H in sizes:
+        out.append(flat[o:o + Cc * W * H].view(Cc, H, W))
+        o += Cc * W * H
+    return out
+
+
+def render_views(position, scaling, rotation, opacity, shs, cams, bg=0.0, render_depth=True,
+                 extra_features=None, nearest=ops.NEAREST_DEFAULT):
+    """Renders every camera of ``cams`` (objects with W, H, intr [1,4] or [4],
+    extr [4,4] world->camera, center [3]) in one batch.  Features are
+    rgb (+ depth) (+ ``extra_features`` [N,c]) as in ``MsplatRender``.
+    Returns (list of [C,H,W] images, list of per-view uv, list of radius)."""
+    n = position.shape[0]
+    uvs, depths, conics, radii, tiles, feats = [], [], [], [], [], []
+    shc = shs.permute(0, 2, 1)
+    for cam in cams:
+        center = cam.center.reshape(1, 3)
+        d = position - center
+        d = d / d.norm(dim=1, keepdim=True)
+        rgb = (ops.compute_sh(shc, d) + 0.5).clamp(min=0.0)
+        extr = cam.extr[:3, :]
+        uv, depth = ops.project_point(position, cam.intr, extr, cam.W, cam.H, nearest=nearest)
+        vis = depth != 0
+        cov = ops.compute_cov3d(scaling, rotation, vis)
+        conic, radius, nt = ops.ewa_project(position, cov, cam.intr, extr, uv, cam.W, cam.H, vis)
+        f = [rgb] + ([depth] if render_depth else []) + ([extra_features] if extra_features is not None else [])
+        uvs.append(uv); depths.append(depth); conics.append(conic)
+        radii.append(radius); tiles.append(nt); feats.append(torch.cat(f, 1))
+    sizes = [(cam.W, cam.H) for cam in cams]
+    uv_all, conic_all = torch.cat(uvs), torch.cat(conics)
+    ids, rng = sort_views(uv_all, torch.cat(depths), torch.cat(radii), torch.cat(tiles), sizes, n)
+    op_all = opacity.reshape(1, n).expand(len(cams), n).reshape(-1)
+    imgs = blend_views(uv_all, conic_all, op_all, torch.cat(feats), ids, rng, bg, sizes, n)
+    return imgs, uvs, radii
