@@ -133,6 +133,26 @@ int pgb_sort_gaussian_finish(const float* uv, const int32_t* radius, const int32
                              int32_t* ids_out, int32_t* tile_range_out, void* stream);
 
 /* ---------------------------------------------------------------------
+ * pgb_sort_gaussian_finish_capacity -- no counterpart in the reference
+ * (whose sort_gaussian, pointrix/model/renderer/msplat.py:133-135, always
+ * returns K-sized outputs).  Phase two without the host read-back of K:
+ * K is read on the device from info[0] (left there by
+ * pgb_sort_gaussian_begin), and every K-sized buffer (scratch_k from
+ * pgb_sort_scratch_bytes(n, k_capacity, ...), ids_out [k_capacity]) is
+ * sized for the capacity.  Only ids_out[0 .. K) is written; tile_range_out
+ * is the same as with pgb_sort_gaussian_finish.  A K above k_capacity sets
+ * info[1] = PGB_ERR_OVERFLOW and leaves every tile range [0,0].  Nothing on
+ * the host depends on device data, so begin + finish_capacity can be
+ * captured in a CUDA graph.
+ * ------------------------------------------------------------------- */
+int pgb_sort_gaussian_finish_capacity(const float* uv, const int32_t* radius,
+                                      const int32_t* tiles_touched, int64_t n, int width,
+                                      int height, int64_t k_capacity, void* scratch_n,
+                                      size_t bytes_n, void* scratch_k, size_t bytes_k,
+                                      int64_t* info, int32_t* ids_out, int32_t* tile_range_out,
+                                      void* stream);
+
+/* ---------------------------------------------------------------------
  * pgb_sort_gaussian_noalloc -- no counterpart in the reference.
  * The same result as pgb_sort_gaussian_begin + finish, for callers that
  * cannot allocate device memory: code running inside a host application that
@@ -209,6 +229,13 @@ int pgb_sort_gaussian_finish_views(const float* uv, const int32_t* radius,
                                    const int32_t* sizes, int nviews, int64_t k, void* scratch_n,
                                    size_t bytes_n, void* scratch_k, size_t bytes_k, int64_t* info,
                                    int32_t* ids_out, int32_t* tile_range_out, void* stream);
+/* The batch form of pgb_sort_gaussian_finish_capacity (K on the device). */
+int pgb_sort_gaussian_finish_views_capacity(const float* uv, const int32_t* radius,
+                                            const int32_t* tiles_touched, int64_t n_per_view,
+                                            const int32_t* sizes, int nviews, int64_t k_capacity,
+                                            void* scratch_n, size_t bytes_n, void* scratch_k,
+                                            size_t bytes_k, int64_t* info, int32_t* ids_out,
+                                            int32_t* tile_range_out, void* stream);
 int pgb_alpha_blending_forward_views(const float* uv, const float* conic, const float* opacity,
                                      const float* feature, int64_t n_per_view, int channels,
                                      const int32_t* ids, int64_t k, const int32_t* tile_range,

@@ -33,8 +33,12 @@ SIGNATURES = {
     "pgb_sort_scratch_bytes": [i64, i64, i32, i32, C.POINTER(szt), C.POINTER(szt)],
     "pgb_sort_gaussian_begin": [vp, vp, vp, i64, i32, i32, vp, szt, vp, vp],
     "pgb_sort_gaussian_finish": [vp, vp, vp, i64, i32, i32, i64, vp, szt, vp, szt, vp, vp, vp, vp],
+    "pgb_sort_gaussian_finish_capacity": [vp, vp, vp, i64, i32, i32, i64, vp, szt, vp, szt, vp, vp,
+                                          vp, vp],
     "pgb_sort_gaussian_noalloc": [vp, vp, vp, vp, i64, i32, i32, vp, i64, vp, C.POINTER(i64), vp],
     "pgb_sort_gaussian_finish_views": [vp, vp, vp, i64, vp, i32, i64, vp, szt, vp, szt, vp, vp, vp, vp],
+    "pgb_sort_gaussian_finish_views_capacity": [vp, vp, vp, i64, vp, i32, i64, vp, szt, vp, szt, vp,
+                                                vp, vp, vp],
     "pgb_alpha_blending_forward_views": [vp, vp, vp, vp, i64, i32, vp, i64, vp, f32, vp, i32, vp, vp, vp, vp, vp, vp],
     "pgb_alpha_blending_backward_views": [vp, i64, i32, vp, i64, vp, f32, vp, i32, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp],
     "pgb_blend_record_floats": [i32],

@@ -37,9 +37,6 @@ constexpr int kBatch = 256;
 constexpr uint32_t kWaitLimit = 1u << 22;
 
 // ---------------------------------------------------------------- PTX helpers
-__device__ inline uint32_t smem_addr(const void* p) {
-  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
-}
 __device__ inline void mbar_init(uint64_t* bar, uint32_t count) {
   asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count)
                : "memory");
@@ -76,19 +73,6 @@ __device__ inline void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint
           "r"(smem_addr(dst)),
       "l"(src), "r"(bytes), "r"(smem_addr(bar))
       : "memory");
-}
-
-// 16-byte asynchronous global -> shared copy (cp.async, L1 bypass), and the
-// group commit / wait that orders it; the wait is a hardware wait for this
-// thread's own copies, it cannot spin.
-__device__ inline void cp_async16(void* dst, const void* src) {
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_addr(dst)), "l"(src)
-               : "memory");
-}
-__device__ inline void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-template <int N>
-__device__ inline void cp_async_wait() {
-  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
 }
 
 __device__ inline void set_info(int64_t* info, int code) {

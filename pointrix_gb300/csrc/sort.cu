@@ -13,37 +13,46 @@
 //      and sums tiles_touched into K;
 //   2. four onesweep passes sort the N Gaussians by depth (stable, so equal
 //      depths stay in id order);
-//   3. scan_rect: a single-pass decoupled-look-back scan of tiles_touched in
-//      depth order gives each Gaussian its output offset and tile rectangle;
-//      emit then writes the (tile id, Gaussian id) pairs chunk by chunk of
-//      the output (load-balanced however unevenly the tiles are spread over
+//   3. rect: each Gaussian's tile rectangle and entry count (coalesced, in
+//      id order); scan_rect: a single-pass decoupled-look-back scan of the
+//      counts in depth order gives each Gaussian its output offset; emit
+//      then writes the (tile id, Gaussian id) pairs chunk by chunk of the
+//      output (load-balanced however unevenly the tiles are spread over
 //      Gaussians) and accumulates the tile digit histograms;
-//   4. ceil(log2(T)/8) stable onesweep passes (one for T <= 256, two up to
-//      65,536 tiles) sort the pairs by tile id;
-//   5. a range pass marks each tile's [start, end).
+//   4. one stable onesweep pass for T <= 256 tiles, two 8-bit passes up to
+//      65,536 tiles, two 9-bit passes up to 2^18 (batches of views), else
+//      three, sort the pairs by tile id; the last pass writes only the ids
+//      and records each tile's [start, end) as it goes;
+//   5. tiles that no entry reached get [0, 0).
 // A stable sort by tile of a depth-ordered sequence is exactly the order of
 // the 64-bit key sort, with K * 16 bytes of traffic per tile pass instead of
 // K * 24 per 64-bit pass.
 //
-// Onesweep pass: each CTA takes the next 4096-key partition from an atomic
-// counter, ranks its keys stably (warp match_any + per-warp histograms),
+// Onesweep pass: each CTA takes the next 6144-key partition from an atomic
+// counter, ranks its keys stably (warp ballots + per-warp histograms),
 // publishes per-digit counts, resolves its global per-digit offset by
 // decoupled look-back over earlier partitions, stages the keys in shared
 // memory in digit order and writes them out in runs.  A CTA only waits on
 // partitions handed out before its own, which are resident or done, and
 // every wait is bounded: past the limit the CTA records PGB_ERR_TIMEOUT in
 // the info word and carries on, so a fault can never hang the GPU.
+//
+// Phase two can also run without the host knowing K (capacity mode): the
+// K-sized grids cover a capacity, and every kernel reads K from the info
+// word that phase one left on the device.
+#include <algorithm>
+
 #include "pgb_common.cuh"
 
 namespace pgb {
 
 constexpr int kSortThreads = 256;
-constexpr int kSortItems = 16;
-constexpr int kPartKeys = kSortThreads * kSortItems;  // 4096
+constexpr int kPartKeys = 6144;  // keys per onesweep partition
 constexpr int kScanItems = 8;
 constexpr int kScanPart = kSortThreads * kScanItems;  // 2048
 constexpr int kDepthPasses = 4;
 constexpr int kMaxTilePasses = 3;
+constexpr int kTileHistWords = 1024;  // 3 passes x 256 digits or 2 x 512
 constexpr uint32_t kFlagAgg = 1u << 30;
 constexpr uint32_t kFlagInc = 2u << 30;
 constexpr uint32_t kValMask = (1u << 30) - 1;
@@ -165,171 +174,275 @@ __global__ void __launch_bounds__(kSortThreads) sort_prepare_kernel(
 }
 
 // ---------------------------------------------------------------------------
-// 2/4. one stable LSD onesweep pass over 8 bits starting at `shift`
+// 2/4. one stable LSD onesweep pass over RB bits starting at `shift`
 //
-// 512 threads x 8 keys = one 4096-key partition per CTA; the first 256
-// threads also act as the 256 digits for the cross-warp prefix, the status
-// publication and the look-back.
+// A partition is NT threads x IT keys (6144).  Keys are ranked in registers
+// (warp-striped: key it of a lane is element it * 32 + lane of its warp's
+// slice, so warp order = element order and ranks are stable); the
+// partition's values travel global -> shared by cp.async meanwhile, so a
+// thread holds only its keys and ranks.  Within a warp equal digits are found
+// with RB ballots, one per digit bit.  The first R threads also act as the R
+// digits for the cross-warp prefix, the status publication and the
+// look-back, which runs while the other warps stage the keys in digit order.
+//
+// `n_dev` (optional) holds the element count on the device -- the tile
+// passes of a capacity-sized sort, whose grid covers the capacity `cap` --
+// and partitions past that count return at once.  Without KEYS_OUT the keys
+// are not written (the last pass).  With RANGES the pass is the last tile
+// pass and also records each tile's [start, end): in the output every key
+// run is consecutive, so a staged key whose predecessor in shared memory
+// differs may start its tile's run (atomicMin of its position) and one whose
+// successor differs may end it (atomicMax); the table starts at (INT_MAX, 0)
+// and untouched tiles become (0, 0) afterwards.
 // ---------------------------------------------------------------------------
-constexpr int kOsThreads = 512;
-constexpr int kOsItems = kPartKeys / kOsThreads;  // 8
-constexpr int kOsWarps = kOsThreads / 32;
-constexpr size_t kOsSmem = (size_t)kOsWarps * 256 * 4 + 2 * (size_t)kPartKeys * 4;
+template <int RB>
+struct OsCfg;
+template <>
+struct OsCfg<8> {
+  static constexpr int NT = 384, IT = 16;
+};
+template <>
+struct OsCfg<9> {
+  static constexpr int NT = 512, IT = 12;
+};
 
-__global__ void __launch_bounds__(kOsThreads) onesweep_kernel(
+template <int RB>
+struct Os {
+  static constexpr int NT = OsCfg<RB>::NT, IT = OsCfg<RB>::IT, NW = NT / 32;
+  static constexpr int PART = NT * IT;
+  static constexpr int R = 1 << RB;
+  static constexpr size_t SMEM = ((size_t)NW * R + 3 * (size_t)PART) * sizeof(uint32_t);
+  static_assert(PART == kPartKeys, "one partition size for every digit width");
+  static_assert(NT >= R, "one thread per digit");
+};
+
+// Element count of a pass: the host value, or the device count when it
+// fits the capacity (a count past the capacity is reported by scan_rect and
+// makes every pass empty).
+__device__ inline int64_t pass_count(const int64_t* n_dev, int64_t cap) {
+  if (!n_dev) return cap;
+  const int64_t k = *n_dev;
+  return (k >= 0 && k <= cap) ? k : 0;
+}
+
+// Lanes of the warp whose RB-bit digit equals this lane's (among `valid` lanes).
+template <int RB>
+__device__ inline uint32_t match_digit(uint32_t d, bool valid) {
+  uint32_t peers = __ballot_sync(0xffffffffu, valid);
+#pragma unroll
+  for (int b = 0; b < RB; ++b) {
+    const bool bit = (d >> b) & 1u;
+    const uint32_t bb = __ballot_sync(0xffffffffu, bit);
+    peers &= bit ? bb : ~bb;
+  }
+  return peers;
+}
+
+template <int RB, bool KEYS_OUT, bool RANGES>
+__global__ void __launch_bounds__(Os<RB>::NT, 2) onesweep_kernel(
     const uint32_t* __restrict__ keys_in, const uint32_t* __restrict__ vals_in,
-    uint32_t* __restrict__ keys_out, uint32_t* __restrict__ vals_out, int64_t n, int shift,
-    const uint32_t* __restrict__ pass_hist, uint32_t* __restrict__ status,
-    uint32_t* __restrict__ part_counter, int64_t* __restrict__ info) {
+    uint32_t* __restrict__ keys_out, uint32_t* __restrict__ vals_out, int64_t cap,
+    const int64_t* __restrict__ n_dev, int shift, const uint32_t* __restrict__ pass_hist,
+    uint32_t* __restrict__ status, uint32_t* __restrict__ part_counter, int2* __restrict__ range,
+    uint32_t T, int64_t* __restrict__ info) {
+  using P = Os<RB>;
+  constexpr int NT = P::NT, IT = P::IT, NW = P::NW, PART = P::PART, R = P::R;
   extern __shared__ __align__(16) uint32_t os_smem[];
-  uint32_t (*warp_hist)[256] = reinterpret_cast<uint32_t (*)[256]>(os_smem);
-  uint32_t* s_keys = os_smem + kOsWarps * 256;
-  uint32_t* s_vals = s_keys + kPartKeys;
-  __shared__ uint32_t s_block_excl[256];
-  __shared__ uint32_t s_global_base[256];
-  __shared__ uint32_t s_warp_tot[kOsWarps];
+  uint32_t* warp_hist = os_smem;       // [NW][R]: per-warp counts, then exclusive offsets
+  uint32_t* s_vin = os_smem + NW * R;  // the partition's values in input order
+  uint32_t* s_keys = s_vin + PART;     // keys in digit order
+  uint32_t* s_vals = s_keys + PART;    // values in digit order
+  __shared__ uint32_t s_block_excl[R];
+  __shared__ uint32_t s_global_base[R];
+  __shared__ uint32_t s_warp_tot[NW];
   __shared__ uint32_t s_part;
 
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  if (threadIdx.x == 0) s_part = atomicAdd(part_counter, 1u);
-  for (int i = lane; i < 256; i += 32) warp_hist[warp][i] = 0;
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+  const int64_t n = pass_count(n_dev, cap);
+  if (t == 0) s_part = atomicAdd(part_counter, 1u);
+  for (int i = t; i < NW * R; i += NT) warp_hist[i] = 0;
   __syncthreads();
   const int part = (int)s_part;
-  const int64_t base = (int64_t)part * kPartKeys + (int64_t)warp * (32 * kOsItems);
+  const int64_t pbase = (int64_t)part * PART;
+  if (pbase >= n) return;  // whole CTA: past the element count
+  const int64_t rem = n - pbase;
+  const int cnt = rem < (int64_t)PART ? (int)rem : PART;
+  if (cnt == PART) {
+    for (int q = t; q < PART / 4; q += NT) cp_async16(s_vin + 4 * q, vals_in + pbase + 4 * q);
+    cp_async_commit();
+  } else {
+    for (int q = t; q < cnt; q += NT) s_vin[q] = vals_in[pbase + q];
+  }
 
-  uint32_t key[kOsItems], val[kOsItems], rank[kOsItems];
+  const int wofs = warp * 32 * IT;
+  uint32_t key[IT], rank[IT];
   const uint32_t lt = lanemask_lt();
 #pragma unroll
-  for (int it = 0; it < kOsItems; ++it) {
-    const int64_t e = base + it * 32 + lane;
-    const bool valid = e < n;
-    key[it] = valid ? keys_in[e] : 0u;
-    val[it] = valid ? vals_in[e] : 0u;
+  for (int it = 0; it < IT; ++it) {
+    const int j = wofs + it * 32 + lane;
+    key[it] = j < cnt ? keys_in[pbase + j] : 0u;
   }
 #pragma unroll
-  for (int it = 0; it < kOsItems; ++it) {
-    const bool valid = base + it * 32 + lane < n;
-    const uint32_t d = (key[it] >> shift) & 0xFFu;  // 0 for invalid lanes
-    const uint32_t peers = __match_any_sync(0xffffffffu, valid ? d : 256u);
-    const uint32_t old = warp_hist[warp][d];
+  for (int it = 0; it < IT; ++it) {
+    const bool valid = wofs + it * 32 + lane < cnt;
+    const uint32_t d = (key[it] >> shift) & (R - 1);
+    const uint32_t peers = match_digit<RB>(d, valid);
+    const uint32_t old = warp_hist[warp * R + d];
     rank[it] = old + __popc(peers & lt);
     __syncwarp();
-    if (valid && (peers & lt) == 0) warp_hist[warp][d] = old + __popc(peers);
+    if (valid && (peers & lt) == 0) warp_hist[warp * R + d] = old + __popc(peers);
     __syncwarp();
   }
   __syncthreads();
 
-  // Per digit (threads 0..255): exclusive offsets across warps, partition
-  // count, status publication, look-back.
-  const int t = threadIdx.x;
-  const bool is_digit = t < 256;
+  // Per digit: exclusive offsets across warps, partition count, aggregate
+  // publication; then the digit's global start and its local start.
   uint32_t count = 0;
-  if (is_digit) {
-#pragma unroll
-    for (int w = 0; w < kOsWarps; ++w) {
-      const uint32_t c = warp_hist[w][t];
-      warp_hist[w][t] = count;
+  if (t < R) {
+#pragma unroll 4
+    for (int w = 0; w < NW; ++w) {
+      const uint32_t c = warp_hist[w * R + t];
+      warp_hist[w * R + t] = count;
       count += c;
     }
-    uint32_t* my_status = status + (size_t)part * 256 + t;
-    st_volatile(my_status, (part == 0 ? kFlagInc : kFlagAgg) | count);
+    st_volatile(status + (size_t)part * R + t, (part == 0 ? kFlagInc : kFlagAgg) | count);
   }
-  uint32_t unused;
+  uint32_t unused, local_total;
   const uint32_t digit_start =
-      block_excl_scan<kOsThreads>(is_digit ? pass_hist[t] : 0u, unused, s_warp_tot);
-  if (is_digit) {
+      block_excl_scan<NT>(t < R ? pass_hist[t] : 0u, unused, s_warp_tot);
+  const uint32_t bex = block_excl_scan<NT>(t < R ? count : 0u, local_total, s_warp_tot);
+  if (t < R) s_block_excl[t] = bex;
+  if (cnt == PART) cp_async_wait<0>();
+  __syncthreads();
+
+  // Stage in digit order; the digit threads resolve the global bases.
+#pragma unroll
+  for (int it = 0; it < IT; ++it) {
+    const int j = wofs + it * 32 + lane;
+    if (j < cnt) {
+      const uint32_t d = (key[it] >> shift) & (R - 1);
+      const uint32_t lp = s_block_excl[d] + warp_hist[warp * R + d] + rank[it];
+      s_keys[lp] = key[it];
+      s_vals[lp] = s_vin[j];
+    }
+  }
+  if (t < R) {
     uint32_t prior = 0;
     if (part > 0) {
-      prior = look_back(status + t, part, 256, info);
-      st_volatile(status + (size_t)part * 256 + t, kFlagInc | ((prior + count) & kValMask));
+      prior = look_back(status + t, part, R, info);
+      st_volatile(status + (size_t)part * R + t, kFlagInc | ((prior + count) & kValMask));
     }
     s_global_base[t] = digit_start + prior;
   }
-  uint32_t local_total;
-  const uint32_t bex = block_excl_scan<kOsThreads>(is_digit ? count : 0u, local_total, s_warp_tot);
-  if (is_digit) s_block_excl[t] = bex;
   __syncthreads();
 
-  // Stage in digit order.
-#pragma unroll
-  for (int it = 0; it < kOsItems; ++it) {
-    const int64_t e = base + it * 32 + lane;
-    if (e < n) {
-      const uint32_t d = (key[it] >> shift) & 0xFFu;
-      const uint32_t lp = s_block_excl[d] + warp_hist[warp][d] + rank[it];
-      s_keys[lp] = key[it];
-      s_vals[lp] = val[it];
-    }
-  }
-  __syncthreads();
-  for (uint32_t j = threadIdx.x; j < local_total; j += kOsThreads) {
+  for (int j = t; j < cnt; j += NT) {
     const uint32_t k = s_keys[j];
-    const uint32_t d = (k >> shift) & 0xFFu;
-    const uint32_t dst = s_global_base[d] + (j - s_block_excl[d]);
+    const uint32_t d = (k >> shift) & (R - 1);
+    const uint32_t dst = s_global_base[d] + (uint32_t)(j - (int)s_block_excl[d]);
     if ((int64_t)dst >= n) {  // only if the histogram disagrees with the keys
       set_error(info, PGB_ERR_OVERFLOW);
       continue;
     }
-    keys_out[dst] = k;
+    if (KEYS_OUT) keys_out[dst] = k;
     vals_out[dst] = s_vals[j];
+    if (RANGES) {
+      if (k >= T) {
+        set_error(info, PGB_ERR_OVERFLOW);
+        continue;
+      }
+      if (j == 0 || s_keys[j - 1] != k) atomicMin(&range[k].x, (int)dst);
+      if (j + 1 == cnt || s_keys[j + 1] != k) atomicMax(&range[k].y, (int)dst + 1);
+    }
   }
 }
 
-static int onesweep_attr() {
-  return cudaFuncSetAttribute(onesweep_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              (int)kOsSmem) == cudaSuccess
-             ? PGB_OK
-             : PGB_ERR_CUDA;
+// One pass: digit width, whether keys are written, whether ranges are made.
+template <int RB, bool KEYS_OUT, bool RANGES>
+static int launch_onesweep(int parts, cudaStream_t s, const uint32_t* ki, const uint32_t* vi,
+                           uint32_t* ko, uint32_t* vo, int64_t cap, const int64_t* n_dev,
+                           int shift, const uint32_t* hist, uint32_t* status, uint32_t* counter,
+                           int2* range, uint32_t T, int64_t* info) {
+  using P = Os<RB>;
+  auto kern = onesweep_kernel<RB, KEYS_OUT, RANGES>;
+  // the attribute is set on every call: the call is cheap, allowed while a
+  // stream is being captured, and per device
+  if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)P::SMEM) !=
+      cudaSuccess)
+    return PGB_ERR_CUDA;
+  kern<<<parts, P::NT, P::SMEM, s>>>(ki, vi, ko, vo, cap, n_dev, shift, hist, status, counter,
+                                     range, T, info);
+  return PGB_OK;
 }
 
 // ---------------------------------------------------------------------------
-// 3a. scan of tiles_touched in depth order
+// 3a. tile rectangles in Gaussian order (coalesced)
+//
+// rect[g] = (first tile, w | h << 16, row stride gx, count): the global id
+// of the rectangle's top-left tile (the view's first tile added), its size
+// in tiles, the tile-grid width of g's view, and the number of entries g
+// emits (tiles_touched when radius > 0, else 0).  A count that disagrees
+// with the rectangle is reported as PGB_ERR_MISMATCH.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kStreamThreads) rect_kernel(
+    const float* __restrict__ uv, const int32_t* __restrict__ radius,
+    const int32_t* __restrict__ tiles, int64_t n, ViewTable vt, uint4* __restrict__ rect,
+    int64_t* __restrict__ info) {
+  for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < n;
+       g += (int64_t)gridDim.x * blockDim.x) {
+    const int r = radius[g];
+    uint4 out = make_uint4(0u, 0u, 0u, 0u);
+    if (r > 0) {
+      const float2 p = reinterpret_cast<const float2*>(uv)[g];
+      int gx, gy, x0, x1, y0, y1;
+      uint32_t tile_base;
+      element_view(vt, (uint32_t)g, gx, gy, tile_base);
+      tile_rect(p.x, p.y, (float)r, gx, gy, x0, x1, y0, y1);
+      const uint32_t cnt = (uint32_t)max(tiles[g], 0);
+      if ((int64_t)(x1 - x0) * (y1 - y0) != (int64_t)cnt) set_error(info, PGB_ERR_MISMATCH);
+      out = make_uint4(tile_base + (uint32_t)y0 * (uint32_t)gx + (uint32_t)x0,
+                       (uint32_t)(x1 - x0) | ((uint32_t)(y1 - y0) << 16), (uint32_t)gx, cnt);
+    }
+    rect[g] = out;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// 3b. scan of the entry counts in depth order
 //
 // For depth-sorted position i (Gaussian g = order[i]) writes its output
-// offset offs[i], its tile rectangle rect[i] = (x0 | y0 << 16, w | h << 16),
-// and, for every emission chunk boundary b * kEmitChunk that falls inside
-// [offs[i], offs[i] + count), chunk_first[b] = i.
+// offset offs[i] and, for every emission chunk boundary b * kEmitChunk that
+// falls inside [offs[i], offs[i] + count), chunk_first[b] = i.  K is the
+// host value k_cap, or the device count k_dev (written by the depth phase)
+// bounded by the capacity k_cap.
 // ---------------------------------------------------------------------------
 constexpr int kEmitChunk = 1024;
 constexpr int kEmitThreads = 256;
 
 __global__ void __launch_bounds__(kSortThreads) scan_rect_kernel(
-    const uint32_t* __restrict__ order, int64_t n, const int32_t* __restrict__ tiles,
-    const int32_t* __restrict__ radius, const float* __restrict__ uv, ViewTable vt, int64_t K,
-    uint32_t* __restrict__ status, uint32_t* __restrict__ part_counter,
-    uint32_t* __restrict__ offs, uint2* __restrict__ rect, uint32_t* __restrict__ chunk_first,
-    int64_t* __restrict__ info) {
+    const uint32_t* __restrict__ order, int64_t n, const uint4* __restrict__ rect, int64_t k_cap,
+    const int64_t* __restrict__ k_dev, uint32_t* __restrict__ status,
+    uint32_t* __restrict__ part_counter, uint32_t* __restrict__ offs,
+    uint32_t* __restrict__ chunk_first, int64_t* __restrict__ info) {
   __shared__ uint32_t s_warp_tot[kSortThreads / 32];
   __shared__ uint32_t s_part, s_prior;
+  // a device count past the capacity: reported once, nothing is emitted
+  if (k_dev && (*k_dev < 0 || *k_dev > k_cap)) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) set_error(info, PGB_ERR_OVERFLOW);
+    return;
+  }
+  const int64_t K = pass_count(k_dev, k_cap);
   if (threadIdx.x == 0) s_part = atomicAdd(part_counter, 1u);
   __syncthreads();
   const int part = (int)s_part;
   const int64_t base = (int64_t)part * kScanPart + (int64_t)threadIdx.x * kScanItems;
 
   uint32_t cnt[kScanItems];
-  uint2 rc[kScanItems];
   uint32_t sum = 0;
 #pragma unroll
   for (int it = 0; it < kScanItems; ++it) {
     const int64_t e = base + it;
-    cnt[it] = 0;
-    rc[it] = make_uint2(0u, 0u);
-    if (e < n) {
-      const uint32_t g = order[e];
-      const int r = radius[g];
-      if (r > 0) {
-        cnt[it] = (uint32_t)max(tiles[g], 0);
-        const float2 p = reinterpret_cast<const float2*>(uv)[g];
-        int x0, x1, y0, y1;
-        int gx, gy;
-        uint32_t tile_base;
-        element_view(vt, g, gx, gy, tile_base);
-        tile_rect(p.x, p.y, (float)r, gx, gy, x0, x1, y0, y1);
-        if ((int64_t)(x1 - x0) * (y1 - y0) != (int64_t)cnt[it]) set_error(info, PGB_ERR_MISMATCH);
-        rc[it] = make_uint2((uint32_t)x0 | ((uint32_t)y0 << 16),
-                            (uint32_t)(x1 - x0) | ((uint32_t)(y1 - y0) << 16));
-      }
-    }
+    cnt[it] = e < n ? rect[order[e]].w : 0u;
     sum += cnt[it];
   }
   uint32_t total;
@@ -357,7 +470,6 @@ __global__ void __launch_bounds__(kSortThreads) scan_rect_kernel(
         set_error(info, PGB_ERR_OVERFLOW);
       } else {
         offs[e] = (uint32_t)off;
-        rect[e] = rc[it];
         // chunk boundaries owned by this Gaussian, and the owner of the
         // last entry (stored after the last chunk's)
         for (int64_t b = (off + kEmitChunk - 1) / kEmitChunk; b * kEmitChunk < end; ++b)
@@ -370,129 +482,172 @@ __global__ void __launch_bounds__(kSortThreads) scan_rect_kernel(
 }
 
 // ---------------------------------------------------------------------------
-// 3b. emission of (tile id, Gaussian id) pairs over output chunks
+// 3c. emission of (tile id, Gaussian id) pairs over output chunks
 //
-// CTA b writes entries [b*kEmitChunk, min(K, (b+1)*kEmitChunk)): it stages
-// the offsets, rectangles and ids of the Gaussians that own them in shared
-// memory; each thread takes 8 consecutive entries, finds the owner of the
-// first by binary search and walks forward; the pairs are staged in shared
-// memory and written with 16-byte stores.  Every CTA does the same amount of
-// work however unevenly the tiles are spread over Gaussians.
+// A persistent grid walks the output chunks: for chunk b, entries
+// [b*kEmitChunk, min(K, (b+1)*kEmitChunk)), the CTA stages the offsets, ids
+// and rectangles of the Gaussians that own them in shared memory; each
+// thread takes 4 consecutive entries, finds the owner of the first by binary
+// search and walks forward; the pairs are staged in shared memory and
+// written with 16-byte stores.  Every chunk is the same amount of work
+// however unevenly the tiles are spread over Gaussians.  The tile digit
+// histograms of the chunks a CTA emitted are accumulated in shared memory
+// (one atomic per run of equal digits within a warp) and added to the global
+// histograms once per CTA.  The grid also sets the tile-range table to
+// (INT_MAX, 0) for the last tile pass.
 // ---------------------------------------------------------------------------
 constexpr int kEmitPer = kEmitChunk / kEmitThreads;  // 4
+constexpr int kEmitBlocksPerSM = 6;
 
 __global__ void __launch_bounds__(kEmitThreads) emit_kernel(
     const uint32_t* __restrict__ order, const uint32_t* __restrict__ offs,
-    const uint2* __restrict__ rect, const uint32_t* __restrict__ chunk_first, int64_t n_sorted,
-    int64_t K, ViewTable vt, int tile_passes, uint32_t* __restrict__ tkeys, uint32_t* __restrict__ tvals,
-    uint32_t* __restrict__ tile_hist, int64_t* __restrict__ info) {
+    const uint4* __restrict__ rect, const uint32_t* __restrict__ chunk_first, int64_t n_sorted,
+    int64_t k_cap, const int64_t* __restrict__ k_dev, int tile_passes, int digit_bits,
+    uint32_t* __restrict__ tkeys, uint32_t* __restrict__ tvals, uint32_t* __restrict__ tile_hist,
+    int2* __restrict__ range, uint32_t T, int64_t* __restrict__ info) {
   constexpr int CAP = kEmitChunk + 1;
   __shared__ uint32_t s_off[CAP];
-  __shared__ uint2 s_rect[CAP];
   __shared__ uint32_t s_g[CAP];
+  __shared__ uint32_t s_t0[CAP];  // first tile of the rectangle
+  __shared__ uint32_t s_wg[CAP];  // w | gx << 16
   __shared__ __align__(16) uint32_t s_key[kEmitChunk];
   __shared__ __align__(16) uint32_t s_val[kEmitChunk];
-  __shared__ uint32_t s_hist[kMaxTilePasses][256];
-  const int64_t e0 = (int64_t)blockIdx.x * kEmitChunk;
-  const int64_t e1 = min(K, e0 + kEmitChunk);
-  // owners of this chunk's first entry and of the next chunk's first entry
-  // (for the last chunk: of entry K - 1)
-  const int64_t i0 = chunk_first[blockIdx.x];
-  const int64_t i1 = chunk_first[blockIdx.x + 1];
-  const int64_t m = i1 - i0 + 1;
-  for (int i = threadIdx.x; i < kMaxTilePasses * 256; i += kEmitThreads) (&s_hist[0][0])[i] = 0;
-  const bool ok_range = i0 <= i1 && i1 < n_sorted;
-  if (!ok_range && threadIdx.x == 0) set_error(info, PGB_ERR_OVERFLOW);
-  const bool staged = ok_range && m <= CAP;
-  if (staged) {
-    for (int64_t i = threadIdx.x; i < m; i += kEmitThreads) {
-      s_off[i] = offs[i0 + i];
-      s_rect[i] = rect[i0 + i];
-      s_g[i] = order[i0 + i];
-    }
-  }
-  __syncthreads();
-  const int64_t ebeg = e0 + (int64_t)threadIdx.x * kEmitPer;
-  if (ok_range && ebeg < e1) {
-    auto off_at = [&](int64_t p) -> int64_t { return staged ? s_off[p] : offs[i0 + p]; };
-    // owner of ebeg: the last position p in [0, i1 - i0] with offs <= ebeg
-    int64_t lo = 0, hi = i1 - i0;
-    while (lo < hi) {
-      const int64_t mid = (lo + hi + 1) >> 1;
-      if (off_at(mid) <= ebeg) lo = mid; else hi = mid - 1;
-    }
-    int64_t own = lo;
-    int64_t next_off = own < i1 - i0 ? off_at(own + 1) : INT64_MAX;
-    for (int j = 0; j < kEmitPer; ++j) {
-      const int64_t e = ebeg + j;
-      if (e >= e1) break;
-      while (e >= next_off) {  // walk to the owner of e (skips zero-count Gaussians)
-        ++own;
-        next_off = own < i1 - i0 ? off_at(own + 1) : INT64_MAX;
-      }
-      const uint32_t o = (uint32_t)off_at(own);
-      const uint2 rc = staged ? s_rect[own] : rect[i0 + own];
-      const uint32_t g = staged ? s_g[own] : order[i0 + own];
-      const uint32_t jj = (uint32_t)(e - o);
-      const uint32_t w = rc.y & 0xFFFFu, h = rc.y >> 16;
-      int gx, gy;
-      uint32_t tile_base;
-      element_view(vt, g, gx, gy, tile_base);
-      uint32_t tid = tile_base;  // a tiles_touched/rectangle mismatch leaves the view's first tile (reported)
-      if (w > 0 && jj < w * h)
-        tid = tile_base + ((rc.x >> 16) + jj / w) * (uint32_t)gx + (rc.x & 0xFFFFu) + jj % w;
-      s_key[threadIdx.x * kEmitPer + j] = tid;
-      s_val[threadIdx.x * kEmitPer + j] = g;
-    }
-  }
-  __syncthreads();
-  // coalesced write-out and tile digit histograms (digits of consecutive
-  // keys read by consecutive lanes)
-  const int cnt = ok_range ? (int)(e1 - e0) : 0;
-  if (cnt == kEmitChunk) {
-    for (int q = threadIdx.x; q < kEmitChunk / 4; q += kEmitThreads) {
-      reinterpret_cast<uint4*>(tkeys + e0)[q] = reinterpret_cast<const uint4*>(s_key)[q];
-      reinterpret_cast<uint4*>(tvals + e0)[q] = reinterpret_cast<const uint4*>(s_val)[q];
-    }
-  } else {
-    for (int q = threadIdx.x; q < cnt; q += kEmitThreads) {
-      tkeys[e0 + q] = s_key[q];
-      tvals[e0 + q] = s_val[q];
-    }
-  }
+  __shared__ uint32_t s_hist[kTileHistWords];
+  for (int64_t i = (int64_t)blockIdx.x * kEmitThreads + threadIdx.x; i < T;
+       i += (int64_t)gridDim.x * kEmitThreads)
+    range[i] = make_int2(INT_MAX, 0);
+  const int64_t K = pass_count(k_dev, k_cap);
+  const int64_t nchunks = (K + kEmitChunk - 1) / kEmitChunk;
+  if ((int64_t)blockIdx.x >= nchunks) return;
+  const int R = 1 << digit_bits;
   const uint32_t lane = threadIdx.x & 31;
-  for (int q0 = 0; q0 < kEmitChunk; q0 += kEmitThreads) {
-    const int q = q0 + threadIdx.x;
-    const bool valid = q < cnt;
-    const uint32_t tid = valid ? s_key[q] : 0u;
-    for (int p = 0; p < tile_passes; ++p) {
-      const uint32_t d = (tid >> (8 * p)) & 0xFFu;
-      const uint32_t peers = __match_any_sync(0xffffffffu, valid ? d : 256u + lane);
-      if (valid && (peers & lanemask_lt()) == 0) atomicAdd(&s_hist[p][d], (uint32_t)__popc(peers));
+  for (int i = threadIdx.x; i < tile_passes * R; i += kEmitThreads) s_hist[i] = 0;
+
+  for (int64_t b = blockIdx.x; b < nchunks; b += gridDim.x) {
+    const int64_t e0 = b * kEmitChunk;
+    const int64_t e1 = min(K, e0 + kEmitChunk);
+    // owners of this chunk's first entry and of the next chunk's first entry
+    // (for the last chunk: of entry K - 1)
+    const int64_t i0 = chunk_first[b];
+    const int64_t i1 = chunk_first[b + 1];
+    const int64_t m = i1 - i0 + 1;
+    const bool ok_range = i0 <= i1 && i1 < n_sorted;
+    if (!ok_range && threadIdx.x == 0) set_error(info, PGB_ERR_OVERFLOW);
+    const bool staged = ok_range && m <= CAP;
+    __syncthreads();  // the previous chunk is out of the staging arrays
+    if (staged) {
+      for (int64_t i = threadIdx.x; i < m; i += kEmitThreads) {
+        const uint32_t g = order[i0 + i];
+        const uint4 rc = rect[g];
+        s_off[i] = offs[i0 + i];
+        s_g[i] = g;
+        s_t0[i] = rc.x;
+        s_wg[i] = (rc.y & 0xFFFFu) | (rc.z << 16);
+      }
+    }
+    __syncthreads();
+    const int64_t ebeg = e0 + (int64_t)threadIdx.x * kEmitPer;
+    if (ok_range && ebeg < e1) {
+      auto off_at = [&](int64_t p) -> int64_t { return staged ? s_off[p] : offs[i0 + p]; };
+      // owner of ebeg: the last position p in [0, i1 - i0] with offs <= ebeg
+      int64_t lo = 0, hi = i1 - i0;
+      while (lo < hi) {
+        const int64_t mid = (lo + hi + 1) >> 1;
+        if (off_at(mid) <= ebeg) lo = mid; else hi = mid - 1;
+      }
+      int64_t own = lo;
+      int64_t next_off = own < i1 - i0 ? off_at(own + 1) : INT64_MAX;
+      uint32_t g = 0, t0 = 0, w = 0, gx = 0, row = 0, col = 0;
+      bool fresh = true;
+      for (int j = 0; j < kEmitPer; ++j) {
+        const int64_t e = ebeg + j;
+        if (e >= e1) break;
+        while (e >= next_off) {  // walk to the owner of e (skips zero-count Gaussians)
+          ++own;
+          next_off = own < i1 - i0 ? off_at(own + 1) : INT64_MAX;
+          fresh = true;
+        }
+        if (fresh) {  // first entry of this owner for the thread: position by division
+          uint32_t wg;
+          if (staged) {
+            g = s_g[own];
+            t0 = s_t0[own];
+            wg = s_wg[own];
+          } else {
+            g = order[i0 + own];
+            const uint4 rc = rect[g];
+            t0 = rc.x;
+            wg = (rc.y & 0xFFFFu) | (rc.z << 16);
+          }
+          w = wg & 0xFFFFu;
+          gx = wg >> 16;
+          const uint32_t jj = (uint32_t)(e - off_at(own));
+          row = w ? jj / w : 0u;
+          col = jj - row * w;
+          fresh = false;
+        } else if (++col == w) {  // next entry of the same owner: next column / row
+          col = 0;
+          ++row;
+        }
+        s_key[threadIdx.x * kEmitPer + j] = t0 + row * gx + col;
+        s_val[threadIdx.x * kEmitPer + j] = g;
+      }
+    }
+    __syncthreads();
+    // coalesced write-out; digit histograms, consecutive keys read by
+    // consecutive lanes: a lane whose digit differs from its left neighbour's
+    // heads a run and adds the run's length
+    const int cnt = ok_range ? (int)(e1 - e0) : 0;
+    if (cnt == kEmitChunk) {
+      for (int q = threadIdx.x; q < kEmitChunk / 4; q += kEmitThreads) {
+        reinterpret_cast<uint4*>(tkeys + e0)[q] = reinterpret_cast<const uint4*>(s_key)[q];
+        reinterpret_cast<uint4*>(tvals + e0)[q] = reinterpret_cast<const uint4*>(s_val)[q];
+      }
+    } else {
+      for (int q = threadIdx.x; q < cnt; q += kEmitThreads) {
+        tkeys[e0 + q] = s_key[q];
+        tvals[e0 + q] = s_val[q];
+      }
+    }
+    for (int q0 = 0; q0 < cnt; q0 += kEmitThreads) {
+      const int q = q0 + threadIdx.x;
+      const bool valid = q < cnt;
+      const uint32_t nvalid = __popc(__ballot_sync(0xffffffffu, valid));
+      const uint32_t tid = valid ? s_key[q] : 0u;
+      for (int p = 0; p < tile_passes; ++p) {
+        const uint32_t d = (tid >> (digit_bits * p)) & (uint32_t)(R - 1);
+        const uint32_t left = __shfl_up_sync(0xffffffffu, d, 1);
+        const bool head = valid && (lane == 0 || left != d);
+        const uint32_t heads = __ballot_sync(0xffffffffu, head);
+        if (head) {
+          const uint32_t above = heads & ~((2u << lane) - 1u);
+          const uint32_t next = above ? (uint32_t)(__ffs(above) - 1) : nvalid;
+          atomicAdd(&s_hist[p * R + d], next - lane);
+        }
+      }
     }
   }
   __syncthreads();
-  for (int i = threadIdx.x; i < tile_passes * 256; i += kEmitThreads) {
-    const uint32_t v = (&s_hist[0][0])[i];
+  for (int i = threadIdx.x; i < tile_passes * R; i += kEmitThreads) {
+    const uint32_t v = s_hist[i];
     if (v) atomicAdd(tile_hist + i, v);
   }
 }
 
 // ---------------------------------------------------------------------------
-// 5. tile ranges from the sorted tile keys
+// 5. tiles that no entry reached: (INT_MAX, 0) -> (0, 0)
 // ---------------------------------------------------------------------------
-__global__ void tile_range_kernel(const uint32_t* __restrict__ keys, int64_t K, uint32_t T,
-                                  int2* __restrict__ range, int64_t* __restrict__ info) {
-  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < K;
+__global__ void range_fix_kernel(int2* __restrict__ range, uint32_t T) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < T;
        i += (int64_t)gridDim.x * blockDim.x) {
-    const uint32_t k = keys[i];
-    if (k >= T) {
-      set_error(info, PGB_ERR_OVERFLOW);
-      continue;
-    }
-    if (i == 0 || keys[i - 1] != k) range[k].x = (int)i;
-    if (i == K - 1 || keys[i + 1] != k) range[k].y = (int)(i + 1);
+    if (range[i].x == INT_MAX) range[i] = make_int2(0, 0);
   }
+}
+
+// A device count past a capacity that leaves nothing to launch.
+__global__ void capacity_check_kernel(const int64_t* __restrict__ k_dev, int64_t k_cap,
+                                      int64_t* __restrict__ info) {
+  if (threadIdx.x == 0 && (*k_dev < 0 || *k_dev > k_cap)) set_error(info, PGB_ERR_OVERFLOW);
 }
 
 // ---------------------------------------------------------------------------
@@ -513,7 +668,7 @@ inline ScratchN layout_n(int64_t n) {
   size_t o = 0;
   L.counters = o; o += align256(16 * sizeof(uint32_t));
   L.depth_hist = o; o += align256(kDepthPasses * 256 * sizeof(uint32_t));
-  L.tile_hist = o; o += align256(kMaxTilePasses * 256 * sizeof(uint32_t));
+  L.tile_hist = o; o += align256(kTileHistWords * sizeof(uint32_t));
   L.depth_status = o; o += align256((size_t)kDepthPasses * L.parts * 256 * sizeof(uint32_t));
   L.scan_status = o; o += align256((size_t)L.scan_parts * sizeof(uint32_t));
   L.zero_bytes = o;
@@ -523,7 +678,7 @@ inline ScratchN layout_n(int64_t n) {
   L.dk1 = o; o += nb;
   L.dv1 = o; o += nb;
   L.offs = o; o += nb;
-  L.rect = o; o += align256((size_t)n * sizeof(uint2));
+  L.rect = o; o += align256((size_t)n * sizeof(uint4));
   L.total = o;
   return L;
 }
@@ -543,22 +698,51 @@ inline ScratchK layout_k(int64_t k) {
   L.tv0 = o; o += kb;
   L.tk1 = o; o += kb;
   L.tv1 = o; o += kb;
-  L.status = o; o += align256((size_t)kMaxTilePasses * L.parts * 256 * sizeof(uint32_t));
+  L.status = o; o += align256((size_t)L.parts * kTileHistWords * sizeof(uint32_t));
   L.chunks = (k + kEmitChunk - 1) / kEmitChunk;
   L.chunk_first = o; o += align256((size_t)(L.chunks + 2) * sizeof(uint32_t));
   L.total = o;
   return L;
 }
 
-inline int tile_passes_for(uint32_t T) {
-  int bits = 0;
-  while (bits < 32 && (T - 1) >> bits) ++bits;
-  return bits <= 8 ? 1 : (bits + 7) / 8;
+// Tile passes for T tiles: digit width and count (one 8-bit pass up to 256
+// tiles, two up to 2^16, two 9-bit passes up to 2^18, else three 8-bit).
+struct TilePlan {
+  int passes, bits;
+};
+
+inline TilePlan tile_plan(uint32_t T) {
+  int b = 0;
+  while (b < 32 && ((T - 1) >> b)) ++b;
+  if (b <= 8) return {1, 8};
+  if (b <= 16) return {2, 8};
+  if (b <= 18) return {2, 9};
+  return {3, 8};
 }
 
 template <typename P>
 inline P* at(void* base, size_t off) {
   return reinterpret_cast<P*>(static_cast<char*>(base) + off);
+}
+
+// One tile pass p of `plan` (the last one writes ids and ranges, no keys).
+static int tile_pass(const TilePlan& plan, int p, int parts, cudaStream_t s, const uint32_t* ki,
+                     const uint32_t* vi, uint32_t* ko, uint32_t* vo, int64_t cap,
+                     const int64_t* n_dev, const uint32_t* hist, uint32_t* status,
+                     uint32_t* counter, int2* range, uint32_t T, int64_t* info) {
+  const bool last = p == plan.passes - 1;
+  const int shift = plan.bits * p;
+  const uint32_t* h = hist + (size_t)p * (1u << plan.bits);
+  uint32_t* st = status + (size_t)p * parts * (1u << plan.bits);
+  if (plan.bits == 9)
+    return last ? launch_onesweep<9, false, true>(parts, s, ki, vi, ko, vo, cap, n_dev, shift, h, st,
+                                                  counter, range, T, info)
+                : launch_onesweep<9, true, false>(parts, s, ki, vi, ko, vo, cap, n_dev, shift, h,
+                                                  st, counter, range, T, info);
+  return last ? launch_onesweep<8, false, true>(parts, s, ki, vi, ko, vo, cap, n_dev, shift, h, st,
+                                                counter, range, T, info)
+              : launch_onesweep<8, true, false>(parts, s, ki, vi, ko, vo, cap, n_dev, shift, h, st,
+                                                counter, range, T, info);
 }
 
 }  // namespace pgb
@@ -588,7 +772,6 @@ int pgb_sort_gaussian_begin(const float* depth, const int32_t* radius,
   if (cudaMemsetAsync(info, 0, 2 * sizeof(int64_t), s) != cudaSuccess) return PGB_ERR_CUDA;
   if (cudaMemsetAsync(scratch_n, 0, L.zero_bytes, s) != cudaSuccess) return PGB_ERR_CUDA;
   if (n == 0) return PGB_OK;
-  if (onesweep_attr() != PGB_OK) return PGB_ERR_CUDA;
   uint32_t* counters = at<uint32_t>(scratch_n, L.counters);
   uint32_t* hist = at<uint32_t>(scratch_n, L.depth_hist);
   uint32_t* status = at<uint32_t>(scratch_n, L.depth_status);
@@ -603,21 +786,31 @@ int pgb_sort_gaussian_begin(const float* depth, const int32_t* radius,
     const uint32_t* vi = (p & 1) ? v1 : v0;
     uint32_t* ko = (p & 1) ? k0 : k1;
     uint32_t* vo = (p & 1) ? v0 : v1;
-    onesweep_kernel<<<L.parts, kOsThreads, kOsSmem, s>>>(ki, vi, ko, vo, n, 8 * p, hist + 256 * p,
-                                                         status + (size_t)p * L.parts * 256,
-                                                         counters + p, info);
+    uint32_t* st = status + (size_t)p * L.parts * 256;
+    // the keys of the last pass are not needed: only the order is
+    const int rc = p == kDepthPasses - 1
+                       ? launch_onesweep<8, false, false>(L.parts, s, ki, vi, ko, vo, n, nullptr,
+                                                          8 * p, hist + 256 * p, st, counters + p,
+                                                          nullptr, 0, info)
+                       : launch_onesweep<8, true, false>(L.parts, s, ki, vi, ko, vo, n, nullptr,
+                                                         8 * p, hist + 256 * p, st, counters + p,
+                                                         nullptr, 0, info);
+    if (rc != PGB_OK) return rc;
   }
-  // four passes: the depth order ends in (k0, v0)
+  // four passes: the depth order ends in v0
   return launch_status();
 }
 
 }  // extern "C"
 
 // Phase two for one image or a batch of views (vt), over T global tiles.
+// K is the host value k, or (device_k) the count the depth phase left in
+// info[0], with every K-sized buffer sized for the capacity k.
 static int sort_finish_impl(const float* uv, const int32_t* radius, const int32_t* tiles_touched,
-                            int64_t n, const ViewTable& vt, uint32_t T, int64_t k, void* scratch_n,
-                            size_t bytes_n, void* scratch_k, size_t bytes_k, int64_t* info,
-                            int32_t* ids_out, int32_t* tile_range_out, void* stream) {
+                            int64_t n, const ViewTable& vt, uint32_t T, int64_t k, bool device_k,
+                            void* scratch_n, size_t bytes_n, void* scratch_k, size_t bytes_k,
+                            int64_t* info, int32_t* ids_out, int32_t* tile_range_out,
+                            void* stream) {
   if (n < 0 || k < 0 || !info || !tile_range_out) return PGB_ERR_INVALID;
   if (k >= (int64_t)kValMask) return PGB_ERR_OVERFLOW;
   const ScratchN LN = layout_n(n);
@@ -626,14 +819,19 @@ static int sort_finish_impl(const float* uv, const int32_t* radius, const int32_
   if (k > 0 && (!scratch_k || bytes_k < LK.total || !ids_out)) return PGB_ERR_INVALID;
   if (T == 0 || T > (1u << (8 * kMaxTilePasses))) return PGB_ERR_INVALID;
   cudaStream_t s = as_stream(stream);
-  if (cudaMemsetAsync(tile_range_out, 0, (size_t)T * 2 * sizeof(int32_t), s) != cudaSuccess)
-    return PGB_ERR_CUDA;
-  if (k == 0 || n == 0) return PGB_OK;
-  const int passes = tile_passes_for(T);
+  if (k == 0 || n == 0) {
+    // nothing can be emitted (a device count above 0 overflows the capacity)
+    if (cudaMemsetAsync(tile_range_out, 0, (size_t)T * 2 * sizeof(int32_t), s) != cudaSuccess)
+      return PGB_ERR_CUDA;
+    if (device_k) capacity_check_kernel<<<1, 32, 0, s>>>(info, k, info);
+    return launch_status();
+  }
+  const TilePlan plan = tile_plan(T);
   if (cudaMemsetAsync(at<char>(scratch_k, LK.status), 0,
-                      (size_t)kMaxTilePasses * LK.parts * 256 * sizeof(uint32_t), s) != cudaSuccess)
+                      (size_t)LK.parts * plan.passes * (1u << plan.bits) * sizeof(uint32_t),
+                      s) != cudaSuccess)
     return PGB_ERR_CUDA;
-  if (onesweep_attr() != PGB_OK) return PGB_ERR_CUDA;
+  const int64_t* k_dev = device_k ? info : nullptr;
   uint32_t* counters = at<uint32_t>(scratch_n, LN.counters);
   uint32_t* thist = at<uint32_t>(scratch_n, LN.tile_hist);
   const uint32_t* order = at<uint32_t>(scratch_n, LN.dv0);
@@ -641,24 +839,28 @@ static int sort_finish_impl(const float* uv, const int32_t* radius, const int32_
   uint32_t* bufv[2] = {at<uint32_t>(scratch_k, LK.tv0), at<uint32_t>(scratch_k, LK.tv1)};
   uint32_t* status = at<uint32_t>(scratch_k, LK.status);
   uint32_t* offs = at<uint32_t>(scratch_n, LN.offs);
-  uint2* rect = at<uint2>(scratch_n, LN.rect);
+  uint4* rect = at<uint4>(scratch_n, LN.rect);
   uint32_t* chunk_first = at<uint32_t>(scratch_k, LK.chunk_first);
+  int2* range = reinterpret_cast<int2*>(tile_range_out);
+  rect_kernel<<<stream_grid(n), kStreamThreads, 0, s>>>(uv, radius, tiles_touched, n, vt, rect,
+                                                        info);
   scan_rect_kernel<<<LN.scan_parts, kSortThreads, 0, s>>>(
-      order, n, tiles_touched, radius, uv, vt, k, at<uint32_t>(scratch_n, LN.scan_status),
-      counters + 4, offs, rect, chunk_first, info);
-  emit_kernel<<<(unsigned)LK.chunks, kEmitThreads, 0, s>>>(order, offs, rect, chunk_first, n, k, vt,
-                                                           passes, bufk[0], bufv[0], thist, info);
+      order, n, rect, k, k_dev, at<uint32_t>(scratch_n, LN.scan_status), counters + 4, offs,
+      chunk_first, info);
+  const int64_t emit_grid = std::min<int64_t>(LK.chunks, (int64_t)kNumSMs * kEmitBlocksPerSM);
+  emit_kernel<<<(unsigned)emit_grid, kEmitThreads, 0, s>>>(order, offs, rect, chunk_first, n, k,
+                                                           k_dev, plan.passes, plan.bits, bufk[0],
+                                                           bufv[0], thist, range, T, info);
   int cur = 0;
-  for (int p = 0; p < passes; ++p) {
-    const bool last = p == passes - 1;
+  for (int p = 0; p < plan.passes; ++p) {
+    const bool last = p == plan.passes - 1;
     uint32_t* vo = last ? reinterpret_cast<uint32_t*>(ids_out) : bufv[cur ^ 1];
-    onesweep_kernel<<<LK.parts, kOsThreads, kOsSmem, s>>>(
-        bufk[cur], bufv[cur], bufk[cur ^ 1], vo, k, 8 * p, thist + 256 * p,
-        status + (size_t)p * LK.parts * 256, counters + 5 + p, info);
+    const int rc = tile_pass(plan, p, LK.parts, s, bufk[cur], bufv[cur], bufk[cur ^ 1], vo, k, k_dev,
+                             thist, status, counters + 5 + p, range, T, info);
+    if (rc != PGB_OK) return rc;
     cur ^= 1;
   }
-  tile_range_kernel<<<stream_grid(k), kStreamThreads, 0, s>>>(
-      bufk[cur], k, T, reinterpret_cast<int2*>(tile_range_out), info);
+  range_fix_kernel<<<stream_grid(T), kStreamThreads, 0, s>>>(range, T);
   return launch_status();
 }
 
@@ -671,8 +873,23 @@ int pgb_sort_gaussian_finish(const float* uv, const int32_t* radius, const int32
   if (width <= 0 || height <= 0 || grid_x(width) > 65535 || grid_y(height) > 65535)
     return PGB_ERR_INVALID;
   const uint32_t T = (uint32_t)grid_x(width) * (uint32_t)grid_y(height);
-  return sort_finish_impl(uv, radius, tiles_touched, n, single_view(width, height), T, k, scratch_n,
-                          bytes_n, scratch_k, bytes_k, info, ids_out, tile_range_out, stream);
+  return sort_finish_impl(uv, radius, tiles_touched, n, single_view(width, height), T, k, false,
+                          scratch_n, bytes_n, scratch_k, bytes_k, info, ids_out, tile_range_out,
+                          stream);
+}
+
+int pgb_sort_gaussian_finish_capacity(const float* uv, const int32_t* radius,
+                                      const int32_t* tiles_touched, int64_t n, int width,
+                                      int height, int64_t k_capacity, void* scratch_n,
+                                      size_t bytes_n, void* scratch_k, size_t bytes_k,
+                                      int64_t* info, int32_t* ids_out, int32_t* tile_range_out,
+                                      void* stream) {
+  if (width <= 0 || height <= 0 || grid_x(width) > 65535 || grid_y(height) > 65535)
+    return PGB_ERR_INVALID;
+  const uint32_t T = (uint32_t)grid_x(width) * (uint32_t)grid_y(height);
+  return sort_finish_impl(uv, radius, tiles_touched, n, single_view(width, height), T, k_capacity,
+                          true, scratch_n, bytes_n, scratch_k, bytes_k, info, ids_out,
+                          tile_range_out, stream);
 }
 
 int pgb_sort_gaussian_finish_views(const float* uv, const int32_t* radius,
@@ -684,8 +901,24 @@ int pgb_sort_gaussian_finish_views(const float* uv, const int32_t* radius,
   uint32_t T = 0;
   int64_t pixels = 0;
   if (!make_views(sizes, nviews, n_per_view, vt, T, pixels)) return PGB_ERR_INVALID;
-  return sort_finish_impl(uv, radius, tiles_touched, n_per_view * nviews, vt, T, k, scratch_n,
-                          bytes_n, scratch_k, bytes_k, info, ids_out, tile_range_out, stream);
+  return sort_finish_impl(uv, radius, tiles_touched, n_per_view * nviews, vt, T, k, false,
+                          scratch_n, bytes_n, scratch_k, bytes_k, info, ids_out, tile_range_out,
+                          stream);
+}
+
+int pgb_sort_gaussian_finish_views_capacity(const float* uv, const int32_t* radius,
+                                            const int32_t* tiles_touched, int64_t n_per_view,
+                                            const int32_t* sizes, int nviews, int64_t k_capacity,
+                                            void* scratch_n, size_t bytes_n, void* scratch_k,
+                                            size_t bytes_k, int64_t* info, int32_t* ids_out,
+                                            int32_t* tile_range_out, void* stream) {
+  ViewTable vt;
+  uint32_t T = 0;
+  int64_t pixels = 0;
+  if (!make_views(sizes, nviews, n_per_view, vt, T, pixels)) return PGB_ERR_INVALID;
+  return sort_finish_impl(uv, radius, tiles_touched, n_per_view * nviews, vt, T, k_capacity, true,
+                          scratch_n, bytes_n, scratch_k, bytes_k, info, ids_out, tile_range_out,
+                          stream);
 }
 
 }  // extern "C"

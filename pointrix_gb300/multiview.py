@@ -37,25 +37,32 @@ def _tiles(W, H):
     return ((W + TILE - 1) // TILE) * ((H + TILE - 1) // TILE)
 
 
-def sort_views(uv, depth, radius, tiles_touched, sizes, n_per_view):
+def sort_views(uv, depth, radius, tiles_touched, sizes, n_per_view, capacity=None):
     """Tile lists of V views at once: ids [K] (element ids v*N + g) and
-    tile_range [sum of tiles, 2] over the views' concatenated tile space."""
+    tile_range [sum of tiles, 2] over the views' concatenated tile space.
+    With ``capacity`` K stays on the device (ids has ``capacity`` entries)
+    and nothing synchronises, as in :func:`ops.sort_gaussian`."""
     W0, H0 = sizes[0]
-    h = ops.sort_gaussian_begin(uv, depth, W0, H0, radius, tiles_touched)
-    K = h.count()
+    h = ops.sort_gaussian_begin(uv, depth, W0, H0, radius, tiles_touched,
+                                read_count=capacity is None)
+    K = h.count() if capacity is None else int(capacity)
     dev = uv.device
     T = sum(_tiles(W, H) for W, H in sizes)
     _, bk = ops._sort_scratch(h.n, K, W0, H0)
     scratch_k = torch.empty(max(bk, 1), dtype=torch.uint8, device=dev)
-    ids = torch.empty(K, dtype=torch.int32, device=dev)
+    ids = torch.empty(max(K, 1), dtype=torch.int32, device=dev)[:K]
     rng = torch.empty(T, 2, dtype=torch.int32, device=dev)
-    passes = 1 if T <= 256 else (2 if T <= 65536 else 3)
-    with _timed("sort_finish", dev, (2 + passes) if (K and h.n) else 0):
-        call("pgb_sort_gaussian_finish_views", _ptr(h.uv), _ptr(h.radius), _ptr(h.tiles),
-             n_per_view, _sizes_array(sizes), len(sizes), K, _ptr(h.scratch_n), h.bn,
-             _ptr(scratch_k), bk, _ptr(h.info), _ptr(ids) if K else None, _ptr(rng),
-             _stream(dev))
-    ops._defer_check(h.info[1:], "sort_views (tile passes)")
+    entry = "pgb_sort_gaussian_finish_views" if capacity is None else \
+        "pgb_sort_gaussian_finish_views_capacity"
+    with _timed("sort_finish", dev, (3 + ops._tile_passes(T)) if (K and h.n) else
+                (0 if capacity is None else 1)):
+        call(entry, _ptr(h.uv), _ptr(h.radius), _ptr(h.tiles), n_per_view, _sizes_array(sizes),
+             len(sizes), K, _ptr(h.scratch_n), h.bn, _ptr(scratch_k), bk, _ptr(h.info),
+             _ptr(ids) if K else None, _ptr(rng), _stream(dev))
+    if capacity is None:
+        ops._defer_check(h.info[1:], "sort_views (tile passes)")
+    else:
+        ops._fold_status(h.info[1:2], dev)
     return ids, rng
 
 

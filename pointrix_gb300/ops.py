@@ -127,14 +127,14 @@ class _timed:
         self.name, self.dev, self.kernels = name, dev, kernels
 
     def __enter__(self):
-        if _timing is not None:
+        if _timing is not None and not _capturing():
             self.ev = torch.cuda.Event(enable_timing=True)
             self.ev.record(torch.cuda.current_stream(self.dev))
         return self
 
     def __exit__(self, *exc):
         t = _timing
-        if t is not None and exc[0] is None:
+        if t is not None and exc[0] is None and not _capturing():
             end = torch.cuda.Event(enable_timing=True)
             end.record(torch.cuda.current_stream(self.dev))
             t.events.setdefault(self.name, []).append((self.ev, end))
@@ -161,7 +161,15 @@ def _status_word(device) -> torch.Tensor:
     return t
 
 
+def _capturing() -> bool:
+    """True while the current stream is being captured into a CUDA graph:
+    nothing may then wait on, or read back, device data."""
+    return torch.cuda.is_current_stream_capturing()
+
+
 def _defer_check(word: torch.Tensor, what: str):
+    if _capturing():  # a graph's replays are checked with check_device_status
+        return
     host = torch.empty(word.numel(), dtype=torch.int64, pin_memory=True)
     host.copy_(word, non_blocking=True)
     ev = torch.cuda.Event()
@@ -433,18 +441,53 @@ class SortHandle:
             scratch_k = torch.empty(max(bk, 1), dtype=torch.uint8, device=dev)
             ids = torch.empty(K, dtype=torch.int32, device=dev)
             rng = torch.empty(T, 2, dtype=torch.int32, device=dev)
-            passes = 1 if T <= 256 else (2 if T <= 65536 else 3)
-            with _timed("sort_finish", dev, (2 + passes) if (K and n) else 0):
+            with _timed("sort_finish", dev, (3 + _tile_passes(T)) if (K and n) else 0):
                 call("pgb_sort_gaussian_finish", _ptr(self.uv), _ptr(self.radius), _ptr(self.tiles),
                      n, W, H, K, _ptr(self.scratch_n), self.bn, _ptr(scratch_k), bk, _ptr(self.info),
                      _ptr(ids) if K else None, _ptr(rng), self.stream.cuda_stream)
             _defer_check(self.info[1:], "sort_gaussian (tile passes)")
         return ids, rng
 
+    def finish_capacity(self, capacity: int):
+        """Phase two with K left on the device: ids [capacity] (entries past K
+        unspecified) and tile_range [T,2].  No host read-back, so the whole
+        sort can be captured in a CUDA graph.  A K above ``capacity`` leaves
+        every tile empty and raises at the next :func:`check_device_status`;
+        ``self.info[0]`` holds K on the device."""
+        W, H, n, dev = self.W, self.H, self.n, self.dev
+        cap = int(capacity)
+        if cap < 0:
+            raise ValueError(f"sort capacity must be >= 0, got {cap}")
+        T = ((W + TILE - 1) // TILE) * ((H + TILE - 1) // TILE)
+        with torch.cuda.stream(self.stream):
+            _, bk = _sort_scratch(n, cap, W, H)
+            scratch_k = torch.empty(max(bk, 1), dtype=torch.uint8, device=dev)
+            ids = torch.empty(max(cap, 1), dtype=torch.int32, device=dev)[:cap]
+            rng = torch.empty(T, 2, dtype=torch.int32, device=dev)
+            with _timed("sort_finish", dev, (3 + _tile_passes(T)) if (cap and n) else 1):
+                call("pgb_sort_gaussian_finish_capacity", _ptr(self.uv), _ptr(self.radius),
+                     _ptr(self.tiles), n, W, H, cap, _ptr(self.scratch_n), self.bn, _ptr(scratch_k),
+                     bk, _ptr(self.info), _ptr(ids) if cap else None, _ptr(rng),
+                     self.stream.cuda_stream)
+            _fold_status(self.info[1:2], dev)
+        return ids, rng
 
-def sort_gaussian_begin(uv, depth, W, H, radius, tiles_touched) -> SortHandle:
+
+def _tile_passes(T: int) -> int:
+    """Tile-sort passes of the library for T tiles (launch accounting)."""
+    return 1 if T <= 256 else (2 if T <= (1 << 18) else 3)
+
+
+def _fold_status(word: torch.Tensor, dev):
+    """Merges a per-call device status (int64 [1]) into the device's status
+    word on the stream, for :func:`check_device_status` (no host read)."""
+    w = _status_word(dev)[1:2]
+    torch.maximum(w, word, out=w)
+
+
+def sort_gaussian_begin(uv, depth, W, H, radius, tiles_touched, read_count=True) -> SortHandle:
     """Phase one of :func:`sort_gaussian` without blocking the host: sorts the
-    Gaussians by depth and starts the read-back of K."""
+    Gaussians by depth and (``read_count``) starts the read-back of K."""
     _need(uv, "uv", ndim=2, last=2)
     _need(depth, "depth")
     _need(radius, "radius", dtype=torch.int32)
@@ -465,18 +508,29 @@ def sort_gaussian_begin(uv, depth, W, H, radius, tiles_touched) -> SortHandle:
     with _timed("sort_begin", h.dev, 5 if n else 0):
         call("pgb_sort_gaussian_begin", _ptr(h.depth), _ptr(h.radius), _ptr(h.tiles), n, W, H,
              _ptr(h.scratch_n), h.bn, _ptr(h.info), h.stream.cuda_stream)
-    h.host = torch.empty(2, dtype=torch.int64, pin_memory=True)
-    h.host.copy_(h.info, non_blocking=True)
-    h.event = torch.cuda.Event()
-    h.event.record(h.stream)
+    h.host = h.event = None
+    if read_count:
+        h.host = torch.empty(2, dtype=torch.int64, pin_memory=True)
+        h.host.copy_(h.info, non_blocking=True)
+        h.event = torch.cuda.Event()
+        h.event.record(h.stream)
     return h
 
 
-def sort_gaussian(uv, depth, W, H, radius, tiles_touched):
+def sort_gaussian(uv, depth, W, H, radius, tiles_touched, capacity=None):
     """Tile binning: ``gaussian_ids_sorted`` [K] int32 (ids ordered by tile,
     then depth, then id) and ``tile_range`` [T,2] int32 ([start, end) per
     16x16 tile, [0,0] when empty), K = sum of ``tiles_touched`` over
-    Gaussians with ``radius > 0``.  Reads K back to the host (one sync)."""
+    Gaussians with ``radius > 0``.  Reads K back to the host (one sync).
+
+    ``capacity`` (not in the reference signature): K stays on the device and
+    ``gaussian_ids_sorted`` has ``capacity`` entries, of which the first K are
+    the result (the tile ranges never reach past K); nothing synchronises, so
+    the call can be captured in a CUDA graph.  A K above the capacity leaves
+    every tile empty and raises at the next :func:`check_device_status`."""
+    if capacity is not None:
+        h = sort_gaussian_begin(uv, depth, W, H, radius, tiles_touched, read_count=False)
+        return h.finish_capacity(capacity)
     h = sort_gaussian_begin(uv, depth, W, H, radius, tiles_touched)
     h.count()
     _drain_pending(block=False)
