@@ -11,10 +11,13 @@ are seeded synthetic tensors with the stated distributions.
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
 
 Prints one JSON line.  ``value`` is training iterations per second with the
-scene resident in HBM (device-timed with CUDA events); ``e2e`` is the same
-metric through the ``MsplatRender`` plug-in with the per-step camera and
-target image copied in from pinned host memory and the loss read back every
-step.  ``--impl reference`` times the CPU float64 rendition of the same step
+scene resident in HBM (device-timed with CUDA events) of the step captured
+once as a CUDA graph and replayed (``pointrix_gb300.graph.GraphedStep``: the
+sort keeps K on the device, Adam keeps its step counts there);
+``eager_ms_per_step`` is the same step launched call by call, which also
+gives the per-operator times.  ``e2e`` is the same metric through the same
+calls with the per-step camera and target image copied in from pinned host
+memory and the loss read back every step.  ``--impl reference`` times the CPU float64 rendition of the same step
 (the oracle: the reference operator backend itself is absent) on a bounded
 sample of tiles, on all host cores.
 """
@@ -176,27 +179,41 @@ class CameraParams:
         return [self.q, self.t, self.intr]
 
 
-def training_step(renderer, scene, camp, target, WL, optimizer=None):
-    """Forward, L1 + 0.2 L2 loss, backward, and (when given) the Adam step."""
-    F = torch.nn.functional
-    pos, sc, q, op, shs = scene.activated()
-    normal = WL.normals_from_scene(sc, q)
+def training_step(renderer, scene, camp, target, WL, optimizer=None, fused=True):
+    """Gradients to None, forward, L1 + 0.2 L2 loss, backward, and (when
+    given) the Adam step.  ``fused``: the parameter activations + normal and
+    the loss each as one library kernel (same arithmetic as the torch
+    composition, which ``fused=False`` runs)."""
+    if optimizer is not None:
+        optimizer.zero_grad(set_to_none=True)
+    if fused:
+        from pointrix_gb300 import fused as FU
+        sc, q, op, normal = FU.gaussian_activations(scene.log_scale, scene.quat_raw,
+                                                    scene.opacity_logit)
+        pos, shs = scene.position, scene.shs
+    else:
+        pos, sc, q, op, shs = scene.activated()
+        normal = WL.normals_from_scene(sc, q)
     E, center = camp.pose()
     out = renderer.render_iter(camp.H, camp.W, E, camp.intr, center,
                                pos, op, sc, q, shs, extra_features={"normal": normal})
-    f = out["rendered_features_split"]
-    img = torch.cat([f["rgb"], f["depth"], f["normal"]], 0)
-    loss = F.l1_loss(img, target) + 0.2 * F.mse_loss(img, target)
+    if fused:
+        loss = FU.l1_l2_loss(out["rendered_features"], target, 0.2)
+    else:
+        F = torch.nn.functional
+        f = out["rendered_features_split"]
+        img = torch.cat([f["rgb"], f["depth"], f["normal"]], 0)
+        loss = F.l1_loss(img, target) + 0.2 * F.mse_loss(img, target)
     loss.backward()
     if optimizer is not None:
         optimizer.step()
-        optimizer.zero_grad(set_to_none=True)
     return loss
 
 
-def make_optimizer(scene, camp):
+def make_optimizer(scene, camp, capturable=False):
     """Adam with 3DGS-style per-group learning rates over every Gaussian
-    parameter and the camera pose/intrinsics (one kernel launch per step)."""
+    parameter and the camera pose/intrinsics (one kernel launch per step;
+    two with device-side step counts for graph capture)."""
     groups = [
         {"params": [scene.position], "lr": 1.6e-4},
         {"params": [scene.log_scale], "lr": 5e-3},
@@ -208,7 +225,20 @@ def make_optimizer(scene, camp):
     ]
     from pointrix_gb300.optim import Adam
 
-    return Adam(groups, eps=1e-15)
+    return Adam(groups, eps=1e-15, capturable=capturable)
+
+
+def count_entries(scene, camp, W, H):
+    """K: the (Gaussian, tile) entries of the current scene and camera."""
+    from pointrix_gb300 import ops
+    with torch.no_grad():
+        pos, sc, q, op, shs = scene.activated()
+        E = camp.pose()[0][:3]
+        uv, depth = ops.project_point(pos, camp.intr, E, W, H)
+        vis = depth != 0
+        cov = ops.compute_cov3d(sc, q, vis)
+        conic, radius, tiles = ops.ewa_project(pos, cov, camp.intr, E, uv, W, H, vis)
+        return int(tiles[radius > 0].sum())
 
 
 def zero_grads(tensors):
@@ -482,6 +512,7 @@ def run_gb300(args):
     torch.cuda.set_device(device)
     from pointrix_gb300 import ops
     from pointrix_gb300 import workloads as WL
+    from pointrix_gb300.graph import GraphedStep
     from pointrix_gb300.renderer import MsplatRender
 
     scene_cpu, cam = WL.scene_train_view(1, n=args.n)
@@ -492,33 +523,56 @@ def run_gb300(args):
     target = target_cpu.to(device)
     renderer = MsplatRender(MsplatRender.Config(render_depth=True, max_sh_degree=3), device=device)
     renderer.sh_degree = 3
-    params = [scene.position, scene.log_scale, scene.quat_raw, scene.opacity_logit, scene.shs] + camp.leaves()
-    optimizer = make_optimizer(scene, camp)
+    optimizer = make_optimizer(scene, camp, capturable=True)
     W, H = cam.W, cam.H
     stream = torch.cuda.current_stream(device)
 
-    for _ in range(max(3, args.warmup)):
-        training_step(renderer, scene, camp, target, WL, optimizer)
-    torch.cuda.synchronize(device)
+    def step():
+        return training_step(renderer, scene, camp, target, WL, optimizer)
 
-    # -- device-resident timed region
+    for _ in range(max(3, args.warmup)):
+        step()
+    torch.cuda.synchronize(device)
+    # the sort keeps K on the device from here on: lists sized for a capacity
+    # above the K of this camera, so that no step synchronises with the host
+    renderer.cfg.sort_capacity = int(1.25 * count_entries(scene, camp, W, H)) + 65536
+
+    # -- eager launches (same kernels as the graph): per-operator CUDA-event
+    #    times for the roofline, and the launch count
+    barrier(world)
+    torch.cuda.synchronize(device)
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ops.kernel_timing() as kt:
+        start.record(stream)
+        for _ in range(args.steps):
+            step()
+        end.record(stream)
+        torch.cuda.synchronize(device)
+    eager_ms = max_over_ranks(start.elapsed_time(end) / args.steps, world, device)
+    ops.check_device_status(device)
+
+    # -- the step captured once as a CUDA graph and replayed (device-resident
+    #    inputs): the headline
+    graphed = GraphedStep(step, warmup=2, device=device)
+    for _ in range(max(3, args.warmup)):
+        graphed()
+    torch.cuda.synchronize(device)
     with ClockSampler(device.index) as clocks:
         barrier(world)
         torch.cuda.synchronize(device)
-        start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        with ops.kernel_timing() as kt:
-            start.record(stream)
-            for _ in range(args.steps):
-                training_step(renderer, scene, camp, target, WL, optimizer)
-            end.record(stream)
-            torch.cuda.synchronize(device)
+        start.record(stream)
+        for _ in range(args.steps):
+            graphed()
+        end.record(stream)
+        torch.cuda.synchronize(device)
         barrier(world)
-    ms = start.elapsed_time(end) / args.steps
-    ms = max_over_ranks(ms, world, device)
+    ms = max_over_ranks(start.elapsed_time(end) / args.steps, world, device)
     value = world / (ms / 1e3)
     ops.check_device_status(device)
 
-    # -- end to end through the plug-in, host buffers
+    # -- end to end through the same public calls, host buffers: each step
+    #    copies the camera and target in from pinned memory, replays the
+    #    step and reads the loss back
     target_host = target_cpu.pin_memory()
     cam_host = [t.detach().cpu().pin_memory() for t in camp.leaves()]
     loss_host = torch.empty((), dtype=torch.float32).pin_memory()
@@ -531,25 +585,19 @@ def run_gb300(args):
             target.copy_(target_host, non_blocking=True)
             for dst, src in zip(camp.leaves(), cam_host):
                 dst.copy_(src, non_blocking=True)
-        loss = training_step(renderer, scene, camp, target, WL, optimizer)
+        loss = graphed()
         loss_host.copy_(loss.detach(), non_blocking=True)
         stream.synchronize()
     e2e_s = (time.perf_counter() - t0) / args.steps
     e2e_s = max_over_ranks(e2e_s, world, device)
     barrier(world)
+    ops.check_device_status(device)
 
     # -- dominant kernel and its roofline (live CUDA-event durations)
     per_op = {name: statistics.mean(kt.ms(name)) for name in kt.names()}
     calls = {name: len(kt.ms(name)) // args.steps for name in kt.names()}
     dom = max(per_op, key=lambda k: per_op[k] * calls[k])
-    with torch.no_grad():
-        pos, sc, q, op, shs = scene.activated()
-        E = camp.pose()[0][:3]
-        uv, depth = ops.project_point(pos, camp.intr, E, W, H)
-        vis = depth != 0
-        cov = ops.compute_cov3d(sc, q, vis)
-        conic, radius, tiles = ops.ewa_project(pos, cov, camp.intr, E, uv, W, H, vis)
-        K = int(tiles[radius > 0].sum())
+    K = count_entries(scene, camp, W, H)
     T = ((W + 15) // 16) * ((H + 15) // 16)
     n = args.n
     algo = {"alpha_blending_fwd": blend_fwd_bytes(n, 7, K, T, W, H),
@@ -593,6 +641,7 @@ def run_gb300(args):
             "metric": METRIC, "value": value, "unit": "iters/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+            "eager_ms_per_step": eager_ms,
             "config": {"workload": WORKLOAD, "gaussians": n, "width": W, "height": H, "channels": 7,
                        "sh_degree": 3, "K_duplicates": K, "tiles": T,
                        "l2": "inputs larger than L2 (0.31 GB of Gaussian parameters + 47 MB target per step)",

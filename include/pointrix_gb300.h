@@ -272,6 +272,66 @@ typedef struct {
 int pgb_adam_step(const pgb_adam_segment* segments, int nsegments, float beta1, float beta2,
                   float eps, void* stream);
 
+/* The same update with the step counts on the device, for a step captured
+ * in a CUDA graph: step_counts[i] (int32, device) is segment i's count t,
+ * incremented by the call before use; the bias corrections 1 - beta^t are
+ * formed on the device in double precision into bias_corrections (float,
+ * device, 2 per segment) -- the bias_correction fields of the segments are
+ * ignored.  Two launches. */
+int pgb_adam_step_device(const pgb_adam_segment* segments, int nsegments, double beta1,
+                         double beta2, float eps, int32_t* step_counts, float* bias_corrections,
+                         void* stream);
+
+/* ---------------------------------------------------------------------
+ * Fused caller-side passes of the training step -- no msplat counterpart.
+ * They replace torch glue that surrounds the operators above, with the same
+ * arithmetic.
+ *
+ * pgb_gaussian_activate_*: the parameter activations of GaussianPointCloud
+ * (pointrix/model/point_cloud/gaussian_points.py:70-80: exp, sigmoid,
+ * F.normalize) and the normal feature of examples/supervise/model.py:50-62
+ * (column argmin(log_scale) of the rotation matrix of
+ * pointrix/utils/pose.py:40-84, normalised).  log_scale [N,3], quat [N,4]
+ * wxyz, opacity_logit [N] -> scaling [N,3], rotation [N,4], opacity [N],
+ * normal [N,3] (NULL: not computed).  quat, rotation, d_rotation and d_quat
+ * must be 16-byte aligned.  The backward takes the incoming gradients (any of
+ * them NULL: zero) and writes the parameter gradients.
+ * ------------------------------------------------------------------- */
+int pgb_gaussian_activate_forward(const float* log_scale, const float* quat,
+                                  const float* opacity_logit, int64_t n, float* scaling,
+                                  float* rotation, float* opacity, float* normal, void* stream);
+int pgb_gaussian_activate_backward(const float* log_scale, const float* quat,
+                                   const float* opacity_logit, int64_t n, const float* d_scaling,
+                                   const float* d_rotation, const float* d_opacity,
+                                   const float* d_normal, float* d_log_scale, float* d_quat,
+                                   float* d_opacity_logit, void* stream);
+
+/* pgb_sh_rgb_*: the view colour of MsplatRender.render_iter
+ * (pointrix/model/renderer/msplat.py:94-105): direction = normalise(xyz -
+ * center), the SH mask (coefficients k >= active are zero), compute_sh, +0.5
+ * and clamp(min=0), in one pass.  sh is the dense [N,K,3] storage (the
+ * tensor msplat.py:99 permutes), 16-byte aligned; center [3].  The backward
+ * writes d_sh [N,K,3] (zero for k >= active), d_xyz [N,3] and d_center [3]
+ * (deterministic, through scratch of pgb_sh_rgb_scratch_floats(n) floats). */
+int pgb_sh_rgb_scratch_floats(int64_t n);
+int pgb_sh_rgb_forward(const float* sh, int64_t n, int k, int active, const float* xyz,
+                       const float* center, float* rgb, void* stream);
+int pgb_sh_rgb_backward(const float* sh, int64_t n, int k, int active, const float* xyz,
+                        const float* center, const float* d_rgb, float* d_sh, float* d_xyz,
+                        float* d_center, float* scratch, int64_t scratch_floats, void* stream);
+
+/* pgb_l1_l2_loss_*: L = mean|x - t| + w * mean((x - t)^2) over n floats
+ * (the L1 term of pointrix/model/loss.py:27-33 plus a weighted L2 term), x
+ * and t 16-byte aligned.  The forward writes L to loss[0] (device) through
+ * scratch of pgb_l1_l2_loss_scratch_doubles(n) doubles, summed in a fixed
+ * order; the backward reads dL from d_loss[0] (device) and writes
+ * d_x = sign(x - t) dL / n + (2 / n)(x - t) w dL. */
+int pgb_l1_l2_loss_scratch_doubles(int64_t n);
+int pgb_l1_l2_loss_forward(const float* x, const float* target, int64_t n, float w,
+                           double* scratch, int64_t scratch_doubles, float* loss, void* stream);
+int pgb_l1_l2_loss_backward(const float* x, const float* target, int64_t n, float w,
+                            const float* d_loss, float* d_x, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -53,6 +53,18 @@ class AdamSegment(C.Structure):
 
 
 SIGNATURES["pgb_adam_step"] = [C.POINTER(AdamSegment), i32, f32, f32, f32, vp]
+SIGNATURES["pgb_adam_step_device"] = [C.POINTER(AdamSegment), i32, C.c_double, C.c_double, f32, vp,
+                                      vp, vp]
+SIGNATURES.update({
+    "pgb_gaussian_activate_forward": [vp, vp, vp, i64, vp, vp, vp, vp, vp],
+    "pgb_gaussian_activate_backward": [vp, vp, vp, i64, vp, vp, vp, vp, vp, vp, vp, vp],
+    "pgb_sh_rgb_scratch_floats": [i64],
+    "pgb_sh_rgb_forward": [vp, i64, i32, i32, vp, vp, vp, vp],
+    "pgb_sh_rgb_backward": [vp, i64, i32, i32, vp, vp, vp, vp, vp, vp, vp, i64, vp],
+    "pgb_l1_l2_loss_scratch_doubles": [i64],
+    "pgb_l1_l2_loss_forward": [vp, vp, i64, f32, vp, i64, vp, vp],
+    "pgb_l1_l2_loss_backward": [vp, vp, i64, f32, vp, vp, vp],
+})
 
 _RESTYPES = {"pgb_status_string": C.c_char_p, "pgb_camera_grad_scratch_bytes": szt}
 

@@ -30,8 +30,24 @@ __device__ __forceinline__ void adam_one(float& p, float g, float& m, float& v, 
   p -= step_size * m / (sqrtf(v) * inv_sqrt_bc2 + eps);
 }
 
+// Step counts on the device (graph-captured steps): every segment's count
+// goes up by one, and its bias corrections 1 - beta^t are formed once, in
+// double as the host does, for the update to read.
+__global__ void adam_tick_kernel(int32_t* __restrict__ steps, float* __restrict__ bc, int nseg,
+                                 double b1d, double b2d) {
+  const int s = threadIdx.x;
+  if (s < nseg) {
+    const int t = steps[s] + 1;
+    steps[s] = t;
+    bc[2 * s] = (float)(1.0 - pow(b1d, (double)t));
+    bc[2 * s + 1] = (float)(1.0 - pow(b2d, (double)t));
+  }
+}
+
+// bc == nullptr: the table's bias corrections; else those the tick formed.
 __global__ void __launch_bounds__(kAdamThreads) adam_kernel(AdamTable t, float b1, float b2,
-                                                            float eps) {
+                                                            float eps,
+                                                            const float* __restrict__ bc) {
   const int64_t total = t.start4[t.nseg];
   int s = 0;
   for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < total;
@@ -39,8 +55,10 @@ __global__ void __launch_bounds__(kAdamThreads) adam_kernel(AdamTable t, float b
     while (q >= t.start4[s + 1]) ++s;  // q only grows for a thread
     const pgb_adam_segment& sg = t.seg[s];
     const int64_t i = (q - t.start4[s]) * 4;
-    const float step_size = sg.lr / sg.bias_correction1;
-    const float inv_sqrt_bc2 = 1.0f / sqrtf(sg.bias_correction2);
+    const float bc1 = bc ? bc[2 * s] : sg.bias_correction1;
+    const float bc2 = bc ? bc[2 * s + 1] : sg.bias_correction2;
+    const float step_size = sg.lr / bc1;
+    const float inv_sqrt_bc2 = 1.0f / sqrtf(bc2);
     if (i + 4 <= sg.n && (((uintptr_t)sg.param | (uintptr_t)sg.grad | (uintptr_t)sg.exp_avg |
                            (uintptr_t)sg.exp_avg_sq) & 15) == 0) {
       float4 p = reinterpret_cast<float4*>(sg.param)[i / 4];
@@ -62,12 +80,9 @@ __global__ void __launch_bounds__(kAdamThreads) adam_kernel(AdamTable t, float b
   }
 }
 
-}  // namespace pgb
-
-using namespace pgb;
-
-extern "C" int pgb_adam_step(const pgb_adam_segment* segments, int nsegments, float beta1,
-                             float beta2, float eps, void* stream) {
+static int adam_launch(const pgb_adam_segment* segments, int nsegments, float beta1, float beta2,
+                       float eps, int32_t* steps, float* bc, double b1d, double b2d,
+                       cudaStream_t st) {
   if (nsegments < 0 || nsegments > kMaxAdamSegments || (nsegments > 0 && !segments))
     return PGB_ERR_INVALID;
   AdamTable t;
@@ -77,13 +92,31 @@ extern "C" int pgb_adam_step(const pgb_adam_segment* segments, int nsegments, fl
     const pgb_adam_segment& s = segments[i];
     if (s.n < 0 || (s.n > 0 && (!s.param || !s.grad || !s.exp_avg || !s.exp_avg_sq)))
       return PGB_ERR_INVALID;
-    if (!(s.bias_correction1 > 0.f) || !(s.bias_correction2 > 0.f)) return PGB_ERR_INVALID;
+    if (!steps && (!(s.bias_correction1 > 0.f) || !(s.bias_correction2 > 0.f)))
+      return PGB_ERR_INVALID;
     t.seg[i] = s;
     t.start4[i + 1] = t.start4[i] + (s.n + 3) / 4;
   }
+  if (steps) adam_tick_kernel<<<1, 32, 0, st>>>(steps, bc, nsegments, b1d, b2d);
   const int64_t total = t.start4[nsegments];
-  if (total == 0) return PGB_OK;
-  adam_kernel<<<stream_grid(total, kAdamThreads, 8), kAdamThreads, 0, as_stream(stream)>>>(
-      t, beta1, beta2, eps);
+  if (total > 0)
+    adam_kernel<<<stream_grid(total, kAdamThreads, 8), kAdamThreads, 0, st>>>(t, beta1, beta2, eps,
+                                                                              steps ? bc : nullptr);
   return launch_status();
+}
+
+}  // namespace pgb
+
+extern "C" int pgb_adam_step(const pgb_adam_segment* segments, int nsegments, float beta1,
+                             float beta2, float eps, void* stream) {
+  return pgb::adam_launch(segments, nsegments, beta1, beta2, eps, nullptr, nullptr, 0.0, 0.0,
+                          pgb::as_stream(stream));
+}
+
+extern "C" int pgb_adam_step_device(const pgb_adam_segment* segments, int nsegments, double beta1,
+                                    double beta2, float eps, int32_t* step_counts,
+                                    float* bias_corrections, void* stream) {
+  if ((!step_counts || !bias_corrections) && nsegments > 0) return PGB_ERR_INVALID;
+  return pgb::adam_launch(segments, nsegments, (float)beta1, (float)beta2, eps, step_counts,
+                          bias_corrections, beta1, beta2, pgb::as_stream(stream));
 }

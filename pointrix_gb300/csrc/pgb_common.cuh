@@ -151,6 +151,27 @@ __device__ inline void cp_async_wait() {
   asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
 }
 
+// Deterministic sum over rows b < nrows of v[b * stride + col] for NCOL
+// columns, run by one CTA of NCOL * TPC threads: thread j of a column sums
+// rows j, j + TPC, ... in order (in double), then a fixed shared-memory tree
+// adds the TPC partial sums.  Returns the column's total in the column's
+// thread j == 0 (others: unspecified).  `s` holds NCOL * TPC doubles.
+template <int NCOL, int TPC, typename T>
+__device__ inline double column_sum(const T* __restrict__ v, int nrows, int stride, double* s) {
+  static_assert((TPC & (TPC - 1)) == 0, "TPC must be a power of two");
+  const int col = threadIdx.x / TPC, j = threadIdx.x % TPC;
+  double acc = 0.0;
+  if (col < NCOL)
+    for (int b = j; b < nrows; b += TPC) acc += (double)v[(size_t)b * stride + col];
+  s[threadIdx.x] = acc;
+  __syncthreads();
+  for (int h = TPC / 2; h > 0; h >>= 1) {
+    if (j < h) s[threadIdx.x] += s[threadIdx.x + h];
+    __syncthreads();
+  }
+  return s[threadIdx.x];
+}
+
 __device__ inline float warp_sum(float v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);

@@ -76,18 +76,21 @@ __device__ inline void block_write_partials(float (&acc)[16], float* __restrict_
   }
 }
 
-__global__ void cam_grad_finish_kernel(const float* __restrict__ partials, int nblocks,
-                                       float* __restrict__ d_intr, float* __restrict__ d_extr) {
-  // 16 warps, warp i sums column i over blocks.
-  const int lane = threadIdx.x & 31, col = threadIdx.x >> 5;
-  float s = 0.f;
-  for (int b = lane; b < nblocks; b += 32) s += partials[b * 16 + col];
-  s = warp_sum(s);
-  if (lane == 0) {
+// 16 columns x 64 threads: column c sums partials[b * 16 + c] over blocks in
+// a fixed order (in double).
+constexpr int kCamTPC = 64;
+
+__global__ void __launch_bounds__(16 * kCamTPC) cam_grad_finish_kernel(
+    const float* __restrict__ partials, int nblocks, float* __restrict__ d_intr,
+    float* __restrict__ d_extr) {
+  __shared__ double s[16 * kCamTPC];
+  const double t = column_sum<16, kCamTPC>(partials, nblocks, 16, s);
+  if (threadIdx.x % kCamTPC == 0) {
+    const int col = threadIdx.x / kCamTPC;
     if (col < 4)
-      d_intr[col] = s;
+      d_intr[col] = (float)t;
     else
-      d_extr[col - 4] = s;
+      d_extr[col - 4] = (float)t;
   }
 }
 
@@ -514,7 +517,7 @@ int pgb_project_point_backward(const float* xyz, int64_t n, const float* intr, c
   project_point_bwd_kernel<<<grid, kStreamThreads, 0, s>>>(xyz, n, intr, extr, width, height,
                                                            nearest, extent, d_uv, d_depth, d_xyz,
                                                            partials);
-  cam_grad_finish_kernel<<<1, 16 * 32, 0, s>>>(partials, grid, d_intr, d_extr);
+  cam_grad_finish_kernel<<<1, 16 * kCamTPC, 0, s>>>(partials, grid, d_intr, d_extr);
   return launch_status();
 }
 
@@ -560,7 +563,7 @@ int pgb_ewa_project_backward(const float* xyz, const float* cov3d, const float* 
   float* partials = static_cast<float*>(scratch);
   ewa_bwd_kernel<<<grid, kStreamThreads, 0, s>>>(xyz, cov3d, intr, extr, radius, n, width, height,
                                                  d_conic, d_xyz, d_cov3d, partials);
-  cam_grad_finish_kernel<<<1, 16 * 32, 0, s>>>(partials, grid, d_intr, d_extr);
+  cam_grad_finish_kernel<<<1, 16 * kCamTPC, 0, s>>>(partials, grid, d_intr, d_extr);
   return launch_status();
 }
 

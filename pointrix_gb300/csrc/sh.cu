@@ -12,6 +12,8 @@
 // through the permute, or a contiguous [N,3,K]) the 3K coefficients of a
 // Gaussian are one contiguous, 16-byte aligned block and are moved with
 // float4 loads and stores; any other stride pattern takes a scalar path.
+#include <algorithm>
+
 #include "pgb_common.cuh"
 
 namespace pgb {
@@ -252,6 +254,205 @@ static void launch_bwd(int L, const float* sh, int64_t n, int64_t sn, int64_t sc
                                                                d_dirs);
 }
 
+// ---------------------------------------------------------------------------
+// Fused view colour: rgb = clamp(sum_{k < active} c_k Y_k(d) + 0.5, min 0)
+// with d = (xyz - center) / |xyz - center|, the glue of msplat.py:94-105
+// around compute_sh (view direction, SH mask, offset and clamp) in one pass.
+// Coefficients are the dense [N,K,3] storage (kKC).  Each warp moves the
+// 32 * 3K coefficients of its 32 Gaussians between global memory and a
+// per-warp shared stage with 16-byte coalesced accesses; a lane then reads
+// its own 3K floats at an odd stride (no bank conflicts).
+// ---------------------------------------------------------------------------
+constexpr int kShWarps = 4;
+
+template <int K>
+struct ShStage {
+  static constexpr int F = 3 * K;                     // floats per Gaussian
+  static constexpr int P = (F % 2 == 1) ? F : F + 1;  // per-lane stride in the stage
+};
+
+template <int K>
+__device__ inline void stage_in(const float* __restrict__ src, int64_t g0, int cnt,
+                                float* __restrict__ stage, int lane) {
+  constexpr int F = ShStage<K>::F, P = ShStage<K>::P;
+  const float* p = src + g0 * F;
+  if (cnt == 32) {  // 32 * F floats: a multiple of 4, 16-byte aligned
+    for (int q = lane; q < 8 * F; q += 32) {
+      const float4 v = reinterpret_cast<const float4*>(p)[q];
+      const float vv[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+      for (int c = 0; c < 4; ++c) {
+        const int f = 4 * q + c;
+        stage[(f / F) * P + f % F] = vv[c];
+      }
+    }
+  } else {
+    for (int f = lane; f < cnt * F; f += 32) stage[(f / F) * P + f % F] = p[f];
+  }
+  __syncwarp();
+}
+
+template <int K>
+__device__ inline void stage_out(float* __restrict__ dst, int64_t g0, int cnt,
+                                 const float* __restrict__ stage, int lane) {
+  constexpr int F = ShStage<K>::F, P = ShStage<K>::P;
+  __syncwarp();
+  float* p = dst + g0 * F;
+  if (cnt == 32) {
+    for (int q = lane; q < 8 * F; q += 32) {
+      float vv[4];
+#pragma unroll
+      for (int c = 0; c < 4; ++c) {
+        const int f = 4 * q + c;
+        vv[c] = stage[(f / F) * P + f % F];
+      }
+      reinterpret_cast<float4*>(p)[q] = make_float4(vv[0], vv[1], vv[2], vv[3]);
+    }
+  } else {
+    for (int f = lane; f < cnt * F; f += 32) p[f] = stage[(f / F) * P + f % F];
+  }
+}
+
+// Unit view direction of Gaussian i (no epsilon, like the torch division).
+__device__ inline void view_dir(const float* __restrict__ xyz, int64_t i, float cx, float cy,
+                                float cz, float& dx, float& dy, float& dz, float& nrm) {
+  const float vx = xyz[3 * i] - cx, vy = xyz[3 * i + 1] - cy, vz = xyz[3 * i + 2] - cz;
+  nrm = sqrtf(vx * vx + vy * vy + vz * vz);
+  dx = vx / nrm;
+  dy = vy / nrm;
+  dz = vz / nrm;
+}
+
+template <int K>
+__device__ inline float sh_channel(const float* __restrict__ c, const float (&Y)[K], int ch,
+                                   int active) {
+  float s = 0.f;
+#pragma unroll
+  for (int k = 0; k < K; ++k)
+    if (k < active) s += c[k * 3 + ch] * Y[k];
+  return s;
+}
+
+template <int K>
+__global__ void __launch_bounds__(kShWarps * 32) sh_rgb_fwd_kernel(
+    const float* __restrict__ sh, int64_t n, int active, const float* __restrict__ xyz,
+    const float* __restrict__ center, float* __restrict__ rgb) {
+  __shared__ float stage_all[kShWarps][32 * ShStage<K>::P];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  float* stage = stage_all[warp];
+  const float cx = center[0], cy = center[1], cz = center[2];
+  const int64_t nblocks = (n + 31) / 32;
+  for (int64_t wb = (int64_t)blockIdx.x * kShWarps + warp; wb < nblocks;
+       wb += (int64_t)gridDim.x * kShWarps) {
+    const int64_t g0 = wb * 32;
+    const int cnt = n - g0 < 32 ? (int)(n - g0) : 32;
+    __syncwarp();
+    stage_in<K>(sh, g0, cnt, stage, lane);
+    if (lane < cnt) {
+      const int64_t i = g0 + lane;
+      float dx, dy, dz, nrm;
+      view_dir(xyz, i, cx, cy, cz, dx, dy, dz, nrm);
+      float Y[K];
+      sh_basis<K>(dx, dy, dz, Y);
+      const float* c = stage + lane * ShStage<K>::P;
+#pragma unroll
+      for (int ch = 0; ch < 3; ++ch) {
+        const float x = sh_channel<K>(c, Y, ch, active) + 0.5f;
+        rgb[3 * i + ch] = x < 0.f ? 0.f : x;  // NaN passes, as torch.clamp
+      }
+    }
+  }
+}
+
+// Backward: d_sh (zero for k >= active), d_xyz, and per-block partial sums
+// of -d(xyz - center) for the centre's gradient.
+template <int K>
+__global__ void __launch_bounds__(kShWarps * 32) sh_rgb_bwd_kernel(
+    const float* __restrict__ sh, int64_t n, int active, const float* __restrict__ xyz,
+    const float* __restrict__ center, const float* __restrict__ d_rgb, float* __restrict__ d_sh,
+    float* __restrict__ d_xyz, float* __restrict__ partial) {
+  __shared__ float stage_all[kShWarps][32 * ShStage<K>::P];
+  __shared__ float s_red[kShWarps][3];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  float* stage = stage_all[warp];
+  const float cx = center[0], cy = center[1], cz = center[2];
+  float ax = 0.f, ay = 0.f, az = 0.f;
+  const int64_t nblocks = (n + 31) / 32;
+  for (int64_t wb = (int64_t)blockIdx.x * kShWarps + warp; wb < nblocks;
+       wb += (int64_t)gridDim.x * kShWarps) {
+    const int64_t g0 = wb * 32;
+    const int cnt = n - g0 < 32 ? (int)(n - g0) : 32;
+    __syncwarp();
+    stage_in<K>(sh, g0, cnt, stage, lane);
+    if (lane < cnt) {
+      const int64_t i = g0 + lane;
+      float dx, dy, dz, nrm;
+      view_dir(xyz, i, cx, cy, cz, dx, dy, dz, nrm);
+      float Y[K];
+      sh_basis<K>(dx, dy, dz, Y);
+      float* c = stage + lane * ShStage<K>::P;
+      float g[3];
+#pragma unroll
+      for (int ch = 0; ch < 3; ++ch) {
+        const float x = sh_channel<K>(c, Y, ch, active) + 0.5f;
+        g[ch] = x >= 0.f ? d_rgb[3 * i + ch] : 0.f;  // clamp_min passes where x >= 0
+      }
+      float G[K];
+#pragma unroll
+      for (int k = 0; k < K; ++k) {
+        const bool on = k < active;
+        G[k] = on ? g[0] * c[k * 3] + g[1] * c[k * 3 + 1] + g[2] * c[k * 3 + 2] : 0.f;
+#pragma unroll
+        for (int ch = 0; ch < 3; ++ch) c[k * 3 + ch] = on ? g[ch] * Y[k] : 0.f;
+      }
+      float gx, gy, gz;
+      sh_basis_grad<K>(dx, dy, dz, G, gx, gy, gz);
+      const float dot = dx * gx + dy * gy + dz * gz;
+      const float vx = (gx - dx * dot) / nrm, vy = (gy - dy * dot) / nrm,
+                  vz = (gz - dz * dot) / nrm;
+      d_xyz[3 * i] = vx;
+      d_xyz[3 * i + 1] = vy;
+      d_xyz[3 * i + 2] = vz;
+      ax += vx;
+      ay += vy;
+      az += vz;
+    }
+    stage_out<K>(d_sh, g0, cnt, stage, lane);
+  }
+  ax = warp_sum(ax);
+  ay = warp_sum(ay);
+  az = warp_sum(az);
+  if (lane == 0) {
+    s_red[warp][0] = ax;
+    s_red[warp][1] = ay;
+    s_red[warp][2] = az;
+  }
+  __syncthreads();
+  if (threadIdx.x < 3) {
+    float t = 0.f;
+    for (int w = 0; w < kShWarps; ++w) t += s_red[w][threadIdx.x];
+    partial[3 * blockIdx.x + threadIdx.x] = -t;
+  }
+}
+
+// d_center[c] = sum over blocks of partial[b][c] (fixed order).
+constexpr int kCenterTPC = 128;
+
+__global__ void __launch_bounds__(4 * kCenterTPC) sh_center_finish_kernel(
+    const float* __restrict__ partial, int blocks, float* __restrict__ d_center) {
+  __shared__ double s[4 * kCenterTPC];
+  const double t = column_sum<3, kCenterTPC>(partial, blocks, 3, s);
+  if (threadIdx.x % kCenterTPC == 0 && threadIdx.x / kCenterTPC < 3)
+    d_center[threadIdx.x / kCenterTPC] = (float)t;
+}
+
+constexpr int kShRgbBlocksMax = kNumSMs * 8;
+
+inline int sh_rgb_grid(int64_t n) {
+  const int64_t need = ((n + 31) / 32 + kShWarps - 1) / kShWarps;
+  return (int)std::max<int64_t>(1, std::min<int64_t>(need, kShRgbBlocksMax));
+}
+
 }  // namespace pgb
 
 using namespace pgb;
@@ -288,6 +489,49 @@ int pgb_compute_sh_backward(const float* sh, int64_t n, int k, int64_t sn, int64
     case 9: launch_bwd<9>(L, sh, n, sn, sc, sk, dirs, d_rgb, d_sh, d_dirs, s); break;
     default: launch_bwd<16>(L, sh, n, sn, sc, sk, dirs, d_rgb, d_sh, d_dirs, s); break;
   }
+  return launch_status();
+}
+
+int pgb_sh_rgb_scratch_floats(int64_t n) { return 3 * sh_rgb_grid(n); }
+
+int pgb_sh_rgb_forward(const float* sh, int64_t n, int k, int active, const float* xyz,
+                       const float* center, float* rgb, void* stream) {
+  if (n < 0 || !(k == 1 || k == 4 || k == 9 || k == 16) || active < 0) return PGB_ERR_INVALID;
+  if (n == 0) return PGB_OK;
+  if (!sh || !xyz || !center || !rgb || (reinterpret_cast<uintptr_t>(sh) & 15))
+    return PGB_ERR_INVALID;
+  cudaStream_t s = as_stream(stream);
+  const int grid = sh_rgb_grid(n);
+  switch (k) {
+    case 1: sh_rgb_fwd_kernel<1><<<grid, kShWarps * 32, 0, s>>>(sh, n, active, xyz, center, rgb); break;
+    case 4: sh_rgb_fwd_kernel<4><<<grid, kShWarps * 32, 0, s>>>(sh, n, active, xyz, center, rgb); break;
+    case 9: sh_rgb_fwd_kernel<9><<<grid, kShWarps * 32, 0, s>>>(sh, n, active, xyz, center, rgb); break;
+    default: sh_rgb_fwd_kernel<16><<<grid, kShWarps * 32, 0, s>>>(sh, n, active, xyz, center, rgb); break;
+  }
+  return launch_status();
+}
+
+int pgb_sh_rgb_backward(const float* sh, int64_t n, int k, int active, const float* xyz,
+                        const float* center, const float* d_rgb, float* d_sh, float* d_xyz,
+                        float* d_center, float* scratch, int64_t scratch_floats, void* stream) {
+  if (n < 0 || !(k == 1 || k == 4 || k == 9 || k == 16) || active < 0) return PGB_ERR_INVALID;
+  cudaStream_t s = as_stream(stream);
+  if (n == 0) {
+    if (d_center && cudaMemsetAsync(d_center, 0, 3 * sizeof(float), s) != cudaSuccess)
+      return PGB_ERR_CUDA;
+    return PGB_OK;
+  }
+  const int grid = sh_rgb_grid(n);
+  if (!sh || !xyz || !center || !d_rgb || !d_sh || !d_xyz || !d_center || !scratch ||
+      scratch_floats < 3 * grid || ((reinterpret_cast<uintptr_t>(sh) | reinterpret_cast<uintptr_t>(d_sh)) & 15))
+    return PGB_ERR_INVALID;
+  switch (k) {
+    case 1: sh_rgb_bwd_kernel<1><<<grid, kShWarps * 32, 0, s>>>(sh, n, active, xyz, center, d_rgb, d_sh, d_xyz, scratch); break;
+    case 4: sh_rgb_bwd_kernel<4><<<grid, kShWarps * 32, 0, s>>>(sh, n, active, xyz, center, d_rgb, d_sh, d_xyz, scratch); break;
+    case 9: sh_rgb_bwd_kernel<9><<<grid, kShWarps * 32, 0, s>>>(sh, n, active, xyz, center, d_rgb, d_sh, d_xyz, scratch); break;
+    default: sh_rgb_bwd_kernel<16><<<grid, kShWarps * 32, 0, s>>>(sh, n, active, xyz, center, d_rgb, d_sh, d_xyz, scratch); break;
+  }
+  sh_center_finish_kernel<<<1, 4 * kCenterTPC, 0, s>>>(scratch, grid, d_center);
   return launch_status();
 }
 

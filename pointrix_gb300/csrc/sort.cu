@@ -410,11 +410,12 @@ __global__ void __launch_bounds__(kStreamThreads) rect_kernel(
 // ---------------------------------------------------------------------------
 // 3b. scan of the entry counts in depth order
 //
-// For depth-sorted position i (Gaussian g = order[i]) writes its output
-// offset offs[i] and, for every emission chunk boundary b * kEmitChunk that
-// falls inside [offs[i], offs[i] + count), chunk_first[b] = i.  K is the
-// host value k_cap, or the device count k_dev (written by the depth phase)
-// bounded by the capacity k_cap.
+// For depth-sorted position i (Gaussian g = order[i]) writes the emission
+// record owner[i] = (first tile, w | gx << 16, g, output offset) and, for
+// every emission chunk boundary b * kEmitChunk that falls inside
+// [offset, offset + count), chunk_first[b] = i.  K is the host value k_cap,
+// or the device count k_dev (written by the depth phase) bounded by the
+// capacity k_cap.
 // ---------------------------------------------------------------------------
 constexpr int kEmitChunk = 1024;
 constexpr int kEmitThreads = 256;
@@ -422,7 +423,7 @@ constexpr int kEmitThreads = 256;
 __global__ void __launch_bounds__(kSortThreads) scan_rect_kernel(
     const uint32_t* __restrict__ order, int64_t n, const uint4* __restrict__ rect, int64_t k_cap,
     const int64_t* __restrict__ k_dev, uint32_t* __restrict__ status,
-    uint32_t* __restrict__ part_counter, uint32_t* __restrict__ offs,
+    uint32_t* __restrict__ part_counter, uint4* __restrict__ owner,
     uint32_t* __restrict__ chunk_first, int64_t* __restrict__ info) {
   __shared__ uint32_t s_warp_tot[kSortThreads / 32];
   __shared__ uint32_t s_part, s_prior;
@@ -437,12 +438,20 @@ __global__ void __launch_bounds__(kSortThreads) scan_rect_kernel(
   const int part = (int)s_part;
   const int64_t base = (int64_t)part * kScanPart + (int64_t)threadIdx.x * kScanItems;
 
-  uint32_t cnt[kScanItems];
+  uint32_t cnt[kScanItems], t0[kScanItems], wg[kScanItems], gid[kScanItems];
   uint32_t sum = 0;
 #pragma unroll
   for (int it = 0; it < kScanItems; ++it) {
     const int64_t e = base + it;
-    cnt[it] = e < n ? rect[order[e]].w : 0u;
+    uint4 r = make_uint4(0u, 0u, 0u, 0u);
+    gid[it] = 0;
+    if (e < n) {
+      gid[it] = order[e];
+      r = rect[gid[it]];
+    }
+    t0[it] = r.x;
+    wg[it] = (r.y & 0xFFFFu) | (r.z << 16);
+    cnt[it] = r.w;
     sum += cnt[it];
   }
   uint32_t total;
@@ -469,7 +478,7 @@ __global__ void __launch_bounds__(kSortThreads) scan_rect_kernel(
       if (end > K) {
         set_error(info, PGB_ERR_OVERFLOW);
       } else {
-        offs[e] = (uint32_t)off;
+        owner[e] = make_uint4(t0[it], wg[it], gid[it], (uint32_t)off);
         // chunk boundaries owned by this Gaussian, and the owner of the
         // last entry (stored after the last chunk's)
         for (int64_t b = (off + kEmitChunk - 1) / kEmitChunk; b * kEmitChunk < end; ++b)
@@ -485,8 +494,8 @@ __global__ void __launch_bounds__(kSortThreads) scan_rect_kernel(
 // 3c. emission of (tile id, Gaussian id) pairs over output chunks
 //
 // A persistent grid walks the output chunks: for chunk b, entries
-// [b*kEmitChunk, min(K, (b+1)*kEmitChunk)), the CTA stages the offsets, ids
-// and rectangles of the Gaussians that own them in shared memory; each
+// [b*kEmitChunk, min(K, (b+1)*kEmitChunk)), the CTA stages the emission
+// records of the Gaussians that own them in shared memory; each
 // thread takes 4 consecutive entries, finds the owner of the first by binary
 // search and walks forward; the pairs are staged in shared memory and
 // written with 16-byte stores.  Every chunk is the same amount of work
@@ -497,19 +506,16 @@ __global__ void __launch_bounds__(kSortThreads) scan_rect_kernel(
 // (INT_MAX, 0) for the last tile pass.
 // ---------------------------------------------------------------------------
 constexpr int kEmitPer = kEmitChunk / kEmitThreads;  // 4
-constexpr int kEmitBlocksPerSM = 6;
+constexpr int kEmitBlocksPerSM = 7;
 
 __global__ void __launch_bounds__(kEmitThreads) emit_kernel(
-    const uint32_t* __restrict__ order, const uint32_t* __restrict__ offs,
-    const uint4* __restrict__ rect, const uint32_t* __restrict__ chunk_first, int64_t n_sorted,
+    const uint4* __restrict__ owner, const uint32_t* __restrict__ chunk_first, int64_t n_sorted,
     int64_t k_cap, const int64_t* __restrict__ k_dev, int tile_passes, int digit_bits,
     uint32_t* __restrict__ tkeys, uint32_t* __restrict__ tvals, uint32_t* __restrict__ tile_hist,
     int2* __restrict__ range, uint32_t T, int64_t* __restrict__ info) {
   constexpr int CAP = kEmitChunk + 1;
-  __shared__ uint32_t s_off[CAP];
-  __shared__ uint32_t s_g[CAP];
-  __shared__ uint32_t s_t0[CAP];  // first tile of the rectangle
-  __shared__ uint32_t s_wg[CAP];  // w | gx << 16
+  // (first tile, w | gx << 16, g, offset) of the chunk's owners
+  __shared__ __align__(16) uint4 s_own[CAP];
   __shared__ __align__(16) uint32_t s_key[kEmitChunk];
   __shared__ __align__(16) uint32_t s_val[kEmitChunk];
   __shared__ uint32_t s_hist[kTileHistWords];
@@ -535,20 +541,13 @@ __global__ void __launch_bounds__(kEmitThreads) emit_kernel(
     if (!ok_range && threadIdx.x == 0) set_error(info, PGB_ERR_OVERFLOW);
     const bool staged = ok_range && m <= CAP;
     __syncthreads();  // the previous chunk is out of the staging arrays
-    if (staged) {
-      for (int64_t i = threadIdx.x; i < m; i += kEmitThreads) {
-        const uint32_t g = order[i0 + i];
-        const uint4 rc = rect[g];
-        s_off[i] = offs[i0 + i];
-        s_g[i] = g;
-        s_t0[i] = rc.x;
-        s_wg[i] = (rc.y & 0xFFFFu) | (rc.z << 16);
-      }
-    }
+    if (staged)
+      for (int64_t i = threadIdx.x; i < m; i += kEmitThreads) s_own[i] = owner[i0 + i];
     __syncthreads();
     const int64_t ebeg = e0 + (int64_t)threadIdx.x * kEmitPer;
     if (ok_range && ebeg < e1) {
-      auto off_at = [&](int64_t p) -> int64_t { return staged ? s_off[p] : offs[i0 + p]; };
+      auto own_at = [&](int64_t p) -> uint4 { return staged ? s_own[p] : owner[i0 + p]; };
+      auto off_at = [&](int64_t p) -> int64_t { return staged ? s_own[p].w : owner[i0 + p].w; };
       // owner of ebeg: the last position p in [0, i1 - i0] with offs <= ebeg
       int64_t lo = 0, hi = i1 - i0;
       while (lo < hi) {
@@ -568,20 +567,12 @@ __global__ void __launch_bounds__(kEmitThreads) emit_kernel(
           fresh = true;
         }
         if (fresh) {  // first entry of this owner for the thread: position by division
-          uint32_t wg;
-          if (staged) {
-            g = s_g[own];
-            t0 = s_t0[own];
-            wg = s_wg[own];
-          } else {
-            g = order[i0 + own];
-            const uint4 rc = rect[g];
-            t0 = rc.x;
-            wg = (rc.y & 0xFFFFu) | (rc.z << 16);
-          }
-          w = wg & 0xFFFFu;
-          gx = wg >> 16;
-          const uint32_t jj = (uint32_t)(e - off_at(own));
+          const uint4 o = own_at(own);
+          t0 = o.x;
+          w = o.y & 0xFFFFu;
+          gx = o.y >> 16;
+          g = o.z;
+          const uint32_t jj = (uint32_t)(e - o.w);
           row = w ? jj / w : 0u;
           col = jj - row * w;
           fresh = false;
@@ -657,7 +648,7 @@ inline size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
 struct ScratchN {
   size_t counters, depth_hist, tile_hist, depth_status, scan_status, zero_bytes;
-  size_t dk0, dv0, dk1, dv1, offs, rect, total;
+  size_t dk0, dv0, dk1, dv1, owner, rect, total;
   int parts, scan_parts;
 };
 
@@ -677,7 +668,7 @@ inline ScratchN layout_n(int64_t n) {
   L.dv0 = o; o += nb;
   L.dk1 = o; o += nb;
   L.dv1 = o; o += nb;
-  L.offs = o; o += nb;
+  L.owner = o; o += align256((size_t)n * sizeof(uint4));
   L.rect = o; o += align256((size_t)n * sizeof(uint4));
   L.total = o;
   return L;
@@ -838,18 +829,18 @@ static int sort_finish_impl(const float* uv, const int32_t* radius, const int32_
   uint32_t* bufk[2] = {at<uint32_t>(scratch_k, LK.tk0), at<uint32_t>(scratch_k, LK.tk1)};
   uint32_t* bufv[2] = {at<uint32_t>(scratch_k, LK.tv0), at<uint32_t>(scratch_k, LK.tv1)};
   uint32_t* status = at<uint32_t>(scratch_k, LK.status);
-  uint32_t* offs = at<uint32_t>(scratch_n, LN.offs);
+  uint4* owner = at<uint4>(scratch_n, LN.owner);
   uint4* rect = at<uint4>(scratch_n, LN.rect);
   uint32_t* chunk_first = at<uint32_t>(scratch_k, LK.chunk_first);
   int2* range = reinterpret_cast<int2*>(tile_range_out);
   rect_kernel<<<stream_grid(n), kStreamThreads, 0, s>>>(uv, radius, tiles_touched, n, vt, rect,
                                                         info);
   scan_rect_kernel<<<LN.scan_parts, kSortThreads, 0, s>>>(
-      order, n, rect, k, k_dev, at<uint32_t>(scratch_n, LN.scan_status), counters + 4, offs,
+      order, n, rect, k, k_dev, at<uint32_t>(scratch_n, LN.scan_status), counters + 4, owner,
       chunk_first, info);
   const int64_t emit_grid = std::min<int64_t>(LK.chunks, (int64_t)kNumSMs * kEmitBlocksPerSM);
-  emit_kernel<<<(unsigned)emit_grid, kEmitThreads, 0, s>>>(order, offs, rect, chunk_first, n, k,
-                                                           k_dev, plan.passes, plan.bits, bufk[0],
+  emit_kernel<<<(unsigned)emit_grid, kEmitThreads, 0, s>>>(owner, chunk_first, n, k, k_dev,
+                                                           plan.passes, plan.bits, bufk[0],
                                                            bufv[0], thist, range, T, info);
   int cur = 0;
   for (int p = 0; p < plan.passes; ++p) {

@@ -1,0 +1,198 @@
+"""Fused caller-side passes of the training step (no msplat counterpart).
+
+Around the msplat operators, a Pointrix training step spends a dozen torch
+kernels each on the parameter activations and the normal feature
+(``pointrix/model/point_cloud/gaussian_points.py:70-80``,
+``examples/supervise/model.py:50-62``), on the view colour glue of
+``MsplatRender.render_iter`` (``pointrix/model/renderer/msplat.py:94-105``)
+and on the loss.  Each function here does the same arithmetic in one kernel
+forward and one backward:
+
+* :func:`gaussian_activations` -- exp(log_scale), F.normalize(quat),
+  sigmoid(logit) and the shortest-axis normal;
+* :func:`sh_rgb` -- clamp(compute_sh(masked sh, normalize(xyz - center)) +
+  0.5, min=0), with gradients to sh, xyz and the camera centre;
+* :func:`l1_l2_loss` -- mean|x - t| + w mean((x - t)^2).
+"""
+from __future__ import annotations
+
+import torch
+
+from . import _lib
+from ._lib import call
+from .ops import _c, _ptr, _stream, _timed
+
+__all__ = ["gaussian_activations", "sh_rgb", "sh_rgb_supported", "l1_l2_loss"]
+
+
+def _aligned(t: torch.Tensor) -> bool:
+    return t.data_ptr() % 16 == 0
+
+
+def _c16(t: torch.Tensor) -> torch.Tensor:
+    """Contiguous float32 with a 16-byte aligned start (copied if not)."""
+    t = _c(t)
+    return t if _aligned(t) else t.clone()
+
+
+# ---------------------------------------------------------------------------
+class _Activate(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, log_scale, quat, logit, normals):
+        n = log_scale.shape[0]
+        dev = log_scale.device
+        scaling = torch.empty(n, 3, dtype=torch.float32, device=dev)
+        rotation = torch.empty(n, 4, dtype=torch.float32, device=dev)
+        opacity = torch.empty(logit.shape, dtype=torch.float32, device=dev)
+        normal = torch.empty(n, 3, dtype=torch.float32, device=dev) if normals else None
+        with _timed("gaussian_activate_fwd", dev, 1 if n else 0):
+            call("pgb_gaussian_activate_forward", _ptr(log_scale), _ptr(quat), _ptr(logit), n,
+                 _ptr(scaling), _ptr(rotation), _ptr(opacity), _ptr(normal) if normals else None,
+                 _stream(dev))
+        ctx.save_for_backward(log_scale, quat, logit)
+        if normal is None:
+            normal = torch.empty(0, 3, dtype=torch.float32, device=dev)
+            ctx.mark_non_differentiable(normal)
+        return scaling, rotation, opacity, normal
+
+    @staticmethod
+    def backward(ctx, d_scaling, d_rotation, d_opacity, d_normal):
+        log_scale, quat, logit = ctx.saved_tensors
+        n = log_scale.shape[0]
+        dev = log_scale.device
+        d_ls = torch.empty_like(log_scale)
+        d_q = torch.empty_like(quat)
+        d_lg = torch.empty_like(logit)
+
+        def g(t, aligned=False):
+            if t is None or t.numel() == 0:
+                return None
+            return _c16(t) if aligned else _c(t)
+
+        d_scaling, d_rotation = g(d_scaling), g(d_rotation, True)
+        d_opacity, d_normal = g(d_opacity), g(d_normal)
+        with _timed("gaussian_activate_bwd", dev, 1 if n else 0):
+            call("pgb_gaussian_activate_backward", _ptr(log_scale), _ptr(quat), _ptr(logit), n,
+                 _ptr(d_scaling) if d_scaling is not None else None,
+                 _ptr(d_rotation) if d_rotation is not None else None,
+                 _ptr(d_opacity) if d_opacity is not None else None,
+                 _ptr(d_normal) if d_normal is not None else None,
+                 _ptr(d_ls), _ptr(d_q), _ptr(d_lg), _stream(dev))
+        return d_ls, d_q, d_lg, None
+
+
+def gaussian_activations(log_scale, quat, opacity_logit, normals=True):
+    """(scaling [N,3], rotation [N,4], opacity (shape of the logit), normal
+    [N,3] or None) from the stored Gaussian parameters: exp, F.normalize
+    (eps 1e-12), sigmoid, and normalize(R(rotation)[:, argmin(log_scale)])
+    with R the wxyz unit-quaternion matrix.  Differentiable in all three
+    inputs."""
+    if log_scale.dim() != 2 or log_scale.shape[1] != 3:
+        raise ValueError(f"log_scale must be [N,3], got {tuple(log_scale.shape)}")
+    n = log_scale.shape[0]
+    if tuple(quat.shape) != (n, 4):
+        raise ValueError(f"quat must be [N,4], got {tuple(quat.shape)}")
+    if opacity_logit.numel() != n:
+        raise ValueError("opacity_logit must hold N values")
+    for name, t in (("log_scale", log_scale), ("quat", quat), ("opacity_logit", opacity_logit)):
+        if not t.is_cuda or t.dtype != torch.float32:
+            raise ValueError(f"{name} must be a CUDA float32 tensor")
+    s, r, o, nrm = _Activate.apply(_c(log_scale), _c16(quat), _c(opacity_logit), bool(normals))
+    return s, r, o, (nrm if normals else None)
+
+
+# ---------------------------------------------------------------------------
+_SH_K = (1, 4, 9, 16)
+
+
+def sh_rgb_supported(shs) -> bool:
+    """True when ``shs`` ([N,K,3]) is dense storage the fused kernel reads."""
+    return (shs.is_cuda and shs.dtype == torch.float32 and shs.dim() == 3 and shs.shape[2] == 3
+            and shs.shape[1] in _SH_K and shs.is_contiguous() and _aligned(shs))
+
+
+class _ShRgb(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, shs, xyz, center, active):
+        n, K = shs.shape[0], shs.shape[1]
+        dev = shs.device
+        rgb = torch.empty(n, 3, dtype=torch.float32, device=dev)
+        with _timed("sh_rgb_fwd", dev, 1 if n else 0):
+            call("pgb_sh_rgb_forward", _ptr(shs), n, K, active, _ptr(xyz), _ptr(center), _ptr(rgb),
+                 _stream(dev))
+        ctx.save_for_backward(shs, xyz, center)
+        ctx.active = active
+        return rgb
+
+    @staticmethod
+    def backward(ctx, d_rgb):
+        shs, xyz, center = ctx.saved_tensors
+        n, K = shs.shape[0], shs.shape[1]
+        dev = shs.device
+        d_sh = torch.empty_like(shs)
+        d_xyz = torch.empty_like(xyz)
+        d_center = torch.empty(3, dtype=torch.float32, device=dev)
+        nf = _lib.lib().pgb_sh_rgb_scratch_floats(n)
+        scratch = torch.empty(max(nf, 1), dtype=torch.float32, device=dev)
+        with _timed("sh_rgb_bwd", dev, 2 if n else 0):
+            call("pgb_sh_rgb_backward", _ptr(shs), n, K, ctx.active, _ptr(xyz), _ptr(center),
+                 _ptr(_c(d_rgb)), _ptr(d_sh), _ptr(d_xyz), _ptr(d_center), _ptr(scratch), nf,
+                 _stream(dev))
+        return d_sh, d_xyz, d_center, None
+
+
+def sh_rgb(shs, position, camera_center, active=None):
+    """clamp(compute_sh(shs.permute(0,2,1) * mask, normalize(position -
+    center)) + 0.5, min=0) -> [N,3], the mask keeping the first ``active``
+    coefficients (all when None).  ``shs`` is the [N,K,3] storage (see
+    :func:`sh_rgb_supported`); gradients flow to shs, position and the
+    camera centre ([3] or any shape of 3 elements)."""
+    if not sh_rgb_supported(shs):
+        raise ValueError("sh_rgb needs dense, 16-byte aligned CUDA float32 shs [N,K,3], K in 1/4/9/16")
+    n, K = shs.shape[0], shs.shape[1]
+    if tuple(position.shape) != (n, 3):
+        raise ValueError(f"position must be [N,3], got {tuple(position.shape)}")
+    if camera_center.numel() != 3:
+        raise ValueError("camera_center must hold 3 values")
+    active = K if active is None else max(0, min(int(active), K))
+    return _ShRgb.apply(shs, _c(position), _c(camera_center.reshape(3)), active)
+
+
+# ---------------------------------------------------------------------------
+class _L1L2(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, x, t, w):
+        n = x.numel()
+        dev = x.device
+        nd = _lib.lib().pgb_l1_l2_loss_scratch_doubles(n)
+        scratch = torch.empty(nd, dtype=torch.float64, device=dev)
+        loss = torch.empty((), dtype=torch.float32, device=dev)
+        with _timed("l1_l2_loss_fwd", dev, 2):
+            call("pgb_l1_l2_loss_forward", _ptr(x), _ptr(t), n, w, _ptr(scratch), nd, _ptr(loss),
+                 _stream(dev))
+        ctx.save_for_backward(x, t)
+        ctx.w = w
+        return loss
+
+    @staticmethod
+    def backward(ctx, d_loss):
+        x, t = ctx.saved_tensors
+        dev = x.device
+        dx = torch.empty_like(x)
+        with _timed("l1_l2_loss_bwd", dev, 1):
+            call("pgb_l1_l2_loss_backward", _ptr(x), _ptr(t), x.numel(), ctx.w,
+                 _ptr(_c(d_loss.reshape(1))), _ptr(dx), _stream(dev))
+        return dx, None, None
+
+
+def l1_l2_loss(x, target, w_l2=0.0):
+    """mean|x - target| + w_l2 * mean((x - target)^2) as a 0-dim tensor;
+    differentiable in ``x`` (the same gradient as torch's l1_loss +
+    w_l2 * mse_loss)."""
+    if x.shape != target.shape:
+        raise ValueError(f"shape mismatch {tuple(x.shape)} vs {tuple(target.shape)}")
+    if x.numel() == 0:
+        raise ValueError("l1_l2_loss of an empty tensor")
+    if not (x.is_cuda and target.is_cuda and x.dtype == torch.float32 and target.dtype == torch.float32):
+        raise ValueError("l1_l2_loss takes CUDA float32 tensors")
+    return _L1L2.apply(_c16(x), _c16(target.detach()), float(w_l2))

@@ -599,28 +599,28 @@ class _RasterizeRecompute(torch.autograd.Function):
     keeping them alive between forward and backward."""
 
     @staticmethod
-    def forward(ctx, uv, conic, opacity, feature, depth, radius, tiles, bg, W, H, ndc):
-        ids, rng = sort_gaussian(uv, depth, W, H, radius, tiles)
+    def forward(ctx, uv, conic, opacity, feature, depth, radius, tiles, bg, W, H, ndc, capacity):
+        ids, rng = sort_gaussian(uv, depth, W, H, radius, tiles, capacity=capacity)
         _, out, _, _ = _blend_forward_raw(uv, conic, opacity, feature, ids, rng, bg, W, H)
         ctx.save_for_backward(uv, conic, opacity, feature, depth, radius, tiles)
-        ctx.cfg = (float(bg), W, H, ndc is not None)
+        ctx.cfg = (float(bg), W, H, ndc is not None, capacity)
         return out
 
     @staticmethod
     def backward(ctx, d_out):
         uv, conic, opacity, feature, depth, radius, tiles = ctx.saved_tensors
-        bg, W, H, has_ndc = ctx.cfg
+        bg, W, H, has_ndc, capacity = ctx.cfg
         n, C = feature.shape
-        ids, rng = sort_gaussian(uv, depth, W, H, radius, tiles)
+        ids, rng = sort_gaussian(uv, depth, W, H, radius, tiles, capacity=capacity)
         records, _, final_T, ncon = _blend_forward_raw(uv, conic, opacity, feature, ids, rng, bg, W, H)
         d_uv, d_conic, d_op, d_feat = _blend_backward_raw(records, ids, rng, final_T, ncon, d_out,
                                                           n, C, bg, W, H)
         d_ndc = d_uv.clone() if has_ndc else None
-        return d_uv, d_conic, d_op, d_feat, None, None, None, None, None, None, d_ndc
+        return d_uv, d_conic, d_op, d_feat, None, None, None, None, None, None, d_ndc, None
 
 
 def rasterize(uv, conic, opacity, feature, depth, radius, tiles_touched, bg, W, H, ndc=None,
-              recompute=False):
+              recompute=False, capacity=None):
     """``sort_gaussian`` followed by ``alpha_blending`` -> [C,H,W].
 
     With ``recompute=False`` this is exactly the two operators.  With
@@ -628,9 +628,10 @@ def rasterize(uv, conic, opacity, feature, depth, radius, tiles_touched, bg, W, 
     instead of keeping the tile lists, records and per-pixel state alive from
     the forward: less memory held between forward and backward (what limits
     4K views of millions of Gaussians), one more sort and blend forward per
-    step.  Gradients are the same in both modes."""
+    step.  Gradients are the same in both modes.  ``capacity`` is passed to
+    :func:`sort_gaussian` (K kept on the device, no synchronisation)."""
     if not recompute:
-        ids, rng = sort_gaussian(uv, depth, W, H, radius, tiles_touched)
+        ids, rng = sort_gaussian(uv, depth, W, H, radius, tiles_touched, capacity=capacity)
         return alpha_blending(uv, conic, opacity, feature, ids, rng, bg, W, H, ndc)
     _need(feature, "feature", ndim=2)
     n, C = feature.shape
@@ -639,7 +640,8 @@ def rasterize(uv, conic, opacity, feature, depth, radius, tiles_touched, bg, W, 
     if isinstance(bg, torch.Tensor):
         bg = float(bg)
     return _RasterizeRecompute.apply(_c(uv), _c(conic), _c(opacity.reshape(n)), _c(feature),
-                                     depth, radius, tiles_touched, bg, int(W), int(H), ndc)
+                                     depth, radius, tiles_touched, bg, int(W), int(H), ndc,
+                                     capacity)
 
 
 def alpha_blending_with_state(uv, conic, opacity, feature, gaussian_ids_sorted, tile_range, bg, W, H,

@@ -6,7 +6,9 @@ parameter group is one entry of a segment table and the whole update is a
 single HBM stream (28 bytes per element).  Same update rule as
 ``torch.optim.Adam`` (no weight decay, no amsgrad); the step count and bias
 corrections are kept on the host (per parameter, as torch does), so a step
-never synchronises.
+never synchronises.  With ``capturable=True`` the step counts live on the
+device instead and the bias corrections are formed there, so a step can be
+captured in a CUDA graph and replayed.
 """
 from __future__ import annotations
 
@@ -19,10 +21,12 @@ from .ops import _timed
 
 
 class Adam(torch.optim.Optimizer):
-    def __init__(self, params, lr=1e-3, betas=(0.9, 0.999), eps=1e-8):
+    def __init__(self, params, lr=1e-3, betas=(0.9, 0.999), eps=1e-8, capturable=False):
         if not 0.0 <= eps:
             raise ValueError(f"invalid eps {eps}")
         super().__init__(params, dict(lr=lr, betas=betas, eps=eps))
+        self.capturable = bool(capturable)
+        self._steps_dev = None   # int32 [segments] of the capturable mode
 
     @torch.no_grad()
     def step(self, closure=None):
@@ -57,12 +61,25 @@ class Adam(torch.optim.Optimizer):
         lib = _lib.lib()
         dev = segs[0][0].device
         stream = torch.cuda.current_stream(dev).cuda_stream
+        if self.capturable and (self._steps_dev is None or self._steps_dev.numel() != len(segs)):
+            # the device counts start where the host counts were before this step
+            self._steps_dev = torch.tensor([self.state[p]["step"] - 1 for p, *_ in segs],
+                                           dtype=torch.int32, device=dev)
+            self._bc_dev = torch.empty(2 * len(segs), dtype=torch.float32, device=dev)
         for i in range(0, len(segs), 32):
             chunk = segs[i:i + 32]
             table = (_lib.AdamSegment * len(chunk))(*[
                 _lib.AdamSegment(p.data_ptr(), g.data_ptr(), m.data_ptr(), v.data_ptr(), p.numel(),
                                  lr, bc1, bc2)
                 for p, g, m, v, lr, bc1, bc2 in chunk])
-            with _timed("adam_step", dev, 1):
-                _lib.check(lib.pgb_adam_step(table, len(chunk), b1, b2, eps, stream), "pgb_adam_step")
+            if self.capturable:
+                with _timed("adam_step", dev, 2):
+                    _lib.check(lib.pgb_adam_step_device(table, len(chunk), b1, b2, eps,
+                                                        self._steps_dev[i:].data_ptr(),
+                                                        self._bc_dev[2 * i:].data_ptr(), stream),
+                               "pgb_adam_step_device")
+            else:
+                with _timed("adam_step", dev, 1):
+                    _lib.check(lib.pgb_adam_step(table, len(chunk), b1, b2, eps, stream),
+                               "pgb_adam_step")
         return loss

@@ -22,7 +22,7 @@ from typing import Dict
 
 import torch
 
-from . import ops
+from . import fused, ops
 
 
 class RenderFeatures:
@@ -64,6 +64,12 @@ class MsplatRender:
         # recompute the sorted tile lists and per-pixel state in the backward
         # instead of keeping them from the forward (memory for 4K views)
         recompute_backward: bool = False
+        # view direction + SH mask + compute_sh + 0.5 + clamp in one kernel
+        # (when shs is dense [N,K,3] storage)
+        fused_view_colour: bool = True
+        # > 0: sort with K kept on the device and lists of this capacity (no
+        # host synchronisation; the step can be captured in a CUDA graph)
+        sort_capacity: int = 0
 
     def __init__(self, cfg: "MsplatRender.Config | dict | None" = None, white_bg: bool = False,
                  device="cuda", nearest: float = ops.NEAREST_DEFAULT):
@@ -86,19 +92,21 @@ class MsplatRender:
         Extra keyword tensors listed in ``kwargs['extra_features']`` (a dict
         name -> [N,c]) are blended as additional channels after rgb/depth."""
         n = position.shape[0]
-        direction = position - camera_center.reshape(1, 3).expand(n, 3)
-        direction = direction / direction.norm(dim=1, keepdim=True)
-
-        sh_coeff = shs.permute(0, 2, 1)
         active = (self.sh_degree + 1) ** 2
-        if active >= sh_coeff.shape[-1]:
-            # the warm-up mask is all ones: multiplying by it is the identity
-            rgb = ops.compute_sh(sh_coeff, direction)
+        if self.cfg.fused_view_colour and fused.sh_rgb_supported(shs):
+            rgb = fused.sh_rgb(shs, position, camera_center, active)
         else:
-            sh_mask = torch.zeros_like(sh_coeff)
-            sh_mask[..., :active] = 1.0
-            rgb = ops.compute_sh(sh_coeff * sh_mask, direction)
-        rgb = (rgb + 0.5).clamp(min=0.0)
+            direction = position - camera_center.reshape(1, 3).expand(n, 3)
+            direction = direction / direction.norm(dim=1, keepdim=True)
+            sh_coeff = shs.permute(0, 2, 1)
+            if active >= sh_coeff.shape[-1]:
+                # the warm-up mask is all ones: multiplying by it is the identity
+                rgb = ops.compute_sh(sh_coeff, direction)
+            else:
+                sh_mask = torch.zeros_like(sh_coeff)
+                sh_mask[..., :active] = 1.0
+                rgb = ops.compute_sh(sh_coeff * sh_mask, direction)
+            rgb = (rgb + 0.5).clamp(min=0.0)
 
         extr = extrinsic_matrix[:3, :]
         uv, depth = ops.project_point(position, intrinsic_params, extr, width, height,
@@ -121,8 +129,10 @@ class MsplatRender:
             raise ValueError("ndc does not have grad") from e
         image = ops.rasterize(uv, conic, opacity, packed, depth, radius, tiles_touched,
                               self.bg_color, width, height, ndc,
-                              recompute=self.cfg.recompute_backward)
+                              recompute=self.cfg.recompute_backward,
+                              capacity=self.cfg.sort_capacity or None)
         return {
+            "rendered_features": image,
             "rendered_features_split": render_features.split(image),
             "uv_points": ndc,
             "visibility": radius > 0,

@@ -1,0 +1,152 @@
+"""Fused caller-side passes against the torch compositions they replace.
+
+Bars: forward values within 1e-6 (relative to the largest entry) of the
+float64 composition; gradients within 1e-5 relative to the largest
+gradient entry (they are short float32 chains); the loss gradient equal to
+torch's l1_loss + w * mse_loss gradient to 1 ulp.
+"""
+import pytest
+import torch
+import torch.nn.functional as F
+
+from oracle import msplat_cpu as O
+from pointrix_gb300 import fused, ops
+from pointrix_gb300 import workloads as WL
+from pointrix_gb300.optim import Adam
+from pointrix_gb300.renderer import MsplatRender
+
+pytestmark = pytest.mark.gpu
+DEV = "cuda"
+
+
+def rel(a, b):
+    if b is None:          # no dependence in the reference: expect zeros
+        return float(a.detach().abs().max())
+    a, b = a.detach().double().cpu(), b.detach().double().cpu()
+    return float((a - b).abs().max() / b.abs().max().clamp(min=1e-30))
+
+
+def torch_activations(ls, q, lg):
+    """The reference composition in float64 (gaussian_points.py:70-80,
+    examples/supervise/model.py:50-62 with pose.py's matrix)."""
+    s = torch.exp(ls)
+    r = F.normalize(q, dim=-1)
+    o = torch.sigmoid(lg)
+    idx = torch.argmin(ls, dim=-1)
+    w, x, y, z = r.unbind(-1)
+    cols = torch.stack([
+        torch.stack([x * x - y * y - z * z + w * w, 2 * (x * y + z * w), 2 * (x * z - y * w)], -1),
+        torch.stack([2 * (x * y - z * w), -x * x + y * y - z * z + w * w, 2 * (y * z + x * w)], -1),
+        torch.stack([2 * (x * z + y * w), 2 * (y * z - x * w), -x * x - y * y + z * z + w * w], -1),
+    ], 1)                                           # [N, axis, 3]
+    nrm = cols[torch.arange(ls.shape[0]), idx]
+    return s, r, o, F.normalize(nrm, dim=-1)
+
+
+def test_gaussian_activations_match_torch():
+    g = torch.Generator().manual_seed(0)
+    n = 50_000
+    ls = torch.randn(n, 3, generator=g) * 0.7 - 4
+    ls[:100, 1] = ls[:100, 0]                  # ties: the first minimum wins
+    q = torch.randn(n, 4, generator=g)
+    lg = torch.randn(n, 1, generator=g) * 1.5
+    ups = [torch.randn(n, c, generator=g) for c in (3, 4, 1, 3)]
+    leaves64 = [t.double().requires_grad_(True) for t in (ls, q, lg)]
+    ref = torch_activations(*leaves64)
+    torch.autograd.backward(ref, [u.double() for u in ups])
+    leaves = [t.to(DEV).requires_grad_(True) for t in (ls, q, lg)]
+    out = fused.gaussian_activations(*leaves)
+    for a, b in zip(out, ref):
+        assert rel(a, b) < 1e-6
+    torch.autograd.backward(out, [u.to(DEV) for u in ups])
+    for a, b in zip(leaves, leaves64):
+        assert rel(a.grad, b.grad) < 1e-5
+    # without the normal
+    s, r, o, nrm = fused.gaussian_activations(*[t.detach() for t in leaves], normals=False)
+    assert nrm is None and torch.equal(s, out[0]) and torch.equal(r, out[1])
+
+
+@pytest.mark.parametrize("K,active", [(16, 16), (16, 4), (16, 9), (9, 9), (4, 1), (1, 1)])
+def test_sh_rgb_matches_composition(K, active):
+    g = torch.Generator().manual_seed(K * 10 + active)
+    n = 20_000 + 13                            # a partial last warp block
+    shs = torch.randn(n, K, 3, generator=g) * 0.3
+    pos = torch.randn(n, 3, generator=g) * 1.5
+    center = torch.tensor([0.3, -4.0, 2.5])
+    up = torch.randn(n, 3, generator=g)
+    # float64 composition: direction, mask, compute_sh, +0.5, clamp
+    s64, p64, c64 = (t.double().requires_grad_(True) for t in (shs, pos, center))
+    d = p64 - c64.reshape(1, 3)
+    d = d / d.norm(dim=1, keepdim=True)
+    mask = torch.zeros(1, 3, K, dtype=torch.float64)
+    mask[..., :active] = 1
+    ref = (O.compute_sh(s64.permute(0, 2, 1) * mask, d) + 0.5).clamp(min=0)
+    ref.backward(up.double())
+    sg, pg, cg = (t.to(DEV).requires_grad_(True) for t in (shs, pos, center))
+    out = fused.sh_rgb(sg, pg, cg, active)
+    assert rel(out, ref) < 1e-6
+    out.backward(up.to(DEV))
+    assert rel(sg.grad, s64.grad) < 1e-5
+    assert float(sg.grad[:, active:].abs().max()) == 0.0 if active < K else True
+    assert rel(pg.grad, p64.grad) < 1e-5
+    assert rel(cg.grad, c64.grad) < 1e-5
+
+
+def test_l1_l2_loss_matches_torch():
+    g = torch.Generator().manual_seed(5)
+    x = torch.rand(7, 106, 160, generator=g).to(DEV).requires_grad_(True)
+    t = torch.rand(7, 106, 160, generator=g).to(DEV)
+    t.view(-1)[:1000] = x.detach().view(-1)[:1000]     # zero differences: sign 0
+    x2 = x.detach().clone().requires_grad_(True)
+    ref = F.l1_loss(x2, t) + 0.2 * F.mse_loss(x2, t)
+    ref.backward()
+    loss = fused.l1_l2_loss(x, t, 0.2)
+    assert abs(float(loss) - float(ref)) <= 1e-6 * float(ref)
+    loss.backward()
+    assert float((x.grad - x2.grad).abs().max()) <= 2 ** -23 * float(x2.grad.abs().max())
+    # an odd length (scalar tail) and a scaled upstream gradient
+    y = torch.rand(1001, generator=g).to(DEV).requires_grad_(True)
+    u = torch.rand(1001, generator=g).to(DEV)
+    (3.0 * fused.l1_l2_loss(y, u, 0.5)).backward()
+    y2 = y.detach().clone().requires_grad_(True)
+    (3.0 * (F.l1_loss(y2, u) + 0.5 * F.mse_loss(y2, u))).backward()
+    assert rel(y.grad, y2.grad) < 1e-6
+
+
+def test_capturable_adam_matches_host_steps():
+    g = torch.Generator().manual_seed(2)
+    ps = [torch.randn(1000, 3, generator=g).to(DEV) for _ in range(3)]
+    grads = [[torch.randn(1000, 3, generator=g).to(DEV) for _ in ps] for _ in range(5)]
+    runs = []
+    for capturable in (False, True):
+        leaves = [p.clone().requires_grad_(True) for p in ps]
+        opt = Adam([{"params": leaves[:2], "lr": 1e-2}, {"params": leaves[2:], "lr": 5e-3}],
+                   capturable=capturable)
+        for step in grads:
+            for p, gr in zip(leaves, step):
+                p.grad = gr.clone()
+            opt.step()
+        runs.append(leaves)
+    for a, b in zip(*runs):
+        assert rel(b, a) < 1e-6
+
+
+def test_renderer_fused_colour_matches_unfused():
+    scene, cam = WL.scene_small(0)
+    cam = cam.to(DEV)
+    outs, grads = [], []
+    for fused_on in (True, False):
+        leaves = [t.to(DEV).requires_grad_(True) for t in scene.activated()]
+        pos, sc, q, op, shs = leaves
+        shs3 = shs.detach().repeat(1, 16, 1).contiguous().requires_grad_(True)  # K = 16
+        r = MsplatRender(MsplatRender.Config(render_depth=True, fused_view_colour=fused_on))
+        r.sh_degree = 2
+        out = r.render_iter(cam.H, cam.W, cam.extr, cam.intr, cam.center, pos, op, sc, q, shs3)
+        img = out["rendered_features"]
+        img.backward(torch.ones_like(img))
+        outs.append(img.detach())
+        grads.append([pos.grad, shs3.grad])
+    assert float((outs[0] - outs[1]).abs().max()) < 1e-5
+    for a, b in zip(*grads):
+        assert rel(a, b) < 1e-4
+    ops.check_device_status()
