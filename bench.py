@@ -379,10 +379,14 @@ MULTIVIEW_WORKLOAD = ("batched multi-view: 3,000,000 Gaussians SH3, 16 views on 
 
 
 def multiview_measure(device, n=3_000_000, views=16, steps=3):
-    """Mpix/s of one batched forward+backward over all views against the
-    per-view loop of plain launches (MsplatRender.render_batch's order)."""
-    from pointrix_gb300 import multiview
+    """Mpix/s of the batched forward+backward over all views -- one sort and
+    one blend launch each way for the whole batch, the step captured once as
+    a CUDA graph and replayed -- against the per-view loop of plain launches
+    (MsplatRender.render_batch's order, a host read of K per view).  Both
+    compute the same images (the largest difference is reported)."""
+    from pointrix_gb300 import fused, multiview, ops
     from pointrix_gb300 import workloads as WL
+    from pointrix_gb300.graph import GraphedStep
     from pointrix_gb300.renderer import MsplatRender
 
     scene = WL.scene_sh3(3, n).to(device).leaves()
@@ -394,39 +398,73 @@ def multiview_measure(device, n=3_000_000, views=16, steps=3):
     r = MsplatRender(MsplatRender.Config(render_depth=True), device=device)
     r.sh_degree = 3
     F = torch.nn.functional
+    last = {}
 
     def per_view():
+        zero_grads(params)
         pos, sc, q, op, shs = scene.activated()
-        loss = 0.0
+        loss, imgs = 0.0, []
         for cam, tgt in zip(cams, targets):
             out = r.render_iter(cam.H, cam.W, cam.extr, cam.intr, cam.center, pos, op, sc, q, shs)
-            f = out["rendered_features_split"]
-            loss = loss + F.l1_loss(torch.cat([f["rgb"], f["depth"]], 0), tgt)
+            img = out["rendered_features"]
+            imgs.append(img)
+            loss = loss + F.l1_loss(img, tgt)
         loss.backward()
+        last["per_view"] = [i.detach() for i in imgs]   # no autograd graph kept alive
+
+    cap = {}
 
     def batched():
-        pos, sc, q, op, shs = scene.activated()
-        imgs, _, _ = multiview.render_views(pos, sc, q, op, shs, cams)
-        loss = sum(F.l1_loss(img, tgt) for img, tgt in zip(imgs, targets))
-        loss.backward()
-
-    res = {}
-    for name, fn in (("per_view_loop", per_view), ("batched", batched)):
         zero_grads(params)
+        pos, sc, q, op, shs = scene.activated()
+        imgs, _, _ = multiview.render_views(pos, sc, q, op, shs, cams, capacity=cap.get("k"))
+        loss = fused.l1_l2_loss(imgs[0], targets[0], 0.0)
+        for img, tgt in zip(imgs[1:], targets[1:]):
+            loss = loss + fused.l1_l2_loss(img, tgt, 0.0)
+        loss.backward()
+        last["batched"] = [i.detach() for i in imgs]
+        return loss
+
+    def timed(fn):
         fn()
         torch.cuda.synchronize(device)
         times = []
         for _ in range(steps):
-            zero_grads(params)
             torch.cuda.synchronize(device)
             t0 = time.perf_counter()
             fn()
             torch.cuda.synchronize(device)
             times.append(time.perf_counter() - t0)
         ms = 1e3 * statistics.mean(times)
-        res[name] = {"ms_per_step": ms, "mpix_per_s": pix / (ms * 1e-3) / 1e6}
-    res["speedup"] = res["per_view_loop"]["ms_per_step"] / res["batched"]["ms_per_step"]
-    return {"workload": MULTIVIEW_WORKLOAD, "pixels_per_step": pix, **res}
+        return {"ms_per_step": ms, "mpix_per_s": pix / (ms * 1e-3) / 1e6}
+
+    res = {"per_view_loop": timed(per_view)}
+    per_view_imgs = [t.detach().clone() for t in last["per_view"]]
+    k_batch = multiview_k(scene, cams)
+    cap["k"] = int(1.15 * k_batch) + (1 << 20)
+    graphed = GraphedStep(batched, warmup=1, device=device)
+    res["batched_graph"] = timed(graphed)
+    ops.check_device_status(device)
+    diff = max(float((a - b).abs().max()) for a, b in zip(per_view_imgs, last["batched"]))
+    res["speedup"] = res["per_view_loop"]["ms_per_step"] / res["batched_graph"]["ms_per_step"]
+    return {"workload": MULTIVIEW_WORKLOAD, "pixels_per_step": pix, "K_entries": k_batch,
+            "max_abs_image_diff": diff, **res}
+
+
+def multiview_k(scene, cams):
+    """Total (element, tile) entries of a batch of views (host side)."""
+    from pointrix_gb300 import ops
+    total = 0
+    with torch.no_grad():
+        pos, sc, q, op, shs = scene.activated()
+        for cam in cams:
+            E = cam.extr[:3]
+            uv, depth = ops.project_point(pos, cam.intr, E, cam.W, cam.H)
+            vis = depth != 0
+            cov = ops.compute_cov3d(sc, q, vis)
+            _, radius, tiles = ops.ewa_project(pos, cov, cam.intr, E, uv, cam.W, cam.H, vis)
+            total += int(tiles[radius > 0].sum())
+    return total
 
 
 # -------------------------------------------------------- recompute mode ---

@@ -18,7 +18,7 @@ import ctypes as C
 
 import torch
 
-from . import _lib, ops
+from . import _lib, fused, ops
 from ._lib import call
 from .ops import _c, _ptr, _status_word, _stream, _timed
 
@@ -122,19 +122,32 @@ def blend_views(uv, conic, opacity, feature, ids, tile_range, bg, sizes, n_per_v
 
 
 def render_views(position, scaling, rotation, opacity, shs, cams, bg=0.0, render_depth=True,
-                 extra_features=None, nearest=ops.NEAREST_DEFAULT):
+                 extra_features=None, nearest=ops.NEAREST_DEFAULT, capacity=None, sh_active=None):
     """Renders every camera of ``cams`` (objects with W, H, intr [1,4] or [4],
     extr [4,4] world->camera, center [3]) in one batch.  Features are
-    rgb (+ depth) (+ ``extra_features`` [N,c]) as in ``MsplatRender``.
+    rgb (+ depth) (+ ``extra_features`` [N,c]) as in ``MsplatRender``; the
+    colour uses the first ``sh_active`` SH coefficients (all when None).
+    ``capacity`` keeps the batch's K on the device (see :func:`sort_views`),
+    so the whole call can be captured in a CUDA graph.
     Returns (list of [C,H,W] images, list of per-view uv, list of radius)."""
     n = position.shape[0]
+    K = shs.shape[1]
+    active = K if sh_active is None else sh_active
     uvs, depths, conics, radii, tiles, feats = [], [], [], [], [], []
+    use_fused = fused.sh_rgb_supported(shs)
     shc = shs.permute(0, 2, 1)
     for cam in cams:
-        center = cam.center.reshape(1, 3)
-        d = position - center
-        d = d / d.norm(dim=1, keepdim=True)
-        rgb = (ops.compute_sh(shc, d) + 0.5).clamp(min=0.0)
+        if use_fused:
+            rgb = fused.sh_rgb(shs, position, cam.center, active)
+        else:
+            d = position - cam.center.reshape(1, 3)
+            d = d / d.norm(dim=1, keepdim=True)
+            sh_in = shc
+            if active < K:
+                mask = torch.zeros_like(shc)
+                mask[..., :active] = 1.0
+                sh_in = shc * mask
+            rgb = (ops.compute_sh(sh_in, d) + 0.5).clamp(min=0.0)
         extr = cam.extr[:3, :]
         uv, depth = ops.project_point(position, cam.intr, extr, cam.W, cam.H, nearest=nearest)
         vis = depth != 0
@@ -145,7 +158,8 @@ def render_views(position, scaling, rotation, opacity, shs, cams, bg=0.0, render
         radii.append(radius); tiles.append(nt); feats.append(torch.cat(f, 1))
     sizes = [(cam.W, cam.H) for cam in cams]
     uv_all, conic_all = torch.cat(uvs), torch.cat(conics)
-    ids, rng = sort_views(uv_all, torch.cat(depths), torch.cat(radii), torch.cat(tiles), sizes, n)
+    ids, rng = sort_views(uv_all, torch.cat(depths), torch.cat(radii), torch.cat(tiles), sizes, n,
+                          capacity=capacity)
     op_all = opacity.reshape(1, n).expand(len(cams), n).reshape(-1)
     imgs = blend_views(uv_all, conic_all, op_all, torch.cat(feats), ids, rng, bg, sizes, n)
     return imgs, uvs, radii

@@ -66,3 +66,26 @@ def test_view_count_limits():
                               torch.zeros(0, dtype=torch.int32, device="cuda"),
                               torch.zeros(1, 2, dtype=torch.int32, device="cuda"), 0.0,
                               [(16, 16)] * 65, 10)
+
+
+def test_batched_views_capacity_mode_in_a_graph():
+    """The batch with K kept on the device, captured once and replayed:
+    the same images as the host-K batch."""
+    from pointrix_gb300.graph import GraphedStep
+    cams = _cams()
+    leaves = [t.detach() for t in _leaves()]
+    ref, _, _ = multiview.render_views(*leaves, cams, bg=0.1)
+    K = sum(int(r.numel()) for r in ref)           # an ample capacity: entries <= pixels * N
+    cap = 64 * K
+
+    def fn():
+        imgs, _, _ = multiview.render_views(*leaves, cams, bg=0.1, capacity=cap)
+        return imgs
+
+    graphed = GraphedStep(fn, warmup=1)
+    for _ in range(2):
+        out = graphed()
+        torch.cuda.synchronize()
+        for a, b in zip(ref, out):
+            assert torch.equal(a, b)
+    ops.check_device_status()
