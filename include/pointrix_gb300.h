@@ -332,6 +332,17 @@ int pgb_l1_l2_loss_forward(const float* x, const float* target, int64_t n, float
 int pgb_l1_l2_loss_backward(const float* x, const float* target, int64_t n, float w,
                             const float* d_loss, float* d_x, void* stream);
 
+/* pgb_densify_accumulate: the densification statistics update of
+ * DensificationController.preprocess (pointrix/controller/gs.py:318-333,
+ * gradient from accumulate_viewspace_grad, gs.py:260-284) for the points
+ * with radius > 0: max_radii[i] = max(max_radii[i], radius[i]);
+ * grad_accum[i] += |(d_uv[i].x * sx, d_uv[i].y * sy)|; acc_steps[i] += 1.
+ * d_uv [N,2] (8-byte aligned) is the screen-space gradient (summed over the
+ * views of a batch), sx = W/2, sy = H/2 with normalize_grad (else 1). */
+int pgb_densify_accumulate(const float* d_uv, int64_t n, const int32_t* radius, float sx,
+                           float sy, float* grad_accum, float* acc_steps, float* max_radii,
+                           void* stream);
+
 #ifdef __cplusplus
 }
 #endif

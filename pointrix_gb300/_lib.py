@@ -64,6 +64,7 @@ SIGNATURES.update({
     "pgb_l1_l2_loss_scratch_doubles": [i64],
     "pgb_l1_l2_loss_forward": [vp, vp, i64, f32, vp, i64, vp, vp],
     "pgb_l1_l2_loss_backward": [vp, vp, i64, f32, vp, vp, vp],
+    "pgb_densify_accumulate": [vp, i64, vp, f32, f32, vp, vp, vp, vp],
 })
 
 _RESTYPES = {"pgb_status_string": C.c_char_p, "pgb_camera_grad_scratch_bytes": szt}

@@ -13,16 +13,22 @@
 // last-contributor count.
 //
 // GB300 design:
-//  * pack: one pass writes a 64- or 128-byte record per Gaussian
-//    (u, v, a, b, c, o, f_0..f_{C-1}, zero padding) so that a splat is one
-//    16-byte aligned contiguous block;
-//  * forward/backward: one CTA of 256 threads per tile, one pixel per
-//    thread.  The tile's sorted ids are consumed in batches of 256; each
-//    thread issues a TMA bulk copy (cp.async.bulk, no multicast) of one
-//    record into a double-buffered shared-memory stage that completes on an
-//    mbarrier, so batch b+1 streams in while batch b is composited.  Every
-//    mbarrier wait is bounded; on expiry the CTA records PGB_ERR_TIMEOUT,
-//    drains its own copies (bounded again) and returns;
+//  * pack: one pass writes a record per Gaussian (u, v, a, b, c, o, tau,
+//    thr, f_0..f_{C-1}, zero padding: 48 to 144 bytes) so that a splat is
+//    one 16-byte aligned contiguous block read with 16-byte loads;
+//  * forward/backward: one CTA of 128 threads per tile, two pixels per
+//    thread; each warp owns an 8x8 pixel box and, per batch, culls the
+//    staged splats against it (exact minimum of the conic over the box) into
+//    a list, so every per-splat step serves 64 pixels.  The tile's sorted
+//    ids are consumed in batches of 128.  Forward: each thread issues a TMA
+//    bulk copy (cp.async.bulk, no multicast) of one record into a
+//    double-buffered shared-memory stage that completes on an mbarrier, so
+//    batch b+1 streams in while batch b is composited; every mbarrier wait
+//    is bounded, and on expiry the CTA records PGB_ERR_TIMEOUT, drains its
+//    own copies (bounded again) and returns.  Backward: the same stage
+//    filled with 16-byte cp.async copies;
+//  * the alpha test is a comparison of the exponent with a per-splat
+//    threshold -ln(255 o), before the exponential;
 //  * forward early exit per CTA (__syncthreads_count) and per warp;
 //  * backward: per-Gaussian gradients are summed across the warp with a
 //    reduce-scatter butterfly (16 shuffles for 16 values instead of 80),
@@ -32,8 +38,7 @@
 
 namespace pgb {
 
-constexpr int kBlendThreads = 256;
-constexpr int kBatch = 256;
+constexpr int kBatch = 256;  // default batch of the culling helper
 constexpr uint32_t kWaitLimit = 1u << 22;
 
 // ---------------------------------------------------------------- PTX helpers
@@ -88,18 +93,18 @@ __device__ __forceinline__ float splat_power(float a, float b, float c, float dx
   return __fmaf_rn(-0.5f, q, -bxy);
 }
 
-// Issue the bulk copies of one batch: thread t fetches the record of list
-// entry first + t (if below last) into stage slot t.  One arrive per warp
-// carries the warp's byte count (the barrier expects kBlendThreads/32
-// arrivals per phase).
+// Issue the bulk copies of one batch of B records: thread t fetches the
+// record of list entry first + t (+ NT, ...) (if below last) into stage slot
+// t.  One arrive per warp carries the warp's byte count (the barrier expects
+// NT/32 arrivals per phase).
 // Ids outside [0, n) (a corrupt list) are recorded in `info` and their
 // copies skipped; the byte count expected on the barrier counts only the
 // copies issued, so the phase still completes.
-template <int RF, int NT = kBatch>
+template <int RF, int NT, int B>
 __device__ inline void issue_batch(const float* __restrict__ records,
                                    const int32_t* __restrict__ ids, int64_t first, int64_t last,
                                    int64_t n, float* stage, uint64_t* bar, int64_t* info) {
-  constexpr int PER = kBatch / NT;  // slots per thread
+  constexpr int PER = B / NT;  // slots per thread
   const int lane = threadIdx.x & 31;
   int32_t g[PER];
   bool ok[PER];
@@ -122,12 +127,12 @@ __device__ inline void issue_batch(const float* __restrict__ records,
 
 // Stage one batch with cp.async: thread t copies the records of slots
 // t, t + NT, ... (16 bytes per instruction) and commits one group.
-template <int RF, int NT>
+template <int RF, int NT, int B>
 __device__ inline void stage_batch(const float* __restrict__ records,
                                    const int32_t* __restrict__ ids, int64_t first, int64_t last,
                                    int64_t n, float* stage, int64_t* info) {
 #pragma unroll
-  for (int k = 0; k < kBatch / NT; ++k) {
+  for (int k = 0; k < B / NT; ++k) {
     const int slot = threadIdx.x + k * NT;
     const int64_t e = first + slot;
     if (e < last) {
@@ -146,13 +151,13 @@ __device__ inline void stage_batch(const float* __restrict__ records,
 }
 
 // ------------------------------------------------------------------ pack
-// Record of one splat: u, v, a, b, c, o, tau, f_0..f_{C-1}, zero padding to
-// a multiple of 4 floats.  tau bounds the splat's support: alpha >= 1/255
+// Record of one splat: u, v, a, b, c, o, tau, thr, f_0..f_{C-1}, zero
+// padding to a multiple of 4 floats.  tau bounds the splat's support: alpha >= 1/255
 // requires Q(d) = a dx^2 + 2 b dx dy + c dy^2 <= 2 ln(255 o); tau is that
 // level plus a small margin, -1 when o < 1/255 (the splat never passes the
 // alpha test) and +inf when the conic is not positive definite (no bound).
-constexpr int kRecFeat = 7;  // offset of the first feature in a record
-__host__ __device__ constexpr int rec_floats(int C) { return ((kRecFeat + C + 3) / 4) * 4; }
+constexpr int kRecFeat = 8;  // offset of the first feature in a record (16-byte aligned)
+__host__ __device__ constexpr int rec_floats(int C) { return kRecFeat + ((C + 3) / 4) * 4; }
 __host__ __device__ constexpr int grad_floats(int C) { return 6 + C <= 16 ? 16 : 32; }
 
 template <int RF>
@@ -180,6 +185,10 @@ __global__ void pack_kernel(const float* __restrict__ uv, const float* __restric
     else
       tau = __int_as_float(0x7f800000);  // +inf: never culled
     r[6] = tau;
+    // alpha >= 1/255 <=> power >= -ln(255 o): the per-pair test before the
+    // exponential (never passes for o <= 0; a NaN opacity keeps NaN, which
+    // no comparison rejects, as the alpha test did not)
+    r[7] = o > 0.f ? -logf(255.0f * o) : __int_as_float(0x7f800000);
 #pragma unroll
     for (int k = 0; k < RF - kRecFeat; ++k) r[kRecFeat + k] = k < C ? feature[i * C + k] : 0.f;
     float4* dst = reinterpret_cast<float4*>(records + i * RF);
@@ -232,14 +241,14 @@ __device__ __forceinline__ bool splat_may_touch_box(const float* rec, float x0, 
 // Builds this warp's list of batch slots (in increasing order) whose splat
 // may touch the warp's pixel box; slots >= cnt are ignored.  Returns the
 // list length.
-template <int BW, int BH>
+template <int BW, int BH, int B = kBatch>
 __device__ __forceinline__ int warp_cull(const float* stage, int RF, int cnt, float x0, float y0,
                                          uint8_t* list) {
   const int lane = threadIdx.x & 31;
   const uint32_t lt = (1u << lane) - 1u;
   int n = 0;
 #pragma unroll
-  for (int k = 0; k < kBatch / 32; ++k) {
+  for (int k = 0; k < B / 32; ++k) {
     const int j = k * 32 + lane;
     const bool keep = j < cnt && splat_may_touch_box<BW, BH>(stage + j * RF, x0, y0);
     const uint32_t m = __ballot_sync(0xffffffffu, keep);
@@ -251,101 +260,137 @@ __device__ __forceinline__ int warp_cull(const float* stage, int RF, int cnt, fl
 }
 
 // --------------------------------------------------------------- forward
+// 128 threads per tile, two pixels per thread: warp w owns the 8x8 box at
+// (8 (w % 2), 8 (w / 2)); lane l owns pixels (l % 8, l / 8) and
+// (l % 8, l / 8 + 4), the layout of the backward.  Every culling test,
+// list entry and record read serves 64 pixels.  Batches of 128 records,
+// one TMA bulk copy per thread per batch.
+constexpr int kFwdThreads = 128;
+constexpr int kFwdPix = 2;
+constexpr int kFwdBatch = 128;
+
 template <int NC, int RF>
-__global__ void __launch_bounds__(kBlendThreads) blend_fwd_kernel(
+__global__ void __launch_bounds__(kFwdThreads) blend_fwd_kernel(
     const float* __restrict__ records, const int32_t* __restrict__ ids,
     const int2* __restrict__ ranges, int64_t n, float bg, const ViewTable vt, int C,
     float* __restrict__ out, float* __restrict__ final_T, int32_t* __restrict__ n_contrib,
     int64_t* __restrict__ info) {
   extern __shared__ __align__(128) float smem[];
   __shared__ __align__(8) uint64_t bars[2];
+  __shared__ uint8_t s_list[kFwdThreads / 32][kFwdBatch];
 
-  __shared__ uint8_t s_list[kBlendThreads / 32][kBatch];
   const int tile = blockIdx.x;  // global tile (of its view, for a batch)
   int W, H, gx, ltile;
   int64_t pbase;
   tile_view(vt, tile, W, H, gx, ltile, pbase);
-  int px, py, bx0, by0;
-  tile_pixel(ltile, gx, px, py, bx0, by0);
-  const bool inside = px < W && py < H;
-  const float pxf = (float)px, pyf = (float)py;
-  uint8_t* my_list = s_list[threadIdx.x >> 5];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int bx0 = (ltile % gx) * kTile + 8 * (w & 1);
+  const int by0 = (ltile / gx) * kTile + 8 * (w >> 1);
+  uint8_t* my_list = s_list[w];
 
   if (threadIdx.x == 0) {
-    mbar_init(&bars[0], kBlendThreads / 32);
-    mbar_init(&bars[1], kBlendThreads / 32);
+    mbar_init(&bars[0], kFwdThreads / 32);
+    mbar_init(&bars[1], kFwdThreads / 32);
     fence_mbar_init();
   }
   __syncthreads();
 
   const int2 rg = ranges[tile];
   const int64_t start = rg.x, end = rg.y;
-  const int nb = end > start ? (int)((end - start + kBatch - 1) / kBatch) : 0;
+  const int nb = end > start ? (int)((end - start + kFwdBatch - 1) / kFwdBatch) : 0;
 
-  float acc[NC];
+  const int px = bx0 + (lane & 7);
+  float pyf[kFwdPix], T[kFwdPix], acc[kFwdPix][NC];
+  int last[kFwdPix];
+  bool done[kFwdPix], inside[kFwdPix];
+  const float pxf = (float)px;
 #pragma unroll
-  for (int c = 0; c < NC; ++c) acc[c] = 0.f;
-  float T = 1.f;
-  int last = 0;
-  bool done = !inside;
+  for (int q = 0; q < kFwdPix; ++q) {
+    const int py = by0 + (lane >> 3) + 4 * q;
+    pyf[q] = (float)py;
+    inside[q] = px < W && py < H;
+    done[q] = !inside[q];
+    T[q] = 1.f;
+    last[q] = 0;
+#pragma unroll
+    for (int c = 0; c < NC; ++c) acc[q][c] = 0.f;
+  }
   bool timed_out = false;
 
-  if (nb > 0) issue_batch<RF>(records, ids, start, end, n, smem, &bars[0], info);
+  if (nb > 0)
+    issue_batch<RF, kFwdThreads, kFwdBatch>(records, ids, start, end, n, smem, &bars[0], info);
   for (int b = 0; b < nb; ++b) {
     const int buf = b & 1;
-    const int64_t first = start + (int64_t)b * kBatch;
+    const int64_t first = start + (int64_t)b * kFwdBatch;
     if (b + 1 < nb)
-      issue_batch<RF>(records, ids, first + kBatch, end, n, smem + (buf ^ 1) * kBatch * RF,
-                      &bars[buf ^ 1], info);
+      issue_batch<RF, kFwdThreads, kFwdBatch>(records, ids, first + kFwdBatch, end, n,
+                                              smem + (buf ^ 1) * kFwdBatch * RF, &bars[buf ^ 1],
+                                              info);
     // every thread observes the phase (that makes the TMA writes visible to
     // it); the outcome is made block-uniform before any warp collective
     timed_out = __syncthreads_or(!mbar_wait_bounded(&bars[buf], (b >> 1) & 1));
     if (timed_out && threadIdx.x == 0) set_info(info, PGB_ERR_TIMEOUT);
-    const int cnt = (int)(end - first < kBatch ? end - first : kBatch);
-    const float* st = smem + buf * kBatch * RF;
-    if (!timed_out && !__all_sync(0xffffffffu, done)) {
-      const int nl = warp_cull<8, 4>(st, RF, cnt, (float)bx0, (float)by0, my_list);
-      if (!done) {
-        for (int t = 0; t < nl; ++t) {
-          const int j = my_list[t];
-          const float4 r0 = *reinterpret_cast<const float4*>(st + j * RF);
-          const float2 r1 = *reinterpret_cast<const float2*>(st + j * RF + 4);
-          const float dx = __fsub_rn(r0.x, pxf), dy = __fsub_rn(r0.y, pyf);
-          const float power = splat_power(r0.z, r0.w, r1.x, dx, dy);
-          if (power > 0.f) continue;
-          const float alpha = fminf(0.99f, __fmul_rn(r1.y, __expf(power)));
-          if (alpha < (1.0f / 255.0f)) continue;
-          const float test_T = __fmul_rn(T, __fsub_rn(1.0f, alpha));
-          if (test_T < 1e-4f) {
-            done = true;
-            break;
-          }
-          const float w = alpha * T;
-          const float* f = st + j * RF + kRecFeat;
+    const int cnt = (int)(end - first < kFwdBatch ? end - first : kFwdBatch);
+    const float* st = smem + buf * kFwdBatch * RF;
+    bool all_done = true;
 #pragma unroll
-          for (int c = 0; c < NC; ++c) acc[c] = fmaf(f[c], w, acc[c]);
-          T = test_T;
-          last = (int)(first - start) + j + 1;
+    for (int q = 0; q < kFwdPix; ++q) all_done &= done[q];
+    if (!timed_out && !__all_sync(0xffffffffu, all_done)) {
+      const int nl = warp_cull<8, 8, kFwdBatch>(st, RF, cnt, (float)bx0, (float)by0, my_list);
+      const int base = (int)(first - start) + 1;
+      for (int t = 0; t < nl; ++t) {
+        const int j = my_list[t];
+        const float* rec = st + j * RF;
+        const float4 r0 = *reinterpret_cast<const float4*>(rec);
+        const float4 r1 = *reinterpret_cast<const float4*>(rec + 4);
+        const float dx = __fsub_rn(r0.x, pxf);
+        bool live = false;
+#pragma unroll
+        for (int q = 0; q < kFwdPix; ++q) {
+          if (done[q]) continue;
+          live = true;
+          const float dy = __fsub_rn(r0.y, pyf[q]);
+          const float power = splat_power(r0.z, r0.w, r1.x, dx, dy);
+          if (power > 0.f || power < r1.w) continue;  // alpha < 1/255: no exp needed
+          const float alpha = fminf(0.99f, __fmul_rn(r1.y, __expf(power)));
+          const float test_T = __fmul_rn(T[q], __fsub_rn(1.0f, alpha));
+          if (test_T < 1e-4f) {
+            done[q] = true;
+            continue;
+          }
+          const float wgt = alpha * T[q];
+          const float* f = rec + kRecFeat;
+#pragma unroll
+          for (int c = 0; c < NC; ++c) acc[q][c] = fmaf(f[c], wgt, acc[q][c]);
+          T[q] = test_T;
+          last[q] = base + j;
         }
+        if (!live) break;
       }
       __syncwarp();
     }
-    const int ndone = __syncthreads_count(done || timed_out);
-    if (ndone == kBlendThreads || timed_out) {
+    bool mine_done = true;
+#pragma unroll
+    for (int q = 0; q < kFwdPix; ++q) mine_done &= done[q];
+    const int ndone = __syncthreads_count(mine_done || timed_out);
+    if (ndone == kFwdThreads || timed_out) {
       if (b + 1 < nb && !mbar_wait_bounded(&bars[buf ^ 1], ((b + 1) >> 1) & 1))
         set_info(info, PGB_ERR_TIMEOUT);
       break;
     }
   }
 
-  if (inside) {
+  const int64_t plane = (int64_t)W * H;
+#pragma unroll
+  for (int q = 0; q < kFwdPix; ++q) {
+    if (!inside[q]) continue;
+    const int py = by0 + (lane >> 3) + 4 * q;
     const int64_t pix = (int64_t)py * W + px;
-    const int64_t plane = (int64_t)W * H;
 #pragma unroll
     for (int c = 0; c < NC; ++c)
-      if (c < C) out[C * pbase + c * plane + pix] = acc[c] + T * bg;
-    final_T[pbase + pix] = T;
-    n_contrib[pbase + pix] = last;
+      if (c < C) out[C * pbase + c * plane + pix] = acc[q][c] + T[q] * bg;
+    final_T[pbase + pix] = T[q];
+    n_contrib[pbase + pix] = last[q];
   }
 }
 
@@ -375,6 +420,10 @@ __device__ __forceinline__ float warp_reduce_scatter(float (&v)[GR]) {
 // and culling test serves 64 pixels.
 constexpr int kBwdThreads = 128;
 constexpr int kBwdPix = 2;
+// 128 splats per batch: the double-buffered stage and the per-splat
+// gradient sums stay near 25 KB, so registers, not shared memory, bound the
+// CTAs per SM.
+constexpr int kBwdBatch = 128;
 
 template <int NC>
 struct BwdPixel {
@@ -391,14 +440,13 @@ __device__ __forceinline__ bool bwd_pixel(BwdPixel<NC>& P, int j, const float* r
                                           float (&v)[GR]) {
   if (j >= P.nc) return false;
   const float4 r0 = *reinterpret_cast<const float4*>(rec);
-  const float2 r1 = *reinterpret_cast<const float2*>(rec + 4);
+  const float4 r1 = *reinterpret_cast<const float4*>(rec + 4);
   const float dx = __fsub_rn(r0.x, P.pxf), dy = __fsub_rn(r0.y, P.pyf);
   const float power = splat_power(r0.z, r0.w, r1.x, dx, dy);
-  if (power > 0.f) return false;
+  if (power > 0.f || power < r1.w) return false;  // the forward's skip test
   const float G = __expf(power);
   const float araw = __fmul_rn(r1.y, G);
   const float alpha = fminf(0.99f, araw);
-  if (alpha < (1.0f / 255.0f)) return false;
   const float om = __fsub_rn(1.0f, alpha);
   P.T = __fdividef(P.T, om);
   const float* f = rec + kRecFeat;
@@ -433,9 +481,9 @@ __global__ void __launch_bounds__(kBwdThreads) blend_bwd_kernel(
   static_assert(GR == 16 || GR == 32, "gradient records are 16 or 32 floats");
   extern __shared__ __align__(128) float smem[];
   __shared__ int s_max_nc;
-  __shared__ uint8_t s_touched[kBatch];
-  __shared__ uint8_t s_list[kBwdThreads / 32][kBatch];
-  float* gacc = smem + 2 * kBatch * RF;  // [kBatch][GR]
+  __shared__ uint8_t s_touched[kBwdBatch];
+  __shared__ uint8_t s_list[kBwdThreads / 32][kBwdBatch];
+  float* gacc = smem + 2 * kBwdBatch * RF;  // [kBwdBatch][GR]
 
   const int tile = blockIdx.x;  // global tile (of its view, for a batch)
   int W, H, gx, ltile;
@@ -447,8 +495,8 @@ __global__ void __launch_bounds__(kBwdThreads) blend_bwd_kernel(
   uint8_t* my_list = s_list[w];
 
   if (threadIdx.x == 0) s_max_nc = 0;
-  for (int i = threadIdx.x; i < kBatch * GR; i += kBwdThreads) gacc[i] = 0.f;
-  for (int i = threadIdx.x; i < kBatch; i += kBwdThreads) s_touched[i] = 0;
+  for (int i = threadIdx.x; i < kBwdBatch * GR; i += kBwdThreads) gacc[i] = 0.f;
+  for (int i = threadIdx.x; i < kBwdBatch; i += kBwdThreads) s_touched[i] = 0;
   __syncthreads();
 
   const int64_t plane = (int64_t)W * H;
@@ -487,29 +535,32 @@ __global__ void __launch_bounds__(kBwdThreads) blend_bwd_kernel(
   const int list_len = max(0, rg.y - rg.x);
   if (s_max_nc > list_len && threadIdx.x == 0) set_info(info, PGB_ERR_OVERFLOW);
   const int max_nc = min(s_max_nc, list_len);
-  const int nb = (max_nc + kBatch - 1) / kBatch;
+  const int nb = (max_nc + kBwdBatch - 1) / kBwdBatch;
 
-  // batch b covers list positions [hi_b - kBatch, hi_b) with hi_b = max_nc - b*kBatch,
-  // clipped at 0; slot t holds position lo_b + t.
-  auto lo_of = [&](int b) { return max(0, max_nc - (b + 1) * kBatch); };
-  auto hi_of = [&](int b) { return max_nc - b * kBatch; };
+  // batch b covers list positions [hi_b - kBwdBatch, hi_b) with
+  // hi_b = max_nc - b*kBwdBatch, clipped at 0; slot t holds position lo_b + t.
+  auto lo_of = [&](int b) { return max(0, max_nc - (b + 1) * kBwdBatch); };
+  auto hi_of = [&](int b) { return max_nc - b * kBwdBatch; };
 
   if (nb > 0)
-    stage_batch<RF, kBwdThreads>(records, ids, start + lo_of(0), start + hi_of(0), n, smem, info);
+    stage_batch<RF, kBwdThreads, kBwdBatch>(records, ids, start + lo_of(0), start + hi_of(0), n,
+                                            smem, info);
   for (int b = 0; b < nb; ++b) {
     const int buf = b & 1;
     const int lo = lo_of(b), hi = hi_of(b);
     if (b + 1 < nb) {
-      stage_batch<RF, kBwdThreads>(records, ids, start + lo_of(b + 1), start + hi_of(b + 1), n,
-                                   smem + (buf ^ 1) * kBatch * RF, info);
+      stage_batch<RF, kBwdThreads, kBwdBatch>(records, ids, start + lo_of(b + 1),
+                                              start + hi_of(b + 1), n,
+                                              smem + (buf ^ 1) * kBwdBatch * RF, info);
       cp_async_wait<1>();  // this thread's copies of batch b have landed
     } else {
       cp_async_wait<0>();
     }
     __syncthreads();  // ... and everyone's
-    const float* st = smem + buf * kBatch * RF;
+    const float* st = smem + buf * kBwdBatch * RF;
     {
-      const int nl = warp_cull<8, 8>(st, RF, min(hi, warp_nc) - lo, (float)bx0, (float)by0, my_list);
+      const int nl = warp_cull<8, 8, kBwdBatch>(st, RF, min(hi, warp_nc) - lo, (float)bx0,
+                                               (float)by0, my_list);
       for (int t = nl - 1; t >= 0; --t) {
         const int slot = my_list[t];
         const int j = lo + slot;
@@ -585,12 +636,12 @@ static int launch_fwd_nc(const float* records, const int32_t* ids, const int2* r
                          float bg, const ViewTable& vt, int tiles, int C, float* out, float* fT,
                          int32_t* ncon, int64_t* info, cudaStream_t s) {
   constexpr int RF = rec_floats(NC);
-  const size_t smem = 2 * kBatch * RF * sizeof(float);
+  const size_t smem = 2 * kFwdBatch * RF * sizeof(float);
   auto kern = blend_fwd_kernel<NC, RF>;
   if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
       cudaSuccess)
     return PGB_ERR_CUDA;
-  kern<<<tiles, kBlendThreads, smem, s>>>(records, ids, ranges, n, bg, vt, C, out, fT, ncon, info);
+  kern<<<tiles, kFwdThreads, smem, s>>>(records, ids, ranges, n, bg, vt, C, out, fT, ncon, info);
   return launch_status();
 }
 
@@ -601,7 +652,7 @@ static int launch_bwd_nc(const float* records, const int32_t* ids, const int2* r
                          cudaStream_t s) {
   constexpr int RF = rec_floats(NC);
   constexpr int GR = grad_floats(NC);
-  const size_t smem = (2 * RF + GR) * kBatch * sizeof(float);
+  const size_t smem = (2 * RF + GR) * kBwdBatch * sizeof(float);
   auto kern = blend_bwd_kernel<NC, RF, GR>;
   if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
       cudaSuccess)

@@ -150,3 +150,37 @@ def test_renderer_fused_colour_matches_unfused():
     for a, b in zip(*grads):
         assert rel(a, b) < 1e-4
     ops.check_device_status()
+
+
+def test_densification_stats_match_controller():
+    """One kernel against the controller's masked torch update
+    (pointrix/controller/gs.py:318-333), two views, normalize_grad on."""
+    from pointrix_gb300.densify import DensificationStats
+    g = torch.Generator().manual_seed(8)
+    n, W, H = 30_000, 640, 480
+    st = DensificationStats(n, DEV, normalize_grad=True)
+    ga, ac, mr = torch.zeros(n, 1), torch.zeros(n, 1), torch.zeros(n)
+    for step in range(3):
+        uvs, rads = [], []
+        for v in range(2):
+            p = torch.zeros(n, 2, requires_grad=True)
+            p.grad = torch.randn(n, 2, generator=g) * 1e-3
+            r = torch.randint(-2, 30, (n,), generator=g).clamp(min=0).to(torch.int32)
+            uvs.append(p); rads.append(r)
+        # reference update (accumulate_viewspace_grad + preprocess)
+        vg = uvs[0].grad.clone() + uvs[1].grad
+        vg[..., 0] *= W / 2.0
+        vg[..., 1] *= H / 2.0
+        radii = torch.stack(rads).max(dim=0).values
+        vis = torch.stack([r > 0 for r in rads]).any(dim=0)
+        mr[vis] = torch.max(mr[vis], radii[vis])
+        ga[vis] += torch.norm(vg[vis, :2], dim=-1, keepdim=True)
+        ac[vis] += 1
+        dev_uvs = [t.detach().to(DEV).requires_grad_(True) for t in uvs]
+        for a, b in zip(dev_uvs, uvs):
+            a.grad = b.grad.to(DEV)
+        st.preprocess([r.to(DEV) for r in rads], dev_uvs, W, H)
+    assert torch.equal(st.acc_steps.cpu(), ac) and torch.equal(st.max_radii.cpu(), mr)
+    assert rel(st.grad_accum, ga) < 1e-6
+    avg = st.average_grad()
+    assert not bool(avg.isnan().any())
