@@ -31,16 +31,27 @@ __device__ __forceinline__ void adam_one(float& p, float g, float& m, float& v, 
 }
 
 // Step counts on the device (graph-captured steps): every segment's count
-// goes up by one, and its bias corrections 1 - beta^t are formed once, in
-// double as the host does, for the update to read.
+// goes up by one, and its bias corrections 1 - beta^t are formed once for
+// the update to read.  beta^t is the double product of t factors, by binary
+// powering over the bits of t (a few multiplies, not a pow per step).
+__device__ inline double pow_int(double b, int t) {
+  double r = 1.0;
+  while (t > 0) {
+    if (t & 1) r *= b;
+    b *= b;
+    t >>= 1;
+  }
+  return r;
+}
+
 __global__ void adam_tick_kernel(int32_t* __restrict__ steps, float* __restrict__ bc, int nseg,
                                  double b1d, double b2d) {
   const int s = threadIdx.x;
   if (s < nseg) {
     const int t = steps[s] + 1;
     steps[s] = t;
-    bc[2 * s] = (float)(1.0 - pow(b1d, (double)t));
-    bc[2 * s + 1] = (float)(1.0 - pow(b2d, (double)t));
+    bc[2 * s] = (float)(1.0 - pow_int(b1d, t));
+    bc[2 * s + 1] = (float)(1.0 - pow_int(b2d, t));
   }
 }
 

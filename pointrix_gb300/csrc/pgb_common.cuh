@@ -161,8 +161,18 @@ __device__ inline double column_sum(const T* __restrict__ v, int nrows, int stri
   static_assert((TPC & (TPC - 1)) == 0, "TPC must be a power of two");
   const int col = threadIdx.x / TPC, j = threadIdx.x % TPC;
   double acc = 0.0;
-  if (col < NCOL)
-    for (int b = j; b < nrows; b += TPC) acc += (double)v[(size_t)b * stride + col];
+  if (col < NCOL) {
+    // eight rows' loads in flight at a time, added in row order
+    int b = j;
+    for (; b + 7 * TPC < nrows; b += 8 * TPC) {
+      T x[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) x[u] = v[(size_t)(b + u * TPC) * stride + col];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) acc += (double)x[u];
+    }
+    for (; b < nrows; b += TPC) acc += (double)v[(size_t)b * stride + col];
+  }
   s[threadIdx.x] = acc;
   __syncthreads();
   for (int h = TPC / 2; h > 0; h >>= 1) {

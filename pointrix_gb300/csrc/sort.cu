@@ -493,20 +493,25 @@ __global__ void __launch_bounds__(kSortThreads) scan_rect_kernel(
 // ---------------------------------------------------------------------------
 // 3c. emission of (tile id, Gaussian id) pairs over output chunks
 //
-// A persistent grid walks the output chunks: for chunk b, entries
+// The output is cut into chunks of kEmitChunk entries; each CTA of a
+// persistent grid emits a contiguous range of chunks.  For chunk b, entries
 // [b*kEmitChunk, min(K, (b+1)*kEmitChunk)), the CTA stages the emission
-// records of the Gaussians that own them in shared memory; each
-// thread takes 4 consecutive entries, finds the owner of the first by binary
-// search and walks forward; the pairs are staged in shared memory and
-// written with 16-byte stores.  Every chunk is the same amount of work
-// however unevenly the tiles are spread over Gaussians.  The tile digit
-// histograms of the chunks a CTA emitted are accumulated in shared memory
-// (one atomic per run of equal digits within a warp) and added to the global
-// histograms once per CTA.  The grid also sets the tile-range table to
-// (INT_MAX, 0) for the last tile pass.
+// records of the Gaussians that own them in shared memory; each thread takes
+// 4 consecutive entries, finds the owner of the first by binary search and
+// walks forward; the pairs are staged in shared memory and written with
+// 16-byte stores.  Every chunk is the same amount of work however unevenly
+// the tiles are spread over Gaussians.  The chunk boundaries of a range are
+// read up front and the next chunk's owner records travel by cp.async into
+// the second of two stages while the current chunk is emitted, so no chunk
+// waits on a chain of global loads.  The tile digit histograms of the
+// chunks a CTA emitted are accumulated in shared memory (one atomic per run
+// of equal digits within a warp) and added to the global histograms once per
+// CTA.  The grid also sets the tile-range table to (INT_MAX, 0) for the last
+// tile pass.
 // ---------------------------------------------------------------------------
 constexpr int kEmitPer = kEmitChunk / kEmitThreads;  // 4
-constexpr int kEmitBlocksPerSM = 7;
+constexpr int kEmitBlocksPerSM = 4;
+constexpr int kEmitSeg = 256;  // chunk boundaries held in shared memory at a time
 
 __global__ void __launch_bounds__(kEmitThreads) emit_kernel(
     const uint4* __restrict__ owner, const uint32_t* __restrict__ chunk_first, int64_t n_sorted,
@@ -514,106 +519,132 @@ __global__ void __launch_bounds__(kEmitThreads) emit_kernel(
     uint32_t* __restrict__ tkeys, uint32_t* __restrict__ tvals, uint32_t* __restrict__ tile_hist,
     int2* __restrict__ range, uint32_t T, int64_t* __restrict__ info) {
   constexpr int CAP = kEmitChunk + 1;
-  // (first tile, w | gx << 16, g, offset) of the chunk's owners
-  __shared__ __align__(16) uint4 s_own[CAP];
+  // (first tile, w | gx << 16, g, offset) of a chunk's owners, two stages
+  __shared__ __align__(16) uint4 s_own[2][CAP];
   __shared__ __align__(16) uint32_t s_key[kEmitChunk];
   __shared__ __align__(16) uint32_t s_val[kEmitChunk];
   __shared__ uint32_t s_hist[kTileHistWords];
+  __shared__ uint32_t s_cf[kEmitSeg + 1];
   for (int64_t i = (int64_t)blockIdx.x * kEmitThreads + threadIdx.x; i < T;
        i += (int64_t)gridDim.x * kEmitThreads)
     range[i] = make_int2(INT_MAX, 0);
   const int64_t K = pass_count(k_dev, k_cap);
   const int64_t nchunks = (K + kEmitChunk - 1) / kEmitChunk;
-  if ((int64_t)blockIdx.x >= nchunks) return;
+  const int64_t per = (nchunks + gridDim.x - 1) / gridDim.x;
+  const int64_t c0 = (int64_t)blockIdx.x * per;
+  const int64_t c1 = min(nchunks, c0 + per);
+  if (c0 >= c1) return;
   const int R = 1 << digit_bits;
   const uint32_t lane = threadIdx.x & 31;
   for (int i = threadIdx.x; i < tile_passes * R; i += kEmitThreads) s_hist[i] = 0;
 
-  for (int64_t b = blockIdx.x; b < nchunks; b += gridDim.x) {
-    const int64_t e0 = b * kEmitChunk;
-    const int64_t e1 = min(K, e0 + kEmitChunk);
-    // owners of this chunk's first entry and of the next chunk's first entry
-    // (for the last chunk: of entry K - 1)
-    const int64_t i0 = chunk_first[b];
-    const int64_t i1 = chunk_first[b + 1];
-    const int64_t m = i1 - i0 + 1;
-    const bool ok_range = i0 <= i1 && i1 < n_sorted;
-    if (!ok_range && threadIdx.x == 0) set_error(info, PGB_ERR_OVERFLOW);
-    const bool staged = ok_range && m <= CAP;
-    __syncthreads();  // the previous chunk is out of the staging arrays
-    if (staged)
-      for (int64_t i = threadIdx.x; i < m; i += kEmitThreads) s_own[i] = owner[i0 + i];
+  for (int64_t seg = c0; seg < c1; seg += kEmitSeg) {
+    const int nseg = c1 - seg < (int64_t)kEmitSeg ? (int)(c1 - seg) : kEmitSeg;
+    __syncthreads();  // the previous segment is out of s_cf and the stages
+    // owners of each chunk's first entry, and of the next chunk's first
+    // entry (for the last chunk: of entry K - 1)
+    for (int i = threadIdx.x; i <= nseg; i += kEmitThreads) s_cf[i] = chunk_first[seg + i];
     __syncthreads();
-    const int64_t ebeg = e0 + (int64_t)threadIdx.x * kEmitPer;
-    if (ok_range && ebeg < e1) {
-      auto own_at = [&](int64_t p) -> uint4 { return staged ? s_own[p] : owner[i0 + p]; };
-      auto off_at = [&](int64_t p) -> int64_t { return staged ? s_own[p].w : owner[i0 + p].w; };
-      // owner of ebeg: the last position p in [0, i1 - i0] with offs <= ebeg
-      int64_t lo = 0, hi = i1 - i0;
-      while (lo < hi) {
-        const int64_t mid = (lo + hi + 1) >> 1;
-        if (off_at(mid) <= ebeg) lo = mid; else hi = mid - 1;
+    // chunk q of the segment -> stage buf (one commit group per call)
+    auto stage = [&](int q, int buf) {
+      const int64_t i0 = s_cf[q], i1 = s_cf[q + 1];
+      const int64_t m = i1 - i0 + 1;
+      if (i0 <= i1 && i1 < n_sorted && m <= CAP)
+        for (int64_t i = threadIdx.x; i < m; i += kEmitThreads)
+          cp_async16(&s_own[buf][i], owner + i0 + i);
+      cp_async_commit();
+    };
+    stage(0, 0);
+    for (int qc = 0; qc < nseg; ++qc) {
+      const int buf = qc & 1;
+      if (qc + 1 < nseg) {
+        stage(qc + 1, buf ^ 1);
+        cp_async_wait<1>();  // this thread's copies of chunk q have landed
+      } else {
+        cp_async_wait<0>();
       }
-      int64_t own = lo;
-      int64_t next_off = own < i1 - i0 ? off_at(own + 1) : INT64_MAX;
-      uint32_t g = 0, t0 = 0, w = 0, gx = 0, row = 0, col = 0;
-      bool fresh = true;
-      for (int j = 0; j < kEmitPer; ++j) {
-        const int64_t e = ebeg + j;
-        if (e >= e1) break;
-        while (e >= next_off) {  // walk to the owner of e (skips zero-count Gaussians)
-          ++own;
-          next_off = own < i1 - i0 ? off_at(own + 1) : INT64_MAX;
-          fresh = true;
+      __syncthreads();  // ... and everyone's; the previous chunk is written out
+      const int64_t b = seg + qc;
+      const int64_t e0 = b * kEmitChunk;
+      const int64_t e1 = min(K, e0 + kEmitChunk);
+      const int64_t i0 = s_cf[qc];
+      const int64_t i1 = s_cf[qc + 1];
+      const int64_t m = i1 - i0 + 1;
+      const bool ok_range = i0 <= i1 && i1 < n_sorted;
+      if (!ok_range && threadIdx.x == 0) set_error(info, PGB_ERR_OVERFLOW);
+      const bool staged = ok_range && m <= CAP;
+      const int64_t ebeg = e0 + (int64_t)threadIdx.x * kEmitPer;
+      if (ok_range && ebeg < e1) {
+        const uint4* so = s_own[buf];
+        auto own_at = [&](int64_t p) -> uint4 { return staged ? so[p] : owner[i0 + p]; };
+        auto off_at = [&](int64_t p) -> int64_t { return staged ? so[p].w : owner[i0 + p].w; };
+        // owner of ebeg: the last position p in [0, i1 - i0] with offs <= ebeg
+        int64_t lo = 0, hi = i1 - i0;
+        while (lo < hi) {
+          const int64_t mid = (lo + hi + 1) >> 1;
+          if (off_at(mid) <= ebeg) lo = mid; else hi = mid - 1;
         }
-        if (fresh) {  // first entry of this owner for the thread: position by division
-          const uint4 o = own_at(own);
-          t0 = o.x;
-          w = o.y & 0xFFFFu;
-          gx = o.y >> 16;
-          g = o.z;
-          const uint32_t jj = (uint32_t)(e - o.w);
-          row = w ? jj / w : 0u;
-          col = jj - row * w;
-          fresh = false;
-        } else if (++col == w) {  // next entry of the same owner: next column / row
-          col = 0;
-          ++row;
+        int64_t own = lo;
+        int64_t next_off = own < i1 - i0 ? off_at(own + 1) : INT64_MAX;
+        uint32_t g = 0, t0 = 0, w = 0, gx = 0, row = 0, col = 0;
+        bool fresh = true;
+        for (int j = 0; j < kEmitPer; ++j) {
+          const int64_t e = ebeg + j;
+          if (e >= e1) break;
+          while (e >= next_off) {  // walk to the owner of e (skips zero-count Gaussians)
+            ++own;
+            next_off = own < i1 - i0 ? off_at(own + 1) : INT64_MAX;
+            fresh = true;
+          }
+          if (fresh) {  // first entry of this owner for the thread: position by division
+            const uint4 o = own_at(own);
+            t0 = o.x;
+            w = o.y & 0xFFFFu;
+            gx = o.y >> 16;
+            g = o.z;
+            const uint32_t jj = (uint32_t)(e - o.w);
+            row = w ? jj / w : 0u;
+            col = jj - row * w;
+            fresh = false;
+          } else if (++col == w) {  // next entry of the same owner: next column / row
+            col = 0;
+            ++row;
+          }
+          s_key[threadIdx.x * kEmitPer + j] = t0 + row * gx + col;
+          s_val[threadIdx.x * kEmitPer + j] = g;
         }
-        s_key[threadIdx.x * kEmitPer + j] = t0 + row * gx + col;
-        s_val[threadIdx.x * kEmitPer + j] = g;
       }
-    }
-    __syncthreads();
-    // coalesced write-out; digit histograms, consecutive keys read by
-    // consecutive lanes: a lane whose digit differs from its left neighbour's
-    // heads a run and adds the run's length
-    const int cnt = ok_range ? (int)(e1 - e0) : 0;
-    if (cnt == kEmitChunk) {
-      for (int q = threadIdx.x; q < kEmitChunk / 4; q += kEmitThreads) {
-        reinterpret_cast<uint4*>(tkeys + e0)[q] = reinterpret_cast<const uint4*>(s_key)[q];
-        reinterpret_cast<uint4*>(tvals + e0)[q] = reinterpret_cast<const uint4*>(s_val)[q];
+      __syncthreads();
+      // coalesced write-out; digit histograms, consecutive keys read by
+      // consecutive lanes: a lane whose digit differs from its left neighbour's
+      // heads a run and adds the run's length
+      const int cnt = ok_range ? (int)(e1 - e0) : 0;
+      if (cnt == kEmitChunk) {
+        for (int q = threadIdx.x; q < kEmitChunk / 4; q += kEmitThreads) {
+          reinterpret_cast<uint4*>(tkeys + e0)[q] = reinterpret_cast<const uint4*>(s_key)[q];
+          reinterpret_cast<uint4*>(tvals + e0)[q] = reinterpret_cast<const uint4*>(s_val)[q];
+        }
+      } else {
+        for (int q = threadIdx.x; q < cnt; q += kEmitThreads) {
+          tkeys[e0 + q] = s_key[q];
+          tvals[e0 + q] = s_val[q];
+        }
       }
-    } else {
-      for (int q = threadIdx.x; q < cnt; q += kEmitThreads) {
-        tkeys[e0 + q] = s_key[q];
-        tvals[e0 + q] = s_val[q];
-      }
-    }
-    for (int q0 = 0; q0 < cnt; q0 += kEmitThreads) {
-      const int q = q0 + threadIdx.x;
-      const bool valid = q < cnt;
-      const uint32_t nvalid = __popc(__ballot_sync(0xffffffffu, valid));
-      const uint32_t tid = valid ? s_key[q] : 0u;
-      for (int p = 0; p < tile_passes; ++p) {
-        const uint32_t d = (tid >> (digit_bits * p)) & (uint32_t)(R - 1);
-        const uint32_t left = __shfl_up_sync(0xffffffffu, d, 1);
-        const bool head = valid && (lane == 0 || left != d);
-        const uint32_t heads = __ballot_sync(0xffffffffu, head);
-        if (head) {
-          const uint32_t above = heads & ~((2u << lane) - 1u);
-          const uint32_t next = above ? (uint32_t)(__ffs(above) - 1) : nvalid;
-          atomicAdd(&s_hist[p * R + d], next - lane);
+      for (int q0 = 0; q0 < cnt; q0 += kEmitThreads) {
+        const int q = q0 + threadIdx.x;
+        const bool valid = q < cnt;
+        const uint32_t nvalid = __popc(__ballot_sync(0xffffffffu, valid));
+        const uint32_t tid = valid ? s_key[q] : 0u;
+        for (int p = 0; p < tile_passes; ++p) {
+          const uint32_t d = (tid >> (digit_bits * p)) & (uint32_t)(R - 1);
+          const uint32_t left = __shfl_up_sync(0xffffffffu, d, 1);
+          const bool head = valid && (lane == 0 || left != d);
+          const uint32_t heads = __ballot_sync(0xffffffffu, head);
+          if (head) {
+            const uint32_t above = heads & ~((2u << lane) - 1u);
+            const uint32_t next = above ? (uint32_t)(__ffs(above) - 1) : nvalid;
+            atomicAdd(&s_hist[p * R + d], next - lane);
+          }
         }
       }
     }
