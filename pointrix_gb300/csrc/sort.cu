@@ -14,11 +14,12 @@
 //   2. four onesweep passes sort the N Gaussians by depth (stable, so equal
 //      depths stay in id order);
 //   3. rect: each Gaussian's tile rectangle and entry count (coalesced, in
-//      id order); scan_rect: a single-pass decoupled-look-back scan of the
-//      counts in depth order gives each Gaussian its output offset; emit
-//      then writes the (tile id, Gaussian id) pairs chunk by chunk of the
-//      output (load-balanced however unevenly the tiles are spread over
-//      Gaussians) and accumulates the tile digit histograms;
+//      id order), and the tile digit histograms of all its entries (one
+//      update per rectangle row); scan_rect: a single-pass decoupled-look-back
+//      scan of the counts in depth order gives each Gaussian its output
+//      offset; emit then writes the (tile id, Gaussian id) pairs chunk by
+//      chunk of the output (load-balanced however unevenly the tiles are
+//      spread over Gaussians);
 //   4. one stable onesweep pass for T <= 256 tiles, two 8-bit passes up to
 //      65,536 tiles, two 9-bit passes up to 2^18 (batches of views), else
 //      three, sort the pairs by tile id; the last pass writes only the ids
@@ -376,34 +377,141 @@ static int launch_onesweep(int parts, cudaStream_t s, const uint32_t* ki, const 
 }
 
 // ---------------------------------------------------------------------------
-// 3a. tile rectangles in Gaussian order (coalesced)
+// 3a. tile rectangles in Gaussian order (coalesced), and the tile-digit
+//     histograms of every pair that will be emitted
 //
 // rect[g] = (first tile, w | h << 16, row stride gx, count): the global id
 // of the rectangle's top-left tile (the view's first tile added), its size
 // in tiles, the tile-grid width of g's view, and the number of entries g
 // emits (tiles_touched when radius > 0, else 0).  A count that disagrees
 // with the rectangle is reported as PGB_ERR_MISMATCH.
+//
+// Emission writes entry j of g as tile first + (j / w) gx + j % w for
+// j < count (one row of `count` tiles when w = 0): runs of consecutive tile
+// ids, one per rectangle row.  A run [a, a + len) adds to the low digit's
+// histogram one range of consecutive digits (mod R) plus len / R full
+// cycles -- two or four updates of a shared difference array -- and to a
+// higher digit's histogram at most ceil(len / R) + 1 counted digits.  The
+// CTA turns its difference array into counts and adds its histograms to
+// the global ones once.
 // ---------------------------------------------------------------------------
+__device__ inline void hist_run(uint32_t a, uint32_t len, int passes, int bits, int R,
+                                int* __restrict__ s_diff, uint32_t* __restrict__ s_full,
+                                uint32_t* __restrict__ s_hist) {
+  if (len == 0) return;
+  // low digit: len / R full cycles, then len % R consecutive digits from a's
+  const uint32_t full = len >> bits, rem = len & (uint32_t)(R - 1);
+  if (full) atomicAdd(s_full, full);
+  if (rem) {
+    const uint32_t d = a & (uint32_t)(R - 1), e = d + rem;
+    atomicAdd(&s_diff[d], 1);
+    if (e <= (uint32_t)R) {
+      atomicSub(&s_diff[e], 1);
+    } else {  // wraps past digit R - 1
+      atomicAdd(&s_diff[0], 1);
+      atomicSub(&s_diff[e - R], 1);
+    }
+  }
+  for (int p = 1; p < passes; ++p) {
+    const int sh = bits * p;
+    const uint32_t last = a + len - 1;
+    for (uint32_t v = a >> sh; v <= (last >> sh); ++v) {
+      const uint32_t lo = max(a, v << sh), hi = min(last, ((v + 1) << sh) - 1);
+      atomicAdd(&s_hist[p * R + (v & (uint32_t)(R - 1))], hi - lo + 1);
+    }
+  }
+}
+
 __global__ void __launch_bounds__(kStreamThreads) rect_kernel(
     const float* __restrict__ uv, const int32_t* __restrict__ radius,
-    const int32_t* __restrict__ tiles, int64_t n, ViewTable vt, uint4* __restrict__ rect,
-    int64_t* __restrict__ info) {
-  for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < n;
-       g += (int64_t)gridDim.x * blockDim.x) {
-    const int r = radius[g];
+    const int32_t* __restrict__ tiles, int64_t n, ViewTable vt, int tile_passes, int digit_bits,
+    uint4* __restrict__ rect, uint32_t* __restrict__ tile_hist, int64_t* __restrict__ info) {
+  constexpr int NW = kStreamThreads / 32;
+  __shared__ int s_diff[513];
+  __shared__ uint32_t s_hist[kTileHistWords];
+  __shared__ uint32_t s_full;
+  __shared__ uint32_t s_warp_tot[NW];
+  __shared__ uint4 s_rect[NW][32];      // the warp's rectangles
+  __shared__ uint32_t s_runs[NW][33];   // exclusive prefix of their run counts
+  const int R = 1 << digit_bits;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int i = threadIdx.x; i < 513; i += blockDim.x) s_diff[i] = 0;
+  for (int i = threadIdx.x; i < kTileHistWords; i += blockDim.x) s_hist[i] = 0;
+  if (threadIdx.x == 0) s_full = 0;
+  __syncthreads();
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t base = (int64_t)blockIdx.x * blockDim.x + warp * 32; base < n; base += stride) {
+    const int64_t g = base + lane;
     uint4 out = make_uint4(0u, 0u, 0u, 0u);
-    if (r > 0) {
-      const float2 p = reinterpret_cast<const float2*>(uv)[g];
-      int gx, gy, x0, x1, y0, y1;
-      uint32_t tile_base;
-      element_view(vt, (uint32_t)g, gx, gy, tile_base);
-      tile_rect(p.x, p.y, (float)r, gx, gy, x0, x1, y0, y1);
-      const uint32_t cnt = (uint32_t)max(tiles[g], 0);
-      if ((int64_t)(x1 - x0) * (y1 - y0) != (int64_t)cnt) set_error(info, PGB_ERR_MISMATCH);
-      out = make_uint4(tile_base + (uint32_t)y0 * (uint32_t)gx + (uint32_t)x0,
-                       (uint32_t)(x1 - x0) | ((uint32_t)(y1 - y0) << 16), (uint32_t)gx, cnt);
+    uint32_t runs = 0;
+    if (g < n) {
+      const int r = radius[g];
+      if (r > 0) {
+        const float2 p = reinterpret_cast<const float2*>(uv)[g];
+        int gx, gy, x0, x1, y0, y1;
+        uint32_t tile_base;
+        element_view(vt, (uint32_t)g, gx, gy, tile_base);
+        tile_rect(p.x, p.y, (float)r, gx, gy, x0, x1, y0, y1);
+        const uint32_t cnt = (uint32_t)max(tiles[g], 0);
+        const uint32_t w = (uint32_t)(x1 - x0);
+        if ((int64_t)w * (y1 - y0) != (int64_t)cnt) set_error(info, PGB_ERR_MISMATCH);
+        const uint32_t first = tile_base + (uint32_t)y0 * (uint32_t)gx + (uint32_t)x0;
+        out = make_uint4(first, w | ((uint32_t)(y1 - y0) << 16), (uint32_t)gx, cnt);
+        // runs of consecutive tile ids that emission writes for g
+        runs = cnt == 0 ? 0u : (w == 0 ? 1u : cnt / w + (cnt % w ? 1u : 0u));
+      }
+      rect[g] = out;
     }
-    rect[g] = out;
+    // spread the warp's runs over its lanes
+    uint32_t incl = runs;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += y;
+    }
+    s_rect[warp][lane] = out;
+    s_runs[warp][lane + 1] = incl;
+    if (lane == 0) s_runs[warp][0] = 0;
+    __syncwarp();
+    const uint32_t total = s_runs[warp][32];
+    for (uint32_t k = lane; k < total; k += 32) {
+      int lo = 0, hi = 31;  // owner: the last lane whose prefix is <= k
+      while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (s_runs[warp][mid] <= k) lo = mid; else hi = mid - 1;
+      }
+      const uint4 o = s_rect[warp][lo];
+      const uint32_t j = k - s_runs[warp][lo];  // run index within the owner
+      const uint32_t w = o.y & 0xFFFFu, cnt = o.w;
+      uint32_t a, len;
+      if (w == 0) {
+        a = o.x;
+        len = cnt;
+      } else {
+        a = o.x + j * o.z;
+        len = min(w, cnt - j * w);
+      }
+      hist_run(a, len, tile_passes, digit_bits, R, s_diff, &s_full, s_hist);
+    }
+    __syncwarp();
+  }
+  __syncthreads();
+  // low digit: counts = inclusive prefix of the difference array (modular
+  // sums of the signed updates) + the full cycles; then one flush
+  const uint32_t full = s_full;
+  uint32_t carry = 0;
+  for (int base = 0; base < R; base += kStreamThreads) {
+    const int d = base + threadIdx.x;
+    const uint32_t v = (uint32_t)s_diff[d];
+    uint32_t total;
+    const uint32_t ex = block_excl_scan<kStreamThreads>(v, total, s_warp_tot);
+    s_hist[d] = carry + ex + v + full;
+    carry += total;
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < tile_passes * R; i += blockDim.x) {
+    const uint32_t v = s_hist[i];
+    if (v) atomicAdd(tile_hist + i, v);
   }
 }
 
@@ -503,27 +611,24 @@ __global__ void __launch_bounds__(kSortThreads) scan_rect_kernel(
 // the tiles are spread over Gaussians.  The chunk boundaries of a range are
 // read up front and the next chunk's owner records travel by cp.async into
 // the second of two stages while the current chunk is emitted, so no chunk
-// waits on a chain of global loads.  The tile digit histograms of the
-// chunks a CTA emitted are accumulated in shared memory (one atomic per run
-// of equal digits within a warp) and added to the global histograms once per
-// CTA.  The grid also sets the tile-range table to (INT_MAX, 0) for the last
-// tile pass.
+// waits on a chain of global loads.  (The tile digit histograms come from
+// the rectangle pass.)  The grid also sets the tile-range table to
+// (INT_MAX, 0) for the last tile pass.
 // ---------------------------------------------------------------------------
 constexpr int kEmitPer = kEmitChunk / kEmitThreads;  // 4
-constexpr int kEmitBlocksPerSM = 4;
+constexpr int kEmitBlocksPerSM = 5;
 constexpr int kEmitSeg = 256;  // chunk boundaries held in shared memory at a time
 
 __global__ void __launch_bounds__(kEmitThreads) emit_kernel(
     const uint4* __restrict__ owner, const uint32_t* __restrict__ chunk_first, int64_t n_sorted,
-    int64_t k_cap, const int64_t* __restrict__ k_dev, int tile_passes, int digit_bits,
-    uint32_t* __restrict__ tkeys, uint32_t* __restrict__ tvals, uint32_t* __restrict__ tile_hist,
-    int2* __restrict__ range, uint32_t T, int64_t* __restrict__ info) {
+    int64_t k_cap, const int64_t* __restrict__ k_dev, uint32_t* __restrict__ tkeys,
+    uint32_t* __restrict__ tvals, int2* __restrict__ range, uint32_t T,
+    int64_t* __restrict__ info) {
   constexpr int CAP = kEmitChunk + 1;
   // (first tile, w | gx << 16, g, offset) of a chunk's owners, two stages
   __shared__ __align__(16) uint4 s_own[2][CAP];
   __shared__ __align__(16) uint32_t s_key[kEmitChunk];
   __shared__ __align__(16) uint32_t s_val[kEmitChunk];
-  __shared__ uint32_t s_hist[kTileHistWords];
   __shared__ uint32_t s_cf[kEmitSeg + 1];
   for (int64_t i = (int64_t)blockIdx.x * kEmitThreads + threadIdx.x; i < T;
        i += (int64_t)gridDim.x * kEmitThreads)
@@ -534,9 +639,6 @@ __global__ void __launch_bounds__(kEmitThreads) emit_kernel(
   const int64_t c0 = (int64_t)blockIdx.x * per;
   const int64_t c1 = min(nchunks, c0 + per);
   if (c0 >= c1) return;
-  const int R = 1 << digit_bits;
-  const uint32_t lane = threadIdx.x & 31;
-  for (int i = threadIdx.x; i < tile_passes * R; i += kEmitThreads) s_hist[i] = 0;
 
   for (int64_t seg = c0; seg < c1; seg += kEmitSeg) {
     const int nseg = c1 - seg < (int64_t)kEmitSeg ? (int)(c1 - seg) : kEmitSeg;
@@ -615,9 +717,7 @@ __global__ void __launch_bounds__(kEmitThreads) emit_kernel(
         }
       }
       __syncthreads();
-      // coalesced write-out; digit histograms, consecutive keys read by
-      // consecutive lanes: a lane whose digit differs from its left neighbour's
-      // heads a run and adds the run's length
+      // coalesced write-out
       const int cnt = ok_range ? (int)(e1 - e0) : 0;
       if (cnt == kEmitChunk) {
         for (int q = threadIdx.x; q < kEmitChunk / 4; q += kEmitThreads) {
@@ -630,29 +730,7 @@ __global__ void __launch_bounds__(kEmitThreads) emit_kernel(
           tvals[e0 + q] = s_val[q];
         }
       }
-      for (int q0 = 0; q0 < cnt; q0 += kEmitThreads) {
-        const int q = q0 + threadIdx.x;
-        const bool valid = q < cnt;
-        const uint32_t nvalid = __popc(__ballot_sync(0xffffffffu, valid));
-        const uint32_t tid = valid ? s_key[q] : 0u;
-        for (int p = 0; p < tile_passes; ++p) {
-          const uint32_t d = (tid >> (digit_bits * p)) & (uint32_t)(R - 1);
-          const uint32_t left = __shfl_up_sync(0xffffffffu, d, 1);
-          const bool head = valid && (lane == 0 || left != d);
-          const uint32_t heads = __ballot_sync(0xffffffffu, head);
-          if (head) {
-            const uint32_t above = heads & ~((2u << lane) - 1u);
-            const uint32_t next = above ? (uint32_t)(__ffs(above) - 1) : nvalid;
-            atomicAdd(&s_hist[p * R + d], next - lane);
-          }
-        }
-      }
     }
-  }
-  __syncthreads();
-  for (int i = threadIdx.x; i < tile_passes * R; i += kEmitThreads) {
-    const uint32_t v = s_hist[i];
-    if (v) atomicAdd(tile_hist + i, v);
   }
 }
 
@@ -864,15 +942,14 @@ static int sort_finish_impl(const float* uv, const int32_t* radius, const int32_
   uint4* rect = at<uint4>(scratch_n, LN.rect);
   uint32_t* chunk_first = at<uint32_t>(scratch_k, LK.chunk_first);
   int2* range = reinterpret_cast<int2*>(tile_range_out);
-  rect_kernel<<<stream_grid(n), kStreamThreads, 0, s>>>(uv, radius, tiles_touched, n, vt, rect,
-                                                        info);
+  rect_kernel<<<stream_grid(n), kStreamThreads, 0, s>>>(
+      uv, radius, tiles_touched, n, vt, plan.passes, plan.bits, rect, thist, info);
   scan_rect_kernel<<<LN.scan_parts, kSortThreads, 0, s>>>(
       order, n, rect, k, k_dev, at<uint32_t>(scratch_n, LN.scan_status), counters + 4, owner,
       chunk_first, info);
   const int64_t emit_grid = std::min<int64_t>(LK.chunks, (int64_t)kNumSMs * kEmitBlocksPerSM);
   emit_kernel<<<(unsigned)emit_grid, kEmitThreads, 0, s>>>(owner, chunk_first, n, k, k_dev,
-                                                           plan.passes, plan.bits, bufk[0],
-                                                           bufv[0], thist, range, T, info);
+                                                           bufk[0], bufv[0], range, T, info);
   int cur = 0;
   for (int p = 0; p < plan.passes; ++p) {
     const bool last = p == plan.passes - 1;
