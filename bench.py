@@ -467,6 +467,50 @@ def multiview_k(scene, cams):
     return total
 
 
+# --------------------------------------------------------------- SSIM loss ---
+def ssim_measure(device, C=3, H=1060, W=1600, reps=10):
+    """Fused SSIM forward+backward against the torch composition of
+    pointrix/model/loss.py:ssim (conv2d with the 11x11 window), same image."""
+    import math
+    from pointrix_gb300 import fused
+    F = torch.nn.functional
+    g = torch.Generator(device=device).manual_seed(0)
+    y = torch.rand(C, H, W, device=device, generator=g)
+    x = (y + 0.1 * torch.randn(C, H, W, device=device, generator=g)).clamp(0, 1).requires_grad_(True)
+    w1 = torch.tensor([math.exp(-(k - 5) ** 2 / (2 * 1.5 ** 2)) for k in range(11)], device=device)
+    w1 = w1 / w1.sum()
+    win = (w1[:, None] @ w1[None, :])[None, None].expand(C, 1, 11, 11).contiguous()
+
+    def torch_ssim(a, b):
+        conv = lambda t: F.conv2d(t[None], win, padding=5, groups=C)  # noqa: E731
+        mu1, mu2 = conv(a), conv(b)
+        s11, s22, s12 = conv(a * a) - mu1 ** 2, conv(b * b) - mu2 ** 2, conv(a * b) - mu1 * mu2
+        m = ((2 * mu1 * mu2 + 1e-4) * (2 * s12 + 9e-4)) / ((mu1 ** 2 + mu2 ** 2 + 1e-4) * (s11 + s22 + 9e-4))
+        return m.mean()
+
+    res = {"workload": f"SSIM loss forward+backward, {C}x{H}x{W}"}
+    vals = {}
+    for name, fn in (("torch", torch_ssim), ("fused", fused.ssim)):
+        for _ in range(3):
+            x.grad = None
+            fn(x, y).backward()
+        torch.cuda.synchronize(device)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            x.grad = None
+            v = fn(x, y)
+            v.backward()
+        e1.record()
+        torch.cuda.synchronize(device)
+        res[f"{name}_ms"] = e0.elapsed_time(e1) / reps
+        vals[name] = (float(v), x.grad.detach().clone())
+    res["value_abs_diff"] = abs(vals["fused"][0] - vals["torch"][0])
+    gt = vals["torch"][1]
+    res["grad_rel_max"] = float((vals["fused"][1] - gt).abs().max() / gt.abs().max())
+    return res
+
+
 # -------------------------------------------------------- recompute mode ---
 RECOMPUTE_WORKLOAD = ("memory-bound differentiation: 6,000,000 Gaussians SH3, one 3840x2160 view, "
                       "focal 2800, radius 5, RGB+depth, L1 loss, backward to all Gaussian params")
@@ -664,6 +708,7 @@ def run_gb300(args):
     multi = None
     if rank == 0 and not args.no_multiview:
         multi = multiview_measure(device)
+    loss_ssim = ssim_measure(device) if rank == 0 else None
     if rank == 0:
         cpu = None
         if world == 1 and not args.no_cpu_baseline:
@@ -695,6 +740,7 @@ def run_gb300(args):
             "serve": serving,
             "recompute": recompute,
             "multiview": multi,
+            "ssim": loss_ssim,
         }
         print(json.dumps(line), flush=True)
     if world > 1:

@@ -332,6 +332,19 @@ int pgb_l1_l2_loss_forward(const float* x, const float* target, int64_t n, float
 int pgb_l1_l2_loss_backward(const float* x, const float* target, int64_t n, float w,
                             const float* d_loss, float* d_x, void* stream);
 
+/* pgb_ssim_*: the SSIM of pointrix/model/loss.py:71-125 (11x11 Gaussian
+ * window, sigma 1.5, zero padding, C1 = 0.01^2, C2 = 0.03^2, mean over all
+ * pixels) of x against the target y, both `planes` contiguous float planes of
+ * height x width.  The forward writes the mean to ssim_out[0] (device)
+ * through scratch of pgb_ssim_scratch_doubles(...) doubles (fixed-order
+ * sum); the backward reads dL from d_out[0] (device) and writes d_x (y is
+ * not differentiated). */
+int64_t pgb_ssim_scratch_doubles(int planes, int height, int width);
+int pgb_ssim_forward(const float* x, const float* y, int planes, int height, int width,
+                     double* scratch, int64_t scratch_doubles, float* ssim_out, void* stream);
+int pgb_ssim_backward(const float* x, const float* y, int planes, int height, int width,
+                      const float* d_out, float* d_x, void* stream);
+
 /* pgb_densify_accumulate: the densification statistics update of
  * DensificationController.preprocess (pointrix/controller/gs.py:318-333,
  * gradient from accumulate_viewspace_grad, gs.py:260-284) for the points

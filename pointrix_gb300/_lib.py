@@ -65,9 +65,13 @@ SIGNATURES.update({
     "pgb_l1_l2_loss_forward": [vp, vp, i64, f32, vp, i64, vp, vp],
     "pgb_l1_l2_loss_backward": [vp, vp, i64, f32, vp, vp, vp],
     "pgb_densify_accumulate": [vp, i64, vp, f32, f32, vp, vp, vp, vp],
+    "pgb_ssim_scratch_doubles": [i32, i32, i32],
+    "pgb_ssim_forward": [vp, vp, i32, i32, i32, vp, i64, vp, vp],
+    "pgb_ssim_backward": [vp, vp, i32, i32, i32, vp, vp, vp],
 })
 
-_RESTYPES = {"pgb_status_string": C.c_char_p, "pgb_camera_grad_scratch_bytes": szt}
+_RESTYPES = {"pgb_status_string": C.c_char_p, "pgb_camera_grad_scratch_bytes": szt,
+             "pgb_ssim_scratch_doubles": i64}
 
 
 class PgbError(RuntimeError):

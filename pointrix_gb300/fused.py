@@ -12,7 +12,9 @@ forward and one backward:
   sigmoid(logit) and the shortest-axis normal;
 * :func:`sh_rgb` -- clamp(compute_sh(masked sh, normalize(xyz - center)) +
   0.5, min=0), with gradients to sh, xyz and the camera centre;
-* :func:`l1_l2_loss` -- mean|x - t| + w mean((x - t)^2).
+* :func:`l1_l2_loss` -- mean|x - t| + w mean((x - t)^2);
+* :func:`ssim` -- the SSIM of ``pointrix/model/loss.py:71-125`` (one tiled
+  kernel forward, one backward).
 """
 from __future__ import annotations
 
@@ -22,7 +24,7 @@ from . import _lib
 from ._lib import call
 from .ops import _c, _ptr, _stream, _timed
 
-__all__ = ["gaussian_activations", "sh_rgb", "sh_rgb_supported", "l1_l2_loss"]
+__all__ = ["gaussian_activations", "sh_rgb", "sh_rgb_supported", "l1_l2_loss", "ssim"]
 
 
 def _aligned(t: torch.Tensor) -> bool:
@@ -196,3 +198,47 @@ def l1_l2_loss(x, target, w_l2=0.0):
     if not (x.is_cuda and target.is_cuda and x.dtype == torch.float32 and target.dtype == torch.float32):
         raise ValueError("l1_l2_loss takes CUDA float32 tensors")
     return _L1L2.apply(_c16(x), _c16(target.detach()), float(w_l2))
+
+
+# ---------------------------------------------------------------------------
+class _Ssim(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, x, y, planes, H, W):
+        dev = x.device
+        nd = int(_lib.lib().pgb_ssim_scratch_doubles(planes, H, W))
+        scratch = torch.empty(max(nd, 1), dtype=torch.float64, device=dev)
+        out = torch.empty((), dtype=torch.float32, device=dev)
+        with _timed("ssim_fwd", dev, 2):
+            call("pgb_ssim_forward", _ptr(x), _ptr(y), planes, H, W, _ptr(scratch), nd, _ptr(out),
+                 _stream(dev))
+        ctx.save_for_backward(x, y)
+        ctx.dims = (planes, H, W)
+        return out
+
+    @staticmethod
+    def backward(ctx, d_out):
+        x, y = ctx.saved_tensors
+        planes, H, W = ctx.dims
+        dx = torch.empty_like(x)
+        with _timed("ssim_bwd", x.device, 1):
+            call("pgb_ssim_backward", _ptr(x), _ptr(y), planes, H, W, _ptr(_c(d_out.reshape(1))),
+                 _ptr(dx), _stream(x.device))
+        return dx, None, None, None, None
+
+
+def ssim(img1, img2, window_size=11, size_average=True):
+    """SSIM of ``img1`` against the target ``img2`` ([C,H,W] or [B,C,H,W]),
+    as ``pointrix/model/loss.py:ssim`` with its defaults (11x11 window,
+    sigma 1.5, mean over everything); differentiable in ``img1`` (``img2`` is
+    treated as a constant target)."""
+    if window_size != 11 or not size_average:
+        raise ValueError("fused ssim supports window_size=11, size_average=True")
+    if img1.shape != img2.shape or img1.dim() not in (3, 4):
+        raise ValueError(f"ssim takes two [C,H,W] or [B,C,H,W] images of one shape, got "
+                         f"{tuple(img1.shape)} and {tuple(img2.shape)}")
+    if not (img1.is_cuda and img2.is_cuda and img1.dtype == torch.float32
+            and img2.dtype == torch.float32):
+        raise ValueError("ssim takes CUDA float32 images")
+    H, W = img1.shape[-2], img1.shape[-1]
+    planes = img1.numel() // (H * W)
+    return _Ssim.apply(_c(img1), _c(img2.detach()), planes, H, W)

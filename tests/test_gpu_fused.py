@@ -184,3 +184,40 @@ def test_densification_stats_match_controller():
     assert rel(st.grad_accum, ga) < 1e-6
     avg = st.average_grad()
     assert not bool(avg.isnan().any())
+
+
+def _ssim_reference(x, y):
+    """pointrix/model/loss.py:ssim in float64 (conv2d with the separable
+    Gaussian window, zero padding 5, groups = channels)."""
+    import math
+    g = torch.tensor([math.exp(-(k - 5) ** 2 / (2 * 1.5 ** 2)) for k in range(11)],
+                     dtype=torch.float64)
+    g = g / g.sum()
+    win = (g[:, None] @ g[None, :])[None, None]
+    x4, y4 = (t if t.dim() == 4 else t[None] for t in (x, y))
+    C = x4.shape[1]
+    w = win.expand(C, 1, 11, 11).contiguous()
+    conv = lambda t: F.conv2d(t, w, padding=5, groups=C)  # noqa: E731
+    mu1, mu2 = conv(x4), conv(y4)
+    s11 = conv(x4 * x4) - mu1 ** 2
+    s22 = conv(y4 * y4) - mu2 ** 2
+    s12 = conv(x4 * y4) - mu1 * mu2
+    C1, C2 = 0.01 ** 2, 0.03 ** 2
+    m = ((2 * mu1 * mu2 + C1) * (2 * s12 + C2)) / ((mu1 ** 2 + mu2 ** 2 + C1) * (s11 + s22 + C2))
+    return m.mean()
+
+
+@pytest.mark.parametrize("shape", [(3, 70, 101), (2, 3, 33, 64), (1, 32, 32)])
+def test_ssim_matches_reference(shape):
+    g = torch.Generator().manual_seed(sum(shape))
+    y = torch.rand(*shape, generator=g)
+    x = (y + 0.1 * torch.randn(*shape, generator=g)).clamp(0, 1)
+    x64 = x.double().requires_grad_(True)
+    ref = _ssim_reference(x64, y.double())
+    (2.0 * ref).backward()
+    xg = x.to(DEV).requires_grad_(True)
+    out = fused.ssim(xg, y.to(DEV))
+    assert abs(float(out) - float(ref)) < 1e-6
+    (2.0 * out).backward()
+    assert rel(xg.grad, x64.grad) < 1e-5
+    ops.check_device_status()
