@@ -425,12 +425,17 @@ constexpr int kBwdPix = 2;
 // CTAs per SM.
 constexpr int kBwdBatch = 128;
 
+// Per-pixel replay state.  SB = sum_c dout_c B_c, B_c the colour composited
+// behind the current splat (background first): the gradient needs only that
+// sum, dalpha = sum_c dout_c (f_c - B_c) = F - SB with F = sum_c dout_c f_c,
+// and B_c <- alpha f_c + (1 - alpha) B_c gives SB <- alpha F + (1 - alpha) SB.
 template <int NC>
 struct BwdPixel {
   float T;
   int nc;
   float pxf, pyf;
-  float dout[NC], Bk[NC];
+  float SB;
+  float dout[NC];
 };
 
 // Adds one pixel's contribution to the splat gradients v (u, v, a, b, c, o,
@@ -450,15 +455,15 @@ __device__ __forceinline__ bool bwd_pixel(BwdPixel<NC>& P, int j, const float* r
   const float om = __fsub_rn(1.0f, alpha);
   P.T = __fdividef(P.T, om);
   const float* f = rec + kRecFeat;
-  float dalpha = 0.f;
+  float F = 0.f;
   const float wT = alpha * P.T;
 #pragma unroll
   for (int c = 0; c < NC; ++c) {
-    dalpha = fmaf(P.dout[c], f[c] - P.Bk[c], dalpha);
-    P.Bk[c] = fmaf(alpha, f[c], om * P.Bk[c]);
+    F = fmaf(P.dout[c], f[c], F);
     v[6 + c] = fmaf(wT, P.dout[c], v[6 + c]);
   }
-  dalpha *= P.T;
+  const float dalpha = (F - P.SB) * P.T;
+  P.SB = fmaf(alpha, F, om * P.SB);
   if (araw < 0.99f) {
     const float dpow = alpha * dalpha;
     v[5] = fmaf(G, dalpha, v[5]);
@@ -510,10 +515,7 @@ __global__ void __launch_bounds__(kBwdThreads) blend_bwd_kernel(
     P[q].T = 1.f;
     P[q].nc = 0;
 #pragma unroll
-    for (int c = 0; c < NC; ++c) {
-      P[q].dout[c] = 0.f;
-      P[q].Bk[c] = bg;
-    }
+    for (int c = 0; c < NC; ++c) P[q].dout[c] = 0.f;
     if (px < W && py < H) {
       const int64_t pix = (int64_t)py * W + px;
       P[q].T = final_T[pbase + pix];
@@ -522,6 +524,10 @@ __global__ void __launch_bounds__(kBwdThreads) blend_bwd_kernel(
       for (int c = 0; c < NC; ++c)
         if (c < C) P[q].dout[c] = d_out[C * pbase + c * plane + pix];
     }
+    float sd = 0.f;
+#pragma unroll
+    for (int c = 0; c < NC; ++c) sd += P[q].dout[c];
+    P[q].SB = bg * sd;
     my_nc = max(my_nc, P[q].nc);
   }
   int warp_nc = my_nc;
