@@ -332,6 +332,25 @@ int pgb_l1_l2_loss_forward(const float* x, const float* target, int64_t n, float
 int pgb_l1_l2_loss_backward(const float* x, const float* target, int64_t n, float w,
                             const float* d_loss, float* d_x, void* stream);
 
+/* pgb_preprocess_*: project_point + compute_cov3d + ewa_project as the
+ * renderer chains them (pointrix/model/renderer/msplat.py:109-130, visible =
+ * depth != 0), in one pass forward and one backward.  Outputs are
+ * bit-identical to the three operators' (uv [N,2], depth [N,1], conic [N,3],
+ * radius [N], tiles_touched [N]); the backward takes d uv, d depth and
+ * d conic and writes d xyz (both paths summed), d scales, d quats and the
+ * camera gradients d_intr [4], d_extr [12] (scratch of
+ * pgb_camera_grad_scratch_bytes()).  uquats / d_uquats 16-byte aligned. */
+int pgb_preprocess_forward(const float* xyz, const float* scales, const float* uquats, int64_t n,
+                           const float* intr, const float* extr, int width, int height,
+                           float nearest, float extent, float* uv, float* depth, float* conic,
+                           int32_t* radius, int32_t* tiles_touched, void* stream);
+int pgb_preprocess_backward(const float* xyz, const float* scales, const float* uquats, int64_t n,
+                            const float* intr, const float* extr, int width, int height,
+                            float nearest, float extent, const int32_t* radius, const float* d_uv,
+                            const float* d_depth, const float* d_conic, float* d_xyz,
+                            float* d_scales, float* d_uquats, float* d_intr, float* d_extr,
+                            void* scratch, size_t scratch_bytes, void* stream);
+
 /* pgb_ssim_*: the SSIM of pointrix/model/loss.py:71-125 (11x11 Gaussian
  * window, sigma 1.5, zero padding, C1 = 0.01^2, C2 = 0.03^2, mean over all
  * pixels) of x against the target y, both `planes` contiguous float planes of

@@ -66,6 +66,9 @@ SIGNATURES.update({
     "pgb_l1_l2_loss_backward": [vp, vp, i64, f32, vp, vp, vp],
     "pgb_densify_accumulate": [vp, i64, vp, f32, f32, vp, vp, vp, vp],
     "pgb_ssim_scratch_doubles": [i32, i32, i32],
+    "pgb_preprocess_forward": [vp, vp, vp, i64, vp, vp, i32, i32, f32, f32, vp, vp, vp, vp, vp, vp],
+    "pgb_preprocess_backward": [vp, vp, vp, i64, vp, vp, i32, i32, f32, f32, vp, vp, vp, vp, vp, vp,
+                                vp, vp, vp, vp, szt, vp],
     "pgb_ssim_forward": [vp, vp, i32, i32, i32, vp, i64, vp, vp],
     "pgb_ssim_backward": [vp, vp, i32, i32, i32, vp, vp, vp],
 })

@@ -114,6 +114,32 @@ __global__ void project_point_fwd_kernel(const float* __restrict__ xyz, int64_t 
   }
 }
 
+// Backward of project_point for one visible Gaussian (camera point p):
+// d xyz and the camera accumulators from d uv and d depth.
+__device__ inline void project_bwd_one(const Cam& c, float x, float y, float z, float px, float py,
+                                       float pz, float2 du, float dd, float& gx, float& gy,
+                                       float& gz, float (&acc)[16]) {
+  const float iz = 1.0f / pz;
+  const float gpx = du.x * c.fx * iz;
+  const float gpy = du.y * c.fy * iz;
+  const float gpz = dd - (du.x * c.fx * px + du.y * c.fy * py) * iz * iz;
+  gx = c.e[0] * gpx + c.e[4] * gpy + c.e[8] * gpz;
+  gy = c.e[1] * gpx + c.e[5] * gpy + c.e[9] * gpz;
+  gz = c.e[2] * gpx + c.e[6] * gpy + c.e[10] * gpz;
+  acc[0] += du.x * px * iz;
+  acc[1] += du.y * py * iz;
+  acc[2] += du.x;
+  acc[3] += du.y;
+  const float gp[3] = {gpx, gpy, gpz};
+#pragma unroll
+  for (int r = 0; r < 3; ++r) {
+    acc[4 + 4 * r + 0] += gp[r] * x;
+    acc[4 + 4 * r + 1] += gp[r] * y;
+    acc[4 + 4 * r + 2] += gp[r] * z;
+    acc[4 + 4 * r + 3] += gp[r];
+  }
+}
+
 __global__ void project_point_bwd_kernel(const float* __restrict__ xyz, int64_t n,
                                          const float* __restrict__ intr,
                                          const float* __restrict__ extr, int W, int H,
@@ -131,29 +157,9 @@ __global__ void project_point_bwd_kernel(const float* __restrict__ xyz, int64_t 
     float px, py, pz, u, v;
     cam_point(c, x, y, z, px, py, pz);
     float gx = 0.f, gy = 0.f, gz = 0.f;
-    if (project_visible(c, px, py, pz, W, H, nearest, extent, u, v)) {
-      const float2 du = reinterpret_cast<const float2*>(d_uv)[i];
-      const float dd = d_depth[i];
-      const float iz = 1.0f / pz;
-      const float gpx = du.x * c.fx * iz;
-      const float gpy = du.y * c.fy * iz;
-      const float gpz = dd - (du.x * c.fx * px + du.y * c.fy * py) * iz * iz;
-      gx = c.e[0] * gpx + c.e[4] * gpy + c.e[8] * gpz;
-      gy = c.e[1] * gpx + c.e[5] * gpy + c.e[9] * gpz;
-      gz = c.e[2] * gpx + c.e[6] * gpy + c.e[10] * gpz;
-      acc[0] += du.x * px * iz;
-      acc[1] += du.y * py * iz;
-      acc[2] += du.x;
-      acc[3] += du.y;
-      const float gp[3] = {gpx, gpy, gpz};
-#pragma unroll
-      for (int r = 0; r < 3; ++r) {
-        acc[4 + 4 * r + 0] += gp[r] * x;
-        acc[4 + 4 * r + 1] += gp[r] * y;
-        acc[4 + 4 * r + 2] += gp[r] * z;
-        acc[4 + 4 * r + 3] += gp[r];
-      }
-    }
+    if (project_visible(c, px, py, pz, W, H, nearest, extent, u, v))
+      project_bwd_one(c, x, y, z, px, py, pz, reinterpret_cast<const float2*>(d_uv)[i], d_depth[i],
+                      gx, gy, gz, acc);
     d_xyz[3 * i] = gx;
     d_xyz[3 * i + 1] = gy;
     d_xyz[3 * i + 2] = gz;
@@ -185,36 +191,86 @@ __device__ inline Rot quat_rot(float w, float x, float y, float z) {
   return R;
 }
 
+// Sigma = (R S)(R S)^T, upper triangle, of Gaussian i.
+__device__ inline void cov3d_one(const float* __restrict__ scales, const float* __restrict__ q,
+                                 int64_t i, float (&out)[6]) {
+  const float4 qq = reinterpret_cast<const float4*>(q)[i];
+  const float s[3] = {scales[3 * i], scales[3 * i + 1], scales[3 * i + 2]};
+  const Rot R = quat_rot(qq.x, qq.y, qq.z, qq.w);
+  float M[3][3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+#pragma unroll
+    for (int b = 0; b < 3; ++b) M[a][b] = R.r[a][b] * s[b];
+  auto sig = [&](int a, int b) {
+    return M[a][0] * M[b][0] + M[a][1] * M[b][1] + M[a][2] * M[b][2];
+  };
+  out[0] = sig(0, 0);
+  out[1] = sig(0, 1);
+  out[2] = sig(0, 2);
+  out[3] = sig(1, 1);
+  out[4] = sig(1, 2);
+  out[5] = sig(2, 2);
+}
+
 __global__ void cov3d_fwd_kernel(const float* __restrict__ scales, const float* __restrict__ q,
                                  const uint8_t* __restrict__ visible, int64_t n,
                                  float* __restrict__ cov) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x) {
     float out[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-    if (visible[i]) {
-      const float4 qq = reinterpret_cast<const float4*>(q)[i];
-      const float s[3] = {scales[3 * i], scales[3 * i + 1], scales[3 * i + 2]};
-      const Rot R = quat_rot(qq.x, qq.y, qq.z, qq.w);
-      float M[3][3];
-#pragma unroll
-      for (int a = 0; a < 3; ++a)
-#pragma unroll
-        for (int b = 0; b < 3; ++b) M[a][b] = R.r[a][b] * s[b];
-      auto sig = [&](int a, int b) {
-        return M[a][0] * M[b][0] + M[a][1] * M[b][1] + M[a][2] * M[b][2];
-      };
-      out[0] = sig(0, 0);
-      out[1] = sig(0, 1);
-      out[2] = sig(0, 2);
-      out[3] = sig(1, 1);
-      out[4] = sig(1, 2);
-      out[5] = sig(2, 2);
-    }
+    if (visible[i]) cov3d_one(scales, q, i, out);
     float2* o = reinterpret_cast<float2*>(cov + 6 * i);
     o[0] = make_float2(out[0], out[1]);
     o[1] = make_float2(out[2], out[3]);
     o[2] = make_float2(out[4], out[5]);
   }
+}
+
+// d scales and d quaternion of Gaussian i from the stored gradient g[6] of
+// its covariance (upper triangle).
+__device__ inline void cov3d_grad_one(const float* __restrict__ scales,
+                                      const float* __restrict__ q, int64_t i, const float* g,
+                                      float (&ds)[3], float4& dq) {
+  const float4 qq = reinterpret_cast<const float4*>(q)[i];
+  const float w = qq.x, x = qq.y, y = qq.z, z = qq.w;
+  const float s[3] = {scales[3 * i], scales[3 * i + 1], scales[3 * i + 2]};
+  const Rot R = quat_rot(w, x, y, z);
+  float M[3][3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+#pragma unroll
+    for (int b = 0; b < 3; ++b) M[a][b] = R.r[a][b] * s[b];
+  // Symmetric full gradient: off-diagonal stored entries feed both
+  // halves of Sigma.
+  float G[3][3];
+  G[0][0] = g[0];
+  G[1][1] = g[3];
+  G[2][2] = g[5];
+  G[0][1] = G[1][0] = 0.5f * g[1];
+  G[0][2] = G[2][0] = 0.5f * g[2];
+  G[1][2] = G[2][1] = 0.5f * g[4];
+  float dM[3][3];  // dL/dM = 2 G M
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+#pragma unroll
+    for (int b = 0; b < 3; ++b)
+      dM[a][b] = 2.f * (G[a][0] * M[0][b] + G[a][1] * M[1][b] + G[a][2] * M[2][b]);
+  float dR[3][3];
+#pragma unroll
+  for (int b = 0; b < 3; ++b) {
+    ds[b] = dM[0][b] * R.r[0][b] + dM[1][b] * R.r[1][b] + dM[2][b] * R.r[2][b];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) dR[a][b] = dM[a][b] * s[b];
+  }
+  dq.x = 2.f * (-z * dR[0][1] + y * dR[0][2] + z * dR[1][0] - x * dR[1][2] - y * dR[2][0] +
+                x * dR[2][1]);
+  dq.y = 2.f * (y * dR[0][1] + z * dR[0][2] + y * dR[1][0] - 2.f * x * dR[1][1] -
+                w * dR[1][2] + z * dR[2][0] + w * dR[2][1] - 2.f * x * dR[2][2]);
+  dq.z = 2.f * (-2.f * y * dR[0][0] + x * dR[0][1] + w * dR[0][2] + x * dR[1][0] +
+                z * dR[1][2] - w * dR[2][0] + z * dR[2][1] - 2.f * y * dR[2][2]);
+  dq.w = 2.f * (-2.f * z * dR[0][0] - w * dR[0][1] + x * dR[0][2] + w * dR[1][0] -
+                2.f * z * dR[1][1] + y * dR[1][2] + x * dR[2][0] + y * dR[2][1]);
 }
 
 __global__ void cov3d_bwd_kernel(const float* __restrict__ scales, const float* __restrict__ q,
@@ -225,48 +281,7 @@ __global__ void cov3d_bwd_kernel(const float* __restrict__ scales, const float* 
        i += (int64_t)gridDim.x * blockDim.x) {
     float ds[3] = {0.f, 0.f, 0.f};
     float4 dq = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (visible[i]) {
-      const float4 qq = reinterpret_cast<const float4*>(q)[i];
-      const float w = qq.x, x = qq.y, y = qq.z, z = qq.w;
-      const float s[3] = {scales[3 * i], scales[3 * i + 1], scales[3 * i + 2]};
-      const Rot R = quat_rot(w, x, y, z);
-      float M[3][3];
-#pragma unroll
-      for (int a = 0; a < 3; ++a)
-#pragma unroll
-        for (int b = 0; b < 3; ++b) M[a][b] = R.r[a][b] * s[b];
-      const float* g = d_cov + 6 * i;
-      // Symmetric full gradient: off-diagonal stored entries feed both
-      // halves of Sigma.
-      float G[3][3];
-      G[0][0] = g[0];
-      G[1][1] = g[3];
-      G[2][2] = g[5];
-      G[0][1] = G[1][0] = 0.5f * g[1];
-      G[0][2] = G[2][0] = 0.5f * g[2];
-      G[1][2] = G[2][1] = 0.5f * g[4];
-      float dM[3][3];  // dL/dM = 2 G M
-#pragma unroll
-      for (int a = 0; a < 3; ++a)
-#pragma unroll
-        for (int b = 0; b < 3; ++b)
-          dM[a][b] = 2.f * (G[a][0] * M[0][b] + G[a][1] * M[1][b] + G[a][2] * M[2][b]);
-      float dR[3][3];
-#pragma unroll
-      for (int b = 0; b < 3; ++b) {
-        ds[b] = dM[0][b] * R.r[0][b] + dM[1][b] * R.r[1][b] + dM[2][b] * R.r[2][b];
-#pragma unroll
-        for (int a = 0; a < 3; ++a) dR[a][b] = dM[a][b] * s[b];
-      }
-      dq.x = 2.f * (-z * dR[0][1] + y * dR[0][2] + z * dR[1][0] - x * dR[1][2] - y * dR[2][0] +
-                    x * dR[2][1]);
-      dq.y = 2.f * (y * dR[0][1] + z * dR[0][2] + y * dR[1][0] - 2.f * x * dR[1][1] -
-                    w * dR[1][2] + z * dR[2][0] + w * dR[2][1] - 2.f * x * dR[2][2]);
-      dq.z = 2.f * (-2.f * y * dR[0][0] + x * dR[0][1] + w * dR[0][2] + x * dR[1][0] +
-                    z * dR[1][2] - w * dR[2][0] + z * dR[2][1] - 2.f * y * dR[2][2]);
-      dq.w = 2.f * (-2.f * z * dR[0][0] - w * dR[0][1] + x * dR[0][2] + w * dR[1][0] -
-                    2.f * z * dR[1][1] + y * dR[1][2] + x * dR[2][0] + y * dR[2][1]);
-    }
+    if (visible[i]) cov3d_grad_one(scales, q, i, d_cov + 6 * i, ds, dq);
     d_scales[3 * i] = ds[0];
     d_scales[3 * i + 1] = ds[1];
     d_scales[3 * i + 2] = ds[2];
@@ -320,6 +335,31 @@ __device__ inline void ewa_core(const Cam& cm, int W, int H, float x, float y, f
   E.det = E.a * E.c - E.b * E.b;
 }
 
+// Conic, radius and tiles touched of one visible Gaussian (uv p).
+__device__ inline void ewa_fwd_one(const Cam& cm, int W, int H, int gx, int gy, float x, float y,
+                                   float z, const float* s6, float2 p, float& c0, float& c1,
+                                   float& c2, int& rad, int& nt) {
+  Ewa E;
+  ewa_core(cm, W, H, x, y, z, s6, E);
+  if (E.det > 0.f) {
+    const float mid = 0.5f * (E.a + E.c);
+    const float disc = fmaxf(kEigFloor, mid * mid - E.det);
+    const float lam = mid + sqrtf(disc);
+    const float rf = fminf(ceilf(3.0f * sqrtf(lam)), kRadiusCap);
+    int x0, x1, y0, y1;
+    tile_rect(p.x, p.y, rf, gx, gy, x0, x1, y0, y1);
+    const int cnt = (x1 - x0) * (y1 - y0);
+    if (cnt > 0) {
+      const float inv = 1.0f / E.det;
+      c0 = E.c * inv;
+      c1 = -E.b * inv;
+      c2 = E.a * inv;
+      rad = (int)rf;
+      nt = cnt;
+    }
+  }
+}
+
 __global__ void ewa_fwd_kernel(const float* __restrict__ xyz, const float* __restrict__ cov,
                                const float* __restrict__ intr, const float* __restrict__ extr,
                                const float* __restrict__ uv, const uint8_t* __restrict__ visible,
@@ -336,32 +376,113 @@ __global__ void ewa_fwd_kernel(const float* __restrict__ xyz, const float* __res
       const float2* cv = reinterpret_cast<const float2*>(cov + 6 * i);
       const float2 q0 = cv[0], q1 = cv[1], q2 = cv[2];
       s6[0] = q0.x; s6[1] = q0.y; s6[2] = q1.x; s6[3] = q1.y; s6[4] = q2.x; s6[5] = q2.y;
-      Ewa E;
-      ewa_core(cm, W, H, xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2], s6, E);
-      if (E.det > 0.f) {
-        const float mid = 0.5f * (E.a + E.c);
-        const float disc = fmaxf(kEigFloor, mid * mid - E.det);
-        const float lam = mid + sqrtf(disc);
-        const float rf = fminf(ceilf(3.0f * sqrtf(lam)), kRadiusCap);
-        const float2 p = reinterpret_cast<const float2*>(uv)[i];
-        int x0, x1, y0, y1;
-        tile_rect(p.x, p.y, rf, gx, gy, x0, x1, y0, y1);
-        const int cnt = (x1 - x0) * (y1 - y0);
-        if (cnt > 0) {
-          const float inv = 1.0f / E.det;
-          c0 = E.c * inv;
-          c1 = -E.b * inv;
-          c2 = E.a * inv;
-          rad = (int)rf;
-          nt = cnt;
-        }
-      }
+      ewa_fwd_one(cm, W, H, gx, gy, xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2], s6,
+                  reinterpret_cast<const float2*>(uv)[i], c0, c1, c2, rad, nt);
     }
     conic[3 * i] = c0;
     conic[3 * i + 1] = c1;
     conic[3 * i + 2] = c2;
     radius[i] = rad;
     tiles[i] = nt;
+  }
+}
+
+// Backward of ewa_project for one Gaussian with radius > 0: d xyz
+// (gxw, gyw, gzw), d cov3d (dS) and the camera accumulators acc
+// (d_intr[4], d_extr[12]) from the conic gradient (g0, g1, g2).
+__device__ inline void ewa_bwd_one(const Cam& cm, int W, int H, float x, float y, float z,
+                                   const float* s6, float g0, float g1, float g2, float& gxw,
+                                   float& gyw, float& gzw, float (&dS)[6], float (&acc)[16]) {
+  Ewa E;
+  ewa_core(cm, W, H, x, y, z, s6, E);
+  const float a = E.a, b = E.b, c = E.c;
+  const float id = 1.0f / E.det;
+  const float id2 = id * id;
+  // conic = (c, -b, a) / det, det = a c - b^2
+  const float da = -g0 * c * c * id2 + g1 * b * c * id2 + g2 * (id - a * c * id2);
+  const float dc = g0 * (id - a * c * id2) + g1 * a * b * id2 - g2 * a * a * id2;
+  const float db = 2.f * g0 * b * c * id2 + g1 * (-id - 2.f * b * b * id2) + 2.f * g2 * a * b * id2;
+  // symmetric 2x2 gradient G2 = [[da, db/2], [db/2, dc]]
+  const float G00 = da, G01 = 0.5f * db, G11 = dc;
+  const float* T0 = E.T0;
+  const float* T1 = E.T1;
+  // dSigma_full = T^T G2 T; stored off-diagonals take both halves
+  float U0[3], U1[3];  // (G2 T) rows
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    U0[k] = G00 * T0[k] + G01 * T1[k];
+    U1[k] = G01 * T0[k] + G11 * T1[k];
+  }
+  auto full = [&](int p, int q) { return T0[p] * U0[q] + T1[p] * U1[q]; };
+  dS[0] = full(0, 0);
+  dS[1] = full(0, 1) + full(1, 0);
+  dS[2] = full(0, 2) + full(2, 0);
+  dS[3] = full(1, 1);
+  dS[4] = full(1, 2) + full(2, 1);
+  dS[5] = full(2, 2);
+  // dT = 2 G2 T Sigma
+  float S[3][3];
+  S[0][0] = s6[0]; S[0][1] = S[1][0] = s6[1]; S[0][2] = S[2][0] = s6[2];
+  S[1][1] = s6[3]; S[1][2] = S[2][1] = s6[4]; S[2][2] = s6[5];
+  float dT0[3], dT1[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    dT0[k] = 2.f * (U0[0] * S[0][k] + U0[1] * S[1][k] + U0[2] * S[2][k]);
+    dT1[k] = 2.f * (U1[0] * S[0][k] + U1[1] * S[1][k] + U1[2] * S[2][k]);
+  }
+  const float* e = cm.e;
+  const float dJ00 = dT0[0] * e[0] + dT0[1] * e[1] + dT0[2] * e[2];
+  const float dJ02 = dT0[0] * e[8] + dT0[1] * e[9] + dT0[2] * e[10];
+  const float dJ11 = dT1[0] * e[4] + dT1[1] * e[5] + dT1[2] * e[6];
+  const float dJ12 = dT1[0] * e[8] + dT1[1] * e[9] + dT1[2] * e[10];
+  // W = R part of the extrinsic: dW0 = J00 dT0, dW1 = J11 dT1, dW2 = J02 dT0 + J12 dT1
+  float dR[3][3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    dR[0][k] = E.J00 * dT0[k];
+    dR[1][k] = E.J11 * dT1[k];
+    dR[2][k] = E.J02 * dT0[k] + E.J12 * dT1[k];
+  }
+  const float pz = E.pz, iz = 1.0f / pz, iz2 = iz * iz, iz3 = iz2 * iz;
+  const float fx = cm.fx, fy = cm.fy;
+  float dpz = -fx * iz2 * dJ00 - fy * iz2 * dJ11 + 2.f * fx * E.tx * iz3 * dJ02 +
+              2.f * fy * E.ty * iz3 * dJ12;
+  const float dtx = -fx * iz2 * dJ02;
+  const float dty = -fy * iz2 * dJ12;
+  float dfx = dJ00 * iz - E.tx * iz2 * dJ02;
+  float dfy = dJ11 * iz - E.ty * iz2 * dJ12;
+  float dpx = 0.f, dpy = 0.f;
+  if (E.txtz < -E.limx) {
+    dpz += -E.limx * dtx;
+    dfx += (-pz * dtx) * (-E.limx / fx);
+  } else if (E.txtz > E.limx) {
+    dpz += E.limx * dtx;
+    dfx += (pz * dtx) * (-E.limx / fx);
+  } else {
+    dpx = dtx;
+  }
+  if (E.tytz < -E.limy) {
+    dpz += -E.limy * dty;
+    dfy += (-pz * dty) * (-E.limy / fy);
+  } else if (E.tytz > E.limy) {
+    dpz += E.limy * dty;
+    dfy += (pz * dty) * (-E.limy / fy);
+  } else {
+    dpy = dty;
+  }
+  // p = R x + t
+  gxw = e[0] * dpx + e[4] * dpy + e[8] * dpz;
+  gyw = e[1] * dpx + e[5] * dpy + e[9] * dpz;
+  gzw = e[2] * dpx + e[6] * dpy + e[10] * dpz;
+  const float dp[3] = {dpx, dpy, dpz};
+  const float xw[3] = {x, y, z};
+  acc[0] += dfx;
+  acc[1] += dfy;
+#pragma unroll
+  for (int r = 0; r < 3; ++r) {
+#pragma unroll
+    for (int k = 0; k < 3; ++k) acc[4 + 4 * r + k] += dR[r][k] + dp[r] * xw[k];
+    acc[4 + 4 * r + 3] += dp[r];
   }
 }
 
@@ -379,102 +500,11 @@ __global__ void ewa_bwd_kernel(const float* __restrict__ xyz, const float* __res
     float gxw = 0.f, gyw = 0.f, gzw = 0.f;
     float dS[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
     if (radius[i] > 0) {
-      const float x = xyz[3 * i], y = xyz[3 * i + 1], z = xyz[3 * i + 2];
       float s6[6];
 #pragma unroll
       for (int k = 0; k < 6; ++k) s6[k] = cov[6 * i + k];
-      Ewa E;
-      ewa_core(cm, W, H, x, y, z, s6, E);
-      const float g0 = d_conic[3 * i], g1 = d_conic[3 * i + 1], g2 = d_conic[3 * i + 2];
-      const float a = E.a, b = E.b, c = E.c;
-      const float id = 1.0f / E.det;
-      const float id2 = id * id;
-      // conic = (c, -b, a) / det, det = a c - b^2
-      const float da = -g0 * c * c * id2 + g1 * b * c * id2 + g2 * (id - a * c * id2);
-      const float dc = g0 * (id - a * c * id2) + g1 * a * b * id2 - g2 * a * a * id2;
-      const float db = 2.f * g0 * b * c * id2 + g1 * (-id - 2.f * b * b * id2) + 2.f * g2 * a * b * id2;
-      // symmetric 2x2 gradient G2 = [[da, db/2], [db/2, dc]]
-      const float G00 = da, G01 = 0.5f * db, G11 = dc;
-      const float* T0 = E.T0;
-      const float* T1 = E.T1;
-      // dSigma_full = T^T G2 T; stored off-diagonals take both halves
-      float U0[3], U1[3];  // (G2 T) rows
-#pragma unroll
-      for (int k = 0; k < 3; ++k) {
-        U0[k] = G00 * T0[k] + G01 * T1[k];
-        U1[k] = G01 * T0[k] + G11 * T1[k];
-      }
-      auto full = [&](int p, int q) { return T0[p] * U0[q] + T1[p] * U1[q]; };
-      dS[0] = full(0, 0);
-      dS[1] = full(0, 1) + full(1, 0);
-      dS[2] = full(0, 2) + full(2, 0);
-      dS[3] = full(1, 1);
-      dS[4] = full(1, 2) + full(2, 1);
-      dS[5] = full(2, 2);
-      // dT = 2 G2 T Sigma
-      float S[3][3];
-      S[0][0] = s6[0]; S[0][1] = S[1][0] = s6[1]; S[0][2] = S[2][0] = s6[2];
-      S[1][1] = s6[3]; S[1][2] = S[2][1] = s6[4]; S[2][2] = s6[5];
-      float dT0[3], dT1[3];
-#pragma unroll
-      for (int k = 0; k < 3; ++k) {
-        dT0[k] = 2.f * (U0[0] * S[0][k] + U0[1] * S[1][k] + U0[2] * S[2][k]);
-        dT1[k] = 2.f * (U1[0] * S[0][k] + U1[1] * S[1][k] + U1[2] * S[2][k]);
-      }
-      const float* e = cm.e;
-      const float dJ00 = dT0[0] * e[0] + dT0[1] * e[1] + dT0[2] * e[2];
-      const float dJ02 = dT0[0] * e[8] + dT0[1] * e[9] + dT0[2] * e[10];
-      const float dJ11 = dT1[0] * e[4] + dT1[1] * e[5] + dT1[2] * e[6];
-      const float dJ12 = dT1[0] * e[8] + dT1[1] * e[9] + dT1[2] * e[10];
-      // W = R part of the extrinsic: dW0 = J00 dT0, dW1 = J11 dT1, dW2 = J02 dT0 + J12 dT1
-      float dR[3][3];
-#pragma unroll
-      for (int k = 0; k < 3; ++k) {
-        dR[0][k] = E.J00 * dT0[k];
-        dR[1][k] = E.J11 * dT1[k];
-        dR[2][k] = E.J02 * dT0[k] + E.J12 * dT1[k];
-      }
-      const float pz = E.pz, iz = 1.0f / pz, iz2 = iz * iz, iz3 = iz2 * iz;
-      const float fx = cm.fx, fy = cm.fy;
-      float dpz = -fx * iz2 * dJ00 - fy * iz2 * dJ11 + 2.f * fx * E.tx * iz3 * dJ02 +
-                  2.f * fy * E.ty * iz3 * dJ12;
-      const float dtx = -fx * iz2 * dJ02;
-      const float dty = -fy * iz2 * dJ12;
-      float dfx = dJ00 * iz - E.tx * iz2 * dJ02;
-      float dfy = dJ11 * iz - E.ty * iz2 * dJ12;
-      float dpx = 0.f, dpy = 0.f;
-      if (E.txtz < -E.limx) {
-        dpz += -E.limx * dtx;
-        dfx += (-pz * dtx) * (-E.limx / fx);
-      } else if (E.txtz > E.limx) {
-        dpz += E.limx * dtx;
-        dfx += (pz * dtx) * (-E.limx / fx);
-      } else {
-        dpx = dtx;
-      }
-      if (E.tytz < -E.limy) {
-        dpz += -E.limy * dty;
-        dfy += (-pz * dty) * (-E.limy / fy);
-      } else if (E.tytz > E.limy) {
-        dpz += E.limy * dty;
-        dfy += (pz * dty) * (-E.limy / fy);
-      } else {
-        dpy = dty;
-      }
-      // p = R x + t
-      gxw = e[0] * dpx + e[4] * dpy + e[8] * dpz;
-      gyw = e[1] * dpx + e[5] * dpy + e[9] * dpz;
-      gzw = e[2] * dpx + e[6] * dpy + e[10] * dpz;
-      const float dp[3] = {dpx, dpy, dpz};
-      const float xw[3] = {x, y, z};
-      acc[0] += dfx;
-      acc[1] += dfy;
-#pragma unroll
-      for (int r = 0; r < 3; ++r) {
-#pragma unroll
-        for (int k = 0; k < 3; ++k) acc[4 + 4 * r + k] += dR[r][k] + dp[r] * xw[k];
-        acc[4 + 4 * r + 3] += dp[r];
-      }
+      ewa_bwd_one(cm, W, H, xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2], s6, d_conic[3 * i],
+                  d_conic[3 * i + 1], d_conic[3 * i + 2], gxw, gyw, gzw, dS, acc);
     }
     d_xyz[3 * i] = gxw;
     d_xyz[3 * i + 1] = gyw;
@@ -482,6 +512,96 @@ __global__ void ewa_bwd_kernel(const float* __restrict__ xyz, const float* __res
 #pragma unroll
     for (int k = 0; k < 6; ++k) d_cov[6 * i + k] = dS[k];
   }
+  block_write_partials(acc, partials);
+}
+
+// ---------------------------------------------------------------------------
+// Fused preprocessing: project_point + compute_cov3d + ewa_project of the
+// renderer, in one pass forward and one backward.  The per-Gaussian
+// arithmetic is the same device code as the three operators' (this unit is
+// FMA-free), so every output is bit-identical to the three calls; cov3d is
+// recomputed in the backward instead of stored, the two position and camera
+// gradients are added before they are written.
+// ---------------------------------------------------------------------------
+__global__ void preprocess_fwd_kernel(const float* __restrict__ xyz, const float* __restrict__ scales,
+                                      const float* __restrict__ q, int64_t n,
+                                      const float* __restrict__ intr,
+                                      const float* __restrict__ extr, int W, int H, float nearest,
+                                      float extent, float* __restrict__ uv,
+                                      float* __restrict__ depth, float* __restrict__ conic,
+                                      int32_t* __restrict__ radius, int32_t* __restrict__ tiles) {
+  const Cam cm = load_cam(intr, extr);
+  const int gx = grid_x(W), gy = grid_y(H);
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const float x = xyz[3 * i], y = xyz[3 * i + 1], z = xyz[3 * i + 2];
+    float px, py, pz, u, v;
+    cam_point(cm, x, y, z, px, py, pz);
+    const bool vis = project_visible(cm, px, py, pz, W, H, nearest, extent, u, v);
+    const float2 p = vis ? make_float2(u, v) : make_float2(0.f, 0.f);
+    reinterpret_cast<float2*>(uv)[i] = p;
+    depth[i] = vis ? pz : 0.f;
+    float c0 = 0.f, c1 = 0.f, c2 = 0.f;
+    int rad = 0, nt = 0;
+    if (vis) {
+      float s6[6];
+      cov3d_one(scales, q, i, s6);
+      ewa_fwd_one(cm, W, H, gx, gy, x, y, z, s6, p, c0, c1, c2, rad, nt);
+    }
+    conic[3 * i] = c0;
+    conic[3 * i + 1] = c1;
+    conic[3 * i + 2] = c2;
+    radius[i] = rad;
+    tiles[i] = nt;
+  }
+}
+
+__global__ void preprocess_bwd_kernel(
+    const float* __restrict__ xyz, const float* __restrict__ scales, const float* __restrict__ q,
+    int64_t n, const float* __restrict__ intr, const float* __restrict__ extr, int W, int H,
+    float nearest, float extent, const int32_t* __restrict__ radius,
+    const float* __restrict__ d_uv, const float* __restrict__ d_depth,
+    const float* __restrict__ d_conic, float* __restrict__ d_xyz, float* __restrict__ d_scales,
+    float* __restrict__ d_q, float* __restrict__ partials) {
+  const Cam cm = load_cam(intr, extr);
+  float acc_p[16], acc_e[16];
+#pragma unroll
+  for (int k = 0; k < 16; ++k) acc_p[k] = acc_e[k] = 0.f;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const float x = xyz[3 * i], y = xyz[3 * i + 1], z = xyz[3 * i + 2];
+    float px, py, pz, u, v;
+    cam_point(cm, x, y, z, px, py, pz);
+    float gx = 0.f, gy = 0.f, gz = 0.f;
+    float ds[3] = {0.f, 0.f, 0.f};
+    float4 dq = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (project_visible(cm, px, py, pz, W, H, nearest, extent, u, v)) {
+      project_bwd_one(cm, x, y, z, px, py, pz, reinterpret_cast<const float2*>(d_uv)[i],
+                      d_depth[i], gx, gy, gz, acc_p);
+      if (radius[i] > 0) {
+        float s6[6];
+        cov3d_one(scales, q, i, s6);
+        float ex = 0.f, ey = 0.f, ez = 0.f;
+        float dS[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+        ewa_bwd_one(cm, W, H, x, y, z, s6, d_conic[3 * i], d_conic[3 * i + 1], d_conic[3 * i + 2],
+                    ex, ey, ez, dS, acc_e);
+        gx = gx + ex;
+        gy = gy + ey;
+        gz = gz + ez;
+        cov3d_grad_one(scales, q, i, dS, ds, dq);
+      }
+    }
+    d_xyz[3 * i] = gx;
+    d_xyz[3 * i + 1] = gy;
+    d_xyz[3 * i + 2] = gz;
+    d_scales[3 * i] = ds[0];
+    d_scales[3 * i + 1] = ds[1];
+    d_scales[3 * i + 2] = ds[2];
+    reinterpret_cast<float4*>(d_q)[i] = dq;
+  }
+  float acc[16];
+#pragma unroll
+  for (int k = 0; k < 16; ++k) acc[k] = acc_p[k] + acc_e[k];
   block_write_partials(acc, partials);
 }
 
@@ -563,6 +683,44 @@ int pgb_ewa_project_backward(const float* xyz, const float* cov3d, const float* 
   float* partials = static_cast<float*>(scratch);
   ewa_bwd_kernel<<<grid, kStreamThreads, 0, s>>>(xyz, cov3d, intr, extr, radius, n, width, height,
                                                  d_conic, d_xyz, d_cov3d, partials);
+  cam_grad_finish_kernel<<<1, 16 * kCamTPC, 0, s>>>(partials, grid, d_intr, d_extr);
+  return launch_status();
+}
+
+int pgb_preprocess_forward(const float* xyz, const float* scales, const float* uquats, int64_t n,
+                           const float* intr, const float* extr, int width, int height,
+                           float nearest, float extent, float* uv, float* depth, float* conic,
+                           int32_t* radius, int32_t* tiles_touched, void* stream) {
+  if (n < 0 || width <= 0 || height <= 0) return PGB_ERR_INVALID;
+  if (n == 0) return PGB_OK;
+  if (!xyz || !scales || !uquats || !intr || !extr || !uv || !depth || !conic || !radius ||
+      !tiles_touched || (reinterpret_cast<uintptr_t>(uquats) & 15))
+    return PGB_ERR_INVALID;
+  preprocess_fwd_kernel<<<stream_grid(n), kStreamThreads, 0, as_stream(stream)>>>(
+      xyz, scales, uquats, n, intr, extr, width, height, nearest, extent, uv, depth, conic, radius,
+      tiles_touched);
+  return launch_status();
+}
+
+int pgb_preprocess_backward(const float* xyz, const float* scales, const float* uquats, int64_t n,
+                            const float* intr, const float* extr, int width, int height,
+                            float nearest, float extent, const int32_t* radius, const float* d_uv,
+                            const float* d_depth, const float* d_conic, float* d_xyz,
+                            float* d_scales, float* d_uquats, float* d_intr, float* d_extr,
+                            void* scratch, size_t scratch_bytes, void* stream) {
+  if (n < 0 || width <= 0 || height <= 0) return PGB_ERR_INVALID;
+  if (scratch_bytes < pgb_camera_grad_scratch_bytes() || !scratch || !d_intr || !d_extr)
+    return PGB_ERR_INVALID;
+  if (n > 0 && (!xyz || !scales || !uquats || !intr || !extr || !radius || !d_uv || !d_depth ||
+                !d_conic || !d_xyz || !d_scales || !d_uquats ||
+                ((reinterpret_cast<uintptr_t>(uquats) | reinterpret_cast<uintptr_t>(d_uquats)) & 15)))
+    return PGB_ERR_INVALID;
+  cudaStream_t s = as_stream(stream);
+  const int grid = stream_grid(n);
+  float* partials = static_cast<float*>(scratch);
+  preprocess_bwd_kernel<<<grid, kStreamThreads, 0, s>>>(
+      xyz, scales, uquats, n, intr, extr, width, height, nearest, extent, radius, d_uv, d_depth,
+      d_conic, d_xyz, d_scales, d_uquats, partials);
   cam_grad_finish_kernel<<<1, 16 * kCamTPC, 0, s>>>(partials, grid, d_intr, d_extr);
   return launch_status();
 }

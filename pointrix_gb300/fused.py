@@ -14,7 +14,11 @@ forward and one backward:
   0.5, min=0), with gradients to sh, xyz and the camera centre;
 * :func:`l1_l2_loss` -- mean|x - t| + w mean((x - t)^2);
 * :func:`ssim` -- the SSIM of ``pointrix/model/loss.py:71-125`` (one tiled
-  kernel forward, one backward).
+  kernel forward, one backward);
+* :func:`preprocess` -- ``project_point``, ``compute_cov3d`` and
+  ``ewa_project`` as ``render_iter`` chains them
+  (``pointrix/model/renderer/msplat.py:109-130``), outputs bit-identical to
+  the three operators.
 """
 from __future__ import annotations
 
@@ -22,9 +26,10 @@ import torch
 
 from . import _lib
 from ._lib import call
-from .ops import _c, _ptr, _stream, _timed
+from .ops import EXTENT_DEFAULT, NEAREST_DEFAULT, _c, _extr34, _intr4, _ptr, _stream, _timed
 
-__all__ = ["gaussian_activations", "sh_rgb", "sh_rgb_supported", "l1_l2_loss", "ssim"]
+__all__ = ["gaussian_activations", "sh_rgb", "sh_rgb_supported", "l1_l2_loss", "ssim",
+           "preprocess"]
 
 
 def _aligned(t: torch.Tensor) -> bool:
@@ -242,3 +247,61 @@ def ssim(img1, img2, window_size=11, size_average=True):
     H, W = img1.shape[-2], img1.shape[-1]
     planes = img1.numel() // (H * W)
     return _Ssim.apply(_c(img1), _c(img2.detach()), planes, H, W)
+
+
+# ---------------------------------------------------------------------------
+class _Preprocess(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, xyz, scales, quats, intr, extr, W, H, nearest, extent):
+        n = xyz.shape[0]
+        dev = xyz.device
+        uv = torch.empty(n, 2, dtype=torch.float32, device=dev)
+        depth = torch.empty(n, 1, dtype=torch.float32, device=dev)
+        conic = torch.empty(n, 3, dtype=torch.float32, device=dev)
+        radius = torch.empty(n, dtype=torch.int32, device=dev)
+        tiles = torch.empty(n, dtype=torch.int32, device=dev)
+        with _timed("preprocess_fwd", dev, 1 if n else 0):
+            call("pgb_preprocess_forward", _ptr(xyz), _ptr(scales), _ptr(quats), n, _ptr(intr),
+                 _ptr(extr), W, H, nearest, extent, _ptr(uv), _ptr(depth), _ptr(conic),
+                 _ptr(radius), _ptr(tiles), _stream(dev))
+        ctx.save_for_backward(xyz, scales, quats, intr, extr, radius)
+        ctx.cfg = (W, H, nearest, extent)
+        ctx.mark_non_differentiable(radius, tiles)
+        return uv, depth, conic, radius, tiles
+
+    @staticmethod
+    def backward(ctx, d_uv, d_depth, d_conic, _d_radius, _d_tiles):
+        xyz, scales, quats, intr, extr, radius = ctx.saved_tensors
+        W, H, nearest, extent = ctx.cfg
+        n = xyz.shape[0]
+        dev = xyz.device
+        g = lambda t, *shape: torch.zeros(*shape, device=dev) if t is None else _c(t)  # noqa: E731
+        d_uv, d_depth, d_conic = g(d_uv, n, 2), g(d_depth, n, 1), g(d_conic, n, 3)
+        d_xyz, d_scales, d_quats = torch.empty_like(xyz), torch.empty_like(scales), torch.empty_like(quats)
+        d_intr = torch.empty(4, dtype=torch.float32, device=dev)
+        d_extr = torch.empty(3, 4, dtype=torch.float32, device=dev)
+        nbytes = _lib.lib().pgb_camera_grad_scratch_bytes()
+        scratch = torch.empty(nbytes, dtype=torch.uint8, device=dev)
+        with _timed("preprocess_bwd", dev, 2):
+            call("pgb_preprocess_backward", _ptr(xyz), _ptr(scales), _ptr(quats), n, _ptr(intr),
+                 _ptr(extr), W, H, nearest, extent, _ptr(radius), _ptr(d_uv), _ptr(d_depth),
+                 _ptr(d_conic), _ptr(d_xyz), _ptr(d_scales), _ptr(d_quats), _ptr(d_intr),
+                 _ptr(d_extr), _ptr(scratch), nbytes, _stream(dev))
+        return d_xyz, d_scales, d_quats, d_intr, d_extr, None, None, None, None
+
+
+def preprocess(position, scaling, rotation, intr, extr, W, H, nearest=NEAREST_DEFAULT,
+               extent=EXTENT_DEFAULT):
+    """(uv [N,2], depth [N,1], conic [N,3], radius [N], tiles_touched [N]) of
+    ``project_point`` -> ``compute_cov3d(visible = depth != 0)`` ->
+    ``ewa_project`` in one kernel each way; the same values, bit for bit, as
+    the three operators, and the same gradients up to summation order.
+    ``intr`` is [4] or [1,4], ``extr`` the world->camera [3,4]."""
+    n = position.shape[0]
+    for name, t, last in (("position", position, 3), ("scaling", scaling, 3), ("rotation", rotation, 4)):
+        if t.dim() != 2 or t.shape[0] != n or t.shape[1] != last:
+            raise ValueError(f"{name} must be [N,{last}], got {tuple(t.shape)}")
+        if not (t.is_cuda and t.dtype == torch.float32):
+            raise ValueError(f"{name} must be a CUDA float32 tensor")
+    return _Preprocess.apply(_c(position), _c(scaling), _c16(rotation), _intr4(intr), _extr34(extr),
+                             int(W), int(H), float(nearest), float(extent))

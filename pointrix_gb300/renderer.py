@@ -67,6 +67,8 @@ class MsplatRender:
         # view direction + SH mask + compute_sh + 0.5 + clamp in one kernel
         # (when shs is dense [N,K,3] storage)
         fused_view_colour: bool = True
+        # project_point + compute_cov3d + ewa_project in one kernel each way
+        fused_preprocess: bool = True
         # > 0: sort with K kept on the device and lists of this capacity (no
         # host synchronisation; the step can be captured in a CUDA graph)
         sort_capacity: int = 0
@@ -109,12 +111,17 @@ class MsplatRender:
             rgb = (rgb + 0.5).clamp(min=0.0)
 
         extr = extrinsic_matrix[:3, :]
-        uv, depth = ops.project_point(position, intrinsic_params, extr, width, height,
-                                      nearest=self.nearest)
-        visible = depth != 0
-        cov3d = ops.compute_cov3d(scaling, rotation, visible)
-        conic, radius, tiles_touched = ops.ewa_project(position, cov3d, intrinsic_params, extr, uv,
-                                                       width, height, visible)
+        if self.cfg.fused_preprocess:
+            uv, depth, conic, radius, tiles_touched = fused.preprocess(
+                position, scaling, rotation, intrinsic_params, extr, width, height,
+                nearest=self.nearest)
+        else:
+            uv, depth = ops.project_point(position, intrinsic_params, extr, width, height,
+                                          nearest=self.nearest)
+            visible = depth != 0
+            cov3d = ops.compute_cov3d(scaling, rotation, visible)
+            conic, radius, tiles_touched = ops.ewa_project(position, cov3d, intrinsic_params, extr,
+                                                           uv, width, height, visible)
         feats = {"rgb": rgb}
         if self.cfg.render_depth:
             feats["depth"] = depth

@@ -221,3 +221,34 @@ def test_ssim_matches_reference(shape):
     (2.0 * out).backward()
     assert rel(xg.grad, x64.grad) < 1e-5
     ops.check_device_status()
+
+
+def test_preprocess_matches_three_operators():
+    """Fused project_point + compute_cov3d + ewa_project: every forward output
+    bit-identical to the three operators, gradients (position, scales,
+    quaternions, intrinsics, extrinsics) within 1e-5 of the chained ones."""
+    scene, cam = WL.scene_train_view(1, n=200_000)
+    g = torch.Generator().manual_seed(4)
+    runs = []
+    for fused_on in (True, False):
+        pos, sc, q, op, shs = (t.to(DEV) for t in scene.activated())
+        pos, sc, q = (t.detach().requires_grad_(True) for t in (pos, sc, q))
+        intr = cam.intr.to(DEV).requires_grad_(True)
+        E = cam.extr.to(DEV).requires_grad_(True)
+        extr = E[:3, :]
+        if fused_on:
+            uv, depth, conic, radius, tiles = fused.preprocess(pos, sc, q, intr, extr, cam.W, cam.H)
+        else:
+            uv, depth = ops.project_point(pos, intr, extr, cam.W, cam.H)
+            vis = depth != 0
+            cov = ops.compute_cov3d(sc, q, vis)
+            conic, radius, tiles = ops.ewa_project(pos, cov, intr, extr, uv, cam.W, cam.H, vis)
+        gen = torch.Generator().manual_seed(11)
+        ups = [torch.randn(t.shape, generator=gen).to(DEV) for t in (uv, depth, conic)]
+        torch.autograd.backward([uv, depth, conic], ups)
+        runs.append(([uv, depth, conic, radius, tiles], [pos.grad, sc.grad, q.grad, intr.grad, E.grad]))
+    for a, b in zip(runs[0][0], runs[1][0]):
+        assert torch.equal(a, b)
+    for a, b in zip(runs[0][1], runs[1][1]):
+        assert rel(a, b) < 1e-5
+    ops.check_device_status()
