@@ -320,6 +320,19 @@ int pgb_sh_rgb_backward(const float* sh, int64_t n, int k, int active, const flo
                         const float* center, const float* d_rgb, float* d_sh, float* d_xyz,
                         float* d_center, float* scratch, int64_t scratch_floats, void* stream);
 
+/* pgb_sh_rgb_views_*: pgb_sh_rgb_* for V cameras in one pass over the
+ * coefficients (batches of views).  centres [V,3] on the device (V <= 64),
+ * rgb and d_rgb [V][N][3]; the backward writes d_sh and d_xyz summed over
+ * the views and d_centres [V,3] (deterministic, scratch of
+ * pgb_sh_rgb_views_scratch_floats(n) floats). */
+int pgb_sh_rgb_views_scratch_floats(int64_t n);
+int pgb_sh_rgb_views_forward(const float* sh, int64_t n, int k, int active, const float* xyz,
+                             const float* centres, int nviews, float* rgb, void* stream);
+int pgb_sh_rgb_views_backward(const float* sh, int64_t n, int k, int active, const float* xyz,
+                              const float* centres, int nviews, const float* d_rgb,
+                              float* d_sh, float* d_xyz, float* d_centres, float* scratch,
+                              int64_t scratch_floats, void* stream);
+
 /* pgb_l1_l2_loss_*: L = mean|x - t| + w * mean((x - t)^2) over n floats
  * (the L1 term of pointrix/model/loss.py:27-33 plus a weighted L2 term), x
  * and t 16-byte aligned.  The forward writes L to loss[0] (device) through

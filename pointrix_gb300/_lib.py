@@ -61,6 +61,9 @@ SIGNATURES.update({
     "pgb_sh_rgb_scratch_floats": [i64],
     "pgb_sh_rgb_forward": [vp, i64, i32, i32, vp, vp, vp, vp],
     "pgb_sh_rgb_backward": [vp, i64, i32, i32, vp, vp, vp, vp, vp, vp, vp, i64, vp],
+    "pgb_sh_rgb_views_scratch_floats": [i64],
+    "pgb_sh_rgb_views_forward": [vp, i64, i32, i32, vp, vp, i32, vp, vp],
+    "pgb_sh_rgb_views_backward": [vp, i64, i32, i32, vp, vp, i32, vp, vp, vp, vp, vp, i64, vp],
     "pgb_l1_l2_loss_scratch_doubles": [i64],
     "pgb_l1_l2_loss_forward": [vp, vp, i64, f32, vp, i64, vp, vp],
     "pgb_l1_l2_loss_backward": [vp, vp, i64, f32, vp, vp, vp],

@@ -453,6 +453,142 @@ inline int sh_rgb_grid(int64_t n) {
   return (int)std::max<int64_t>(1, std::min<int64_t>(need, kShRgbBlocksMax));
 }
 
+// ---------------------------------------------------------------------------
+// The fused view colour of V cameras in one pass over the coefficients
+// (batches of views): each warp stages its 32 Gaussians' coefficients once
+// and evaluates every view's direction, basis and colour; the backward
+// accumulates d_sh and d_xyz over the views in registers and writes them
+// once, and each view's centre gradient through per-block partials.
+// rgb and d_rgb are [V][N][3], the centres [V][3] on the device; the view
+// count is at most kMaxViews.
+// ---------------------------------------------------------------------------
+
+template <int K>
+__global__ void __launch_bounds__(kShWarps * 32) sh_rgb_views_fwd_kernel(
+    const float* __restrict__ sh, int64_t n, int active, const float* __restrict__ xyz,
+    const float* __restrict__ centres, int nviews, float* __restrict__ rgb) {
+  __shared__ float stage_all[kShWarps][32 * ShStage<K>::P];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  float* stage = stage_all[warp];
+  const int64_t nblocks = (n + 31) / 32;
+  for (int64_t wb = (int64_t)blockIdx.x * kShWarps + warp; wb < nblocks;
+       wb += (int64_t)gridDim.x * kShWarps) {
+    const int64_t g0 = wb * 32;
+    const int cnt = n - g0 < 32 ? (int)(n - g0) : 32;
+    __syncwarp();
+    stage_in<K>(sh, g0, cnt, stage, lane);
+    if (lane < cnt) {
+      const int64_t i = g0 + lane;
+      const float* c = stage + lane * ShStage<K>::P;
+      for (int v = 0; v < nviews; ++v) {
+        float dx, dy, dz, nrm;
+        view_dir(xyz, i, centres[3 * v], centres[3 * v + 1], centres[3 * v + 2], dx, dy, dz, nrm);
+        float Y[K];
+        sh_basis<K>(dx, dy, dz, Y);
+        float* o = rgb + ((int64_t)v * n + i) * 3;
+#pragma unroll
+        for (int ch = 0; ch < 3; ++ch) {
+          const float x = sh_channel<K>(c, Y, ch, active) + 0.5f;
+          o[ch] = x < 0.f ? 0.f : x;
+        }
+      }
+    }
+  }
+}
+
+template <int K>
+__global__ void __launch_bounds__(kShWarps * 32) sh_rgb_views_bwd_kernel(
+    const float* __restrict__ sh, int64_t n, int active, const float* __restrict__ xyz,
+    const float* __restrict__ centres, int nviews, const float* __restrict__ d_rgb,
+    float* __restrict__ d_sh, float* __restrict__ d_xyz, float* __restrict__ partial) {
+  __shared__ float stage_all[kShWarps][32 * ShStage<K>::P];
+  __shared__ float s_red[kShWarps][kMaxViews * 3];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  float* stage = stage_all[warp];
+  for (int j = lane; j < nviews * 3; j += 32) s_red[warp][j] = 0.f;
+  const int64_t nblocks = (n + 31) / 32;
+  for (int64_t wb = (int64_t)blockIdx.x * kShWarps + warp; wb < nblocks;
+       wb += (int64_t)gridDim.x * kShWarps) {
+    const int64_t g0 = wb * 32;
+    const int cnt = n - g0 < 32 ? (int)(n - g0) : 32;
+    __syncwarp();
+    stage_in<K>(sh, g0, cnt, stage, lane);
+    float dsum[3 * K];
+#pragma unroll
+    for (int j = 0; j < 3 * K; ++j) dsum[j] = 0.f;
+    float sx = 0.f, sy = 0.f, sz = 0.f;
+    const int64_t i = g0 + lane;
+    float* c = stage + lane * ShStage<K>::P;
+    for (int v = 0; v < nviews; ++v) {
+      float vx = 0.f, vy = 0.f, vz = 0.f;
+      if (lane < cnt) {
+        float dx, dy, dz, nrm;
+        view_dir(xyz, i, centres[3 * v], centres[3 * v + 1], centres[3 * v + 2], dx, dy, dz, nrm);
+        float Y[K];
+        sh_basis<K>(dx, dy, dz, Y);
+        const float* gr = d_rgb + ((int64_t)v * n + i) * 3;
+        float g[3];
+#pragma unroll
+        for (int ch = 0; ch < 3; ++ch) {
+          const float x = sh_channel<K>(c, Y, ch, active) + 0.5f;
+          g[ch] = x >= 0.f ? gr[ch] : 0.f;
+        }
+        float G[K];
+#pragma unroll
+        for (int k = 0; k < K; ++k) {
+          const bool on = k < active;
+          G[k] = on ? g[0] * c[k * 3] + g[1] * c[k * 3 + 1] + g[2] * c[k * 3 + 2] : 0.f;
+#pragma unroll
+          for (int ch = 0; ch < 3; ++ch)
+            if (on) dsum[k * 3 + ch] = fmaf(g[ch], Y[k], dsum[k * 3 + ch]);
+        }
+        float gx, gy, gz;
+        sh_basis_grad<K>(dx, dy, dz, G, gx, gy, gz);
+        const float dot = dx * gx + dy * gy + dz * gz;
+        vx = (gx - dx * dot) / nrm;
+        vy = (gy - dy * dot) / nrm;
+        vz = (gz - dz * dot) / nrm;
+        sx += vx;
+        sy += vy;
+        sz += vz;
+      }
+      // this view's centre gradient: -sum of d(xyz - centre) over the warp
+      vx = warp_sum(vx);
+      vy = warp_sum(vy);
+      vz = warp_sum(vz);
+      if (lane == 0) {
+        s_red[warp][3 * v] -= vx;
+        s_red[warp][3 * v + 1] -= vy;
+        s_red[warp][3 * v + 2] -= vz;
+      }
+    }
+    if (lane < cnt) {
+      d_xyz[3 * i] = sx;
+      d_xyz[3 * i + 1] = sy;
+      d_xyz[3 * i + 2] = sz;
+#pragma unroll
+      for (int j = 0; j < 3 * K; ++j) c[j] = dsum[j];
+    }
+    stage_out<K>(d_sh, g0, cnt, stage, lane);
+  }
+  __syncthreads();
+  for (int j = threadIdx.x; j < nviews * 3; j += blockDim.x) {
+    float t = 0.f;
+    for (int w = 0; w < kShWarps; ++w) t += s_red[w][j];
+    partial[(int64_t)blockIdx.x * (kMaxViews * 3) + j] = t;
+  }
+}
+
+// d_centres[v][c] = sum over blocks of partial[b][3v + c] (fixed order):
+// one CTA per (view, axis) column.
+__global__ void __launch_bounds__(256) sh_views_centre_finish_kernel(
+    const float* __restrict__ partial, int blocks, float* __restrict__ d_centres) {
+  __shared__ double s[256];
+  const int j = blockIdx.x;
+  column_sum<1, 256>(partial + j, blocks, kMaxViews * 3, s);
+  if (threadIdx.x == 0) d_centres[j] = (float)s[0];
+}
+
 }  // namespace pgb
 
 using namespace pgb;
@@ -532,6 +668,53 @@ int pgb_sh_rgb_backward(const float* sh, int64_t n, int k, int active, const flo
     default: sh_rgb_bwd_kernel<16><<<grid, kShWarps * 32, 0, s>>>(sh, n, active, xyz, center, d_rgb, d_sh, d_xyz, scratch); break;
   }
   sh_center_finish_kernel<<<1, 4 * kCenterTPC, 0, s>>>(scratch, grid, d_center);
+  return launch_status();
+}
+
+int pgb_sh_rgb_views_scratch_floats(int64_t n) { return kMaxViews * 3 * sh_rgb_grid(n); }
+
+int pgb_sh_rgb_views_forward(const float* sh, int64_t n, int k, int active, const float* xyz,
+                             const float* centres, int nviews, float* rgb, void* stream) {
+  if (n < 0 || !(k == 1 || k == 4 || k == 9 || k == 16) || active < 0 || !centres ||
+      nviews < 1 || nviews > kMaxViews)
+    return PGB_ERR_INVALID;
+  if (n == 0) return PGB_OK;
+  if (!sh || !xyz || !rgb || (reinterpret_cast<uintptr_t>(sh) & 15)) return PGB_ERR_INVALID;
+  cudaStream_t s = as_stream(stream);
+  const int grid = sh_rgb_grid(n);
+  switch (k) {
+    case 1: sh_rgb_views_fwd_kernel<1><<<grid, kShWarps * 32, 0, s>>>(sh, n, active, xyz, centres, nviews, rgb); break;
+    case 4: sh_rgb_views_fwd_kernel<4><<<grid, kShWarps * 32, 0, s>>>(sh, n, active, xyz, centres, nviews, rgb); break;
+    case 9: sh_rgb_views_fwd_kernel<9><<<grid, kShWarps * 32, 0, s>>>(sh, n, active, xyz, centres, nviews, rgb); break;
+    default: sh_rgb_views_fwd_kernel<16><<<grid, kShWarps * 32, 0, s>>>(sh, n, active, xyz, centres, nviews, rgb); break;
+  }
+  return launch_status();
+}
+
+int pgb_sh_rgb_views_backward(const float* sh, int64_t n, int k, int active, const float* xyz,
+                              const float* centres, int nviews, const float* d_rgb,
+                              float* d_sh, float* d_xyz, float* d_centres, float* scratch,
+                              int64_t scratch_floats, void* stream) {
+  if (n < 0 || !(k == 1 || k == 4 || k == 9 || k == 16) || active < 0 || !centres ||
+      nviews < 1 || nviews > kMaxViews || !d_centres)
+    return PGB_ERR_INVALID;
+  cudaStream_t s = as_stream(stream);
+  if (n == 0)
+    return cudaMemsetAsync(d_centres, 0, 3 * sizeof(float) * nviews, s) == cudaSuccess
+               ? PGB_OK
+               : PGB_ERR_CUDA;
+  const int grid = sh_rgb_grid(n);
+  if (!sh || !xyz || !d_rgb || !d_sh || !d_xyz || !scratch ||
+      scratch_floats < (int64_t)kMaxViews * 3 * grid ||
+      ((reinterpret_cast<uintptr_t>(sh) | reinterpret_cast<uintptr_t>(d_sh)) & 15))
+    return PGB_ERR_INVALID;
+  switch (k) {
+    case 1: sh_rgb_views_bwd_kernel<1><<<grid, kShWarps * 32, 0, s>>>(sh, n, active, xyz, centres, nviews, d_rgb, d_sh, d_xyz, scratch); break;
+    case 4: sh_rgb_views_bwd_kernel<4><<<grid, kShWarps * 32, 0, s>>>(sh, n, active, xyz, centres, nviews, d_rgb, d_sh, d_xyz, scratch); break;
+    case 9: sh_rgb_views_bwd_kernel<9><<<grid, kShWarps * 32, 0, s>>>(sh, n, active, xyz, centres, nviews, d_rgb, d_sh, d_xyz, scratch); break;
+    default: sh_rgb_views_bwd_kernel<16><<<grid, kShWarps * 32, 0, s>>>(sh, n, active, xyz, centres, nviews, d_rgb, d_sh, d_xyz, scratch); break;
+  }
+  sh_views_centre_finish_kernel<<<nviews * 3, 256, 0, s>>>(scratch, grid, d_centres);
   return launch_status();
 }
 

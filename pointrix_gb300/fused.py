@@ -28,8 +28,8 @@ from . import _lib
 from ._lib import call
 from .ops import EXTENT_DEFAULT, NEAREST_DEFAULT, _c, _extr34, _intr4, _ptr, _stream, _timed
 
-__all__ = ["gaussian_activations", "sh_rgb", "sh_rgb_supported", "l1_l2_loss", "ssim",
-           "preprocess"]
+__all__ = ["gaussian_activations", "sh_rgb", "sh_rgb_views", "sh_rgb_supported", "l1_l2_loss",
+           "ssim", "preprocess"]
 
 
 def _aligned(t: torch.Tensor) -> bool:
@@ -163,6 +163,53 @@ def sh_rgb(shs, position, camera_center, active=None):
         raise ValueError("camera_center must hold 3 values")
     active = K if active is None else max(0, min(int(active), K))
     return _ShRgb.apply(shs, _c(position), _c(camera_center.reshape(3)), active)
+
+
+class _ShRgbViews(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, shs, xyz, centres, active):
+        n, K = shs.shape[0], shs.shape[1]
+        V = centres.shape[0]
+        dev = shs.device
+        rgb = torch.empty(V, n, 3, dtype=torch.float32, device=dev)
+        with _timed("sh_rgb_views_fwd", dev, 1 if n else 0):
+            call("pgb_sh_rgb_views_forward", _ptr(shs), n, K, active, _ptr(xyz), _ptr(centres), V,
+                 _ptr(rgb), _stream(dev))
+        ctx.save_for_backward(shs, xyz, centres)
+        ctx.active = active
+        return rgb
+
+    @staticmethod
+    def backward(ctx, d_rgb):
+        shs, xyz, centres = ctx.saved_tensors
+        n, K = shs.shape[0], shs.shape[1]
+        V = centres.shape[0]
+        dev = shs.device
+        d_sh = torch.empty_like(shs)
+        d_xyz = torch.empty_like(xyz)
+        d_c = torch.empty(V, 3, dtype=torch.float32, device=dev)
+        nf = _lib.lib().pgb_sh_rgb_views_scratch_floats(n)
+        scratch = torch.empty(max(nf, 1), dtype=torch.float32, device=dev)
+        with _timed("sh_rgb_views_bwd", dev, 2 if n else 0):
+            call("pgb_sh_rgb_views_backward", _ptr(shs), n, K, ctx.active, _ptr(xyz), _ptr(centres),
+                 V, _ptr(_c(d_rgb)), _ptr(d_sh), _ptr(d_xyz), _ptr(d_c), _ptr(scratch), nf,
+                 _stream(dev))
+        return d_sh, d_xyz, d_c, None
+
+
+def sh_rgb_views(shs, position, centres, active=None):
+    """:func:`sh_rgb` for V camera centres ([V,3], V <= 64) in one pass over
+    the coefficients -> [V,N,3]; gradients to shs and position are summed
+    over the views, each centre gets its own."""
+    if not sh_rgb_supported(shs):
+        raise ValueError("sh_rgb_views needs dense, 16-byte aligned CUDA float32 shs [N,K,3]")
+    n, K = shs.shape[0], shs.shape[1]
+    if tuple(position.shape) != (n, 3):
+        raise ValueError(f"position must be [N,3], got {tuple(position.shape)}")
+    if centres.dim() != 2 or centres.shape[1] != 3 or not 1 <= centres.shape[0] <= 64:
+        raise ValueError(f"centres must be [V,3] with 1 <= V <= 64, got {tuple(centres.shape)}")
+    active = K if active is None else max(0, min(int(active), K))
+    return _ShRgbViews.apply(shs, _c(position), _c(centres), active)
 
 
 # ---------------------------------------------------------------------------

@@ -134,11 +134,15 @@ def render_views(position, scaling, rotation, opacity, shs, cams, bg=0.0, render
     K = shs.shape[1]
     active = K if sh_active is None else sh_active
     uvs, depths, conics, radii, tiles, feats = [], [], [], [], [], []
-    use_fused = fused.sh_rgb_supported(shs)
+    use_fused = fused.sh_rgb_supported(shs) and len(cams) <= MAX_VIEWS
     shc = shs.permute(0, 2, 1)
-    for cam in cams:
+    rgb_all = None
+    if use_fused:  # every view's colour in one pass over the coefficients
+        centres = torch.stack([cam.center.reshape(3) for cam in cams])
+        rgb_all = fused.sh_rgb_views(shs, position, centres, active)
+    for v, cam in enumerate(cams):
         if use_fused:
-            rgb = fused.sh_rgb(shs, position, cam.center, active)
+            rgb = rgb_all[v]
         else:
             d = position - cam.center.reshape(1, 3)
             d = d / d.norm(dim=1, keepdim=True)
@@ -149,10 +153,8 @@ def render_views(position, scaling, rotation, opacity, shs, cams, bg=0.0, render
                 sh_in = shc * mask
             rgb = (ops.compute_sh(sh_in, d) + 0.5).clamp(min=0.0)
         extr = cam.extr[:3, :]
-        uv, depth = ops.project_point(position, cam.intr, extr, cam.W, cam.H, nearest=nearest)
-        vis = depth != 0
-        cov = ops.compute_cov3d(scaling, rotation, vis)
-        conic, radius, nt = ops.ewa_project(position, cov, cam.intr, extr, uv, cam.W, cam.H, vis)
+        uv, depth, conic, radius, nt = fused.preprocess(position, scaling, rotation, cam.intr, extr,
+                                                        cam.W, cam.H, nearest=nearest)
         f = [rgb] + ([depth] if render_depth else []) + ([extra_features] if extra_features is not None else [])
         uvs.append(uv); depths.append(depth); conics.append(conic)
         radii.append(radius); tiles.append(nt); feats.append(torch.cat(f, 1))

@@ -252,3 +252,25 @@ def test_preprocess_matches_three_operators():
     for a, b in zip(runs[0][1], runs[1][1]):
         assert rel(a, b) < 1e-5
     ops.check_device_status()
+
+
+def test_sh_rgb_views_matches_per_view():
+    """Colour of several views in one pass equals the per-view fused colour;
+    gradients (summed over views for sh and position, per view for the
+    centres) within 1e-5."""
+    g = torch.Generator().manual_seed(21)
+    n, K, V = 30_000 + 7, 16, 5
+    shs = (torch.randn(n, K, 3, generator=g) * 0.3).to(DEV)
+    pos = (torch.randn(n, 3, generator=g) * 1.5).to(DEV)
+    centres = (torch.randn(V, 3, generator=g) * 4.0).to(DEV)
+    ups = torch.randn(V, n, 3, generator=g).to(DEV)
+    a = [t.clone().requires_grad_(True) for t in (shs, pos, centres)]
+    out = fused.sh_rgb_views(a[0], a[1], a[2], 9)
+    out.backward(ups)
+    b = [t.clone().requires_grad_(True) for t in (shs, pos, centres)]
+    ref = torch.stack([fused.sh_rgb(b[0], b[1], b[2][v], 9) for v in range(V)])
+    ref.backward(ups)
+    assert torch.equal(out, ref.detach())
+    for x, y in zip(a, b):
+        assert rel(x.grad, y.grad) < 1e-5
+    ops.check_device_status()
