@@ -592,7 +592,7 @@ def run_gb300(args):
     dist_init(world, "nccl")
     device = torch.device("cuda", local)
     torch.cuda.set_device(device)
-    from pointrix_gb300 import ops
+    from pointrix_gb300 import autotune, ops
     from pointrix_gb300 import workloads as WL
     from pointrix_gb300.graph import GraphedStep
     from pointrix_gb300.renderer import MsplatRender
@@ -741,6 +741,7 @@ def run_gb300(args):
             "recompute": recompute,
             "multiview": multi,
             "ssim": loss_ssim,
+            "blend_batch": {"/".join(map(str, k)): b for k, b in autotune.table().items()},
         }
         print(json.dumps(line), flush=True)
     if world > 1:

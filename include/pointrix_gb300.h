@@ -250,6 +250,40 @@ int pgb_alpha_blending_backward_views(const float* records, int64_t n_per_view, 
                                       float* d_conic, float* d_opacity, float* d_feature,
                                       int64_t* info, void* stream);
 
+/* The four blend entry points with the per-block splat batch chosen by the
+ * caller (the run-time autotuner of pointrix_gb300.autotune): forward 64 or
+ * 128 records per batch, backward 64, 128 or 256; 0 = the default (128).
+ * Every batch gives the same images, final transmittance and contributor
+ * counts; the backward's gradient sums are formed in a batch-dependent
+ * order (float atomics).  pgb_blend_batches(backward, out) lists the
+ * compiled batches (returns their count, writes them to out if not NULL). */
+int pgb_alpha_blending_forward_with_batch(const float* uv, const float* conic,
+                                          const float* opacity, const float* feature, int64_t n,
+                                          int channels, const int32_t* ids, int64_t k,
+                                          const int32_t* tile_range, float bg, int width,
+                                          int height, float* records, float* out, float* final_T,
+                                          int32_t* n_contrib, int64_t* info, void* stream,
+                                          int batch);
+int pgb_alpha_blending_backward_with_batch(const float* records, int64_t n, int channels,
+                                           const int32_t* ids, int64_t k,
+                                           const int32_t* tile_range, float bg, int width,
+                                           int height, const float* final_T,
+                                           const int32_t* n_contrib, const float* d_out,
+                                           float* grad_records, float* d_uv, float* d_conic,
+                                           float* d_opacity, float* d_feature, int64_t* info,
+                                           void* stream, int batch);
+int pgb_alpha_blending_forward_views_with_batch(
+    const float* uv, const float* conic, const float* opacity, const float* feature,
+    int64_t n_per_view, int channels, const int32_t* ids, int64_t k, const int32_t* tile_range,
+    float bg, const int32_t* sizes, int nviews, float* records, float* out, float* final_T,
+    int32_t* n_contrib, int64_t* info, void* stream, int batch);
+int pgb_alpha_blending_backward_views_with_batch(
+    const float* records, int64_t n_per_view, int channels, const int32_t* ids, int64_t k,
+    const int32_t* tile_range, float bg, const int32_t* sizes, int nviews, const float* final_T,
+    const int32_t* n_contrib, const float* d_out, float* grad_records, float* d_uv,
+    float* d_conic, float* d_opacity, float* d_feature, int64_t* info, void* stream, int batch);
+int pgb_blend_batches(int backward, int32_t* out);
+
 /* ---------------------------------------------------------------------
  * Adam step over several parameter tensors in one launch -- replaces the
  * torch Adam update of the training step (pointrix/optimizer/optimizer.py:

@@ -45,6 +45,15 @@ SIGNATURES = {
     "pgb_blend_grad_record_floats": [i32],
     "pgb_alpha_blending_forward": [vp, vp, vp, vp, i64, i32, vp, i64, vp, f32, i32, i32, vp, vp, vp, vp, vp, vp],
     "pgb_alpha_blending_backward": [vp, i64, i32, vp, i64, vp, f32, i32, i32, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp],
+    "pgb_alpha_blending_forward_with_batch": [vp, vp, vp, vp, i64, i32, vp, i64, vp, f32, i32, i32, vp, vp,
+                                              vp, vp, vp, vp, i32],
+    "pgb_alpha_blending_backward_with_batch": [vp, i64, i32, vp, i64, vp, f32, i32, i32, vp, vp, vp, vp,
+                                               vp, vp, vp, vp, vp, vp, i32],
+    "pgb_alpha_blending_forward_views_with_batch": [vp, vp, vp, vp, i64, i32, vp, i64, vp, f32, vp, i32,
+                                                    vp, vp, vp, vp, vp, vp, i32],
+    "pgb_alpha_blending_backward_views_with_batch": [vp, i64, i32, vp, i64, vp, f32, vp, i32, vp, vp, vp,
+                                                     vp, vp, vp, vp, vp, vp, vp, i32],
+    "pgb_blend_batches": [i32, vp],
 }
 class AdamSegment(C.Structure):
     """``pgb_adam_segment`` of include/pointrix_gb300.h."""

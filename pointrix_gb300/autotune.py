@@ -1,0 +1,84 @@
+"""Run-time choice of the blend kernels' per-block splat batch.
+
+The blend kernels stage a tile's depth-sorted splats into shared memory in
+batches; the best batch size depends on the image, the channel count and how
+many splats a tile's list holds (short lists waste a large batch's staging,
+long lists pay a small batch's extra barriers).  The library compiles a few
+batch sizes (``pgb_blend_batches``: forward 64/128, backward 64/128/256); all
+give the same images, and the backward the same gradients up to the order of
+its float sums.  On the first call of a workload class this module times
+every compiled batch on the live inputs (CUDA events, one warm-up and two
+timed runs each) and keeps the fastest for the class; later calls -- and
+calls while a CUDA graph is being captured -- use the kept choice (or the
+default before any).  ``PGB_AUTOTUNE=0`` in the environment disables timing
+(the default batch is used).
+
+A class is (kernel, channel count, log2 of the pixel count, log2 of the
+mean list length per tile): the quantities that move the optimum.
+"""
+from __future__ import annotations
+
+import math
+import os
+import threading
+
+import torch
+
+__all__ = ["choose", "workload_class", "table", "reset", "set_enabled"]
+
+_lock = threading.Lock()
+_cache: dict = {}
+_enabled = os.environ.get("PGB_AUTOTUNE", "1") != "0"
+
+
+def workload_class(kind: str, channels: int, pixels: int, entries: int, tiles: int) -> tuple:
+    """The cache key of a blend call."""
+    per_tile = entries / max(tiles, 1)
+    return (kind, int(channels), int(math.log2(max(pixels, 1))), int(math.log2(per_tile + 1)))
+
+
+def _cuda_timer(fn, device) -> float:
+    stream = torch.cuda.current_stream(device)
+    fn()  # warm-up
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    fn()
+    fn()
+    e1.record(stream)
+    e1.synchronize()
+    return e0.elapsed_time(e1) / 2.0
+
+
+def choose(key, candidates, run, device=None, timer=None) -> int:
+    """The batch for ``key``: the cached choice, else (when enabled and not
+    capturing) the fastest of ``candidates`` timed with ``run(batch)``, else
+    0 (the library default)."""
+    with _lock:
+        hit = _cache.get(key)
+    if hit is not None:
+        return hit
+    capturing = torch.cuda.is_available() and torch.cuda.is_current_stream_capturing()
+    if not _enabled or capturing or not candidates:
+        return 0
+    timer = timer or (lambda fn: _cuda_timer(fn, device))
+    times = {b: timer(lambda b=b: run(b)) for b in candidates}
+    best = min(times, key=lambda b: (times[b], b))
+    with _lock:
+        _cache.setdefault(key, best)
+        return _cache[key]
+
+
+def table() -> dict:
+    """The kept choices (class -> batch)."""
+    with _lock:
+        return dict(_cache)
+
+
+def reset() -> None:
+    with _lock:
+        _cache.clear()
+
+
+def set_enabled(flag: bool) -> None:
+    global _enabled
+    _enabled = bool(flag)

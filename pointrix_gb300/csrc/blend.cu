@@ -104,17 +104,19 @@ template <int RF, int NT, int B>
 __device__ inline void issue_batch(const float* __restrict__ records,
                                    const int32_t* __restrict__ ids, int64_t first, int64_t last,
                                    int64_t n, float* stage, uint64_t* bar, int64_t* info) {
-  constexpr int PER = B / NT;  // slots per thread
+  constexpr int PER = (B + NT - 1) / NT;  // slots per thread (at most one here)
   const int lane = threadIdx.x & 31;
   int32_t g[PER];
   bool ok[PER];
   uint32_t nvalid = 0;
 #pragma unroll
   for (int k = 0; k < PER; ++k) {
-    const int64_t e = first + threadIdx.x + k * NT;
-    g[k] = e < last ? ids[e] : -1;
-    ok[k] = e < last && g[k] >= 0 && (int64_t)g[k] < n;
-    if (e < last && !ok[k]) set_info(info, PGB_ERR_OVERFLOW);
+    const int slot = threadIdx.x + k * NT;
+    const int64_t e = first + slot;
+    const bool in = slot < B && e < last;
+    g[k] = in ? ids[e] : -1;
+    ok[k] = in && g[k] >= 0 && (int64_t)g[k] < n;
+    if (in && !ok[k]) set_info(info, PGB_ERR_OVERFLOW);
     nvalid += __popc(__ballot_sync(0xffffffffu, ok[k]));
   }
   if (lane == 0) mbar_arrive_expect_tx(bar, nvalid * RF * 4u);
@@ -132,10 +134,10 @@ __device__ inline void stage_batch(const float* __restrict__ records,
                                    const int32_t* __restrict__ ids, int64_t first, int64_t last,
                                    int64_t n, float* stage, int64_t* info) {
 #pragma unroll
-  for (int k = 0; k < B / NT; ++k) {
+  for (int k = 0; k < (B + NT - 1) / NT; ++k) {
     const int slot = threadIdx.x + k * NT;
     const int64_t e = first + slot;
-    if (e < last) {
+    if (slot < B && e < last) {
       const int32_t g = ids[e];
       if (g < 0 || (int64_t)g >= n) {
         set_info(info, PGB_ERR_OVERFLOW);
@@ -267,9 +269,9 @@ __device__ __forceinline__ int warp_cull(const float* stage, int RF, int cnt, fl
 // one TMA bulk copy per thread per batch.
 constexpr int kFwdThreads = 128;
 constexpr int kFwdPix = 2;
-constexpr int kFwdBatch = 128;
+constexpr int kFwdBatch = 128;  // default records per batch (64 and 128 are compiled)
 
-template <int NC, int RF>
+template <int NC, int RF, int B>
 __global__ void __launch_bounds__(kFwdThreads) blend_fwd_kernel(
     const float* __restrict__ records, const int32_t* __restrict__ ids,
     const int2* __restrict__ ranges, int64_t n, float bg, const ViewTable vt, int C,
@@ -277,7 +279,7 @@ __global__ void __launch_bounds__(kFwdThreads) blend_fwd_kernel(
     int64_t* __restrict__ info) {
   extern __shared__ __align__(128) float smem[];
   __shared__ __align__(8) uint64_t bars[2];
-  __shared__ uint8_t s_list[kFwdThreads / 32][kFwdBatch];
+  __shared__ uint8_t s_list[kFwdThreads / 32][B];
 
   const int tile = blockIdx.x;  // global tile (of its view, for a batch)
   int W, H, gx, ltile;
@@ -297,7 +299,7 @@ __global__ void __launch_bounds__(kFwdThreads) blend_fwd_kernel(
 
   const int2 rg = ranges[tile];
   const int64_t start = rg.x, end = rg.y;
-  const int nb = end > start ? (int)((end - start + kFwdBatch - 1) / kFwdBatch) : 0;
+  const int nb = end > start ? (int)((end - start + B - 1) / B) : 0;
 
   const int px = bx0 + (lane & 7);
   float pyf[kFwdPix], T[kFwdPix], acc[kFwdPix][NC];
@@ -318,25 +320,25 @@ __global__ void __launch_bounds__(kFwdThreads) blend_fwd_kernel(
   bool timed_out = false;
 
   if (nb > 0)
-    issue_batch<RF, kFwdThreads, kFwdBatch>(records, ids, start, end, n, smem, &bars[0], info);
+    issue_batch<RF, kFwdThreads, B>(records, ids, start, end, n, smem, &bars[0], info);
   for (int b = 0; b < nb; ++b) {
     const int buf = b & 1;
-    const int64_t first = start + (int64_t)b * kFwdBatch;
+    const int64_t first = start + (int64_t)b * B;
     if (b + 1 < nb)
-      issue_batch<RF, kFwdThreads, kFwdBatch>(records, ids, first + kFwdBatch, end, n,
-                                              smem + (buf ^ 1) * kFwdBatch * RF, &bars[buf ^ 1],
+      issue_batch<RF, kFwdThreads, B>(records, ids, first + B, end, n,
+                                              smem + (buf ^ 1) * B * RF, &bars[buf ^ 1],
                                               info);
     // every thread observes the phase (that makes the TMA writes visible to
     // it); the outcome is made block-uniform before any warp collective
     timed_out = __syncthreads_or(!mbar_wait_bounded(&bars[buf], (b >> 1) & 1));
     if (timed_out && threadIdx.x == 0) set_info(info, PGB_ERR_TIMEOUT);
-    const int cnt = (int)(end - first < kFwdBatch ? end - first : kFwdBatch);
-    const float* st = smem + buf * kFwdBatch * RF;
+    const int cnt = (int)(end - first < B ? end - first : B);
+    const float* st = smem + buf * B * RF;
     bool all_done = true;
 #pragma unroll
     for (int q = 0; q < kFwdPix; ++q) all_done &= done[q];
     if (!timed_out && !__all_sync(0xffffffffu, all_done)) {
-      const int nl = warp_cull<8, 8, kFwdBatch>(st, RF, cnt, (float)bx0, (float)by0, my_list);
+      const int nl = warp_cull<8, 8, B>(st, RF, cnt, (float)bx0, (float)by0, my_list);
       const int base = (int)(first - start) + 1;
       for (int t = 0; t < nl; ++t) {
         const int j = my_list[t];
@@ -476,7 +478,7 @@ __device__ __forceinline__ bool bwd_pixel(BwdPixel<NC>& P, int j, const float* r
   return true;
 }
 
-template <int NC, int RF, int GR>
+template <int NC, int RF, int GR, int B>
 __global__ void __launch_bounds__(kBwdThreads) blend_bwd_kernel(
     const float* __restrict__ records, const int32_t* __restrict__ ids,
     const int2* __restrict__ ranges, int64_t n, float bg, const ViewTable vt, int C,
@@ -486,9 +488,9 @@ __global__ void __launch_bounds__(kBwdThreads) blend_bwd_kernel(
   static_assert(GR == 16 || GR == 32, "gradient records are 16 or 32 floats");
   extern __shared__ __align__(128) float smem[];
   __shared__ int s_max_nc;
-  __shared__ uint8_t s_touched[kBwdBatch];
-  __shared__ uint8_t s_list[kBwdThreads / 32][kBwdBatch];
-  float* gacc = smem + 2 * kBwdBatch * RF;  // [kBwdBatch][GR]
+  __shared__ uint8_t s_touched[B];
+  __shared__ uint8_t s_list[kBwdThreads / 32][B];
+  float* gacc = smem + 2 * B * RF;  // [B][GR]
 
   const int tile = blockIdx.x;  // global tile (of its view, for a batch)
   int W, H, gx, ltile;
@@ -500,8 +502,8 @@ __global__ void __launch_bounds__(kBwdThreads) blend_bwd_kernel(
   uint8_t* my_list = s_list[w];
 
   if (threadIdx.x == 0) s_max_nc = 0;
-  for (int i = threadIdx.x; i < kBwdBatch * GR; i += kBwdThreads) gacc[i] = 0.f;
-  for (int i = threadIdx.x; i < kBwdBatch; i += kBwdThreads) s_touched[i] = 0;
+  for (int i = threadIdx.x; i < B * GR; i += kBwdThreads) gacc[i] = 0.f;
+  for (int i = threadIdx.x; i < B; i += kBwdThreads) s_touched[i] = 0;
   __syncthreads();
 
   const int64_t plane = (int64_t)W * H;
@@ -541,31 +543,31 @@ __global__ void __launch_bounds__(kBwdThreads) blend_bwd_kernel(
   const int list_len = max(0, rg.y - rg.x);
   if (s_max_nc > list_len && threadIdx.x == 0) set_info(info, PGB_ERR_OVERFLOW);
   const int max_nc = min(s_max_nc, list_len);
-  const int nb = (max_nc + kBwdBatch - 1) / kBwdBatch;
+  const int nb = (max_nc + B - 1) / B;
 
-  // batch b covers list positions [hi_b - kBwdBatch, hi_b) with
-  // hi_b = max_nc - b*kBwdBatch, clipped at 0; slot t holds position lo_b + t.
-  auto lo_of = [&](int b) { return max(0, max_nc - (b + 1) * kBwdBatch); };
-  auto hi_of = [&](int b) { return max_nc - b * kBwdBatch; };
+  // batch b covers list positions [hi_b - B, hi_b) with
+  // hi_b = max_nc - b*B, clipped at 0; slot t holds position lo_b + t.
+  auto lo_of = [&](int b) { return max(0, max_nc - (b + 1) * B); };
+  auto hi_of = [&](int b) { return max_nc - b * B; };
 
   if (nb > 0)
-    stage_batch<RF, kBwdThreads, kBwdBatch>(records, ids, start + lo_of(0), start + hi_of(0), n,
+    stage_batch<RF, kBwdThreads, B>(records, ids, start + lo_of(0), start + hi_of(0), n,
                                             smem, info);
   for (int b = 0; b < nb; ++b) {
     const int buf = b & 1;
     const int lo = lo_of(b), hi = hi_of(b);
     if (b + 1 < nb) {
-      stage_batch<RF, kBwdThreads, kBwdBatch>(records, ids, start + lo_of(b + 1),
+      stage_batch<RF, kBwdThreads, B>(records, ids, start + lo_of(b + 1),
                                               start + hi_of(b + 1), n,
-                                              smem + (buf ^ 1) * kBwdBatch * RF, info);
+                                              smem + (buf ^ 1) * B * RF, info);
       cp_async_wait<1>();  // this thread's copies of batch b have landed
     } else {
       cp_async_wait<0>();
     }
     __syncthreads();  // ... and everyone's
-    const float* st = smem + buf * kBwdBatch * RF;
+    const float* st = smem + buf * B * RF;
     {
-      const int nl = warp_cull<8, 8, kBwdBatch>(st, RF, min(hi, warp_nc) - lo, (float)bx0,
+      const int nl = warp_cull<8, 8, B>(st, RF, min(hi, warp_nc) - lo, (float)bx0,
                                                (float)by0, my_list);
       for (int t = nl - 1; t >= 0; --t) {
         const int slot = my_list[t];
@@ -637,13 +639,13 @@ __global__ void unpack_kernel(const float* __restrict__ g, int64_t n, int C,
 }
 
 // ------------------------------------------------------------- dispatch
-template <int NC>
-static int launch_fwd_nc(const float* records, const int32_t* ids, const int2* ranges, int64_t n,
-                         float bg, const ViewTable& vt, int tiles, int C, float* out, float* fT,
-                         int32_t* ncon, int64_t* info, cudaStream_t s) {
+template <int NC, int B>
+static int launch_fwd_b(const float* records, const int32_t* ids, const int2* ranges, int64_t n,
+                        float bg, const ViewTable& vt, int tiles, int C, float* out, float* fT,
+                        int32_t* ncon, int64_t* info, cudaStream_t s) {
   constexpr int RF = rec_floats(NC);
-  const size_t smem = 2 * kFwdBatch * RF * sizeof(float);
-  auto kern = blend_fwd_kernel<NC, RF>;
+  const size_t smem = 2 * B * RF * sizeof(float);
+  auto kern = blend_fwd_kernel<NC, RF, B>;
   if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
       cudaSuccess)
     return PGB_ERR_CUDA;
@@ -651,21 +653,48 @@ static int launch_fwd_nc(const float* records, const int32_t* ids, const int2* r
   return launch_status();
 }
 
+// batch: records per batch, 64 or 128 (0: the default).  One TMA bulk copy
+// per thread per phase at most in both.
 template <int NC>
-static int launch_bwd_nc(const float* records, const int32_t* ids, const int2* ranges, int64_t n,
-                         float bg, const ViewTable& vt, int tiles, int C, const float* fT,
-                         const int32_t* ncon, const float* dout, float* grec, int64_t* info,
-                         cudaStream_t s) {
+static int launch_fwd_nc(const float* records, const int32_t* ids, const int2* ranges, int64_t n,
+                         float bg, const ViewTable& vt, int tiles, int C, float* out, float* fT,
+                         int32_t* ncon, int64_t* info, cudaStream_t s, int batch) {
+  switch (batch == 0 ? kFwdBatch : batch) {
+    case 64: return launch_fwd_b<NC, 64>(records, ids, ranges, n, bg, vt, tiles, C, out, fT, ncon, info, s);
+    case 128: return launch_fwd_b<NC, 128>(records, ids, ranges, n, bg, vt, tiles, C, out, fT, ncon, info, s);
+    default: return PGB_ERR_INVALID;
+  }
+}
+
+template <int NC, int B>
+static int launch_bwd_b(const float* records, const int32_t* ids, const int2* ranges, int64_t n,
+                        float bg, const ViewTable& vt, int tiles, int C, const float* fT,
+                        const int32_t* ncon, const float* dout, float* grec, int64_t* info,
+                        cudaStream_t s) {
   constexpr int RF = rec_floats(NC);
   constexpr int GR = grad_floats(NC);
-  const size_t smem = (2 * RF + GR) * kBwdBatch * sizeof(float);
-  auto kern = blend_bwd_kernel<NC, RF, GR>;
+  const size_t smem = (2 * RF + GR) * B * sizeof(float);
+  auto kern = blend_bwd_kernel<NC, RF, GR, B>;
   if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
       cudaSuccess)
     return PGB_ERR_CUDA;
   kern<<<tiles, kBwdThreads, smem, s>>>(records, ids, ranges, n, bg, vt, C, fT, ncon, dout, grec,
                                         info);
   return launch_status();
+}
+
+// batch: 64, 128 or 256 splats per backward batch (0: the default).
+template <int NC>
+static int launch_bwd_nc(const float* records, const int32_t* ids, const int2* ranges, int64_t n,
+                         float bg, const ViewTable& vt, int tiles, int C, const float* fT,
+                         const int32_t* ncon, const float* dout, float* grec, int64_t* info,
+                         cudaStream_t s, int batch) {
+  switch (batch == 0 ? kBwdBatch : batch) {
+    case 64: return launch_bwd_b<NC, 64>(records, ids, ranges, n, bg, vt, tiles, C, fT, ncon, dout, grec, info, s);
+    case 128: return launch_bwd_b<NC, 128>(records, ids, ranges, n, bg, vt, tiles, C, fT, ncon, dout, grec, info, s);
+    case 256: return launch_bwd_b<NC, 256>(records, ids, ranges, n, bg, vt, tiles, C, fT, ncon, dout, grec, info, s);
+    default: return PGB_ERR_INVALID;
+  }
 }
 
 // Channel counts with a compiled kernel; other counts round up (extra
@@ -701,7 +730,7 @@ static int blend_forward_impl(const float* uv, const float* conic, const float* 
                               const float* feature, int64_t n, int channels, const int32_t* ids,
                               int64_t k, const int32_t* tile_range, float bg, const ViewTable& vt,
                               int tiles, float* records, float* out, float* final_T,
-                              int32_t* n_contrib, int64_t* info, void* stream) {
+                              int32_t* n_contrib, int64_t* info, void* stream, int batch) {
   const int nc = nc_bucket(channels);
   if (n < 0 || k < 0 || tiles <= 0 || channels < 1 || nc < 0) return PGB_ERR_INVALID;
   if (!tile_range || !out || !final_T || !n_contrib || (k > 0 && !ids)) return PGB_ERR_INVALID;
@@ -716,7 +745,7 @@ static int blend_forward_impl(const float* uv, const float* conic, const float* 
                                                                            feature, n, channels, \
                                                                            records);            \
     return launch_fwd_nc<N>(records, ids, rg, n, bg, vt, tiles, channels, out, final_T,          \
-                            n_contrib, info, s);
+                            n_contrib, info, s, batch);
     PGB_FOR_NC(PGB_CASE)
 #undef PGB_CASE
     default:
@@ -729,7 +758,7 @@ static int blend_backward_impl(const float* records, int64_t n, int channels, co
                                int tiles, const float* final_T, const int32_t* n_contrib,
                                const float* d_out, float* grad_records, float* d_uv,
                                float* d_conic, float* d_opacity, float* d_feature, int64_t* info,
-                               void* stream) {
+                               void* stream, int batch) {
   const int nc = nc_bucket(channels);
   if (n < 0 || k < 0 || tiles <= 0 || channels < 1 || nc < 0) return PGB_ERR_INVALID;
   if (!tile_range || !final_T || !n_contrib || !d_out || (k > 0 && !ids)) return PGB_ERR_INVALID;
@@ -746,7 +775,7 @@ static int blend_backward_impl(const float* records, int64_t n, int channels, co
 #define PGB_CASE(N)                                                                          \
   case N:                                                                                    \
     st = launch_bwd_nc<N>(records, ids, rg, n, bg, vt, tiles, channels, final_T, n_contrib,  \
-                          d_out, grad_records, info, s);                                     \
+                          d_out, grad_records, info, s, batch);                              \
     break;
     PGB_FOR_NC(PGB_CASE)
 #undef PGB_CASE
@@ -765,15 +794,42 @@ static int blend_backward_impl(const float* records, int64_t n, int channels, co
 
 extern "C" {
 
+int pgb_alpha_blending_forward_with_batch(const float* uv, const float* conic,
+                                          const float* opacity, const float* feature, int64_t n,
+                                          int channels, const int32_t* ids, int64_t k,
+                                          const int32_t* tile_range, float bg, int width,
+                                          int height, float* records, float* out, float* final_T,
+                                          int32_t* n_contrib, int64_t* info, void* stream,
+                                          int batch) {
+  if (width <= 0 || height <= 0) return PGB_ERR_INVALID;
+  return blend_forward_impl(uv, conic, opacity, feature, n, channels, ids, k, tile_range, bg,
+                            single_view(width, height), grid_x(width) * grid_y(height), records,
+                            out, final_T, n_contrib, info, stream, batch);
+}
+
 int pgb_alpha_blending_forward(const float* uv, const float* conic, const float* opacity,
                                const float* feature, int64_t n, int channels, const int32_t* ids,
                                int64_t k, const int32_t* tile_range, float bg, int width,
                                int height, float* records, float* out, float* final_T,
                                int32_t* n_contrib, int64_t* info, void* stream) {
+  return pgb_alpha_blending_forward_with_batch(uv, conic, opacity, feature, n, channels, ids, k,
+                                               tile_range, bg, width, height, records, out,
+                                               final_T, n_contrib, info, stream, 0);
+}
+
+int pgb_alpha_blending_backward_with_batch(const float* records, int64_t n, int channels,
+                                           const int32_t* ids, int64_t k,
+                                           const int32_t* tile_range, float bg, int width,
+                                           int height, const float* final_T,
+                                           const int32_t* n_contrib, const float* d_out,
+                                           float* grad_records, float* d_uv, float* d_conic,
+                                           float* d_opacity, float* d_feature, int64_t* info,
+                                           void* stream, int batch) {
   if (width <= 0 || height <= 0) return PGB_ERR_INVALID;
-  return blend_forward_impl(uv, conic, opacity, feature, n, channels, ids, k, tile_range, bg,
-                            single_view(width, height), grid_x(width) * grid_y(height), records,
-                            out, final_T, n_contrib, info, stream);
+  return blend_backward_impl(records, n, channels, ids, k, tile_range, bg,
+                             single_view(width, height), grid_x(width) * grid_y(height), final_T,
+                             n_contrib, d_out, grad_records, d_uv, d_conic, d_opacity, d_feature,
+                             info, stream, batch);
 }
 
 int pgb_alpha_blending_backward(const float* records, int64_t n, int channels,
@@ -782,11 +838,24 @@ int pgb_alpha_blending_backward(const float* records, int64_t n, int channels,
                                 const int32_t* n_contrib, const float* d_out, float* grad_records,
                                 float* d_uv, float* d_conic, float* d_opacity, float* d_feature,
                                 int64_t* info, void* stream) {
-  if (width <= 0 || height <= 0) return PGB_ERR_INVALID;
-  return blend_backward_impl(records, n, channels, ids, k, tile_range, bg,
-                             single_view(width, height), grid_x(width) * grid_y(height), final_T,
-                             n_contrib, d_out, grad_records, d_uv, d_conic, d_opacity, d_feature,
-                             info, stream);
+  return pgb_alpha_blending_backward_with_batch(records, n, channels, ids, k, tile_range, bg, width,
+                                                height, final_T, n_contrib, d_out, grad_records,
+                                                d_uv, d_conic, d_opacity, d_feature, info, stream,
+                                                0);
+}
+
+int pgb_alpha_blending_forward_views_with_batch(
+    const float* uv, const float* conic, const float* opacity, const float* feature,
+    int64_t n_per_view, int channels, const int32_t* ids, int64_t k, const int32_t* tile_range,
+    float bg, const int32_t* sizes, int nviews, float* records, float* out, float* final_T,
+    int32_t* n_contrib, int64_t* info, void* stream, int batch) {
+  ViewTable vt;
+  uint32_t T = 0;
+  int64_t pixels = 0;
+  if (!make_views(sizes, nviews, n_per_view, vt, T, pixels)) return PGB_ERR_INVALID;
+  return blend_forward_impl(uv, conic, opacity, feature, n_per_view * nviews, channels, ids, k,
+                            tile_range, bg, vt, (int)T, records, out, final_T, n_contrib, info,
+                            stream, batch);
 }
 
 int pgb_alpha_blending_forward_views(const float* uv, const float* conic, const float* opacity,
@@ -795,13 +864,24 @@ int pgb_alpha_blending_forward_views(const float* uv, const float* conic, const 
                                      float bg, const int32_t* sizes, int nviews, float* records,
                                      float* out, float* final_T, int32_t* n_contrib,
                                      int64_t* info, void* stream) {
+  return pgb_alpha_blending_forward_views_with_batch(uv, conic, opacity, feature, n_per_view,
+                                                     channels, ids, k, tile_range, bg, sizes,
+                                                     nviews, records, out, final_T, n_contrib,
+                                                     info, stream, 0);
+}
+
+int pgb_alpha_blending_backward_views_with_batch(
+    const float* records, int64_t n_per_view, int channels, const int32_t* ids, int64_t k,
+    const int32_t* tile_range, float bg, const int32_t* sizes, int nviews, const float* final_T,
+    const int32_t* n_contrib, const float* d_out, float* grad_records, float* d_uv,
+    float* d_conic, float* d_opacity, float* d_feature, int64_t* info, void* stream, int batch) {
   ViewTable vt;
   uint32_t T = 0;
   int64_t pixels = 0;
   if (!make_views(sizes, nviews, n_per_view, vt, T, pixels)) return PGB_ERR_INVALID;
-  return blend_forward_impl(uv, conic, opacity, feature, n_per_view * nviews, channels, ids, k,
-                            tile_range, bg, vt, (int)T, records, out, final_T, n_contrib, info,
-                            stream);
+  return blend_backward_impl(records, n_per_view * nviews, channels, ids, k, tile_range, bg, vt,
+                             (int)T, final_T, n_contrib, d_out, grad_records, d_uv, d_conic,
+                             d_opacity, d_feature, info, stream, batch);
 }
 
 int pgb_alpha_blending_backward_views(const float* records, int64_t n_per_view, int channels,
@@ -811,13 +891,19 @@ int pgb_alpha_blending_backward_views(const float* records, int64_t n_per_view, 
                                       const float* d_out, float* grad_records, float* d_uv,
                                       float* d_conic, float* d_opacity, float* d_feature,
                                       int64_t* info, void* stream) {
-  ViewTable vt;
-  uint32_t T = 0;
-  int64_t pixels = 0;
-  if (!make_views(sizes, nviews, n_per_view, vt, T, pixels)) return PGB_ERR_INVALID;
-  return blend_backward_impl(records, n_per_view * nviews, channels, ids, k, tile_range, bg, vt,
-                             (int)T, final_T, n_contrib, d_out, grad_records, d_uv, d_conic,
-                             d_opacity, d_feature, info, stream);
+  return pgb_alpha_blending_backward_views_with_batch(
+      records, n_per_view, channels, ids, k, tile_range, bg, sizes, nviews, final_T, n_contrib,
+      d_out, grad_records, d_uv, d_conic, d_opacity, d_feature, info, stream, 0);
+}
+
+// Batch sizes compiled for the forward (backward = 0) or the backward (1).
+int pgb_blend_batches(int backward, int32_t* out) {
+  static const int32_t f[] = {64, 128}, b[] = {64, 128, 256};
+  const int32_t* src = backward ? b : f;
+  const int cnt = backward ? 3 : 2;
+  if (out)
+    for (int i = 0; i < cnt; ++i) out[i] = src[i];
+  return cnt;
 }
 
 }  // extern "C"

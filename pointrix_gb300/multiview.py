@@ -18,7 +18,7 @@ import ctypes as C
 
 import torch
 
-from . import _lib, fused, ops
+from . import _lib, autotune, fused, ops
 from ._lib import call
 from .ops import _c, _ptr, _status_word, _stream, _timed
 
@@ -77,11 +77,17 @@ class _BlendViews(torch.autograd.Function):
         final_T = torch.empty(P, dtype=torch.float32, device=dev)
         ncon = torch.empty(P, dtype=torch.int32, device=dev)
         sz = _sizes_array(sizes)
-        with _timed("alpha_blending_fwd", dev, 2 if n else 1):
-            call("pgb_alpha_blending_forward_views", _ptr(uv), _ptr(conic), _ptr(opacity),
+
+        def run(batch):
+            call("pgb_alpha_blending_forward_views_with_batch", _ptr(uv), _ptr(conic), _ptr(opacity),
                  _ptr(feature), n_per_view, Cc, _ptr(ids), ids.numel(), _ptr(tile_range), float(bg),
                  sz, len(sizes), _ptr(records), _ptr(out), _ptr(final_T), _ptr(ncon),
-                 _ptr(_status_word(dev)), _stream(dev))
+                 _ptr(_status_word(dev)), _stream(dev), batch)
+
+        key = autotune.workload_class("blend_fwd", Cc, P, ids.numel(), tile_range.shape[0])
+        batch = autotune.choose(key, ops._blend_batches(0), run, dev) if n else 0
+        with _timed("alpha_blending_fwd", dev, 2 if n else 1):
+            run(batch)
         ctx.save_for_backward(records, ids, tile_range, final_T, ncon)
         ctx.cfg = (n, Cc, float(bg), tuple(sizes), n_per_view)
         return out
@@ -97,11 +103,20 @@ class _BlendViews(torch.autograd.Function):
         d_conic = torch.empty(n, 3, dtype=torch.float32, device=dev)
         d_op = torch.empty(n, dtype=torch.float32, device=dev)
         d_feat = torch.empty(n, Cc, dtype=torch.float32, device=dev)
+        d_out = _c(d_out)
+        sz = _sizes_array(sizes)
+        P = sum(W * H for W, H in sizes)
+
+        def run(batch):
+            call("pgb_alpha_blending_backward_views_with_batch", _ptr(records), n_per_view, Cc,
+                 _ptr(ids), ids.numel(), _ptr(tile_range), bg, sz, len(sizes), _ptr(final_T),
+                 _ptr(ncon), _ptr(d_out), _ptr(grec), _ptr(d_uv), _ptr(d_conic), _ptr(d_op),
+                 _ptr(d_feat), _ptr(_status_word(dev)), _stream(dev), batch)
+
+        key = autotune.workload_class("blend_bwd", Cc, P, ids.numel(), tile_range.shape[0])
+        batch = autotune.choose(key, ops._blend_batches(1), run, dev) if n else 0
         with _timed("alpha_blending_bwd", dev, 2 if n else 0):
-            call("pgb_alpha_blending_backward_views", _ptr(records), n_per_view, Cc, _ptr(ids),
-                 ids.numel(), _ptr(tile_range), bg, _sizes_array(sizes), len(sizes), _ptr(final_T),
-                 _ptr(ncon), _ptr(_c(d_out)), _ptr(grec), _ptr(d_uv), _ptr(d_conic), _ptr(d_op),
-                 _ptr(d_feat), _ptr(_status_word(dev)), _stream(dev))
+            run(batch)
         return d_uv, d_conic, d_op, d_feat, None, None, None, None, None
 
 

@@ -15,7 +15,7 @@ import threading
 
 import torch
 
-from . import _lib
+from . import _lib, autotune
 from ._lib import PgbError, call
 
 __all__ = [
@@ -540,6 +540,21 @@ def sort_gaussian(uv, depth, W, H, radius, tiles_touched, capacity=None):
 # ---------------------------------------------------------------------------
 # alpha_blending
 # ---------------------------------------------------------------------------
+_BATCHES: dict = {}
+
+
+def _blend_batches(backward: int) -> tuple:
+    """Per-block splat batches the library compiled for the forward (0) or
+    the backward (1) blend."""
+    hit = _BATCHES.get(backward)
+    if hit is None:
+        import ctypes as C
+        buf = (C.c_int32 * 8)()
+        cnt = _lib.lib().pgb_blend_batches(backward, buf)
+        hit = _BATCHES[backward] = tuple(buf[i] for i in range(cnt))
+    return hit
+
+
 def _blend_forward_raw(uv, conic, opacity, feature, ids, tile_range, bg, W, H):
     n, C = feature.shape
     dev = feature.device
@@ -549,10 +564,16 @@ def _blend_forward_raw(uv, conic, opacity, feature, ids, tile_range, bg, W, H):
     final_T = torch.empty(H, W, dtype=torch.float32, device=dev)
     ncon = torch.empty(H, W, dtype=torch.int32, device=dev)
     status = _status_word(dev)
+
+    def run(batch):
+        call("pgb_alpha_blending_forward_with_batch", _ptr(uv), _ptr(conic), _ptr(opacity),
+             _ptr(feature), n, C, _ptr(ids), ids.numel(), _ptr(tile_range), float(bg), W, H,
+             _ptr(records), _ptr(out), _ptr(final_T), _ptr(ncon), _ptr(status), _stream(dev), batch)
+
+    key = autotune.workload_class("blend_fwd", C, W * H, ids.numel(), tile_range.shape[0])
+    batch = autotune.choose(key, _blend_batches(0), run, dev) if n else 0
     with _timed("alpha_blending_fwd", dev, 2 if n else 1):
-        call("pgb_alpha_blending_forward", _ptr(uv), _ptr(conic), _ptr(opacity), _ptr(feature), n, C,
-             _ptr(ids), ids.numel(), _ptr(tile_range), float(bg), W, H, _ptr(records), _ptr(out),
-             _ptr(final_T), _ptr(ncon), _ptr(status), _stream(dev))
+        run(batch)
     return records, out, final_T, ncon
 
 
@@ -564,11 +585,17 @@ def _blend_backward_raw(records, ids, tile_range, final_T, ncon, d_out, n, C, bg
     d_op = torch.empty(n, dtype=torch.float32, device=dev)
     d_feat = torch.empty(n, C, dtype=torch.float32, device=dev)
     status = _status_word(dev)
+    d_out = _c(d_out)
+
+    def run(batch):
+        call("pgb_alpha_blending_backward_with_batch", _ptr(records), n, C, _ptr(ids), ids.numel(),
+             _ptr(tile_range), bg, W, H, _ptr(final_T), _ptr(ncon), _ptr(d_out), _ptr(grec),
+             _ptr(d_uv), _ptr(d_conic), _ptr(d_op), _ptr(d_feat), _ptr(status), _stream(dev), batch)
+
+    key = autotune.workload_class("blend_bwd", C, W * H, ids.numel(), tile_range.shape[0])
+    batch = autotune.choose(key, _blend_batches(1), run, dev) if n else 0
     with _timed("alpha_blending_bwd", dev, 2 if n else 0):
-        call("pgb_alpha_blending_backward", _ptr(records), n, C, _ptr(ids), ids.numel(),
-             _ptr(tile_range), bg, W, H, _ptr(final_T), _ptr(ncon), _ptr(_c(d_out)),
-             _ptr(grec), _ptr(d_uv), _ptr(d_conic), _ptr(d_op), _ptr(d_feat), _ptr(status),
-             _stream(dev))
+        run(batch)
     return d_uv, d_conic, d_op, d_feat
 
 

@@ -365,3 +365,35 @@ def test_recompute_backward_matches_stored(small):
     for a, b in zip(outs[False][1], outs[True][1]):
         assert float((a - b).norm() / b.norm()) < 1e-4
     assert torch.equal(outs[True][2], outs[True][1][0])
+
+
+def test_blend_batches_agree(small):
+    """Every compiled per-block batch gives the same forward outputs (bit for
+    bit) and the same gradients (float sums in another order: 1e-5)."""
+    from pointrix_gb300 import autotune
+    p = small
+    C = p.feat.shape[1]
+    key_f = autotune.workload_class("blend_fwd", C, p.W * p.H, p.ids.numel(), p.rng.shape[0])
+    key_b = autotune.workload_class("blend_bwd", C, p.W * p.H, p.ids.numel(), p.rng.shape[0])
+    up = torch.randn((C, p.H, p.W), generator=torch.Generator().manual_seed(3)).to(DEV)
+    outs, grads = [], []
+    try:
+        for bf in ops._blend_batches(0):
+            for bb in ops._blend_batches(1):
+                autotune.reset()
+                autotune._cache[key_f] = bf
+                autotune._cache[key_b] = bb
+                leaves = [t.detach().clone().requires_grad_(True) for t in (p.uv, p.conic, p.op, p.feat)]
+                img, fT, nc = ops.alpha_blending_with_state(*leaves, p.ids, p.rng, 0.1, p.W, p.H)
+                img.backward(up)
+                outs.append((img.detach(), fT, nc))
+                grads.append([t.grad for t in leaves])
+    finally:
+        autotune.reset()
+    for o in outs[1:]:
+        for a, b in zip(o, outs[0]):
+            assert torch.equal(a, b)
+    for g in grads[1:]:
+        for a, b in zip(g, grads[0]):
+            assert scaled_err(a, b) < 1e-5
+    ops.check_device_status()
