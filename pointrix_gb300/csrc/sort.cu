@@ -17,12 +17,14 @@
 //      id order), and the tile digit histograms of all its entries (one
 //      update per rectangle row); scan_rect: a single-pass decoupled-look-back
 //      scan of the counts in depth order gives each Gaussian its output
-//      offset; emit then writes the (tile id, Gaussian id) pairs chunk by
-//      chunk of the output (load-balanced however unevenly the tiles are
-//      spread over Gaussians);
+//      offset (its emission record);
 //   4. one stable onesweep pass for T <= 256 tiles, two 8-bit passes up to
 //      65,536 tiles, two 9-bit passes up to 2^18 (batches of views), else
-//      three, sort the pairs by tile id; the last pass writes only the ids
+//      three, sort the (tile id, Gaussian id) pairs by tile id.  The first
+//      pass generates its partition's pairs from the emission records in
+//      registers (load-balanced: every partition is 6144 pairs however
+//      unevenly the tiles are spread over Gaussians), so the depth-ordered
+//      pair sequence is never written out; the last pass writes only the ids
 //      and records each tile's [start, end) as it goes;
 //   5. tiles that no entry reached get [0, 0).
 // A stable sort by tile of a depth-ordered sequence is exactly the order of
@@ -51,6 +53,9 @@ constexpr int kSortThreads = 256;
 constexpr int kPartKeys = 6144;  // keys per onesweep partition
 constexpr int kScanItems = 8;
 constexpr int kScanPart = kSortThreads * kScanItems;  // 2048
+// Chunk of the tile-entry sequence whose first owner the scan records; a
+// onesweep partition is kPartKeys / kEmitChunk chunks.
+constexpr int kEmitChunk = 1024;
 constexpr int kDepthPasses = 4;
 constexpr int kMaxTilePasses = 3;
 constexpr int kTileHistWords = 1024;  // 3 passes x 256 digits or 2 x 512
@@ -226,26 +231,146 @@ __device__ inline int64_t pass_count(const int64_t* n_dev, int64_t cap) {
   return (k >= 0 && k <= cap) ? k : 0;
 }
 
-// Lanes of the warp whose RB-bit digit equals this lane's (among `valid` lanes).
+// Lanes of the warp whose RB-bit digit equals this lane's (among `valid`
+// lanes); digit bits from `live` on are zero in every key of the pass.
 template <int RB>
-__device__ inline uint32_t match_digit(uint32_t d, bool valid) {
+__device__ inline uint32_t match_digit(uint32_t d, bool valid, int live) {
   uint32_t peers = __ballot_sync(0xffffffffu, valid);
 #pragma unroll
   for (int b = 0; b < RB; ++b) {
-    const bool bit = (d >> b) & 1u;
-    const uint32_t bb = __ballot_sync(0xffffffffu, bit);
-    peers &= bit ? bb : ~bb;
+    if (b < live) {  // uniform
+      const bool bit = (d >> b) & 1u;
+      const uint32_t bb = __ballot_sync(0xffffffffu, bit);
+      peers &= bit ? bb : ~bb;
+    }
   }
   return peers;
 }
 
-template <int RB, bool KEYS_OUT, bool RANGES>
+// q = a / b, r = a % b for b >= 1: a float estimate (exact to +-1 below
+// 2^22: the reciprocal and the product each carry one rounding) corrected
+// once; larger a takes the integer division.
+__device__ inline void divmod_u32(uint32_t a, uint32_t b, uint32_t& q, uint32_t& r) {
+  if (a < (1u << 22)) {
+    uint32_t q0 = __float2uint_rz(__uint2float_rn(a) * __frcp_rn(__uint2float_rn(b)));
+    int r0 = (int)a - (int)(q0 * b);
+    if (r0 < 0) {
+      --q0;
+      r0 += (int)b;
+    } else if (r0 >= (int)b) {
+      ++q0;
+      r0 -= (int)b;
+    }
+    q = q0;
+    r = (uint32_t)r0;
+  } else {
+    q = a / b;
+    r = a - q * b;
+  }
+}
+
+// The owner records (first tile, w | gx << 16, g, offset) of a partition's
+// entries: positions [i0, i1] of the depth order, staged in shared memory
+// (STAGED) when they fit, else read from global memory.
+template <bool STAGED>
+struct OwnerView {
+  const uint4* g;
+  const uint4* s;
+  uint32_t i0;
+  __device__ uint4 rec(uint32_t i) const { return STAGED ? s[i - i0] : g[i]; }
+  __device__ uint32_t off(uint32_t i) const { return STAGED ? s[i - i0].w : g[i].w; }
+};
+
+// Last position in [lo, hi] whose offset is <= e (offset(lo) <= e).
+template <bool STAGED>
+__device__ inline uint32_t owner_search(const OwnerView<STAGED>& ov, uint32_t lo, uint32_t hi,
+                                        uint32_t e) {
+  while (lo < hi) {
+    const uint32_t mid = lo + ((hi - lo + 1) >> 1);
+    if (ov.off(mid) <= e) lo = mid; else hi = mid - 1;
+  }
+  return lo;
+}
+
+// Tile entries e0 + lane (e0 uniform over the warp) of the depth-ordered
+// emission: entry j of Gaussian g (owner record offset o) is tile
+// first + (j / w) gx + j % w (one row of `count` tiles when w = 0), value g.
+// `p` is a position whose offset is <= e0 (on return: the same for
+// e0 + 32).  The 32 owner records p .. p + 31 are read one per lane; a
+// lane's owner is the last of them starting at or before its entry.  Their
+// starts relative to e0, h (non-decreasing in the window index, 0 for the
+// records starting at or before e0), are usually distinct past those: then
+// the owner of lane L is the number of records with h = 0 less one plus the
+// number of starts in [1, L], one OR-reduce and a popcount.  Records of zero entries repeat a start; a window with
+// such a repeat takes a five-step shuffle search instead.  An entry past the
+// window (only behind zero-entry owners) is searched in [p + 32, i1].
+template <bool STAGED>
+__device__ inline void gen_entries(const OwnerView<STAGED>& ov, uint32_t i1, uint32_t& p,
+                                   uint32_t e0, int lane, uint32_t& key, uint32_t& val) {
+  const uint32_t q = p + (uint32_t)lane;
+  const uint4 r = q <= i1 ? ov.rec(q) : make_uint4(0u, 0u, 0u, 0xFFFFFFFFu);
+  const uint32_t x32 = p + 32u <= i1 ? ov.off(p + 32u) : 0xFFFFFFFFu;
+  // start of record `lane` relative to e0, clamped to [0, 33]
+  const uint32_t h = r.w <= e0 ? 0u : min(r.w - e0, 33u);
+  const bool inner = h >= 1u && h <= 31u;
+  const uint32_t heads = __reduce_or_sync(0xffffffffu, inner ? 1u << h : 0u);
+  const uint32_t n_inner = __popc(__ballot_sync(0xffffffffu, inner));
+  // records 1 .. z also start at or before e0 (zero-entry owners)
+  const int z = __popc(__ballot_sync(0xffffffffu, h == 0u)) - 1;
+  int idx;
+  if (__popc(heads) == (int)n_inner) {  // distinct starts (warp-uniform)
+    idx = z + __popc(heads & (0xFFFFFFFFu >> (31 - lane)));
+  } else {
+    idx = 0;
+#pragma unroll
+    for (int st = 16; st >= 1; st >>= 1) {
+      const uint32_t hv = __shfl_sync(0xffffffffu, h, idx + st);
+      if (hv <= (uint32_t)lane) idx += st;
+    }
+  }
+  uint4 o;
+  o.x = __shfl_sync(0xffffffffu, r.x, idx);
+  o.y = __shfl_sync(0xffffffffu, r.y, idx);
+  o.z = __shfl_sync(0xffffffffu, r.z, idx);
+  o.w = __shfl_sync(0xffffffffu, r.w, idx);
+  const uint32_t e = e0 + (uint32_t)lane;
+  if (x32 <= e) o = ov.rec(owner_search(ov, p + 32u, i1, e));  // behind zero-entry owners
+  const uint32_t w = o.y & 0xFFFFu, gx = o.y >> 16;
+  const uint32_t jj = e - o.w;
+  uint32_t row = 0, col = jj;
+  if (w) divmod_u32(jj, w, row, col);
+  key = o.x + row * gx + col;
+  val = o.z;
+  // next window: the last record starting at or before e0 + 32
+  const uint32_t in = __popc(__ballot_sync(0xffffffffu, h <= 32u));
+  p = x32 <= e0 + 32u ? p + 32u : p + in - 1u;
+}
+
+// Keys and values of one warp's IT * 32 entries from ew on (cnt_w of them
+// in range), generated into shared memory.
+template <bool STAGED, int IT>
+__device__ inline void gen_warp(const OwnerView<STAGED>& ov, uint32_t i0, uint32_t i1, uint32_t ew,
+                                int cnt_w, int lane, uint32_t* __restrict__ keys,
+                                uint32_t* __restrict__ vals) {
+  uint32_t pos = owner_search(ov, i0, i1, ew);
+#pragma unroll 1
+  for (int it = 0; it < IT && it * 32 < cnt_w; ++it) {
+    uint32_t k, v;
+    gen_entries(ov, i1, pos, ew + (uint32_t)(it * 32), lane, k, v);
+    const int j = it * 32 + lane;
+    keys[j] = j < cnt_w ? k : 0u;
+    vals[j] = v;
+  }
+}
+
+template <int RB, bool KEYS_OUT, bool RANGES, bool GEN>
 __global__ void __launch_bounds__(Os<RB>::NT, 2) onesweep_kernel(
     const uint32_t* __restrict__ keys_in, const uint32_t* __restrict__ vals_in,
     uint32_t* __restrict__ keys_out, uint32_t* __restrict__ vals_out, int64_t cap,
-    const int64_t* __restrict__ n_dev, int shift, const uint32_t* __restrict__ pass_hist,
+    const int64_t* __restrict__ n_dev, int shift, int live, const uint32_t* __restrict__ pass_hist,
     uint32_t* __restrict__ status, uint32_t* __restrict__ part_counter, int2* __restrict__ range,
-    uint32_t T, int64_t* __restrict__ info) {
+    uint32_t T, const uint4* __restrict__ owner, const uint32_t* __restrict__ chunk_first,
+    int64_t n_sorted, int64_t* __restrict__ info) {
   using P = Os<RB>;
   constexpr int NT = P::NT, IT = P::IT, NW = P::NW, PART = P::PART, R = P::R;
   extern __shared__ __align__(16) uint32_t os_smem[];
@@ -261,33 +386,78 @@ __global__ void __launch_bounds__(Os<RB>::NT, 2) onesweep_kernel(
   const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
   const int64_t n = pass_count(n_dev, cap);
   if (t == 0) s_part = atomicAdd(part_counter, 1u);
-  for (int i = t; i < NW * R; i += NT) warp_hist[i] = 0;
+  // (a generating pass holds owner records in warp_hist until it ranks)
+  if (!GEN)
+    for (int i = t; i < NW * R; i += NT) warp_hist[i] = 0;
   __syncthreads();
   const int part = (int)s_part;
   const int64_t pbase = (int64_t)part * PART;
   if (pbase >= n) return;  // whole CTA: past the element count
   const int64_t rem = n - pbase;
   const int cnt = rem < (int64_t)PART ? (int)rem : PART;
-  if (cnt == PART) {
-    for (int q = t; q < PART / 4; q += NT) cp_async16(s_vin + 4 * q, vals_in + pbase + 4 * q);
-    cp_async_commit();
-  } else {
-    for (int q = t; q < cnt; q += NT) s_vin[q] = vals_in[pbase + q];
-  }
-
   const int wofs = warp * 32 * IT;
   uint32_t key[IT], rank[IT];
   const uint32_t lt = lanemask_lt();
+  if constexpr (GEN) {
+    // keys and values generated from the owner records of the partition's
+    // chunks: positions [i0, i1] (i1: the owner of the next partition's first
+    // entry, or of entry n - 1)
+    static_assert(PART % kEmitChunk == 0, "a partition is whole chunks");
+    constexpr uint32_t kOwn = NW * R / 4;  // owner records that fit in warp_hist
+    uint4* s_own = reinterpret_cast<uint4*>(warp_hist);
+    const int64_t nchunks = (n + kEmitChunk - 1) / kEmitChunk;
+    const int64_t c0 = (int64_t)part * (PART / kEmitChunk);
+    const int64_t c1 = min(nchunks, c0 + PART / kEmitChunk);
+    const uint32_t i0 = chunk_first[c0], i1 = chunk_first[c1];
+    const bool ok = i0 <= i1 && (int64_t)i1 < n_sorted;
+    if (!ok && t == 0) set_error(info, PGB_ERR_OVERFLOW);
+    const uint32_t m = ok ? i1 - i0 + 1 : 0u;
+    const bool staged = m <= kOwn;
+    if (staged) {
+      for (uint32_t q = t; q < m; q += NT) cp_async16(s_own + q, owner + i0 + q);
+      cp_async_commit();
+      cp_async_wait<0>();
+    }
+    __syncthreads();
+    // generated through shared memory (s_keys is free until the staging
+    // below), so the generation loop need not be unrolled; keys past the
+    // count stay 0
+    for (int it = 0; it < IT; ++it) s_keys[wofs + it * 32 + lane] = 0u;
+    __syncwarp();
+    if (ok && wofs < cnt) {
+      const uint32_t ew = (uint32_t)pbase + (uint32_t)wofs;
+      const int cnt_w = min(cnt - wofs, 32 * IT);
+      if (staged)
+        gen_warp<true, IT>(OwnerView<true>{owner, s_own, i0}, i0, i1, ew, cnt_w, lane,
+                           s_keys + wofs, s_vin + wofs);
+      else
+        gen_warp<false, IT>(OwnerView<false>{owner, s_own, i0}, i0, i1, ew, cnt_w, lane,
+                            s_keys + wofs, s_vin + wofs);
+    }
+    __syncwarp();
 #pragma unroll
-  for (int it = 0; it < IT; ++it) {
-    const int j = wofs + it * 32 + lane;
-    key[it] = j < cnt ? keys_in[pbase + j] : 0u;
+    for (int it = 0; it < IT; ++it) key[it] = s_keys[wofs + it * 32 + lane];
+    __syncthreads();  // every warp is done with the owner records
+    for (int i = t; i < NW * R; i += NT) warp_hist[i] = 0;
+    __syncthreads();
+  } else {
+    if (cnt == PART) {
+      for (int q = t; q < PART / 4; q += NT) cp_async16(s_vin + 4 * q, vals_in + pbase + 4 * q);
+      cp_async_commit();
+    } else {
+      for (int q = t; q < cnt; q += NT) s_vin[q] = vals_in[pbase + q];
+    }
+#pragma unroll
+    for (int it = 0; it < IT; ++it) {
+      const int j = wofs + it * 32 + lane;
+      key[it] = j < cnt ? keys_in[pbase + j] : 0u;
+    }
   }
 #pragma unroll
   for (int it = 0; it < IT; ++it) {
     const bool valid = wofs + it * 32 + lane < cnt;
     const uint32_t d = (key[it] >> shift) & (R - 1);
-    const uint32_t peers = match_digit<RB>(d, valid);
+    const uint32_t peers = match_digit<RB>(d, valid, live);
     const uint32_t old = warp_hist[warp * R + d];
     rank[it] = old + __popc(peers & lt);
     __syncwarp();
@@ -313,7 +483,7 @@ __global__ void __launch_bounds__(Os<RB>::NT, 2) onesweep_kernel(
       block_excl_scan<NT>(t < R ? pass_hist[t] : 0u, unused, s_warp_tot);
   const uint32_t bex = block_excl_scan<NT>(t < R ? count : 0u, local_total, s_warp_tot);
   if (t < R) s_block_excl[t] = bex;
-  if (cnt == PART) cp_async_wait<0>();
+  if (!GEN && cnt == PART) cp_async_wait<0>();
   __syncthreads();
 
   // Stage in digit order; the digit threads resolve the global bases.
@@ -358,21 +528,32 @@ __global__ void __launch_bounds__(Os<RB>::NT, 2) onesweep_kernel(
   }
 }
 
-// One pass: digit width, whether keys are written, whether ranges are made.
-template <int RB, bool KEYS_OUT, bool RANGES>
+// Where a generating pass (GEN) reads its entries: the owner records and
+// the chunk table of the scan.
+struct GenSource {
+  const uint4* owner = nullptr;
+  const uint32_t* chunk_first = nullptr;
+  int64_t n_sorted = 0;
+};
+
+// One pass: digit width, whether keys are written, whether ranges are made,
+// whether the keys are generated from owner records (ki / vi unused).
+template <int RB, bool KEYS_OUT, bool RANGES, bool GEN = false>
 static int launch_onesweep(int parts, cudaStream_t s, const uint32_t* ki, const uint32_t* vi,
                            uint32_t* ko, uint32_t* vo, int64_t cap, const int64_t* n_dev,
                            int shift, const uint32_t* hist, uint32_t* status, uint32_t* counter,
-                           int2* range, uint32_t T, int64_t* info) {
+                           int2* range, uint32_t T, int64_t* info, const GenSource& src = {},
+                           int live = RB) {
   using P = Os<RB>;
-  auto kern = onesweep_kernel<RB, KEYS_OUT, RANGES>;
+  auto kern = onesweep_kernel<RB, KEYS_OUT, RANGES, GEN>;
   // the attribute is set on every call: the call is cheap, allowed while a
   // stream is being captured, and per device
   if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)P::SMEM) !=
       cudaSuccess)
     return PGB_ERR_CUDA;
-  kern<<<parts, P::NT, P::SMEM, s>>>(ki, vi, ko, vo, cap, n_dev, shift, hist, status, counter,
-                                     range, T, info);
+  kern<<<parts, P::NT, P::SMEM, s>>>(ki, vi, ko, vo, cap, n_dev, shift, live, hist, status,
+                                     counter, range, T, src.owner, src.chunk_first, src.n_sorted,
+                                     info);
   return PGB_OK;
 }
 
@@ -523,18 +704,22 @@ __global__ void __launch_bounds__(kStreamThreads) rect_kernel(
 // every emission chunk boundary b * kEmitChunk that falls inside
 // [offset, offset + count), chunk_first[b] = i.  K is the host value k_cap,
 // or the device count k_dev (written by the depth phase) bounded by the
-// capacity k_cap.
+// capacity k_cap.  The grid also sets the tile-range table to (INT_MAX, 0)
+// for the last tile pass.
 // ---------------------------------------------------------------------------
-constexpr int kEmitChunk = 1024;
-constexpr int kEmitThreads = 256;
 
 __global__ void __launch_bounds__(kSortThreads) scan_rect_kernel(
     const uint32_t* __restrict__ order, int64_t n, const uint4* __restrict__ rect, int64_t k_cap,
     const int64_t* __restrict__ k_dev, uint32_t* __restrict__ status,
     uint32_t* __restrict__ part_counter, uint4* __restrict__ owner,
-    uint32_t* __restrict__ chunk_first, int64_t* __restrict__ info) {
+    uint32_t* __restrict__ chunk_first, int2* __restrict__ range, uint32_t T,
+    int64_t* __restrict__ info) {
   __shared__ uint32_t s_warp_tot[kSortThreads / 32];
   __shared__ uint32_t s_part, s_prior;
+  // the tile-range table starts at (INT_MAX, 0) for the last tile pass
+  for (int64_t i = (int64_t)blockIdx.x * kSortThreads + threadIdx.x; i < T;
+       i += (int64_t)gridDim.x * kSortThreads)
+    range[i] = make_int2(INT_MAX, 0);
   // a device count past the capacity: reported once, nothing is emitted
   if (k_dev && (*k_dev < 0 || *k_dev > k_cap)) {
     if (blockIdx.x == 0 && threadIdx.x == 0) set_error(info, PGB_ERR_OVERFLOW);
@@ -594,142 +779,6 @@ __global__ void __launch_bounds__(kSortThreads) scan_rect_kernel(
         if (off < K && K <= end) chunk_first[(K + kEmitChunk - 1) / kEmitChunk] = (uint32_t)e;
       }
       off = end;
-    }
-  }
-}
-
-// ---------------------------------------------------------------------------
-// 3c. emission of (tile id, Gaussian id) pairs over output chunks
-//
-// The output is cut into chunks of kEmitChunk entries; each CTA of a
-// persistent grid emits a contiguous range of chunks.  For chunk b, entries
-// [b*kEmitChunk, min(K, (b+1)*kEmitChunk)), the CTA stages the emission
-// records of the Gaussians that own them in shared memory; each thread takes
-// 4 consecutive entries, finds the owner of the first by binary search and
-// walks forward; the pairs are staged in shared memory and written with
-// 16-byte stores.  Every chunk is the same amount of work however unevenly
-// the tiles are spread over Gaussians.  The chunk boundaries of a range are
-// read up front and the next chunk's owner records travel by cp.async into
-// the second of two stages while the current chunk is emitted, so no chunk
-// waits on a chain of global loads.  (The tile digit histograms come from
-// the rectangle pass.)  The grid also sets the tile-range table to
-// (INT_MAX, 0) for the last tile pass.
-// ---------------------------------------------------------------------------
-constexpr int kEmitPer = kEmitChunk / kEmitThreads;  // 4
-constexpr int kEmitBlocksPerSM = 5;
-constexpr int kEmitSeg = 256;  // chunk boundaries held in shared memory at a time
-
-__global__ void __launch_bounds__(kEmitThreads) emit_kernel(
-    const uint4* __restrict__ owner, const uint32_t* __restrict__ chunk_first, int64_t n_sorted,
-    int64_t k_cap, const int64_t* __restrict__ k_dev, uint32_t* __restrict__ tkeys,
-    uint32_t* __restrict__ tvals, int2* __restrict__ range, uint32_t T,
-    int64_t* __restrict__ info) {
-  constexpr int CAP = kEmitChunk + 1;
-  // (first tile, w | gx << 16, g, offset) of a chunk's owners, two stages
-  __shared__ __align__(16) uint4 s_own[2][CAP];
-  __shared__ __align__(16) uint32_t s_key[kEmitChunk];
-  __shared__ __align__(16) uint32_t s_val[kEmitChunk];
-  __shared__ uint32_t s_cf[kEmitSeg + 1];
-  for (int64_t i = (int64_t)blockIdx.x * kEmitThreads + threadIdx.x; i < T;
-       i += (int64_t)gridDim.x * kEmitThreads)
-    range[i] = make_int2(INT_MAX, 0);
-  const int64_t K = pass_count(k_dev, k_cap);
-  const int64_t nchunks = (K + kEmitChunk - 1) / kEmitChunk;
-  const int64_t per = (nchunks + gridDim.x - 1) / gridDim.x;
-  const int64_t c0 = (int64_t)blockIdx.x * per;
-  const int64_t c1 = min(nchunks, c0 + per);
-  if (c0 >= c1) return;
-
-  for (int64_t seg = c0; seg < c1; seg += kEmitSeg) {
-    const int nseg = c1 - seg < (int64_t)kEmitSeg ? (int)(c1 - seg) : kEmitSeg;
-    __syncthreads();  // the previous segment is out of s_cf and the stages
-    // owners of each chunk's first entry, and of the next chunk's first
-    // entry (for the last chunk: of entry K - 1)
-    for (int i = threadIdx.x; i <= nseg; i += kEmitThreads) s_cf[i] = chunk_first[seg + i];
-    __syncthreads();
-    // chunk q of the segment -> stage buf (one commit group per call)
-    auto stage = [&](int q, int buf) {
-      const int64_t i0 = s_cf[q], i1 = s_cf[q + 1];
-      const int64_t m = i1 - i0 + 1;
-      if (i0 <= i1 && i1 < n_sorted && m <= CAP)
-        for (int64_t i = threadIdx.x; i < m; i += kEmitThreads)
-          cp_async16(&s_own[buf][i], owner + i0 + i);
-      cp_async_commit();
-    };
-    stage(0, 0);
-    for (int qc = 0; qc < nseg; ++qc) {
-      const int buf = qc & 1;
-      if (qc + 1 < nseg) {
-        stage(qc + 1, buf ^ 1);
-        cp_async_wait<1>();  // this thread's copies of chunk q have landed
-      } else {
-        cp_async_wait<0>();
-      }
-      __syncthreads();  // ... and everyone's; the previous chunk is written out
-      const int64_t b = seg + qc;
-      const int64_t e0 = b * kEmitChunk;
-      const int64_t e1 = min(K, e0 + kEmitChunk);
-      const int64_t i0 = s_cf[qc];
-      const int64_t i1 = s_cf[qc + 1];
-      const int64_t m = i1 - i0 + 1;
-      const bool ok_range = i0 <= i1 && i1 < n_sorted;
-      if (!ok_range && threadIdx.x == 0) set_error(info, PGB_ERR_OVERFLOW);
-      const bool staged = ok_range && m <= CAP;
-      const int64_t ebeg = e0 + (int64_t)threadIdx.x * kEmitPer;
-      if (ok_range && ebeg < e1) {
-        const uint4* so = s_own[buf];
-        auto own_at = [&](int64_t p) -> uint4 { return staged ? so[p] : owner[i0 + p]; };
-        auto off_at = [&](int64_t p) -> int64_t { return staged ? so[p].w : owner[i0 + p].w; };
-        // owner of ebeg: the last position p in [0, i1 - i0] with offs <= ebeg
-        int64_t lo = 0, hi = i1 - i0;
-        while (lo < hi) {
-          const int64_t mid = (lo + hi + 1) >> 1;
-          if (off_at(mid) <= ebeg) lo = mid; else hi = mid - 1;
-        }
-        int64_t own = lo;
-        int64_t next_off = own < i1 - i0 ? off_at(own + 1) : INT64_MAX;
-        uint32_t g = 0, t0 = 0, w = 0, gx = 0, row = 0, col = 0;
-        bool fresh = true;
-        for (int j = 0; j < kEmitPer; ++j) {
-          const int64_t e = ebeg + j;
-          if (e >= e1) break;
-          while (e >= next_off) {  // walk to the owner of e (skips zero-count Gaussians)
-            ++own;
-            next_off = own < i1 - i0 ? off_at(own + 1) : INT64_MAX;
-            fresh = true;
-          }
-          if (fresh) {  // first entry of this owner for the thread: position by division
-            const uint4 o = own_at(own);
-            t0 = o.x;
-            w = o.y & 0xFFFFu;
-            gx = o.y >> 16;
-            g = o.z;
-            const uint32_t jj = (uint32_t)(e - o.w);
-            row = w ? jj / w : 0u;
-            col = jj - row * w;
-            fresh = false;
-          } else if (++col == w) {  // next entry of the same owner: next column / row
-            col = 0;
-            ++row;
-          }
-          s_key[threadIdx.x * kEmitPer + j] = t0 + row * gx + col;
-          s_val[threadIdx.x * kEmitPer + j] = g;
-        }
-      }
-      __syncthreads();
-      // coalesced write-out
-      const int cnt = ok_range ? (int)(e1 - e0) : 0;
-      if (cnt == kEmitChunk) {
-        for (int q = threadIdx.x; q < kEmitChunk / 4; q += kEmitThreads) {
-          reinterpret_cast<uint4*>(tkeys + e0)[q] = reinterpret_cast<const uint4*>(s_key)[q];
-          reinterpret_cast<uint4*>(tvals + e0)[q] = reinterpret_cast<const uint4*>(s_val)[q];
-        }
-      } else {
-        for (int q = threadIdx.x; q < cnt; q += kEmitThreads) {
-          tkeys[e0 + q] = s_key[q];
-          tvals[e0 + q] = s_val[q];
-        }
-      }
     }
   }
 }
@@ -825,24 +874,31 @@ inline P* at(void* base, size_t off) {
   return reinterpret_cast<P*>(static_cast<char*>(base) + off);
 }
 
-// One tile pass p of `plan` (the last one writes ids and ranges, no keys).
+// One tile pass p of `plan` (the last one writes ids and ranges, no keys;
+// the first generates its entries from the owner records).
 static int tile_pass(const TilePlan& plan, int p, int parts, cudaStream_t s, const uint32_t* ki,
                      const uint32_t* vi, uint32_t* ko, uint32_t* vo, int64_t cap,
                      const int64_t* n_dev, const uint32_t* hist, uint32_t* status,
-                     uint32_t* counter, int2* range, uint32_t T, int64_t* info) {
+                     uint32_t* counter, int2* range, uint32_t T, int64_t* info,
+                     const GenSource& src) {
   const bool last = p == plan.passes - 1;
   const int shift = plan.bits * p;
   const uint32_t* h = hist + (size_t)p * (1u << plan.bits);
   uint32_t* st = status + (size_t)p * parts * (1u << plan.bits);
-  if (plan.bits == 9)
-    return last ? launch_onesweep<9, false, true>(parts, s, ki, vi, ko, vo, cap, n_dev, shift, h, st,
-                                                  counter, range, T, info)
-                : launch_onesweep<9, true, false>(parts, s, ki, vi, ko, vo, cap, n_dev, shift, h,
-                                                  st, counter, range, T, info);
-  return last ? launch_onesweep<8, false, true>(parts, s, ki, vi, ko, vo, cap, n_dev, shift, h, st,
-                                                counter, range, T, info)
-              : launch_onesweep<8, true, false>(parts, s, ki, vi, ko, vo, cap, n_dev, shift, h, st,
-                                                counter, range, T, info);
+  // digit bits that some tile id has set in this pass
+  int live = 0;
+  while (live < plan.bits && ((T - 1) >> (shift + live))) ++live;
+  live = live < 1 ? 1 : live;
+#define PGB_PASS(RB, KO, RG, GN) \
+  launch_onesweep<RB, KO, RG, GN>(parts, s, ki, vi, ko, vo, cap, n_dev, shift, h, st, counter, \
+                                  range, T, info, src, live)
+  if (p == 0) {
+    if (last) return PGB_PASS(8, false, true, true);  // one pass: at most 256 tiles
+    return plan.bits == 9 ? PGB_PASS(9, true, false, true) : PGB_PASS(8, true, false, true);
+  }
+  if (plan.bits == 9) return last ? PGB_PASS(9, false, true, false) : PGB_PASS(9, true, false, false);
+  return last ? PGB_PASS(8, false, true, false) : PGB_PASS(8, true, false, false);
+#undef PGB_PASS
 }
 
 }  // namespace pgb
@@ -946,16 +1002,17 @@ static int sort_finish_impl(const float* uv, const int32_t* radius, const int32_
       uv, radius, tiles_touched, n, vt, plan.passes, plan.bits, rect, thist, info);
   scan_rect_kernel<<<LN.scan_parts, kSortThreads, 0, s>>>(
       order, n, rect, k, k_dev, at<uint32_t>(scratch_n, LN.scan_status), counters + 4, owner,
-      chunk_first, info);
-  const int64_t emit_grid = std::min<int64_t>(LK.chunks, (int64_t)kNumSMs * kEmitBlocksPerSM);
-  emit_kernel<<<(unsigned)emit_grid, kEmitThreads, 0, s>>>(owner, chunk_first, n, k, k_dev,
-                                                           bufk[0], bufv[0], range, T, info);
+      chunk_first, range, T, info);
+  GenSource src;
+  src.owner = owner;
+  src.chunk_first = chunk_first;
+  src.n_sorted = n;
   int cur = 0;
   for (int p = 0; p < plan.passes; ++p) {
     const bool last = p == plan.passes - 1;
     uint32_t* vo = last ? reinterpret_cast<uint32_t*>(ids_out) : bufv[cur ^ 1];
     const int rc = tile_pass(plan, p, LK.parts, s, bufk[cur], bufv[cur], bufk[cur ^ 1], vo, k, k_dev,
-                             thist, status, counters + 5 + p, range, T, info);
+                             thist, status, counters + 5 + p, range, T, info, src);
     if (rc != PGB_OK) return rc;
     cur ^= 1;
   }
