@@ -742,6 +742,8 @@ def run_gb300(args):
             "multiview": multi,
             "ssim": loss_ssim,
             "blend_batch": {"/".join(map(str, k)): b for k, b in autotune.table().items()},
+            "blend_batch_ms": {"/".join(map(str, k)): {str(b): round(t, 4) for b, t in v.items()}
+                               for k, v in autotune.timings().items()},
         }
         print(json.dumps(line), flush=True)
     if world > 1:

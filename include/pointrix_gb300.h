@@ -250,13 +250,16 @@ int pgb_alpha_blending_backward_views(const float* records, int64_t n_per_view, 
                                       float* d_conic, float* d_opacity, float* d_feature,
                                       int64_t* info, void* stream);
 
-/* The four blend entry points with the per-block splat batch chosen by the
- * caller (the run-time autotuner of pointrix_gb300.autotune): forward 64 or
- * 128 records per batch, backward 64, 128 or 256; 0 = the default (128).
- * Every batch gives the same images, final transmittance and contributor
- * counts; the backward's gradient sums are formed in a batch-dependent
- * order (float atomics).  pgb_blend_batches(backward, out) lists the
- * compiled batches (returns their count, writes them to out if not NULL). */
+/* The four blend entry points with the kernel variant chosen by the caller
+ * (the run-time autotuner of pointrix_gb300.autotune).  Forward: 64 or 128
+ * records per batch.  Backward: 64, 128 or 256 records per batch with two
+ * pixels per thread, or 4096 + 32 / 64 / 128 for four pixels per thread
+ * (64 threads per tile, 8x16 pixel boxes per warp).  0 = the default (128,
+ * two pixels per thread).  Every variant gives the same images, final
+ * transmittance and contributor counts; the backward's gradient sums are
+ * formed in a variant-dependent order (float atomics).
+ * pgb_blend_batches(backward, out) lists the compiled variants (returns
+ * their count, writes them to out if not NULL). */
 int pgb_alpha_blending_forward_with_batch(const float* uv, const float* conic,
                                           const float* opacity, const float* feature, int64_t n,
                                           int channels, const int32_t* ids, int64_t k,

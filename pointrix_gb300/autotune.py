@@ -1,12 +1,16 @@
-"""Run-time choice of the blend kernels' per-block splat batch.
+"""Run-time choice of the blend kernels' variant (per-block splat batch,
+and for the backward the pixels per thread).
 
 The blend kernels stage a tile's depth-sorted splats into shared memory in
 batches; the best batch size depends on the image, the channel count and how
 many splats a tile's list holds (short lists waste a large batch's staging,
-long lists pay a small batch's extra barriers).  The library compiles a few
-batch sizes (``pgb_blend_batches``: forward 64/128, backward 64/128/256); all
-give the same images, and the backward the same gradients up to the order of
-its float sums.  On the first call of a workload class this module times
+long lists pay a small batch's extra barriers).  The backward also comes
+with two or four pixels per thread (four: half the per-splat warp reductions
+per pixel, coarser culling boxes).  The library compiles a few variants
+(``pgb_blend_batches``: forward 64/128 records per batch, backward 64/128/256
+with two pixels per thread and 4096 + 64/128 with four); all give the same
+images, and the backward the same gradients up to the order of its float
+sums.  On the first call of a workload class this module times
 every compiled batch on the live inputs (CUDA events, one warm-up and two
 timed runs each) and keeps the fastest for the class; later calls -- and
 calls while a CUDA graph is being captured -- use the kept choice (or the
@@ -24,10 +28,11 @@ import threading
 
 import torch
 
-__all__ = ["choose", "workload_class", "table", "reset", "set_enabled"]
+__all__ = ["choose", "workload_class", "table", "timings", "reset", "set_enabled"]
 
 _lock = threading.Lock()
 _cache: dict = {}
+_times: dict = {}
 _enabled = os.environ.get("PGB_AUTOTUNE", "1") != "0"
 
 
@@ -64,6 +69,7 @@ def choose(key, candidates, run, device=None, timer=None) -> int:
     times = {b: timer(lambda b=b: run(b)) for b in candidates}
     best = min(times, key=lambda b: (times[b], b))
     with _lock:
+        _times.setdefault(key, times)
         _cache.setdefault(key, best)
         return _cache[key]
 
@@ -74,9 +80,16 @@ def table() -> dict:
         return dict(_cache)
 
 
+def timings() -> dict:
+    """The measured milliseconds per candidate of every timed class."""
+    with _lock:
+        return {k: dict(v) for k, v in _times.items()}
+
+
 def reset() -> None:
     with _lock:
         _cache.clear()
+        _times.clear()
 
 
 def set_enabled(flag: bool) -> None:

@@ -84,13 +84,17 @@ __device__ inline void set_info(int64_t* info, int code) {
   if (info) atomicCAS(reinterpret_cast<unsigned long long*>(info), 0ull, (unsigned long long)code);
 }
 
-// Power and alpha of one (pixel, splat) pair, written with explicit
-// rounding intrinsics so that the forward and the backward take identical
-// skip/stop decisions whatever the compiler contracts elsewhere.
-__device__ __forceinline__ float splat_power(float a, float b, float c, float dx, float dy) {
-  const float q = __fmaf_rn(__fmul_rn(a, dx), dx, __fmul_rn(__fmul_rn(c, dy), dy));
-  const float bxy = __fmul_rn(__fmul_rn(b, dx), dy);
-  return __fmaf_rn(-0.5f, q, -bxy);
+// Power of one (pixel, splat) pair, -(a dx^2 + 2 b dx dy + c dy^2) / 2 =
+// -(dx g0 + dy g1) / 2 with g0 = a dx + b dy, g1 = b dx + c dy (the
+// gradient of the power with respect to uv is -(g0, g1), which the backward
+// reuses).  Written with explicit rounding intrinsics so that the forward and
+// the backward take identical skip/stop decisions whatever the compiler
+// contracts elsewhere.
+__device__ __forceinline__ float splat_power(float a, float b, float c, float dx, float dy,
+                                             float& g0, float& g1) {
+  g0 = __fmaf_rn(a, dx, __fmul_rn(b, dy));
+  g1 = __fmaf_rn(b, dx, __fmul_rn(c, dy));
+  return __fmul_rn(-0.5f, __fmaf_rn(dx, g0, __fmul_rn(dy, g1)));
 }
 
 // Issue the bulk copies of one batch of B records: thread t fetches the
@@ -352,7 +356,8 @@ __global__ void __launch_bounds__(kFwdThreads) blend_fwd_kernel(
           if (done[q]) continue;
           live = true;
           const float dy = __fsub_rn(r0.y, pyf[q]);
-          const float power = splat_power(r0.z, r0.w, r1.x, dx, dy);
+          float g0, g1;
+          const float power = splat_power(r0.z, r0.w, r1.x, dx, dy, g0, g1);
           if (power > 0.f || power < r1.w) continue;  // alpha < 1/255: no exp needed
           const float alpha = fminf(0.99f, __fmul_rn(r1.y, __expf(power)));
           const float test_T = __fmul_rn(T[q], __fsub_rn(1.0f, alpha));
@@ -416,16 +421,19 @@ __device__ __forceinline__ float warp_reduce_scatter(float (&v)[GR]) {
   return v[0];
 }
 
-// Backward: 128 threads per tile, two pixels per thread.  Warp w owns the
-// 8x8 box at (8 (w % 2), 8 (w / 2)); lane l owns pixels (l % 8, l / 8) and
-// (l % 8, l / 8 + 4) of it, so every per-splat warp reduction, record read
-// and culling test serves 64 pixels.
-constexpr int kBwdThreads = 128;
-constexpr int kBwdPix = 2;
+// Backward: PX pixels per thread, 256 / PX threads per tile.  Warp w owns
+// an 8 x BH box (8x8 for PX = 2, 8x16 for PX = 4) at (8 (w % 2), BH (w / 2));
+// lane l owns pixels (l % 8, l / 8 + 4q), q < PX, of it, so every per-splat
+// warp reduction, record read and culling test serves 32 PX pixels: more
+// pixels per thread, fewer reductions per pixel and coarser culling.  (Eight
+// pixels per thread, one warp per tile, measured slower than either.)
 // 128 splats per batch: the double-buffered stage and the per-splat
 // gradient sums stay near 25 KB, so registers, not shared memory, bound the
 // CTAs per SM.
 constexpr int kBwdBatch = 128;
+// Backward variant code: records per batch, plus kBwdPx4 for four pixels
+// per thread.
+constexpr int kBwdPx4 = 4096;
 
 // Per-pixel replay state.  SB = sum_c dout_c B_c, B_c the colour composited
 // behind the current splat (background first): the gradient needs only that
@@ -440,8 +448,12 @@ struct BwdPixel {
   float dout[NC];
 };
 
-// Adds one pixel's contribution to the splat gradients v (u, v, a, b, c, o,
-// f...); replays the forward's skip decisions exactly.
+// Adds one pixel's contribution to the splat's gradient moments v:
+// sum g0 dp, sum g1 dp, sum dx^2 dp, sum dx dy dp, sum dy^2 dp (dp the
+// gradient of the power), sum G dalpha (the opacity gradient), then the
+// feature gradients; the unpack pass turns the moments into the uv and
+// conic gradients (-v0, -v1; -v2 / 2, -v3, -v4 / 2).  Replays the forward's
+// skip decisions exactly.
 template <int NC, int GR>
 __device__ __forceinline__ bool bwd_pixel(BwdPixel<NC>& P, int j, const float* rec,
                                           float (&v)[GR]) {
@@ -449,7 +461,8 @@ __device__ __forceinline__ bool bwd_pixel(BwdPixel<NC>& P, int j, const float* r
   const float4 r0 = *reinterpret_cast<const float4*>(rec);
   const float4 r1 = *reinterpret_cast<const float4*>(rec + 4);
   const float dx = __fsub_rn(r0.x, P.pxf), dy = __fsub_rn(r0.y, P.pyf);
-  const float power = splat_power(r0.z, r0.w, r1.x, dx, dy);
+  float g0, g1;
+  const float power = splat_power(r0.z, r0.w, r1.x, dx, dy, g0, g1);
   if (power > 0.f || power < r1.w) return false;  // the forward's skip test
   const float G = __expf(power);
   const float araw = __fmul_rn(r1.y, G);
@@ -469,27 +482,33 @@ __device__ __forceinline__ bool bwd_pixel(BwdPixel<NC>& P, int j, const float* r
   if (araw < 0.99f) {
     const float dpow = alpha * dalpha;
     v[5] = fmaf(G, dalpha, v[5]);
-    v[2] = fmaf(-0.5f * dx * dx, dpow, v[2]);
-    v[3] = fmaf(-dx * dy, dpow, v[3]);
-    v[4] = fmaf(-0.5f * dy * dy, dpow, v[4]);
-    v[0] = fmaf(-r0.z * dx - r0.w * dy, dpow, v[0]);
-    v[1] = fmaf(-r1.x * dy - r0.w * dx, dpow, v[1]);
+    v[0] = fmaf(g0, dpow, v[0]);
+    v[1] = fmaf(g1, dpow, v[1]);
+    const float tx = dpow * dx;
+    v[2] = fmaf(tx, dx, v[2]);
+    v[3] = fmaf(tx, dy, v[3]);
+    v[4] = fmaf(dpow * dy, dy, v[4]);
   }
   return true;
 }
 
-template <int NC, int RF, int GR, int B>
-__global__ void __launch_bounds__(kBwdThreads) blend_bwd_kernel(
+template <int NC, int RF, int GR, int B, int PX>
+__global__ void __launch_bounds__(256 / PX) blend_bwd_kernel(
     const float* __restrict__ records, const int32_t* __restrict__ ids,
     const int2* __restrict__ ranges, int64_t n, float bg, const ViewTable vt, int C,
     const float* __restrict__ final_T, const int32_t* __restrict__ n_contrib,
     const float* __restrict__ d_out, float* __restrict__ grad_records,
     int64_t* __restrict__ info) {
   static_assert(GR == 16 || GR == 32, "gradient records are 16 or 32 floats");
+  static_assert(PX == 2 || PX == 4, "two or four pixels per thread");
+  constexpr int NT = 256 / PX;
+  constexpr int BW = 8;         // warp box width
+  constexpr int RS = 32 / BW;   // box rows per pixel step
+  constexpr int BH = RS * PX;   // warp box height
   extern __shared__ __align__(128) float smem[];
   __shared__ int s_max_nc;
   __shared__ uint8_t s_touched[B];
-  __shared__ uint8_t s_list[kBwdThreads / 32][B];
+  __shared__ uint8_t s_list[NT / 32][B];
   float* gacc = smem + 2 * B * RF;  // [B][GR]
 
   const int tile = blockIdx.x;  // global tile (of its view, for a batch)
@@ -497,21 +516,21 @@ __global__ void __launch_bounds__(kBwdThreads) blend_bwd_kernel(
   int64_t pbase;
   tile_view(vt, tile, W, H, gx, ltile, pbase);
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int bx0 = (ltile % gx) * kTile + 8 * (w & 1);
-  const int by0 = (ltile / gx) * kTile + 8 * (w >> 1);
+  const int bx0 = (ltile % gx) * kTile + BW * (w & 1);
+  const int by0 = (ltile / gx) * kTile + BH * (w >> 1);
   uint8_t* my_list = s_list[w];
 
   if (threadIdx.x == 0) s_max_nc = 0;
-  for (int i = threadIdx.x; i < B * GR; i += kBwdThreads) gacc[i] = 0.f;
-  for (int i = threadIdx.x; i < B; i += kBwdThreads) s_touched[i] = 0;
+  for (int i = threadIdx.x; i < B * GR; i += NT) gacc[i] = 0.f;
+  for (int i = threadIdx.x; i < B; i += NT) s_touched[i] = 0;
   __syncthreads();
 
   const int64_t plane = (int64_t)W * H;
-  BwdPixel<NC> P[kBwdPix];
+  BwdPixel<NC> P[PX];
   int my_nc = 0;
 #pragma unroll
-  for (int q = 0; q < kBwdPix; ++q) {
-    const int px = bx0 + (lane & 7), py = by0 + (lane >> 3) + 4 * q;
+  for (int q = 0; q < PX; ++q) {
+    const int px = bx0 + lane % BW, py = by0 + lane / BW + RS * q;
     P[q].pxf = (float)px;
     P[q].pyf = (float)py;
     P[q].T = 1.f;
@@ -551,15 +570,13 @@ __global__ void __launch_bounds__(kBwdThreads) blend_bwd_kernel(
   auto hi_of = [&](int b) { return max_nc - b * B; };
 
   if (nb > 0)
-    stage_batch<RF, kBwdThreads, B>(records, ids, start + lo_of(0), start + hi_of(0), n,
-                                            smem, info);
+    stage_batch<RF, NT, B>(records, ids, start + lo_of(0), start + hi_of(0), n, smem, info);
   for (int b = 0; b < nb; ++b) {
     const int buf = b & 1;
     const int lo = lo_of(b), hi = hi_of(b);
     if (b + 1 < nb) {
-      stage_batch<RF, kBwdThreads, B>(records, ids, start + lo_of(b + 1),
-                                              start + hi_of(b + 1), n,
-                                              smem + (buf ^ 1) * B * RF, info);
+      stage_batch<RF, NT, B>(records, ids, start + lo_of(b + 1), start + hi_of(b + 1), n,
+                             smem + (buf ^ 1) * B * RF, info);
       cp_async_wait<1>();  // this thread's copies of batch b have landed
     } else {
       cp_async_wait<0>();
@@ -567,8 +584,8 @@ __global__ void __launch_bounds__(kBwdThreads) blend_bwd_kernel(
     __syncthreads();  // ... and everyone's
     const float* st = smem + buf * B * RF;
     {
-      const int nl = warp_cull<8, 8, B>(st, RF, min(hi, warp_nc) - lo, (float)bx0,
-                                               (float)by0, my_list);
+      const int nl = warp_cull<BW, BH, B>(st, RF, min(hi, warp_nc) - lo, (float)bx0,
+                                          (float)by0, my_list);
       for (int t = nl - 1; t >= 0; --t) {
         const int slot = my_list[t];
         const int j = lo + slot;
@@ -578,7 +595,7 @@ __global__ void __launch_bounds__(kBwdThreads) blend_bwd_kernel(
         for (int q = 0; q < GR; ++q) v[q] = 0.f;
         bool contrib = false;
 #pragma unroll
-        for (int q = 0; q < kBwdPix; ++q) contrib |= bwd_pixel<NC, GR>(P[q], j, rec, v);
+        for (int q = 0; q < PX; ++q) contrib |= bwd_pixel<NC, GR>(P[q], j, rec, v);
         if (__any_sync(0xffffffffu, contrib)) {
           const float sum = warp_reduce_scatter<GR>(v);
           if (GR == 32) {
@@ -593,7 +610,7 @@ __global__ void __launch_bounds__(kBwdThreads) blend_bwd_kernel(
     }
     __syncthreads();
     // flush this batch's per-splat sums: one set of vector atomics per splat
-    for (int t = threadIdx.x; t < hi - lo; t += kBwdThreads) {
+    for (int t = threadIdx.x; t < hi - lo; t += NT) {
       if (!s_touched[t]) continue;
       const int32_t g = ids[start + lo + t];
       if (g < 0 || (int64_t)g >= n) {
@@ -627,10 +644,11 @@ __global__ void unpack_kernel(const float* __restrict__ g, int64_t n, int C,
       const float4 x = s[q];
       r[4 * q] = x.x; r[4 * q + 1] = x.y; r[4 * q + 2] = x.z; r[4 * q + 3] = x.w;
     }
-    reinterpret_cast<float2*>(d_uv)[i] = make_float2(r[0], r[1]);
-    d_conic[3 * i] = r[2];
-    d_conic[3 * i + 1] = r[3];
-    d_conic[3 * i + 2] = r[4];
+    // gradient moments -> uv and conic gradients
+    reinterpret_cast<float2*>(d_uv)[i] = make_float2(-r[0], -r[1]);
+    d_conic[3 * i] = -0.5f * r[2];
+    d_conic[3 * i + 1] = -r[3];
+    d_conic[3 * i + 2] = -0.5f * r[4];
     d_opacity[i] = r[5];
 #pragma unroll
     for (int c = 0; c < RF - 6; ++c)
@@ -666,7 +684,7 @@ static int launch_fwd_nc(const float* records, const int32_t* ids, const int2* r
   }
 }
 
-template <int NC, int B>
+template <int NC, int B, int PX>
 static int launch_bwd_b(const float* records, const int32_t* ids, const int2* ranges, int64_t n,
                         float bg, const ViewTable& vt, int tiles, int C, const float* fT,
                         const int32_t* ncon, const float* dout, float* grec, int64_t* info,
@@ -674,27 +692,34 @@ static int launch_bwd_b(const float* records, const int32_t* ids, const int2* ra
   constexpr int RF = rec_floats(NC);
   constexpr int GR = grad_floats(NC);
   const size_t smem = (2 * RF + GR) * B * sizeof(float);
-  auto kern = blend_bwd_kernel<NC, RF, GR, B>;
+  auto kern = blend_bwd_kernel<NC, RF, GR, B, PX>;
   if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
       cudaSuccess)
     return PGB_ERR_CUDA;
-  kern<<<tiles, kBwdThreads, smem, s>>>(records, ids, ranges, n, bg, vt, C, fT, ncon, dout, grec,
-                                        info);
+  kern<<<tiles, 256 / PX, smem, s>>>(records, ids, ranges, n, bg, vt, C, fT, ncon, dout, grec,
+                                     info);
   return launch_status();
 }
 
-// batch: 64, 128 or 256 splats per backward batch (0: the default).
+// batch: a backward variant code -- 64, 128 or 256 splats per batch with two
+// pixels per thread, kBwdPx4 + 32 / 64 / 128 with four (0: the default).
 template <int NC>
 static int launch_bwd_nc(const float* records, const int32_t* ids, const int2* ranges, int64_t n,
                          float bg, const ViewTable& vt, int tiles, int C, const float* fT,
                          const int32_t* ncon, const float* dout, float* grec, int64_t* info,
                          cudaStream_t s, int batch) {
+#define PGB_BWD(B, PX) \
+  launch_bwd_b<NC, B, PX>(records, ids, ranges, n, bg, vt, tiles, C, fT, ncon, dout, grec, info, s)
   switch (batch == 0 ? kBwdBatch : batch) {
-    case 64: return launch_bwd_b<NC, 64>(records, ids, ranges, n, bg, vt, tiles, C, fT, ncon, dout, grec, info, s);
-    case 128: return launch_bwd_b<NC, 128>(records, ids, ranges, n, bg, vt, tiles, C, fT, ncon, dout, grec, info, s);
-    case 256: return launch_bwd_b<NC, 256>(records, ids, ranges, n, bg, vt, tiles, C, fT, ncon, dout, grec, info, s);
+    case 64: return PGB_BWD(64, 2);
+    case 128: return PGB_BWD(128, 2);
+    case 256: return PGB_BWD(256, 2);
+    case kBwdPx4 + 32: return PGB_BWD(32, 4);
+    case kBwdPx4 + 64: return PGB_BWD(64, 4);
+    case kBwdPx4 + 128: return PGB_BWD(128, 4);
     default: return PGB_ERR_INVALID;
   }
+#undef PGB_BWD
 }
 
 // Channel counts with a compiled kernel; other counts round up (extra
@@ -898,9 +923,10 @@ int pgb_alpha_blending_backward_views(const float* records, int64_t n_per_view, 
 
 // Batch sizes compiled for the forward (backward = 0) or the backward (1).
 int pgb_blend_batches(int backward, int32_t* out) {
-  static const int32_t f[] = {64, 128}, b[] = {64, 128, 256};
+  static const int32_t f[] = {64, 128},
+                       b[] = {64, 128, 256, kBwdPx4 + 32, kBwdPx4 + 64, kBwdPx4 + 128};
   const int32_t* src = backward ? b : f;
-  const int cnt = backward ? 3 : 2;
+  const int cnt = backward ? 6 : 2;
   if (out)
     for (int i = 0; i < cnt; ++i) out[i] = src[i];
   return cnt;
