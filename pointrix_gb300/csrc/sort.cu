@@ -187,7 +187,9 @@ __global__ void __launch_bounds__(kSortThreads) sort_prepare_kernel(
 // slice, so warp order = element order and ranks are stable); the
 // partition's values travel global -> shared by cp.async meanwhile, so a
 // thread holds only its keys and ranks.  Within a warp equal digits are found
-// with RB ballots, one per digit bit.  The first R threads also act as the R
+// by OR-ing each lane's bit into a per-warp digit mask in shared memory
+// (8-bit digits) or with RB ballots, one per digit bit (9-bit digits, whose
+// masks would not fit beside the staging).  The first R threads also act as the R
 // digits for the cross-warp prefix, the status publication and the
 // look-back, which runs while the other warps stage the keys in digit order.
 //
@@ -217,7 +219,12 @@ struct Os {
   static constexpr int NT = OsCfg<RB>::NT, IT = OsCfg<RB>::IT, NW = NT / 32;
   static constexpr int PART = NT * IT;
   static constexpr int R = 1 << RB;
-  static constexpr size_t SMEM = ((size_t)NW * R + 3 * (size_t)PART) * sizeof(uint32_t);
+  // 8-bit digits: equal digits of a warp found by OR-ing lane bits into a
+  // per-warp digit mask in shared memory (one atomic and one load per key);
+  // 9-bit digits (no room for the masks): RB ballots
+  static constexpr bool OR_MATCH = RB == 8;
+  static constexpr int HW = (OR_MATCH ? 2 : 1) * NW * R;  // histogram (+ mask) words
+  static constexpr size_t SMEM = ((size_t)HW + 3 * (size_t)PART) * sizeof(uint32_t);
   static_assert(PART == kPartKeys, "one partition size for every digit width");
   static_assert(NT >= R, "one thread per digit");
 };
@@ -374,8 +381,10 @@ __global__ void __launch_bounds__(Os<RB>::NT, 2) onesweep_kernel(
   using P = Os<RB>;
   constexpr int NT = P::NT, IT = P::IT, NW = P::NW, PART = P::PART, R = P::R;
   extern __shared__ __align__(16) uint32_t os_smem[];
+  constexpr int HW = P::HW;
   uint32_t* warp_hist = os_smem;       // [NW][R]: per-warp counts, then exclusive offsets
-  uint32_t* s_vin = os_smem + NW * R;  // the partition's values in input order
+  uint32_t* s_match = os_smem + NW * R;  // [NW][R] digit masks (OR_MATCH)
+  uint32_t* s_vin = os_smem + HW;      // the partition's values in input order
   uint32_t* s_keys = s_vin + PART;     // keys in digit order
   uint32_t* s_vals = s_keys + PART;    // values in digit order
   __shared__ uint32_t s_block_excl[R];
@@ -388,7 +397,7 @@ __global__ void __launch_bounds__(Os<RB>::NT, 2) onesweep_kernel(
   if (t == 0) s_part = atomicAdd(part_counter, 1u);
   // (a generating pass holds owner records in warp_hist until it ranks)
   if (!GEN)
-    for (int i = t; i < NW * R; i += NT) warp_hist[i] = 0;
+    for (int i = t; i < HW; i += NT) warp_hist[i] = 0;
   __syncthreads();
   const int part = (int)s_part;
   const int64_t pbase = (int64_t)part * PART;
@@ -403,7 +412,7 @@ __global__ void __launch_bounds__(Os<RB>::NT, 2) onesweep_kernel(
     // chunks: positions [i0, i1] (i1: the owner of the next partition's first
     // entry, or of entry n - 1)
     static_assert(PART % kEmitChunk == 0, "a partition is whole chunks");
-    constexpr uint32_t kOwn = NW * R / 4;  // owner records that fit in warp_hist
+    constexpr uint32_t kOwn = HW / 4;  // owner records that fit in warp_hist (+ masks)
     uint4* s_own = reinterpret_cast<uint4*>(warp_hist);
     const int64_t nchunks = (n + kEmitChunk - 1) / kEmitChunk;
     const int64_t c0 = (int64_t)part * (PART / kEmitChunk);
@@ -438,7 +447,7 @@ __global__ void __launch_bounds__(Os<RB>::NT, 2) onesweep_kernel(
 #pragma unroll
     for (int it = 0; it < IT; ++it) key[it] = s_keys[wofs + it * 32 + lane];
     __syncthreads();  // every warp is done with the owner records
-    for (int i = t; i < NW * R; i += NT) warp_hist[i] = 0;
+    for (int i = t; i < HW; i += NT) warp_hist[i] = 0;
     __syncthreads();
   } else {
     if (cnt == PART) {
@@ -453,16 +462,37 @@ __global__ void __launch_bounds__(Os<RB>::NT, 2) onesweep_kernel(
       key[it] = j < cnt ? keys_in[pbase + j] : 0u;
     }
   }
+  if constexpr (P::OR_MATCH) {
+    uint32_t* wm = s_match + warp * R;
+    const uint32_t bit = 1u << lane;
 #pragma unroll
-  for (int it = 0; it < IT; ++it) {
-    const bool valid = wofs + it * 32 + lane < cnt;
-    const uint32_t d = (key[it] >> shift) & (R - 1);
-    const uint32_t peers = match_digit<RB>(d, valid, live);
-    const uint32_t old = warp_hist[warp * R + d];
-    rank[it] = old + __popc(peers & lt);
-    __syncwarp();
-    if (valid && (peers & lt) == 0) warp_hist[warp * R + d] = old + __popc(peers);
-    __syncwarp();
+    for (int it = 0; it < IT; ++it) {
+      const bool valid = wofs + it * 32 + lane < cnt;
+      const uint32_t d = (key[it] >> shift) & (R - 1);
+      if (valid) atomicOr(&wm[d], bit);
+      __syncwarp();
+      const uint32_t peers = valid ? wm[d] : 0u;
+      const uint32_t old = warp_hist[warp * R + d];
+      rank[it] = old + __popc(peers & lt);
+      __syncwarp();
+      if (valid && (peers & lt) == 0) {  // the digit's first lane
+        warp_hist[warp * R + d] = old + __popc(peers);
+        wm[d] = 0u;
+      }
+      __syncwarp();
+    }
+  } else {
+#pragma unroll
+    for (int it = 0; it < IT; ++it) {
+      const bool valid = wofs + it * 32 + lane < cnt;
+      const uint32_t d = (key[it] >> shift) & (R - 1);
+      const uint32_t peers = match_digit<RB>(d, valid, live);
+      const uint32_t old = warp_hist[warp * R + d];
+      rank[it] = old + __popc(peers & lt);
+      __syncwarp();
+      if (valid && (peers & lt) == 0) warp_hist[warp * R + d] = old + __popc(peers);
+      __syncwarp();
+    }
   }
   __syncthreads();
 
