@@ -58,6 +58,8 @@ def parse_args():
                     help="skip the 16-view batched-vs-per-view leg")
     ap.add_argument("--no-recompute", action="store_true",
                     help="skip the 6M-Gaussian 4K stored-vs-recompute leg")
+    ap.add_argument("--no-ssim", action="store_true",
+                    help="skip the fused-vs-torch SSIM loss leg")
     return ap.parse_args()
 
 
@@ -708,7 +710,7 @@ def run_gb300(args):
     multi = None
     if rank == 0 and not args.no_multiview:
         multi = multiview_measure(device)
-    loss_ssim = ssim_measure(device) if rank == 0 else None
+    loss_ssim = ssim_measure(device) if rank == 0 and not args.no_ssim else None
     if rank == 0:
         cpu = None
         if world == 1 and not args.no_cpu_baseline:

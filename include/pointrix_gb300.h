@@ -287,6 +287,26 @@ int pgb_alpha_blending_backward_views_with_batch(
     float* d_conic, float* d_opacity, float* d_feature, int64_t* info, void* stream, int batch);
 int pgb_blend_batches(int backward, int32_t* out);
 
+/* Feature pieces (no counterpart in the reference): the single-view blend
+ * with the [N,C] feature given as npieces [N,w_p] row-major device tensors
+ * (pieces / widths are HOST arrays; sum of widths = C <= 26), e.g. rgb,
+ * depth and a normal without concatenating them; the backward writes each
+ * piece's gradient to d_pieces[p] ([N,w_p]).  Same results as the [N,C]
+ * entry points on the concatenation; `batch` as above. */
+int pgb_alpha_blending_forward_pieces(const float* uv, const float* conic, const float* opacity,
+                                      const float* const* pieces, const int32_t* widths,
+                                      int npieces, int64_t n, const int32_t* ids, int64_t k,
+                                      const int32_t* tile_range, float bg, int width, int height,
+                                      float* records, float* out, float* final_T,
+                                      int32_t* n_contrib, int64_t* info, void* stream, int batch);
+int pgb_alpha_blending_backward_pieces(const float* records, int64_t n, const int32_t* widths,
+                                       int npieces, const int32_t* ids, int64_t k,
+                                       const int32_t* tile_range, float bg, int width, int height,
+                                       const float* final_T, const int32_t* n_contrib,
+                                       const float* d_out, float* grad_records, float* d_uv,
+                                       float* d_conic, float* d_opacity, float* const* d_pieces,
+                                       int64_t* info, void* stream, int batch);
+
 /* ---------------------------------------------------------------------
  * Adam step over several parameter tensors in one launch -- replaces the
  * torch Adam update of the training step (pointrix/optimizer/optimizer.py:

@@ -54,6 +54,10 @@ SIGNATURES = {
     "pgb_alpha_blending_backward_views_with_batch": [vp, i64, i32, vp, i64, vp, f32, vp, i32, vp, vp, vp,
                                                      vp, vp, vp, vp, vp, vp, vp, i32],
     "pgb_blend_batches": [i32, vp],
+    "pgb_alpha_blending_forward_pieces": [vp, vp, vp, vp, vp, i32, i64, vp, i64, vp, f32, i32, i32,
+                                          vp, vp, vp, vp, vp, vp, i32],
+    "pgb_alpha_blending_backward_pieces": [vp, i64, vp, i32, vp, i64, vp, f32, i32, i32, vp, vp, vp,
+                                           vp, vp, vp, vp, vp, vp, vp, i32],
 }
 class AdamSegment(C.Structure):
     """``pgb_adam_segment`` of include/pointrix_gb300.h."""

@@ -15,25 +15,60 @@ every compiled batch on the live inputs (CUDA events, one warm-up and two
 timed runs each) and keeps the fastest for the class; later calls -- and
 calls while a CUDA graph is being captured -- use the kept choice (or the
 default before any).  ``PGB_AUTOTUNE=0`` in the environment disables timing
-(the default batch is used).
+(the default batch is used).  ``PGB_AUTOTUNE_CACHE=<file>`` keeps the
+choices in a JSON file: read on first use, rewritten after every new choice,
+so a later process (a profiler run, a restarted trainer) takes the same
+variants without timing them again.
 
 A class is (kernel, channel count, log2 of the pixel count, log2 of the
 mean list length per tile): the quantities that move the optimum.
 """
 from __future__ import annotations
 
+import json
 import math
 import os
 import threading
 
 import torch
 
-__all__ = ["choose", "workload_class", "table", "timings", "reset", "set_enabled"]
+__all__ = ["choose", "workload_class", "table", "timings", "reset", "set_enabled",
+           "set_cache_file"]
 
 _lock = threading.Lock()
 _cache: dict = {}
 _times: dict = {}
 _enabled = os.environ.get("PGB_AUTOTUNE", "1") != "0"
+_cache_file = os.environ.get("PGB_AUTOTUNE_CACHE") or None
+_loaded = False
+
+
+def _key_str(key) -> str:
+    return "/".join(map(str, key))
+
+
+def _load_locked() -> None:
+    global _loaded
+    if _loaded or not _cache_file:
+        return
+    _loaded = True
+    try:
+        with open(_cache_file) as f:
+            saved = json.load(f)
+    except (OSError, ValueError):
+        return
+    for k, b in saved.items():
+        kind, *rest = k.split("/")
+        _cache.setdefault((kind, *map(int, rest)), int(b))
+
+
+def _save_locked() -> None:
+    if not _cache_file:
+        return
+    tmp = _cache_file + ".tmp"
+    with open(tmp, "w") as f:
+        json.dump({_key_str(k): b for k, b in _cache.items()}, f)
+    os.replace(tmp, _cache_file)
 
 
 def workload_class(kind: str, channels: int, pixels: int, entries: int, tiles: int) -> tuple:
@@ -59,6 +94,7 @@ def choose(key, candidates, run, device=None, timer=None) -> int:
     capturing) the fastest of ``candidates`` timed with ``run(batch)``, else
     0 (the library default)."""
     with _lock:
+        _load_locked()
         hit = _cache.get(key)
     if hit is not None:
         return hit
@@ -71,6 +107,7 @@ def choose(key, candidates, run, device=None, timer=None) -> int:
     with _lock:
         _times.setdefault(key, times)
         _cache.setdefault(key, best)
+        _save_locked()
         return _cache[key]
 
 
@@ -90,6 +127,15 @@ def reset() -> None:
     with _lock:
         _cache.clear()
         _times.clear()
+
+
+def set_cache_file(path) -> None:
+    """Keep the choices in ``path`` (None: in memory only); loads it now."""
+    global _cache_file, _loaded
+    with _lock:
+        _cache_file = os.fspath(path) if path else None
+        _loaded = False
+        _load_locked()
 
 
 def set_enabled(flag: bool) -> None:

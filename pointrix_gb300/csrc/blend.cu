@@ -166,10 +166,49 @@ constexpr int kRecFeat = 8;  // offset of the first feature in a record (16-byte
 __host__ __device__ constexpr int rec_floats(int C) { return kRecFeat + ((C + 3) / 4) * 4; }
 __host__ __device__ constexpr int grad_floats(int C) { return 6 + C <= 16 ? 16 : 32; }
 
+// Where feature channel c of Gaussian i lives: src[c][i * stride[c]] (one
+// [N,C] tensor: src[c] = feature + c, stride C; or the columns of several
+// [N,w] pieces, so that a caller need not concatenate them).  The gradient
+// side writes dst[c][i * stride[c]].  Sized for the largest record.
+constexpr int kMaxCols = 28;
+struct FeatCols {
+  const float* src[kMaxCols];
+  int stride[kMaxCols];
+};
+struct FeatGradCols {
+  float* dst[kMaxCols];
+  int stride[kMaxCols];
+};
+
+// Columns of pieces (device pointers, widths) -> table; false when the
+// widths are not positive or add up to more than 26.
+template <typename T, typename Cols>
+inline bool make_cols(T* const* pieces, const int32_t* widths, int npieces, Cols& cols,
+                      int& channels, T** (*slot)(Cols&, int)) {
+  channels = 0;
+  if (!pieces || !widths || npieces < 1) return false;
+  for (int p = 0; p < npieces; ++p) {
+    const int w = widths[p];
+    if (w < 1 || channels + w > 26 || !pieces[p]) return false;
+    for (int c = 0; c < w; ++c) {
+      *slot(cols, channels) = pieces[p] + c;
+      cols.stride[channels] = w;
+      ++channels;
+    }
+  }
+  for (int c = channels; c < kMaxCols; ++c) {
+    *slot(cols, c) = nullptr;
+    cols.stride[c] = 0;
+  }
+  return true;
+}
+inline const float** src_slot(FeatCols& c, int k) { return &c.src[k]; }
+inline float** dst_slot(FeatGradCols& c, int k) { return &c.dst[k]; }
+
 template <int RF>
 __global__ void pack_kernel(const float* __restrict__ uv, const float* __restrict__ conic,
-                            const float* __restrict__ opacity, const float* __restrict__ feature,
-                            int64_t n, int C, float* __restrict__ records) {
+                            const float* __restrict__ opacity, const FeatCols fc, int64_t n, int C,
+                            float* __restrict__ records) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x) {
     float r[RF];
@@ -196,7 +235,8 @@ __global__ void pack_kernel(const float* __restrict__ uv, const float* __restric
     // no comparison rejects, as the alpha test did not)
     r[7] = o > 0.f ? -logf(255.0f * o) : __int_as_float(0x7f800000);
 #pragma unroll
-    for (int k = 0; k < RF - kRecFeat; ++k) r[kRecFeat + k] = k < C ? feature[i * C + k] : 0.f;
+    for (int k = 0; k < RF - kRecFeat; ++k)
+      r[kRecFeat + k] = k < C ? fc.src[k][i * fc.stride[k]] : 0.f;
     float4* dst = reinterpret_cast<float4*>(records + i * RF);
 #pragma unroll
     for (int q = 0; q < RF / 4; ++q)
@@ -634,7 +674,7 @@ __global__ void __launch_bounds__(256 / PX) blend_bwd_kernel(
 template <int RF>
 __global__ void unpack_kernel(const float* __restrict__ g, int64_t n, int C,
                               float* __restrict__ d_uv, float* __restrict__ d_conic,
-                              float* __restrict__ d_opacity, float* __restrict__ d_feature) {
+                              float* __restrict__ d_opacity, const FeatGradCols gc) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x) {
     float r[RF];
@@ -652,7 +692,7 @@ __global__ void unpack_kernel(const float* __restrict__ g, int64_t n, int C,
     d_opacity[i] = r[5];
 #pragma unroll
     for (int c = 0; c < RF - 6; ++c)
-      if (c < C) d_feature[i * C + c] = r[6 + c];
+      if (c < C) gc.dst[c][i * gc.stride[c]] = r[6 + c];
   }
 }
 
@@ -751,15 +791,33 @@ int pgb_blend_grad_record_floats(int channels) {
 
 }  // extern "C"
 
+// One [N,C] tensor as a column table.
+static FeatCols cols_of(const float* feature, int C) {
+  FeatCols fc;
+  for (int c = 0; c < kMaxCols; ++c) {
+    fc.src[c] = c < C && feature ? feature + c : nullptr;
+    fc.stride[c] = C;
+  }
+  return fc;
+}
+static FeatGradCols grad_cols_of(float* d_feature, int C) {
+  FeatGradCols gc;
+  for (int c = 0; c < kMaxCols; ++c) {
+    gc.dst[c] = c < C && d_feature ? d_feature + c : nullptr;
+    gc.stride[c] = C;
+  }
+  return gc;
+}
+
 static int blend_forward_impl(const float* uv, const float* conic, const float* opacity,
-                              const float* feature, int64_t n, int channels, const int32_t* ids,
+                              const FeatCols& fc, int64_t n, int channels, const int32_t* ids,
                               int64_t k, const int32_t* tile_range, float bg, const ViewTable& vt,
                               int tiles, float* records, float* out, float* final_T,
                               int32_t* n_contrib, int64_t* info, void* stream, int batch) {
   const int nc = nc_bucket(channels);
   if (n < 0 || k < 0 || tiles <= 0 || channels < 1 || nc < 0) return PGB_ERR_INVALID;
   if (!tile_range || !out || !final_T || !n_contrib || (k > 0 && !ids)) return PGB_ERR_INVALID;
-  if (n > 0 && (!uv || !conic || !opacity || !feature || !records)) return PGB_ERR_INVALID;
+  if (n > 0 && (!uv || !conic || !opacity || !fc.src[0] || !records)) return PGB_ERR_INVALID;
   cudaStream_t s = as_stream(stream);
   const int2* rg = reinterpret_cast<const int2*>(tile_range);
   switch (nc) {
@@ -767,7 +825,7 @@ static int blend_forward_impl(const float* uv, const float* conic, const float* 
   case N:                                                                                       \
     if (n > 0)                                                                                  \
       pack_kernel<rec_floats(N)><<<stream_grid(n), kStreamThreads, 0, s>>>(uv, conic, opacity,  \
-                                                                           feature, n, channels, \
+                                                                           fc, n, channels,      \
                                                                            records);            \
     return launch_fwd_nc<N>(records, ids, rg, n, bg, vt, tiles, channels, out, final_T,          \
                             n_contrib, info, s, batch);
@@ -782,12 +840,12 @@ static int blend_backward_impl(const float* records, int64_t n, int channels, co
                                int64_t k, const int32_t* tile_range, float bg, const ViewTable& vt,
                                int tiles, const float* final_T, const int32_t* n_contrib,
                                const float* d_out, float* grad_records, float* d_uv,
-                               float* d_conic, float* d_opacity, float* d_feature, int64_t* info,
-                               void* stream, int batch) {
+                               float* d_conic, float* d_opacity, const FeatGradCols& gc,
+                               int64_t* info, void* stream, int batch) {
   const int nc = nc_bucket(channels);
   if (n < 0 || k < 0 || tiles <= 0 || channels < 1 || nc < 0) return PGB_ERR_INVALID;
   if (!tile_range || !final_T || !n_contrib || !d_out || (k > 0 && !ids)) return PGB_ERR_INVALID;
-  if (n > 0 && (!records || !grad_records || !d_uv || !d_conic || !d_opacity || !d_feature))
+  if (n > 0 && (!records || !grad_records || !d_uv || !d_conic || !d_opacity || !gc.dst[0]))
     return PGB_ERR_INVALID;
   if (n == 0) return PGB_OK;
   cudaStream_t s = as_stream(stream);
@@ -810,10 +868,10 @@ static int blend_backward_impl(const float* records, int64_t n, int channels, co
   if (st != PGB_OK) return st;
   if (GRf == 16)
     unpack_kernel<16><<<stream_grid(n), kStreamThreads, 0, s>>>(grad_records, n, channels, d_uv,
-                                                                d_conic, d_opacity, d_feature);
+                                                                d_conic, d_opacity, gc);
   else
     unpack_kernel<32><<<stream_grid(n), kStreamThreads, 0, s>>>(grad_records, n, channels, d_uv,
-                                                                d_conic, d_opacity, d_feature);
+                                                                d_conic, d_opacity, gc);
   return launch_status();
 }
 
@@ -827,9 +885,10 @@ int pgb_alpha_blending_forward_with_batch(const float* uv, const float* conic,
                                           int32_t* n_contrib, int64_t* info, void* stream,
                                           int batch) {
   if (width <= 0 || height <= 0) return PGB_ERR_INVALID;
-  return blend_forward_impl(uv, conic, opacity, feature, n, channels, ids, k, tile_range, bg,
-                            single_view(width, height), grid_x(width) * grid_y(height), records,
-                            out, final_T, n_contrib, info, stream, batch);
+  return blend_forward_impl(uv, conic, opacity, cols_of(feature, channels), n, channels, ids, k,
+                            tile_range, bg, single_view(width, height),
+                            grid_x(width) * grid_y(height), records, out, final_T, n_contrib, info,
+                            stream, batch);
 }
 
 int pgb_alpha_blending_forward(const float* uv, const float* conic, const float* opacity,
@@ -853,8 +912,8 @@ int pgb_alpha_blending_backward_with_batch(const float* records, int64_t n, int 
   if (width <= 0 || height <= 0) return PGB_ERR_INVALID;
   return blend_backward_impl(records, n, channels, ids, k, tile_range, bg,
                              single_view(width, height), grid_x(width) * grid_y(height), final_T,
-                             n_contrib, d_out, grad_records, d_uv, d_conic, d_opacity, d_feature,
-                             info, stream, batch);
+                             n_contrib, d_out, grad_records, d_uv, d_conic, d_opacity,
+                             grad_cols_of(d_feature, channels), info, stream, batch);
 }
 
 int pgb_alpha_blending_backward(const float* records, int64_t n, int channels,
@@ -878,9 +937,9 @@ int pgb_alpha_blending_forward_views_with_batch(
   uint32_t T = 0;
   int64_t pixels = 0;
   if (!make_views(sizes, nviews, n_per_view, vt, T, pixels)) return PGB_ERR_INVALID;
-  return blend_forward_impl(uv, conic, opacity, feature, n_per_view * nviews, channels, ids, k,
-                            tile_range, bg, vt, (int)T, records, out, final_T, n_contrib, info,
-                            stream, batch);
+  return blend_forward_impl(uv, conic, opacity, cols_of(feature, channels), n_per_view * nviews,
+                            channels, ids, k, tile_range, bg, vt, (int)T, records, out, final_T,
+                            n_contrib, info, stream, batch);
 }
 
 int pgb_alpha_blending_forward_views(const float* uv, const float* conic, const float* opacity,
@@ -906,7 +965,7 @@ int pgb_alpha_blending_backward_views_with_batch(
   if (!make_views(sizes, nviews, n_per_view, vt, T, pixels)) return PGB_ERR_INVALID;
   return blend_backward_impl(records, n_per_view * nviews, channels, ids, k, tile_range, bg, vt,
                              (int)T, final_T, n_contrib, d_out, grad_records, d_uv, d_conic,
-                             d_opacity, d_feature, info, stream, batch);
+                             d_opacity, grad_cols_of(d_feature, channels), info, stream, batch);
 }
 
 int pgb_alpha_blending_backward_views(const float* records, int64_t n_per_view, int channels,
@@ -919,6 +978,40 @@ int pgb_alpha_blending_backward_views(const float* records, int64_t n_per_view, 
   return pgb_alpha_blending_backward_views_with_batch(
       records, n_per_view, channels, ids, k, tile_range, bg, sizes, nviews, final_T, n_contrib,
       d_out, grad_records, d_uv, d_conic, d_opacity, d_feature, info, stream, 0);
+}
+
+int pgb_alpha_blending_forward_pieces(const float* uv, const float* conic, const float* opacity,
+                                      const float* const* pieces, const int32_t* widths,
+                                      int npieces, int64_t n, const int32_t* ids, int64_t k,
+                                      const int32_t* tile_range, float bg, int width, int height,
+                                      float* records, float* out, float* final_T,
+                                      int32_t* n_contrib, int64_t* info, void* stream, int batch) {
+  if (width <= 0 || height <= 0) return PGB_ERR_INVALID;
+  FeatCols fc;
+  int channels = 0;
+  if (!make_cols<const float, FeatCols>(pieces, widths, npieces, fc, channels, src_slot))
+    return PGB_ERR_INVALID;
+  return blend_forward_impl(uv, conic, opacity, fc, n, channels, ids, k, tile_range, bg,
+                            single_view(width, height), grid_x(width) * grid_y(height), records,
+                            out, final_T, n_contrib, info, stream, batch);
+}
+
+int pgb_alpha_blending_backward_pieces(const float* records, int64_t n, const int32_t* widths,
+                                       int npieces, const int32_t* ids, int64_t k,
+                                       const int32_t* tile_range, float bg, int width, int height,
+                                       const float* final_T, const int32_t* n_contrib,
+                                       const float* d_out, float* grad_records, float* d_uv,
+                                       float* d_conic, float* d_opacity, float* const* d_pieces,
+                                       int64_t* info, void* stream, int batch) {
+  if (width <= 0 || height <= 0) return PGB_ERR_INVALID;
+  FeatGradCols gc;
+  int channels = 0;
+  if (!make_cols<float, FeatGradCols>(d_pieces, widths, npieces, gc, channels, dst_slot))
+    return PGB_ERR_INVALID;
+  return blend_backward_impl(records, n, channels, ids, k, tile_range, bg,
+                             single_view(width, height), grid_x(width) * grid_y(height), final_T,
+                             n_contrib, d_out, grad_records, d_uv, d_conic, d_opacity, gc, info,
+                             stream, batch);
 }
 
 // Batch sizes compiled for the forward (backward = 0) or the backward (1).

@@ -11,6 +11,7 @@ device; all work is enqueued on the current CUDA stream.  Errors raise
 """
 from __future__ import annotations
 
+import ctypes
 import threading
 
 import torch
@@ -21,7 +22,8 @@ from ._lib import PgbError, call
 __all__ = [
     "compute_sh", "project_point", "compute_cov3d", "ewa_project", "sort_gaussian",
     "sort_gaussian_begin", "SortHandle", "rasterize",
-    "alpha_blending", "alpha_blending_with_state", "check_device_status", "kernel_timing",
+    "alpha_blending", "alpha_blending_with_state", "alpha_blending_pieces", "check_device_status",
+    "kernel_timing",
     "NEAREST_DEFAULT", "EXTENT_DEFAULT",
 ]
 
@@ -555,9 +557,23 @@ def _blend_batches(backward: int) -> tuple:
     return hit
 
 
+def _piece_table(tensors):
+    """Host arrays (device pointers, widths) of [N,w] pieces."""
+    ptrs = (ctypes.c_void_p * len(tensors))(*[t.data_ptr() for t in tensors])
+    widths = (ctypes.c_int32 * len(tensors))(*[t.shape[1] for t in tensors])
+    return ptrs, widths
+
+
 def _blend_forward_raw(uv, conic, opacity, feature, ids, tile_range, bg, W, H):
-    n, C = feature.shape
-    dev = feature.device
+    """``feature``: one [N,C] tensor, or a list of contiguous [N,w] pieces
+    (blended as their concatenation, which is never built)."""
+    pieces = list(feature) if isinstance(feature, (list, tuple)) else None
+    if pieces is None:
+        n, C = feature.shape
+        dev = feature.device
+    else:
+        n, C = pieces[0].shape[0], sum(t.shape[1] for t in pieces)
+        dev = pieces[0].device
     rf = _lib.lib().pgb_blend_record_floats(C)
     records = torch.empty(n, rf, dtype=torch.float32, device=dev)
     out = torch.empty(C, H, W, dtype=torch.float32, device=dev)
@@ -565,10 +581,20 @@ def _blend_forward_raw(uv, conic, opacity, feature, ids, tile_range, bg, W, H):
     ncon = torch.empty(H, W, dtype=torch.int32, device=dev)
     status = _status_word(dev)
 
-    def run(batch):
-        call("pgb_alpha_blending_forward_with_batch", _ptr(uv), _ptr(conic), _ptr(opacity),
-             _ptr(feature), n, C, _ptr(ids), ids.numel(), _ptr(tile_range), float(bg), W, H,
-             _ptr(records), _ptr(out), _ptr(final_T), _ptr(ncon), _ptr(status), _stream(dev), batch)
+    if pieces is None:
+        def run(batch):
+            call("pgb_alpha_blending_forward_with_batch", _ptr(uv), _ptr(conic), _ptr(opacity),
+                 _ptr(feature), n, C, _ptr(ids), ids.numel(), _ptr(tile_range), float(bg), W, H,
+                 _ptr(records), _ptr(out), _ptr(final_T), _ptr(ncon), _ptr(status), _stream(dev),
+                 batch)
+    else:
+        ptrs, widths = _piece_table(pieces)
+
+        def run(batch):
+            call("pgb_alpha_blending_forward_pieces", _ptr(uv), _ptr(conic), _ptr(opacity), ptrs,
+                 widths, len(pieces), n, _ptr(ids), ids.numel(), _ptr(tile_range), float(bg), W, H,
+                 _ptr(records), _ptr(out), _ptr(final_T), _ptr(ncon), _ptr(status), _stream(dev),
+                 batch)
 
     key = autotune.workload_class("blend_fwd", C, W * H, ids.numel(), tile_range.shape[0])
     batch = autotune.choose(key, _blend_batches(0), run, dev) if n else 0
@@ -577,20 +603,35 @@ def _blend_forward_raw(uv, conic, opacity, feature, ids, tile_range, bg, W, H):
     return records, out, final_T, ncon
 
 
-def _blend_backward_raw(records, ids, tile_range, final_T, ncon, d_out, n, C, bg, W, H):
+def _blend_backward_raw(records, ids, tile_range, final_T, ncon, d_out, n, C, bg, W, H,
+                        widths=None):
+    """Gradients (uv, conic, opacity, feature); with ``widths`` the feature
+    gradient is a list of [N,w] pieces."""
     dev = records.device
     grec = torch.empty(n, _lib.lib().pgb_blend_grad_record_floats(C), dtype=torch.float32, device=dev)
     d_uv = torch.empty(n, 2, dtype=torch.float32, device=dev)
     d_conic = torch.empty(n, 3, dtype=torch.float32, device=dev)
     d_op = torch.empty(n, dtype=torch.float32, device=dev)
-    d_feat = torch.empty(n, C, dtype=torch.float32, device=dev)
     status = _status_word(dev)
     d_out = _c(d_out)
 
-    def run(batch):
-        call("pgb_alpha_blending_backward_with_batch", _ptr(records), n, C, _ptr(ids), ids.numel(),
-             _ptr(tile_range), bg, W, H, _ptr(final_T), _ptr(ncon), _ptr(d_out), _ptr(grec),
-             _ptr(d_uv), _ptr(d_conic), _ptr(d_op), _ptr(d_feat), _ptr(status), _stream(dev), batch)
+    if widths is None:
+        d_feat = torch.empty(n, C, dtype=torch.float32, device=dev)
+
+        def run(batch):
+            call("pgb_alpha_blending_backward_with_batch", _ptr(records), n, C, _ptr(ids),
+                 ids.numel(), _ptr(tile_range), bg, W, H, _ptr(final_T), _ptr(ncon), _ptr(d_out),
+                 _ptr(grec), _ptr(d_uv), _ptr(d_conic), _ptr(d_op), _ptr(d_feat), _ptr(status),
+                 _stream(dev), batch)
+    else:
+        d_feat = [torch.empty(n, w, dtype=torch.float32, device=dev) for w in widths]
+        ptrs, wtab = _piece_table(d_feat)
+
+        def run(batch):
+            call("pgb_alpha_blending_backward_pieces", _ptr(records), n, wtab, len(d_feat),
+                 _ptr(ids), ids.numel(), _ptr(tile_range), bg, W, H, _ptr(final_T), _ptr(ncon),
+                 _ptr(d_out), _ptr(grec), _ptr(d_uv), _ptr(d_conic), _ptr(d_op), ptrs,
+                 _ptr(status), _stream(dev), batch)
 
     key = autotune.workload_class("blend_bwd", C, W * H, ids.numel(), tile_range.shape[0])
     batch = autotune.choose(key, _blend_batches(1), run, dev) if n else 0
@@ -618,6 +659,31 @@ class _AlphaBlending(torch.autograd.Function):
                                                           d_out, n, C, bg, W, H)
         d_ndc = d_uv.clone() if has_ndc else None
         return d_uv, d_conic, d_op, d_feat, None, None, None, None, None, d_ndc
+
+
+class _AlphaBlendingPieces(torch.autograd.Function):
+    """alpha_blending over the concatenation of [N,w] feature pieces, which
+    is never built; each piece gets its own gradient tensor."""
+
+    @staticmethod
+    def forward(ctx, uv, conic, opacity, ids, tile_range, bg, W, H, ndc, *pieces):
+        n = uv.shape[0]
+        widths = [t.shape[1] for t in pieces]
+        records, out, final_T, ncon = _blend_forward_raw(uv, conic, opacity, pieces, ids,
+                                                         tile_range, bg, W, H)
+        ctx.save_for_backward(records, ids, tile_range, final_T, ncon)
+        ctx.cfg = (n, sum(widths), widths, float(bg), W, H, ndc is not None)
+        ctx.mark_non_differentiable(final_T, ncon)
+        return out, final_T, ncon
+
+    @staticmethod
+    def backward(ctx, d_out, _dT, _dn):
+        records, ids, tile_range, final_T, ncon = ctx.saved_tensors
+        n, C, widths, bg, W, H, has_ndc = ctx.cfg
+        d_uv, d_conic, d_op, d_feat = _blend_backward_raw(records, ids, tile_range, final_T, ncon,
+                                                          d_out, n, C, bg, W, H, widths)
+        d_ndc = d_uv.clone() if has_ndc else None
+        return (d_uv, d_conic, d_op, None, None, None, None, None, d_ndc, *d_feat)
 
 
 class _RasterizeRecompute(torch.autograd.Function):
@@ -649,6 +715,8 @@ class _RasterizeRecompute(torch.autograd.Function):
 def rasterize(uv, conic, opacity, feature, depth, radius, tiles_touched, bg, W, H, ndc=None,
               recompute=False, capacity=None):
     """``sort_gaussian`` followed by ``alpha_blending`` -> [C,H,W].
+    ``feature`` is [N,C] or a list of [N,w] pieces (blended as their
+    concatenation, without building it).
 
     With ``recompute=False`` this is exactly the two operators.  With
     ``recompute=True`` the backward re-runs the sort and the blend forward
@@ -659,7 +727,11 @@ def rasterize(uv, conic, opacity, feature, depth, radius, tiles_touched, bg, W, 
     :func:`sort_gaussian` (K kept on the device, no synchronisation)."""
     if not recompute:
         ids, rng = sort_gaussian(uv, depth, W, H, radius, tiles_touched, capacity=capacity)
+        if isinstance(feature, (list, tuple)):
+            return alpha_blending_pieces(uv, conic, opacity, feature, ids, rng, bg, W, H, ndc)
         return alpha_blending(uv, conic, opacity, feature, ids, rng, bg, W, H, ndc)
+    if isinstance(feature, (list, tuple)):
+        feature = torch.cat(list(feature), dim=-1)
     _need(feature, "feature", ndim=2)
     n, C = feature.shape
     if C < 1 or C > 26:
@@ -697,6 +769,41 @@ def alpha_blending_with_state(uv, conic, opacity, feature, gaussian_ids_sorted, 
         raise ValueError(f"ndc must be [N,2], got {tuple(ndc.shape)}")
     return _AlphaBlending.apply(_c(uv), _c(conic), _c(opacity.reshape(n)), _c(feature),
                                 _c(gaussian_ids_sorted), _c(tile_range), bg, W, H, ndc)
+
+
+def alpha_blending_pieces(uv, conic, opacity, pieces, gaussian_ids_sorted, tile_range, bg, W, H,
+                          ndc=None):
+    """:func:`alpha_blending` of ``torch.cat(pieces, 1)`` without building
+    the concatenation: ``pieces`` are [N,w] feature tensors (at most 26
+    channels in all), each receiving its own gradient."""
+    pieces = [t if t.dim() == 2 else t.reshape(t.shape[0], -1) for t in pieces]
+    if not pieces:
+        raise ValueError("alpha_blending_pieces needs at least one feature piece")
+    n = uv.shape[0]
+    for t in pieces:
+        if not (t.is_cuda and t.dtype == torch.float32) or t.shape[0] != n or t.shape[1] < 1:
+            raise ValueError(f"feature pieces must be CUDA float32 [N,w], got {tuple(t.shape)}")
+    C = sum(t.shape[1] for t in pieces)
+    if C > 26:
+        raise ValueError(f"alpha_blending supports 1..26 feature channels, got {C}")
+    _need(uv, "uv", ndim=2, last=2)
+    _need(conic, "conic", ndim=2, last=3)
+    _need(opacity, "opacity")
+    _need(gaussian_ids_sorted, "gaussian_ids_sorted", dtype=torch.int32)
+    _need(tile_range, "tile_range", dtype=torch.int32, ndim=2, last=2)
+    if conic.shape[0] != n or opacity.numel() != n:
+        raise ValueError("alpha_blending: uv, conic, opacity and feature disagree on N")
+    W, H = int(W), int(H)
+    T = ((W + TILE - 1) // TILE) * ((H + TILE - 1) // TILE)
+    if tile_range.shape[0] != T:
+        raise ValueError(f"tile_range has {tile_range.shape[0]} rows, the {W}x{H} image has {T} tiles")
+    if isinstance(bg, torch.Tensor):
+        bg = float(bg)
+    if ndc is not None and tuple(ndc.shape) != (n, 2):
+        raise ValueError(f"ndc must be [N,2], got {tuple(ndc.shape)}")
+    return _AlphaBlendingPieces.apply(_c(uv), _c(conic), _c(opacity.reshape(n)),
+                                      _c(gaussian_ids_sorted), _c(tile_range), bg, W, H, ndc,
+                                      *[t.contiguous() for t in pieces])[0]
 
 
 def alpha_blending(uv, conic, opacity, feature, gaussian_ids_sorted, tile_range, bg, W, H, ndc=None):

@@ -127,7 +127,10 @@ class MsplatRender:
             feats["depth"] = depth
         feats.update(kwargs.get("extra_features") or {})
         render_features = RenderFeatures(**feats)
-        packed = render_features.combine()
+        if self.cfg.recompute_backward:
+            packed = render_features.combine()
+        else:  # blended as one [N,C] feature without concatenating the pieces
+            packed = [v.reshape(n, -1) for _, v in render_features._items()]
 
         ndc = torch.zeros_like(uv, requires_grad=True)
         try:

@@ -33,3 +33,20 @@ def test_classes_and_disable():
     finally:
         autotune.set_enabled(True)
         autotune.reset()
+
+
+def test_cache_file_round_trip(tmp_path):
+    path = tmp_path / "tune.json"
+    autotune.reset()
+    autotune.set_cache_file(path)
+    try:
+        key = autotune.workload_class("blend_fwd", 7, 1600 * 1060, 16_600_000, 6700)
+        assert autotune.choose(key, (64, 128), lambda b: None,
+                               timer=lambda fn: 1.0) == 64  # tie: the smaller
+        autotune.reset()
+        autotune.set_cache_file(path)      # a new process: choices come back untimed
+        assert autotune.choose(key, (64, 128), lambda b: None,
+                               timer=lambda fn: (_ for _ in ()).throw(AssertionError)) == 64
+    finally:
+        autotune.set_cache_file(None)
+        autotune.reset()

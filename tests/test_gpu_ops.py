@@ -397,3 +397,28 @@ def test_blend_batches_agree(small):
         for a, b in zip(g, grads[0]):
             assert scaled_err(a, b) < 1e-5
     ops.check_device_status()
+
+
+def test_alpha_blending_pieces_matches_concatenation(small):
+    """Pieces blend exactly like their concatenation; each piece gets the
+    matching columns of the feature gradient."""
+    p = small
+    f = p.feat
+    pieces = [f[:, :3].contiguous(), f[:, 3:4].contiguous()]
+    up = torch.randn((f.shape[1], p.H, p.W), generator=torch.Generator().manual_seed(5)).to(DEV)
+    leaves_a = [t.detach().clone().requires_grad_(True) for t in (p.uv, p.conic, p.op, f)]
+    img_a = ops.alpha_blending(*leaves_a, p.ids, p.rng, 0.3, p.W, p.H)
+    img_a.backward(up)
+    leaves_b = [t.detach().clone().requires_grad_(True) for t in (p.uv, p.conic, p.op)]
+    pieces_b = [t.detach().clone().requires_grad_(True) for t in pieces]
+    ndc = torch.zeros_like(p.uv, requires_grad=True)
+    img_b = ops.alpha_blending_pieces(*leaves_b, pieces_b, p.ids, p.rng, 0.3, p.W, p.H, ndc)
+    img_b.backward(up)
+    assert torch.equal(img_a, img_b)
+    for a, b in zip(leaves_a[:3], leaves_b):
+        assert scaled_err(b.grad, a.grad) < 1e-5
+    assert scaled_err(torch.cat([t.grad for t in pieces_b], 1), leaves_a[3].grad) < 1e-5
+    assert torch.equal(ndc.grad, leaves_b[0].grad)
+    with pytest.raises(ValueError):
+        ops.alpha_blending_pieces(p.uv, p.conic, p.op, [], p.ids, p.rng, 0.0, p.W, p.H)
+    ops.check_device_status()
