@@ -121,6 +121,9 @@ int pgb_ewa_project_backward(const float* xyz, const float* cov3d, const float* 
  * After finish, info[1] holds a PGB_* status raised on the device
  * (PGB_ERR_TIMEOUT, PGB_ERR_MISMATCH, PGB_ERR_OVERFLOW) or 0.
  * Scratch: bytes_n for (n), bytes_k for (k); pass k = 0 to size bytes_n.
+ * bytes_k depends on the tile count of (width, height); for a batch of
+ * views pass any (width, height) with the batch's total tile count
+ * (e.g. 16 T x 16).
  * ------------------------------------------------------------------- */
 int pgb_sort_scratch_bytes(int64_t n, int64_t k, int width, int height, size_t* bytes_n,
                            size_t* bytes_k);

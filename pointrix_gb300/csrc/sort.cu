@@ -862,35 +862,13 @@ inline ScratchN layout_n(int64_t n) {
   return L;
 }
 
-struct ScratchK {
-  size_t tk0, tv0, tk1, tv1, status, chunk_first, total;
-  int parts;
-  int64_t chunks;
-};
-
-inline ScratchK layout_k(int64_t k) {
-  ScratchK L;
-  L.parts = (int)((k + kPartKeys - 1) / kPartKeys);
-  size_t o = 0;
-  const size_t kb = align256((size_t)k * sizeof(uint32_t));
-  L.tk0 = o; o += kb;
-  L.tv0 = o; o += kb;
-  L.tk1 = o; o += kb;
-  L.tv1 = o; o += kb;
-  L.status = o; o += align256((size_t)L.parts * kTileHistWords * sizeof(uint32_t));
-  L.chunks = (k + kEmitChunk - 1) / kEmitChunk;
-  L.chunk_first = o; o += align256((size_t)(L.chunks + 2) * sizeof(uint32_t));
-  L.total = o;
-  return L;
-}
-
 // Tile passes for T tiles: digit width and count (one 8-bit pass up to 256
 // tiles, two up to 2^16, two 9-bit passes up to 2^18, else three 8-bit).
 struct TilePlan {
   int passes, bits;
 };
 
-inline TilePlan tile_plan(uint32_t T) {
+inline TilePlan tile_plan(uint64_t T) {
   int b = 0;
   while (b < 32 && ((T - 1) >> b)) ++b;
   if (b <= 8) return {1, 8};
@@ -898,6 +876,34 @@ inline TilePlan tile_plan(uint32_t T) {
   if (b <= 18) return {2, 9};
   return {3, 8};
 }
+
+struct ScratchK {
+  size_t tk0, tv0, tk1, tv1, status, chunk_first, total;
+  int parts;
+  int64_t chunks;
+};
+
+// K-sized pair buffers: pass 0 generates its pairs and writes pair buffer 1,
+// pass 1 reads it and writes buffer 0, pass 2 reads that; the last pass
+// writes the ids out.  So one tile pass needs no buffer, two need buffer 1,
+// three need both.
+inline ScratchK layout_k(int64_t k, int passes) {
+  ScratchK L;
+  L.parts = (int)((k + kPartKeys - 1) / kPartKeys);
+  size_t o = 0;
+  const size_t kb = align256((size_t)k * sizeof(uint32_t));
+  const size_t kb0 = passes >= 3 ? kb : 0, kb1 = passes >= 2 ? kb : 0;
+  L.tk0 = o; o += kb0;
+  L.tv0 = o; o += kb0;
+  L.tk1 = o; o += kb1;
+  L.tv1 = o; o += kb1;
+  L.status = o; o += align256((size_t)L.parts * kTileHistWords * sizeof(uint32_t));
+  L.chunks = (k + kEmitChunk - 1) / kEmitChunk;
+  L.chunk_first = o; o += align256((size_t)(L.chunks + 2) * sizeof(uint32_t));
+  L.total = o;
+  return L;
+}
+
 
 template <typename P>
 inline P* at(void* base, size_t off) {
@@ -940,8 +946,9 @@ extern "C" {
 int pgb_sort_scratch_bytes(int64_t n, int64_t k, int width, int height, size_t* bytes_n,
                            size_t* bytes_k) {
   if (n < 0 || k < 0 || width <= 0 || height <= 0) return PGB_ERR_INVALID;
+  const uint64_t T = (uint64_t)grid_x(width) * (uint64_t)grid_y(height);
   if (bytes_n) *bytes_n = layout_n(n).total;
-  if (bytes_k) *bytes_k = layout_k(k).total;
+  if (bytes_k) *bytes_k = layout_k(k, tile_plan(T).passes).total;
   return PGB_OK;
 }
 
@@ -1000,7 +1007,8 @@ static int sort_finish_impl(const float* uv, const int32_t* radius, const int32_
   if (n < 0 || k < 0 || !info || !tile_range_out) return PGB_ERR_INVALID;
   if (k >= (int64_t)kValMask) return PGB_ERR_OVERFLOW;
   const ScratchN LN = layout_n(n);
-  const ScratchK LK = layout_k(k);
+  const TilePlan plan = tile_plan(T);
+  const ScratchK LK = layout_k(k, plan.passes);
   if (!scratch_n || bytes_n < LN.total) return PGB_ERR_INVALID;
   if (k > 0 && (!scratch_k || bytes_k < LK.total || !ids_out)) return PGB_ERR_INVALID;
   if (T == 0 || T > (1u << (8 * kMaxTilePasses))) return PGB_ERR_INVALID;
@@ -1012,7 +1020,6 @@ static int sort_finish_impl(const float* uv, const int32_t* radius, const int32_
     if (device_k) capacity_check_kernel<<<1, 32, 0, s>>>(info, k, info);
     return launch_status();
   }
-  const TilePlan plan = tile_plan(T);
   if (cudaMemsetAsync(at<char>(scratch_k, LK.status), 0,
                       (size_t)LK.parts * plan.passes * (1u << plan.bits) * sizeof(uint32_t),
                       s) != cudaSuccess)

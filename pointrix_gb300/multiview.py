@@ -48,7 +48,8 @@ def sort_views(uv, depth, radius, tiles_touched, sizes, n_per_view, capacity=Non
     K = h.count() if capacity is None else int(capacity)
     dev = uv.device
     T = sum(_tiles(W, H) for W, H in sizes)
-    _, bk = ops._sort_scratch(h.n, K, W0, H0)
+    # the K-sized scratch depends on the tile count: a 16T x 16 "image" has T tiles
+    _, bk = ops._sort_scratch(h.n, K, 16 * T, 16)
     scratch_k = torch.empty(max(bk, 1), dtype=torch.uint8, device=dev)
     ids = torch.empty(max(K, 1), dtype=torch.int32, device=dev)[:K]
     rng = torch.empty(T, 2, dtype=torch.int32, device=dev)

@@ -44,7 +44,15 @@ def test_invalid_arguments_rejected_without_launch():
     assert lib.pgb_blend_record_floats(27) == -1
     bn, bk = C.c_size_t(0), C.c_size_t(0)
     assert lib.pgb_sort_scratch_bytes(1000, 5000, 64, 64, C.byref(bn), C.byref(bk)) == 0
-    assert bn.value >= 16 * 1000 and bk.value >= 16 * 5000
+    assert bn.value >= 16 * 1000
+    # K-sized pair buffers by tile passes: none for one pass (16 tiles), one
+    # (key, value) pair buffer for two, two for three
+    one = bk.value
+    assert lib.pgb_sort_scratch_bytes(1000, 5000, 1600, 1060, C.byref(bn), C.byref(bk)) == 0
+    two = bk.value
+    assert lib.pgb_sort_scratch_bytes(1000, 5000, 16 * 300000, 16, C.byref(bn), C.byref(bk)) == 0
+    three = bk.value
+    assert two - one >= 8 * 5000 and three - two >= 8 * 5000
     assert lib.pgb_sort_scratch_bytes(-1, 0, 64, 64, C.byref(bn), C.byref(bk)) == 1
     # scratch too small is refused before any CUDA call
     assert lib.pgb_sort_gaussian_begin(None, None, None, 1000, 64, 64, None, 0, None, None) == 1
