@@ -55,39 +55,91 @@ __global__ void adam_tick_kernel(int32_t* __restrict__ steps, float* __restrict_
   }
 }
 
+// One float4 group q of the table: segment s (found by walking forward from
+// the caller's s, since a thread's q only grows), element offset i, and
+// whether the group is a whole aligned float4 of the segment.
+struct AdamGroup {
+  const pgb_adam_segment* sg;
+  int64_t i;
+  float step_size, inv_sqrt_bc2;
+  bool vec;
+};
+
+__device__ __forceinline__ AdamGroup adam_group(const AdamTable& t, const float* bc, int64_t q,
+                                                int& s) {
+  while (q >= t.start4[s + 1]) ++s;
+  AdamGroup gr;
+  gr.sg = &t.seg[s];
+  gr.i = (q - t.start4[s]) * 4;
+  const float bc1 = bc ? bc[2 * s] : gr.sg->bias_correction1;
+  const float bc2 = bc ? bc[2 * s + 1] : gr.sg->bias_correction2;
+  gr.step_size = gr.sg->lr / bc1;
+  gr.inv_sqrt_bc2 = 1.0f / sqrtf(bc2);
+  gr.vec = gr.i + 4 <= gr.sg->n &&
+           (((uintptr_t)gr.sg->param | (uintptr_t)gr.sg->grad | (uintptr_t)gr.sg->exp_avg |
+             (uintptr_t)gr.sg->exp_avg_sq) & 15) == 0;
+  return gr;
+}
+
+__device__ __forceinline__ void adam_scalar(const AdamGroup& gr, float b1, float b2, float eps) {
+  const pgb_adam_segment& sg = *gr.sg;
+  for (int64_t j = gr.i; j < gr.i + 4 && j < sg.n; ++j)
+    adam_one(sg.param[j], sg.grad[j], sg.exp_avg[j], sg.exp_avg_sq[j], b1, b2, eps, gr.step_size,
+             gr.inv_sqrt_bc2);
+}
+
+__device__ __forceinline__ void adam_vec4(float4& p, const float4& g, float4& m, float4& v, float b1,
+                                          float b2, float eps, const AdamGroup& gr) {
+  adam_one(p.x, g.x, m.x, v.x, b1, b2, eps, gr.step_size, gr.inv_sqrt_bc2);
+  adam_one(p.y, g.y, m.y, v.y, b1, b2, eps, gr.step_size, gr.inv_sqrt_bc2);
+  adam_one(p.z, g.z, m.z, v.z, b1, b2, eps, gr.step_size, gr.inv_sqrt_bc2);
+  adam_one(p.w, g.w, m.w, v.w, b1, b2, eps, gr.step_size, gr.inv_sqrt_bc2);
+}
+
 // bc == nullptr: the table's bias corrections; else those the tick formed.
+// Each thread takes two float4 groups per iteration (q and q + stride) and
+// issues all eight loads before the arithmetic, so twice the bytes are in
+// flight per thread.
 __global__ void __launch_bounds__(kAdamThreads) adam_kernel(AdamTable t, float b1, float b2,
                                                             float eps,
                                                             const float* __restrict__ bc) {
   const int64_t total = t.start4[t.nseg];
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   int s = 0;
-  for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < total;
-       q += (int64_t)gridDim.x * blockDim.x) {
-    while (q >= t.start4[s + 1]) ++s;  // q only grows for a thread
-    const pgb_adam_segment& sg = t.seg[s];
-    const int64_t i = (q - t.start4[s]) * 4;
-    const float bc1 = bc ? bc[2 * s] : sg.bias_correction1;
-    const float bc2 = bc ? bc[2 * s + 1] : sg.bias_correction2;
-    const float step_size = sg.lr / bc1;
-    const float inv_sqrt_bc2 = 1.0f / sqrtf(bc2);
-    if (i + 4 <= sg.n && (((uintptr_t)sg.param | (uintptr_t)sg.grad | (uintptr_t)sg.exp_avg |
-                           (uintptr_t)sg.exp_avg_sq) & 15) == 0) {
-      float4 p = reinterpret_cast<float4*>(sg.param)[i / 4];
-      const float4 g = reinterpret_cast<const float4*>(sg.grad)[i / 4];
-      float4 m = reinterpret_cast<float4*>(sg.exp_avg)[i / 4];
-      float4 v = reinterpret_cast<float4*>(sg.exp_avg_sq)[i / 4];
-      adam_one(p.x, g.x, m.x, v.x, b1, b2, eps, step_size, inv_sqrt_bc2);
-      adam_one(p.y, g.y, m.y, v.y, b1, b2, eps, step_size, inv_sqrt_bc2);
-      adam_one(p.z, g.z, m.z, v.z, b1, b2, eps, step_size, inv_sqrt_bc2);
-      adam_one(p.w, g.w, m.w, v.w, b1, b2, eps, step_size, inv_sqrt_bc2);
-      reinterpret_cast<float4*>(sg.param)[i / 4] = p;
-      reinterpret_cast<float4*>(sg.exp_avg)[i / 4] = m;
-      reinterpret_cast<float4*>(sg.exp_avg_sq)[i / 4] = v;
+  for (int64_t q0 = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q0 < total;
+       q0 += 2 * stride) {
+    const int64_t q1 = q0 + stride;
+    const bool has1 = q1 < total;
+    const AdamGroup g0 = adam_group(t, bc, q0, s);
+    int s1 = s;
+    const AdamGroup g1 = has1 ? adam_group(t, bc, q1, s1) : g0;
+    if (g0.vec && (!has1 || g1.vec)) {
+      float4 p0 = reinterpret_cast<float4*>(g0.sg->param)[g0.i / 4];
+      const float4 gg0 = reinterpret_cast<const float4*>(g0.sg->grad)[g0.i / 4];
+      float4 m0 = reinterpret_cast<float4*>(g0.sg->exp_avg)[g0.i / 4];
+      float4 v0 = reinterpret_cast<float4*>(g0.sg->exp_avg_sq)[g0.i / 4];
+      float4 p1, gg1, m1, v1;
+      if (has1) {
+        p1 = reinterpret_cast<float4*>(g1.sg->param)[g1.i / 4];
+        gg1 = reinterpret_cast<const float4*>(g1.sg->grad)[g1.i / 4];
+        m1 = reinterpret_cast<float4*>(g1.sg->exp_avg)[g1.i / 4];
+        v1 = reinterpret_cast<float4*>(g1.sg->exp_avg_sq)[g1.i / 4];
+      }
+      adam_vec4(p0, gg0, m0, v0, b1, b2, eps, g0);
+      reinterpret_cast<float4*>(g0.sg->param)[g0.i / 4] = p0;
+      reinterpret_cast<float4*>(g0.sg->exp_avg)[g0.i / 4] = m0;
+      reinterpret_cast<float4*>(g0.sg->exp_avg_sq)[g0.i / 4] = v0;
+      if (has1) {
+        adam_vec4(p1, gg1, m1, v1, b1, b2, eps, g1);
+        reinterpret_cast<float4*>(g1.sg->param)[g1.i / 4] = p1;
+        reinterpret_cast<float4*>(g1.sg->exp_avg)[g1.i / 4] = m1;
+        reinterpret_cast<float4*>(g1.sg->exp_avg_sq)[g1.i / 4] = v1;
+      }
     } else {
-      for (int64_t j = i; j < i + 4 && j < sg.n; ++j)
-        adam_one(sg.param[j], sg.grad[j], sg.exp_avg[j], sg.exp_avg_sq[j], b1, b2, eps, step_size,
-                 inv_sqrt_bc2);
+      adam_scalar(g0, b1, b2, eps);
+      if (has1) adam_scalar(g1, b1, b2, eps);
     }
+    s = s1;
   }
 }
 

@@ -564,9 +564,9 @@ __global__ void preprocess_bwd_kernel(
     const float* __restrict__ d_conic, float* __restrict__ d_xyz, float* __restrict__ d_scales,
     float* __restrict__ d_q, float* __restrict__ partials) {
   const Cam cm = load_cam(intr, extr);
-  float acc_p[16], acc_e[16];
+  float acc[16];  // camera-gradient partials of the projection and the EWA terms
 #pragma unroll
-  for (int k = 0; k < 16; ++k) acc_p[k] = acc_e[k] = 0.f;
+  for (int k = 0; k < 16; ++k) acc[k] = 0.f;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x) {
     const float x = xyz[3 * i], y = xyz[3 * i + 1], z = xyz[3 * i + 2];
@@ -577,14 +577,14 @@ __global__ void preprocess_bwd_kernel(
     float4 dq = make_float4(0.f, 0.f, 0.f, 0.f);
     if (project_visible(cm, px, py, pz, W, H, nearest, extent, u, v)) {
       project_bwd_one(cm, x, y, z, px, py, pz, reinterpret_cast<const float2*>(d_uv)[i],
-                      d_depth[i], gx, gy, gz, acc_p);
+                      d_depth[i], gx, gy, gz, acc);
       if (radius[i] > 0) {
         float s6[6];
         cov3d_one(scales, q, i, s6);
         float ex = 0.f, ey = 0.f, ez = 0.f;
         float dS[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
         ewa_bwd_one(cm, W, H, x, y, z, s6, d_conic[3 * i], d_conic[3 * i + 1], d_conic[3 * i + 2],
-                    ex, ey, ez, dS, acc_e);
+                    ex, ey, ez, dS, acc);
         gx = gx + ex;
         gy = gy + ey;
         gz = gz + ez;
@@ -599,9 +599,6 @@ __global__ void preprocess_bwd_kernel(
     d_scales[3 * i + 2] = ds[2];
     reinterpret_cast<float4*>(d_q)[i] = dq;
   }
-  float acc[16];
-#pragma unroll
-  for (int k = 0; k < 16; ++k) acc[k] = acc_p[k] + acc_e[k];
   block_write_partials(acc, partials);
 }
 
