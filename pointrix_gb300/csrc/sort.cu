@@ -23,9 +23,11 @@
 //      three, sort the (tile id, Gaussian id) pairs by tile id.  The first
 //      pass generates its partition's pairs from the emission records in
 //      registers (load-balanced: every partition is 6144 pairs however
-//      unevenly the tiles are spread over Gaussians), so the depth-ordered
-//      pair sequence is never written out; the last pass writes only the ids
-//      and records each tile's [start, end) as it goes;
+//      unevenly the tiles are spread over Gaussians): each owner marks the
+//      rectangle rows it starts inside the partition, and a running maximum
+//      over the marks gives every entry its owner and row.  The
+//      depth-ordered pair sequence is never written out; the last pass
+//      writes only the ids and records each tile's [start, end) as it goes;
 //   5. tiles that no entry reached get [0, 0).
 // A stable sort by tile of a depth-ordered sequence is exactly the order of
 // the 64-bit key sort, with K * 16 bytes of traffic per tile pass instead of
@@ -299,8 +301,10 @@ __device__ inline uint32_t owner_search(const OwnerView<STAGED>& ov, uint32_t lo
   return lo;
 }
 
-// Tile entries e0 + lane (e0 uniform over the warp) of the depth-ordered
-// emission: entry j of Gaussian g (owner record offset o) is tile
+// Fallback generation, for a partition with more owners than fit in shared
+// memory (Gaussians of one or two tiles each).  Tile entries e0 + lane (e0
+// uniform over the warp) of the depth-ordered emission: entry j of Gaussian
+// g (owner record offset o) is tile
 // first + (j / w) gx + j % w (one row of `count` tiles when w = 0), value g.
 // `p` is a position whose offset is <= e0 (on return: the same for
 // e0 + 32).  The 32 owner records p .. p + 31 are read one per lane; a
@@ -428,24 +432,85 @@ __global__ void __launch_bounds__(Os<RB>::NT, 2) onesweep_kernel(
       cp_async_wait<0>();
     }
     __syncthreads();
-    // generated through shared memory (s_keys is free until the staging
-    // below), so the generation loop need not be unrolled; keys past the
-    // count stay 0
-    for (int it = 0; it < IT; ++it) s_keys[wofs + it * 32 + lane] = 0u;
-    __syncwarp();
-    if (ok && wofs < cnt) {
-      const uint32_t ew = (uint32_t)pbase + (uint32_t)wofs;
-      const int cnt_w = min(cnt - wofs, 32 * IT);
-      if (staged)
-        gen_warp<true, IT>(OwnerView<true>{owner, s_own, i0}, i0, i1, ew, cnt_w, lane,
-                           s_keys + wofs, s_vin + wofs);
-      else
+    if (staged) {
+      // Row marks: every row of an owner that starts inside the partition
+      // writes (owner + 1) << 16 | row at its start position (s_vals is free
+      // until the staging below); position 0 gets the row holding the
+      // partition's first entry.  Marks grow with the position, so a running
+      // maximum gives every entry its owner and row: no search, no division.
+      __shared__ uint32_t s_wmax[NW];
+      for (int j = t; j < PART; j += NT) s_vals[j] = 0u;
+      __syncthreads();
+      if (ok) {
+        const uint32_t pb = (uint32_t)pbase, pend = pb + (uint32_t)cnt;
+        if (t == 0) {
+          const uint4 r0 = s_own[0];
+          const uint32_t w0 = r0.y & 0xFFFFu;
+          s_vals[0] = (1u << 16) | (w0 ? (pb - r0.w) / w0 : 0u);
+        }
+        for (uint32_t pl = t; pl < m; pl += NT) {
+          const uint4 rec = s_own[pl];
+          const uint32_t off = rec.w, w = rec.y & 0xFFFFu;
+          const uint32_t off_next = pl + 1 < m ? s_own[pl + 1].w : (uint32_t)n;
+          if (off_next <= off) continue;  // no entries
+          const uint32_t tag = (pl + 1) << 16;
+          if (w == 0) {  // one row of `count` tiles
+            if (off >= pb && off < pend) s_vals[off - pb] = tag;
+            continue;
+          }
+          uint32_t r = off < pb ? (pb - off + w - 1) / w : 0u;
+          for (uint32_t st = off + r * w; st < off_next && st < pend; st += w, ++r)
+            s_vals[st - pb] = tag | r;
+        }
+      }
+      __syncthreads();
+      // running maximum in the pass's striped order: per warp over its
+      // 32 * IT positions, then across the warps before it
+      uint32_t run = 0;
+#pragma unroll
+      for (int it = 0; it < IT; ++it) {
+        uint32_t v = s_vals[wofs + it * 32 + lane];
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const uint32_t u = __shfl_up_sync(0xffffffffu, v, o);
+          if (lane >= o) v = max(v, u);
+        }
+        v = max(v, run);
+        run = __shfl_sync(0xffffffffu, v, 31);
+        key[it] = v;
+      }
+      if (lane == 31) s_wmax[warp] = run;
+      __syncthreads();
+      uint32_t pre = 0;
+      for (int w2 = 0; w2 < warp; ++w2) pre = max(pre, s_wmax[w2]);
+#pragma unroll
+      for (int it = 0; it < IT; ++it) {
+        const int j = wofs + it * 32 + lane;
+        const uint32_t mk = max(pre, key[it]);
+        key[it] = 0u;
+        if (ok && j < cnt && mk >= (1u << 16)) {
+          const uint4 rec = s_own[(mk >> 16) - 1];
+          const uint32_t r = mk & 0xFFFFu, w = rec.y & 0xFFFFu, gx = rec.y >> 16;
+          const uint32_t e = (uint32_t)pbase + (uint32_t)j;
+          key[it] = rec.x + r * gx + (e - rec.w - r * w);
+          s_vin[j] = rec.z;  // read back by this thread only
+        }
+      }
+    } else {
+      // more owners than fit in shared memory: the warp-cooperative window
+      // search over owner records in global memory, through s_keys
+      for (int it = 0; it < IT; ++it) s_keys[wofs + it * 32 + lane] = 0u;
+      __syncwarp();
+      if (ok && wofs < cnt) {
+        const uint32_t ew = (uint32_t)pbase + (uint32_t)wofs;
+        const int cnt_w = min(cnt - wofs, 32 * IT);
         gen_warp<false, IT>(OwnerView<false>{owner, s_own, i0}, i0, i1, ew, cnt_w, lane,
                             s_keys + wofs, s_vin + wofs);
-    }
-    __syncwarp();
+      }
+      __syncwarp();
 #pragma unroll
-    for (int it = 0; it < IT; ++it) key[it] = s_keys[wofs + it * 32 + lane];
+      for (int it = 0; it < IT; ++it) key[it] = s_keys[wofs + it * 32 + lane];
+    }
     __syncthreads();  // every warp is done with the owner records
     for (int i = t; i < HW; i += NT) warp_hist[i] = 0;
     __syncthreads();
