@@ -185,16 +185,17 @@ __global__ void __launch_bounds__(kSortThreads) sort_prepare_kernel(
 // 2/4. one stable LSD onesweep pass over RB bits starting at `shift`
 //
 // A partition is NT threads x IT keys (6144: 512 x 12 for 8- and 9-bit
-// digits, 32 warps per SM at two CTAs; 384 x 16 measured 1 % slower).  Keys are ranked in registers
-// (warp-striped: key it of a lane is element it * 32 + lane of its warp's
-// slice, so warp order = element order and ranks are stable); the
-// partition's values travel global -> shared by cp.async meanwhile, so a
-// thread holds only its keys and ranks.  Within a warp equal digits are found
-// by OR-ing each lane's bit into a per-warp digit mask in shared memory
-// (8-bit digits) or with RB ballots, one per digit bit (9-bit digits, whose
-// masks would not fit beside the staging).  The first R threads also act as the R
-// digits for the cross-warp prefix, the status publication and the
-// look-back, which runs while the other warps stage the keys in digit order.
+// digits, 32 warps per SM at two CTAs; 384 x 16 measured 1 % slower).
+// Keys are ranked in registers (warp-striped: key it of a lane is element
+// it * 32 + lane of its warp's slice, so warp order = element order and
+// ranks are stable); the partition's values travel global -> shared by
+// cp.async meanwhile, so a thread holds only its keys and ranks.  Within a
+// warp equal digits are found by OR-ing each lane's bit into a per-warp
+// digit mask in shared memory (8-bit digits) or with RB ballots, one per
+// digit bit (9-bit digits, whose masks would not fit beside the staging).
+// The first R threads also act as the R digits for the cross-warp prefix,
+// the status publication and the look-back, which runs while the other
+// warps stage the keys in digit order.
 //
 // `n_dev` (optional) holds the element count on the device -- the tile
 // passes of a capacity-sized sort, whose grid covers the capacity `cap` --
