@@ -223,10 +223,18 @@ int pgb_alpha_blending_backward(const float* records, int64_t n, int channels,
  * the views' tile counts <= 2^24, tile_range has T rows) and per-pixel
  * arrays hold the views one after another (out: per-view [C,H,W] blocks;
  * final_T, n_contrib: per-view [H,W] blocks).  Phase one of the sort is
- * pgb_sort_gaussian_begin over all V * n_per_view elements (any view's size
- * may be passed there).  Within a tile the order is depth, then element id,
- * so each view's image equals rendering it alone.
+ * pgb_sort_gaussian_begin_views (which orders the elements by view, then
+ * depth, then id; the finish_views entries require it).  The batch's pairs
+ * are then sorted by their view-local tile id, so ids_out holds, for every
+ * local tile t, the lists of view 0, 1, ... one after another, and
+ * tile_range_out[tile_base(v) + t] is view v's list of tile t; within a list
+ * the order is depth, then element id, so each view's image equals
+ * rendering it alone.  Scratch: pgb_sort_scratch_bytes with the largest
+ * view's tile count (e.g. width 16 T_v, height 16).
  * ------------------------------------------------------------------- */
+int pgb_sort_gaussian_begin_views(const float* depth, const int32_t* radius,
+                                  const int32_t* tiles_touched, int64_t n_per_view, int nviews,
+                                  void* scratch_n, size_t bytes_n, int64_t* info, void* stream);
 int pgb_sort_gaussian_finish_views(const float* uv, const int32_t* radius,
                                    const int32_t* tiles_touched, int64_t n_per_view,
                                    const int32_t* sizes, int nviews, int64_t k, void* scratch_n,

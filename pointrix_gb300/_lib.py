@@ -32,6 +32,7 @@ SIGNATURES = {
     "pgb_ewa_project_backward": [vp, vp, vp, vp, vp, i64, i32, i32, vp, vp, vp, vp, vp, vp, szt, vp],
     "pgb_sort_scratch_bytes": [i64, i64, i32, i32, C.POINTER(szt), C.POINTER(szt)],
     "pgb_sort_gaussian_begin": [vp, vp, vp, i64, i32, i32, vp, szt, vp, vp],
+    "pgb_sort_gaussian_begin_views": [vp, vp, vp, i64, i32, vp, szt, vp, vp],
     "pgb_sort_gaussian_finish": [vp, vp, vp, i64, i32, i32, i64, vp, szt, vp, szt, vp, vp, vp, vp],
     "pgb_sort_gaussian_finish_capacity": [vp, vp, vp, i64, i32, i32, i64, vp, szt, vp, szt, vp, vp,
                                           vp, vp],

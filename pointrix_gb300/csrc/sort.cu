@@ -59,6 +59,9 @@ constexpr int kScanPart = kSortThreads * kScanItems;  // 2048
 // onesweep partition is kPartKeys / kEmitChunk chunks.
 constexpr int kEmitChunk = 1024;
 constexpr int kDepthPasses = 4;
+// A batch of views adds one pass over the view index after the depth
+// passes, so that the emission is view-major (depth order within a view).
+constexpr int kViewPass = kDepthPasses;
 constexpr int kMaxTilePasses = 3;
 constexpr int kTileHistWords = 1024;  // 3 passes x 256 digits or 2 x 512
 constexpr uint32_t kFlagAgg = 1u << 30;
@@ -154,8 +157,13 @@ __device__ inline uint32_t look_back(const uint32_t* status, int part, int strid
 __global__ void __launch_bounds__(kSortThreads) sort_prepare_kernel(
     const float* __restrict__ depth, const int32_t* __restrict__ radius,
     const int32_t* __restrict__ tiles, int64_t n, uint32_t* __restrict__ keys,
-    uint32_t* __restrict__ vals, uint32_t* __restrict__ hist, int64_t* __restrict__ info) {
+    uint32_t* __restrict__ vals, uint32_t* __restrict__ hist, int nviews, int64_t n_per_view,
+    int64_t* __restrict__ info) {
   __shared__ uint32_t h[kDepthPasses][256];
+  // the view pass's histogram: n_per_view elements in each view
+  if (blockIdx.x == 0)
+    for (int v = threadIdx.x; v < nviews; v += blockDim.x)
+      hist[kViewPass * 256 + v] = (uint32_t)n_per_view;
   for (int i = threadIdx.x; i < kDepthPasses * 256; i += blockDim.x) (&h[0][0])[i] = 0;
   __syncthreads();
   unsigned long long ksum = 0;
@@ -231,6 +239,39 @@ struct Os {
   static constexpr size_t SMEM = ((size_t)HW + 3 * (size_t)PART) * sizeof(uint32_t);
   static_assert(PART == kPartKeys, "one partition size for every digit width");
   static_assert(NT >= R, "one thread per digit");
+};
+
+// Exact a / d for a < 2^30 with one 64-bit multiply and shift (Granlund and
+// Montgomery's round-up method): s = 32 + ceil(log2 d), m = ceil(2^s / d).
+// Then m < 2^34, a * m < 2^64, and m d - 2^s < d keeps the error of
+// a m / 2^s below a / 2^32 < 1 / d, so the floor is exact.
+struct FastDiv {
+  uint64_t m;
+  int s;
+};
+
+inline FastDiv fast_div(uint32_t d) {
+  int L = 0;
+  while ((1ull << L) < (uint64_t)d) ++L;
+  const int s = 32 + L;
+  return FastDiv{((1ull << s) + d - 1) / d, s};
+}
+
+__device__ __forceinline__ uint32_t fdiv(uint32_t a, const FastDiv& f) {
+  return (uint32_t)(((uint64_t)a * f.m) >> f.s);
+}
+
+// What a pass knows of a batch of views (nviews == 0: one image).  Element
+// ids are v * n_per_view + g; `vdiv` divides by n_per_view.  key_from_val:
+// the keys written are the views of the values (the depth pass before the
+// view pass).  With nviews > 0 the tile passes sort local tile ids, and the
+// last one records the range of view v's local tile t as global tile
+// tile_base[v] + t.
+struct PassViews {
+  FastDiv vdiv;
+  int key_from_val;
+  int nviews;
+  uint32_t tile_base[kMaxViews];
 };
 
 // Element count of a pass: the host value, or the device count when it
@@ -383,7 +424,7 @@ __global__ void __launch_bounds__(Os<RB>::NT, 2) onesweep_kernel(
     const int64_t* __restrict__ n_dev, int shift, int live, const uint32_t* __restrict__ pass_hist,
     uint32_t* __restrict__ status, uint32_t* __restrict__ part_counter, int2* __restrict__ range,
     uint32_t T, const uint4* __restrict__ owner, const uint32_t* __restrict__ chunk_first,
-    int64_t n_sorted, int64_t* __restrict__ info) {
+    int64_t n_sorted, const PassViews px, int64_t* __restrict__ info) {
   using P = Os<RB>;
   constexpr int NT = P::NT, IT = P::IT, NW = P::NW, PART = P::PART, R = P::R;
   extern __shared__ __align__(16) uint32_t os_smem[];
@@ -612,15 +653,28 @@ __global__ void __launch_bounds__(Os<RB>::NT, 2) onesweep_kernel(
       set_error(info, PGB_ERR_OVERFLOW);
       continue;
     }
-    if (KEYS_OUT) keys_out[dst] = k;
-    vals_out[dst] = s_vals[j];
+    const uint32_t val = s_vals[j];
+    if (KEYS_OUT) keys_out[dst] = px.key_from_val ? fdiv(val, px.vdiv) : k;
+    vals_out[dst] = val;
     if (RANGES) {
-      if (k >= T) {
+      bool first = j == 0 || s_keys[j - 1] != k, last = j + 1 == cnt || s_keys[j + 1] != k;
+      uint32_t gt = k;
+      if (px.nviews > 0) {  // runs of one local tile hold the views in order
+        const uint32_t v = fdiv(val, px.vdiv);
+        if (v >= (uint32_t)px.nviews) {
+          set_error(info, PGB_ERR_OVERFLOW);
+          continue;
+        }
+        gt = px.tile_base[v] + k;
+        if (!first) first = fdiv(s_vals[j - 1], px.vdiv) != v;
+        if (!last) last = fdiv(s_vals[j + 1], px.vdiv) != v;
+      }
+      if (gt >= T) {
         set_error(info, PGB_ERR_OVERFLOW);
         continue;
       }
-      if (j == 0 || s_keys[j - 1] != k) atomicMin(&range[k].x, (int)dst);
-      if (j + 1 == cnt || s_keys[j + 1] != k) atomicMax(&range[k].y, (int)dst + 1);
+      if (first) atomicMin(&range[gt].x, (int)dst);
+      if (last) atomicMax(&range[gt].y, (int)dst + 1);
     }
   }
 }
@@ -640,7 +694,7 @@ static int launch_onesweep(int parts, cudaStream_t s, const uint32_t* ki, const 
                            uint32_t* ko, uint32_t* vo, int64_t cap, const int64_t* n_dev,
                            int shift, const uint32_t* hist, uint32_t* status, uint32_t* counter,
                            int2* range, uint32_t T, int64_t* info, const GenSource& src = {},
-                           int live = RB) {
+                           int live = RB, const PassViews& px = PassViews{}) {
   using P = Os<RB>;
   auto kern = onesweep_kernel<RB, KEYS_OUT, RANGES, GEN>;
   // the attribute is set on every call: the call is cheap, allowed while a
@@ -650,7 +704,7 @@ static int launch_onesweep(int parts, cudaStream_t s, const uint32_t* ki, const 
     return PGB_ERR_CUDA;
   kern<<<parts, P::NT, P::SMEM, s>>>(ki, vi, ko, vo, cap, n_dev, shift, live, hist, status,
                                      counter, range, T, src.owner, src.chunk_first, src.n_sorted,
-                                     info);
+                                     px, info);
   return PGB_OK;
 }
 
@@ -733,7 +787,10 @@ __global__ void __launch_bounds__(kStreamThreads) rect_kernel(
         const uint32_t cnt = (uint32_t)max(tiles[g], 0);
         const uint32_t w = (uint32_t)(x1 - x0);
         if ((int64_t)w * (y1 - y0) != (int64_t)cnt) set_error(info, PGB_ERR_MISMATCH);
-        const uint32_t first = tile_base + (uint32_t)y0 * (uint32_t)gx + (uint32_t)x0;
+        // tile ids local to the element's view: a batch is sorted by local
+        // tile over a view-major emission (the last pass adds the bases)
+        (void)tile_base;
+        const uint32_t first = (uint32_t)y0 * (uint32_t)gx + (uint32_t)x0;
         out = make_uint4(first, w | ((uint32_t)(y1 - y0) << 16), (uint32_t)gx, cnt);
         // runs of consecutive tile ids that emission writes for g
         runs = cnt == 0 ? 0u : (w == 0 ? 1u : cnt / w + (cnt % w ? 1u : 0u));
@@ -913,9 +970,9 @@ inline ScratchN layout_n(int64_t n) {
   L.scan_parts = (int)((n + kScanPart - 1) / kScanPart);
   size_t o = 0;
   L.counters = o; o += align256(16 * sizeof(uint32_t));
-  L.depth_hist = o; o += align256(kDepthPasses * 256 * sizeof(uint32_t));
+  L.depth_hist = o; o += align256((kDepthPasses + 1) * 256 * sizeof(uint32_t));
   L.tile_hist = o; o += align256(kTileHistWords * sizeof(uint32_t));
-  L.depth_status = o; o += align256((size_t)kDepthPasses * L.parts * 256 * sizeof(uint32_t));
+  L.depth_status = o; o += align256((size_t)(kDepthPasses + 1) * L.parts * 256 * sizeof(uint32_t));
   L.scan_status = o; o += align256((size_t)L.scan_parts * sizeof(uint32_t));
   L.zero_bytes = o;
   const size_t nb = align256((size_t)n * sizeof(uint32_t));
@@ -982,19 +1039,19 @@ inline P* at(void* base, size_t off) {
 static int tile_pass(const TilePlan& plan, int p, int parts, cudaStream_t s, const uint32_t* ki,
                      const uint32_t* vi, uint32_t* ko, uint32_t* vo, int64_t cap,
                      const int64_t* n_dev, const uint32_t* hist, uint32_t* status,
-                     uint32_t* counter, int2* range, uint32_t T, int64_t* info,
-                     const GenSource& src) {
+                     uint32_t* counter, int2* range, uint32_t T, uint32_t T_local, int64_t* info,
+                     const GenSource& src, const PassViews& px) {
   const bool last = p == plan.passes - 1;
   const int shift = plan.bits * p;
   const uint32_t* h = hist + (size_t)p * (1u << plan.bits);
   uint32_t* st = status + (size_t)p * parts * (1u << plan.bits);
-  // digit bits that some tile id has set in this pass
+  // digit bits that some (local) tile id has set in this pass
   int live = 0;
-  while (live < plan.bits && ((T - 1) >> (shift + live))) ++live;
+  while (live < plan.bits && ((T_local - 1) >> (shift + live))) ++live;
   live = live < 1 ? 1 : live;
 #define PGB_PASS(RB, KO, RG, GN) \
   launch_onesweep<RB, KO, RG, GN>(parts, s, ki, vi, ko, vo, cap, n_dev, shift, h, st, counter, \
-                                  range, T, info, src, live)
+                                  range, T, info, src, live, px)
   if (p == 0) {
     if (last) return PGB_PASS(8, false, true, true);  // one pass: at most 256 tiles
     return plan.bits == 9 ? PGB_PASS(9, true, false, true) : PGB_PASS(8, true, false, true);
@@ -1019,15 +1076,19 @@ int pgb_sort_scratch_bytes(int64_t n, int64_t k, int width, int height, size_t* 
   return PGB_OK;
 }
 
-int pgb_sort_gaussian_begin(const float* depth, const int32_t* radius,
-                            const int32_t* tiles_touched, int64_t n, int width, int height,
-                            void* scratch_n, size_t bytes_n, int64_t* info, void* stream) {
-  if (n < 0 || width <= 0 || height <= 0 || !info) return PGB_ERR_INVALID;
+}  // extern "C"
+
+// Phase one.  nviews == 0: one image, the depth order ends in v0.  A batch
+// (nviews views of n_per_view elements): the fourth depth pass writes the
+// views of its values as keys and a fifth pass sorts by view, so the order
+// (in v1) is by view, then depth, then id.
+static int sort_begin_impl(const float* depth, const int32_t* radius, const int32_t* tiles_touched,
+                           int64_t n, int nviews, int64_t n_per_view, void* scratch_n,
+                           size_t bytes_n, int64_t* info, void* stream) {
+  if (n < 0 || !info) return PGB_ERR_INVALID;
   if (n >= (int64_t)kValMask) return PGB_ERR_OVERFLOW;
   const ScratchN L = layout_n(n);
   if (!scratch_n || bytes_n < L.total) return PGB_ERR_INVALID;
-  const uint32_t T = (uint32_t)grid_x(width) * (uint32_t)grid_y(height);
-  if (T > (1u << (8 * kMaxTilePasses))) return PGB_ERR_INVALID;
   cudaStream_t s = as_stream(stream);
   if (cudaMemsetAsync(info, 0, 2 * sizeof(int64_t), s) != cudaSuccess) return PGB_ERR_CUDA;
   if (cudaMemsetAsync(scratch_n, 0, L.zero_bytes, s) != cudaSuccess) return PGB_ERR_CUDA;
@@ -1040,25 +1101,59 @@ int pgb_sort_gaussian_begin(const float* depth, const int32_t* radius,
   uint32_t* k1 = at<uint32_t>(scratch_n, L.dk1);
   uint32_t* v1 = at<uint32_t>(scratch_n, L.dv1);
   sort_prepare_kernel<<<stream_grid(n, kSortThreads, 4), kSortThreads, 0, s>>>(
-      depth, radius, tiles_touched, n, k0, v0, hist, info);
-  for (int p = 0; p < kDepthPasses; ++p) {
+      depth, radius, tiles_touched, n, k0, v0, hist, nviews, n_per_view, info);
+  PassViews px{};
+  if (nviews > 0) px.vdiv = fast_div((uint32_t)n_per_view);
+  const int passes = kDepthPasses + (nviews > 0 ? 1 : 0);
+  for (int p = 0; p < passes; ++p) {
     const uint32_t* ki = (p & 1) ? k1 : k0;
     const uint32_t* vi = (p & 1) ? v1 : v0;
     uint32_t* ko = (p & 1) ? k0 : k1;
     uint32_t* vo = (p & 1) ? v0 : v1;
     uint32_t* st = status + (size_t)p * L.parts * 256;
-    // the keys of the last pass are not needed: only the order is
-    const int rc = p == kDepthPasses - 1
-                       ? launch_onesweep<8, false, false>(L.parts, s, ki, vi, ko, vo, n, nullptr,
-                                                          8 * p, hist + 256 * p, st, counters + p,
-                                                          nullptr, 0, info)
-                       : launch_onesweep<8, true, false>(L.parts, s, ki, vi, ko, vo, n, nullptr,
+    int rc;
+    if (p == kViewPass) {  // by view (keys: the views the previous pass wrote)
+      int live = 1;
+      while ((1 << live) < nviews) ++live;
+      rc = launch_onesweep<8, false, false>(L.parts, s, ki, vi, ko, vo, n, nullptr, 0,
+                                            hist + 256 * p, st, counters + 8, nullptr, 0, info,
+                                            GenSource{}, live);
+    } else if (p == kDepthPasses - 1) {
+      // the last depth pass: for a batch it writes the views as the next
+      // pass's keys; for one image only the order is needed
+      px.key_from_val = 1;
+      rc = nviews > 0 ? launch_onesweep<8, true, false>(L.parts, s, ki, vi, ko, vo, n, nullptr,
+                                                        8 * p, hist + 256 * p, st, counters + p,
+                                                        nullptr, 0, info, GenSource{}, 8, px)
+                      : launch_onesweep<8, false, false>(L.parts, s, ki, vi, ko, vo, n, nullptr,
                                                          8 * p, hist + 256 * p, st, counters + p,
                                                          nullptr, 0, info);
+    } else {
+      rc = launch_onesweep<8, true, false>(L.parts, s, ki, vi, ko, vo, n, nullptr, 8 * p,
+                                           hist + 256 * p, st, counters + p, nullptr, 0, info);
+    }
     if (rc != PGB_OK) return rc;
   }
-  // four passes: the depth order ends in v0
   return launch_status();
+}
+
+extern "C" {
+
+int pgb_sort_gaussian_begin(const float* depth, const int32_t* radius,
+                            const int32_t* tiles_touched, int64_t n, int width, int height,
+                            void* scratch_n, size_t bytes_n, int64_t* info, void* stream) {
+  if (width <= 0 || height <= 0) return PGB_ERR_INVALID;
+  const uint64_t T = (uint64_t)grid_x(width) * (uint64_t)grid_y(height);
+  if (T > (1u << (8 * kMaxTilePasses))) return PGB_ERR_INVALID;
+  return sort_begin_impl(depth, radius, tiles_touched, n, 0, 0, scratch_n, bytes_n, info, stream);
+}
+
+int pgb_sort_gaussian_begin_views(const float* depth, const int32_t* radius,
+                                  const int32_t* tiles_touched, int64_t n_per_view, int nviews,
+                                  void* scratch_n, size_t bytes_n, int64_t* info, void* stream) {
+  if (nviews < 1 || nviews > kMaxViews || n_per_view < 0) return PGB_ERR_INVALID;
+  return sort_begin_impl(depth, radius, tiles_touched, n_per_view * nviews, nviews, n_per_view,
+                         scratch_n, bytes_n, info, stream);
 }
 
 }  // extern "C"
@@ -1074,7 +1169,14 @@ static int sort_finish_impl(const float* uv, const int32_t* radius, const int32_
   if (n < 0 || k < 0 || !info || !tile_range_out) return PGB_ERR_INVALID;
   if (k >= (int64_t)kValMask) return PGB_ERR_OVERFLOW;
   const ScratchN LN = layout_n(n);
-  const TilePlan plan = tile_plan(T);
+  // a batch sorts local tile ids: the plan is that of the largest view
+  uint32_t T_local = T;
+  if (vt.nviews > 0) {
+    T_local = 1;
+    for (int v = 0; v < vt.nviews; ++v)
+      T_local = std::max<uint32_t>(T_local, (uint32_t)grid_x(vt.w[v]) * (uint32_t)grid_y(vt.h[v]));
+  }
+  const TilePlan plan = tile_plan(T_local);
   const ScratchK LK = layout_k(k, plan.passes);
   if (!scratch_n || bytes_n < LN.total) return PGB_ERR_INVALID;
   if (k > 0 && (!scratch_k || bytes_k < LK.total || !ids_out)) return PGB_ERR_INVALID;
@@ -1094,7 +1196,8 @@ static int sort_finish_impl(const float* uv, const int32_t* radius, const int32_
   const int64_t* k_dev = device_k ? info : nullptr;
   uint32_t* counters = at<uint32_t>(scratch_n, LN.counters);
   uint32_t* thist = at<uint32_t>(scratch_n, LN.tile_hist);
-  const uint32_t* order = at<uint32_t>(scratch_n, LN.dv0);
+  // the depth order (view-major for a batch: begin_views ends in v1)
+  const uint32_t* order = at<uint32_t>(scratch_n, vt.nviews > 0 ? LN.dv1 : LN.dv0);
   uint32_t* bufk[2] = {at<uint32_t>(scratch_k, LK.tk0), at<uint32_t>(scratch_k, LK.tk1)};
   uint32_t* bufv[2] = {at<uint32_t>(scratch_k, LK.tv0), at<uint32_t>(scratch_k, LK.tv1)};
   uint32_t* status = at<uint32_t>(scratch_k, LK.status);
@@ -1111,12 +1214,18 @@ static int sort_finish_impl(const float* uv, const int32_t* radius, const int32_
   src.owner = owner;
   src.chunk_first = chunk_first;
   src.n_sorted = n;
+  PassViews px{};
+  if (vt.nviews > 0) {
+    px.vdiv = fast_div((uint32_t)vt.n_per_view);
+    px.nviews = vt.nviews;
+    for (int v = 0; v < vt.nviews; ++v) px.tile_base[v] = (uint32_t)vt.tile_base[v];
+  }
   int cur = 0;
   for (int p = 0; p < plan.passes; ++p) {
     const bool last = p == plan.passes - 1;
     uint32_t* vo = last ? reinterpret_cast<uint32_t*>(ids_out) : bufv[cur ^ 1];
     const int rc = tile_pass(plan, p, LK.parts, s, bufk[cur], bufv[cur], bufk[cur ^ 1], vo, k, k_dev,
-                             thist, status, counters + 5 + p, range, T, info, src);
+                             thist, status, counters + 5 + p, range, T, T_local, info, src, px);
     if (rc != PGB_OK) return rc;
     cur ^= 1;
   }

@@ -40,22 +40,27 @@ def _tiles(W, H):
 def sort_views(uv, depth, radius, tiles_touched, sizes, n_per_view, capacity=None):
     """Tile lists of V views at once: ids [K] (element ids v*N + g) and
     tile_range [sum of tiles, 2] over the views' concatenated tile space.
+    The pairs are sorted by view-local tile over a view-major emission, so
+    ids holds, for each local tile, the views' lists one after another;
+    tile_range[base_v + t] selects view v's list of tile t (depth, then id).
     With ``capacity`` K stays on the device (ids has ``capacity`` entries)
     and nothing synchronises, as in :func:`ops.sort_gaussian`."""
     W0, H0 = sizes[0]
     h = ops.sort_gaussian_begin(uv, depth, W0, H0, radius, tiles_touched,
-                                read_count=capacity is None)
+                                read_count=capacity is None, views=(len(sizes), n_per_view))
     K = h.count() if capacity is None else int(capacity)
     dev = uv.device
     T = sum(_tiles(W, H) for W, H in sizes)
-    # the K-sized scratch depends on the tile count: a 16T x 16 "image" has T tiles
-    _, bk = ops._sort_scratch(h.n, K, 16 * T, 16)
+    # the batch sorts local tile ids: its K-sized scratch is that of the
+    # largest view's tile count (a 16T x 16 "image" has T tiles)
+    T_local = max(_tiles(W, H) for W, H in sizes)
+    _, bk = ops._sort_scratch(h.n, K, 16 * T_local, 16)
     scratch_k = torch.empty(max(bk, 1), dtype=torch.uint8, device=dev)
     ids = torch.empty(max(K, 1), dtype=torch.int32, device=dev)[:K]
     rng = torch.empty(T, 2, dtype=torch.int32, device=dev)
     entry = "pgb_sort_gaussian_finish_views" if capacity is None else \
         "pgb_sort_gaussian_finish_views_capacity"
-    with _timed("sort_finish", dev, (3 + ops._tile_passes(T)) if (K and h.n) else
+    with _timed("sort_finish", dev, (3 + ops._tile_passes(T_local)) if (K and h.n) else
                 (0 if capacity is None else 1)):
         call(entry, _ptr(h.uv), _ptr(h.radius), _ptr(h.tiles), n_per_view, _sizes_array(sizes),
              len(sizes), K, _ptr(h.scratch_n), h.bn, _ptr(scratch_k), bk, _ptr(h.info),

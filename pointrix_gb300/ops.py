@@ -487,9 +487,13 @@ def _fold_status(word: torch.Tensor, dev):
     torch.maximum(w, word, out=w)
 
 
-def sort_gaussian_begin(uv, depth, W, H, radius, tiles_touched, read_count=True) -> SortHandle:
+def sort_gaussian_begin(uv, depth, W, H, radius, tiles_touched, read_count=True,
+                        views=None) -> SortHandle:
     """Phase one of :func:`sort_gaussian` without blocking the host: sorts the
-    Gaussians by depth and (``read_count``) starts the read-back of K."""
+    Gaussians by depth and (``read_count``) starts the read-back of K.
+    ``views`` = (nviews, n_per_view): the elements are a batch of views
+    (element v * n_per_view + g), sorted by view, then depth, then id, for
+    the batch's tile passes (``multiview.sort_views``)."""
     _need(uv, "uv", ndim=2, last=2)
     _need(depth, "depth")
     _need(radius, "radius", dtype=torch.int32)
@@ -507,9 +511,17 @@ def sort_gaussian_begin(uv, depth, W, H, radius, tiles_touched, read_count=True)
     h.bn, _ = _sort_scratch(n, 0, W, H)
     h.scratch_n = torch.empty(max(h.bn, 1), dtype=torch.uint8, device=h.dev)
     h.info = torch.empty(2, dtype=torch.int64, device=h.dev)
-    with _timed("sort_begin", h.dev, 5 if n else 0):
-        call("pgb_sort_gaussian_begin", _ptr(h.depth), _ptr(h.radius), _ptr(h.tiles), n, W, H,
-             _ptr(h.scratch_n), h.bn, _ptr(h.info), h.stream.cuda_stream)
+    if views is None:
+        with _timed("sort_begin", h.dev, 5 if n else 0):
+            call("pgb_sort_gaussian_begin", _ptr(h.depth), _ptr(h.radius), _ptr(h.tiles), n, W, H,
+                 _ptr(h.scratch_n), h.bn, _ptr(h.info), h.stream.cuda_stream)
+    else:
+        nviews, n_per_view = int(views[0]), int(views[1])
+        if nviews * n_per_view != n:
+            raise ValueError(f"sort_gaussian_begin: {nviews} views of {n_per_view} is not N = {n}")
+        with _timed("sort_begin", h.dev, 6 if n else 0):
+            call("pgb_sort_gaussian_begin_views", _ptr(h.depth), _ptr(h.radius), _ptr(h.tiles),
+                 n_per_view, nviews, _ptr(h.scratch_n), h.bn, _ptr(h.info), h.stream.cuda_stream)
     h.host = h.event = None
     if read_count:
         h.host = torch.empty(2, dtype=torch.int64, pin_memory=True)

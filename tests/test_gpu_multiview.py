@@ -89,3 +89,39 @@ def test_batched_views_capacity_mode_in_a_graph():
         for a, b in zip(ref, out):
             assert torch.equal(a, b)
     ops.check_device_status()
+
+
+@pytest.mark.parametrize("capacity_extra", [None, 4096])
+def test_batched_sort_lists_match_per_view_sorts(capacity_extra):
+    """The batch sorts view-local tile ids over a view-major emission: for
+    every view v and tile t, tile_range[base_v + t] must select exactly the
+    list that sorting view v alone gives for t (element ids offset by v N)."""
+    cams = _cams()
+    pos, sc, q, op, shs = _leaves()
+    n = pos.shape[0]
+    uvs, depths, radii, tiles, per = [], [], [], [], []
+    with torch.no_grad():
+        for cam in cams:
+            extr = cam.extr[:3, :]
+            uv, depth = ops.project_point(pos, cam.intr, extr, cam.W, cam.H)
+            vis = depth != 0
+            cov = ops.compute_cov3d(sc, q, vis)
+            _, radius, nt = ops.ewa_project(pos, cov, cam.intr, extr, uv, cam.W, cam.H, vis)
+            uvs.append(uv); depths.append(depth); radii.append(radius); tiles.append(nt)
+            per.append(ops.sort_gaussian(uv, depth, cam.W, cam.H, radius, nt))
+    K = sum(int(i.numel()) for i, _ in per)
+    cap = None if capacity_extra is None else K + capacity_extra
+    sizes = [(c.W, c.H) for c in cams]
+    ids, rng = multiview.sort_views(torch.cat(uvs), torch.cat(depths), torch.cat(radii),
+                                    torch.cat(tiles), sizes, n, capacity=cap)
+    ids, rng = ids.cpu().long(), rng.cpu().long()
+    assert int((rng[:, 1] - rng[:, 0]).sum()) == K
+    base = 0
+    for v, (ids_v, rng_v) in enumerate(per):
+        T_v = rng_v.shape[0]
+        got = torch.cat([ids[rng[base + t, 0]:rng[base + t, 1]] for t in range(T_v)]) - v * n
+        assert torch.equal(got, ids_v.cpu().long()), v
+        empty = (rng_v[:, 1] == rng_v[:, 0]).cpu()
+        assert bool((rng[base:base + T_v][empty] == 0).all())
+        base += T_v
+    ops.check_device_status()
