@@ -171,8 +171,13 @@ class CameraParams:
         self.intr = cam.intr.clone().to(device).requires_grad_(grad)
         self.bottom = torch.tensor([[0.0, 0, 0, 1]], device=device)
 
-    def pose(self):
-        """(world->camera [4,4], camera centre [3]) from the 6-DoF leaves."""
+    def pose(self, fused=True):
+        """(world->camera [4,4], camera centre [3]) from the 6-DoF leaves: one
+        library kernel each way (``fused.camera_pose``), or the torch
+        composition with the same arithmetic."""
+        if fused and self.q.is_cuda:
+            from pointrix_gb300 import fused as FU
+            return FU.camera_pose(self.q, self.t)
         R = quat_to_rot(self.q)
         E = torch.cat([torch.cat([R, self.t[:, None]], 1), self.bottom], 0)
         return E, -(R.T @ self.t)
@@ -196,7 +201,7 @@ def training_step(renderer, scene, camp, target, WL, optimizer=None, fused=True)
     else:
         pos, sc, q, op, shs = scene.activated()
         normal = WL.normals_from_scene(sc, q)
-    E, center = camp.pose()
+    E, center = camp.pose(fused)
     out = renderer.render_iter(camp.H, camp.W, E, camp.intr, center,
                                pos, op, sc, q, shs, extra_features={"normal": normal})
     if fused:

@@ -298,6 +298,18 @@ int pgb_alpha_blending_backward_views_with_batch(
     float* d_conic, float* d_opacity, float* d_feature, int64_t* info, void* stream, int batch);
 int pgb_blend_batches(int backward, int32_t* out);
 
+/* Camera pose (the camera model around the path,
+ * pointrix/utils/pose.py:40-84): world_to_camera [4,4] row-major and the
+ * camera centre [3] from a wxyz quaternion [4] (normalised) and a
+ * translation [3]; the backward takes d_world_to_camera and d_centre (either
+ * may be NULL) and writes d_quat [4], d_translation [3].  One single-block
+ * launch each way. */
+int pgb_camera_pose_forward(const float* quat, const float* translation, float* world_to_camera,
+                            float* centre, void* stream);
+int pgb_camera_pose_backward(const float* quat, const float* translation,
+                             const float* d_world_to_camera, const float* d_centre, float* d_quat,
+                             float* d_translation, void* stream);
+
 /* Feature pieces (no counterpart in the reference): the single-view blend
  * with the [N,C] feature given as npieces [N,w_p] row-major device tensors
  * (pieces / widths are HOST arrays; sum of widths = C <= 26), e.g. rgb,

@@ -33,6 +33,8 @@ SIGNATURES = {
     "pgb_sort_scratch_bytes": [i64, i64, i32, i32, C.POINTER(szt), C.POINTER(szt)],
     "pgb_sort_gaussian_begin": [vp, vp, vp, i64, i32, i32, vp, szt, vp, vp],
     "pgb_sort_gaussian_begin_views": [vp, vp, vp, i64, i32, vp, szt, vp, vp],
+    "pgb_camera_pose_forward": [vp, vp, vp, vp, vp],
+    "pgb_camera_pose_backward": [vp, vp, vp, vp, vp, vp, vp],
     "pgb_sort_gaussian_finish": [vp, vp, vp, i64, i32, i32, i64, vp, szt, vp, szt, vp, vp, vp, vp],
     "pgb_sort_gaussian_finish_capacity": [vp, vp, vp, i64, i32, i32, i64, vp, szt, vp, szt, vp, vp,
                                           vp, vp],

@@ -29,7 +29,7 @@ from ._lib import call
 from .ops import EXTENT_DEFAULT, NEAREST_DEFAULT, _c, _extr34, _intr4, _ptr, _stream, _timed
 
 __all__ = ["gaussian_activations", "sh_rgb", "sh_rgb_views", "sh_rgb_supported", "l1_l2_loss",
-           "ssim", "preprocess"]
+           "ssim", "preprocess", "camera_pose"]
 
 
 def _aligned(t: torch.Tensor) -> bool:
@@ -352,3 +352,44 @@ def preprocess(position, scaling, rotation, intr, extr, W, H, nearest=NEAREST_DE
             raise ValueError(f"{name} must be a CUDA float32 tensor")
     return _Preprocess.apply(_c(position), _c(scaling), _c16(rotation), _intr4(intr), _extr34(extr),
                              int(W), int(H), float(nearest), float(extent))
+
+
+# ---------------------------------------------------------------------------
+# camera pose of a differentiable camera
+# ---------------------------------------------------------------------------
+class _CameraPose(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, quat, translation):
+        dev = quat.device
+        E = torch.empty(4, 4, dtype=torch.float32, device=dev)
+        centre = torch.empty(3, dtype=torch.float32, device=dev)
+        with _timed("camera_pose_fwd", dev, 1):
+            call("pgb_camera_pose_forward", _ptr(quat), _ptr(translation), _ptr(E), _ptr(centre),
+                 _stream(dev))
+        ctx.save_for_backward(quat, translation)
+        return E, centre
+
+    @staticmethod
+    def backward(ctx, dE, dcentre):
+        quat, translation = ctx.saved_tensors
+        dev = quat.device
+        dq = torch.empty(4, dtype=torch.float32, device=dev)
+        dt = torch.empty(3, dtype=torch.float32, device=dev)
+        dE = None if dE is None else dE.contiguous()
+        dcentre = None if dcentre is None else dcentre.contiguous()
+        with _timed("camera_pose_bwd", dev, 1):
+            call("pgb_camera_pose_backward", _ptr(quat), _ptr(translation), _ptr(dE),
+                 _ptr(dcentre), _ptr(dq), _ptr(dt), _stream(dev))
+        return dq, dt
+
+
+def camera_pose(quat, translation):
+    """(world->camera [4,4], camera centre [3]) of a camera stored as a wxyz
+    quaternion [4] (normalised here) and a translation [3]: the rotation of
+    ``pointrix/utils/pose.py:40-84`` applied to q / |q|, E = [R t; 0 0 0 1],
+    centre = -R^T t; one kernel each way (the torch composition is a dozen
+    kernels forward and as many backward)."""
+    for name, t, k in (("quat", quat, 4), ("translation", translation, 3)):
+        if t.numel() != k or not (t.is_cuda and t.dtype == torch.float32):
+            raise ValueError(f"{name} must be a CUDA float32 tensor of {k} values")
+    return _CameraPose.apply(quat.reshape(4).contiguous(), translation.reshape(3).contiguous())

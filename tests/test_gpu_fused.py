@@ -274,3 +274,35 @@ def test_sh_rgb_views_matches_per_view():
     for x, y in zip(a, b):
         assert rel(x.grad, y.grad) < 1e-5
     ops.check_device_status()
+
+
+def test_camera_pose_matches_torch_composition():
+    """fused.camera_pose against the torch composition (quaternion
+    normalisation, homogeneous rotation, [R t; 0 1], -R^T t): values and the
+    gradients of both outputs to 1e-5."""
+    g = torch.Generator().manual_seed(9)
+    q0 = torch.randn(4, generator=g) * 2.0
+    t0 = torch.randn(3, generator=g) * 3.0
+    dE = torch.randn(4, 4, generator=g).to(DEV)
+    dc = torch.randn(3, generator=g).to(DEV)
+    q, t = q0.to(DEV).requires_grad_(True), t0.to(DEV).requires_grad_(True)
+    E, c = fused.camera_pose(q, t)
+    ((E * dE).sum() + (c * dc).sum()).backward()
+    qr, tr = q0.to(DEV).requires_grad_(True), t0.to(DEV).requires_grad_(True)
+    R = WL.rotation_from_unit_quat(qr / qr.norm())
+    Er = torch.cat([torch.cat([R, tr[:, None]], 1), torch.tensor([[0.0, 0, 0, 1]], device=DEV)], 0)
+    cr = -(R.T @ tr)
+    ((Er * dE).sum() + (cr * dc).sum()).backward()
+    assert torch.allclose(E, Er, atol=1e-6) and torch.allclose(c, cr, atol=1e-5)
+    assert torch.allclose(q.grad, qr.grad, rtol=1e-5, atol=1e-5)
+    assert torch.allclose(t.grad, tr.grad, rtol=1e-5, atol=1e-5)
+    # one output unused: its gradient arrives as None
+    q2, t2 = q0.to(DEV).requires_grad_(True), t0.to(DEV).requires_grad_(True)
+    E2, _ = fused.camera_pose(q2, t2)
+    (E2 * dE).sum().backward()
+    q3, t3 = q0.to(DEV).requires_grad_(True), t0.to(DEV).requires_grad_(True)
+    R3 = WL.rotation_from_unit_quat(q3 / q3.norm())
+    E3 = torch.cat([torch.cat([R3, t3[:, None]], 1), torch.tensor([[0.0, 0, 0, 1]], device=DEV)], 0)
+    (E3 * dE).sum().backward()
+    assert torch.allclose(q2.grad, q3.grad, rtol=1e-5, atol=1e-5)
+    assert torch.allclose(t2.grad, t3.grad, rtol=1e-5, atol=1e-5)
