@@ -13,8 +13,8 @@
 // last-contributor count.
 //
 // GB300 design:
-//  * pack: one pass writes a record per Gaussian (u, v, a, b, c, o, tau,
-//    thr, f_0..f_{C-1}, zero padding: 48 to 144 bytes) so that a splat is
+//  * pack: one pass writes a record per Gaussian (u, v, scaled conic, o,
+//    tau, thr, f_0..f_{C-1}, zero padding: 48 to 144 bytes) so that a splat is
 //    one 16-byte aligned contiguous block read with 16-byte loads;
 //  * forward/backward: one CTA of 128 threads per tile, two pixels per
 //    thread; each warp owns an 8x8 pixel box and, per batch, culls the
@@ -27,8 +27,10 @@
 //    is bounded, and on expiry the CTA records PGB_ERR_TIMEOUT, drains its
 //    own copies (bounded again) and returns.  Backward: the same stage
 //    filled with 16-byte cp.async copies;
-//  * the alpha test is a comparison of the exponent with a per-splat
-//    threshold -ln(255 o), before the exponential;
+//  * the record's conic is pre-scaled by -log2(e) / 2, so a pair's power
+//    comes out as a base-2 exponent for one ex2; the alpha test is a
+//    comparison of that exponent with a per-splat threshold -log2(255 o),
+//    before the exponential;
 //  * forward early exit per CTA (__syncthreads_count) and per warp;
 //  * backward: per-Gaussian gradients are summed across the warp with a
 //    reduce-scatter butterfly (16 shuffles for 16 values instead of 80),
@@ -84,17 +86,31 @@ __device__ inline void set_info(int64_t* info, int code) {
   if (info) atomicCAS(reinterpret_cast<unsigned long long*>(info), 0ull, (unsigned long long)code);
 }
 
-// Power of one (pixel, splat) pair, -(a dx^2 + 2 b dx dy + c dy^2) / 2 =
-// -(dx g0 + dy g1) / 2 with g0 = a dx + b dy, g1 = b dx + c dy (the
-// gradient of the power with respect to uv is -(g0, g1), which the backward
-// reuses).  Written with explicit rounding intrinsics so that the forward and
-// the backward take identical skip/stop decisions whatever the compiler
-// contracts elsewhere.
-__device__ __forceinline__ float splat_power(float a, float b, float c, float dx, float dy,
-                                             float& g0, float& g1) {
-  g0 = __fmaf_rn(a, dx, __fmul_rn(b, dy));
-  g1 = __fmaf_rn(b, dx, __fmul_rn(c, dy));
-  return __fmul_rn(-0.5f, __fmaf_rn(dx, g0, __fmul_rn(dy, g1)));
+// Records hold the conic scaled by K = -log2(e) / 2 (A = K a, B = K b,
+// C = K c), so that a pair's power comes out as a base-2 exponent:
+// p2 = log2(e) power = dx g0 + dy g1 with g0 = A dx + B dy, g1 = B dx + C dy,
+// and e^power = 2^p2 is one ex2.  The gradient of the power with respect to
+// uv is -(g0, g1) / K, which the backward accumulates as moments and the
+// unpack pass rescales once per Gaussian.
+constexpr float kConicScale = -0.72134752044448170f;    // -log2(e) / 2
+constexpr float kInvConicScale = -1.38629436111989061f;  // 1 / kConicScale = -2 ln 2
+
+// Base-2 power of one (pixel, splat) pair from the scaled conic, written
+// with explicit rounding intrinsics so that the forward and the backward
+// take identical skip/stop decisions whatever the compiler contracts
+// elsewhere.
+__device__ __forceinline__ float splat_power2(float A, float B, float C, float dx, float dy,
+                                              float& g0, float& g1) {
+  g0 = __fmaf_rn(A, dx, __fmul_rn(B, dy));
+  g1 = __fmaf_rn(B, dx, __fmul_rn(C, dy));
+  return __fmaf_rn(dx, g0, __fmul_rn(dy, g1));
+}
+
+// 2^x by the special-function unit (the exponential of the pair's alpha).
+__device__ __forceinline__ float ex2_approx(float x) {
+  float y;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
 }
 
 // Issue the bulk copies of one batch of B records: thread t fetches the
@@ -157,7 +173,8 @@ __device__ inline void stage_batch(const float* __restrict__ records,
 }
 
 // ------------------------------------------------------------------ pack
-// Record of one splat: u, v, a, b, c, o, tau, thr, f_0..f_{C-1}, zero
+// Record of one splat: u, v, K a, K b, K c (the conic scaled by
+// K = -log2(e) / 2), o, tau, thr = -log2(255 o), f_0..f_{C-1}, zero
 // padding to a multiple of 4 floats.  tau bounds the splat's support: alpha >= 1/255
 // requires Q(d) = a dx^2 + 2 b dx dy + c dy^2 <= 2 ln(255 o); tau is that
 // level plus a small margin, -1 when o < 1/255 (the splat never passes the
@@ -216,9 +233,9 @@ __global__ void pack_kernel(const float* __restrict__ uv, const float* __restric
     r[1] = uv[2 * i + 1];
     const float a = conic[3 * i], b = conic[3 * i + 1], c = conic[3 * i + 2];
     const float o = opacity[i];
-    r[2] = a;
-    r[3] = b;
-    r[4] = c;
+    r[2] = kConicScale * a;  // scaled: the power comes out base 2
+    r[3] = kConicScale * b;
+    r[4] = kConicScale * c;
     r[5] = o;
     float tau;
     if (!(isfinite(r[0]) && isfinite(r[1]) && isfinite(o)))
@@ -230,10 +247,10 @@ __global__ void pack_kernel(const float* __restrict__ uv, const float* __restric
     else
       tau = __int_as_float(0x7f800000);  // +inf: never culled
     r[6] = tau;
-    // alpha >= 1/255 <=> power >= -ln(255 o): the per-pair test before the
+    // alpha >= 1/255 <=> p2 >= -log2(255 o): the per-pair test before the
     // exponential (never passes for o <= 0; a NaN opacity keeps NaN, which
     // no comparison rejects, as the alpha test did not)
-    r[7] = o > 0.f ? -logf(255.0f * o) : __int_as_float(0x7f800000);
+    r[7] = o > 0.f ? -log2f(255.0f * o) : __int_as_float(0x7f800000);
 #pragma unroll
     for (int k = 0; k < RF - kRecFeat; ++k)
       r[kRecFeat + k] = k < C ? fc.src[k][i * fc.stride[k]] : 0.f;
@@ -264,7 +281,9 @@ template <int BW, int BH>
 __device__ __forceinline__ bool splat_may_touch_box(const float* rec, float x0, float y0) {
   const float tau = rec[6];
   if (!(tau < 3.0e38f)) return true;
-  const float u = rec[0], v = rec[1], a = rec[2], b = rec[3], c = rec[4];
+  // the record's conic is scaled by kConicScale
+  const float u = rec[0], v = rec[1], a = rec[2] * kInvConicScale, b = rec[3] * kInvConicScale,
+              c = rec[4] * kInvConicScale;
   const float dx0 = u - (x0 + (float)(BW - 1)), dx1 = u - x0;
   const float dy0 = v - (y0 + (float)(BH - 1)), dy1 = v - y0;
   if (dx0 <= 0.f && dx1 >= 0.f && dy0 <= 0.f && dy1 >= 0.f) return tau >= 0.f;
@@ -397,9 +416,9 @@ __global__ void __launch_bounds__(kFwdThreads) blend_fwd_kernel(
           live = true;
           const float dy = __fsub_rn(r0.y, pyf[q]);
           float g0, g1;
-          const float power = splat_power(r0.z, r0.w, r1.x, dx, dy, g0, g1);
-          if (power > 0.f || power < r1.w) continue;  // alpha < 1/255: no exp needed
-          const float alpha = fminf(0.99f, __fmul_rn(r1.y, __expf(power)));
+          const float p2 = splat_power2(r0.z, r0.w, r1.x, dx, dy, g0, g1);
+          if (p2 > 0.f || p2 < r1.w) continue;  // alpha < 1/255: no exp needed
+          const float alpha = fminf(0.99f, __fmul_rn(r1.y, ex2_approx(p2)));
           const float test_T = __fmul_rn(T[q], __fsub_rn(1.0f, alpha));
           if (test_T < 1e-4f) {
             done[q] = true;
@@ -490,10 +509,10 @@ struct BwdPixel {
 
 // Adds one pixel's contribution to the splat's gradient moments v:
 // sum g0 dp, sum g1 dp, sum dx^2 dp, sum dx dy dp, sum dy^2 dp (dp the
-// gradient of the power), sum G dalpha (the opacity gradient), then the
-// feature gradients; the unpack pass turns the moments into the uv and
-// conic gradients (-v0, -v1; -v2 / 2, -v3, -v4 / 2).  Replays the forward's
-// skip decisions exactly.
+// gradient of the natural-base power; g0, g1 from the scaled conic), sum
+// G dalpha (the opacity gradient), then the feature gradients; the unpack
+// pass turns the moments into the uv and conic gradients (-(v0, v1) / K;
+// -v2 / 2, -v3, -v4 / 2).  Replays the forward's skip decisions exactly.
 template <int NC, int GR>
 __device__ __forceinline__ bool bwd_pixel(BwdPixel<NC>& P, int j, const float* rec,
                                           float (&v)[GR]) {
@@ -502,9 +521,9 @@ __device__ __forceinline__ bool bwd_pixel(BwdPixel<NC>& P, int j, const float* r
   const float4 r1 = *reinterpret_cast<const float4*>(rec + 4);
   const float dx = __fsub_rn(r0.x, P.pxf), dy = __fsub_rn(r0.y, P.pyf);
   float g0, g1;
-  const float power = splat_power(r0.z, r0.w, r1.x, dx, dy, g0, g1);
-  if (power > 0.f || power < r1.w) return false;  // the forward's skip test
-  const float G = __expf(power);
+  const float p2 = splat_power2(r0.z, r0.w, r1.x, dx, dy, g0, g1);
+  if (p2 > 0.f || p2 < r1.w) return false;  // the forward's skip test
+  const float G = ex2_approx(p2);
   const float araw = __fmul_rn(r1.y, G);
   const float alpha = fminf(0.99f, araw);
   const float om = __fsub_rn(1.0f, alpha);
@@ -684,8 +703,9 @@ __global__ void unpack_kernel(const float* __restrict__ g, int64_t n, int C,
       const float4 x = s[q];
       r[4 * q] = x.x; r[4 * q + 1] = x.y; r[4 * q + 2] = x.z; r[4 * q + 3] = x.w;
     }
-    // gradient moments -> uv and conic gradients
-    reinterpret_cast<float2*>(d_uv)[i] = make_float2(-r[0], -r[1]);
+    // gradient moments -> uv and conic gradients (g0, g1 carried the scale K)
+    reinterpret_cast<float2*>(d_uv)[i] =
+        make_float2(-r[0] * kInvConicScale, -r[1] * kInvConicScale);
     d_conic[3 * i] = -0.5f * r[2];
     d_conic[3 * i + 1] = -r[3];
     d_conic[3 * i + 2] = -0.5f * r[4];
