@@ -95,15 +95,26 @@ __device__ inline void set_info(int64_t* info, int code) {
 constexpr float kConicScale = -0.72134752044448170f;    // -log2(e) / 2
 constexpr float kInvConicScale = -1.38629436111989061f;  // 1 / kConicScale = -2 ln 2
 
-// Base-2 power of one (pixel, splat) pair from the scaled conic, written
-// with explicit rounding intrinsics so that the forward and the backward
-// take identical skip/stop decisions whatever the compiler contracts
-// elsewhere.
-__device__ __forceinline__ float splat_power2(float A, float B, float C, float dx, float dy,
-                                              float& g0, float& g1) {
-  g0 = __fmaf_rn(A, dx, __fmul_rn(B, dy));
-  g1 = __fmaf_rn(B, dx, __fmul_rn(C, dy));
-  return __fmaf_rn(dx, g0, __fmul_rn(dy, g1));
+// Base-2 power of (pixel, splat) pairs from the scaled conic.  A thread's
+// pixels share one column, so dx is fixed per (thread, splat): the
+// x-only terms Adx = A dx, Bdx = B dx and A dx^2 are formed once per splat,
+// and each pixel's p2 = A dx^2 + dy (2 Bdx + C dy) is two FMAs.  Written with
+// explicit rounding intrinsics so that the forward and the backward take
+// identical skip/stop decisions whatever the compiler contracts elsewhere.
+struct SplatX {
+  float Adx, Bdx, Adx2;
+};
+
+__device__ __forceinline__ SplatX splat_x(float A, float B, float dx) {
+  SplatX sx;
+  sx.Adx = __fmul_rn(A, dx);
+  sx.Bdx = __fmul_rn(B, dx);
+  sx.Adx2 = __fmul_rn(sx.Adx, dx);
+  return sx;
+}
+
+__device__ __forceinline__ float splat_power2(const SplatX& sx, float C, float dy) {
+  return __fmaf_rn(dy, __fmaf_rn(C, dy, __fadd_rn(sx.Bdx, sx.Bdx)), sx.Adx2);
 }
 
 // 2^x by the special-function unit (the exponential of the pair's alpha).
@@ -409,14 +420,14 @@ __global__ void __launch_bounds__(kFwdThreads) blend_fwd_kernel(
         const float4 r0 = *reinterpret_cast<const float4*>(rec);
         const float4 r1 = *reinterpret_cast<const float4*>(rec + 4);
         const float dx = __fsub_rn(r0.x, pxf);
+        const SplatX sx = splat_x(r0.z, r0.w, dx);
         bool live = false;
 #pragma unroll
         for (int q = 0; q < kFwdPix; ++q) {
           if (done[q]) continue;
           live = true;
           const float dy = __fsub_rn(r0.y, pyf[q]);
-          float g0, g1;
-          const float p2 = splat_power2(r0.z, r0.w, r1.x, dx, dy, g0, g1);
+          const float p2 = splat_power2(sx, r1.x, dy);
           if (p2 > 0.f || p2 < r1.w) continue;  // alpha < 1/255: no exp needed
           const float alpha = fminf(0.99f, __fmul_rn(r1.y, ex2_approx(p2)));
           const float test_T = __fmul_rn(T[q], __fsub_rn(1.0f, alpha));
@@ -515,14 +526,14 @@ struct BwdPixel {
 // -v2 / 2, -v3, -v4 / 2).  Replays the forward's skip decisions exactly.
 template <int NC, int GR>
 __device__ __forceinline__ bool bwd_pixel(BwdPixel<NC>& P, int j, const float* rec,
-                                          float (&v)[GR]) {
+                                          const SplatX& sx, float dx, float (&v)[GR]) {
   if (j >= P.nc) return false;
   const float4 r0 = *reinterpret_cast<const float4*>(rec);
   const float4 r1 = *reinterpret_cast<const float4*>(rec + 4);
-  const float dx = __fsub_rn(r0.x, P.pxf), dy = __fsub_rn(r0.y, P.pyf);
-  float g0, g1;
-  const float p2 = splat_power2(r0.z, r0.w, r1.x, dx, dy, g0, g1);
+  const float dy = __fsub_rn(r0.y, P.pyf);
+  const float p2 = splat_power2(sx, r1.x, dy);
   if (p2 > 0.f || p2 < r1.w) return false;  // the forward's skip test
+  const float g0 = __fmaf_rn(r0.w, dy, sx.Adx), g1 = __fmaf_rn(r1.x, dy, sx.Bdx);
   const float G = ex2_approx(p2);
   const float araw = __fmul_rn(r1.y, G);
   const float alpha = fminf(0.99f, araw);
@@ -653,8 +664,11 @@ __global__ void __launch_bounds__(256 / PX) blend_bwd_kernel(
 #pragma unroll
         for (int q = 0; q < GR; ++q) v[q] = 0.f;
         bool contrib = false;
+        const float4 r0 = *reinterpret_cast<const float4*>(rec);
+        const float dx = __fsub_rn(r0.x, P[0].pxf);  // the thread's pixels share a column
+        const SplatX sx = splat_x(r0.z, r0.w, dx);
 #pragma unroll
-        for (int q = 0; q < PX; ++q) contrib |= bwd_pixel<NC, GR>(P[q], j, rec, v);
+        for (int q = 0; q < PX; ++q) contrib |= bwd_pixel<NC, GR>(P[q], j, rec, sx, dx, v);
         if (__any_sync(0xffffffffu, contrib)) {
           const float sum = warp_reduce_scatter<GR>(v);
           if (GR == 32) {
