@@ -16,11 +16,13 @@
 //  * pack: one pass writes a record per Gaussian (u, v, scaled conic, o,
 //    tau, thr, f_0..f_{C-1}, zero padding: 48 to 144 bytes) so that a splat is
 //    one 16-byte aligned contiguous block read with 16-byte loads;
-//  * forward/backward: one CTA of 128 threads per tile, two pixels per
-//    thread; each warp owns an 8x8 pixel box and, per batch, culls the
-//    staged splats against it (exact minimum of the conic over the box) into
-//    a list, so every per-splat step serves 64 pixels.  The tile's sorted
-//    ids are consumed in batches of 128.  Forward: each thread issues a TMA
+//  * forward/backward: one CTA per tile, two pixels per thread and 8x8
+//    warp boxes (the backward also four pixels per thread, 64 threads and
+//    8x16 boxes); each warp culls the staged splats of a batch against its
+//    box (exact minimum of the conic over the box) into a list, so every
+//    per-splat step serves 64 (128) pixels.  The tile's sorted ids are
+//    consumed in batches of 64-256 records (the kernel variants, chosen at
+//    run time by the caller's autotuner).  Forward: each thread issues a TMA
 //    bulk copy (cp.async.bulk, no multicast) of one record into a
 //    double-buffered shared-memory stage that completes on an mbarrier, so
 //    batch b+1 streams in while batch b is composited; every mbarrier wait
@@ -40,7 +42,6 @@
 
 namespace pgb {
 
-constexpr int kBatch = 256;  // default batch of the culling helper
 constexpr uint32_t kWaitLimit = 1u << 22;
 
 // ---------------------------------------------------------------- PTX helpers
@@ -272,16 +273,6 @@ __global__ void pack_kernel(const float* __restrict__ uv, const float* __restric
   }
 }
 
-// Pixel of thread t in a 16x16 tile: warp w covers the 8x4 box at
-// (8 (w % 2), 4 (w / 2)); lane l is pixel (l % 8, l / 8) of that box.
-__device__ __forceinline__ void tile_pixel(int tile, int gx, int& px, int& py, int& bx0, int& by0) {
-  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
-  bx0 = (tile % gx) * kTile + 8 * (w & 1);
-  by0 = (tile / gx) * kTile + 4 * (w >> 1);
-  px = bx0 + (l & 7);
-  py = by0 + (l >> 3);
-}
-
 // Conservative test: can the splat pass the alpha test at any pixel centre
 // of the box [x0, x0 + BW - 1] x [y0, y0 + BH - 1]?  Minimum of the (convex) quadratic
 // form over the box -- zero if the centre is inside, else the least of its
@@ -317,7 +308,7 @@ __device__ __forceinline__ bool splat_may_touch_box(const float* rec, float x0, 
 // Builds this warp's list of batch slots (in increasing order) whose splat
 // may touch the warp's pixel box; slots >= cnt are ignored.  Returns the
 // list length.
-template <int BW, int BH, int B = kBatch>
+template <int BW, int BH, int B>
 __device__ __forceinline__ int warp_cull(const float* stage, int RF, int cnt, float x0, float y0,
                                          uint8_t* list) {
   const int lane = threadIdx.x & 31;
