@@ -62,6 +62,8 @@ constexpr int kDepthPasses = 4;
 // A batch of views adds one pass over the view index after the depth
 // passes, so that the emission is view-major (depth order within a view).
 constexpr int kViewPass = kDepthPasses;
+// counter word where phase one records its view count (0: one image)
+constexpr int kViewsMark = 12;
 constexpr int kMaxTilePasses = 3;
 constexpr int kTileHistWords = 1024;  // 3 passes x 256 digits or 2 x 512
 constexpr uint32_t kFlagAgg = 1u << 30;
@@ -158,8 +160,10 @@ __global__ void __launch_bounds__(kSortThreads) sort_prepare_kernel(
     const float* __restrict__ depth, const int32_t* __restrict__ radius,
     const int32_t* __restrict__ tiles, int64_t n, uint32_t* __restrict__ keys,
     uint32_t* __restrict__ vals, uint32_t* __restrict__ hist, int nviews, int64_t n_per_view,
-    int64_t* __restrict__ info) {
+    uint32_t* __restrict__ views_mark, int64_t* __restrict__ info) {
   __shared__ uint32_t h[kDepthPasses][256];
+  // phase two checks that phase one sorted the same way (one image or views)
+  if (blockIdx.x == 0 && threadIdx.x == 0) *views_mark = (uint32_t)nviews;
   // the view pass's histogram: n_per_view elements in each view
   if (blockIdx.x == 0)
     for (int v = threadIdx.x; v < nviews; v += blockDim.x)
@@ -867,13 +871,19 @@ __global__ void __launch_bounds__(kSortThreads) scan_rect_kernel(
     const int64_t* __restrict__ k_dev, uint32_t* __restrict__ status,
     uint32_t* __restrict__ part_counter, uint4* __restrict__ owner,
     uint32_t* __restrict__ chunk_first, int2* __restrict__ range, uint32_t T,
-    int64_t* __restrict__ info) {
+    const uint32_t* __restrict__ views_mark, uint32_t nviews, int64_t* __restrict__ info) {
   __shared__ uint32_t s_warp_tot[kSortThreads / 32];
   __shared__ uint32_t s_part, s_prior;
   // the tile-range table starts at (INT_MAX, 0) for the last tile pass
   for (int64_t i = (int64_t)blockIdx.x * kSortThreads + threadIdx.x; i < T;
        i += (int64_t)gridDim.x * kSortThreads)
     range[i] = make_int2(INT_MAX, 0);
+  // phase one of a batch (view-major order) must precede phase two of a
+  // batch, and the one-image phase one the one-image phase two
+  if (*views_mark != nviews) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) set_error(info, PGB_ERR_INVALID);
+    return;
+  }
   // a device count past the capacity: reported once, nothing is emitted
   if (k_dev && (*k_dev < 0 || *k_dev > k_cap)) {
     if (blockIdx.x == 0 && threadIdx.x == 0) set_error(info, PGB_ERR_OVERFLOW);
@@ -1101,7 +1111,8 @@ static int sort_begin_impl(const float* depth, const int32_t* radius, const int3
   uint32_t* k1 = at<uint32_t>(scratch_n, L.dk1);
   uint32_t* v1 = at<uint32_t>(scratch_n, L.dv1);
   sort_prepare_kernel<<<stream_grid(n, kSortThreads, 4), kSortThreads, 0, s>>>(
-      depth, radius, tiles_touched, n, k0, v0, hist, nviews, n_per_view, info);
+      depth, radius, tiles_touched, n, k0, v0, hist, nviews, n_per_view, counters + kViewsMark,
+      info);
   PassViews px{};
   if (nviews > 0) px.vdiv = fast_div((uint32_t)n_per_view);
   const int passes = kDepthPasses + (nviews > 0 ? 1 : 0);
@@ -1209,7 +1220,7 @@ static int sort_finish_impl(const float* uv, const int32_t* radius, const int32_
       uv, radius, tiles_touched, n, vt, plan.passes, plan.bits, rect, thist, info);
   scan_rect_kernel<<<LN.scan_parts, kSortThreads, 0, s>>>(
       order, n, rect, k, k_dev, at<uint32_t>(scratch_n, LN.scan_status), counters + 4, owner,
-      chunk_first, range, T, info);
+      chunk_first, range, T, counters + kViewsMark, (uint32_t)vt.nviews, info);
   GenSource src;
   src.owner = owner;
   src.chunk_first = chunk_first;

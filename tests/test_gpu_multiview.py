@@ -125,3 +125,39 @@ def test_batched_sort_lists_match_per_view_sorts(capacity_extra):
         assert bool((rng[base:base + T_v][empty] == 0).all())
         base += T_v
     ops.check_device_status()
+
+
+def test_finish_views_after_one_image_begin_is_reported():
+    """Phase two of a batch needs the batch's phase one (view-major depth
+    order): after the one-image phase one it reports PGB_ERR_INVALID in the
+    info word instead of sorting from the wrong order."""
+    from pointrix_gb300 import _lib
+    cams = _cams()[:2]
+    pos, sc, q, op, shs = _leaves()
+    n = pos.shape[0]
+    uvs, depths, radii, tiles = [], [], [], []
+    with torch.no_grad():
+        for cam in cams:
+            extr = cam.extr[:3, :]
+            uv, depth = ops.project_point(pos, cam.intr, extr, cam.W, cam.H)
+            vis = depth != 0
+            cov = ops.compute_cov3d(sc, q, vis)
+            _, radius, nt = ops.ewa_project(pos, cov, cam.intr, extr, uv, cam.W, cam.H, vis)
+            uvs.append(uv); depths.append(depth); radii.append(radius); tiles.append(nt)
+    uv, depth, radius, nt = (torch.cat(x) for x in (uvs, depths, radii, tiles))
+    sizes = [(c.W, c.H) for c in cams]
+    h = ops.sort_gaussian_begin(uv, depth, sizes[0][0], sizes[0][1], radius, nt)  # one image
+    K = h.count()
+    T = sum(multiview._tiles(W, H) for W, H in sizes)
+    T_local = max(multiview._tiles(W, H) for W, H in sizes)
+    _, bk = ops._sort_scratch(h.n, K, 16 * T_local, 16)
+    scratch_k = torch.empty(max(bk, 1), dtype=torch.uint8, device="cuda")
+    ids = torch.empty(max(K, 1), dtype=torch.int32, device="cuda")
+    rng = torch.empty(T, 2, dtype=torch.int32, device="cuda")
+    _lib.call("pgb_sort_gaussian_finish_views", h.uv.data_ptr(), h.radius.data_ptr(),
+              h.tiles.data_ptr(), n, multiview._sizes_array(sizes), len(sizes), K,
+              h.scratch_n.data_ptr(), h.bn, scratch_k.data_ptr(), bk, h.info.data_ptr(),
+              ids.data_ptr(), rng.data_ptr(), torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    assert int(h.info[1]) == 1  # PGB_ERR_INVALID
+    assert bool((rng == 0).all())  # nothing sorted: every tile empty after the range fix
