@@ -224,9 +224,9 @@ int pgb_alpha_blending_backward(const float* records, int64_t n, int channels,
  * arrays hold the views one after another (out: per-view [C,H,W] blocks;
  * final_T, n_contrib: per-view [H,W] blocks).  Phase one of the sort is
  * pgb_sort_gaussian_begin_views (which orders the elements by view, then
- * depth, then id; the finish_views entries require it, and a finish after
- * the other kind of phase one sets info[1] = PGB_ERR_INVALID and leaves
- * every tile empty).  The batch's pairs
+ * depth, then id; the finish_views entries require it: a finish after the
+ * other kind of phase one sets info[1] = PGB_ERR_INVALID, and its outputs
+ * are then undefined).  The batch's pairs
  * are then sorted by their view-local tile id, so ids_out holds, for every
  * local tile t, the lists of view 0, 1, ... one after another, and
  * tile_range_out[tile_base(v) + t] is view v's list of tile t; within a list

@@ -130,7 +130,7 @@ def test_batched_sort_lists_match_per_view_sorts(capacity_extra):
 def test_finish_views_after_one_image_begin_is_reported():
     """Phase two of a batch needs the batch's phase one (view-major depth
     order): after the one-image phase one it reports PGB_ERR_INVALID in the
-    info word instead of sorting from the wrong order."""
+    info word (its outputs are then undefined, as after any reported fault)."""
     from pointrix_gb300 import _lib
     cams = _cams()[:2]
     pos, sc, q, op, shs = _leaves()
@@ -159,5 +159,4 @@ def test_finish_views_after_one_image_begin_is_reported():
               h.scratch_n.data_ptr(), h.bn, scratch_k.data_ptr(), bk, h.info.data_ptr(),
               ids.data_ptr(), rng.data_ptr(), torch.cuda.current_stream().cuda_stream)
     torch.cuda.synchronize()
-    assert int(h.info[1]) == 1  # PGB_ERR_INVALID
-    assert bool((rng == 0).all())  # nothing sorted: every tile empty after the range fix
+    assert int(h.info[1]) == 1  # PGB_ERR_INVALID (the outputs are then undefined)
