@@ -12,8 +12,6 @@ captured in a CUDA graph and replayed.
 """
 from __future__ import annotations
 
-import math
-
 import torch
 
 from . import _lib

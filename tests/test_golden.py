@@ -8,8 +8,6 @@ import os
 import pytest
 import torch
 
-from oracle import msplat_cpu as O
-
 HERE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 CASES = sorted(f[:-3] for f in os.listdir(HERE) if f.endswith(".pt"))
 

@@ -3,7 +3,6 @@ gradients (torch.autograd.gradcheck in float64), float32/float64 agreement and
 the sort's structural properties.  No GPU."""
 import math
 
-import numpy as np
 import pytest
 import torch
 
