@@ -1,5 +1,6 @@
 """CPU tests of the C ABI: the library builds, loads, exports every entry point
-declared in include/pointrix_gb300.h, and rejects bad arguments before any
+declared in include/pointrix_gb300.h with ctypes argument and return types
+that match the prototypes, and rejects bad arguments before any
 CUDA call.  No kernel is launched."""
 import ctypes as C
 import re
@@ -56,3 +57,45 @@ def test_invalid_arguments_rejected_without_launch():
     assert lib.pgb_sort_scratch_bytes(-1, 0, 64, 64, C.byref(bn), C.byref(bk)) == 1
     # scratch too small is refused before any CUDA call
     assert lib.pgb_sort_gaussian_begin(None, None, None, 1000, 64, 64, None, 0, None, None) == 1
+
+
+def _prototypes():
+    """{name: (return type, [parameter types])} of every prototype in the header."""
+    text = re.sub(r"/\*.*?\*/", "", HEADER.read_text(), flags=re.S)
+    text = re.sub(r"//[^\n]*", "", text)
+    out = {}
+    for ret, name, args in re.findall(
+            r"([A-Za-z_][A-Za-z0-9_ *]*?)\b(pgb_[a-z0-9_]+)\s*\(([^)]*)\)\s*;", text):
+        params = []
+        for a in args.split(","):
+            a = " ".join(a.split())
+            if a and a != "void":
+                params.append(re.sub(r"\s*\b[A-Za-z_][A-Za-z0-9_]*$", "", a).replace(" *", "*"))
+        out[name] = (" ".join(ret.split()), params)
+    return out
+
+
+_SCALARS = {"int": C.c_int, "int64_t": C.c_int64, "float": C.c_float, "double": C.c_double,
+            "size_t": C.c_size_t}
+_POINTEES = {"size_t*": C.c_size_t, "int64_t*": C.c_int64,
+             "const pgb_adam_segment*": _lib.AdamSegment}
+_RETURNS = {"int": C.c_int, "int64_t": C.c_int64, "size_t": C.c_size_t, "const char*": C.c_char_p}
+
+
+def test_ctypes_signatures_match_the_header_prototypes():
+    """Each bound argument has the C type of its parameter (a wrong width
+    would pass a corrupted value to the library), and each return type is
+    read at its declared width."""
+    protos = _prototypes()
+    assert set(protos) == set(declared_functions())
+    for name, (ret, params) in protos.items():
+        bound = _lib.SIGNATURES[name]
+        assert len(bound) == len(params), (name, len(bound), len(params))
+        for i, (p, b) in enumerate(zip(params, bound)):
+            if p.endswith("*"):
+                want = _POINTEES.get(p)
+                ok = b is C.c_void_p or (want is not None and b is C.POINTER(want))
+            else:
+                ok = b is _SCALARS[p]
+            assert ok, f"{name} parameter {i}: header {p!r}, bound {b}"
+        assert _lib._RESTYPES.get(name, C.c_int) is _RETURNS[ret], (name, ret)
