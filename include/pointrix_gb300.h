@@ -15,6 +15,14 @@
  *    the call returns without synchronising (unless stated);
  *  - nothing is allocated and no caller memory is freed: scratch is passed
  *    in, sized by the matching *_scratch_bytes query;
+ *  - a buffer may be NULL only where its entry point says so, or when its
+ *    array is empty; otherwise the call returns PGB_ERR_INVALID before any
+ *    CUDA call.  Arrays the kernels access with vector loads or stores must
+ *    start on that vector's boundary, else PGB_ERR_INVALID: 8 bytes for
+ *    [N,2] arrays (uv, d_uv), cov3d [N,6], tile ranges [T,2] and the int64
+ *    `info` words; 16 bytes for quaternions [N,4], blend records, gradient
+ *    records and sort scratch (allocations from cudaMalloc or the torch
+ *    allocator always are);
  *  - the return value is a PGB_* status; a non-zero value means nothing
  *    useful was written.  Device-side faults that can only be seen after the
  *    kernels ran are reported through the `info` words named below.
@@ -196,7 +204,7 @@ int pgb_sort_gaussian_noalloc(const float* uv, const float* depth, const int32_t
  * [N,3], d_opacity [N,1], d_feature [N,C]; grad_records is scratch of
  * N * pgb_blend_grad_record_floats(C) floats.  `info` is one device int64 word that the caller
  * zeroes beforehand; a bounded device-side wait that expires writes
- * PGB_ERR_TIMEOUT into it.
+ * PGB_ERR_TIMEOUT into it (info may be NULL: that status is then dropped).
  * ------------------------------------------------------------------- */
 int pgb_blend_record_floats(int channels);
 /* Floats per Gaussian of the backward's gradient scratch (16 or 32). */

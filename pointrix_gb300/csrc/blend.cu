@@ -843,6 +843,10 @@ static int blend_forward_impl(const float* uv, const float* conic, const float* 
   if (n < 0 || k < 0 || tiles <= 0 || channels < 1 || nc < 0) return PGB_ERR_INVALID;
   if (!tile_range || !out || !final_T || !n_contrib || (k > 0 && !ids)) return PGB_ERR_INVALID;
   if (n > 0 && (!uv || !conic || !opacity || !fc.src[0] || !records)) return PGB_ERR_INVALID;
+  // records are staged by bulk copies and read as float4; the ranges as int2
+  // (info, when given, takes a 64-bit atomic)
+  if (misaligned(records, 16) || misaligned(tile_range, 8) || misaligned(info, 8))
+    return PGB_ERR_INVALID;
   cudaStream_t s = as_stream(stream);
   const int2* rg = reinterpret_cast<const int2*>(tile_range);
   switch (nc) {
@@ -871,6 +875,9 @@ static int blend_backward_impl(const float* records, int64_t n, int channels, co
   if (n < 0 || k < 0 || tiles <= 0 || channels < 1 || nc < 0) return PGB_ERR_INVALID;
   if (!tile_range || !final_T || !n_contrib || !d_out || (k > 0 && !ids)) return PGB_ERR_INVALID;
   if (n > 0 && (!records || !grad_records || !d_uv || !d_conic || !d_opacity || !gc.dst[0]))
+    return PGB_ERR_INVALID;
+  if (misaligned(records, 16) || misaligned(grad_records, 16) || misaligned(d_uv, 8) ||
+      misaligned(tile_range, 8) || misaligned(info, 8))
     return PGB_ERR_INVALID;
   if (n == 0) return PGB_OK;
   cudaStream_t s = as_stream(stream);

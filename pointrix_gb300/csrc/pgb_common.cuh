@@ -15,6 +15,12 @@ constexpr int kNumSMs = 152;         // GB300: 2 dies x 76 SMs
 // count (grid-stride loop beyond that).
 constexpr int kStreamThreads = 256;
 
+// True when p is not a multiple of `bytes`: the entry points refuse buffers
+// that a kernel would access with wider loads or stores than their start allows.
+inline bool misaligned(const void* p, uintptr_t bytes) {
+  return (reinterpret_cast<uintptr_t>(p) & (bytes - 1)) != 0;
+}
+
 inline int stream_grid(int64_t n, int threads = kStreamThreads, int per_sm = 8) {
   int64_t need = (n + threads - 1) / threads;
   int64_t cap = (int64_t)kNumSMs * per_sm;

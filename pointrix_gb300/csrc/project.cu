@@ -615,7 +615,7 @@ int pgb_project_point_forward(const float* xyz, int64_t n, const float* intr, co
                               float* depth, void* stream) {
   if (n < 0 || width <= 0 || height <= 0) return PGB_ERR_INVALID;
   if (n == 0) return PGB_OK;
-  if (!xyz || !intr || !extr || !uv || !depth) return PGB_ERR_INVALID;
+  if (!xyz || !intr || !extr || !uv || !depth || misaligned(uv, 8)) return PGB_ERR_INVALID;
   project_point_fwd_kernel<<<stream_grid(n), kStreamThreads, 0, as_stream(stream)>>>(
       xyz, n, intr, extr, width, height, nearest, extent, uv, depth);
   return launch_status();
@@ -627,7 +627,10 @@ int pgb_project_point_backward(const float* xyz, int64_t n, const float* intr, c
                                float* d_intr, float* d_extr, void* scratch, size_t scratch_bytes,
                                void* stream) {
   if (n < 0 || width <= 0 || height <= 0) return PGB_ERR_INVALID;
-  if (scratch_bytes < pgb_camera_grad_scratch_bytes() || !scratch) return PGB_ERR_INVALID;
+  if (scratch_bytes < pgb_camera_grad_scratch_bytes() || !scratch || !intr || !extr || !d_intr ||
+      !d_extr)
+    return PGB_ERR_INVALID;
+  if (n > 0 && (!xyz || !d_uv || !d_depth || !d_xyz || misaligned(d_uv, 8))) return PGB_ERR_INVALID;
   cudaStream_t s = as_stream(stream);
   const int grid = stream_grid(n);
   float* partials = static_cast<float*>(scratch);
@@ -642,6 +645,8 @@ int pgb_compute_cov3d_forward(const float* scales, const float* uquats, const ui
                               int64_t n, float* cov3d, void* stream) {
   if (n < 0) return PGB_ERR_INVALID;
   if (n == 0) return PGB_OK;
+  if (!scales || !uquats || !visible || !cov3d || misaligned(uquats, 16) || misaligned(cov3d, 8))
+    return PGB_ERR_INVALID;
   cov3d_fwd_kernel<<<stream_grid(n), kStreamThreads, 0, as_stream(stream)>>>(scales, uquats,
                                                                              visible, n, cov3d);
   return launch_status();
@@ -652,6 +657,9 @@ int pgb_compute_cov3d_backward(const float* scales, const float* uquats, const u
                                void* stream) {
   if (n < 0) return PGB_ERR_INVALID;
   if (n == 0) return PGB_OK;
+  if (!scales || !uquats || !visible || !d_cov3d || !d_scales || !d_uquats ||
+      misaligned(uquats, 16) || misaligned(d_uquats, 16))
+    return PGB_ERR_INVALID;
   cov3d_bwd_kernel<<<stream_grid(n), kStreamThreads, 0, as_stream(stream)>>>(
       scales, uquats, visible, n, d_cov3d, d_scales, d_uquats);
   return launch_status();
@@ -663,6 +671,9 @@ int pgb_ewa_project_forward(const float* xyz, const float* cov3d, const float* i
                             int32_t* tiles_touched, void* stream) {
   if (n < 0 || width <= 0 || height <= 0) return PGB_ERR_INVALID;
   if (n == 0) return PGB_OK;
+  if (!xyz || !cov3d || !intr || !extr || !uv || !visible || !conic || !radius || !tiles_touched ||
+      misaligned(cov3d, 8) || misaligned(uv, 8))
+    return PGB_ERR_INVALID;
   ewa_fwd_kernel<<<stream_grid(n), kStreamThreads, 0, as_stream(stream)>>>(
       xyz, cov3d, intr, extr, uv, visible, n, width, height, conic, radius, tiles_touched);
   return launch_status();
@@ -674,7 +685,11 @@ int pgb_ewa_project_backward(const float* xyz, const float* cov3d, const float* 
                              float* d_intr, float* d_extr, void* scratch, size_t scratch_bytes,
                              void* stream) {
   if (n < 0 || width <= 0 || height <= 0) return PGB_ERR_INVALID;
-  if (scratch_bytes < pgb_camera_grad_scratch_bytes() || !scratch) return PGB_ERR_INVALID;
+  if (scratch_bytes < pgb_camera_grad_scratch_bytes() || !scratch || !intr || !extr || !d_intr ||
+      !d_extr)
+    return PGB_ERR_INVALID;
+  if (n > 0 && (!xyz || !cov3d || !radius || !d_conic || !d_xyz || !d_cov3d))
+    return PGB_ERR_INVALID;
   cudaStream_t s = as_stream(stream);
   const int grid = stream_grid(n);
   float* partials = static_cast<float*>(scratch);
@@ -691,7 +706,7 @@ int pgb_preprocess_forward(const float* xyz, const float* scales, const float* u
   if (n < 0 || width <= 0 || height <= 0) return PGB_ERR_INVALID;
   if (n == 0) return PGB_OK;
   if (!xyz || !scales || !uquats || !intr || !extr || !uv || !depth || !conic || !radius ||
-      !tiles_touched || (reinterpret_cast<uintptr_t>(uquats) & 15))
+      !tiles_touched || misaligned(uquats, 16) || misaligned(uv, 8))
     return PGB_ERR_INVALID;
   preprocess_fwd_kernel<<<stream_grid(n), kStreamThreads, 0, as_stream(stream)>>>(
       xyz, scales, uquats, n, intr, extr, width, height, nearest, extent, uv, depth, conic, radius,
@@ -709,8 +724,8 @@ int pgb_preprocess_backward(const float* xyz, const float* scales, const float* 
   if (scratch_bytes < pgb_camera_grad_scratch_bytes() || !scratch || !d_intr || !d_extr)
     return PGB_ERR_INVALID;
   if (n > 0 && (!xyz || !scales || !uquats || !intr || !extr || !radius || !d_uv || !d_depth ||
-                !d_conic || !d_xyz || !d_scales || !d_uquats ||
-                ((reinterpret_cast<uintptr_t>(uquats) | reinterpret_cast<uintptr_t>(d_uquats)) & 15)))
+                !d_conic || !d_xyz || !d_scales || !d_uquats || misaligned(uquats, 16) ||
+                misaligned(d_uquats, 16) || misaligned(d_uv, 8)))
     return PGB_ERR_INVALID;
   cudaStream_t s = as_stream(stream);
   const int grid = stream_grid(n);

@@ -1095,10 +1095,12 @@ int pgb_sort_scratch_bytes(int64_t n, int64_t k, int width, int height, size_t* 
 static int sort_begin_impl(const float* depth, const int32_t* radius, const int32_t* tiles_touched,
                            int64_t n, int nviews, int64_t n_per_view, void* scratch_n,
                            size_t bytes_n, int64_t* info, void* stream) {
-  if (n < 0 || !info) return PGB_ERR_INVALID;
+  if (n < 0 || !info || misaligned(info, 8)) return PGB_ERR_INVALID;
+  if (n > 0 && (!depth || !radius || !tiles_touched)) return PGB_ERR_INVALID;
   if (n >= (int64_t)kValMask) return PGB_ERR_OVERFLOW;
   const ScratchN L = layout_n(n);
-  if (!scratch_n || bytes_n < L.total) return PGB_ERR_INVALID;
+  // the scratch holds uint4 arrays at 256-byte offsets from its start
+  if (!scratch_n || bytes_n < L.total || misaligned(scratch_n, 16)) return PGB_ERR_INVALID;
   cudaStream_t s = as_stream(stream);
   if (cudaMemsetAsync(info, 0, 2 * sizeof(int64_t), s) != cudaSuccess) return PGB_ERR_CUDA;
   if (cudaMemsetAsync(scratch_n, 0, L.zero_bytes, s) != cudaSuccess) return PGB_ERR_CUDA;
@@ -1178,6 +1180,10 @@ static int sort_finish_impl(const float* uv, const int32_t* radius, const int32_
                             int64_t* info, int32_t* ids_out, int32_t* tile_range_out,
                             void* stream) {
   if (n < 0 || k < 0 || !info || !tile_range_out) return PGB_ERR_INVALID;
+  // uv is read as float2 and the ranges written as int2: 8-byte starts
+  if (misaligned(uv, 8) || misaligned(tile_range_out, 8) || misaligned(info, 8))
+    return PGB_ERR_INVALID;
+  if (n > 0 && (!uv || !radius || !tiles_touched)) return PGB_ERR_INVALID;
   if (k >= (int64_t)kValMask) return PGB_ERR_OVERFLOW;
   const ScratchN LN = layout_n(n);
   // a batch sorts local tile ids: the plan is that of the largest view
@@ -1189,8 +1195,9 @@ static int sort_finish_impl(const float* uv, const int32_t* radius, const int32_
   }
   const TilePlan plan = tile_plan(T_local);
   const ScratchK LK = layout_k(k, plan.passes);
-  if (!scratch_n || bytes_n < LN.total) return PGB_ERR_INVALID;
-  if (k > 0 && (!scratch_k || bytes_k < LK.total || !ids_out)) return PGB_ERR_INVALID;
+  if (!scratch_n || bytes_n < LN.total || misaligned(scratch_n, 16)) return PGB_ERR_INVALID;
+  if (k > 0 && (!scratch_k || bytes_k < LK.total || !ids_out || misaligned(scratch_k, 16)))
+    return PGB_ERR_INVALID;
   if (T == 0 || T > (1u << (8 * kMaxTilePasses))) return PGB_ERR_INVALID;
   cudaStream_t s = as_stream(stream);
   if (k == 0 || n == 0) {

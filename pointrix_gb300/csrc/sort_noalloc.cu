@@ -63,6 +63,8 @@ extern "C" int pgb_sort_gaussian_noalloc(const float* uv, const float* depth,
     return PGB_ERR_INVALID;
   if (n > kMaxGaussians) return PGB_ERR_INVALID;  // beyond the fixed capacity
   if (n > 0 && (!uv || !depth || !radius || !tiles_touched)) return PGB_ERR_INVALID;
+  if (ids_capacity > 0 && !ids_out) return PGB_ERR_INVALID;
+  if (pgb::misaligned(uv, 8) || pgb::misaligned(tile_range_out, 8)) return PGB_ERR_INVALID;
   size_t bytes_n = 0, bytes_k = 0;
   int st = pgb_sort_scratch_bytes(n, 0, width, height, &bytes_n, nullptr);
   if (st != PGB_OK) return st;

@@ -99,3 +99,28 @@ def test_ctypes_signatures_match_the_header_prototypes():
                 ok = b is _SCALARS[p]
             assert ok, f"{name} parameter {i}: header {p!r}, bound {b}"
         assert _lib._RESTYPES.get(name, C.c_int) is _RETURNS[ret], (name, ret)
+
+
+_SIZE_QUERIES = {"pgb_status_string", "pgb_abi_version", "pgb_camera_grad_scratch_bytes",
+                 "pgb_blend_record_floats", "pgb_blend_grad_record_floats",
+                 "pgb_sh_rgb_scratch_floats", "pgb_sh_rgb_views_scratch_floats",
+                 "pgb_l1_l2_loss_scratch_doubles", "pgb_ssim_scratch_doubles",
+                 "pgb_sort_scratch_bytes", "pgb_blend_batches"}
+
+
+def test_every_compute_entry_rejects_null_buffers():
+    """Null buffers with a non-empty problem (16 of everything, 0.5 for
+    every float) are refused with PGB_ERR_INVALID before any CUDA call, by
+    every entry point that launches work."""
+    import torch
+
+    if torch.cuda.is_available():
+        import pytest
+        pytest.skip("argument checks are exercised where no device can be reached")
+    lib = _lib.lib()
+    launching = sorted(set(_lib.SIGNATURES) - _SIZE_QUERIES)
+    assert len(launching) >= 40
+    for name in launching:
+        args = [None if (t is C.c_void_p or issubclass(t, C._Pointer)) else
+                (0.5 if t in (C.c_float, C.c_double) else 16) for t in _lib.SIGNATURES[name]]
+        assert getattr(lib, name)(*args) == 1, name
