@@ -29,6 +29,7 @@ import json
 import math
 import os
 import threading
+import warnings
 
 import torch
 
@@ -57,18 +58,31 @@ def _load_locked() -> None:
             saved = json.load(f)
     except (OSError, ValueError):
         return
-    for k, b in saved.items():
-        kind, *rest = k.split("/")
-        _cache.setdefault((kind, *map(int, rest)), int(b))
+    for k, b in (saved.items() if isinstance(saved, dict) else ()):
+        try:
+            kind, *rest = str(k).split("/")
+            _cache.setdefault((kind, *map(int, rest)), int(b))
+        except (TypeError, ValueError):
+            continue  # an entry this version cannot read: that class is timed again
 
 
 def _save_locked() -> None:
+    # a temporary file of this process and thread, renamed over the cache, so
+    # that processes sharing one cache file never see half a file
     if not _cache_file:
         return
-    tmp = _cache_file + ".tmp"
-    with open(tmp, "w") as f:
-        json.dump({_key_str(k): b for k, b in _cache.items()}, f)
-    os.replace(tmp, _cache_file)
+    tmp = f"{_cache_file}.{os.getpid()}.{threading.get_ident()}.tmp"
+    try:
+        with open(tmp, "w") as f:
+            json.dump({_key_str(k): b for k, b in _cache.items()}, f)
+        os.replace(tmp, _cache_file)
+    except OSError as e:
+        # the file only spares later processes the timing runs
+        warnings.warn(f"autotune cache {_cache_file} not written: {e}", RuntimeWarning)
+        try:
+            os.remove(tmp)
+        except OSError:
+            pass
 
 
 def workload_class(kind: str, channels: int, pixels: int, entries: int, tiles: int) -> tuple:
@@ -92,11 +106,13 @@ def _cuda_timer(fn, device) -> float:
 def choose(key, candidates, run, device=None, timer=None) -> int:
     """The batch for ``key``: the cached choice, else (when enabled and not
     capturing) the fastest of ``candidates`` timed with ``run(batch)``, else
-    0 (the library default)."""
+    0 (the library default).  A cached choice that is not among
+    ``candidates`` (a cache file from a build with other variants) is not
+    used."""
     with _lock:
         _load_locked()
         hit = _cache.get(key)
-    if hit is not None:
+    if hit is not None and hit in candidates:
         return hit
     capturing = torch.cuda.is_available() and torch.cuda.is_current_stream_capturing()
     if not _enabled or capturing or not candidates:
@@ -106,7 +122,8 @@ def choose(key, candidates, run, device=None, timer=None) -> int:
     best = min(times, key=lambda b: (times[b], b))
     with _lock:
         _times.setdefault(key, times)
-        _cache.setdefault(key, best)
+        if _cache.get(key) not in candidates:  # keep a valid choice another thread made
+            _cache[key] = best
         _save_locked()
         return _cache[key]
 

@@ -50,3 +50,51 @@ def test_cache_file_round_trip(tmp_path):
     finally:
         autotune.set_cache_file(None)
         autotune.reset()
+
+
+def test_unreadable_entries_and_stale_choices_are_timed_again(tmp_path):
+    import json
+
+    key = autotune.workload_class("blend_bwd", 7, 1600 * 1060, 16_600_000, 6700)
+    path = tmp_path / "tune.json"
+    # a foreign key, a non-integer choice, and this class holding a variant
+    # that the current build does not offer
+    path.write_text(json.dumps({"blend_fwd/x/1": 64, "blend_fwd/7/20/1": "big",
+                                autotune._key_str(key): 999}))
+    autotune.reset()
+    autotune.set_cache_file(path)
+    try:
+        timed = []
+        assert autotune.choose(key, (64, 4096 + 64), lambda b: timed.append(b),
+                               timer=lambda fn: (fn(), 1.0)[1]) == 64
+        assert timed == [64, 4096 + 64]
+        assert json.loads(path.read_text())[autotune._key_str(key)] == 64
+        # disabled timing with a stale entry: the library default
+        autotune.reset()
+        autotune.set_cache_file(None)
+        autotune._cache[key] = 999
+        autotune.set_enabled(False)
+        assert autotune.choose(key, (64, 128), lambda b: None) == 0
+    finally:
+        autotune.set_enabled(True)
+        autotune.set_cache_file(None)
+        autotune.reset()
+
+
+def test_unwritable_cache_file_warns_and_still_chooses(tmp_path):
+    import pytest
+
+    blocker = tmp_path / "not_a_dir"
+    blocker.write_text("")
+    autotune.reset()
+    autotune.set_cache_file(blocker / "tune.json")  # its parent is a file
+    try:
+        key = autotune.workload_class("blend_fwd", 3, 640 * 480, 1_000_000, 1200)
+        with pytest.warns(RuntimeWarning, match="not written"):
+            assert autotune.choose(key, (64, 128), lambda b: None,
+                                   timer=lambda fn: 1.0) == 64
+        assert autotune.table()[key] == 64
+        assert list(tmp_path.iterdir()) == [blocker]   # no temporary file left
+    finally:
+        autotune.set_cache_file(None)
+        autotune.reset()
