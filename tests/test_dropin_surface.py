@@ -104,3 +104,40 @@ def test_render_features_pack_in_keyword_order():
     assert list(parts) == ["rgb", "depth", "normal"]
     assert torch.equal(parts["rgb"], img[:3]) and torch.equal(parts["depth"], img[3:4])
     assert torch.equal(parts["normal"], img[4:])
+
+
+def test_render_batch_aggregates_views_as_pointrix(monkeypatch):
+    """render_batch (pointrix/model/renderer/msplat.py:160-213) with
+    render_iter stubbed: per-view slices of the batched keys only, features
+    stacked per name, uv_points kept as a list, visibility any() and radii
+    max() over the views."""
+    B, N, H, W = 3, 5, 4, 6
+    seen = []
+
+    def fake_iter(self, **kw):
+        i = len(seen)
+        seen.append(kw)
+        return {"rendered_features_split": {"rgb": torch.full((3, H, W), float(i)),
+                                            "depth": torch.full((1, H, W), 10.0 + i)},
+                "uv_points": torch.full((N, 2), float(i)),
+                "visibility": torch.arange(N) == i,
+                "radii": torch.arange(N, dtype=torch.int32) * (i + 1)}
+
+    monkeypatch.setattr(MsplatRender, "render_iter", fake_iter)
+    r = MsplatRender()
+    extr = torch.randn(B, 4, 4)
+    centres = torch.randn(B, 3)
+    intr = torch.tensor([[100.0, 100.0, 3.0, 2.0]])
+    shs = torch.zeros(N, 16, 3)
+    out = r.render_batch({"extrinsic_matrix": extr, "camera_center": centres,
+                          "intrinsic_params": intr, "shs": shs, "height": H, "width": W})
+    assert len(seen) == B
+    for i, kw in enumerate(seen):
+        assert torch.equal(kw["extrinsic_matrix"], extr[i])
+        assert torch.equal(kw["camera_center"], centres[i])
+        assert kw["intrinsic_params"] is intr and kw["shs"] is shs  # not sliced
+    assert out["rgb"].shape == (B, 3, H, W) and out["depth"].shape == (B, 1, H, W)
+    assert [float(out["rgb"][i, 0, 0, 0]) for i in range(B)] == [0.0, 1.0, 2.0]
+    assert isinstance(out["uv_points"], list) and len(out["uv_points"]) == B
+    assert out["visibility"].tolist() == [True, True, True, False, False]
+    assert torch.equal(out["radii"], torch.arange(N, dtype=torch.int32) * B)
