@@ -21,7 +21,7 @@
 //    8x16 boxes); each warp culls the staged splats of a batch against its
 //    box (exact minimum of the conic over the box) into a list, so every
 //    per-splat step serves 64 (128) pixels.  The tile's sorted ids are
-//    consumed in batches of 64-256 records (the kernel variants, chosen at
+//    consumed in batches of 32-256 records (the kernel variants, chosen at
 //    run time by the caller's autotuner).  Forward: each thread issues a TMA
 //    bulk copy (cp.async.bulk, no multicast) of one record into a
 //    double-buffered shared-memory stage that completes on an mbarrier, so

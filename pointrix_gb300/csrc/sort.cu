@@ -12,20 +12,23 @@
 //      (0xFFFFFFFF for culled ones) and all four digit histograms at once,
 //      and sums tiles_touched into K;
 //   2. four onesweep passes sort the N Gaussians by depth (stable, so equal
-//      depths stay in id order);
+//      depths stay in id order); a batch of views adds a fifth, by view, so
+//      the order is view-major;
 //   3. rect: each Gaussian's tile rectangle and entry count (coalesced, in
 //      id order), and the tile digit histograms of all its entries (one
 //      update per rectangle row); scan_rect: a single-pass decoupled-look-back
 //      scan of the counts in depth order gives each Gaussian its output
 //      offset (its emission record);
 //   4. one stable onesweep pass for T <= 256 tiles, two 8-bit passes up to
-//      65,536 tiles, two 9-bit passes up to 2^18 (batches of views), else
-//      three, sort the (tile id, Gaussian id) pairs by tile id.  The first
-//      pass generates its partition's pairs from the emission records in
-//      registers (load-balanced: every partition is 6144 pairs however
-//      unevenly the tiles are spread over Gaussians): each owner marks the
-//      rectangle rows it starts inside the partition, and a running maximum
-//      over the marks gives every entry its owner and row.  The
+//      65,536 tiles, two 9-bit passes up to 2^18, else three, sort the
+//      (tile id, Gaussian id) pairs by tile id (a batch of views sorts
+//      view-local tile ids with the plan of its largest view).  The first
+//      pass generates its partition's pairs from the emission records
+//      (load-balanced: every partition is 6144 pairs however unevenly the
+//      tiles are spread over Gaussians): the partition's owners are staged
+//      in shared memory, each marks the rectangle rows it starts inside the
+//      partition, and a running maximum over the marks gives every entry its
+//      owner and row.  The
 //      depth-ordered pair sequence is never written out; the last pass
 //      writes only the ids and records each tile's [start, end) as it goes;
 //   5. tiles that no entry reached get [0, 0).
