@@ -179,7 +179,12 @@ int pgb_sort_gaussian_finish_capacity(const float* uv, const int32_t* radius,
  * Synchronous: returns when the results are complete on `stream`; a
  * device-side fault comes back as the return value.  The first call on a
  * device looks up the array's device address (with that device current);
- * make that first call before any stream capture.  All calls share the one
+ * make that first call before any stream capture.  Under CUDA's lazy module
+ * loading (the default since CUDA 12.2) that first call is also when the
+ * library's device code, and with it the array, is set up on the device, so
+ * it can fail with PGB_ERR_CUDA when device memory is short: make one warm-up
+ * call per device at start-up, before the memory budget is tight (or load
+ * modules eagerly with CUDA_MODULE_LOADING=EAGER).  All calls share the one
  * array (each clears what must start at zero): calls that overlap on the GPU,
  * e.g. from two streams or threads, race and must be serialised by the
  * caller.

@@ -422,6 +422,77 @@ def alpha_blending(uv, conic, opacity, feature, ids, tile_range, bg, W, H,
     return out
 
 
+def threshold_pixels(uv, conic, opacity, ids, tile_range, W, H, tiles=None,
+                     rel_alpha=1e-5, rel_T=1e-4, rel_clamp=1e-5):
+    """Where a float32 and a float64 rendition may legitimately disagree.
+
+    Evaluates, in float64, every (pixel, splat) pair that a pixel considers
+    (up to and including the pair at which it stops) and flags the pixel when
+    one of its pairs sits within a relative margin of a decision threshold of
+    the blend contract (``alpha_blending`` above):
+
+    * the skip test alpha >= 1/255 (``|o e^power - 1/255| <= rel_alpha/255``);
+    * the stop test T (1 - alpha) < 1e-4 (``|T (1 - alpha) - 1e-4| <=
+      rel_T 1e-4``; T carries the rounding of every earlier factor, hence
+      the wider margin);
+    * the 0.99 clamp (``|o e^power - 0.99| <= rel_clamp``), where the image is
+      continuous but its gradient jumps -- flagged in the second mask only.
+
+    The margins are ten to a hundred times the relative error of a float32
+    evaluation of one pair's power, exponential and transmittance.  Returns
+    ``(pix [H,W] bool, pix_grad [H,W] bool, gauss [N] bool)``: pixels whose
+    value may flip, pixels whose gradient may jump (a superset), and the
+    Gaussians any gradient-flagged pixel considers.
+    """
+    dt = torch.float64
+    n = uv.shape[0]
+    gx, gy = tile_grid(W, H)
+    ids = ids.long()
+    rng = tile_range.long()
+    pix_flag = torch.zeros(H * W, dtype=torch.bool)
+    grad_flag = torch.zeros(H * W, dtype=torch.bool)
+    gauss = torch.zeros(n, dtype=torch.bool)
+    ly, lx = torch.meshgrid(torch.arange(TILE), torch.arange(TILE), indexing="ij")
+    ly, lx = ly.reshape(-1), lx.reshape(-1)
+    u64, c64 = uv.detach().to(dt), conic.detach().to(dt)
+    o64 = opacity.detach().reshape(-1).to(dt)
+    for t in (range(gx * gy) if tiles is None else tiles):
+        t = int(t)
+        s, e = int(rng[t, 0]), int(rng[t, 1])
+        if e <= s:
+            continue
+        tx, ty = t % gx, t // gx
+        pxi, pyi = tx * TILE + lx, ty * TILE + ly
+        inside = (pxi < W) & (pyi < H)
+        pxi, pyi = pxi[inside], pyi[inside]
+        pix = pyi * W + pxi
+        g = ids[s:e]
+        dx = u64[g, 0][None, :] - pxi.to(dt)[:, None]
+        dy = u64[g, 1][None, :] - pyi.to(dt)[:, None]
+        ca, cb, cc = (c64[g, i][None, :] for i in range(3))
+        power = -0.5 * (ca * dx * dx + cc * dy * dy) - cb * dx * dy
+        araw = o64[g][None, :] * torch.exp(power)
+        alpha = araw.clamp(max=ALPHA_MAX)
+        valid = (power <= 0) & (alpha >= ALPHA_MIN)
+        a_v = torch.where(valid, alpha, torch.zeros_like(alpha))
+        Tinc = torch.cumprod(1.0 - a_v, dim=1)
+        stops = valid & (Tinc < T_MIN)
+        # a pair is considered when no earlier pair stopped the pixel
+        stopped_before = torch.cumsum(stops.int(), dim=1) - stops.int() > 0
+        considered = ~stopped_before
+        near_skip = (araw - ALPHA_MIN).abs() <= rel_alpha * ALPHA_MIN
+        near_stop = valid & ((Tinc - T_MIN).abs() <= rel_T * T_MIN)
+        near_clamp = (araw - ALPHA_MAX).abs() <= rel_clamp * ALPHA_MAX
+        f_val = ((near_skip | near_stop) & considered).any(dim=1)
+        f_grad = f_val | (near_clamp & valid & considered).any(dim=1)
+        pix_flag[pix[f_val]] = True
+        grad_flag[pix[f_grad]] = True
+        if bool(f_grad.any()):
+            touched = considered[f_grad].any(dim=0)
+            gauss[g[touched]] = True
+    return pix_flag.reshape(H, W), grad_flag.reshape(H, W), gauss
+
+
 # ---------------------------------------------------------------------------
 # The whole per-view path, as MsplatRender.render_iter chains it
 # (pointrix/model/renderer/msplat.py:94-151)

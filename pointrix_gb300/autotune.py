@@ -18,7 +18,12 @@ default before any).  ``PGB_AUTOTUNE=0`` in the environment disables timing
 (the default batch is used).  ``PGB_AUTOTUNE_CACHE=<file>`` keeps the
 choices in a JSON file: read on first use, rewritten after every new choice,
 so a later process (a profiler run, a restarted trainer) takes the same
-variants without timing them again.
+variants without timing them again.  ``PGB_BLEND_VARIANT=fwd=<b>,bwd=<b>``
+pins the variant of every class of that kernel (e.g. ``fwd=128,bwd=4160``:
+forward 128-record batches, backward four pixels per thread with 64-record
+batches), so that a run -- a profile, a comparison -- is reproducible
+without any cache file; a pinned value the build does not compile is
+ignored.
 
 A class is (kernel, channel count, log2 of the pixel count, log2 of the
 mean list length per tile): the quantities that move the optimum.
@@ -34,7 +39,7 @@ import warnings
 import torch
 
 __all__ = ["choose", "workload_class", "table", "timings", "reset", "set_enabled",
-           "set_cache_file"]
+           "set_cache_file", "set_pins"]
 
 _lock = threading.Lock()
 _cache: dict = {}
@@ -42,6 +47,19 @@ _times: dict = {}
 _enabled = os.environ.get("PGB_AUTOTUNE", "1") != "0"
 _cache_file = os.environ.get("PGB_AUTOTUNE_CACHE") or None
 _loaded = False
+
+
+def _parse_pins(text: str) -> dict:
+    pins = {}
+    for part in (text or "").split(","):
+        name, _, val = part.partition("=")
+        name = name.strip()
+        if name in ("fwd", "bwd") and val.strip().lstrip("-").isdigit():
+            pins["blend_" + name] = int(val)
+    return pins
+
+
+_pins = _parse_pins(os.environ.get("PGB_BLEND_VARIANT", ""))
 
 
 def _key_str(key) -> str:
@@ -109,6 +127,9 @@ def choose(key, candidates, run, device=None, timer=None) -> int:
     0 (the library default).  A cached choice that is not among
     ``candidates`` (a cache file from a build with other variants) is not
     used."""
+    pin = _pins.get(key[0]) if key else None
+    if pin is not None and pin in candidates:
+        return pin
     with _lock:
         _load_locked()
         hit = _cache.get(key)
@@ -153,6 +174,12 @@ def set_cache_file(path) -> None:
         _cache_file = os.fspath(path) if path else None
         _loaded = False
         _load_locked()
+
+
+def set_pins(text: str) -> None:
+    """Pins as in ``PGB_BLEND_VARIANT`` ("" clears them)."""
+    global _pins
+    _pins = _parse_pins(text)
 
 
 def set_enabled(flag: bool) -> None:

@@ -24,7 +24,14 @@ class Adam(torch.optim.Optimizer):
             raise ValueError(f"invalid eps {eps}")
         super().__init__(params, dict(lr=lr, betas=betas, eps=eps))
         self.capturable = bool(capturable)
-        self._steps_dev = None   # int32 [segments] of the capturable mode
+        # capturable mode: one device step count per parameter (a fixed slot
+        # each, in _count_all), gathered into _steps_dev in the order of the
+        # segments of the current step; re-gathered whenever the set of
+        # parameters with a gradient changes
+        self._slots: dict = {}
+        self._count_all = None
+        self._steps_dev = None
+        self._steps_key = None
 
     @torch.no_grad()
     def step(self, closure=None):
@@ -55,15 +62,13 @@ class Adam(torch.optim.Optimizer):
                              1.0 - b1 ** t, 1.0 - b2 ** t))
         if not segs:
             return loss
+
         b1, b2, eps = cfg
         lib = _lib.lib()
         dev = segs[0][0].device
         stream = torch.cuda.current_stream(dev).cuda_stream
-        if self.capturable and (self._steps_dev is None or self._steps_dev.numel() != len(segs)):
-            # the device counts start where the host counts were before this step
-            self._steps_dev = torch.tensor([self.state[p]["step"] - 1 for p, *_ in segs],
-                                           dtype=torch.int32, device=dev)
-            self._bc_dev = torch.empty(2 * len(segs), dtype=torch.float32, device=dev)
+        if self.capturable:
+            self._gather_counts([p for p, *_ in segs], dev)
         for i in range(0, len(segs), 32):
             chunk = segs[i:i + 32]
             table = (_lib.AdamSegment * len(chunk))(*[
@@ -81,3 +86,33 @@ class Adam(torch.optim.Optimizer):
                     _lib.check(lib.pgb_adam_step(table, len(chunk), b1, b2, eps, stream),
                                "pgb_adam_step")
         return loss
+
+    def _gather_counts(self, params, dev):
+        """Device step counts of ``params`` (this step's segments, in order)
+        in ``_steps_dev``.  A parameter seen for the first time starts from
+        its host count before this step; counts of parameters left out of a
+        step stay in their slots untouched."""
+        key = tuple(id(p) for p in params)
+        if key == self._steps_key:
+            return
+        new = [p for p in params if id(p) not in self._slots]
+        if new:
+            for p in new:
+                self._slots[id(p)] = len(self._slots)
+            init = torch.tensor([self.state[p]["step"] - 1 for p in new], dtype=torch.int32,
+                                device=dev)
+            self._count_all = init if self._count_all is None else torch.cat(
+                [self._write_back(), init])
+        else:
+            self._count_all = self._write_back()
+        self._slots_dev = torch.tensor([self._slots[id(p)] for p in params], dtype=torch.int64,
+                                       device=dev)
+        self._steps_dev = self._count_all.index_select(0, self._slots_dev)
+        self._bc_dev = torch.empty(2 * len(params), dtype=torch.float32, device=dev)
+        self._steps_key = key
+
+    def _write_back(self):
+        """_count_all with the counts the previous segments advanced."""
+        if self._steps_dev is not None:
+            self._count_all.index_copy_(0, self._slots_dev, self._steps_dev)
+        return self._count_all

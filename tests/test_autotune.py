@@ -98,3 +98,25 @@ def test_unwritable_cache_file_warns_and_still_chooses(tmp_path):
     finally:
         autotune.set_cache_file(None)
         autotune.reset()
+
+
+def test_pins_override_timing_and_cache():
+    """PGB_BLEND_VARIANT-style pins take precedence over the cache and the
+    timer; a pinned value the build does not compile is ignored."""
+    from pointrix_gb300 import autotune as A
+    A.reset()
+    calls = []
+    timer = lambda fn: (calls.append(1), fn())[1]  # noqa: E731
+    try:
+        A.set_pins("fwd=128,bwd=4160")
+        kf = ("blend_fwd", 7, 20, 11)
+        kb = ("blend_bwd", 7, 20, 11)
+        assert A.choose(kf, [64, 128], lambda b: float(b), timer=timer) == 128
+        assert A.choose(kb, [64, 128, 4160], lambda b: float(b), timer=timer) == 4160
+        assert calls == []
+        A.set_pins("bwd=999")
+        assert A.choose(kb, [64, 128], lambda b: float(b), timer=timer) == 64   # timed instead
+        assert calls
+    finally:
+        A.set_pins("")
+        A.reset()

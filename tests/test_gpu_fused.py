@@ -5,6 +5,8 @@ float64 composition; gradients within 1e-5 relative to the largest
 gradient entry (they are short float32 chains); the loss gradient equal to
 torch's l1_loss + w * mse_loss gradient to 1 ulp.
 """
+import os
+
 import pytest
 import torch
 import torch.nn.functional as F
@@ -13,7 +15,9 @@ from oracle import msplat_cpu as O
 from pointrix_gb300 import fused, ops
 from pointrix_gb300 import workloads as WL
 from pointrix_gb300.optim import Adam
+from pointrix_gb300.camera import unitquat_to_rotmat as cam_rotmat
 from pointrix_gb300.renderer import MsplatRender
+from tests import refload
 
 pytestmark = pytest.mark.gpu
 DEV = "cuda"
@@ -26,6 +30,14 @@ def rel(a, b):
     return float((a - b).abs().max() / b.abs().max().clamp(min=1e-30))
 
 
+def _rotmat():
+    """``pointrix/utils/pose.py:unitquat_to_rotmat`` itself where the reference
+    is installed, else the camera model's form (equal to it bit for bit on the
+    fixture, ``tests/test_reference_glue.py``)."""
+    pose = refload.pose()
+    return pose.unitquat_to_rotmat if pose is not None else cam_rotmat
+
+
 def torch_activations(ls, q, lg):
     """The reference composition in float64 (gaussian_points.py:70-80,
     examples/supervise/model.py:50-62 with pose.py's matrix)."""
@@ -33,12 +45,7 @@ def torch_activations(ls, q, lg):
     r = F.normalize(q, dim=-1)
     o = torch.sigmoid(lg)
     idx = torch.argmin(ls, dim=-1)
-    w, x, y, z = r.unbind(-1)
-    cols = torch.stack([
-        torch.stack([x * x - y * y - z * z + w * w, 2 * (x * y + z * w), 2 * (x * z - y * w)], -1),
-        torch.stack([2 * (x * y - z * w), -x * x + y * y - z * z + w * w, 2 * (y * z + x * w)], -1),
-        torch.stack([2 * (x * z + y * w), 2 * (y * z - x * w), -x * x - y * y + z * z + w * w], -1),
-    ], 1)                                           # [N, axis, 3]
+    cols = _rotmat()(r).transpose(-1, -2)           # [N, axis, 3]
     nrm = cols[torch.arange(ls.shape[0]), idx]
     return s, r, o, F.normalize(nrm, dim=-1)
 
@@ -127,7 +134,8 @@ def test_capturable_adam_matches_host_steps():
                 p.grad = gr.clone()
             opt.step()
         runs.append(leaves)
-    for a, b in zip(*runs):
+    for a, b, p0 in zip(*runs, ps):
+        assert float((a - p0).abs().max()) > 1e-4      # the steps moved the parameters
         assert rel(b, a) < 1e-6
 
 
@@ -152,68 +160,100 @@ def test_renderer_fused_colour_matches_unfused():
     ops.check_device_status()
 
 
-def test_densification_stats_match_controller():
-    """One kernel against the controller's masked torch update
-    (pointrix/controller/gs.py:318-333), two views, normalize_grad on."""
+GLUE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "reference", "glue.pt")
+
+
+def _glue():
+    return torch.load(GLUE, weights_only=False)
+
+
+def _reference_controller(n, W, H):
+    """The reference's ``DensificationController`` (``pointrix/controller/gs.py``)
+    with only the state its ``preprocess`` reads; None where the reference is
+    not installed."""
+    gs = refload.gs_controller()
+    if gs is None:
+        return None
+    from types import SimpleNamespace
+    ctrl = object.__new__(gs.DensificationController)
+    ctrl.cfg = SimpleNamespace(normalize_grad=True)
+    ctrl.width, ctrl.height = W, H
+    ctrl.grad_accum = torch.zeros(n, 1)
+    ctrl.acc_steps = torch.zeros(n, 1)
+    ctrl.max_radii = torch.zeros(n)
+    return ctrl
+
+
+def _stats_step(st, rads, grads, W, H):
+    dev_uvs = []
+    for gr in grads:
+        p = torch.zeros(gr.shape, device=DEV, requires_grad=True)
+        p.grad = gr.to(DEV)
+        dev_uvs.append(p)
+    st.preprocess([r.to(DEV) for r in rads], dev_uvs, W, H)
+
+
+def test_densification_stats_match_controller_fixture():
+    """One kernel against the reference controller's masked torch update
+    (``preprocess`` + ``accumulate_viewspace_grad``, pointrix/controller/gs.py:
+    260-284, 318-333), as recorded by executing it: two views per step,
+    normalize_grad on, three steps."""
+    from pointrix_gb300.densify import DensificationStats
+    c = _glue()["controller"]
+    st = DensificationStats(c["n"], DEV, normalize_grad=True)
+    for step in c["steps"]:
+        _stats_step(st, step["radii"], step["uv_grads"], c["W"], c["H"])
+        assert torch.equal(st.acc_steps.cpu(), step["acc_steps"])
+        assert torch.equal(st.max_radii.cpu(), step["max_radii"])
+        assert rel(st.grad_accum, step["grad_accum"]) < 1e-6
+    assert not bool(st.average_grad().isnan().any())
+
+
+@pytest.mark.skipif(refload.pointrix_dir() is None, reason="reference source not installed")
+def test_densification_stats_match_controller_live():
+    """The same against the reference controller run here, 30,000 points."""
     from pointrix_gb300.densify import DensificationStats
     g = torch.Generator().manual_seed(8)
     n, W, H = 30_000, 640, 480
+    ctrl = _reference_controller(n, W, H)
     st = DensificationStats(n, DEV, normalize_grad=True)
-    ga, ac, mr = torch.zeros(n, 1), torch.zeros(n, 1), torch.zeros(n)
-    for step in range(3):
+    for _ in range(3):
         uvs, rads = [], []
-        for v in range(2):
+        for _v in range(2):
             p = torch.zeros(n, 2, requires_grad=True)
             p.grad = torch.randn(n, 2, generator=g) * 1e-3
-            r = torch.randint(-2, 30, (n,), generator=g).clamp(min=0).to(torch.int32)
-            uvs.append(p); rads.append(r)
-        # reference update (accumulate_viewspace_grad + preprocess)
-        vg = uvs[0].grad.clone() + uvs[1].grad
-        vg[..., 0] *= W / 2.0
-        vg[..., 1] *= H / 2.0
-        radii = torch.stack(rads).max(dim=0).values
-        vis = torch.stack([r > 0 for r in rads]).any(dim=0)
-        mr[vis] = torch.max(mr[vis], radii[vis])
-        ga[vis] += torch.norm(vg[vis, :2], dim=-1, keepdim=True)
-        ac[vis] += 1
-        dev_uvs = [t.detach().to(DEV).requires_grad_(True) for t in uvs]
-        for a, b in zip(dev_uvs, uvs):
-            a.grad = b.grad.to(DEV)
-        st.preprocess([r.to(DEV) for r in rads], dev_uvs, W, H)
-    assert torch.equal(st.acc_steps.cpu(), ac) and torch.equal(st.max_radii.cpu(), mr)
-    assert rel(st.grad_accum, ga) < 1e-6
-    avg = st.average_grad()
-    assert not bool(avg.isnan().any())
+            uvs.append(p)
+            rads.append(torch.randint(-2, 30, (n,), generator=g).clamp(min=0).to(torch.int32))
+        vis = torch.cat([(r > 0).unsqueeze(0) for r in rads]).any(dim=0)
+        radii = torch.cat([r.unsqueeze(0) for r in rads], 0).max(dim=0).values
+        ctrl.preprocess(visibility=vis, radii=radii, uv_points=uvs)
+        _stats_step(st, rads, [p.grad for p in uvs], W, H)
+    assert torch.equal(st.acc_steps.cpu(), ctrl.acc_steps)
+    assert torch.equal(st.max_radii.cpu(), ctrl.max_radii)
+    assert rel(st.grad_accum, ctrl.grad_accum) < 1e-6
 
 
-def _ssim_reference(x, y):
-    """pointrix/model/loss.py:ssim in float64 (conv2d with the separable
-    Gaussian window, zero padding 5, groups = channels)."""
-    import math
-    g = torch.tensor([math.exp(-(k - 5) ** 2 / (2 * 1.5 ** 2)) for k in range(11)],
-                     dtype=torch.float64)
-    g = g / g.sum()
-    win = (g[:, None] @ g[None, :])[None, None]
-    x4, y4 = (t if t.dim() == 4 else t[None] for t in (x, y))
-    C = x4.shape[1]
-    w = win.expand(C, 1, 11, 11).contiguous()
-    conv = lambda t: F.conv2d(t, w, padding=5, groups=C)  # noqa: E731
-    mu1, mu2 = conv(x4), conv(y4)
-    s11 = conv(x4 * x4) - mu1 ** 2
-    s22 = conv(y4 * y4) - mu2 ** 2
-    s12 = conv(x4 * y4) - mu1 * mu2
-    C1, C2 = 0.01 ** 2, 0.03 ** 2
-    m = ((2 * mu1 * mu2 + C1) * (2 * s12 + C2)) / ((mu1 ** 2 + mu2 ** 2 + C1) * (s11 + s22 + C2))
-    return m.mean()
+def test_ssim_matches_reference_fixture():
+    """Fused SSIM against the value and gradient the reference's ``ssim``
+    (pointrix/model/loss.py:71-125) gave in float64."""
+    c = _glue()["ssim"]
+    xg = c["x"].float().to(DEV).requires_grad_(True)
+    out = fused.ssim(xg, c["y"].float().to(DEV))
+    assert abs(float(out) - float(c["value"])) < 1e-6
+    out.backward()
+    assert rel(xg.grad, c["grad"]) < 1e-5
+    ops.check_device_status()
 
 
+@pytest.mark.skipif(refload.pointrix_dir() is None, reason="reference source not installed")
 @pytest.mark.parametrize("shape", [(3, 70, 101), (2, 3, 33, 64), (1, 32, 32)])
-def test_ssim_matches_reference(shape):
+def test_ssim_matches_reference_live(shape):
+    ssim_ref = refload.loss().ssim
     g = torch.Generator().manual_seed(sum(shape))
     y = torch.rand(*shape, generator=g)
     x = (y + 0.1 * torch.randn(*shape, generator=g)).clamp(0, 1)
     x64 = x.double().requires_grad_(True)
-    ref = _ssim_reference(x64, y.double())
+    ref = ssim_ref(x64, y.double())
     (2.0 * ref).backward()
     xg = x.to(DEV).requires_grad_(True)
     out = fused.ssim(xg, y.to(DEV))

@@ -4,10 +4,15 @@ Bars (stated per test):
 * integer outputs (radius, tiles_touched, sorted ids, tile ranges) and the
   float outputs of the FMA-free projection kernels (uv, depth, cov3d, conic):
   bit-exact against the float32 oracle;
-* images and SH colours: within 1e-5 abs of the float64 oracle on the same
-  inputs (depth channel: 1e-5 relative to the scene depth);
+* images (every channel, depth included) and SH colours: within 1e-5 abs
+  of the float64 oracle on the same inputs, on every pixel whose float64
+  skip/stop decisions do not sit on a threshold (``tests/bars.py``; such
+  pixels are counted and must stay rare), and the last-contributor counts
+  equal there;
 * gradients: within 1e-4 of the float64 oracle's autograd gradient,
-  relative to the largest gradient entry of that tensor.
+  relative to the largest gradient entry of that tensor (the chain
+  gradients: 1e-4 relative L2, and 1e-4 of the largest entry for every
+  Gaussian no threshold pixel considers).
 """
 import pytest
 import torch
@@ -15,6 +20,7 @@ import torch
 from oracle import msplat_cpu as O
 from pointrix_gb300 import ops
 from pointrix_gb300 import workloads as WL
+from tests.bars import assert_grad_close, assert_image_close
 
 pytestmark = pytest.mark.gpu
 DEV = "cuda"
@@ -144,13 +150,10 @@ def test_alpha_blending_forward_close(small):
     img, fT, nc = ops.alpha_blending_with_state(p.uv, p.conic, p.op, p.feat, p.ids, p.rng, 0.0, p.W, p.H)
     u, c, o, f = blend_inputs64(p)
     ref, fT_o, nc_o = O.alpha_blending(u, c, o, f, cpu(p.ids), cpu(p.rng), 0.0, p.W, p.H, return_state=True)
-    img = cpu(img, torch.float64)
-    assert (img[:3] - ref[:3]).abs().max() < IMG_ATOL
-    depth_scale = float(p.depth.max())
-    assert (img[3] - ref[3]).abs().max() < IMG_ATOL * depth_scale
-    # skip/stop decisions taken in float32 vs float64 may differ on a handful of pixels at most
-    assert (cpu(nc) != nc_o).float().mean() < 1e-3
-    assert (cpu(fT, torch.float64) - fT_o).abs().max() < 1e-5
+    flagged = O.threshold_pixels(cpu(p.uv), cpu(p.conic), cpu(p.op), cpu(p.ids), cpu(p.rng), p.W, p.H)[0]
+    assert_image_close(img, ref, flagged)
+    assert bool((cpu(nc) == nc_o)[~flagged].all())
+    assert_image_close(fT, fT_o, flagged, what="final T")
 
 
 def test_alpha_blending_background(small):
@@ -270,14 +273,11 @@ def test_end_to_end_gradients_match_oracle(small):
     loss_o.backward()
     assert abs(float(loss.detach()) - float(loss_o.detach())) < 1e-5
     # A float32 and a float64 rendition may still take a different skip/stop
-    # decision for a (pixel, splat) pair that sits on a threshold, which moves
-    # a handful of entries.  The bar is the relative L2 error of each
-    # gradient tensor (1e-4), with a looser bound on the worst single entry.
+    # decision for a (pixel, splat) pair that sits on a threshold; the
+    # Gaussians such pixels consider are excluded from the worst-entry bar.
+    gflag = O.threshold_pixels(gd["uv"], gd["conic"], cpu(p.op), cpu(ids), cpu(rng), p.W, p.H)[2]
     for name, a, b in zip(("position", "scale", "rotation", "opacity", "shs", "intr", "extr"), leaves, r):
-        A, B = a.grad.detach().double().cpu(), b.grad.double()
-        rel_l2 = float((A - B).norm() / B.norm().clamp(min=1e-30))
-        e = scaled_err(a.grad, b.grad)
-        assert rel_l2 < GRAD_RTOL and e < 1e-3, (name, rel_l2, e)
+        assert_grad_close(a.grad, b.grad, gflag, what=name)
 
 
 # ------------------------------------------------------------ edge cases ---
@@ -292,7 +292,8 @@ def test_odd_image_sizes(W, H):
     img = ops.alpha_blending(p.uv, p.conic, p.op, p.feat, p.ids, p.rng, 0.1, W, H)
     ref = O.alpha_blending(*blend_inputs64(p), cpu(p.ids), cpu(p.rng), 0.1, W, H)
     assert img.shape == (4, H, W)
-    assert (cpu(img, torch.float64)[:3] - ref[:3]).abs().max() < IMG_ATOL
+    flagged = O.threshold_pixels(cpu(p.uv), cpu(p.conic), cpu(p.op), cpu(p.ids), cpu(p.rng), W, H)[0]
+    assert_image_close(img, ref, flagged)
 
 
 def test_everything_culled_gives_background():

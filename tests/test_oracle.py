@@ -30,21 +30,6 @@ def test_cov3d_identity_rotation_is_diag_s2():
     assert torch.allclose(cov, torch.tensor([[0.01, 0, 0, 0.04, 0, 0.09]], dtype=torch.float64))
 
 
-def test_cov3d_matches_rotation_matrix_of_pose_convention():
-    # quaternion -> rotation agrees with pointrix/utils/pose.py:40-84 (wxyz)
-    g = torch.Generator().manual_seed(1)
-    q = torch.randn(64, 4, generator=g, dtype=torch.float64)
-    q = q / q.norm(dim=1, keepdim=True)
-    R = O.quat_to_rot(q)
-    w, x, y, z = q.unbind(1)
-    ref = torch.stack([
-        torch.stack([x*x - y*y - z*z + w*w, 2*(x*y - z*w), 2*(x*z + y*w)], 1),
-        torch.stack([2*(x*y + z*w), -x*x + y*y - z*z + w*w, 2*(y*z - x*w)], 1),
-        torch.stack([2*(x*z - y*w), 2*(y*z + x*w), -x*x - y*y + z*z + w*w], 1)], 1)
-    mine = torch.stack([torch.stack(list(r), 1) for r in R], 1)
-    assert torch.allclose(mine, ref, atol=1e-12)
-
-
 def test_project_point_known_answer_and_culling():
     intr = torch.tensor([[100.0, 120.0, 50.0, 40.0]], dtype=torch.float64)
     extr = torch.cat([torch.eye(3), torch.zeros(3, 1)], 1).double()

@@ -23,8 +23,9 @@ PGB_ERR_INVALID, PGB_ERR_OVERFLOW = 1, 3
 MAX_GAUSSIANS = 262144
 
 
-def sort_inputs(seed, n, W, H, f, radius):
+def sort_inputs(seed, n, W, H, f, radius, log_scale_shift=0.0):
     scene, _ = WL.scene_small(seed, n=n)
+    scene.log_scale += log_scale_shift
     g = torch.Generator().manual_seed(100 + seed)
     cam = WL.make_camera(g, W, H, f, radius)
     pos, sc, q, op, shs = (t.cuda() for t in scene.activated())
@@ -80,3 +81,17 @@ def test_noalloc_rejects_sizes_beyond_its_limits():
     zi = torch.zeros(big, dtype=torch.int32, device="cuda")
     status, k, _, _ = call_noalloc(z2, z1, zi, zi, 64, 64, 16)
     assert status == PGB_ERR_INVALID and k == -1
+
+
+def test_noalloc_rejects_k_beyond_the_static_array():
+    """n within the limit, but K (large splats on a large image) beyond what
+    the rest of the static array holds: refused after phase one with K
+    reported, the caller's id buffer untouched even though it is big enough."""
+    uv, depth, rad, tiles, W, H = sort_inputs(1, 65536, 1024, 1024, 1024.0, 4.0,
+                                              log_scale_shift=3.0)
+    K = int(tiles[rad > 0].sum())
+    assert K > 2_000_000          # well past the ~1.0M entries the array holds
+    status, k, ids, rng = call_noalloc(uv, depth, rad, tiles, W, H, K)
+    assert status == PGB_ERR_OVERFLOW and k == K
+    assert bool((ids == -1).all())
+    assert bool((rng == -7).all())
