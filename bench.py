@@ -50,8 +50,8 @@ def parse_args():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--n", type=int, default=1_000_000, help="Gaussians (workload default 1M)")
-    ap.add_argument("--cpu-tile-stride", type=int, default=0,
-                    help="CPU sample: blend every k-th tile (0 = choose for ~10-30 s of CPU work)")
+    ap.add_argument("--cpu-budget", type=float, default=150.0,
+                    help="seconds of full CPU steps the reference arm may spend (at least one step)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-serve", action="store_true", help="skip the serving p50/p99 leg")
     ap.add_argument("--no-multiview", action="store_true",
@@ -109,7 +109,7 @@ class ClockSampler:
             os.close(fd)
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", "50"],
                 stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
         except Exception:
             self.proc = None
@@ -286,95 +286,147 @@ def load_peaks():
 
 
 # ------------------------------------------------------ CPU (the oracle) ---
-def cpu_step_time(scene, cam, target, tile_stride, threads):
-    """One float64 CPU training step of the oracle: the per-Gaussian operators
-    and their backward on all N Gaussians, the sort, and blending forward +
-    backward on every ``tile_stride``-th tile, the blending time scaled to all
-    tiles.  Returns (seconds per full step, details)."""
-    from oracle import msplat_cpu as O
+CPU_LRS = (1.6e-4, 5e-3, 1e-3, 5e-2, 2.5e-3, 1e-4, 1e-4, 1e-3)   # as make_optimizer
+
+
+class CpuStep:
+    """The training step in float64 on the host cores with the oracle's
+    operators: activations and normal, camera pose from its quaternion and
+    translation, SH colour, projection, covariance, EWA, the sort, blending
+    forward and backward over every tile, L1 + 0.2 L2 on all seven channels,
+    the backward to every Gaussian parameter and the camera, and the Adam
+    step (torch.optim.Adam, float64).  Nothing is sampled or scaled."""
+
+    def __init__(self, scene, cam, target, threads):
+        from pointrix_gb300 import workloads as WL
+
+        self.WL = WL
+        self.threads = threads
+        torch.set_num_threads(threads)
+        dt = torch.float64
+        self.leaves = [t.detach().to(dt).clone().requires_grad_(True) for t in
+                       (scene.position, scene.log_scale, scene.quat_raw, scene.opacity_logit,
+                        scene.shs)]
+        self.camq = rot_to_quat(cam.extr[:3, :3]).to(dt).requires_grad_(True)
+        self.camt = cam.extr[:3, 3].to(dt).clone().requires_grad_(True)
+        self.intr = cam.intr.to(dt).clone().requires_grad_(True)
+        self.W, self.H = cam.W, cam.H
+        self.target = target.to(dt)
+        params = self.leaves + [self.camq, self.camt, self.intr]
+        self.opt = torch.optim.Adam([{"params": [p], "lr": lr} for p, lr in zip(params, CPU_LRS)],
+                                    eps=1e-15)
+        # the blend's worker processes, started once (not part of a step);
+        # list capacity from the entries of the initial parameters
+        from oracle import msplat_cpu as O
+        from oracle.blend_pool import BlendPool
+        with torch.no_grad():
+            pos = self.leaves[0]
+            R = WL.rotation_from_unit_quat(self.camq / self.camq.norm())
+            extr = torch.cat([R, self.camt[:, None]], 1)
+            uv, depth = O.project_point(pos, self.intr, extr, cam.W, cam.H, nearest=0.2)
+            sc = torch.exp(self.leaves[1])
+            q = self.leaves[2] / self.leaves[2].norm(dim=1, keepdim=True)
+            cov = O.compute_cov3d(sc, q, depth != 0)
+            _, radius, nt = O.ewa_project(pos, cov, self.intr, extr, uv, cam.W, cam.H, depth != 0)
+            K = int(nt[radius > 0].sum())
+        self.pool = BlendPool(pos.shape[0], 7, int(1.3 * K) + 65536, cam.W, cam.H, self.target,
+                              workers=threads, scale=1.0 / self.target.numel())
+
+    def close(self):
+        self.pool.close()
+
+    def run(self):
+        """One step; returns (seconds, details)."""
+        from oracle import msplat_cpu as O
+
+        WL = self.WL
+        W, H = self.W, self.H
+        t0 = time.perf_counter()
+        self.opt.zero_grad(set_to_none=True)
+        pos, logs, qr, opl, shs = self.leaves
+        sc = torch.exp(logs)
+        q = qr / qr.norm(dim=1, keepdim=True)
+        op = torch.sigmoid(opl)
+        R = WL.rotation_from_unit_quat(self.camq / self.camq.norm())
+        extr = torch.cat([R, self.camt[:, None]], 1)
+        center = -(R.T @ self.camt)
+        d = pos - center[None]
+        d = d / d.norm(dim=1, keepdim=True)
+        rgb = (O.compute_sh(shs.permute(0, 2, 1), d) + 0.5).clamp(min=0)
+        uv, depth = O.project_point(pos, self.intr, extr, W, H, nearest=0.2)
+        vis = depth != 0
+        cov = O.compute_cov3d(sc, q, vis)
+        conic, radius, ntiles = O.ewa_project(pos, cov, self.intr, extr, uv, W, H, vis)
+        normal = WL.normals_from_scene(sc, q)
+        feat = torch.cat([rgb, depth, normal], 1)
+        t1 = time.perf_counter()
+        ids, rng = O.sort_gaussian(uv.detach(), depth.detach(), W, H, radius, ntiles)
+        t2 = time.perf_counter()
+        # blend forward and backward tile by tile (bounded memory), the
+        # tiles spread over worker processes on the host cores; then the
+        # chain's backward
+        loss, gu, gc, go, gf = self.pool.run(uv, conic, op, feat, ids, rng)
+        t3 = time.perf_counter()
+        torch.autograd.backward([uv, conic, op, feat], [gu, gc, go, gf])
+        t4 = time.perf_counter()
+        self.opt.step()
+        t5 = time.perf_counter()
+        return t5 - t0, {"preprocess_fwd_s": t1 - t0, "sort_s": t2 - t1,
+                         "blend_fwd_bwd_s": t3 - t2, "chain_backward_s": t4 - t3, "adam_s": t5 - t4, "K": int(ids.numel()),
+                         "tiles": int(rng.shape[0]), "loss": float(loss)}
+
+
+def cpu_timed_steps(args, budget_s):
+    """Full float64 CPU steps of the workload: one warm-up step when
+    ``args.warmup`` > 0, then timed steps until ``args.steps`` are done or
+    the next would end past ``budget_s`` (at least one).  Returns (mean s per
+    step, steps timed, warm-up steps run, threads, details of the last)."""
     from pointrix_gb300 import workloads as WL
 
-    torch.set_num_threads(threads)
-    dt = torch.float64
-    leaves = [t.detach().to(dt).requires_grad_(True) for t in
-              (scene.position, scene.log_scale, scene.quat_raw, scene.opacity_logit, scene.shs)]
-    intr = cam.intr.to(dt).requires_grad_(True)
-    extr = cam.extr[:3].to(dt).requires_grad_(True)
-    center = cam.center.to(dt)
-    W, H = cam.W, cam.H
-    gx, gy = O.tile_grid(W, H)
-    T = gx * gy
-    tiles = list(range(0, T, tile_stride))
-    t0 = time.perf_counter()
-    pos, logs, qr, opl, shs = leaves
-    sc = torch.exp(logs)
-    q = qr / qr.norm(dim=1, keepdim=True)
-    op = torch.sigmoid(opl)
-    d = pos - center[None]
-    d = d / d.norm(dim=1, keepdim=True)
-    rgb = (O.compute_sh(shs.permute(0, 2, 1), d) + 0.5).clamp(min=0)
-    uv, depth = O.project_point(pos, intr, extr, W, H, nearest=0.2)
-    vis = depth != 0
-    cov = O.compute_cov3d(sc, q, vis)
-    conic, radius, ntiles = O.ewa_project(pos, cov, intr, extr, uv, W, H, vis)
-    normal = WL.normals_from_scene(sc, q)
-    feat = torch.cat([rgb, depth, normal], 1)
-    t1 = time.perf_counter()
-    ids, rng = O.sort_gaussian(uv.detach(), depth.detach(), W, H, radius, ntiles)
-    t2 = time.perf_counter()
-    bl = [uv, conic, op, feat]
-    bl_in = [x.detach().requires_grad_(True) for x in bl]
-    img = O.alpha_blending(*bl_in, ids, rng, 0.0, W, H, tiles=tiles)
-    diff = img - target.to(dt)
-    loss = diff.abs().mean() + 0.2 * (diff * diff).mean()
-    t3 = time.perf_counter()
-    grads = torch.autograd.grad(loss, bl_in)
-    t4 = time.perf_counter()
-    torch.autograd.backward(bl, grads)
-    t5 = time.perf_counter()
-    blend = (t3 - t2) + (t4 - t3)
-    full = (t1 - t0) + (t2 - t1) + blend * (T / len(tiles)) + (t5 - t4)
-    return full, {"preprocess_fwd_s": t1 - t0, "sort_s": t2 - t1, "blend_sample_s": blend,
-                  "preprocess_bwd_s": t5 - t4, "tiles_sampled": len(tiles), "tiles": T,
-                  "K": int(ids.numel())}
+    scene, cam = WL.scene_train_view(1, n=args.n)
+    g = torch.Generator().manual_seed(7)
+    target = torch.rand(7, cam.H, cam.W, generator=g)
+    threads = len(os.sched_getaffinity(0))
+    step = CpuStep(scene, cam, target, threads)
+    try:
+        t_start = time.perf_counter()
+        warm = 0
+        if args.warmup > 0:
+            step.run()
+            warm = 1
+        times, det = [], {}
+        while len(times) < max(1, args.steps):
+            s, det = step.run()
+            times.append(s)
+            if time.perf_counter() - t_start + statistics.mean(times) > budget_s:
+                break
+    finally:
+        step.close()
+    return statistics.mean(times), len(times), warm, threads, det
 
 
-def choose_stride(T):
-    # about 1/48 of the tiles keeps one CPU step near 10-20 s on 8-16 cores
-    return max(1, T // 140)
+def cpu_sample_string(n, steps, warm):
+    return (f"float64 oracle training step on the host cores, all {n} Gaussians and all tiles "
+            f"(nothing sampled or scaled): activations, camera pose, SH colour, projection, EWA, "
+            f"sort, blend fwd+bwd over every tile, L1+0.2*L2, backward, Adam; "
+            f"{steps} timed full step(s) after {warm} warm-up step(s)")
 
 
 def run_reference(args):
     world, rank, _ = dist_env()
     if rank != 0:
         return
-    from pointrix_gb300 import workloads as WL
-
-    scene, cam = WL.scene_train_view(1, n=args.n)
-    g = torch.Generator().manual_seed(7)
-    target = torch.rand(7, cam.H, cam.W, generator=g)
-    T = ((cam.W + 15) // 16) * ((cam.H + 15) // 16)
-    stride = args.cpu_tile_stride or choose_stride(T)
-    threads = len(os.sched_getaffinity(0))
-    for _ in range(args.warmup):
-        cpu_step_time(scene, cam, target, stride, threads)
-    times = []
-    for _ in range(args.steps):
-        s, det = cpu_step_time(scene, cam, target, stride, threads)
-        times.append(s)
-    sec = statistics.mean(times)
+    sec, steps, warm, threads, det = cpu_timed_steps(args, budget_s=args.cpu_budget)
     value = 1.0 / sec
-    sample = (f"float64 oracle step: all {args.n} Gaussians through the per-Gaussian operators and the sort; "
-              f"blending fwd+bwd on every {stride}-th tile ({det['tiles_sampled']} of {det['tiles']}), "
-              f"blending time scaled to all tiles")
     print(json.dumps({
         "impl": "reference", "metric": METRIC, "value": value, "unit": "iters/s", "n_gpus": args.gpus,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": sec * 1e3, "higher_is_better": True,
+        "steps": steps, "warmup": warm, "steps_requested": args.steps,
+        "warmup_requested": args.warmup, "ms_per_step": sec * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
-        "config": {"workload": WORKLOAD, "gaussians": args.n, "width": cam.W, "height": cam.H,
+        "config": {"workload": WORKLOAD, "gaussians": args.n, "width": 1600, "height": 1060,
                    "channels": 7, "sh_degree": 3, "parallelism": "cpu, host cores"},
         "cpu_baseline": {"value": value, "unit": "iters/s", "cores": threads, "kind": "port",
-                         "sample": sample, "detail": det},
+                         "sample": cpu_sample_string(args.n, steps, warm), "detail": det},
         "e2e": {"value": value, "unit": "iters/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }), flush=True)
 
@@ -593,7 +645,148 @@ def serve_measure(device, rates=(100, 400, 1000), duration=1.5):
     return {"workload": SERVE_WORKLOAD, "duration_s": duration, "rates": out}
 
 
+# ------------------------------------------------------------ roofline ---
+# FP32 operations per composited (pixel, splat) pair, C channels (an FMA
+# counts two).  Forward: dy, the base-2 power (two FMAs), alpha = min(0.99,
+# o 2^p), T (1 - alpha), alpha T, C feature FMAs: 9 + 2C.  Backward: dy,
+# power, g0 and g1 (two FMAs), alpha, 1 - alpha, T / (1 - alpha), F = sum
+# dout f (C FMAs), the feature gradients (C FMAs), dalpha, the SB update,
+# dpow and the six moment FMAs: 35 + 4C.  The exponential is on the SFU and
+# not counted.
+def fwd_flop_per_pair(C):
+    return 9 + 2 * C
+
+
+def bwd_flop_per_pair(C):
+    return 35 + 4 * C
+
+
+def fp32_peak_tflops(sm_mhz):
+    """152 SMs x 128 FP32 lanes x 2 (FMA) at the given SM clock."""
+    return 152 * 128 * 2 * sm_mhz * 1e6 / 1e12
+
+
+def issue_peak(sm_mhz):
+    """Warp instructions per second: 152 SMs x 4 schedulers x 1 per cycle."""
+    return 152 * 4 * sm_mhz * 1e6
+
+
+def blend_census(scene, camp, W, H):
+    """(evaluated, composited) (pixel, splat) pairs of the step's blend, on
+    the device (``ops.blend_pair_census``), outside the timed region."""
+    from pointrix_gb300 import ops
+    with torch.no_grad():
+        pos, sc, q, op, shs = scene.activated()
+        E = camp.pose()[0][:3]
+        uv, depth = ops.project_point(pos, camp.intr, E, W, H)
+        vis = depth != 0
+        cov = ops.compute_cov3d(sc, q, vis)
+        conic, radius, tiles = ops.ewa_project(pos, cov, camp.intr, E, uv, W, H, vis)
+        ids, rng = ops.sort_gaussian(uv, depth, W, H, radius, tiles)
+        feat = torch.zeros(pos.shape[0], 7, device=pos.device)
+        return ops.blend_pair_census(uv, conic, op, feat, ids, rng, W, H)
+
+
+def hbm_bytes(n, K, T, W, H, params):
+    """Algorithmic bytes per launch of the HBM-streaming kernels of the step
+    (each input and output once; n Gaussians, K list entries, T tiles)."""
+    pix = W * H
+    passes = 1 if T <= 256 else 2
+    return {
+        "gaussian_activate_fwd": 76 * n, "gaussian_activate_bwd": 108 * n,
+        "sh_rgb_fwd": 216 * n, "sh_rgb_bwd": 420 * n,
+        "preprocess_fwd": 72 * n, "preprocess_bwd": 104 * n,
+        "sort_begin": n * (12 + 8 + 4 * 16),
+        "sort_finish": n * 28 + K * (8 + passes * 16 + 4) + T * 8,
+        "l1_l2_loss_fwd": 8 * 7 * pix, "l1_l2_loss_bwd": 12 * 7 * pix,
+        "adam_step": 28 * params,
+    }
+
+
+def blend_roofline(scene, camp, W, H, n, K, T, per_op, clk):
+    """The dominant kernel's roofline.  The blend kernels are bound by
+    instruction issue and the FP32 pipe, not by HBM (their DRAM traffic is a
+    few percent of peak): ``achieved`` is FP32 work per second (composited
+    pairs x FLOP per pair / live launch time) against the FP32 peak at the
+    measured SM clock; ``issue`` is the warp-instruction rate (instructions
+    per launch from the committed ncu capture / live launch time) against
+    the issue peak.  ``hbm_kernels`` gives the HBM-streaming kernels against
+    the copy bandwidth."""
+    peaks, peak_kind = load_peaks()
+    hbm_peak = float(peaks.get("hbm_gbs", PEAKS_FALLBACK["hbm_gbs"]))
+    mhz = float(clk.get("sm_mhz") or 2070.0)
+    try:
+        with open(os.path.join(ROOT, "profiles", "dram_traffic.json")) as f:
+            prof = json.load(f)
+    except Exception:
+        prof = {}
+    traffic = prof.get("bytes_per_launch", {})
+    insts = prof.get("warp_instructions_per_launch", {})
+    ev, comp = blend_census(scene, camp, W, H)
+    fp32_peak = fp32_peak_tflops(mhz)
+    kern = {}
+    for name, flop in (("alpha_blending_fwd", fwd_flop_per_pair(7)),
+                       ("alpha_blending_bwd", bwd_flop_per_pair(7))):
+        if name not in per_op:
+            continue
+        t = per_op[name] * 1e-3
+        ach = flop * comp / t / 1e12
+        entry = {"launch_ms": per_op[name], "flop_per_composited_pair": flop,
+                 "achieved_tflops": ach, "fp32_peak_tflops": fp32_peak, "fp32_frac": ach / fp32_peak,
+                 "pairs_per_ns": comp / t * 1e-9, "dram_bytes_per_launch": traffic.get(name)}
+        if insts.get(name):
+            rate = insts[name] / t
+            entry.update({"warp_instructions_per_launch": insts[name],
+                          "issue_rate": rate, "issue_peak": issue_peak(mhz),
+                          "issue_frac": rate / issue_peak(mhz)})
+        kern[name] = entry
+    params = sum(p.numel() for p in (scene.position, scene.log_scale, scene.quat_raw,
+                                     scene.opacity_logit, scene.shs)) + 11
+    hbm = []
+    for name, b in hbm_bytes(n, K, T, W, H, params).items():
+        if name in per_op:
+            gbs = b / (per_op[name] * 1e-3) / 1e9
+            hbm.append({"kernel": name, "launch_ms": round(per_op[name], 4), "bytes": b,
+                        "achieved_gbs": round(gbs, 1), "frac": round(gbs / hbm_peak, 3)})
+    dom = "alpha_blending_bwd" if "alpha_blending_bwd" in kern else next(iter(kern), None)
+    d = kern.get(dom, {})
+    return {"bound": "fp32/issue", "kernel": dom,
+            "achieved": d.get("achieved_tflops"), "peak": fp32_peak, "unit": "TFLOP/s",
+            "frac": d.get("fp32_frac"), "traffic": d.get("dram_bytes_per_launch"),
+            "peak_source": f"derived: 152 SMs x 128 FP32 lanes x 2 at the measured {mhz:.0f} MHz",
+            "issue_frac": d.get("issue_frac"),
+            "pairs": {"evaluated": ev, "composited": comp},
+            "blend": kern, "hbm_kernels": hbm, "hbm_peak_gbs": hbm_peak, "hbm_peak_source": peak_kind}
+
+
 # ------------------------------------------------------------- GPU arm ---
+class StepState:
+    """A copy of everything a training step updates -- the Gaussian and
+    camera parameters and Adam's moments and device step counts -- restored
+    in place (the captured graph keeps its buffers) before each measured
+    phase, so that the eager, graph-replay and end-to-end timings all start
+    from the same scene: the scene drifts as it trains, and an unreset run
+    would time a different workload in each phase."""
+
+    def __init__(self, scene, camp, optimizer):
+        self.tensors = [scene.position, scene.log_scale, scene.quat_raw, scene.opacity_logit,
+                        scene.shs, *camp.leaves()]
+        for p in list(self.tensors):
+            st = optimizer.state.get(p, {})
+            self.tensors += [st[k] for k in ("exp_avg", "exp_avg_sq") if k in st]
+        for name in ("_count_all", "_steps_dev"):
+            t = getattr(optimizer, name, None)
+            if t is not None:
+                self.tensors.append(t)
+        with torch.no_grad():
+            self.saved = [t.detach().clone() for t in self.tensors]
+
+    def restore(self):
+        with torch.no_grad():
+            for t, v in zip(self.tensors, self.saved):
+                t.copy_(v)
+
+
 def run_gb300(args):
     world, rank, local = dist_env()
     dist_init(world, "nccl")
@@ -625,12 +818,14 @@ def run_gb300(args):
     # the sort keeps K on the device from here on: lists sized for a capacity
     # above the K of this camera, so that no step synchronises with the host
     renderer.cfg.sort_capacity = int(1.25 * count_entries(scene, camp, W, H)) + 65536
+    state = StepState(scene, camp, optimizer)
 
     # -- eager launches (same kernels as the graph): per-operator CUDA-event
     #    times for the roofline, and the launch count
     barrier(world)
     torch.cuda.synchronize(device)
     start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    state.restore()
     with ops.kernel_timing() as kt:
         start.record(stream)
         for _ in range(args.steps):
@@ -645,6 +840,7 @@ def run_gb300(args):
     graphed = GraphedStep(step, warmup=2, device=device)
     for _ in range(max(3, args.warmup)):
         graphed()
+    state.restore()
     torch.cuda.synchronize(device)
     with ClockSampler(device.index) as clocks:
         barrier(world)
@@ -665,6 +861,7 @@ def run_gb300(args):
     #    stream while step i computes (two staging buffers, event-ordered);
     #    the host reads each step's loss one step later, as a training loop
     #    that logs asynchronously does.  Every copy is inside the timed region.
+    state.restore()       # the camera copied in each step is the starting camera
     target_host = target_cpu.pin_memory()
     cam_host = [t.detach().cpu().pin_memory() for t in camp.leaves()]
     h2d = target_host.numel() * 4 + sum(t.numel() * 4 for t in cam_host)
@@ -687,6 +884,7 @@ def run_gb300(args):
                 dst.copy_(src, non_blocking=True)
             ready[b].record(copy_stream)
 
+    state.restore()
     barrier(world)
     torch.cuda.synchronize(device)
     t0 = time.perf_counter()
@@ -714,28 +912,12 @@ def run_gb300(args):
 
     # -- dominant kernel and its roofline (live CUDA-event durations)
     per_op = {name: statistics.mean(kt.ms(name)) for name in kt.names()}
-    calls = {name: len(kt.ms(name)) // args.steps for name in kt.names()}
-    dom = max(per_op, key=lambda k: per_op[k] * calls[k])
+    state.restore()       # the roofline's counts are taken on the starting scene
     K = count_entries(scene, camp, W, H)
     T = ((W + 15) // 16) * ((H + 15) // 16)
     n = args.n
-    algo = {"alpha_blending_fwd": blend_fwd_bytes(n, 7, K, T, W, H),
-            "alpha_blending_bwd": blend_bwd_bytes(n, 7, K, T, W, H),
-            "sort_finish": sort_bytes(n, K, T)}
-    traffic = None
-    try:
-        with open(os.path.join(ROOT, "profiles", "dram_traffic.json")) as f:
-            traffic = json.load(f)["bytes_per_launch"]
-    except Exception:
-        traffic = {}
-    peaks, peak_kind = load_peaks()
-    hbm_peak = float(peaks.get("hbm_gbs", PEAKS_FALLBACK["hbm_gbs"]))
-    dom_bytes = algo.get(dom)
-    achieved = dom_bytes / (per_op[dom] * 1e-3) / 1e9 if dom_bytes else None
-    roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-                "frac": (achieved / hbm_peak) if achieved else None, "traffic": traffic.get(dom),
-                "peak_source": peak_kind, "launch_ms": per_op[dom],
-                "algorithmic_bytes_per_launch": dom_bytes}
+    clk = clocks.summary()
+    roofline = blend_roofline(scene, camp, W, H, n, K, T, per_op, clk)
 
     serving = recompute = None
     if rank == 0 and not args.no_serve:
@@ -749,14 +931,11 @@ def run_gb300(args):
     if rank == 0:
         cpu = None
         if world == 1 and not args.no_cpu_baseline:
-            stride = args.cpu_tile_stride or choose_stride(T)
-            threads = len(os.sched_getaffinity(0))
-            sec, det = cpu_step_time(scene_cpu, cam, target_cpu, stride, threads)
+            # one full, unsampled float64 step
+            cargs = argparse.Namespace(n=n, steps=1, warmup=0)
+            sec, steps_c, warm_c, threads, det = cpu_timed_steps(cargs, budget_s=0.0)
             cpu = {"value": 1.0 / sec, "unit": "iters/s", "cores": threads, "kind": "port",
-                   "sample": (f"one float64 oracle step: all Gaussians through the per-Gaussian operators "
-                              f"and the sort; blending fwd+bwd on every {stride}-th tile "
-                              f"({det['tiles_sampled']} of {det['tiles']}), scaled to all tiles"),
-                   "detail": det}
+                   "sample": cpu_sample_string(n, steps_c, warm_c), "detail": det}
         line = {
             "metric": METRIC, "value": value, "unit": "iters/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
@@ -774,7 +953,7 @@ def run_gb300(args):
             "roofline": roofline,
             "per_op_ms": {k: round(v, 4) for k, v in per_op.items()},
             "gpu_launches": kt.total_launches(),
-            "clocks": clocks.summary(),
+            "clocks": clk,
             "cpu_baseline": cpu,
             "serve": serving,
             "recompute": recompute,

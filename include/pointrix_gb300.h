@@ -313,6 +313,17 @@ int pgb_alpha_blending_backward_views_with_batch(
     float* d_conic, float* d_opacity, float* d_feature, int64_t* info, void* stream, int batch);
 int pgb_blend_batches(int backward, int32_t* out);
 
+/* pgb_blend_pair_census -- no counterpart in the reference: a measurement
+ * aid, not part of the training path.  For the blend a forward call made
+ * (its records, sorted ids, tile ranges and n_contrib [H,W]), adds to
+ * counts[0] (device, uint64) the list entries up to each pixel's last
+ * contributor -- the (pixel, splat) pairs the backward replays -- and to
+ * counts[1] the composited ones among them (alpha >= 1/255 by the forward's
+ * own test on the record).  The caller zeroes counts.  One launch. */
+int pgb_blend_pair_census(const float* records, int channels, int64_t n, const int32_t* ids,
+                          int64_t k, const int32_t* tile_range, int width, int height,
+                          const int32_t* n_contrib, unsigned long long* counts, void* stream);
+
 /* Camera pose (the camera model around the path,
  * pointrix/utils/pose.py:40-84): world_to_camera [4,4] row-major and the
  * camera centre [3] from a wxyz quaternion [4] (normalised) and a

@@ -67,6 +67,8 @@ RADIUS_CAP = 1048576.0
 ALPHA_MAX = 0.99
 ALPHA_MIN = 1.0 / 255.0
 T_MIN = 1e-4
+# splats per step of the oracle's blend loop over a tile's list
+BLEND_CHUNK = 256
 
 # Real spherical-harmonic normalisation constants, from their closed forms.
 SH_C0 = 0.5 / math.sqrt(math.pi)
@@ -348,6 +350,64 @@ def sort_gaussian(uv, depth, W, H, radius, tiles_touched):
 # ---------------------------------------------------------------------------
 # alpha_blending  (call site pointrix/model/renderer/msplat.py:148-151)
 # ---------------------------------------------------------------------------
+def _tile_pixels(t, W, H):
+    """Pixel coordinates (x, y) and flat indices of tile ``t``, row-major."""
+    gx, _ = tile_grid(W, H)
+    ly, lx = torch.meshgrid(torch.arange(TILE), torch.arange(TILE), indexing="ij")
+    pxi = (t % gx) * TILE + lx.reshape(-1)
+    pyi = (t // gx) * TILE + ly.reshape(-1)
+    inside = (pxi < W) & (pyi < H)
+    pxi, pyi = pxi[inside], pyi[inside]
+    return pxi, pyi, pyi * W + pxi
+
+
+def blend_tile(uv, conic, opacity, feature, g, pxi, pyi):
+    """One tile's compositing: the pixels (pxi, pyi) over the depth-sorted
+    splats ``g`` (indices into the per-Gaussian inputs).  Returns
+    (colour [P,C] before the background, final T [P], index of the last
+    contributor in ``g`` [P], -1 for none); differentiable in the inputs.
+
+    The list is walked in chunks of BLEND_CHUNK, the transmittance carried
+    across chunks; the walk stops once every pixel has stopped (nothing later
+    in the list can contribute)."""
+    dt = feature.dtype
+    C = feature.shape[1]
+    amin, amax, tmin = _s(ALPHA_MIN, feature), _s(ALPHA_MAX, feature), _s(T_MIN, feature)
+    half = _s(0.5, feature)
+    pxf = pxi.to(dt)[:, None]
+    pyf = pyi.to(dt)[:, None]
+    P = pxi.numel()
+    Tprev = torch.ones(P, dtype=dt)
+    col = torch.zeros(P, C, dtype=dt)
+    last = torch.full((P,), -1, dtype=torch.long)
+    Tf = torch.ones(P, dtype=dt)
+    n = g.numel()
+    for c0 in range(0, n, BLEND_CHUNK):
+        gc = g[c0:c0 + BLEND_CHUNK]
+        dx = uv[gc, 0].to(dt)[None, :] - pxf
+        dy = uv[gc, 1].to(dt)[None, :] - pyf
+        ca, cb, cc = (conic[gc, i].to(dt)[None, :] for i in range(3))
+        power = -half * (ca * dx * dx + cc * dy * dy) - cb * dx * dy
+        o = opacity.reshape(-1)[gc].to(dt)[None, :]
+        alpha = torch.minimum(amax, o * torch.exp(power))
+        valid = (power <= 0) & (alpha >= amin)
+        a_v = torch.where(valid, alpha, torch.zeros_like(alpha))
+        Tinc = Tprev[:, None] * torch.cumprod(1.0 - a_v, dim=1)
+        Texc = torch.cat([Tprev[:, None], Tinc[:, :-1]], dim=1)
+        incl = valid & (Tinc.detach() >= tmin)
+        w = torch.where(incl, a_v * Texc, torch.zeros_like(a_v))
+        col = col + w @ feature[gc].to(dt)
+        idx = torch.arange(c0, c0 + gc.numel())[None, :].expand_as(incl)
+        lastc = torch.where(incl, idx, torch.full_like(idx, -1)).max(dim=1).values
+        has = lastc >= 0
+        Tf = torch.where(has, Tinc.gather(1, (lastc - c0).clamp(min=0)[:, None])[:, 0], Tf)
+        last = torch.where(has, lastc, last)
+        Tprev = Tinc[:, -1]
+        if bool((Tprev.detach() < tmin).all()):
+            break
+    return col, Tf, last
+
+
 def alpha_blending(uv, conic, opacity, feature, ids, tile_range, bg, W, H,
                    tiles=None, return_state=False):
     """Front-to-back compositing of ``feature`` [N,C] over 16x16 tiles.
@@ -356,7 +416,7 @@ def alpha_blending(uv, conic, opacity, feature, ids, tile_range, bg, W, H,
     transmittance [H,W] and the per-pixel count of list entries up to and
     including the last contributor [H,W].  ``tiles`` restricts the work to a
     subset of tile ids (the rest of the image is left at ``bg``), which the
-    CPU baseline uses to time a bounded sample.
+    tests use to check sampled tiles of a full-size view.
 
     Differentiable (torch autograd) in uv, conic, opacity and feature.
     """
@@ -368,46 +428,14 @@ def alpha_blending(uv, conic, opacity, feature, ids, tile_range, bg, W, H,
     out = torch.full((C, H * W), float(bg), dtype=dt)
     finalT = torch.ones(H * W, dtype=dt)
     ncon = torch.zeros(H * W, dtype=torch.int32)
-    ly, lx = torch.meshgrid(torch.arange(TILE), torch.arange(TILE), indexing="ij")
-    ly, lx = ly.reshape(-1), lx.reshape(-1)
-    pieces, pix_all = [], []
-    tile_list = range(gx * gy) if tiles is None else tiles
-    amin, amax, tmin = _s(ALPHA_MIN, feature), _s(ALPHA_MAX, feature), _s(T_MIN, feature)
-    half = _s(0.5, feature)
-    for t in tile_list:
+    pieces = []
+    for t in (range(gx * gy) if tiles is None else tiles):
         t = int(t)
-        tx, ty = t % gx, t // gx
-        pxi = tx * TILE + lx
-        pyi = ty * TILE + ly
-        inside = (pxi < W) & (pyi < H)
-        pxi, pyi = pxi[inside], pyi[inside]
-        pix = pyi * W + pxi
         s, e = int(rng[t, 0]), int(rng[t, 1])
         if e <= s:
             continue
-        g = ids[s:e]
-        pxf = pxi.to(dt)[:, None]
-        pyf = pyi.to(dt)[:, None]
-        dx = uv[g, 0].to(dt)[None, :] - pxf
-        dy = uv[g, 1].to(dt)[None, :] - pyf
-        ca, cb, cc = (conic[g, i].to(dt)[None, :] for i in range(3))
-        power = -half * (ca * dx * dx + cc * dy * dy) - cb * dx * dy
-        o = opacity.reshape(-1)[g].to(dt)[None, :]
-        alpha = torch.minimum(amax, o * torch.exp(power))
-        valid = (power <= 0) & (alpha >= amin)
-        a_v = torch.where(valid, alpha, torch.zeros_like(alpha))
-        om = 1.0 - a_v
-        Tinc = torch.cumprod(om, dim=1)
-        Texc = torch.cat([torch.ones_like(Tinc[:, :1]), Tinc[:, :-1]], dim=1)
-        incl = valid & (Tinc.detach() >= tmin)
-        w = torch.where(incl, a_v * Texc, torch.zeros_like(a_v))
-        col = w @ feature[g].to(dt)                               # [P,C]
-        n = e - s
-        idx = torch.arange(n)[None, :].expand_as(incl)
-        last = torch.where(incl, idx, torch.full_like(idx, -1)).max(dim=1).values
-        Tf = torch.where(last[:, None] >= 0,
-                         Tinc.gather(1, last.clamp(min=0)[:, None]),
-                         torch.ones_like(Tinc[:, :1]))[:, 0]
+        pxi, pyi, pix = _tile_pixels(t, W, H)
+        col, Tf, last = blend_tile(uv, conic, opacity, feature, ids[s:e], pxi, pyi)
         pieces.append((pix, col + Tf[:, None] * bg, Tf))
         ncon[pix] = (last + 1).to(torch.int32)
     if pieces:
@@ -420,6 +448,64 @@ def alpha_blending(uv, conic, opacity, feature, ids, tile_range, bg, W, H,
     if return_state:
         return out, finalT.reshape(H, W), ncon.reshape(H, W)
     return out
+
+
+def blend_loss_grad(uv, conic, opacity, feature, ids, tile_range, bg, W, H, pixel_loss,
+                    workers=1):
+    """The blend and the gradient of a per-pixel loss, tile by tile, in
+    bounded memory (a full-size view's autograd graph over all tiles would
+    not fit): each tile is composited with autograd on copies of its splats'
+    inputs, its share of the loss is back-propagated at once and the
+    gradients are summed into per-Gaussian buffers.  ``pixel_loss(img [C,P],
+    pix [P])`` returns that tile's scalar share (the loss must be a sum over
+    pixels).  ``workers`` threads take tiles in turn.  Returns (loss,
+    image [C,H,W], d_uv, d_conic, d_opacity, d_feature), all detached."""
+    import threading
+    from concurrent.futures import ThreadPoolExecutor
+
+    dt = feature.dtype
+    C = feature.shape[1]
+    gx, gy = tile_grid(W, H)
+    ids = ids.long()
+    rng = tile_range.long()
+    U, Cn, Op, F = (x.detach() for x in (uv, conic, opacity.reshape(-1, 1), feature))
+    grads = [torch.zeros_like(x) for x in (U, Cn, Op, F)]
+    out = torch.full((C, H * W), float(bg), dtype=dt)
+    lock = threading.Lock()
+    total = [0.0]
+
+    def one(t):
+        s, e = int(rng[t, 0]), int(rng[t, 1])
+        pxi, pyi, pix = _tile_pixels(t, W, H)
+        if e <= s:
+            with torch.no_grad():
+                img = torch.full((C, pix.numel()), float(bg), dtype=dt)
+            loss = pixel_loss(img, pix)
+            with lock:
+                total[0] += float(loss)
+            return
+        g = ids[s:e]               # a splat is listed at most once per tile
+        leaves = [x[g].clone().requires_grad_(True) for x in (U, Cn, Op, F)]
+        col, Tf, _ = blend_tile(*leaves, torch.arange(g.numel()), pxi, pyi)
+        img = (col + Tf[:, None] * bg).t()
+        loss = pixel_loss(img, pix)
+        gl = torch.autograd.grad(loss, leaves, allow_unused=True)
+        with lock:
+            total[0] += float(loss.detach())
+            out[:, pix] = img.detach()
+            for buf, gr in zip(grads, gl):
+                if gr is not None:
+                    buf.index_add_(0, g, gr)
+
+    tiles = range(gx * gy)
+    if workers > 1:
+        with ThreadPoolExecutor(workers) as ex:
+            list(ex.map(one, tiles))
+    else:
+        for t in tiles:
+            one(t)
+    return (total[0], out.reshape(C, H, W), grads[0], grads[1], grads[2].reshape(opacity.shape),
+            grads[3])
 
 
 def threshold_pixels(uv, conic, opacity, ids, tile_range, W, H, tiles=None,

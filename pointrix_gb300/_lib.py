@@ -57,6 +57,7 @@ SIGNATURES = {
     "pgb_alpha_blending_backward_views_with_batch": [vp, i64, i32, vp, i64, vp, f32, vp, i32, vp, vp, vp,
                                                      vp, vp, vp, vp, vp, vp, vp, i32],
     "pgb_blend_batches": [i32, vp],
+    "pgb_blend_pair_census": [vp, i32, i64, vp, i64, vp, i32, i32, vp, vp, vp],
     "pgb_alpha_blending_forward_pieces": [vp, vp, vp, vp, vp, i32, i64, vp, i64, vp, f32, i32, i32,
                                           vp, vp, vp, vp, vp, vp, i32],
     "pgb_alpha_blending_backward_pieces": [vp, i64, vp, i32, vp, i64, vp, f32, i32, i32, vp, vp, vp,

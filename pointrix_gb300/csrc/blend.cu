@@ -721,6 +721,51 @@ __global__ void unpack_kernel(const float* __restrict__ g, int64_t n, int C,
   }
 }
 
+// ---------------------------------------------------------------- census
+// The work of one blend, counted for the benchmark's roofline (not on the
+// training path): per pixel, the list entries up to its last contributor
+// (the pairs the backward replays) and, among them, the composited ones
+// (the forward's own alpha test on the record, bit for bit).  One thread per
+// pixel of a tile; warp sums, then one 64-bit atomic per warp and counter.
+template <int RF>
+__global__ void __launch_bounds__(256) census_kernel(const float* __restrict__ records,
+                                                     const int32_t* __restrict__ ids,
+                                                     const int2* __restrict__ ranges, int64_t n,
+                                                     const ViewTable vt,
+                                                     const int32_t* __restrict__ n_contrib,
+                                                     unsigned long long* __restrict__ counts) {
+  const int tile = blockIdx.x;
+  int W, H, gx, ltile;
+  int64_t pbase;
+  tile_view(vt, tile, W, H, gx, ltile, pbase);
+  const int px = (ltile % gx) * kTile + (threadIdx.x & (kTile - 1));
+  const int py = (ltile / gx) * kTile + (threadIdx.x / kTile);
+  unsigned long long evaluated = 0, composited = 0;
+  if (px < W && py < H) {
+    const int2 rg = ranges[tile];
+    const int m = min(n_contrib[pbase + (int64_t)py * W + px], max(0, rg.y - rg.x));
+    evaluated = (unsigned long long)max(m, 0);
+    const float pxf = (float)px, pyf = (float)py;
+    for (int j = 0; j < m; ++j) {
+      const int32_t g = ids[rg.x + j];
+      if (g < 0 || (int64_t)g >= n) continue;
+      const float* rec = records + (int64_t)g * RF;
+      const SplatX sx = splat_x(rec[2], rec[3], __fsub_rn(rec[0], pxf));
+      const float p2 = splat_power2(sx, rec[4], __fsub_rn(rec[1], pyf));
+      if (!(p2 > 0.f || p2 < rec[7])) ++composited;
+    }
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    evaluated += __shfl_xor_sync(0xffffffffu, evaluated, o);
+    composited += __shfl_xor_sync(0xffffffffu, composited, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicAdd(&counts[0], evaluated);
+    atomicAdd(&counts[1], composited);
+  }
+}
+
 // ------------------------------------------------------------- dispatch
 template <int NC, int B>
 static int launch_fwd_b(const float* records, const int32_t* ids, const int2* ranges, int64_t n,
@@ -1044,6 +1089,32 @@ int pgb_alpha_blending_backward_pieces(const float* records, int64_t n, const in
                              single_view(width, height), grid_x(width) * grid_y(height), final_T,
                              n_contrib, d_out, grad_records, d_uv, d_conic, d_opacity, gc, info,
                              stream, batch);
+}
+
+// Pair census of a blend (no msplat counterpart): counts[0] += list entries
+// up to each pixel's last contributor, counts[1] += the composited ones.
+int pgb_blend_pair_census(const float* records, int channels, int64_t n, const int32_t* ids,
+                          int64_t k, const int32_t* tile_range, int width, int height,
+                          const int32_t* n_contrib, unsigned long long* counts, void* stream) {
+  const int nc = nc_bucket(channels);
+  if (width <= 0 || height <= 0 || n < 0 || k < 0 || channels < 1 || nc < 0) return PGB_ERR_INVALID;
+  if (!tile_range || !n_contrib || !counts || (k > 0 && !ids) || (n > 0 && !records))
+    return PGB_ERR_INVALID;
+  if (misaligned(records, 16) || misaligned(tile_range, 8) || misaligned(counts, 8))
+    return PGB_ERR_INVALID;
+  const ViewTable vt = single_view(width, height);
+  const int tiles = grid_x(width) * grid_y(height);
+  const int2* rg = reinterpret_cast<const int2*>(tile_range);
+  cudaStream_t s = as_stream(stream);
+  switch (rec_floats(nc)) {
+    case 12: census_kernel<12><<<tiles, 256, 0, s>>>(records, ids, rg, n, vt, n_contrib, counts); break;
+    case 16: census_kernel<16><<<tiles, 256, 0, s>>>(records, ids, rg, n, vt, n_contrib, counts); break;
+    case 20: census_kernel<20><<<tiles, 256, 0, s>>>(records, ids, rg, n, vt, n_contrib, counts); break;
+    case 24: census_kernel<24><<<tiles, 256, 0, s>>>(records, ids, rg, n, vt, n_contrib, counts); break;
+    case 36: census_kernel<36><<<tiles, 256, 0, s>>>(records, ids, rg, n, vt, n_contrib, counts); break;
+    default: return PGB_ERR_INVALID;
+  }
+  return launch_status();
 }
 
 // Batch sizes compiled for the forward (backward = 0) or the backward (1).

@@ -828,3 +828,21 @@ def alpha_blending(uv, conic, opacity, feature, gaussian_ids_sorted, tile_range,
     """
     return alpha_blending_with_state(uv, conic, opacity, feature, gaussian_ids_sorted, tile_range,
                                      bg, W, H, ndc)[0]
+
+
+def blend_pair_census(uv, conic, opacity, feature, gaussian_ids_sorted, tile_range, W, H):
+    """(evaluated, composited): the (pixel, splat) pairs of this blend up to
+    each pixel's last contributor, and the composited ones among them
+    (``pgb_blend_pair_census``).  A measurement aid for the benchmark's
+    roofline: runs one forward to get the records and contributor counts."""
+    ids = _c(gaussian_ids_sorted.to(torch.int32))
+    rng = _c(tile_range.to(torch.int32))
+    with torch.no_grad():
+        records, _, _, ncon = _blend_forward_raw(uv.detach(), conic.detach(), opacity.detach(),
+                                                 feature.detach(), ids, rng, 0.0, W, H)
+    counts = torch.zeros(2, dtype=torch.int64, device=records.device)
+    call("pgb_blend_pair_census", _ptr(records), int(feature.shape[1]), int(records.shape[0]),
+         _ptr(ids), int(ids.numel()), _ptr(rng), int(W), int(H), _ptr(ncon), _ptr(counts),
+         _stream(records.device))
+    c = counts.tolist()
+    return int(c[0]), int(c[1])

@@ -423,3 +423,33 @@ def test_alpha_blending_pieces_matches_concatenation(small):
     with pytest.raises(ValueError):
         ops.alpha_blending_pieces(p.uv, p.conic, p.op, [], p.ids, p.rng, 0.0, p.W, p.H)
     ops.check_device_status()
+
+
+def test_blend_pair_census_counts_the_replayed_and_composited_pairs(small):
+    """The measurement aid behind the benchmark's blend roofline: evaluated
+    pairs = the sum of the contributor counts; composited pairs = the
+    oracle's count of list entries before each pixel's last contributor
+    that pass the alpha test (float64; threshold pairs may differ)."""
+    p = small
+    ev, comp = ops.blend_pair_census(p.uv, p.conic, p.op, p.feat, p.ids, p.rng, p.W, p.H)
+    _, _, nc = ops.alpha_blending_with_state(p.uv, p.conic, p.op, p.feat, p.ids, p.rng, 0.0, p.W, p.H)
+    assert ev == int(nc.long().sum())
+    u, c, o, _ = blend_inputs64(p)
+    gx, gy = O.tile_grid(p.W, p.H)
+    ncc = cpu(nc).reshape(-1).long()
+    ref = 0
+    for t in range(gx * gy):
+        s, e = int(p.rng[t, 0]), int(p.rng[t, 1])
+        if e <= s:
+            continue
+        pxi, pyi, pix = O._tile_pixels(t, p.W, p.H)
+        g = cpu(p.ids)[s:e].long()
+        dx = u[g, 0][None] - pxi.double()[:, None]
+        dy = u[g, 1][None] - pyi.double()[:, None]
+        pw = -0.5 * (c[g, 0][None] * dx * dx + c[g, 2][None] * dy * dy) - c[g, 1][None] * dx * dy
+        a = o.reshape(-1)[g][None] * torch.exp(pw)
+        before = torch.arange(e - s)[None] < ncc[pix][:, None]
+        ref += int(((pw <= 0) & (a >= 1 / 255) & before).sum())
+    assert 0 < comp <= ev
+    assert abs(comp - ref) <= max(2, 1e-4 * ref), (comp, ref)
+    ops.check_device_status()

@@ -176,3 +176,68 @@ def test_empty_inputs():
     img = O.alpha_blending(torch.zeros(0, 2), torch.zeros(0, 3), torch.zeros(0, 1), torch.zeros(0, 3),
                            ids, rng, 0.5, 20, 20)
     assert torch.all(img == 0.5)
+
+
+def test_tilewise_loss_gradient_equals_autograd_over_the_image():
+    """``blend_loss_grad`` (tile by tile, bounded memory, threads) gives the
+    loss, image and gradients of ``alpha_blending`` + autograd."""
+    scene, cam = WL.scene_small(6, n=1500)
+    a = [t.double() for t in scene.activated()]
+    img32, uv32, rad32, aux = O.render_view(*[t.float() for t in a], None, cam.center, cam.intr,
+                                            cam.extr[:3], cam.W, cam.H)
+    g = torch.Generator().manual_seed(3)
+    N = a[0].shape[0]
+    uv = uv32.double()
+    conic, op = aux["conic"].double(), a[3]
+    feat = torch.rand(N, 5, generator=g, dtype=torch.float64)
+    target = torch.rand(5, cam.H, cam.W, generator=g, dtype=torch.float64)
+    leaves = [x.clone().requires_grad_(True) for x in (uv, conic, op, feat)]
+    img = O.alpha_blending(*leaves, aux["ids"], aux["tile_range"], 0.3, cam.W, cam.H)
+    d = img - target
+    loss = d.abs().sum() + 0.2 * (d * d).sum()
+    loss.backward()
+    tflat = target.reshape(5, -1)
+
+    def pixel_loss(im, pix):
+        dd = im - tflat[:, pix]
+        return dd.abs().sum() + 0.2 * (dd * dd).sum()
+
+    for workers in (1, 3):
+        L, im2, *gr = O.blend_loss_grad(uv, conic, op, feat, aux["ids"], aux["tile_range"], 0.3,
+                                        cam.W, cam.H, pixel_loss, workers=workers)
+        assert abs(L - float(loss)) < 1e-9 * float(loss)
+        assert torch.allclose(im2, img.detach(), atol=1e-13)
+        for x, y in zip(gr, leaves):
+            assert torch.allclose(x, y.grad, atol=1e-11, rtol=1e-9)
+
+
+def test_blend_pool_equals_tilewise_gradient():
+    """The spawned-process pool (bench's CPU legs) gives the loss and the
+    gradients of ``blend_loss_grad``."""
+    from oracle.blend_pool import BlendPool
+    scene, cam = WL.scene_small(7, n=1200)
+    a = [t.float() for t in scene.activated()]
+    _, uv32, _, aux = O.render_view(*a, None, cam.center, cam.intr, cam.extr[:3], cam.W, cam.H)
+    g = torch.Generator().manual_seed(4)
+    uv, conic, op = uv32.double(), aux["conic"].double(), a[3].double()
+    feat = torch.rand(uv.shape[0], 4, generator=g, dtype=torch.float64)
+    target = torch.rand(4, cam.H, cam.W, generator=g, dtype=torch.float64)
+    tflat = target.reshape(4, -1)
+    scale = 1.0 / tflat.numel()
+
+    def pixel_loss(im, pix):
+        dd = im - tflat[:, pix]
+        return (dd.abs().sum() + 0.2 * (dd * dd).sum()) * scale
+
+    L, _, *ref = O.blend_loss_grad(uv, conic, op, feat, aux["ids"], aux["tile_range"], 0.0,
+                                   cam.W, cam.H, pixel_loss)
+    pool = BlendPool(uv.shape[0], 4, aux["ids"].numel() + 10, cam.W, cam.H, target, workers=2,
+                     scale=scale)
+    try:
+        for _ in range(2):      # the shared buffers are reused
+            L2, *got = pool.run(uv, conic, op, feat, aux["ids"], aux["tile_range"])
+            assert abs(L2 - L) < 1e-12
+            for x, y in zip(got, ref):
+                assert torch.allclose(x, y, atol=1e-15, rtol=1e-10)
+    finally:
+        pool.close()

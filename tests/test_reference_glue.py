@@ -94,6 +94,8 @@ def test_fixture_is_the_installed_reference(glue):
         elif isinstance(a, (list, tuple)):
             for i, (x, y) in enumerate(zip(a, b)):
                 same(x, y, f"{path}[{i}]")
+        elif torch.is_tensor(a) and a.is_floating_point():
+            assert torch.allclose(a, b, rtol=1e-12, atol=1e-14), path
         elif torch.is_tensor(a):
             assert torch.equal(a, b), path
         else:

@@ -54,7 +54,7 @@ def test_reference_arm_prints_once_under_the_launcher(tmp_path):
     script.write_text(
         "import runpy, sys\n"
         "sys.argv = ['bench.py', '--impl', 'reference', '--gpus', '2', '--n', '3000',\n"
-        "            '--steps', '1', '--warmup', '0', '--cpu-tile-stride', '400']\n"
+        "            '--steps', '1', '--warmup', '0']\n"
         f"runpy.run_path({str(ROOT / 'bench.py')!r}, run_name='__main__')\n")
     r = _launch([str(script)])
     assert r.returncode == 0, r.stderr[-2000:]
