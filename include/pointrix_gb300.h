@@ -280,7 +280,11 @@ int pgb_alpha_blending_backward_views(const float* records, int64_t n_per_view, 
  * (the run-time autotuner of pointrix_gb300.autotune).  Forward: 64 or 128
  * records per batch.  Backward: 64, 128 or 256 records per batch with two
  * pixels per thread, or 4096 + 32 / 64 / 128 for four pixels per thread
- * (64 threads per tile, 8x16 pixel boxes per warp).  0 = the default (128,
+ * (64 threads per tile, 8x16 pixel boxes per warp); 8192 + 64, 8192 + 512 +
+ * 32 and 8192 + 1024 + 32 select the second four-pixel form (d_out in shared
+ * memory, packed f32x2 accumulation; butterfly or transposed per-splat
+ * reduction; at most 85 registers for the last), which up to eight channels
+ * use and wider features replace by the first form.  0 = the default (128,
  * two pixels per thread).  Every variant gives the same images, final
  * transmittance and contributor counts; the backward's gradient sums are
  * formed in a variant-dependent order (float atomics).

@@ -694,6 +694,234 @@ __global__ void __launch_bounds__(256 / PX) blend_bwd_kernel(
   }
 }
 
+// Backward, second form: the same replay and reductions as
+// blend_bwd_kernel, with fewer registers and fewer instructions per pair.
+//  * d_out lives in shared memory (two 16-byte planes per pixel: channels
+//    0-3 and 4-7), read only by a pixel that composites the splat, instead
+//    of NC registers per pixel; pixel coordinates are formed from the lane.
+//    The per-pixel registers are T, SB and the contributor count.
+//  * Packed FP32 pairs (fma.rn.f32x2, sm_100 and later) for the channel sums
+//    F = sum dout f and the feature gradients (two channels per
+//    instruction) and for the moment updates (two moments per instruction).
+// The skip decisions use the forward's exact arithmetic (splat_power2).
+// Variant codes: kBwdV2 + records per batch (butterfly reduction),
+// kBwdV2 + 512 + records (transposed reduction), kBwdV2 + 1024 + records
+// (transposed reduction, at most 85 registers: twelve CTAs per SM); four
+// pixels per thread.
+constexpr int kBwdV2 = 8192;
+
+__device__ __forceinline__ float2 f2(float x, float y) { return make_float2(x, y); }
+
+// Transposed per-splat reduction (XRED): each lane stores its GR partial
+// sums as a row of a per-warp [32][20] shared table, then lane k < 16 sums
+// column k over rows 0-15 and lane 16 + k over rows 16-31 (visited in the
+// order r ^ 4, which keeps the two half-warps on distinct banks), and one
+// shuffle adds the halves: 4 stores, 16 loads and 16 adds per lane instead
+// of the butterfly's 16 shuffles, 16 adds and 32 selects.
+constexpr int kRedStride = 20;  // floats per row: 16-byte rows on distinct bank groups
+
+template <int NC, int RF, int GR, int B, int PX, int MINB, bool XRED>
+__global__ void __launch_bounds__(256 / PX, MINB) blend_bwd2_kernel(
+    const float* __restrict__ records, const int32_t* __restrict__ ids,
+    const int2* __restrict__ ranges, int64_t n, float bg, const ViewTable vt, int C,
+    const float* __restrict__ final_T, const int32_t* __restrict__ n_contrib,
+    const float* __restrict__ d_out, float* __restrict__ grad_records,
+    int64_t* __restrict__ info) {
+  static_assert(GR == 16 || GR == 32, "gradient records are 16 or 32 floats");
+  static_assert(PX == 2 || PX == 4, "two or four pixels per thread");
+  static_assert(NC <= 8, "the d_out planes hold eight channels");
+  constexpr int NT = 256 / PX;
+  constexpr int BW = 8;
+  constexpr int RS = 32 / BW;
+  constexpr int BH = RS * PX;
+  constexpr int NP = (NC + 1) / 2;  // channel pairs
+  extern __shared__ __align__(128) float smem[];
+  __shared__ int s_max_nc;
+  __shared__ uint8_t s_touched[B];
+  __shared__ uint8_t s_list[NT / 32][B];
+  __shared__ __align__(16) float4 s_dout[2][256];  // [plane][q * NT + thread]
+  __shared__ __align__(16) float s_red[XRED ? NT / 32 : 1][XRED ? 32 * kRedStride : 1];
+  float* gacc = smem + 2 * B * RF;                  // [B][GR]
+
+  const int tile = blockIdx.x;
+  int W, H, gx, ltile;
+  int64_t pbase;
+  tile_view(vt, tile, W, H, gx, ltile, pbase);
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int bx0 = (ltile % gx) * kTile + BW * (w & 1);
+  const int by0 = (ltile / gx) * kTile + BH * (w >> 1);
+  uint8_t* my_list = s_list[w];
+
+  if (threadIdx.x == 0) s_max_nc = 0;
+  for (int i = threadIdx.x; i < B * GR; i += NT) gacc[i] = 0.f;
+  for (int i = threadIdx.x; i < B; i += NT) s_touched[i] = 0;
+
+  const int64_t plane = (int64_t)W * H;
+  const int pxi = bx0 + (lane & (BW - 1));
+  const float pxf = (float)pxi;
+  const float py0 = (float)(by0 + lane / BW);
+  float T[PX], SB[PX];
+  int nc[PX];
+  int my_nc = 0;
+#pragma unroll
+  for (int q = 0; q < PX; ++q) {
+    const int py = by0 + lane / BW + RS * q;
+    float dv[8];
+#pragma unroll
+    for (int c = 0; c < 8; ++c) dv[c] = 0.f;
+    T[q] = 1.f;
+    nc[q] = 0;
+    if (pxi < W && py < H) {
+      const int64_t pix = (int64_t)py * W + pxi;
+      T[q] = final_T[pbase + pix];
+      nc[q] = n_contrib[pbase + pix];
+#pragma unroll
+      for (int c = 0; c < NC; ++c)
+        if (c < C) dv[c] = d_out[C * pbase + c * plane + pix];
+    }
+    float sd = 0.f;
+#pragma unroll
+    for (int c = 0; c < NC; ++c) sd += dv[c];
+    SB[q] = bg * sd;
+    s_dout[0][q * NT + threadIdx.x] = make_float4(dv[0], dv[1], dv[2], dv[3]);
+    s_dout[1][q * NT + threadIdx.x] = make_float4(dv[4], dv[5], dv[6], dv[7]);
+    my_nc = max(my_nc, nc[q]);
+  }
+  int warp_nc = my_nc;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) warp_nc = max(warp_nc, __shfl_xor_sync(0xffffffffu, warp_nc, o));
+  __syncthreads();  // gacc, s_touched and s_max_nc initialised
+  if (lane == 0) atomicMax(&s_max_nc, warp_nc);
+  __syncthreads();
+  const int2 rg = ranges[tile];
+  const int64_t start = rg.x;
+  const int list_len = max(0, rg.y - rg.x);
+  if (s_max_nc > list_len && threadIdx.x == 0) set_info(info, PGB_ERR_OVERFLOW);
+  const int max_nc = min(s_max_nc, list_len);
+  const int nb = (max_nc + B - 1) / B;
+  auto lo_of = [&](int b) { return max(0, max_nc - (b + 1) * B); };
+  auto hi_of = [&](int b) { return max_nc - b * B; };
+
+  if (nb > 0)
+    stage_batch<RF, NT, B>(records, ids, start + lo_of(0), start + hi_of(0), n, smem, info);
+  for (int b = 0; b < nb; ++b) {
+    const int buf = b & 1;
+    const int lo = lo_of(b), hi = hi_of(b);
+    if (b + 1 < nb) {
+      stage_batch<RF, NT, B>(records, ids, start + lo_of(b + 1), start + hi_of(b + 1), n,
+                             smem + (buf ^ 1) * B * RF, info);
+      cp_async_wait<1>();
+    } else {
+      cp_async_wait<0>();
+    }
+    __syncthreads();
+    const float* st = smem + buf * B * RF;
+    const int nl = warp_cull<BW, BH, B>(st, RF, min(hi, warp_nc) - lo, (float)bx0, (float)by0,
+                                        my_list);
+    for (int t = nl - 1; t >= 0; --t) {
+      const int slot = my_list[t];
+      const int j = lo + slot;
+      const float* rec = st + slot * RF;
+      const float4 r0 = *reinterpret_cast<const float4*>(rec);  // u, v, A, B
+      const float4 r1 = *reinterpret_cast<const float4*>(rec + 4);  // C, o, tau, thr
+      const float dx = __fsub_rn(r0.x, pxf);
+      const SplatX sx = splat_x(r0.z, r0.w, dx);
+      float2 v[GR / 2];
+#pragma unroll
+      for (int k = 0; k < GR / 2; ++k) v[k] = f2(0.f, 0.f);
+      bool contrib = false;
+#pragma unroll
+      for (int q = 0; q < PX; ++q) {
+        if (j >= nc[q]) continue;
+        const float dy = __fsub_rn(r0.y, py0 + (float)(RS * q));
+        const float p2 = splat_power2(sx, r1.x, dy);
+        if (p2 > 0.f || p2 < r1.w) continue;  // the forward's skip test
+        contrib = true;
+        const float g0 = __fmaf_rn(r0.w, dy, sx.Adx), g1 = __fmaf_rn(r1.x, dy, sx.Bdx);
+        const float G = ex2_approx(p2);
+        const float araw = __fmul_rn(r1.y, G);
+        const float alpha = fminf(0.99f, araw);
+        const float om = __fsub_rn(1.0f, alpha);
+        T[q] = __fdividef(T[q], om);
+        const float4 dlo = s_dout[0][q * NT + threadIdx.x];
+        const float4 dhi = s_dout[1][q * NT + threadIdx.x];
+        const float2 dp[4] = {f2(dlo.x, dlo.y), f2(dlo.z, dlo.w), f2(dhi.x, dhi.y),
+                              f2(dhi.z, dhi.w)};
+        const float2* fp = reinterpret_cast<const float2*>(rec + kRecFeat);
+        float2 F2 = __fmul2_rn(dp[0], fp[0]);
+#pragma unroll
+        for (int k = 1; k < NP; ++k) F2 = __ffma2_rn(dp[k], fp[k], F2);
+        const float F = F2.x + F2.y;
+        const float wT = alpha * T[q];
+        const float2 wT2 = f2(wT, wT);
+#pragma unroll
+        for (int k = 0; k < NP; ++k) v[3 + k] = __ffma2_rn(wT2, dp[k], v[3 + k]);
+        const float dalpha = (F - SB[q]) * T[q];
+        SB[q] = fmaf(alpha, F, om * SB[q]);
+        if (araw < 0.99f) {
+          const float dpow = alpha * dalpha;
+          const float tx = dpow * dx;
+          v[0] = __ffma2_rn(f2(g0, g1), f2(dpow, dpow), v[0]);            // sum g0 dp, g1 dp
+          v[1] = __ffma2_rn(f2(tx, tx), f2(dx, dy), v[1]);                // dx^2 dp, dx dy dp
+          v[2] = __ffma2_rn(f2(dpow * dy, G), f2(dy, dalpha), v[2]);      // dy^2 dp, G dalpha
+        }
+      }
+      if (__any_sync(0xffffffffu, contrib)) {
+        if constexpr (XRED && GR == 16) {
+          float* tab = s_red[w];
+          float4* row = reinterpret_cast<float4*>(tab + lane * kRedStride);
+#pragma unroll
+          for (int k = 0; k < 4; ++k) row[k] = make_float4(v[2 * k].x, v[2 * k].y, v[2 * k + 1].x, v[2 * k + 1].y);
+          __syncwarp();
+          const int h = lane >> 4;
+          const float* a0 = tab + h * 16 * kRedStride + (lane & 15);
+          const float* ap = a0 + h * 4 * kRedStride;   // rows r ^ 4 with bit 2 of r clear
+          const float* am = a0 - h * 4 * kRedStride;   // ... and set
+          float sum = 0.f;
+#pragma unroll
+          for (int r = 0; r < 16; ++r) sum += ((r & 4) ? am : ap)[r * kRedStride];
+          sum += __shfl_xor_sync(0xffffffffu, sum, 16);
+          if (lane < 6 + NC) atomicAdd(&gacc[slot * GR + lane], sum);
+          __syncwarp();   // the table is rewritten by the next splat
+        } else {
+          float vf[GR];
+#pragma unroll
+          for (int k = 0; k < GR / 2; ++k) {
+            vf[2 * k] = v[k].x;
+            vf[2 * k + 1] = v[k].y;
+          }
+          const float sum = warp_reduce_scatter<GR>(vf);
+          if (GR == 32) {
+            if (lane < 6 + NC) atomicAdd(&gacc[slot * GR + lane], sum);
+          } else if ((lane & 1) == 0 && (lane >> 1) < 6 + NC) {
+            atomicAdd(&gacc[slot * GR + (lane >> 1)], sum);
+          }
+        }
+        if (lane == 0) s_touched[slot] = 1;
+      }
+    }
+    __syncwarp();
+    __syncthreads();
+    for (int t = threadIdx.x; t < hi - lo; t += NT) {
+      if (!s_touched[t]) continue;
+      const int32_t g = ids[start + lo + t];
+      if (g < 0 || (int64_t)g >= n) {
+        set_info(info, PGB_ERR_OVERFLOW);
+        continue;
+      }
+      float4* dst = reinterpret_cast<float4*>(grad_records + (int64_t)g * GR);
+      float4* srcv = reinterpret_cast<float4*>(gacc + t * GR);
+#pragma unroll
+      for (int q = 0; q < (6 + NC + 3) / 4; ++q) {
+        atomicAdd(dst + q, srcv[q]);
+        srcv[q] = make_float4(0.f, 0.f, 0.f, 0.f);
+      }
+      s_touched[t] = 0;
+    }
+    __syncthreads();
+  }
+}
+
 // ---------------------------------------------------------------- unpack
 template <int RF>
 __global__ void unpack_kernel(const float* __restrict__ g, int64_t n, int C,
@@ -794,6 +1022,25 @@ static int launch_fwd_nc(const float* records, const int32_t* ids, const int2* r
   }
 }
 
+template <int NC, int B, int PX, int MINB, bool XRED>
+static int launch_bwd2_b(const float* records, const int32_t* ids, const int2* ranges, int64_t n,
+                         float bg, const ViewTable& vt, int tiles, int C, const float* fT,
+                         const int32_t* ncon, const float* dout, float* grec, int64_t* info,
+                         cudaStream_t s) {
+  constexpr int RF = rec_floats(NC);
+  constexpr int GR = grad_floats(NC);
+  const size_t smem = (2 * RF + GR) * B * sizeof(float);
+  auto kern = blend_bwd2_kernel<NC, RF, GR, B, PX, MINB, XRED>;
+  if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+          cudaSuccess ||
+      cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout,
+                           cudaSharedmemCarveoutMaxShared) != cudaSuccess)
+    return PGB_ERR_CUDA;
+  kern<<<tiles, 256 / PX, smem, s>>>(records, ids, ranges, n, bg, vt, C, fT, ncon, dout, grec,
+                                     info);
+  return launch_status();
+}
+
 template <int NC, int B, int PX>
 static int launch_bwd_b(const float* records, const int32_t* ids, const int2* ranges, int64_t n,
                         float bg, const ViewTable& vt, int tiles, int C, const float* fT,
@@ -827,9 +1074,31 @@ static int launch_bwd_nc(const float* records, const int32_t* ids, const int2* r
     case kBwdPx4 + 32: return PGB_BWD(32, 4);
     case kBwdPx4 + 64: return PGB_BWD(64, 4);
     case kBwdPx4 + 128: return PGB_BWD(128, 4);
-    default: return PGB_ERR_INVALID;
+    default: break;
+  }
+  if constexpr (NC <= 8) {
+#define PGB_BWD2(B, PX, MINB, XRED)                                                            \
+  launch_bwd2_b<NC, B, PX, MINB, XRED>(records, ids, ranges, n, bg, vt, tiles, C, fT, ncon, dout, \
+                                       grec, info, s)
+    switch (batch) {
+      case kBwdV2 + 64: return PGB_BWD2(64, 4, 1, false);
+      case kBwdV2 + 512 + 32: return PGB_BWD2(32, 4, 1, true);
+      case kBwdV2 + 1024 + 32: return PGB_BWD2(32, 4, 12, true);
+      default: break;
+    }
+#undef PGB_BWD2
+  } else {
+    // the second form keeps eight channels of d_out in shared memory: wider
+    // features take the first form's four-pixel kernel with the same batch
+    switch (batch) {
+      case kBwdV2 + 64: return PGB_BWD(64, 4);
+      case kBwdV2 + 512 + 32:
+      case kBwdV2 + 1024 + 32: return PGB_BWD(32, 4);
+      default: break;
+    }
   }
 #undef PGB_BWD
+  return PGB_ERR_INVALID;
 }
 
 // Channel counts with a compiled kernel; other counts round up (extra
@@ -1120,9 +1389,10 @@ int pgb_blend_pair_census(const float* records, int channels, int64_t n, const i
 // Batch sizes compiled for the forward (backward = 0) or the backward (1).
 int pgb_blend_batches(int backward, int32_t* out) {
   static const int32_t f[] = {64, 128},
-                       b[] = {64, 128, 256, kBwdPx4 + 32, kBwdPx4 + 64, kBwdPx4 + 128};
+                       b[] = {64, 128, 256, kBwdPx4 + 32, kBwdPx4 + 64, kBwdPx4 + 128,
+                              kBwdV2 + 64, kBwdV2 + 512 + 32, kBwdV2 + 1024 + 32};
   const int32_t* src = backward ? b : f;
-  const int cnt = backward ? 6 : 2;
+  const int cnt = backward ? 9 : 2;
   if (out)
     for (int i = 0; i < cnt; ++i) out[i] = src[i];
   return cnt;

@@ -563,7 +563,8 @@ def _blend_batches(backward: int) -> tuple:
     hit = _BATCHES.get(backward)
     if hit is None:
         import ctypes as C
-        buf = (C.c_int32 * 8)()
+        cnt = _lib.lib().pgb_blend_batches(backward, None)   # the count first
+        buf = (C.c_int32 * max(cnt, 1))()
         cnt = _lib.lib().pgb_blend_batches(backward, buf)
         hit = _BATCHES[backward] = tuple(buf[i] for i in range(cnt))
     return hit

@@ -124,3 +124,17 @@ def test_every_compute_entry_rejects_null_buffers():
         args = [None if (t is C.c_void_p or issubclass(t, C._Pointer)) else
                 (0.5 if t in (C.c_float, C.c_double) else 16) for t in _lib.SIGNATURES[name]]
         assert getattr(lib, name)(*args) == 1, name
+
+
+def test_blend_variant_list_is_sized_by_its_own_count():
+    """pgb_blend_batches(backward, NULL) returns the count; the list then
+    fits a buffer of exactly that size (the Python layer sizes it so)."""
+    lib = _lib.lib()
+    for backward in (0, 1):
+        cnt = lib.pgb_blend_batches(backward, None)
+        assert cnt >= 2
+        buf = (C.c_int32 * cnt)()
+        assert lib.pgb_blend_batches(backward, buf) == cnt
+        assert len(set(buf)) == cnt
+    from pointrix_gb300 import ops
+    assert len(ops._blend_batches(1)) == lib.pgb_blend_batches(1, None)
