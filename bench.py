@@ -585,9 +585,13 @@ def recompute_measure(device, n=6_000_000, steps=3):
     g = torch.Generator().manual_seed(44)
     cam = WL.make_camera(g, 3840, 2160, 2800.0, 5.0).to(device)
     target = torch.rand(4, cam.H, cam.W, generator=g).to(device)
+    from pointrix_gb300 import ops
     res, grads = {}, {}
-    for mode in (False, True):
-        r = MsplatRender(MsplatRender.Config(render_depth=True, recompute_backward=mode), device=device)
+    K = count_entries_cam(scene, cam)
+    modes = {"stored": (False, 0), "recompute": (True, 0), "recompute_4_bands": (True, 4)}
+    for name, (mode, bands) in modes.items():
+        r = MsplatRender(MsplatRender.Config(render_depth=True, recompute_backward=mode,
+                                             recompute_bands=bands), device=device)
         r.sh_degree = 3
         params = [scene.position, scene.log_scale, scene.quat_raw, scene.opacity_logit, scene.shs]
         times, held = [], 0
@@ -608,12 +612,29 @@ def recompute_measure(device, n=6_000_000, steps=3):
             if it > 0:
                 times.append(time.perf_counter() - t0)
         peak = torch.cuda.max_memory_allocated(device) - base
-        grads[mode] = [p.grad.detach().clone() for p in params]
-        res["recompute" if mode else "stored"] = {
-            "ms_per_step": 1e3 * statistics.mean(times), "peak_gb": peak / 1e9,
-            "held_fwd_to_bwd_gb": held / 1e9}
-    rel = max(float((a - b).norm() / b.norm().clamp(min=1e-30)) for a, b in zip(grads[True], grads[False]))
-    return {"workload": RECOMPUTE_WORKLOAD, **res, "grad_rel_l2_max": rel}
+        grads[name] = [p.grad.detach().clone() for p in params]
+        res[name] = {"ms_per_step": 1e3 * statistics.mean(times), "peak_gb": peak / 1e9,
+                     "held_fwd_to_bwd_gb": held / 1e9}
+        if mode:
+            res[name]["bands"] = len(ops.last_band_plan)
+            res[name]["max_band_entries"] = max(k for _, _, k in ops.last_band_plan)
+    rel = {name: max(float((a - b).norm() / b.norm().clamp(min=1e-30))
+                     for a, b in zip(grads[name], grads["stored"])) for name in modes if name != "stored"}
+    return {"workload": RECOMPUTE_WORKLOAD, "K_entries": K, **res,
+            "grad_rel_l2_max": max(rel.values()), "grad_rel_l2": rel}
+
+
+def count_entries_cam(scene, cam):
+    """K of a scene for a fixed camera (cam.extr [4,4], cam.intr)."""
+    from pointrix_gb300 import ops
+    with torch.no_grad():
+        pos, sc, q, op, shs = scene.activated()
+        E = cam.extr[:3]
+        uv, depth = ops.project_point(pos, cam.intr, E, cam.W, cam.H)
+        vis = depth != 0
+        cov = ops.compute_cov3d(sc, q, vis)
+        conic, radius, tiles = ops.ewa_project(pos, cov, cam.intr, E, uv, cam.W, cam.H, vis)
+        return int(tiles[radius > 0].sum())
 
 
 # --------------------------------------------------------------- serving ---

@@ -317,6 +317,59 @@ int pgb_alpha_blending_backward_views_with_batch(
     float* d_conic, float* d_opacity, float* d_feature, int64_t* info, void* stream, int batch);
 int pgb_blend_batches(int backward, int32_t* out);
 
+/* ---------------------------------------------------------------------
+ * Bands of tile rows -- no counterpart in the reference.  They serve the
+ * recompute-in-backward mode of large views (ops.rasterize(recompute=True)):
+ * one image is sorted and blended one band of tile rows [row0, row1) at a
+ * time, so the K-sized sort buffers and id list hold one band's entries
+ * instead of the whole image's.  The per-tile lists, images, contributor
+ * counts and gradients equal those of the whole-image calls.
+ *
+ * pgb_band_tiles: tiles_out[g] = entries of Gaussian g inside the band (its
+ * tile rectangle clipped to the rows; 0 for radius <= 0).
+ * pgb_sort_gaussian_rebegin: after a pgb_sort_gaussian_begin on the same
+ * Gaussians (whose depth order scratch_n keeps), prepares phase two for
+ * another band: sums the band's tiles_touched into info[0] (K of the band)
+ * and clears what phase two counts in.
+ * pgb_sort_gaussian_finish_band: phase two for the band, K = k: ids [k] and
+ * tile_range [gx * (row1 - row0), 2] with band-local tile ids (row r of the
+ * band is tile row row0 + r); scratch as pgb_sort_scratch_bytes(n, k, width,
+ * height) gives for the whole image.
+ * pgb_alpha_blending_forward_band / _backward_band: the blend of the band's
+ * tiles, reading that tile_range, writing (reading) only the band's pixels
+ * of the whole-image out, final_T, n_contrib (d_out).  Forward: pack = 0
+ * reuses records packed by an earlier band's call.  Backward: first != 0
+ * zeroes grad_records, last != 0 unpacks the gradients summed over all bands
+ * (d_uv, d_conic, d_opacity, d_feature may be NULL while last == 0).
+ * ------------------------------------------------------------------- */
+int pgb_band_tiles(const float* uv, const int32_t* radius, int64_t n, int width, int height,
+                   int row0, int row1, int32_t* tiles_out, void* stream);
+/* K of every band at once: bands (device int32 [nbands + 1], increasing
+ * tile rows; band b is rows [bands[b], bands[b + 1])), counts (device
+ * uint64 [nbands], overwritten).  nbands <= 1024. */
+int pgb_band_counts(const float* uv, const int32_t* radius, int64_t n, int width, int height,
+                    const int32_t* bands, int nbands, unsigned long long* counts, void* stream);
+int pgb_sort_gaussian_rebegin(const int32_t* radius, const int32_t* tiles_touched, int64_t n,
+                              void* scratch_n, size_t bytes_n, int64_t* info, void* stream);
+int pgb_sort_gaussian_finish_band(const float* uv, const int32_t* radius,
+                                  const int32_t* tiles_touched, int64_t n, int width, int height,
+                                  int row0, int row1, int64_t k, void* scratch_n, size_t bytes_n,
+                                  void* scratch_k, size_t bytes_k, int64_t* info, int32_t* ids_out,
+                                  int32_t* tile_range_out, void* stream);
+int pgb_alpha_blending_forward_band(const float* uv, const float* conic, const float* opacity,
+                                    const float* feature, int64_t n, int channels,
+                                    const int32_t* ids, int64_t k, const int32_t* tile_range,
+                                    float bg, int width, int height, int row0, int row1, int pack,
+                                    float* records, float* out, float* final_T,
+                                    int32_t* n_contrib, int64_t* info, void* stream, int batch);
+int pgb_alpha_blending_backward_band(const float* records, int64_t n, int channels,
+                                     const int32_t* ids, int64_t k, const int32_t* tile_range,
+                                     float bg, int width, int height, int row0, int row1,
+                                     const float* final_T, const int32_t* n_contrib,
+                                     const float* d_out, float* grad_records, int first, int last,
+                                     float* d_uv, float* d_conic, float* d_opacity,
+                                     float* d_feature, int64_t* info, void* stream, int batch);
+
 /* pgb_blend_pair_census -- no counterpart in the reference: a measurement
  * aid, not part of the training path.  For the blend a forward call made
  * (its records, sorted ids, tile ranges and n_contrib [H,W]), adds to

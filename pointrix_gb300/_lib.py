@@ -58,6 +58,15 @@ SIGNATURES = {
                                                      vp, vp, vp, vp, vp, vp, vp, i32],
     "pgb_blend_batches": [i32, vp],
     "pgb_blend_pair_census": [vp, i32, i64, vp, i64, vp, i32, i32, vp, vp, vp],
+    "pgb_band_tiles": [vp, vp, i64, i32, i32, i32, i32, vp, vp],
+    "pgb_band_counts": [vp, vp, i64, i32, i32, vp, i32, vp, vp],
+    "pgb_sort_gaussian_rebegin": [vp, vp, i64, vp, szt, vp, vp],
+    "pgb_sort_gaussian_finish_band": [vp, vp, vp, i64, i32, i32, i32, i32, i64, vp, szt, vp, szt,
+                                      vp, vp, vp, vp],
+    "pgb_alpha_blending_forward_band": [vp, vp, vp, vp, i64, i32, vp, i64, vp, f32, i32, i32, i32,
+                                        i32, i32, vp, vp, vp, vp, vp, vp, i32],
+    "pgb_alpha_blending_backward_band": [vp, i64, i32, vp, i64, vp, f32, i32, i32, i32, i32, vp,
+                                         vp, vp, vp, i32, i32, vp, vp, vp, vp, vp, vp, i32],
     "pgb_alpha_blending_forward_pieces": [vp, vp, vp, vp, vp, i32, i64, vp, i64, vp, f32, i32, i32,
                                           vp, vp, vp, vp, vp, vp, i32],
     "pgb_alpha_blending_backward_pieces": [vp, i64, vp, i32, vp, i64, vp, f32, i32, i32, vp, vp, vp,

@@ -1152,11 +1152,13 @@ static int blend_forward_impl(const float* uv, const float* conic, const float* 
                               const FeatCols& fc, int64_t n, int channels, const int32_t* ids,
                               int64_t k, const int32_t* tile_range, float bg, const ViewTable& vt,
                               int tiles, float* records, float* out, float* final_T,
-                              int32_t* n_contrib, int64_t* info, void* stream, int batch) {
+                              int32_t* n_contrib, int64_t* info, void* stream, int batch,
+                              bool pack = true) {
   const int nc = nc_bucket(channels);
   if (n < 0 || k < 0 || tiles <= 0 || channels < 1 || nc < 0) return PGB_ERR_INVALID;
   if (!tile_range || !out || !final_T || !n_contrib || (k > 0 && !ids)) return PGB_ERR_INVALID;
-  if (n > 0 && (!uv || !conic || !opacity || !fc.src[0] || !records)) return PGB_ERR_INVALID;
+  if (n > 0 && (!records || (pack && (!uv || !conic || !opacity || !fc.src[0]))))
+    return PGB_ERR_INVALID;
   // records are staged by bulk copies and read as float4; the ranges as int2
   // (info, when given, takes a 64-bit atomic)
   if (misaligned(records, 16) || misaligned(tile_range, 8) || misaligned(info, 8))
@@ -1166,7 +1168,7 @@ static int blend_forward_impl(const float* uv, const float* conic, const float* 
   switch (nc) {
 #define PGB_CASE(N)                                                                             \
   case N:                                                                                       \
-    if (n > 0)                                                                                  \
+    if (n > 0 && pack)                                                                          \
       pack_kernel<rec_floats(N)><<<stream_grid(n), kStreamThreads, 0, s>>>(uv, conic, opacity,  \
                                                                            fc, n, channels,      \
                                                                            records);            \
@@ -1184,11 +1186,13 @@ static int blend_backward_impl(const float* records, int64_t n, int channels, co
                                int tiles, const float* final_T, const int32_t* n_contrib,
                                const float* d_out, float* grad_records, float* d_uv,
                                float* d_conic, float* d_opacity, const FeatGradCols& gc,
-                               int64_t* info, void* stream, int batch) {
+                               int64_t* info, void* stream, int batch, bool first = true,
+                               bool last = true) {
   const int nc = nc_bucket(channels);
   if (n < 0 || k < 0 || tiles <= 0 || channels < 1 || nc < 0) return PGB_ERR_INVALID;
   if (!tile_range || !final_T || !n_contrib || !d_out || (k > 0 && !ids)) return PGB_ERR_INVALID;
-  if (n > 0 && (!records || !grad_records || !d_uv || !d_conic || !d_opacity || !gc.dst[0]))
+  if (n > 0 && (!records || !grad_records ||
+                (last && (!d_uv || !d_conic || !d_opacity || !gc.dst[0]))))
     return PGB_ERR_INVALID;
   if (misaligned(records, 16) || misaligned(grad_records, 16) || misaligned(d_uv, 8) ||
       misaligned(tile_range, 8) || misaligned(info, 8))
@@ -1196,7 +1200,7 @@ static int blend_backward_impl(const float* records, int64_t n, int channels, co
   if (n == 0) return PGB_OK;
   cudaStream_t s = as_stream(stream);
   const int GRf = grad_floats(nc);
-  if (cudaMemsetAsync(grad_records, 0, (size_t)n * GRf * sizeof(float), s) != cudaSuccess)
+  if (first && cudaMemsetAsync(grad_records, 0, (size_t)n * GRf * sizeof(float), s) != cudaSuccess)
     return PGB_ERR_CUDA;
   const int2* rg = reinterpret_cast<const int2*>(tile_range);
   int st = PGB_ERR_INVALID;
@@ -1212,6 +1216,7 @@ static int blend_backward_impl(const float* records, int64_t n, int channels, co
       break;
   }
   if (st != PGB_OK) return st;
+  if (!last) return PGB_OK;  // later bands add to the same gradient records
   if (GRf == 16)
     unpack_kernel<16><<<stream_grid(n), kStreamThreads, 0, s>>>(grad_records, n, channels, d_uv,
                                                                 d_conic, d_opacity, gc);
@@ -1358,6 +1363,43 @@ int pgb_alpha_blending_backward_pieces(const float* records, int64_t n, const in
                              single_view(width, height), grid_x(width) * grid_y(height), final_T,
                              n_contrib, d_out, grad_records, d_uv, d_conic, d_opacity, gc, info,
                              stream, batch);
+}
+
+// One band of tile rows [row0, row1) of an image (no msplat counterpart):
+// tile_range holds the band's gx * (row1 - row0) tiles with band-local ids
+// (pgb_sort_gaussian_finish_band), out/final_T/n_contrib are the whole
+// image's and only the band's pixels are written.  pack = 0 reuses the
+// records a previous band's call packed.
+int pgb_alpha_blending_forward_band(const float* uv, const float* conic, const float* opacity,
+                                    const float* feature, int64_t n, int channels,
+                                    const int32_t* ids, int64_t k, const int32_t* tile_range,
+                                    float bg, int width, int height, int row0, int row1, int pack,
+                                    float* records, float* out, float* final_T,
+                                    int32_t* n_contrib, int64_t* info, void* stream, int batch) {
+  ViewTable vt;
+  if (!band_view(width, height, row0, row1, vt)) return PGB_ERR_INVALID;
+  return blend_forward_impl(uv, conic, opacity, cols_of(feature, channels), n, channels, ids, k,
+                            tile_range, bg, vt, grid_x(width) * (row1 - row0), records, out,
+                            final_T, n_contrib, info, stream, batch, pack != 0);
+}
+
+// The backward of one band: first != 0 zeroes grad_records first, last != 0
+// turns the records summed over every band into d_uv, d_conic, d_opacity
+// and d_feature (which may be NULL on the other bands).
+int pgb_alpha_blending_backward_band(const float* records, int64_t n, int channels,
+                                     const int32_t* ids, int64_t k, const int32_t* tile_range,
+                                     float bg, int width, int height, int row0, int row1,
+                                     const float* final_T, const int32_t* n_contrib,
+                                     const float* d_out, float* grad_records, int first, int last,
+                                     float* d_uv, float* d_conic, float* d_opacity,
+                                     float* d_feature, int64_t* info, void* stream, int batch) {
+  ViewTable vt;
+  if (!band_view(width, height, row0, row1, vt)) return PGB_ERR_INVALID;
+  return blend_backward_impl(records, n, channels, ids, k, tile_range, bg, vt,
+                             grid_x(width) * (row1 - row0), final_T, n_contrib, d_out,
+                             grad_records, d_uv, d_conic, d_opacity,
+                             grad_cols_of(d_feature, channels), info, stream, batch, first != 0,
+                             last != 0);
 }
 
 // Pair census of a blend (no msplat counterpart): counts[0] += list entries

@@ -60,9 +60,15 @@ __device__ inline void tile_rect(float u, float v, float r, int gx, int gy, int&
 // g / n_per_view.
 constexpr int kMaxViews = 64;
 
+// One image may also be processed in bands of tile rows [band0, band1):
+// the sort then emits only the entries of those rows, with tile ids local to
+// the band (row r of the band is tile row band0 + r of the image), and a
+// blend launch covers only the band's tiles, reading band-local tile ranges
+// and writing the image's own pixels.  single_view covers every row.
 struct ViewTable {
   int nviews;
   int W, H;
+  int band0, band1;
   int64_t n_per_view;
   int32_t w[kMaxViews], h[kMaxViews], tile_base[kMaxViews];
   int64_t pixel_base[kMaxViews];
@@ -73,7 +79,19 @@ inline ViewTable single_view(int W, int H) {
   vt.nviews = 0;
   vt.W = W;
   vt.H = H;
+  vt.band0 = 0;
+  vt.band1 = grid_y(H);
   return vt;
+}
+
+// One image restricted to tile rows [row0, row1); false when the rows are
+// not a non-empty range of the image's tile rows.
+inline bool band_view(int W, int H, int row0, int row1, ViewTable& vt) {
+  if (W <= 0 || H <= 0 || row0 < 0 || row1 <= row0 || row1 > grid_y(H)) return false;
+  vt = single_view(W, H);
+  vt.band0 = row0;
+  vt.band1 = row1;
+  return true;
 }
 
 // A batch from host (width, height) pairs; fills the bases and returns the
@@ -126,7 +144,7 @@ __device__ inline void tile_view(const ViewTable& vt, int tile, int& W, int& H, 
     W = vt.W;
     H = vt.H;
     gx = grid_x(W);
-    local = tile;
+    local = tile + vt.band0 * gx;  // the band's tiles are launched from 0
     pixel_base = 0;
     return;
   }

@@ -791,6 +791,12 @@ __global__ void __launch_bounds__(kStreamThreads) rect_kernel(
         uint32_t tile_base;
         element_view(vt, (uint32_t)g, gx, gy, tile_base);
         tile_rect(p.x, p.y, (float)r, gx, gy, x0, x1, y0, y1);
+        if (vt.nviews == 0) {  // one image: the rows of its band, band-local
+          y0 = max(y0, vt.band0);
+          y1 = max(min(y1, vt.band1), y0);
+          y0 -= vt.band0;
+          y1 -= vt.band0;
+        }
         const uint32_t cnt = (uint32_t)max(tiles[g], 0);
         const uint32_t w = (uint32_t)(x1 - x0);
         if ((int64_t)w * (y1 - y0) != (int64_t)cnt) set_error(info, PGB_ERR_MISMATCH);
@@ -1074,6 +1080,80 @@ static int tile_pass(const TilePlan& plan, int p, int parts, cudaStream_t s, con
 #undef PGB_PASS
 }
 
+// ---------------------------------------------------------------------------
+// 6. bands of tile rows (one image processed a band at a time)
+//
+// band_tiles: the entries of each Gaussian inside tile rows [row0, row1) --
+// its tile rectangle (tile_rect, as the sort computes it) clipped to the
+// band, 0 for radius <= 0.  band_count: the sum of those counts over the
+// Gaussians with radius > 0 (the band's K), into info[0].
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kStreamThreads) band_tiles_kernel(
+    const float* __restrict__ uv, const int32_t* __restrict__ radius, int64_t n, int gx, int gy,
+    int row0, int row1, int32_t* __restrict__ tiles_out) {
+  for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < n;
+       g += (int64_t)gridDim.x * blockDim.x) {
+    const int r = radius[g];
+    int cnt = 0;
+    if (r > 0) {
+      const float2 p = reinterpret_cast<const float2*>(uv)[g];
+      int x0, x1, y0, y1;
+      tile_rect(p.x, p.y, (float)r, gx, gy, x0, x1, y0, y1);
+      const int rows = min(y1, row1) - max(y0, row0);
+      cnt = rows > 0 ? (x1 - x0) * rows : 0;
+    }
+    tiles_out[g] = cnt;
+  }
+}
+
+__global__ void __launch_bounds__(kStreamThreads) band_count_kernel(
+    const int32_t* __restrict__ radius, const int32_t* __restrict__ tiles, int64_t n,
+    int64_t* __restrict__ info) {
+  unsigned long long sum = 0;
+  for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < n;
+       g += (int64_t)gridDim.x * blockDim.x)
+    if (radius[g] > 0) sum += (unsigned long long)max(tiles[g], 0);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+  if ((threadIdx.x & 31) == 0 && sum)
+    atomicAdd(reinterpret_cast<unsigned long long*>(info), sum);
+}
+
+// band_counts: K of every band at once.  bands holds nbands + 1 increasing
+// tile rows (band b is rows [bands[b], bands[b + 1])); each Gaussian adds
+// its rectangle's entries in every band it crosses.  Per-CTA partial sums
+// in shared memory, one 64-bit atomic per band and CTA.
+constexpr int kMaxBands = 1024;
+
+__global__ void __launch_bounds__(kStreamThreads) band_counts_kernel(
+    const float* __restrict__ uv, const int32_t* __restrict__ radius, int64_t n, int gx, int gy,
+    const int32_t* __restrict__ bands, int nbands, unsigned long long* __restrict__ counts) {
+  __shared__ unsigned long long s_cnt[kMaxBands];
+  __shared__ int s_rows[kMaxBands + 1];
+  for (int i = threadIdx.x; i < nbands; i += blockDim.x) s_cnt[i] = 0ull;
+  for (int i = threadIdx.x; i <= nbands; i += blockDim.x) s_rows[i] = bands[i];
+  __syncthreads();
+  for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < n;
+       g += (int64_t)gridDim.x * blockDim.x) {
+    const int r = radius[g];
+    if (r <= 0) continue;
+    const float2 p = reinterpret_cast<const float2*>(uv)[g];
+    int x0, x1, y0, y1;
+    tile_rect(p.x, p.y, (float)r, gx, gy, x0, x1, y0, y1);
+    if (x1 <= x0 || y1 <= y0) continue;
+    // the first band that reaches row y0 (bands are short lists: linear scan)
+    int b = 0;
+    while (b < nbands && s_rows[b + 1] <= y0) ++b;
+    for (; b < nbands && s_rows[b] < y1; ++b) {
+      const int rows = min(y1, s_rows[b + 1]) - max(y0, s_rows[b]);
+      if (rows > 0) atomicAdd(&s_cnt[b], (unsigned long long)((x1 - x0) * rows));
+    }
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < nbands; i += blockDim.x)
+    if (s_cnt[i]) atomicAdd(&counts[i], s_cnt[i]);
+}
+
 }  // namespace pgb
 
 using namespace pgb;
@@ -1309,6 +1389,72 @@ int pgb_sort_gaussian_finish_views_capacity(const float* uv, const int32_t* radi
   return sort_finish_impl(uv, radius, tiles_touched, n_per_view * nviews, vt, T, k_capacity, true,
                           scratch_n, bytes_n, scratch_k, bytes_k, info, ids_out, tile_range_out,
                           stream);
+}
+
+}  // extern "C"
+
+extern "C" {
+
+int pgb_band_tiles(const float* uv, const int32_t* radius, int64_t n, int width, int height,
+                   int row0, int row1, int32_t* tiles_out, void* stream) {
+  ViewTable vt;
+  if (n < 0 || !band_view(width, height, row0, row1, vt)) return PGB_ERR_INVALID;
+  if (n > 0 && (!uv || !radius || !tiles_out)) return PGB_ERR_INVALID;
+  if (misaligned(uv, 8)) return PGB_ERR_INVALID;
+  if (n == 0) return PGB_OK;
+  band_tiles_kernel<<<stream_grid(n), kStreamThreads, 0, as_stream(stream)>>>(
+      uv, radius, n, grid_x(width), grid_y(height), row0, row1, tiles_out);
+  return launch_status();
+}
+
+int pgb_sort_gaussian_rebegin(const int32_t* radius, const int32_t* tiles_touched, int64_t n,
+                              void* scratch_n, size_t bytes_n, int64_t* info, void* stream) {
+  if (n < 0 || !info || misaligned(info, 8)) return PGB_ERR_INVALID;
+  if (n > 0 && (!radius || !tiles_touched)) return PGB_ERR_INVALID;
+  const ScratchN L = layout_n(n);
+  if (!scratch_n || bytes_n < L.total || misaligned(scratch_n, 16)) return PGB_ERR_INVALID;
+  cudaStream_t s = as_stream(stream);
+  // the depth order stays; phase two's counters, tile histograms and scan
+  // status start again from zero
+  if (cudaMemsetAsync(info, 0, 2 * sizeof(int64_t), s) != cudaSuccess ||
+      cudaMemsetAsync(at<char>(scratch_n, L.counters), 0, L.depth_hist - L.counters, s) !=
+          cudaSuccess ||
+      cudaMemsetAsync(at<char>(scratch_n, L.tile_hist), 0, L.depth_status - L.tile_hist, s) !=
+          cudaSuccess ||
+      cudaMemsetAsync(at<char>(scratch_n, L.scan_status), 0, L.zero_bytes - L.scan_status, s) !=
+          cudaSuccess)
+    return PGB_ERR_CUDA;
+  if (n == 0) return PGB_OK;
+  band_count_kernel<<<stream_grid(n), kStreamThreads, 0, s>>>(radius, tiles_touched, n, info);
+  return launch_status();
+}
+
+int pgb_sort_gaussian_finish_band(const float* uv, const int32_t* radius,
+                                  const int32_t* tiles_touched, int64_t n, int width, int height,
+                                  int row0, int row1, int64_t k, void* scratch_n, size_t bytes_n,
+                                  void* scratch_k, size_t bytes_k, int64_t* info, int32_t* ids_out,
+                                  int32_t* tile_range_out, void* stream) {
+  ViewTable vt;
+  if (!band_view(width, height, row0, row1, vt)) return PGB_ERR_INVALID;
+  const uint32_t T = (uint32_t)grid_x(width) * (uint32_t)(row1 - row0);
+  return sort_finish_impl(uv, radius, tiles_touched, n, vt, T, k, false, scratch_n, bytes_n,
+                          scratch_k, bytes_k, info, ids_out, tile_range_out, stream);
+}
+
+int pgb_band_counts(const float* uv, const int32_t* radius, int64_t n, int width, int height,
+                    const int32_t* bands, int nbands, unsigned long long* counts, void* stream) {
+  if (n < 0 || width <= 0 || height <= 0 || nbands < 1 || nbands > kMaxBands || !bands ||
+      !counts)
+    return PGB_ERR_INVALID;
+  if (n > 0 && (!uv || !radius)) return PGB_ERR_INVALID;
+  if (misaligned(uv, 8) || misaligned(counts, 8)) return PGB_ERR_INVALID;
+  cudaStream_t s = as_stream(stream);
+  if (cudaMemsetAsync(counts, 0, (size_t)nbands * sizeof(unsigned long long), s) != cudaSuccess)
+    return PGB_ERR_CUDA;
+  if (n == 0) return PGB_OK;
+  band_counts_kernel<<<stream_grid(n), kStreamThreads, 0, s>>>(
+      uv, radius, n, grid_x(width), grid_y(height), bands, nbands, counts);
+  return launch_status();
 }
 
 }  // extern "C"

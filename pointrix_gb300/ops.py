@@ -699,34 +699,195 @@ class _AlphaBlendingPieces(torch.autograd.Function):
         return (d_uv, d_conic, d_op, None, None, None, None, None, d_ndc, *d_feat)
 
 
+# target entries per band of the recompute mode: ids and sort scratch of
+# about 0.7 GB
+BAND_ENTRIES = 1 << 25
+
+
+def band_rows(K: int, H: int, bands=None, max_entries: int = BAND_ENTRIES):
+    """Equal-height tile-row bands [(row0, row1), ...] covering an image of
+    height H: the given number of bands, or enough that a band holds about
+    ``max_entries`` of the image's K entries if they were spread evenly."""
+    gy = (int(H) + TILE - 1) // TILE
+    nb = int(bands) if bands else -(-int(K) // int(max_entries))
+    nb = max(1, min(gy, nb))
+    rows = -(-gy // nb)
+    return [(r0, min(gy, r0 + rows)) for r0 in range(0, gy, rows)]
+
+
+def group_rows(row_k, bands=None, max_entries: int = BAND_ENTRIES):
+    """Bands from the entries of each tile row (``row_k``): consecutive rows
+    grouped front to back, a new band starting when the next row would take
+    the band past the target -- ``max_entries``, or K / ``bands`` when a
+    band count is given.  Returns [(row0, row1, K of the band), ...]."""
+    K = int(sum(row_k))
+    gy = len(row_k)
+    target = max(1, -(-K // max(1, int(bands)))) if bands else int(max_entries)
+    out, r0, acc = [], 0, 0
+    for r, k in enumerate(row_k):
+        k = int(k)
+        if r > r0 and acc + k > target and (not bands or len(out) < int(bands) - 1):
+            out.append((r0, r, acc))
+            r0, acc = r, 0
+        acc += k
+    out.append((r0, gy, acc))
+    return out
+
+
+# the band plan [(row0, row1, entries), ...] of the latest banded call (for
+# measurements)
+last_band_plan: list = []
+
+
+class _BandSort:
+    """The depth sort of one image done once, then phase two of the sort for
+    one band of tile rows at a time (``pgb_sort_gaussian_rebegin`` /
+    ``pgb_sort_gaussian_finish_band``).  The entries of every tile row are
+    counted in one pass and read back once; the bands group rows up to the
+    target, and one set of K-sized buffers, sized for the largest band, is
+    reused by every band."""
+
+    def __init__(self, uv, depth, W, H, radius, tiles, bands=None,
+                 max_entries: int = BAND_ENTRIES):
+        self.h = h = sort_gaussian_begin(uv, depth, W, H, radius, tiles, read_count=False)
+        dev, n = h.dev, h.n
+        gy = (int(H) + TILE - 1) // TILE
+        rows = torch.arange(gy + 1, dtype=torch.int32, device=dev)
+        row_k = torch.empty(gy, dtype=torch.int64, device=dev)
+        call("pgb_band_counts", _ptr(h.uv), _ptr(h.radius), n, h.W, h.H, _ptr(rows), gy,
+             _ptr(row_k), h.stream.cuda_stream)
+        row_k = row_k.tolist()                      # the one synchronisation
+        self.K = int(sum(row_k))
+        self.plan = group_rows(row_k, bands, max_entries)
+        kmax = max(k for _, _, k in self.plan)
+        _, self.bk = _sort_scratch(n, kmax, h.W, h.H)
+        self.scratch_k = torch.empty(max(self.bk, 1), dtype=torch.uint8, device=dev)
+        self.ids = torch.empty(max(kmax, 1), dtype=torch.int32, device=dev)
+        self.tiles_b = torch.empty_like(h.tiles)
+
+    def band(self, i):
+        """(ids [K_b] -- a view of the shared buffer --, tile_range
+        [gx * rows, 2]) of band i."""
+        h = self.h
+        r0, r1, k = self.plan[i]
+        dev, n, W, H = h.dev, h.n, h.W, h.H
+        gx = (W + TILE - 1) // TILE
+        s = h.stream.cuda_stream
+        call("pgb_band_tiles", _ptr(h.uv), _ptr(h.radius), n, W, H, r0, r1, _ptr(self.tiles_b), s)
+        call("pgb_sort_gaussian_rebegin", _ptr(h.radius), _ptr(self.tiles_b), n,
+             _ptr(h.scratch_n), h.bn, _ptr(h.info), s)
+        ids = self.ids[:k]
+        rng = torch.empty(gx * (r1 - r0), 2, dtype=torch.int32, device=dev)
+        with _timed("sort_finish", dev, (3 + _tile_passes(rng.shape[0])) if (k and n) else 0):
+            call("pgb_sort_gaussian_finish_band", _ptr(h.uv), _ptr(h.radius), _ptr(self.tiles_b),
+                 n, W, H, r0, r1, k, _ptr(h.scratch_n), h.bn, _ptr(self.scratch_k), self.bk,
+                 _ptr(h.info), _ptr(ids) if k else None, _ptr(rng), s)
+        _defer_check(h.info[1:], "sort_gaussian (band tile passes)")
+        return ids, rng
+
+
+def _blend_band_forward(uv, conic, opacity, feature, ids, rng, bg, W, H, r0, r1, pack, records,
+                        out, final_T, ncon):
+    n, C = feature.shape
+    dev = feature.device
+    status = _status_word(dev)
+
+    def run(batch):
+        call("pgb_alpha_blending_forward_band", _ptr(uv), _ptr(conic), _ptr(opacity),
+             _ptr(feature), n, C, _ptr(ids), ids.numel(), _ptr(rng), float(bg), W, H, r0, r1,
+             1 if pack else 0, _ptr(records), _ptr(out), _ptr(final_T), _ptr(ncon),
+             _ptr(status), _stream(dev), batch)
+
+    key = autotune.workload_class("blend_fwd", C, W * (r1 - r0) * TILE, ids.numel(),
+                                  rng.shape[0])
+    batch = autotune.choose(key, _blend_batches(0), run, dev) if n else 0
+    with _timed("alpha_blending_fwd", dev, 2 if (pack and n) else 1):
+        run(batch)
+
+
+def _rasterize_banded_forward(uv, conic, opacity, feature, depth, radius, tiles, bg, W, H, bands,
+                              backward=None):
+    """Sort and blend one band of tile rows at a time.  ``backward`` =
+    (d_out, grad outputs...) runs each band's blend backward right after the
+    band's forward, while its lists are alive."""
+    n, C = feature.shape
+    dev = feature.device
+    bs = _BandSort(uv, depth, W, H, radius, tiles, bands)
+    plan = bs.plan
+    last_band_plan[:] = plan
+    rf = _lib.lib().pgb_blend_record_floats(C)
+    records = torch.empty(n, rf, dtype=torch.float32, device=dev)
+    out = torch.empty(C, H, W, dtype=torch.float32, device=dev)
+    final_T = torch.empty(H, W, dtype=torch.float32, device=dev)
+    ncon = torch.empty(H, W, dtype=torch.int32, device=dev)
+    for i, (r0, r1, _) in enumerate(plan):
+        ids, rng = bs.band(i)
+        _blend_band_forward(uv, conic, opacity, feature, ids, rng, bg, W, H, r0, r1, i == 0,
+                            records, out, final_T, ncon)
+        if backward is not None:
+            backward(records, ids, rng, final_T, ncon, r0, r1, i == 0, i == len(plan) - 1)
+        del ids, rng
+    return out, len(plan)
+
+
 class _RasterizeRecompute(torch.autograd.Function):
     """Sort + blend whose backward recomputes the tile lists, the records and
     the per-pixel final transmittance / last-contributor counts instead of
-    keeping them alive between forward and backward."""
+    keeping them alive between forward and backward.  Both directions work
+    one band of tile rows at a time (``band_rows``), so the K-sized sort
+    buffers and id list hold one band's entries."""
 
     @staticmethod
-    def forward(ctx, uv, conic, opacity, feature, depth, radius, tiles, bg, W, H, ndc, capacity):
-        ids, rng = sort_gaussian(uv, depth, W, H, radius, tiles, capacity=capacity)
-        _, out, _, _ = _blend_forward_raw(uv, conic, opacity, feature, ids, rng, bg, W, H)
+    def forward(ctx, uv, conic, opacity, feature, depth, radius, tiles, bg, W, H, ndc, bands):
+        out, _ = _rasterize_banded_forward(uv, conic, opacity, feature, depth, radius, tiles, bg,
+                                           W, H, bands)
         ctx.save_for_backward(uv, conic, opacity, feature, depth, radius, tiles)
-        ctx.cfg = (float(bg), W, H, ndc is not None, capacity)
+        ctx.cfg = (float(bg), W, H, ndc is not None, bands)
         return out
 
     @staticmethod
     def backward(ctx, d_out):
         uv, conic, opacity, feature, depth, radius, tiles = ctx.saved_tensors
-        bg, W, H, has_ndc, capacity = ctx.cfg
+        bg, W, H, has_ndc, bands = ctx.cfg
         n, C = feature.shape
-        ids, rng = sort_gaussian(uv, depth, W, H, radius, tiles, capacity=capacity)
-        records, _, final_T, ncon = _blend_forward_raw(uv, conic, opacity, feature, ids, rng, bg, W, H)
-        d_uv, d_conic, d_op, d_feat = _blend_backward_raw(records, ids, rng, final_T, ncon, d_out,
-                                                          n, C, bg, W, H)
+        dev = feature.device
+        d_out = _c(d_out)
+        grec = torch.empty(n, _lib.lib().pgb_blend_grad_record_floats(C), dtype=torch.float32,
+                           device=dev)
+        d_uv = torch.empty(n, 2, dtype=torch.float32, device=dev)
+        d_conic = torch.empty(n, 3, dtype=torch.float32, device=dev)
+        d_op = torch.empty(n, dtype=torch.float32, device=dev)
+        d_feat = torch.empty(n, C, dtype=torch.float32, device=dev)
+        status = _status_word(dev)
+
+        def band_backward(records, ids, rng, final_T, ncon, r0, r1, first, last):
+            def run(batch, first=first, last=last):
+                call("pgb_alpha_blending_backward_band", _ptr(records), n, C, _ptr(ids),
+                     ids.numel(), _ptr(rng), bg, W, H, r0, r1, _ptr(final_T), _ptr(ncon),
+                     _ptr(d_out), _ptr(grec), 1 if first else 0, 1 if last else 0, _ptr(d_uv),
+                     _ptr(d_conic), _ptr(d_op), _ptr(d_feat), _ptr(status), _stream(dev), batch)
+            key = autotune.workload_class("blend_bwd", C, W * (r1 - r0) * TILE, ids.numel(),
+                                          rng.shape[0])
+            if key not in autotune.table() and autotune._enabled and not _capturing():
+                # timing runs add into the records: time them on a scratch copy
+                saved = grec.clone() if not first else None
+                batch = autotune.choose(key, _blend_batches(1),
+                                        lambda b: run(b, first=True, last=False), dev)
+                if saved is not None:
+                    grec.copy_(saved)
+            else:
+                batch = autotune.choose(key, _blend_batches(1), run, dev)
+            with _timed("alpha_blending_bwd", dev, 2 if last else 1):
+                run(batch)
+
+        _rasterize_banded_forward(uv, conic, opacity, feature, depth, radius, tiles, bg, W, H,
+                                  bands, backward=band_backward)
         d_ndc = d_uv.clone() if has_ndc else None
         return d_uv, d_conic, d_op, d_feat, None, None, None, None, None, None, d_ndc, None
 
 
 def rasterize(uv, conic, opacity, feature, depth, radius, tiles_touched, bg, W, H, ndc=None,
-              recompute=False, capacity=None):
+              recompute=False, capacity=None, bands=None):
     """``sort_gaussian`` followed by ``alpha_blending`` -> [C,H,W].
     ``feature`` is [N,C] or a list of [N,w] pieces (blended as their
     concatenation, without building it).
@@ -736,8 +897,13 @@ def rasterize(uv, conic, opacity, feature, depth, radius, tiles_touched, bg, W, 
     instead of keeping the tile lists, records and per-pixel state alive from
     the forward: less memory held between forward and backward (what limits
     4K views of millions of Gaussians), one more sort and blend forward per
-    step.  Gradients are the same in both modes.  ``capacity`` is passed to
-    :func:`sort_gaussian` (K kept on the device, no synchronisation)."""
+    step.  Gradients are the same in both modes.  The recompute mode also
+    sorts and blends one band of tile rows at a time, in both directions
+    (``bands`` of them, or as many as keep a band near ``BAND_ENTRIES``
+    entries), so the K-sized sort buffers and id list -- the peak of a large
+    view -- hold one band's entries.  ``capacity`` is passed to
+    :func:`sort_gaussian` in the stored mode (K kept on the device, no
+    synchronisation); the recompute mode reads each band's K back."""
     if not recompute:
         ids, rng = sort_gaussian(uv, depth, W, H, radius, tiles_touched, capacity=capacity)
         if isinstance(feature, (list, tuple)):
@@ -753,7 +919,7 @@ def rasterize(uv, conic, opacity, feature, depth, radius, tiles_touched, bg, W, 
         bg = float(bg)
     return _RasterizeRecompute.apply(_c(uv), _c(conic), _c(opacity.reshape(n)), _c(feature),
                                      depth, radius, tiles_touched, bg, int(W), int(H), ndc,
-                                     capacity)
+                                     bands)
 
 
 def alpha_blending_with_state(uv, conic, opacity, feature, gaussian_ids_sorted, tile_range, bg, W, H,

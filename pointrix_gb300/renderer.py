@@ -64,6 +64,9 @@ class MsplatRender:
         # recompute the sorted tile lists and per-pixel state in the backward
         # instead of keeping them from the forward (memory for 4K views)
         recompute_backward: bool = False
+        # bands of tile rows for the recompute mode (0: enough that a band
+        # holds about ops.BAND_ENTRIES entries)
+        recompute_bands: int = 0
         # view direction + SH mask + compute_sh + 0.5 + clamp in one kernel
         # (when shs is dense [N,K,3] storage)
         fused_view_colour: bool = True
@@ -140,6 +143,7 @@ class MsplatRender:
         image = ops.rasterize(uv, conic, opacity, packed, depth, radius, tiles_touched,
                               self.bg_color, width, height, ndc,
                               recompute=self.cfg.recompute_backward,
+                              bands=self.cfg.recompute_bands or None,
                               capacity=self.cfg.sort_capacity or None)
         return {
             "rendered_features": image,

@@ -141,3 +141,18 @@ def test_render_batch_aggregates_views_as_pointrix(monkeypatch):
     assert isinstance(out["uv_points"], list) and len(out["uv_points"]) == B
     assert out["visibility"].tolist() == [True, True, True, False, False]
     assert torch.equal(out["radii"], torch.arange(N, dtype=torch.int32) * B)
+
+
+def test_band_grouping_of_tile_rows():
+    """The recompute mode's bands: consecutive tile rows grouped up to the
+    target, covering every row once, entry counts preserved."""
+    from pointrix_gb300.ops import band_rows, group_rows
+    rows = [3, 9, 0, 4, 4, 4, 12, 1]
+    for kw in (dict(max_entries=10), dict(bands=3), dict(bands=1), dict(max_entries=1)):
+        plan = group_rows(rows, **kw)
+        assert plan[0][0] == 0 and plan[-1][1] == len(rows)
+        assert all(a[1] == b[0] and a[0] < a[1] for a, b in zip(plan, plan[1:]))
+        assert [k for *_, k in plan] == [sum(rows[a:b]) for a, b, _ in plan]
+    assert len(group_rows(rows, bands=3)) == 3
+    assert group_rows(rows, bands=1) == [(0, 8, 37)]
+    assert band_rows(100, 16 * 9, bands=3) == [(0, 3), (3, 6), (6, 9)]

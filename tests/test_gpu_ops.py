@@ -349,16 +349,19 @@ def test_bad_arguments_raise(small):
         ops.sort_gaussian(p.uv, p.depth, p.W, p.H, p.radius.float(), p.tiles)
 
 
-def test_recompute_backward_matches_stored(small):
+@pytest.mark.parametrize("bands", [None, 3, 16])
+def test_recompute_backward_matches_stored(small, bands):
     """rasterize(recompute=True) re-runs the sort and blend forward in the
-    backward; image and gradients equal the stored mode (1e-4 relative L2
-    for gradients: the backward's float atomics may add in another order)."""
+    backward, one band of tile rows at a time in both directions; image and
+    gradients equal the stored mode (1e-4 relative L2 for gradients: the
+    backward's float atomics may add in another order)."""
     p = small
     outs = {}
     for mode in (False, True):
         leaves = [t.detach().clone().requires_grad_(True) for t in (p.uv, p.conic, p.op, p.feat)]
         ndc = torch.zeros_like(p.uv, requires_grad=True)
-        img = ops.rasterize(*leaves, p.depth, p.radius, p.tiles, 0.2, p.W, p.H, ndc, recompute=mode)
+        img = ops.rasterize(*leaves, p.depth, p.radius, p.tiles, 0.2, p.W, p.H, ndc, recompute=mode,
+                            bands=bands)
         g = torch.Generator().manual_seed(5)
         img.backward(torch.randn(img.shape, generator=g).to(DEV))
         outs[mode] = (img.detach(), [t.grad for t in leaves], ndc.grad)
@@ -452,4 +455,28 @@ def test_blend_pair_census_counts_the_replayed_and_composited_pairs(small):
         ref += int(((pw <= 0) & (a >= 1 / 255) & before).sum())
     assert 0 < comp <= ev
     assert abs(comp - ref) <= max(2, 1e-4 * ref), (comp, ref)
+    ops.check_device_status()
+
+
+@pytest.mark.parametrize("bands", [1, 2, 5, 16])
+def test_band_sort_lists_are_the_whole_image_lists(small, bands):
+    """Each band's (band-local) tile lists are the whole image's lists of
+    the same tiles, bit for bit; the bands cover every tile row once and
+    their entry counts add up to K."""
+    p = small
+    gx, gy = O.tile_grid(p.W, p.H)
+    bs = ops._BandSort(p.uv, p.depth, p.W, p.H, p.radius, p.tiles, bands)
+    assert bs.K == p.ids.numel()
+    ids, rng = cpu(p.ids), cpu(p.rng).long()
+    plan = bs.plan
+    assert plan[0][0] == 0 and plan[-1][1] == gy and len(plan) <= min(bands, gy)
+    assert all(a[1] == b[0] for a, b in zip(plan, plan[1:]))
+    assert sum(k for _, _, k in plan) == bs.K
+    for i, (r0, r1, k) in enumerate(plan):
+        bi, br = (cpu(t) for t in bs.band(i))
+        br = br.long()
+        assert br.shape[0] == gx * (r1 - r0) and bi.numel() == k
+        for tl in range(br.shape[0]):
+            t = r0 * gx + tl
+            assert torch.equal(bi[br[tl, 0]:br[tl, 1]], ids[rng[t, 0]:rng[t, 1]]), (r0, r1, tl)
     ops.check_device_status()
