@@ -437,7 +437,7 @@ MULTIVIEW_WORKLOAD = ("batched multi-view: 3,000,000 Gaussians SH3, 16 views on 
                       "forward+backward for all views")
 
 
-def multiview_measure(device, n=3_000_000, views=16, steps=3):
+def multiview_measure(device, n=3_000_000, views=16, steps=20):
     """Mpix/s of the batched forward+backward over all views -- one sort and
     one blend launch each way for the whole batch, the step captured once as
     a CUDA graph and replayed -- against the per-view loop of plain launches
@@ -485,6 +485,8 @@ def multiview_measure(device, n=3_000_000, views=16, steps=3):
         return loss
 
     def timed(fn):
+        """Per-step latency of ``steps`` steps (each bracketed by
+        synchronisations), after one untimed step."""
         fn()
         torch.cuda.synchronize(device)
         times = []
@@ -493,9 +495,12 @@ def multiview_measure(device, n=3_000_000, views=16, steps=3):
             t0 = time.perf_counter()
             fn()
             torch.cuda.synchronize(device)
-            times.append(time.perf_counter() - t0)
-        ms = 1e3 * statistics.mean(times)
-        return {"ms_per_step": ms, "mpix_per_s": pix / (ms * 1e-3) / 1e6}
+            times.append(1e3 * (time.perf_counter() - t0))
+        ms = statistics.mean(times)
+        q = sorted(times)
+        return {"ms_per_step": ms, "mpix_per_s": pix / (ms * 1e-3) / 1e6, "steps": steps,
+                "p50_ms": statistics.median(q), "p99_ms": q[min(len(q) - 1, int(0.99 * len(q)))],
+                "max_ms": q[-1]}
 
     res = {"per_view_loop": timed(per_view)}
     per_view_imgs = [t.detach().clone() for t in last["per_view"]]

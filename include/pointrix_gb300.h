@@ -527,6 +527,29 @@ int pgb_preprocess_backward(const float* xyz, const float* scales, const float* 
                             float* d_scales, float* d_uquats, float* d_intr, float* d_extr,
                             void* scratch, size_t scratch_bytes, void* stream);
 
+/* pgb_preprocess_views_*: the same for V views of one set of Gaussians (the
+ * batched multi-view path; no msplat counterpart): view v's camera is
+ * intrs[4v..4v+3] and extrs[12v..12v+11] (device, [V,4] and [V,3,4]), its
+ * image size sizes[2v], sizes[2v+1] (host); outputs are view-major [V*N, .]
+ * (element v*N + i), each equal bit for bit to the single-view call for that
+ * view.  The backward takes the view-major d uv / d depth / d conic and
+ * writes d xyz, d scales, d quats summed over the views (in view order, one
+ * thread per Gaussian: deterministic) and d_intrs [V,4], d_extrs [V,3,4]
+ * (scratch of pgb_camera_grad_views_scratch_bytes(V)).  V <= 64. */
+size_t pgb_camera_grad_views_scratch_bytes(int nviews);
+int pgb_preprocess_views_forward(const float* xyz, const float* scales, const float* uquats,
+                                 int64_t n, const float* intrs, const float* extrs,
+                                 const int32_t* sizes, int nviews, float nearest, float extent,
+                                 float* uv, float* depth, float* conic, int32_t* radius,
+                                 int32_t* tiles_touched, void* stream);
+int pgb_preprocess_views_backward(const float* xyz, const float* scales, const float* uquats,
+                                  int64_t n, const float* intrs, const float* extrs,
+                                  const int32_t* sizes, int nviews, float nearest, float extent,
+                                  const int32_t* radius, const float* d_uv, const float* d_depth,
+                                  const float* d_conic, float* d_xyz, float* d_scales,
+                                  float* d_uquats, float* d_intrs, float* d_extrs, void* scratch,
+                                  size_t scratch_bytes, void* stream);
+
 /* pgb_ssim_*: the SSIM of pointrix/model/loss.py:71-125 (11x11 Gaussian
  * window, sigma 1.5, zero padding, C1 = 0.01^2, C2 = 0.03^2, mean over all
  * pixels) of x against the target y, both `planes` contiguous float planes of

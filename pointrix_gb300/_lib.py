@@ -99,10 +99,16 @@ SIGNATURES.update({
     "pgb_preprocess_backward": [vp, vp, vp, i64, vp, vp, i32, i32, f32, f32, vp, vp, vp, vp, vp, vp,
                                 vp, vp, vp, vp, szt, vp],
     "pgb_ssim_forward": [vp, vp, i32, i32, i32, vp, i64, vp, vp],
+    "pgb_camera_grad_views_scratch_bytes": [i32],
+    "pgb_preprocess_views_forward": [vp, vp, vp, i64, vp, vp, vp, i32, f32, f32, vp, vp, vp, vp,
+                                     vp, vp],
+    "pgb_preprocess_views_backward": [vp, vp, vp, i64, vp, vp, vp, i32, f32, f32, vp, vp, vp, vp,
+                                      vp, vp, vp, vp, vp, vp, szt, vp],
     "pgb_ssim_backward": [vp, vp, i32, i32, i32, vp, vp, vp],
 })
 
 _RESTYPES = {"pgb_status_string": C.c_char_p, "pgb_camera_grad_scratch_bytes": szt,
+             "pgb_camera_grad_views_scratch_bytes": szt,
              "pgb_ssim_scratch_doubles": i64}
 
 

@@ -602,6 +602,137 @@ __global__ void preprocess_bwd_kernel(
   block_write_partials(acc, partials);
 }
 
+// ---------------------------------------------------------------------------
+// Fused preprocessing of V views of the same Gaussians (the batched
+// multi-view path): view v's camera is intrs[4v..], extrs[12v..], its image
+// size sizes[2v], sizes[2v + 1]; outputs are view-major (element v N + i).
+// The forward is the single-view arithmetic per (Gaussian, view), so every
+// output equals the single-view call's bit for bit.  The backward loops the
+// views in order inside one thread per Gaussian, so the Gaussian gradients
+// are summed over views in registers and written once per view pass
+// (read-modify-write by the thread that owns the Gaussian: deterministic),
+// and each view's camera partials are reduced per block as in the
+// single-view kernel.
+// ---------------------------------------------------------------------------
+struct ViewSizes {
+  int nviews;
+  int w[kMaxViews], h[kMaxViews];
+};
+
+__global__ void preprocess_views_fwd_kernel(
+    const float* __restrict__ xyz, const float* __restrict__ scales, const float* __restrict__ q,
+    int64_t n, const float* __restrict__ intrs, const float* __restrict__ extrs,
+    const ViewSizes vs, float nearest, float extent, float* __restrict__ uv,
+    float* __restrict__ depth, float* __restrict__ conic, int32_t* __restrict__ radius,
+    int32_t* __restrict__ tiles) {
+  const int v = blockIdx.y;
+  const Cam cm = load_cam(intrs + 4 * v, extrs + 12 * v);
+  const int W = vs.w[v], H = vs.h[v];
+  const int gx = grid_x(W), gy = grid_y(H);
+  const int64_t o = (int64_t)v * n;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const float x = xyz[3 * i], y = xyz[3 * i + 1], z = xyz[3 * i + 2];
+    float px, py, pz, u, vv;
+    cam_point(cm, x, y, z, px, py, pz);
+    const bool vis = project_visible(cm, px, py, pz, W, H, nearest, extent, u, vv);
+    const float2 p = vis ? make_float2(u, vv) : make_float2(0.f, 0.f);
+    const int64_t e = o + i;
+    reinterpret_cast<float2*>(uv)[e] = p;
+    depth[e] = vis ? pz : 0.f;
+    float c0 = 0.f, c1 = 0.f, c2 = 0.f;
+    int rad = 0, nt = 0;
+    if (vis) {
+      float s6[6];
+      cov3d_one(scales, q, i, s6);
+      ewa_fwd_one(cm, W, H, gx, gy, x, y, z, s6, p, c0, c1, c2, rad, nt);
+    }
+    conic[3 * e] = c0;
+    conic[3 * e + 1] = c1;
+    conic[3 * e + 2] = c2;
+    radius[e] = rad;
+    tiles[e] = nt;
+  }
+}
+
+__global__ void preprocess_views_bwd_kernel(
+    const float* __restrict__ xyz, const float* __restrict__ scales, const float* __restrict__ q,
+    int64_t n, const float* __restrict__ intrs, const float* __restrict__ extrs,
+    const ViewSizes vs, float nearest, float extent, const int32_t* __restrict__ radius,
+    const float* __restrict__ d_uv, const float* __restrict__ d_depth,
+    const float* __restrict__ d_conic, float* __restrict__ d_xyz, float* __restrict__ d_scales,
+    float* __restrict__ d_q, float* __restrict__ partials) {
+  for (int v = 0; v < vs.nviews; ++v) {
+    const Cam cm = load_cam(intrs + 4 * v, extrs + 12 * v);
+    const int W = vs.w[v], H = vs.h[v];
+    const int64_t o = (int64_t)v * n;
+    float acc[16];
+#pragma unroll
+    for (int k = 0; k < 16; ++k) acc[k] = 0.f;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+      const int64_t e = o + i;
+      const float x = xyz[3 * i], y = xyz[3 * i + 1], z = xyz[3 * i + 2];
+      float px, py, pz, u, uy;
+      cam_point(cm, x, y, z, px, py, pz);
+      float gx = 0.f, gy = 0.f, gz = 0.f;
+      float ds[3] = {0.f, 0.f, 0.f};
+      float4 dq = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (project_visible(cm, px, py, pz, W, H, nearest, extent, u, uy)) {
+        project_bwd_one(cm, x, y, z, px, py, pz, reinterpret_cast<const float2*>(d_uv)[e],
+                        d_depth[e], gx, gy, gz, acc);
+        if (radius[e] > 0) {
+          float s6[6];
+          cov3d_one(scales, q, i, s6);
+          float ex = 0.f, ey = 0.f, ez = 0.f;
+          float dS[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+          ewa_bwd_one(cm, W, H, x, y, z, s6, d_conic[3 * e], d_conic[3 * e + 1],
+                      d_conic[3 * e + 2], ex, ey, ez, dS, acc);
+          gx = gx + ex;
+          gy = gy + ey;
+          gz = gz + ez;
+          cov3d_grad_one(scales, q, i, dS, ds, dq);
+        }
+      }
+      if (v > 0) {  // this thread wrote Gaussian i's sums of the earlier views
+        gx = d_xyz[3 * i] + gx;
+        gy = d_xyz[3 * i + 1] + gy;
+        gz = d_xyz[3 * i + 2] + gz;
+        ds[0] = d_scales[3 * i] + ds[0];
+        ds[1] = d_scales[3 * i + 1] + ds[1];
+        ds[2] = d_scales[3 * i + 2] + ds[2];
+        const float4 p = reinterpret_cast<const float4*>(d_q)[i];
+        dq = make_float4(p.x + dq.x, p.y + dq.y, p.z + dq.z, p.w + dq.w);
+      }
+      d_xyz[3 * i] = gx;
+      d_xyz[3 * i + 1] = gy;
+      d_xyz[3 * i + 2] = gz;
+      d_scales[3 * i] = ds[0];
+      d_scales[3 * i + 1] = ds[1];
+      d_scales[3 * i + 2] = ds[2];
+      reinterpret_cast<float4*>(d_q)[i] = dq;
+    }
+    block_write_partials(acc, partials + (size_t)v * gridDim.x * 16);
+    __syncthreads();  // the partials' shared buffer is reused by the next view
+  }
+}
+
+// One block per view: view v's camera gradient from its block partials.
+__global__ void __launch_bounds__(16 * kCamTPC) cam_grad_views_finish_kernel(
+    const float* __restrict__ partials, int nblocks, float* __restrict__ d_intrs,
+    float* __restrict__ d_extrs) {
+  __shared__ double s[16 * kCamTPC];
+  const int v = blockIdx.x;
+  const double t = column_sum<16, kCamTPC>(partials + (size_t)v * nblocks * 16, nblocks, 16, s);
+  if (threadIdx.x % kCamTPC == 0) {
+    const int col = threadIdx.x / kCamTPC;
+    if (col < 4)
+      d_intrs[4 * v + col] = (float)t;
+    else
+      d_extrs[12 * v + col - 4] = (float)t;
+  }
+}
+
 }  // namespace pgb
 
 using namespace pgb;
@@ -734,6 +865,65 @@ int pgb_preprocess_backward(const float* xyz, const float* scales, const float* 
       xyz, scales, uquats, n, intr, extr, width, height, nearest, extent, radius, d_uv, d_depth,
       d_conic, d_xyz, d_scales, d_uquats, partials);
   cam_grad_finish_kernel<<<1, 16 * kCamTPC, 0, s>>>(partials, grid, d_intr, d_extr);
+  return launch_status();
+}
+
+static bool view_sizes(const int32_t* sizes, int nviews, ViewSizes& vs) {
+  if (!sizes || nviews < 1 || nviews > kMaxViews) return false;
+  vs.nviews = nviews;
+  for (int v = 0; v < nviews; ++v) {
+    vs.w[v] = sizes[2 * v];
+    vs.h[v] = sizes[2 * v + 1];
+    if (vs.w[v] <= 0 || vs.h[v] <= 0) return false;
+  }
+  return true;
+}
+
+size_t pgb_camera_grad_views_scratch_bytes(int nviews) {
+  return (size_t)(nviews > 0 ? nviews : 0) * kCamGradBlocksMax * 16 * sizeof(float);
+}
+
+int pgb_preprocess_views_forward(const float* xyz, const float* scales, const float* uquats,
+                                 int64_t n, const float* intrs, const float* extrs,
+                                 const int32_t* sizes, int nviews, float nearest, float extent,
+                                 float* uv, float* depth, float* conic, int32_t* radius,
+                                 int32_t* tiles_touched, void* stream) {
+  ViewSizes vs;
+  if (n < 0 || !view_sizes(sizes, nviews, vs)) return PGB_ERR_INVALID;
+  if (n == 0) return PGB_OK;
+  if (!xyz || !scales || !uquats || !intrs || !extrs || !uv || !depth || !conic || !radius ||
+      !tiles_touched || misaligned(uquats, 16) || misaligned(uv, 8))
+    return PGB_ERR_INVALID;
+  const dim3 grid(stream_grid(n), nviews);
+  preprocess_views_fwd_kernel<<<grid, kStreamThreads, 0, as_stream(stream)>>>(
+      xyz, scales, uquats, n, intrs, extrs, vs, nearest, extent, uv, depth, conic, radius,
+      tiles_touched);
+  return launch_status();
+}
+
+int pgb_preprocess_views_backward(const float* xyz, const float* scales, const float* uquats,
+                                  int64_t n, const float* intrs, const float* extrs,
+                                  const int32_t* sizes, int nviews, float nearest, float extent,
+                                  const int32_t* radius, const float* d_uv, const float* d_depth,
+                                  const float* d_conic, float* d_xyz, float* d_scales,
+                                  float* d_uquats, float* d_intrs, float* d_extrs, void* scratch,
+                                  size_t scratch_bytes, void* stream) {
+  ViewSizes vs;
+  if (n < 0 || !view_sizes(sizes, nviews, vs)) return PGB_ERR_INVALID;
+  if (scratch_bytes < pgb_camera_grad_views_scratch_bytes(nviews) || !scratch || !d_intrs ||
+      !d_extrs)
+    return PGB_ERR_INVALID;
+  if (n > 0 && (!xyz || !scales || !uquats || !intrs || !extrs || !radius || !d_uv || !d_depth ||
+                !d_conic || !d_xyz || !d_scales || !d_uquats || misaligned(uquats, 16) ||
+                misaligned(d_uquats, 16) || misaligned(d_uv, 8)))
+    return PGB_ERR_INVALID;
+  cudaStream_t s = as_stream(stream);
+  const int grid = stream_grid(n);
+  float* partials = static_cast<float*>(scratch);
+  preprocess_views_bwd_kernel<<<grid, kStreamThreads, 0, s>>>(
+      xyz, scales, uquats, n, intrs, extrs, vs, nearest, extent, radius, d_uv, d_depth, d_conic,
+      d_xyz, d_scales, d_uquats, partials);
+  cam_grad_views_finish_kernel<<<nviews, 16 * kCamTPC, 0, s>>>(partials, grid, d_intrs, d_extrs);
   return launch_status();
 }
 

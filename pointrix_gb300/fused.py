@@ -354,6 +354,79 @@ def preprocess(position, scaling, rotation, intr, extr, W, H, nearest=NEAREST_DE
                              int(W), int(H), float(nearest), float(extent))
 
 
+class _PreprocessViews(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, xyz, scales, quats, intrs, extrs, sizes, nearest, extent):
+        n = xyz.shape[0]
+        V = len(sizes)
+        dev = xyz.device
+        uv = torch.empty(V * n, 2, dtype=torch.float32, device=dev)
+        depth = torch.empty(V * n, 1, dtype=torch.float32, device=dev)
+        conic = torch.empty(V * n, 3, dtype=torch.float32, device=dev)
+        radius = torch.empty(V * n, dtype=torch.int32, device=dev)
+        tiles = torch.empty(V * n, dtype=torch.int32, device=dev)
+        sz = _sizes_table(sizes)
+        with _timed("preprocess_fwd", dev, 1 if n else 0):
+            call("pgb_preprocess_views_forward", _ptr(xyz), _ptr(scales), _ptr(quats), n,
+                 _ptr(intrs), _ptr(extrs), sz, V, nearest, extent, _ptr(uv), _ptr(depth),
+                 _ptr(conic), _ptr(radius), _ptr(tiles), _stream(dev))
+        ctx.save_for_backward(xyz, scales, quats, intrs, extrs, radius)
+        ctx.cfg = (tuple(sizes), nearest, extent)
+        ctx.mark_non_differentiable(radius, tiles)
+        return uv, depth, conic, radius, tiles
+
+    @staticmethod
+    def backward(ctx, d_uv, d_depth, d_conic, _d_radius, _d_tiles):
+        xyz, scales, quats, intrs, extrs, radius = ctx.saved_tensors
+        sizes, nearest, extent = ctx.cfg
+        n, V = xyz.shape[0], len(sizes)
+        dev = xyz.device
+        g = lambda t, *shape: torch.zeros(*shape, device=dev) if t is None else _c(t)  # noqa: E731
+        d_uv, d_depth, d_conic = g(d_uv, V * n, 2), g(d_depth, V * n, 1), g(d_conic, V * n, 3)
+        d_xyz, d_scales, d_quats = torch.empty_like(xyz), torch.empty_like(scales), torch.empty_like(quats)
+        d_intrs = torch.empty(V, 4, dtype=torch.float32, device=dev)
+        d_extrs = torch.empty(V, 3, 4, dtype=torch.float32, device=dev)
+        nbytes = _lib.lib().pgb_camera_grad_views_scratch_bytes(V)
+        scratch = torch.empty(nbytes, dtype=torch.uint8, device=dev)
+        with _timed("preprocess_bwd", dev, 2):
+            call("pgb_preprocess_views_backward", _ptr(xyz), _ptr(scales), _ptr(quats), n,
+                 _ptr(intrs), _ptr(extrs), _sizes_table(sizes), V, nearest, extent, _ptr(radius),
+                 _ptr(d_uv), _ptr(d_depth), _ptr(d_conic), _ptr(d_xyz), _ptr(d_scales),
+                 _ptr(d_quats), _ptr(d_intrs), _ptr(d_extrs), _ptr(scratch), nbytes, _stream(dev))
+        return d_xyz, d_scales, d_quats, d_intrs, d_extrs, None, None, None
+
+
+def _sizes_table(sizes):
+    import ctypes
+    arr = (ctypes.c_int32 * (2 * len(sizes)))()
+    for i, (W, H) in enumerate(sizes):
+        arr[2 * i], arr[2 * i + 1] = int(W), int(H)
+    return arr
+
+
+def preprocess_views(position, scaling, rotation, intrs, extrs, sizes, nearest=NEAREST_DEFAULT,
+                     extent=EXTENT_DEFAULT):
+    """:func:`preprocess` for V views at once: ``intrs`` [V,4], ``extrs``
+    [V,3,4], ``sizes`` [(W, H)] * V; returns view-major uv [V*N,2], depth
+    [V*N,1], conic [V*N,3], radius [V*N], tiles_touched [V*N] (each view's
+    block equal bit for bit to its single-view call).  One kernel each way:
+    the backward sums the Gaussian gradients over the views itself, so the
+    V per-view gradients are never materialised and added."""
+    n = position.shape[0]
+    V = len(sizes)
+    if V < 1 or V > 64:
+        raise ValueError(f"preprocess_views takes 1..64 views, got {V}")
+    for name, t, last in (("position", position, 3), ("scaling", scaling, 3), ("rotation", rotation, 4)):
+        if t.dim() != 2 or t.shape[0] != n or t.shape[1] != last:
+            raise ValueError(f"{name} must be [N,{last}], got {tuple(t.shape)}")
+        if not (t.is_cuda and t.dtype == torch.float32):
+            raise ValueError(f"{name} must be a CUDA float32 tensor")
+    intrs = _c(intrs.reshape(V, 4))
+    extrs = _c(extrs.reshape(V, 3, 4))
+    return _PreprocessViews.apply(_c(position), _c(scaling), _c16(rotation), intrs, extrs,
+                                  [tuple(map(int, s)) for s in sizes], float(nearest), float(extent))
+
+
 # ---------------------------------------------------------------------------
 # camera pose of a differentiable camera
 # ---------------------------------------------------------------------------

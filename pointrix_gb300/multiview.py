@@ -153,18 +153,20 @@ def render_views(position, scaling, rotation, opacity, shs, cams, bg=0.0, render
     Returns (list of [C,H,W] images, list of per-view uv, list of radius)."""
     n = position.shape[0]
     K = shs.shape[1]
+    V = len(cams)
     active = K if sh_active is None else sh_active
-    uvs, depths, conics, radii, tiles, feats = [], [], [], [], [], []
-    use_fused = fused.sh_rgb_supported(shs) and len(cams) <= MAX_VIEWS
-    shc = shs.permute(0, 2, 1)
-    rgb_all = None
-    if use_fused:  # every view's colour in one pass over the coefficients
+    sizes = [(cam.W, cam.H) for cam in cams]
+    if V > MAX_VIEWS:
+        raise ValueError(f"render_views takes at most {MAX_VIEWS} views, got {V}")
+    # every view's colour in one pass over the coefficients, every view's
+    # projection in one kernel (gradients summed over views inside it)
+    if fused.sh_rgb_supported(shs):
         centres = torch.stack([cam.center.reshape(3) for cam in cams])
-        rgb_all = fused.sh_rgb_views(shs, position, centres, active)
-    for v, cam in enumerate(cams):
-        if use_fused:
-            rgb = rgb_all[v]
-        else:
+        rgb_all = fused.sh_rgb_views(shs, position, centres, active).reshape(V * n, 3)
+    else:
+        shc = shs.permute(0, 2, 1)
+        rgbs = []
+        for cam in cams:
             d = position - cam.center.reshape(1, 3)
             d = d / d.norm(dim=1, keepdim=True)
             sh_in = shc
@@ -172,17 +174,19 @@ def render_views(position, scaling, rotation, opacity, shs, cams, bg=0.0, render
                 mask = torch.zeros_like(shc)
                 mask[..., :active] = 1.0
                 sh_in = shc * mask
-            rgb = (ops.compute_sh(sh_in, d) + 0.5).clamp(min=0.0)
-        extr = cam.extr[:3, :]
-        uv, depth, conic, radius, nt = fused.preprocess(position, scaling, rotation, cam.intr, extr,
-                                                        cam.W, cam.H, nearest=nearest)
-        f = [rgb] + ([depth] if render_depth else []) + ([extra_features] if extra_features is not None else [])
-        uvs.append(uv); depths.append(depth); conics.append(conic)
-        radii.append(radius); tiles.append(nt); feats.append(torch.cat(f, 1))
-    sizes = [(cam.W, cam.H) for cam in cams]
-    uv_all, conic_all = torch.cat(uvs), torch.cat(conics)
-    ids, rng = sort_views(uv_all, torch.cat(depths), torch.cat(radii), torch.cat(tiles), sizes, n,
-                          capacity=capacity)
-    op_all = opacity.reshape(1, n).expand(len(cams), n).reshape(-1)
-    imgs = blend_views(uv_all, conic_all, op_all, torch.cat(feats), ids, rng, bg, sizes, n)
+            rgbs.append((ops.compute_sh(sh_in, d) + 0.5).clamp(min=0.0))
+        rgb_all = torch.cat(rgbs)
+    intrs = torch.stack([cam.intr.reshape(4) for cam in cams])
+    extrs = torch.stack([cam.extr[:3, :] for cam in cams])
+    uv_all, depth_all, conic_all, radius_all, tiles_all = fused.preprocess_views(
+        position, scaling, rotation, intrs, extrs, sizes, nearest=nearest)
+    f = [rgb_all] + ([depth_all] if render_depth else [])
+    if extra_features is not None:
+        f.append(extra_features.repeat(V, 1))
+    feat_all = torch.cat(f, 1) if len(f) > 1 else f[0]
+    ids, rng = sort_views(uv_all, depth_all, radius_all, tiles_all, sizes, n, capacity=capacity)
+    op_all = opacity.reshape(1, n).expand(V, n).reshape(-1)
+    imgs = blend_views(uv_all, conic_all, op_all, feat_all, ids, rng, bg, sizes, n)
+    uvs = list(uv_all.split(n))
+    radii = list(radius_all.split(n))
     return imgs, uvs, radii

@@ -346,3 +346,36 @@ def test_camera_pose_matches_torch_composition():
     (E3 * dE).sum().backward()
     assert torch.allclose(q2.grad, q3.grad, rtol=1e-5, atol=1e-5)
     assert torch.allclose(t2.grad, t3.grad, rtol=1e-5, atol=1e-5)
+
+
+def test_preprocess_views_matches_per_view_preprocess():
+    """The batched projection of V views: each view's outputs equal the
+    single-view preprocess bit for bit; the Gaussian gradients (summed over
+    views in the kernel) and every camera's gradients equal the per-view
+    calls' autograd sums within 1e-5."""
+    g = torch.Generator().manual_seed(12)
+    scene = WL.scene_sh3(12, 60_000)
+    cams = [WL.make_camera(g, W, H, 0.72 * W, 4.5) for W, H in ((320, 240), (200, 150), (257, 190))]
+    pos, sc, q, _, _ = (t.to(DEV) for t in scene.activated())
+    leaves = lambda: [t.detach().clone().requires_grad_(True) for t in (pos, sc, q)]  # noqa: E731
+    intr = [c.intr.to(DEV).reshape(4).clone().requires_grad_(True) for c in cams]
+    extr = [c.extr[:3].to(DEV).contiguous().requires_grad_(True) for c in cams]
+    sizes = [(c.W, c.H) for c in cams]
+    ups = [torch.randn(len(cams) * pos.shape[0], k, generator=g).to(DEV) for k in (2, 1, 3)]
+    la = leaves()
+    outs = fused.preprocess_views(*la, torch.stack(intr), torch.stack(extr), sizes)
+    torch.autograd.backward(list(outs[:3]), ups)
+    ga = [t.grad.clone() for t in la] + [t.grad.clone() for t in intr + extr]
+    for t in intr + extr:
+        t.grad = None
+    lb = leaves()
+    per = [fused.preprocess(*lb, intr[v], extr[v], W, H) for v, (W, H) in enumerate(sizes)]
+    for k in range(5):
+        assert torch.equal(outs[k], torch.cat([p[k] for p in per])), k
+    n = pos.shape[0]
+    torch.autograd.backward([p[k] for p in per for k in range(3)],
+                            [u[v * n:(v + 1) * n] for v in range(len(cams)) for u in ups])
+    gb = [t.grad for t in lb] + [t.grad for t in intr + extr]
+    for a, b in zip(ga, gb):
+        assert rel(a, b) < 1e-5
+    ops.check_device_status()
