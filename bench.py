@@ -476,7 +476,8 @@ def multiview_measure(device, n=3_000_000, views=16, steps=20):
     def batched():
         zero_grads(params)
         pos, sc, q, op, shs = scene.activated()
-        imgs, _, _ = multiview.render_views(pos, sc, q, op, shs, cams, capacity=cap.get("k"))
+        imgs, _, _ = multiview.render_views(pos, sc, q, op, shs, cams, capacity=cap.get("k"),
+                                            tile_height=cap.get("th", 16))
         loss = fused.l1_l2_loss(imgs[0], targets[0], 0.0)
         for img, tgt in zip(imgs[1:], targets[1:]):
             loss = loss + fused.l1_l2_loss(img, tgt, 0.0)
@@ -505,19 +506,33 @@ def multiview_measure(device, n=3_000_000, views=16, steps=20):
     res = {"per_view_loop": timed(per_view)}
     per_view_imgs = [t.detach().clone() for t in last["per_view"]]
     k_batch = multiview_k(scene, cams)
-    cap["k"] = int(1.15 * k_batch) + (1 << 20)
-    graphed = GraphedStep(batched, warmup=1, device=device)
-    res["batched_graph"] = timed(graphed)
-    ops.check_device_status(device)
-    diff = max(float((a - b).abs().max()) for a, b in zip(per_view_imgs, last["batched"]))
+    # the tile shape is tuned by timing the whole batched step with each
+    # (the per-block splat batches are tuned by the blend autotuner inside)
+    shapes, diffs, ks = {}, {}, {}
+    for th in multiview.TILE_HEIGHTS:
+        ks[th] = multiview_k(scene, cams, th)
+        cap["k"] = int(1.15 * ks[th]) + (1 << 20)
+        cap["th"] = th
+        graphed = GraphedStep(batched, warmup=1, device=device)
+        shapes[f"16x{th}"] = timed(graphed)
+        ops.check_device_status(device)
+        diffs[f"16x{th}"] = max(float((a - b).abs().max())
+                                for a, b in zip(per_view_imgs, last["batched"]))
+        del graphed
+        torch.cuda.empty_cache()
+    best = min(shapes, key=lambda k: shapes[k]["ms_per_step"])
+    res["batched_graph"] = shapes[best]
     res["speedup"] = res["per_view_loop"]["ms_per_step"] / res["batched_graph"]["ms_per_step"]
     return {"workload": MULTIVIEW_WORKLOAD, "pixels_per_step": pix, "K_entries": k_batch,
-            "max_abs_image_diff": diff, **res}
+            "K_entries_by_tile": {f"16x{th}": k for th, k in ks.items()},
+            "max_abs_image_diff": max(diffs.values()), "image_diff_by_tile": diffs,
+            "tile_shape": best, "by_tile_shape": shapes, **res}
 
 
-def multiview_k(scene, cams):
-    """Total (element, tile) entries of a batch of views (host side)."""
-    from pointrix_gb300 import ops
+def multiview_k(scene, cams, tile_height=16):
+    """Total (element, tile) entries of a batch of views for 16 x
+    ``tile_height`` tiles."""
+    from pointrix_gb300 import multiview, ops
     total = 0
     with torch.no_grad():
         pos, sc, q, op, shs = scene.activated()
@@ -527,6 +542,9 @@ def multiview_k(scene, cams):
             vis = depth != 0
             cov = ops.compute_cov3d(sc, q, vis)
             _, radius, tiles = ops.ewa_project(pos, cov, cam.intr, E, uv, cam.W, cam.H, vis)
+            if tile_height != 16:
+                tiles = multiview.tile_counts_views(uv, radius, [(cam.W, cam.H)], pos.shape[0],
+                                                    tile_height)
             total += int(tiles[radius > 0].sum())
     return total
 

@@ -318,6 +318,52 @@ int pgb_alpha_blending_backward_views_with_batch(
 int pgb_blend_batches(int backward, int32_t* out);
 
 /* ---------------------------------------------------------------------
+ * Tiles 16 pixels wide and 32 high for a batch of views -- no counterpart
+ * in the reference (the batched multi-view path chooses its tile shape; the
+ * drop-in operators keep msplat's 16 x 16 tiles).  A 16 x 32 tile's list
+ * holds every splat whose 16 x 32 tile rectangle covers it; the blend keeps,
+ * per 8-pixel box, exactly the splats whose 16 x 16 rectangle covers the
+ * box's 16 x 16 tile, so the images and gradients are those of 16 x 16
+ * tiles, with fewer (tile, splat) entries to sort.
+ *
+ * pgb_tile_counts_views: tiles_out [V*N] = entries of each element for
+ * 16 x tile_height tiles (the tiles_touched of the sort below).
+ * pgb_sort_gaussian_finish_views_h: pgb_sort_gaussian_finish_views (k_on_device
+ * = 0) or _capacity (k_on_device != 0, k the capacity) for 16 x tile_height
+ * tiles; tile_range covers the views' 16 x tile_height tiles.
+ * pgb_alpha_blending_forward/backward_views_h: the views' blend for those
+ * lists; radius [V*N] is required for tile_height 32 (RGB, RGB + depth and
+ * RGB + depth + normal channel counts).  pgb_blend_batches_h lists the
+ * forward batches of 16 x tile_height tiles (32: 64, 128, 256).
+ * tile_height is 16 or 32.
+ * ------------------------------------------------------------------- */
+int pgb_tile_counts_views(const float* uv, const int32_t* radius, int64_t n_per_view,
+                          const int32_t* sizes, int nviews, int tile_height, int32_t* tiles_out,
+                          void* stream);
+int pgb_sort_gaussian_finish_views_h(const float* uv, const int32_t* radius,
+                                     const int32_t* tiles_touched, int64_t n_per_view,
+                                     const int32_t* sizes, int nviews, int tile_height, int64_t k,
+                                     int k_on_device, void* scratch_n, size_t bytes_n,
+                                     void* scratch_k, size_t bytes_k, int64_t* info,
+                                     int32_t* ids_out, int32_t* tile_range_out, void* stream);
+int pgb_alpha_blending_forward_views_h(const float* uv, const float* conic, const float* opacity,
+                                       const float* feature, int64_t n_per_view, int channels,
+                                       const int32_t* ids, int64_t k, const int32_t* tile_range,
+                                       float bg, const int32_t* sizes, int nviews,
+                                       int tile_height, const int32_t* radius, float* records,
+                                       float* out, float* final_T, int32_t* n_contrib,
+                                       int64_t* info, void* stream, int batch);
+int pgb_alpha_blending_backward_views_h(const float* records, int64_t n_per_view, int channels,
+                                        const int32_t* ids, int64_t k, const int32_t* tile_range,
+                                        float bg, const int32_t* sizes, int nviews,
+                                        int tile_height, const int32_t* radius,
+                                        const float* final_T, const int32_t* n_contrib,
+                                        const float* d_out, float* grad_records, float* d_uv,
+                                        float* d_conic, float* d_opacity, float* d_feature,
+                                        int64_t* info, void* stream, int batch);
+int pgb_blend_batches_h(int backward, int tile_height, int32_t* out);
+
+/* ---------------------------------------------------------------------
  * Bands of tile rows -- no counterpart in the reference.  They serve the
  * recompute-in-backward mode of large views (ops.rasterize(recompute=True)):
  * one image is sorted and blended one band of tile rows [row0, row1) at a

@@ -59,6 +59,14 @@ SIGNATURES = {
     "pgb_blend_batches": [i32, vp],
     "pgb_blend_pair_census": [vp, i32, i64, vp, i64, vp, i32, i32, vp, vp, vp],
     "pgb_band_tiles": [vp, vp, i64, i32, i32, i32, i32, vp, vp],
+    "pgb_tile_counts_views": [vp, vp, i64, vp, i32, i32, vp, vp],
+    "pgb_sort_gaussian_finish_views_h": [vp, vp, vp, i64, vp, i32, i32, i64, i32, vp, szt, vp, szt,
+                                         vp, vp, vp, vp],
+    "pgb_alpha_blending_forward_views_h": [vp, vp, vp, vp, i64, i32, vp, i64, vp, f32, vp, i32, i32,
+                                           vp, vp, vp, vp, vp, vp, vp, i32],
+    "pgb_alpha_blending_backward_views_h": [vp, i64, i32, vp, i64, vp, f32, vp, i32, i32, vp, vp,
+                                            vp, vp, vp, vp, vp, vp, vp, vp, vp, i32],
+    "pgb_blend_batches_h": [i32, i32, vp],
     "pgb_band_counts": [vp, vp, i64, i32, i32, vp, i32, vp, vp],
     "pgb_sort_gaussian_rebegin": [vp, vp, i64, vp, szt, vp, vp],
     "pgb_sort_gaussian_finish_band": [vp, vp, vp, i64, i32, i32, i32, i32, i64, vp, szt, vp, szt,

@@ -184,6 +184,23 @@ __device__ inline void stage_batch(const float* __restrict__ records,
   cp_async_commit();
 }
 
+// The radii of one batch's splats (16 x 32 tiles only), plain loads into
+// s_rad[slot]; read after the barrier that publishes the batch.
+template <int NT, int B>
+__device__ inline void stage_radius(const int32_t* __restrict__ ids,
+                                    const int32_t* __restrict__ radius, int64_t first,
+                                    int64_t last, int64_t n, int* s_rad) {
+  for (int slot = threadIdx.x; slot < B; slot += NT) {
+    const int64_t e = first + slot;
+    int r = 0;
+    if (e < last) {
+      const int32_t g = ids[e];
+      if (g >= 0 && (int64_t)g < n) r = radius[g];
+    }
+    s_rad[slot] = r;
+  }
+}
+
 // ------------------------------------------------------------------ pack
 // Record of one splat: u, v, K a, K b, K c (the conic scaled by
 // K = -log2(e) / 2), o, tau, thr = -log2(255 o), f_0..f_{C-1}, zero
@@ -308,16 +325,36 @@ __device__ __forceinline__ bool splat_may_touch_box(const float* rec, float x0, 
 // Builds this warp's list of batch slots (in increasing order) whose splat
 // may touch the warp's pixel box; slots >= cnt are ignored.  Returns the
 // list length.
-template <int BW, int BH, int B>
+// Tiles taller than 16 pixels (16 x 32 for a batch of views) hold the
+// splats of both 16 x 16 tiles they cover.  msplat's lists are per 16 x 16
+// tile: a splat belongs to a 16 x 16 tile's list when its 16 x 16 tile
+// rectangle (tile_rect of its uv and radius) contains the tile.  F16 keeps
+// exactly those splats for the warp's box (which lies in one 16 x 16 tile),
+// so every pixel composites the same splats, in the same depth order, as
+// with 16 x 16 tiles.
+struct List16 {
+  const int* rad;  // staged radii of the batch's splats
+  int tx, ty;      // the box's 16 x 16 tile
+  int gx, gy;      // the view's 16 x 16 tile grid
+};
+
+__device__ __forceinline__ bool in_list16(const float* rec, int r, const List16& f) {
+  int x0, x1, y0, y1;
+  tile_rect(rec[0], rec[1], (float)r, f.gx, f.gy, x0, x1, y0, y1);
+  return r > 0 && f.tx >= x0 && f.tx < x1 && f.ty >= y0 && f.ty < y1;
+}
+
+template <int BW, int BH, int B, bool F16 = false>
 __device__ __forceinline__ int warp_cull(const float* stage, int RF, int cnt, float x0, float y0,
-                                         uint8_t* list) {
+                                         uint8_t* list, const List16& f16 = List16{}) {
   const int lane = threadIdx.x & 31;
   const uint32_t lt = (1u << lane) - 1u;
   int n = 0;
 #pragma unroll
   for (int k = 0; k < B / 32; ++k) {
     const int j = k * 32 + lane;
-    const bool keep = j < cnt && splat_may_touch_box<BW, BH>(stage + j * RF, x0, y0);
+    bool keep = j < cnt && splat_may_touch_box<BW, BH>(stage + j * RF, x0, y0);
+    if constexpr (F16) keep = keep && in_list16(stage + j * RF, f16.rad[j], f16);
     const uint32_t m = __ballot_sync(0xffffffffu, keep);
     if (keep) list[n + __popc(m & lt)] = (uint8_t)j;
     n += __popc(m);
@@ -327,24 +364,27 @@ __device__ __forceinline__ int warp_cull(const float* stage, int RF, int cnt, fl
 }
 
 // --------------------------------------------------------------- forward
-// 128 threads per tile, two pixels per thread: warp w owns the 8x8 box at
+// 128 threads per 16 x 16 tile (256 per 16 x 32 tile), two pixels per
+// thread: warp w owns the 8x8 box at
 // (8 (w % 2), 8 (w / 2)); lane l owns pixels (l % 8, l / 8) and
 // (l % 8, l / 8 + 4), the layout of the backward.  Every culling test,
 // list entry and record read serves 64 pixels.  Batches of 128 records,
 // one TMA bulk copy per thread per batch.
-constexpr int kFwdThreads = 128;
 constexpr int kFwdPix = 2;
 constexpr int kFwdBatch = 128;  // default records per batch (64 and 128 are compiled)
 
-template <int NC, int RF, int B>
-__global__ void __launch_bounds__(kFwdThreads) blend_fwd_kernel(
+template <int NC, int RF, int B, int TH = 16>
+__global__ void __launch_bounds__(64 * (TH / 8)) blend_fwd_kernel(
     const float* __restrict__ records, const int32_t* __restrict__ ids,
     const int2* __restrict__ ranges, int64_t n, float bg, const ViewTable vt, int C,
     float* __restrict__ out, float* __restrict__ final_T, int32_t* __restrict__ n_contrib,
-    int64_t* __restrict__ info) {
+    int64_t* __restrict__ info, const int32_t* __restrict__ radius) {
+  constexpr int NT = 64 * (TH / 8);  // 8 x 8 warp boxes over a 16 x TH tile
+  constexpr bool F16 = TH != kTile;
   extern __shared__ __align__(128) float smem[];
   __shared__ __align__(8) uint64_t bars[2];
-  __shared__ uint8_t s_list[kFwdThreads / 32][B];
+  __shared__ uint8_t s_list[NT / 32][B];
+  __shared__ int s_rad[F16 ? 2 : 1][F16 ? B : 1];
 
   const int tile = blockIdx.x;  // global tile (of its view, for a batch)
   int W, H, gx, ltile;
@@ -352,12 +392,19 @@ __global__ void __launch_bounds__(kFwdThreads) blend_fwd_kernel(
   tile_view(vt, tile, W, H, gx, ltile, pbase);
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int bx0 = (ltile % gx) * kTile + 8 * (w & 1);
-  const int by0 = (ltile / gx) * kTile + 8 * (w >> 1);
+  const int by0 = (ltile / gx) * TH + 8 * (w >> 1);
   uint8_t* my_list = s_list[w];
+  List16 f16{};
+  if constexpr (F16) {
+    f16.tx = bx0 / kTile;
+    f16.ty = by0 / kTile;
+    f16.gx = grid_x(W);
+    f16.gy = grid_y(H);
+  }
 
   if (threadIdx.x == 0) {
-    mbar_init(&bars[0], kFwdThreads / 32);
-    mbar_init(&bars[1], kFwdThreads / 32);
+    mbar_init(&bars[0], NT / 32);
+    mbar_init(&bars[1], NT / 32);
     fence_mbar_init();
   }
   __syncthreads();
@@ -384,15 +431,18 @@ __global__ void __launch_bounds__(kFwdThreads) blend_fwd_kernel(
   }
   bool timed_out = false;
 
-  if (nb > 0)
-    issue_batch<RF, kFwdThreads, B>(records, ids, start, end, n, smem, &bars[0], info);
+  if (nb > 0) {
+    issue_batch<RF, NT, B>(records, ids, start, end, n, smem, &bars[0], info);
+    if constexpr (F16) stage_radius<NT, B>(ids, radius, start, end, n, s_rad[0]);
+  }
   for (int b = 0; b < nb; ++b) {
     const int buf = b & 1;
     const int64_t first = start + (int64_t)b * B;
-    if (b + 1 < nb)
-      issue_batch<RF, kFwdThreads, B>(records, ids, first + B, end, n,
-                                              smem + (buf ^ 1) * B * RF, &bars[buf ^ 1],
-                                              info);
+    if (b + 1 < nb) {
+      issue_batch<RF, NT, B>(records, ids, first + B, end, n, smem + (buf ^ 1) * B * RF,
+                             &bars[buf ^ 1], info);
+      if constexpr (F16) stage_radius<NT, B>(ids, radius, first + B, end, n, s_rad[buf ^ 1]);
+    }
     // every thread observes the phase (that makes the TMA writes visible to
     // it); the outcome is made block-uniform before any warp collective
     timed_out = __syncthreads_or(!mbar_wait_bounded(&bars[buf], (b >> 1) & 1));
@@ -403,7 +453,8 @@ __global__ void __launch_bounds__(kFwdThreads) blend_fwd_kernel(
 #pragma unroll
     for (int q = 0; q < kFwdPix; ++q) all_done &= done[q];
     if (!timed_out && !__all_sync(0xffffffffu, all_done)) {
-      const int nl = warp_cull<8, 8, B>(st, RF, cnt, (float)bx0, (float)by0, my_list);
+      if constexpr (F16) f16.rad = s_rad[buf];
+      const int nl = warp_cull<8, 8, B, F16>(st, RF, cnt, (float)bx0, (float)by0, my_list, f16);
       const int base = (int)(first - start) + 1;
       for (int t = 0; t < nl; ++t) {
         const int j = my_list[t];
@@ -441,7 +492,7 @@ __global__ void __launch_bounds__(kFwdThreads) blend_fwd_kernel(
 #pragma unroll
     for (int q = 0; q < kFwdPix; ++q) mine_done &= done[q];
     const int ndone = __syncthreads_count(mine_done || timed_out);
-    if (ndone == kFwdThreads || timed_out) {
+    if (ndone == NT || timed_out) {
       if (b + 1 < nb && !mbar_wait_bounded(&bars[buf ^ 1], ((b + 1) >> 1) & 1))
         set_info(info, PGB_ERR_TIMEOUT);
       break;
@@ -553,16 +604,17 @@ __device__ __forceinline__ bool bwd_pixel(BwdPixel<NC>& P, int j, const float* r
   return true;
 }
 
-template <int NC, int RF, int GR, int B, int PX>
-__global__ void __launch_bounds__(256 / PX) blend_bwd_kernel(
+template <int NC, int RF, int GR, int B, int PX, int TH = 16>
+__global__ void __launch_bounds__(256 / PX * (TH / 16)) blend_bwd_kernel(
     const float* __restrict__ records, const int32_t* __restrict__ ids,
     const int2* __restrict__ ranges, int64_t n, float bg, const ViewTable vt, int C,
     const float* __restrict__ final_T, const int32_t* __restrict__ n_contrib,
     const float* __restrict__ d_out, float* __restrict__ grad_records,
-    int64_t* __restrict__ info) {
+    int64_t* __restrict__ info, const int32_t* __restrict__ radius) {
   static_assert(GR == 16 || GR == 32, "gradient records are 16 or 32 floats");
   static_assert(PX == 2 || PX == 4, "two or four pixels per thread");
-  constexpr int NT = 256 / PX;
+  constexpr int NT = 256 / PX * (TH / 16);
+  constexpr bool F16 = TH != kTile;
   constexpr int BW = 8;         // warp box width
   constexpr int RS = 32 / BW;   // box rows per pixel step
   constexpr int BH = RS * PX;   // warp box height
@@ -570,6 +622,7 @@ __global__ void __launch_bounds__(256 / PX) blend_bwd_kernel(
   __shared__ int s_max_nc;
   __shared__ uint8_t s_touched[B];
   __shared__ uint8_t s_list[NT / 32][B];
+  __shared__ int s_rad[F16 ? 2 : 1][F16 ? B : 1];
   float* gacc = smem + 2 * B * RF;  // [B][GR]
 
   const int tile = blockIdx.x;  // global tile (of its view, for a batch)
@@ -578,8 +631,15 @@ __global__ void __launch_bounds__(256 / PX) blend_bwd_kernel(
   tile_view(vt, tile, W, H, gx, ltile, pbase);
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int bx0 = (ltile % gx) * kTile + BW * (w & 1);
-  const int by0 = (ltile / gx) * kTile + BH * (w >> 1);
+  const int by0 = (ltile / gx) * TH + BH * (w >> 1);
   uint8_t* my_list = s_list[w];
+  List16 f16{};
+  if constexpr (F16) {
+    f16.tx = bx0 / kTile;
+    f16.ty = by0 / kTile;
+    f16.gx = grid_x(W);
+    f16.gy = grid_y(H);
+  }
 
   if (threadIdx.x == 0) s_max_nc = 0;
   for (int i = threadIdx.x; i < B * GR; i += NT) gacc[i] = 0.f;
@@ -630,14 +690,20 @@ __global__ void __launch_bounds__(256 / PX) blend_bwd_kernel(
   auto lo_of = [&](int b) { return max(0, max_nc - (b + 1) * B); };
   auto hi_of = [&](int b) { return max_nc - b * B; };
 
-  if (nb > 0)
+  if (nb > 0) {
     stage_batch<RF, NT, B>(records, ids, start + lo_of(0), start + hi_of(0), n, smem, info);
+    if constexpr (F16)
+      stage_radius<NT, B>(ids, radius, start + lo_of(0), start + hi_of(0), n, s_rad[0]);
+  }
   for (int b = 0; b < nb; ++b) {
     const int buf = b & 1;
     const int lo = lo_of(b), hi = hi_of(b);
     if (b + 1 < nb) {
       stage_batch<RF, NT, B>(records, ids, start + lo_of(b + 1), start + hi_of(b + 1), n,
                              smem + (buf ^ 1) * B * RF, info);
+      if constexpr (F16)
+        stage_radius<NT, B>(ids, radius, start + lo_of(b + 1), start + hi_of(b + 1), n,
+                            s_rad[buf ^ 1]);
       cp_async_wait<1>();  // this thread's copies of batch b have landed
     } else {
       cp_async_wait<0>();
@@ -645,8 +711,9 @@ __global__ void __launch_bounds__(256 / PX) blend_bwd_kernel(
     __syncthreads();  // ... and everyone's
     const float* st = smem + buf * B * RF;
     {
-      const int nl = warp_cull<BW, BH, B>(st, RF, min(hi, warp_nc) - lo, (float)bx0,
-                                          (float)by0, my_list);
+      if constexpr (F16) f16.rad = s_rad[buf];
+      const int nl = warp_cull<BW, BH, B, F16>(st, RF, min(hi, warp_nc) - lo, (float)bx0,
+                                               (float)by0, my_list, f16);
       for (int t = nl - 1; t >= 0; --t) {
         const int slot = my_list[t];
         const int j = lo + slot;
@@ -995,31 +1062,56 @@ __global__ void __launch_bounds__(256) census_kernel(const float* __restrict__ r
 }
 
 // ------------------------------------------------------------- dispatch
-template <int NC, int B>
+// Tiles 16 x 32 (a batch of views with vt.th == 32) are compiled for the
+// channel buckets of RGB, RGB + depth and RGB + depth + normal.
+template <int NC>
+constexpr bool kTall = NC == 3 || NC == 4 || NC == 7;
+
+inline bool tall_tiles(const ViewTable& vt) { return vt.nviews > 0 && vt.th == 32; }
+
+template <int NC, int B, int TH = 16>
 static int launch_fwd_b(const float* records, const int32_t* ids, const int2* ranges, int64_t n,
                         float bg, const ViewTable& vt, int tiles, int C, float* out, float* fT,
-                        int32_t* ncon, int64_t* info, cudaStream_t s) {
+                        int32_t* ncon, int64_t* info, cudaStream_t s, const int32_t* radius) {
   constexpr int RF = rec_floats(NC);
   const size_t smem = 2 * B * RF * sizeof(float);
-  auto kern = blend_fwd_kernel<NC, RF, B>;
+  auto kern = blend_fwd_kernel<NC, RF, B, TH>;
   if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
       cudaSuccess)
     return PGB_ERR_CUDA;
-  kern<<<tiles, kFwdThreads, smem, s>>>(records, ids, ranges, n, bg, vt, C, out, fT, ncon, info);
+  kern<<<tiles, 64 * (TH / 8), smem, s>>>(records, ids, ranges, n, bg, vt, C, out, fT, ncon, info,
+                                          radius);
   return launch_status();
 }
 
-// batch: records per batch, 64 or 128 (0: the default).  One TMA bulk copy
-// per thread per phase at most in both.
+// batch: records per batch, 64 or 128 (0: the default); 16 x 32 tiles also
+// 256.  Never more records than threads: one TMA bulk copy per thread per
+// phase at most.
 template <int NC>
 static int launch_fwd_nc(const float* records, const int32_t* ids, const int2* ranges, int64_t n,
                          float bg, const ViewTable& vt, int tiles, int C, float* out, float* fT,
-                         int32_t* ncon, int64_t* info, cudaStream_t s, int batch) {
+                         int32_t* ncon, int64_t* info, cudaStream_t s, int batch,
+                         const int32_t* radius) {
+#define PGB_FWD(B, TH) \
+  launch_fwd_b<NC, B, TH>(records, ids, ranges, n, bg, vt, tiles, C, out, fT, ncon, info, s, radius)
+  if (tall_tiles(vt)) {
+    if constexpr (kTall<NC>) {
+      if (!radius) return PGB_ERR_INVALID;
+      switch (batch == 0 ? kFwdBatch : batch) {
+        case 64: return PGB_FWD(64, 32);
+        case 128: return PGB_FWD(128, 32);
+        case 256: return PGB_FWD(256, 32);
+        default: return PGB_ERR_INVALID;
+      }
+    }
+    return PGB_ERR_INVALID;
+  }
   switch (batch == 0 ? kFwdBatch : batch) {
-    case 64: return launch_fwd_b<NC, 64>(records, ids, ranges, n, bg, vt, tiles, C, out, fT, ncon, info, s);
-    case 128: return launch_fwd_b<NC, 128>(records, ids, ranges, n, bg, vt, tiles, C, out, fT, ncon, info, s);
+    case 64: return PGB_FWD(64, 16);
+    case 128: return PGB_FWD(128, 16);
     default: return PGB_ERR_INVALID;
   }
+#undef PGB_FWD
 }
 
 template <int NC, int B, int PX, int MINB, bool XRED>
@@ -1041,32 +1133,54 @@ static int launch_bwd2_b(const float* records, const int32_t* ids, const int2* r
   return launch_status();
 }
 
-template <int NC, int B, int PX>
+template <int NC, int B, int PX, int TH = 16>
 static int launch_bwd_b(const float* records, const int32_t* ids, const int2* ranges, int64_t n,
                         float bg, const ViewTable& vt, int tiles, int C, const float* fT,
                         const int32_t* ncon, const float* dout, float* grec, int64_t* info,
-                        cudaStream_t s) {
+                        cudaStream_t s, const int32_t* radius) {
   constexpr int RF = rec_floats(NC);
   constexpr int GR = grad_floats(NC);
   const size_t smem = (2 * RF + GR) * B * sizeof(float);
-  auto kern = blend_bwd_kernel<NC, RF, GR, B, PX>;
+  auto kern = blend_bwd_kernel<NC, RF, GR, B, PX, TH>;
   if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
       cudaSuccess)
     return PGB_ERR_CUDA;
-  kern<<<tiles, 256 / PX, smem, s>>>(records, ids, ranges, n, bg, vt, C, fT, ncon, dout, grec,
-                                     info);
+  kern<<<tiles, 256 / PX * (TH / 16), smem, s>>>(records, ids, ranges, n, bg, vt, C, fT, ncon,
+                                                 dout, grec, info, radius);
   return launch_status();
 }
 
 // batch: a backward variant code -- 64, 128 or 256 splats per batch with two
-// pixels per thread, kBwdPx4 + 32 / 64 / 128 with four (0: the default).
+// pixels per thread, kBwdPx4 + 32 / 64 / 128 with four, kBwdV2 + ... the
+// second form (0: the default).  16 x 32 tiles take the first form for
+// every code.
 template <int NC>
 static int launch_bwd_nc(const float* records, const int32_t* ids, const int2* ranges, int64_t n,
                          float bg, const ViewTable& vt, int tiles, int C, const float* fT,
                          const int32_t* ncon, const float* dout, float* grec, int64_t* info,
-                         cudaStream_t s, int batch) {
-#define PGB_BWD(B, PX) \
-  launch_bwd_b<NC, B, PX>(records, ids, ranges, n, bg, vt, tiles, C, fT, ncon, dout, grec, info, s)
+                         cudaStream_t s, int batch, const int32_t* radius) {
+#define PGB_BWD_T(B, PX, TH)                                                                      \
+  launch_bwd_b<NC, B, PX, TH>(records, ids, ranges, n, bg, vt, tiles, C, fT, ncon, dout, grec, info, \
+                              s, radius)
+#define PGB_BWD(B, PX) PGB_BWD_T(B, PX, 16)
+  if (tall_tiles(vt)) {
+    if constexpr (kTall<NC>) {
+      if (!radius) return PGB_ERR_INVALID;
+      switch (batch == 0 ? kBwdBatch : batch) {
+        case 64: return PGB_BWD_T(64, 2, 32);
+        case 128: return PGB_BWD_T(128, 2, 32);
+        case 256: return PGB_BWD_T(256, 2, 32);
+        case kBwdPx4 + 32:
+        case kBwdV2 + 512 + 32:
+        case kBwdV2 + 1024 + 32: return PGB_BWD_T(32, 4, 32);
+        case kBwdPx4 + 64:
+        case kBwdV2 + 64: return PGB_BWD_T(64, 4, 32);
+        case kBwdPx4 + 128: return PGB_BWD_T(128, 4, 32);
+        default: return PGB_ERR_INVALID;
+      }
+    }
+    return PGB_ERR_INVALID;
+  }
   switch (batch == 0 ? kBwdBatch : batch) {
     case 64: return PGB_BWD(64, 2);
     case 128: return PGB_BWD(128, 2);
@@ -1098,6 +1212,7 @@ static int launch_bwd_nc(const float* records, const int32_t* ids, const int2* r
     }
   }
 #undef PGB_BWD
+#undef PGB_BWD_T
   return PGB_ERR_INVALID;
 }
 
@@ -1153,7 +1268,7 @@ static int blend_forward_impl(const float* uv, const float* conic, const float* 
                               int64_t k, const int32_t* tile_range, float bg, const ViewTable& vt,
                               int tiles, float* records, float* out, float* final_T,
                               int32_t* n_contrib, int64_t* info, void* stream, int batch,
-                              bool pack = true) {
+                              bool pack = true, const int32_t* radius = nullptr) {
   const int nc = nc_bucket(channels);
   if (n < 0 || k < 0 || tiles <= 0 || channels < 1 || nc < 0) return PGB_ERR_INVALID;
   if (!tile_range || !out || !final_T || !n_contrib || (k > 0 && !ids)) return PGB_ERR_INVALID;
@@ -1173,7 +1288,7 @@ static int blend_forward_impl(const float* uv, const float* conic, const float* 
                                                                            fc, n, channels,      \
                                                                            records);            \
     return launch_fwd_nc<N>(records, ids, rg, n, bg, vt, tiles, channels, out, final_T,          \
-                            n_contrib, info, s, batch);
+                            n_contrib, info, s, batch, radius);
     PGB_FOR_NC(PGB_CASE)
 #undef PGB_CASE
     default:
@@ -1187,7 +1302,7 @@ static int blend_backward_impl(const float* records, int64_t n, int channels, co
                                const float* d_out, float* grad_records, float* d_uv,
                                float* d_conic, float* d_opacity, const FeatGradCols& gc,
                                int64_t* info, void* stream, int batch, bool first = true,
-                               bool last = true) {
+                               bool last = true, const int32_t* radius = nullptr) {
   const int nc = nc_bucket(channels);
   if (n < 0 || k < 0 || tiles <= 0 || channels < 1 || nc < 0) return PGB_ERR_INVALID;
   if (!tile_range || !final_T || !n_contrib || !d_out || (k > 0 && !ids)) return PGB_ERR_INVALID;
@@ -1208,7 +1323,7 @@ static int blend_backward_impl(const float* records, int64_t n, int channels, co
 #define PGB_CASE(N)                                                                          \
   case N:                                                                                    \
     st = launch_bwd_nc<N>(records, ids, rg, n, bg, vt, tiles, channels, final_T, n_contrib,  \
-                          d_out, grad_records, info, s, batch);                              \
+                          d_out, grad_records, info, s, batch, radius);                      \
     break;
     PGB_FOR_NC(PGB_CASE)
 #undef PGB_CASE
@@ -1400,6 +1515,56 @@ int pgb_alpha_blending_backward_band(const float* records, int64_t n, int channe
                              grad_records, d_uv, d_conic, d_opacity,
                              grad_cols_of(d_feature, channels), info, stream, batch, first != 0,
                              last != 0);
+}
+
+// A batch of views with tiles 16 pixels wide and tile_height (16 or 32)
+// high (no msplat counterpart): ids and tile_range from
+// pgb_sort_gaussian_finish_views_h with the same tile height; radius [V*N]
+// (the elements' radii, as the sort took them) lets 16 x 32 tiles keep, per
+// pixel, exactly the splats of msplat's 16 x 16 lists.
+int pgb_alpha_blending_forward_views_h(const float* uv, const float* conic, const float* opacity,
+                                       const float* feature, int64_t n_per_view, int channels,
+                                       const int32_t* ids, int64_t k, const int32_t* tile_range,
+                                       float bg, const int32_t* sizes, int nviews,
+                                       int tile_height, const int32_t* radius, float* records,
+                                       float* out, float* final_T, int32_t* n_contrib,
+                                       int64_t* info, void* stream, int batch) {
+  ViewTable vt;
+  uint32_t T = 0;
+  int64_t pixels = 0;
+  if (!make_views(sizes, nviews, n_per_view, vt, T, pixels, tile_height)) return PGB_ERR_INVALID;
+  return blend_forward_impl(uv, conic, opacity, cols_of(feature, channels), n_per_view * nviews,
+                            channels, ids, k, tile_range, bg, vt, (int)T, records, out, final_T,
+                            n_contrib, info, stream, batch, true, radius);
+}
+
+int pgb_alpha_blending_backward_views_h(const float* records, int64_t n_per_view, int channels,
+                                        const int32_t* ids, int64_t k, const int32_t* tile_range,
+                                        float bg, const int32_t* sizes, int nviews,
+                                        int tile_height, const int32_t* radius,
+                                        const float* final_T, const int32_t* n_contrib,
+                                        const float* d_out, float* grad_records, float* d_uv,
+                                        float* d_conic, float* d_opacity, float* d_feature,
+                                        int64_t* info, void* stream, int batch) {
+  ViewTable vt;
+  uint32_t T = 0;
+  int64_t pixels = 0;
+  if (!make_views(sizes, nviews, n_per_view, vt, T, pixels, tile_height)) return PGB_ERR_INVALID;
+  return blend_backward_impl(records, n_per_view * nviews, channels, ids, k, tile_range, bg, vt,
+                             (int)T, final_T, n_contrib, d_out, grad_records, d_uv, d_conic,
+                             d_opacity, grad_cols_of(d_feature, channels), info, stream, batch,
+                             true, true, radius);
+}
+
+// Forward batch sizes compiled for 16 x tile_height tiles (see
+// pgb_blend_batches for 16 x 16).
+int pgb_blend_batches_h(int backward, int tile_height, int32_t* out) {
+  if (tile_height != 32) return pgb_blend_batches(backward, out);
+  static const int32_t f[] = {64, 128, 256};
+  if (backward) return pgb_blend_batches(backward, out);
+  if (out)
+    for (int i = 0; i < 3; ++i) out[i] = f[i];
+  return 3;
 }
 
 // Pair census of a blend (no msplat counterpart): counts[0] += list entries

@@ -51,6 +51,19 @@ __device__ inline void tile_rect(float u, float v, float r, int gx, int gy, int&
   ymax = (int)fminf((float)gy, fmaxf(0.0f, (v + r + c) / t));
 }
 
+// The same for tiles 16 pixels wide and th (16 or 32) high; th = 16 is
+// tile_rect operation for operation.
+__device__ inline void tile_rect_h(float u, float v, float r, int th, int gx, int gy, int& xmin,
+                                   int& xmax, int& ymin, int& ymax) {
+  const float t = 16.0f, c = 15.0f, ty = (float)th, cy = (float)(th - 1);
+  xmin = (int)fminf((float)gx, fmaxf(0.0f, (u - r) / t));
+  xmax = (int)fminf((float)gx, fmaxf(0.0f, (u + r + c) / t));
+  ymin = (int)fminf((float)gy, fmaxf(0.0f, (v - r) / ty));
+  ymax = (int)fminf((float)gy, fmaxf(0.0f, (v + r + cy) / ty));
+}
+
+__host__ __device__ inline int grid_y_h(int h, int th) { return (h + th - 1) / th; }
+
 // Where the tiles and pixels of a launch live, passed by value in kernel
 // parameters: one image (nviews == 0, size W x H) or a batch of up to
 // kMaxViews views.  In a batch the views own consecutive ranges of one global
@@ -69,6 +82,7 @@ struct ViewTable {
   int nviews;
   int W, H;
   int band0, band1;
+  int th;  // a batch of views: tile height in pixels (16, or 32 for 16x32 tiles)
   int64_t n_per_view;
   int32_t w[kMaxViews], h[kMaxViews], tile_base[kMaxViews];
   int64_t pixel_base[kMaxViews];
@@ -97,10 +111,12 @@ inline bool band_view(int W, int H, int row0, int row1, ViewTable& vt) {
 // A batch from host (width, height) pairs; fills the bases and returns the
 // total tile and pixel counts, or false when a size is invalid.
 inline bool make_views(const int32_t* sizes, int nviews, int64_t n_per_view, ViewTable& vt,
-                       uint32_t& tiles, int64_t& pixels) {
+                       uint32_t& tiles, int64_t& pixels, int th = 16) {
   if (!sizes || nviews < 1 || nviews > kMaxViews || n_per_view < 0) return false;
+  if (th != 16 && th != 32) return false;
   vt = ViewTable{};
   vt.nviews = nviews;
+  vt.th = th;
   vt.n_per_view = n_per_view;
   uint64_t t = 0;
   int64_t p = 0;
@@ -111,7 +127,7 @@ inline bool make_views(const int32_t* sizes, int nviews, int64_t n_per_view, Vie
     vt.h[v] = H;
     vt.tile_base[v] = (int32_t)t;
     vt.pixel_base[v] = p;
-    t += (uint64_t)grid_x(W) * grid_y(H);
+    t += (uint64_t)grid_x(W) * grid_y_h(H, th);
     p += (int64_t)W * H;
     if (t > (1u << 24)) return false;
   }
@@ -132,7 +148,7 @@ __device__ inline void element_view(const ViewTable& vt, uint32_t g, int& gx, in
   int v = (int)((int64_t)g / vt.n_per_view);
   v = v < vt.nviews - 1 ? v : vt.nviews - 1;
   gx = grid_x(vt.w[v]);
-  gy = grid_y(vt.h[v]);
+  gy = grid_y_h(vt.h[v], vt.th);
   tile_base = (uint32_t)vt.tile_base[v];
 }
 

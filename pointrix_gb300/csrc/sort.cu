@@ -790,7 +790,10 @@ __global__ void __launch_bounds__(kStreamThreads) rect_kernel(
         int gx, gy, x0, x1, y0, y1;
         uint32_t tile_base;
         element_view(vt, (uint32_t)g, gx, gy, tile_base);
-        tile_rect(p.x, p.y, (float)r, gx, gy, x0, x1, y0, y1);
+        if (vt.nviews == 0)
+          tile_rect(p.x, p.y, (float)r, gx, gy, x0, x1, y0, y1);
+        else  // a batch of views: 16 x th tiles
+          tile_rect_h(p.x, p.y, (float)r, vt.th, gx, gy, x0, x1, y0, y1);
         if (vt.nviews == 0) {  // one image: the rows of its band, band-local
           y0 = max(y0, vt.band0);
           y1 = max(min(y1, vt.band1), y0);
@@ -1154,6 +1157,28 @@ __global__ void __launch_bounds__(kStreamThreads) band_counts_kernel(
     if (s_cnt[i]) atomicAdd(&counts[i], s_cnt[i]);
 }
 
+// Entries of each element of a batch of views for 16 x th tiles (the
+// tiles_touched the views' sort then takes): its view's tile rectangle,
+// 0 for radius <= 0.
+__global__ void __launch_bounds__(kStreamThreads) view_tiles_kernel(
+    const float* __restrict__ uv, const int32_t* __restrict__ radius, int64_t n, ViewTable vt,
+    int32_t* __restrict__ tiles_out) {
+  for (int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; g < n;
+       g += (int64_t)gridDim.x * blockDim.x) {
+    const int r = radius[g];
+    int cnt = 0;
+    if (r > 0) {
+      int gx, gy, x0, x1, y0, y1;
+      uint32_t base;
+      element_view(vt, (uint32_t)g, gx, gy, base);
+      const float2 p = reinterpret_cast<const float2*>(uv)[g];
+      tile_rect_h(p.x, p.y, (float)r, vt.th, gx, gy, x0, x1, y0, y1);
+      cnt = (x1 - x0) * (y1 - y0);
+    }
+    tiles_out[g] = cnt;
+  }
+}
+
 }  // namespace pgb
 
 using namespace pgb;
@@ -1274,7 +1299,8 @@ static int sort_finish_impl(const float* uv, const int32_t* radius, const int32_
   if (vt.nviews > 0) {
     T_local = 1;
     for (int v = 0; v < vt.nviews; ++v)
-      T_local = std::max<uint32_t>(T_local, (uint32_t)grid_x(vt.w[v]) * (uint32_t)grid_y(vt.h[v]));
+      T_local = std::max<uint32_t>(T_local,
+                                   (uint32_t)grid_x(vt.w[v]) * (uint32_t)grid_y_h(vt.h[v], vt.th));
   }
   const TilePlan plan = tile_plan(T_local);
   const ScratchK LK = layout_k(k, plan.passes);
@@ -1455,6 +1481,36 @@ int pgb_band_counts(const float* uv, const int32_t* radius, int64_t n, int width
   band_counts_kernel<<<stream_grid(n), kStreamThreads, 0, s>>>(
       uv, radius, n, grid_x(width), grid_y(height), bands, nbands, counts);
   return launch_status();
+}
+
+int pgb_tile_counts_views(const float* uv, const int32_t* radius, int64_t n_per_view,
+                          const int32_t* sizes, int nviews, int tile_height, int32_t* tiles_out,
+                          void* stream) {
+  ViewTable vt;
+  uint32_t T = 0;
+  int64_t pixels = 0;
+  if (!make_views(sizes, nviews, n_per_view, vt, T, pixels, tile_height)) return PGB_ERR_INVALID;
+  const int64_t n = n_per_view * nviews;
+  if (n > 0 && (!uv || !radius || !tiles_out || misaligned(uv, 8))) return PGB_ERR_INVALID;
+  if (n == 0) return PGB_OK;
+  view_tiles_kernel<<<stream_grid(n), kStreamThreads, 0, as_stream(stream)>>>(uv, radius, n, vt,
+                                                                              tiles_out);
+  return launch_status();
+}
+
+int pgb_sort_gaussian_finish_views_h(const float* uv, const int32_t* radius,
+                                     const int32_t* tiles_touched, int64_t n_per_view,
+                                     const int32_t* sizes, int nviews, int tile_height, int64_t k,
+                                     int k_on_device, void* scratch_n, size_t bytes_n,
+                                     void* scratch_k, size_t bytes_k, int64_t* info,
+                                     int32_t* ids_out, int32_t* tile_range_out, void* stream) {
+  ViewTable vt;
+  uint32_t T = 0;
+  int64_t pixels = 0;
+  if (!make_views(sizes, nviews, n_per_view, vt, T, pixels, tile_height)) return PGB_ERR_INVALID;
+  return sort_finish_impl(uv, radius, tiles_touched, n_per_view * nviews, vt, T, k,
+                          k_on_device != 0, scratch_n, bytes_n, scratch_k, bytes_k, info, ids_out,
+                          tile_range_out, stream);
 }
 
 }  // extern "C"

@@ -40,11 +40,14 @@ def _per_view(leaves, cams):
     return imgs
 
 
-def test_batched_views_match_per_view():
+@pytest.mark.parametrize("tile_height", [16, 32])
+def test_batched_views_match_per_view(tile_height):
+    """Also with 16 x 32 tiles: the per-box filter keeps exactly the splats
+    of the 16 x 16 lists, so the images are still bit-identical."""
     cams = _cams()
     ref_leaves, bat_leaves = _leaves(), _leaves()
     ref = _per_view(ref_leaves, cams)
-    bat, _, _ = multiview.render_views(*bat_leaves, cams, bg=0.1)
+    bat, _, _ = multiview.render_views(*bat_leaves, cams, bg=0.1, tile_height=tile_height)
     g = torch.Generator().manual_seed(3)
     ups = [torch.randn(r.shape, generator=g).cuda() for r in ref]
     for a, b in zip(ref, bat):
@@ -160,3 +163,42 @@ def test_finish_views_after_one_image_begin_is_reported():
               ids.data_ptr(), rng.data_ptr(), torch.cuda.current_stream().cuda_stream)
     torch.cuda.synchronize()
     assert int(h.info[1]) == 1  # PGB_ERR_INVALID (the outputs are then undefined)
+
+
+def test_tall_tiles_need_fewer_entries_and_every_variant_agrees():
+    """16 x 32 tile lists: fewer entries than 16 x 16 for the same batch, and
+    every compiled forward / backward variant gives the same images (bit for
+    bit) and gradients (1e-5, float sums in another order)."""
+    from pointrix_gb300 import autotune
+    cams = _cams()
+    leaves = _leaves()
+    with torch.no_grad():
+        ref, _, _ = multiview.render_views(*leaves, cams, bg=0.1)
+    pos, sc, q, op, shs = leaves
+    sizes = [(c.W, c.H) for c in cams]
+    with torch.no_grad():
+        uvr = [multiview.fused.preprocess(pos, sc, q, c.intr, c.extr[:3], c.W, c.H) for c in cams]
+    uv = torch.cat([u[0] for u in uvr])
+    radius = torch.cat([u[3] for u in uvr])
+    t16 = torch.cat([u[4] for u in uvr])
+    t32 = multiview.tile_counts_views(uv, radius, sizes, pos.shape[0], 32)
+    assert int(t32.sum()) < int(t16.sum())
+    g = torch.Generator().manual_seed(9)
+    ups = [torch.randn(r.shape, generator=g).cuda() for r in ref]
+    grads = []
+    try:
+        for bf in multiview._blend_batches_h(0, 32):
+            for bb in multiview._blend_batches_h(1, 32):
+                autotune.set_pins(f"fwd={bf},bwd={bb}")
+                lv = [t.detach().clone().requires_grad_(True) for t in leaves]
+                out, _, _ = multiview.render_views(*lv, cams, bg=0.1, tile_height=32)
+                for a, b in zip(out, ref):
+                    assert torch.equal(a, b), (bf, bb)
+                torch.autograd.backward(out, ups)
+                grads.append([t.grad for t in lv])
+    finally:
+        autotune.set_pins("")
+    for gr in grads[1:]:
+        for a, b in zip(gr, grads[0]):
+            assert float((a - b).norm() / b.norm()) < 1e-5
+    ops.check_device_status()
