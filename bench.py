@@ -34,6 +34,10 @@ import time
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
+# every kernel loaded when the context is created: with lazy loading the first
+# launch of each kernel variant (a new image size class in the serving leg,
+# say) stalls its stream for milliseconds inside a timed region
+os.environ.setdefault("CUDA_MODULE_LOADING", "EAGER")
 
 import torch  # noqa: E402
 
@@ -665,15 +669,17 @@ SERVE_WORKLOAD = ("serving: 8 resident SH3 scenes, N log-uniform in [200k, 2M], 
                   "Poisson arrivals, camera radius U[3,6], 512^2/800^2/1280x720/1920x1080")
 
 
-def serve_measure(device, rates=(100, 400, 1000), duration=1.5):
+def serve_measure(device, rates=(50, 100, 200, 500, 1000, 2000), duration=10.0):
     """p50/p99 latency and Mpix/s of the continuous-batching server against
-    the one-request-at-a-time plain path, per Poisson arrival rate."""
+    the one-request-at-a-time plain path, per Poisson arrival rate
+    (``duration`` seconds of arrivals per rate and server; every request is
+    served and counted, including the backlog after the arrivals stop)."""
     from pointrix_gb300 import serve
 
     scenes = serve.serving_scenes(device=device)
     for cls in (serve.PlainServer, serve.RenderServer):   # warm-up of both paths
         srv = cls(scenes)
-        for r in serve.random_requests(16, len(scenes), seed=99):
+        for r in serve.random_requests(64, len(scenes), seed=99):
             srv.submit(r)
         srv.close()
     out = []
@@ -681,12 +687,36 @@ def serve_measure(device, rates=(100, 400, 1000), duration=1.5):
         row = {"rate_req_per_s": rate}
         for name, cls in (("plain", serve.PlainServer), ("continuous", serve.RenderServer)):
             reqs = serve.random_requests(int(rate * duration), len(scenes), seed=rate, rate=rate)
-            srv = cls(scenes)
+            # the client takes each image as it arrives (the host buffers of
+            # tens of thousands of results are not kept)
+            srv = cls(scenes, on_done=_drop_image)
             t0 = serve.drive(srv, reqs)
-            row[name] = {k: round(v, 3) if isinstance(v, float) else v
-                         for k, v in serve.summarize(srv.close(), t0).items()}
+            stats = serve.summarize(srv.close(), t0)
+            if name == "continuous" and srv.batches:
+                stats["mean_batch"] = statistics.mean(srv.batches)
+                stats["max_batch"] = max(srv.batches)
+            row[name] = {k: round(v, 3) if isinstance(v, float) else v for k, v in stats.items()}
         out.append(row)
     return {"workload": SERVE_WORKLOAD, "duration_s": duration, "rates": out}
+
+
+def _drop_image(req):
+    req.image = None
+
+
+def serve_summary(serving):
+    """Compact per-rate line for the end of the bench output: p50/p99 ms and
+    Mpix/s of the plain path and the continuous-batching server."""
+    if not serving:
+        return None
+    out = {}
+    for row in serving["rates"]:
+        p, c = row["plain"], row["continuous"]
+        out[str(row["rate_req_per_s"])] = {
+            "plain_p50_p99_ms": [p.get("p50_ms"), p.get("p99_ms")], "plain_mpix_s": p.get("mpix_per_s"),
+            "cont_p50_p99_ms": [c.get("p50_ms"), c.get("p99_ms")], "cont_mpix_s": c.get("mpix_per_s"),
+            "cont_mean_batch": c.get("mean_batch")}
+    return out
 
 
 # ------------------------------------------------------------ roofline ---
@@ -1006,6 +1036,16 @@ def run_gb300(args):
             "blend_batch": {"/".join(map(str, k)): b for k, b in autotune.table().items()},
             "blend_batch_ms": {"/".join(map(str, k)): {str(b): round(t, 4) for b, t in v.items()}
                                for k, v in autotune.timings().items()},
+            # compact summaries last, where a truncated log still shows them
+            "multiview_summary": None if not multi else {
+                "tile_shape": multi["tile_shape"], "speedup_vs_per_view_loop": multi["speedup"],
+                "batched_p50_p99_ms": [multi["batched_graph"]["p50_ms"], multi["batched_graph"]["p99_ms"]],
+                "loop_p50_p99_ms": [multi["per_view_loop"]["p50_ms"], multi["per_view_loop"]["p99_ms"]],
+                "max_abs_image_diff": multi["max_abs_image_diff"]},
+            "recompute_summary": None if not recompute else {
+                k: {"ms": round(v["ms_per_step"], 2), "peak_gb": round(v["peak_gb"], 2)}
+                for k, v in recompute.items() if isinstance(v, dict) and "peak_gb" in v},
+            "serve_summary": serve_summary(serving),
         }
         print(json.dumps(line), flush=True)
     if world > 1:

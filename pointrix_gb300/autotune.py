@@ -39,7 +39,7 @@ import warnings
 import torch
 
 __all__ = ["choose", "workload_class", "table", "timings", "reset", "set_enabled",
-           "set_cache_file", "set_pins"]
+           "set_cache_file", "set_pins", "timing_in_this_thread"]
 
 _lock = threading.Lock()
 _cache: dict = {}
@@ -60,6 +60,14 @@ def _parse_pins(text: str) -> dict:
 
 
 _pins = _parse_pins(os.environ.get("PGB_BLEND_VARIANT", ""))
+_thread = threading.local()
+
+
+def timing_in_this_thread(flag: bool) -> None:
+    """Allow (True) or forbid (False) timing runs in the calling thread only:
+    a thread that serves requests must not stall on a first-seen class (it
+    then uses the kept choice of the class, or the default)."""
+    _thread.enabled = bool(flag)
 
 
 def _key_str(key) -> str:
@@ -136,7 +144,7 @@ def choose(key, candidates, run, device=None, timer=None) -> int:
     if hit is not None and hit in candidates:
         return hit
     capturing = torch.cuda.is_available() and torch.cuda.is_current_stream_capturing()
-    if not _enabled or capturing or not candidates:
+    if not getattr(_thread, "enabled", _enabled) or capturing or not candidates:
         return 0
     timer = timer or (lambda fn: _cuda_timer(fn, device))
     times = {b: timer(lambda b=b: run(b)) for b in candidates}

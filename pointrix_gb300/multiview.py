@@ -57,6 +57,64 @@ def tile_counts_views(uv, radius, sizes, n_per_view, tile_height):
     return tiles
 
 
+class ViewsSortHandle:
+    """A views sort between its phases (:func:`sort_views_begin`): the depth
+    sort is enqueued and K is being copied to the host; ``ready()`` polls,
+    ``finish()`` enqueues the tile passes (on the stream of the begin)."""
+
+    __slots__ = ("h", "sizes", "n_per_view", "th")
+
+    def ready(self) -> bool:
+        return self.h.ready()
+
+    def count(self) -> int:
+        return self.h.count()
+
+    def finish(self):
+        return _sort_views_finish(self.h, self.sizes, self.n_per_view, self.th, None)
+
+
+def sort_views_begin(uv, depth, radius, tiles_touched, sizes, n_per_view, tile_height=16):
+    """Phase one of :func:`sort_views` without blocking the host (for a
+    server that overlaps requests): returns a :class:`ViewsSortHandle`."""
+    th = int(tile_height)
+    if th not in TILE_HEIGHTS:
+        raise ValueError(f"tile_height must be one of {TILE_HEIGHTS}, got {th}")
+    if th != TILE:
+        tiles_touched = tile_counts_views(_c(uv), _c(radius.reshape(-1)), sizes, n_per_view, th)
+    W0, H0 = sizes[0]
+    hv = ViewsSortHandle()
+    hv.h = ops.sort_gaussian_begin(uv, depth, W0, H0, radius, tiles_touched, read_count=True,
+                                   views=(len(sizes), n_per_view))
+    hv.sizes, hv.n_per_view, hv.th = list(sizes), int(n_per_view), th
+    return hv
+
+
+def _sort_views_finish(h, sizes, n_per_view, th, capacity):
+    K = h.count() if capacity is None else int(capacity)
+    dev = h.dev
+    T = sum(_tiles(W, H, th) for W, H in sizes)
+    # the batch sorts local tile ids: its K-sized scratch is that of the
+    # largest view's tile count (a 16T x 16 "image" has T tiles)
+    T_local = max(_tiles(W, H, th) for W, H in sizes)
+    _, bk = ops._sort_scratch(h.n, K, 16 * T_local, 16)
+    with torch.cuda.stream(h.stream):
+        scratch_k = torch.empty(max(bk, 1), dtype=torch.uint8, device=dev)
+        ids = torch.empty(max(K, 1), dtype=torch.int32, device=dev)[:K]
+        rng = torch.empty(T, 2, dtype=torch.int32, device=dev)
+        with _timed("sort_finish", dev, (3 + ops._tile_passes(T_local)) if (K and h.n) else
+                    (0 if capacity is None else 1)):
+            call("pgb_sort_gaussian_finish_views_h", _ptr(h.uv), _ptr(h.radius), _ptr(h.tiles),
+                 n_per_view, _sizes_array(sizes), len(sizes), th, K, 0 if capacity is None else 1,
+                 _ptr(h.scratch_n), h.bn, _ptr(scratch_k), bk, _ptr(h.info),
+                 _ptr(ids) if K else None, _ptr(rng), h.stream.cuda_stream)
+        if capacity is None:
+            ops._defer_check(h.info[1:], "sort_views (tile passes)")
+        else:
+            ops._fold_status(h.info[1:2], dev)
+    return ids, rng
+
+
 def sort_views(uv, depth, radius, tiles_touched, sizes, n_per_view, capacity=None, tile_height=16):
     """Tile lists of V views at once: ids [K] (element ids v*N + g) and
     tile_range [sum of tiles, 2] over the views' concatenated tile space.
@@ -76,27 +134,7 @@ def sort_views(uv, depth, radius, tiles_touched, sizes, n_per_view, capacity=Non
     W0, H0 = sizes[0]
     h = ops.sort_gaussian_begin(uv, depth, W0, H0, radius, tiles_touched,
                                 read_count=capacity is None, views=(len(sizes), n_per_view))
-    K = h.count() if capacity is None else int(capacity)
-    dev = uv.device
-    T = sum(_tiles(W, H, th) for W, H in sizes)
-    # the batch sorts local tile ids: its K-sized scratch is that of the
-    # largest view's tile count (a 16T x 16 "image" has T tiles)
-    T_local = max(_tiles(W, H, th) for W, H in sizes)
-    _, bk = ops._sort_scratch(h.n, K, 16 * T_local, 16)
-    scratch_k = torch.empty(max(bk, 1), dtype=torch.uint8, device=dev)
-    ids = torch.empty(max(K, 1), dtype=torch.int32, device=dev)[:K]
-    rng = torch.empty(T, 2, dtype=torch.int32, device=dev)
-    with _timed("sort_finish", dev, (3 + ops._tile_passes(T_local)) if (K and h.n) else
-                (0 if capacity is None else 1)):
-        call("pgb_sort_gaussian_finish_views_h", _ptr(h.uv), _ptr(h.radius), _ptr(h.tiles),
-             n_per_view, _sizes_array(sizes), len(sizes), th, K, 0 if capacity is None else 1,
-             _ptr(h.scratch_n), h.bn, _ptr(scratch_k), bk, _ptr(h.info),
-             _ptr(ids) if K else None, _ptr(rng), _stream(dev))
-    if capacity is None:
-        ops._defer_check(h.info[1:], "sort_views (tile passes)")
-    else:
-        ops._fold_status(h.info[1:2], dev)
-    return ids, rng
+    return _sort_views_finish(h, sizes, n_per_view, th, capacity)
 
 
 class _BlendViews(torch.autograd.Function):

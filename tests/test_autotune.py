@@ -120,3 +120,27 @@ def test_pins_override_timing_and_cache():
     finally:
         A.set_pins("")
         A.reset()
+
+
+def test_timing_can_be_forbidden_in_one_thread():
+    """A serving thread turns timing off for itself only: it gets the
+    default for a class nobody has timed, other threads still time."""
+    import threading
+    from pointrix_gb300 import autotune as A
+    A.reset()
+    got = {}
+
+    def server():
+        A.timing_in_this_thread(False)
+        got["server"] = A.choose(("blend_fwd", 3, 10, 4), [64, 128], lambda b: float(b),
+                                 timer=lambda fn: fn())
+
+    t = threading.Thread(target=server)
+    t.start()
+    t.join()
+    try:
+        assert got["server"] == 0
+        assert A.choose(("blend_fwd", 3, 10, 4), [64, 128], lambda b: float(b),
+                        timer=lambda fn: fn()) == 64
+    finally:
+        A.reset()
