@@ -34,11 +34,6 @@ import time
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
-# every kernel loaded when the context is created: with lazy loading the first
-# launch of each kernel variant (a new image size class in the serving leg,
-# say) stalls its stream for milliseconds inside a timed region
-os.environ.setdefault("CUDA_MODULE_LOADING", "EAGER")
-
 import torch  # noqa: E402
 
 METRIC = "train iters/s & Mpix/s at 1M Gaussians SH3; serve p50/p99 ms vs plain path"
