@@ -24,6 +24,7 @@ sample of tiles, on all host cores.
 from __future__ import annotations
 
 import argparse
+import datetime
 import json
 import os
 import statistics
@@ -93,7 +94,7 @@ def max_over_ranks(x, world, device):
 class ClockSampler:
     """Samples nvidia-smi clocks and throttle reasons while running."""
 
-    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+    FIELDS = ("timestamp,index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
@@ -101,6 +102,7 @@ class ClockSampler:
         self.index = index
         self.proc = None
         self.path = None
+        self.marks = {}
 
     def __enter__(self):
         try:
@@ -108,7 +110,7 @@ class ClockSampler:
             os.close(fd)
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
-                 "--format=csv,noheader,nounits", "-lms", "50"],
+                 "--format=csv,noheader,nounits", "-lms", "20"],
                 stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
         except Exception:
             self.proc = None
@@ -123,25 +125,46 @@ class ClockSampler:
                 self.proc.kill()
         return False
 
+    def mark(self, name):
+        """Records the host time of an event (the timed region's start and end)."""
+        self.marks[name] = time.time()
+
     def summary(self):
+        """Median SM clock and the throttle reasons seen over the sampled
+        window.  The caller keeps the GPU loaded for the whole window (the
+        timed region is ~40 ms, shorter than nvidia-smi's start-up), and
+        `in_region` counts the samples stamped between the marks."""
         if not self.path or not os.path.exists(self.path):
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
         rows = []
         for line in open(self.path):
             parts = [p.strip() for p in line.split(",")]
-            if len(parts) < 9:
+            if len(parts) < 10:
                 continue
             try:
-                rows.append((float(parts[1]), float(parts[2]), parts[5:9]))
+                stamp = datetime.datetime.strptime(parts[0], "%Y/%m/%d %H:%M:%S.%f").timestamp()
+                rows.append((float(parts[2]), float(parts[3]), parts[6:10], stamp))
             except ValueError:
                 continue
         os.unlink(self.path)
         if not rows:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        reasons = sorted({names[i] for _, _, flags in rows for i, f in enumerate(flags) if f == "Active"})
+        reasons = sorted({names[i] for _, _, flags, _ in rows for i, f in enumerate(flags) if f == "Active"})
+        t0, t1 = self.marks.get("start"), self.marks.get("end")
+        inside = [r for r in rows if t0 is not None and t1 is not None and t0 - 0.02 <= r[3] <= t1 + 0.02]
         return {"sm_mhz": statistics.median(r[0] for r in rows), "sm_max_mhz": max(r[1] for r in rows),
-                "reasons": reasons, "samples": len(rows)}
+                "reasons": reasons, "samples": len(rows), "in_region": len(inside),
+                "window_s": round(rows[-1][3] - rows[0][3], 3)}
+
+
+def keep_busy(fn, device, seconds):
+    """Replays `fn` for about `seconds` of wall time."""
+    t_end = time.perf_counter() + seconds
+    while time.perf_counter() < t_end:
+        for _ in range(20):
+            fn()
+        torch.cuda.synchronize(device)
 
 
 # ------------------------------------------------------------- workload ---
@@ -585,7 +608,7 @@ def ssim_measure(device, C=3, H=1060, W=1600, reps=10):
         e1.record()
         torch.cuda.synchronize(device)
         res[f"{name}_ms"] = e0.elapsed_time(e1) / reps
-        vals[name] = (float(v), x.grad.detach().clone())
+        vals[name] = (float(v.detach()), x.grad.detach().clone())
     res["value_abs_diff"] = abs(vals["fused"][0] - vals["torch"][0])
     gt = vals["torch"][1]
     res["grad_rel_max"] = float((vals["fused"][1] - gt).abs().max() / gt.abs().max())
@@ -912,14 +935,21 @@ def run_gb300(args):
     state.restore()
     torch.cuda.synchronize(device)
     with ClockSampler(device.index) as clocks:
+        # keep the GPU busy while nvidia-smi starts, so that the samples
+        # around the short timed region are taken under load
+        keep_busy(graphed, device, 0.5)
+        state.restore()
         barrier(world)
         torch.cuda.synchronize(device)
+        clocks.mark("start")
         start.record(stream)
         for _ in range(args.steps):
             graphed()
         end.record(stream)
         torch.cuda.synchronize(device)
+        clocks.mark("end")
         barrier(world)
+        keep_busy(graphed, device, 0.25)
     ms = max_over_ranks(start.elapsed_time(end) / args.steps, world, device)
     value = world / (ms / 1e3)
     ops.check_device_status(device)

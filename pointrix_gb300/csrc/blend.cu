@@ -381,6 +381,10 @@ __global__ void __launch_bounds__(64 * (TH / 8)) blend_fwd_kernel(
     int64_t* __restrict__ info, const int32_t* __restrict__ radius) {
   constexpr int NT = 64 * (TH / 8);  // 8 x 8 warp boxes over a 16 x TH tile
   constexpr bool F16 = TH != kTile;
+  // One bulk copy per thread per phase: the warp's expect_tx and its copies
+  // come from the same predicate, and no thread has a second copy to count.
+  static_assert(B <= NT, "a batch holds at most one record per thread");
+  static_assert(B * RF * 4 < (1 << 20), "a phase's bytes fit the mbarrier tx-count");
   extern __shared__ __align__(128) float smem[];
   __shared__ __align__(8) uint64_t bars[2];
   __shared__ uint8_t s_list[NT / 32][B];
@@ -493,8 +497,11 @@ __global__ void __launch_bounds__(64 * (TH / 8)) blend_fwd_kernel(
     for (int q = 0; q < kFwdPix; ++q) mine_done &= done[q];
     const int ndone = __syncthreads_count(mine_done || timed_out);
     if (ndone == NT || timed_out) {
+      // no copy may still be in flight when the CTA exits: its shared memory
+      // goes to the next CTA on this SM
       if (b + 1 < nb && !mbar_wait_bounded(&bars[buf ^ 1], ((b + 1) >> 1) & 1))
         set_info(info, PGB_ERR_TIMEOUT);
+      if (timed_out) mbar_wait_bounded(&bars[buf], (b >> 1) & 1);
       break;
     }
   }
