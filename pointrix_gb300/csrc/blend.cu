@@ -372,8 +372,11 @@ __device__ __forceinline__ int warp_cull(const float* stage, int RF, int cnt, fl
 // one TMA bulk copy per thread per batch.
 constexpr int kFwdPix = 2;
 constexpr int kFwdBatch = 128;  // default records per batch (64 and 128 are compiled)
+// Forward variant code: records per batch, plus kFwdFlat for the form
+// without per-pixel branches in the compositing step.
+constexpr int kFwdFlat = 2048;
 
-template <int NC, int RF, int B, int TH = 16>
+template <int NC, int RF, int B, int TH = 16, bool FLAT = false>
 __global__ void __launch_bounds__(64 * (TH / 8)) blend_fwd_kernel(
     const float* __restrict__ records, const int32_t* __restrict__ ids,
     const int2* __restrict__ ranges, int64_t n, float bg, const ViewTable vt, int C,
@@ -467,6 +470,44 @@ __global__ void __launch_bounds__(64 * (TH / 8)) blend_fwd_kernel(
         const float4 r1 = *reinterpret_cast<const float4*>(rec + 4);
         const float dx = __fsub_rn(r0.x, pxf);
         const SplatX sx = splat_x(r0.z, r0.w, dx);
+        if constexpr (FLAT) {
+          // both pixels' steps without per-pixel branches (independent
+          // dependency chains): a pixel that skips the splat, has stopped
+          // or stops at it composites nothing and keeps T and last
+          bool any = false;
+          float p2q[kFwdPix];
+          bool okq[kFwdPix];
+#pragma unroll
+          for (int q = 0; q < kFwdPix; ++q) {
+            p2q[q] = splat_power2(sx, r1.x, __fsub_rn(r0.y, pyf[q]));
+            okq[q] = !done[q] && !(p2q[q] > 0.f || p2q[q] < r1.w);  // alpha >= 1/255
+            any |= okq[q];
+          }
+          if (any) {
+            const float* f = rec + kRecFeat;
+            float fr[NC];
+#pragma unroll
+            for (int c = 0; c < NC; ++c) fr[c] = f[c];
+#pragma unroll
+            for (int q = 0; q < kFwdPix; ++q) {
+              const float alpha = fminf(0.99f, __fmul_rn(r1.y, ex2_approx(p2q[q])));
+              const float test_T = __fmul_rn(T[q], __fsub_rn(1.0f, alpha));
+              const bool stop = okq[q] && test_T < 1e-4f;
+              const bool comp = okq[q] && !stop;
+              done[q] = done[q] || stop;
+              const float wgt = comp ? alpha * T[q] : 0.f;
+#pragma unroll
+              for (int c = 0; c < NC; ++c) acc[q][c] = fmaf(fr[c], wgt, acc[q][c]);
+              T[q] = comp ? test_T : T[q];
+              last[q] = comp ? base + j : last[q];
+            }
+          }
+          bool all = true;
+#pragma unroll
+          for (int q = 0; q < kFwdPix; ++q) all &= done[q];
+          if (all) break;
+          continue;
+        }
         bool live = false;
 #pragma unroll
         for (int q = 0; q < kFwdPix; ++q) {
@@ -780,9 +821,16 @@ __global__ void __launch_bounds__(256 / PX * (TH / 16)) blend_bwd_kernel(
 // The skip decisions use the forward's exact arithmetic (splat_power2).
 // Variant codes: kBwdV2 + records per batch (butterfly reduction),
 // kBwdV2 + 512 + records (transposed reduction), kBwdV2 + 1024 + records
-// (transposed reduction, at most 85 registers: twelve CTAs per SM); four
-// pixels per thread.
+// (transposed reduction, at most 85 registers: twelve CTAs per SM),
+// kBwdV2 + kBwdFlat + records (butterfly reduction, the pixels' replay steps
+// without per-pixel branches), kBwdV2 + kBwdFlat + 1024 + records (the same
+// at most 102 registers: ten CTAs per SM); four pixels per thread.
 constexpr int kBwdV2 = 8192;
+constexpr int kBwdFlat = 2048;
+// One warp per CTA (blend_bwd_solo_kernel): kBwdSolo + records per batch
+// (at most 128 registers), + 1024 + records (102 registers), + 2048 +
+// records (85 registers).
+constexpr int kBwdSolo = 16384;
 
 __device__ __forceinline__ float2 f2(float x, float y) { return make_float2(x, y); }
 
@@ -794,7 +842,7 @@ __device__ __forceinline__ float2 f2(float x, float y) { return make_float2(x, y
 // of the butterfly's 16 shuffles, 16 adds and 32 selects.
 constexpr int kRedStride = 20;  // floats per row: 16-byte rows on distinct bank groups
 
-template <int NC, int RF, int GR, int B, int PX, int MINB, bool XRED>
+template <int NC, int RF, int GR, int B, int PX, int MINB, bool XRED, bool FLAT = false>
 __global__ void __launch_bounds__(256 / PX, MINB) blend_bwd2_kernel(
     const float* __restrict__ records, const int32_t* __restrict__ ids,
     const int2* __restrict__ ranges, int64_t n, float bg, const ViewTable vt, int C,
@@ -904,6 +952,57 @@ __global__ void __launch_bounds__(256 / PX, MINB) blend_bwd2_kernel(
 #pragma unroll
       for (int k = 0; k < GR / 2; ++k) v[k] = f2(0.f, 0.f);
       bool contrib = false;
+      if constexpr (FLAT) {
+        // every pixel's skip test first, then one warp-uniform branch and
+        // the pixels' replay steps without per-pixel branches: the PX
+        // dependency chains are independent and interleave.  A pixel that
+        // skips the splat gets alpha = 0 and keeps T and SB exactly.
+        float dyq[PX], p2q[PX];
+        bool okq[PX];
+#pragma unroll
+        for (int q = 0; q < PX; ++q) {
+          dyq[q] = __fsub_rn(r0.y, py0 + (float)(RS * q));
+          p2q[q] = splat_power2(sx, r1.x, dyq[q]);
+          okq[q] = j < nc[q] && !(p2q[q] > 0.f || p2q[q] < r1.w);  // the forward's skip test
+          contrib |= okq[q];
+        }
+        if (!__any_sync(0xffffffffu, contrib)) continue;
+        const float2* fp = reinterpret_cast<const float2*>(rec + kRecFeat);
+        float2 fr[NP];
+#pragma unroll
+        for (int k = 0; k < NP; ++k) fr[k] = fp[k];
+#pragma unroll
+        for (int q = 0; q < PX; ++q) {
+          const float dy = dyq[q];
+          const float g0 = __fmaf_rn(r0.w, dy, sx.Adx), g1 = __fmaf_rn(r1.x, dy, sx.Bdx);
+          const float G = ex2_approx(p2q[q]);
+          const float araw = __fmul_rn(r1.y, G);
+          const float alpha = okq[q] ? fminf(0.99f, araw) : 0.f;
+          const float om = __fsub_rn(1.0f, alpha);
+          T[q] = okq[q] ? __fdividef(T[q], om) : T[q];
+          const float4 dlo = s_dout[0][q * NT + threadIdx.x];
+          const float4 dhi = s_dout[1][q * NT + threadIdx.x];
+          const float2 dp[4] = {f2(dlo.x, dlo.y), f2(dlo.z, dlo.w), f2(dhi.x, dhi.y),
+                                f2(dhi.z, dhi.w)};
+          float2 F2 = __fmul2_rn(dp[0], fr[0]);
+#pragma unroll
+          for (int k = 1; k < NP; ++k) F2 = __ffma2_rn(dp[k], fr[k], F2);
+          const float F = F2.x + F2.y;
+          const float wT = alpha * T[q];
+          const float2 wT2 = f2(wT, wT);
+#pragma unroll
+          for (int k = 0; k < NP; ++k) v[3 + k] = __ffma2_rn(wT2, dp[k], v[3 + k]);
+          const float dalpha = (F - SB[q]) * T[q];
+          SB[q] = fmaf(alpha, F, om * SB[q]);
+          const bool m = okq[q] && araw < 0.99f;
+          const float dpow = m ? alpha * dalpha : 0.f;
+          const float Gm = m ? G : 0.f;
+          const float tx = dpow * dx;
+          v[0] = __ffma2_rn(f2(g0, g1), f2(dpow, dpow), v[0]);
+          v[1] = __ffma2_rn(f2(tx, tx), f2(dx, dy), v[1]);
+          v[2] = __ffma2_rn(f2(dpow * dy, Gm), f2(dy, dalpha), v[2]);
+        }
+      } else {
 #pragma unroll
       for (int q = 0; q < PX; ++q) {
         if (j >= nc[q]) continue;
@@ -940,7 +1039,8 @@ __global__ void __launch_bounds__(256 / PX, MINB) blend_bwd2_kernel(
           v[2] = __ffma2_rn(f2(dpow * dy, G), f2(dy, dalpha), v[2]);      // dy^2 dp, G dalpha
         }
       }
-      if (__any_sync(0xffffffffu, contrib)) {
+      }
+      if (FLAT || __any_sync(0xffffffffu, contrib)) {
         if constexpr (XRED && GR == 16) {
           float* tab = s_red[w];
           float4* row = reinterpret_cast<float4*>(tab + lane * kRedStride);
@@ -993,6 +1093,192 @@ __global__ void __launch_bounds__(256 / PX, MINB) blend_bwd2_kernel(
       s_touched[t] = 0;
     }
     __syncthreads();
+  }
+}
+
+// Backward, one warp per CTA: each 8 x 16 half of a 16 x 16 tile is its own
+// CTA of 32 threads (CTA 2t + h covers half h of tile t), with its own
+// double-buffered record stage, list and per-splat sums.  Nothing is shared
+// between the halves, so the kernel has no CTA-wide barrier: a warp waits
+// only for its own copies (cp.async groups, __syncwarp), walks only its own
+// last-contributor range, and frees its slot on the SM when it finishes.
+// A splat's per-batch sums have one owner lane per component, so they
+// accumulate with plain shared-memory adds (no atomics); each half flushes
+// its own sums with 16-byte vector atomics.  The replay is the flat form of
+// blend_bwd2_kernel (four pixels per lane, no per-pixel branches).
+template <int NC, int RF, int GR, int B, int MINB>
+__global__ void __launch_bounds__(32, MINB) blend_bwd_solo_kernel(
+    const float* __restrict__ records, const int32_t* __restrict__ ids,
+    const int2* __restrict__ ranges, int64_t n, float bg, const ViewTable vt, int C,
+    const float* __restrict__ final_T, const int32_t* __restrict__ n_contrib,
+    const float* __restrict__ d_out, float* __restrict__ grad_records,
+    int64_t* __restrict__ info) {
+  static_assert(GR == 16, "one owner lane per component of a 16-float gradient record");
+  static_assert(NC <= 8, "the d_out planes hold eight channels");
+  constexpr int PX = 4, BW = 8, RS = 4, BH = 16;
+  constexpr int NP = (NC + 1) / 2;
+  extern __shared__ __align__(128) float smem[];
+  __shared__ uint8_t s_touched[B];
+  __shared__ uint8_t s_list[B];
+  __shared__ __align__(16) float4 s_dout[2][PX * 32];  // [plane][q * 32 + lane]
+  float* gacc = smem + 2 * B * RF;                     // [B][GR]
+
+  const int tile = blockIdx.x >> 1;
+  int W, H, gx, ltile;
+  int64_t pbase;
+  tile_view(vt, tile, W, H, gx, ltile, pbase);
+  const int lane = threadIdx.x;
+  const int bx0 = (ltile % gx) * kTile + BW * (blockIdx.x & 1);
+  const int by0 = (ltile / gx) * kTile;
+
+  for (int i = lane; i < B * GR; i += 32) gacc[i] = 0.f;
+  for (int i = lane; i < B; i += 32) s_touched[i] = 0;
+
+  const int64_t plane = (int64_t)W * H;
+  const int pxi = bx0 + (lane & (BW - 1));
+  const float pxf = (float)pxi;
+  const float py0 = (float)(by0 + lane / BW);
+  float T[PX], SB[PX];
+  int nc[PX];
+  int my_nc = 0;
+#pragma unroll
+  for (int q = 0; q < PX; ++q) {
+    const int py = by0 + lane / BW + RS * q;
+    float dv[8];
+#pragma unroll
+    for (int c = 0; c < 8; ++c) dv[c] = 0.f;
+    T[q] = 1.f;
+    nc[q] = 0;
+    if (pxi < W && py < H) {
+      const int64_t pix = (int64_t)py * W + pxi;
+      T[q] = final_T[pbase + pix];
+      nc[q] = n_contrib[pbase + pix];
+#pragma unroll
+      for (int c = 0; c < NC; ++c)
+        if (c < C) dv[c] = d_out[C * pbase + c * plane + pix];
+    }
+    float sd = 0.f;
+#pragma unroll
+    for (int c = 0; c < NC; ++c) sd += dv[c];
+    SB[q] = bg * sd;
+    s_dout[0][q * 32 + lane] = make_float4(dv[0], dv[1], dv[2], dv[3]);
+    s_dout[1][q * 32 + lane] = make_float4(dv[4], dv[5], dv[6], dv[7]);
+    my_nc = max(my_nc, nc[q]);
+  }
+  int warp_nc = my_nc;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) warp_nc = max(warp_nc, __shfl_xor_sync(0xffffffffu, warp_nc, o));
+  const int2 rg = ranges[tile];
+  const int64_t start = rg.x;
+  const int list_len = max(0, rg.y - rg.x);
+  if (warp_nc > list_len && lane == 0) set_info(info, PGB_ERR_OVERFLOW);
+  const int max_nc = min(warp_nc, list_len);
+  const int nb = (max_nc + B - 1) / B;
+  auto lo_of = [&](int b) { return max(0, max_nc - (b + 1) * B); };
+  auto hi_of = [&](int b) { return max_nc - b * B; };
+  __syncwarp();
+
+  if (nb > 0)
+    stage_batch<RF, 32, B>(records, ids, start + lo_of(0), start + hi_of(0), n, smem, info);
+  for (int b = 0; b < nb; ++b) {
+    const int buf = b & 1;
+    const int lo = lo_of(b), hi = hi_of(b);
+    if (b + 1 < nb) {
+      stage_batch<RF, 32, B>(records, ids, start + lo_of(b + 1), start + hi_of(b + 1), n,
+                             smem + (buf ^ 1) * B * RF, info);
+      cp_async_wait<1>();
+    } else {
+      cp_async_wait<0>();
+    }
+    __syncwarp();  // every lane's copies of batch b have landed
+    const float* st = smem + buf * B * RF;
+    const int nl = warp_cull<BW, BH, B>(st, RF, hi - lo, (float)bx0, (float)by0, s_list);
+    for (int t = nl - 1; t >= 0; --t) {
+      const int slot = s_list[t];
+      const int j = lo + slot;
+      const float* rec = st + slot * RF;
+      const float4 r0 = *reinterpret_cast<const float4*>(rec);      // u, v, A, B
+      const float4 r1 = *reinterpret_cast<const float4*>(rec + 4);  // C, o, tau, thr
+      const float dx = __fsub_rn(r0.x, pxf);
+      const SplatX sx = splat_x(r0.z, r0.w, dx);
+      float dyq[PX], p2q[PX];
+      bool okq[PX];
+      bool contrib = false;
+#pragma unroll
+      for (int q = 0; q < PX; ++q) {
+        dyq[q] = __fsub_rn(r0.y, py0 + (float)(RS * q));
+        p2q[q] = splat_power2(sx, r1.x, dyq[q]);
+        okq[q] = j < nc[q] && !(p2q[q] > 0.f || p2q[q] < r1.w);  // the forward's skip test
+        contrib |= okq[q];
+      }
+      if (!__any_sync(0xffffffffu, contrib)) continue;
+      float2 v[8];
+#pragma unroll
+      for (int k = 0; k < 8; ++k) v[k] = f2(0.f, 0.f);
+      const float2* fp = reinterpret_cast<const float2*>(rec + kRecFeat);
+      float2 fr[NP];
+#pragma unroll
+      for (int k = 0; k < NP; ++k) fr[k] = fp[k];
+#pragma unroll
+      for (int q = 0; q < PX; ++q) {
+        const float dy = dyq[q];
+        const float g0 = __fmaf_rn(r0.w, dy, sx.Adx), g1 = __fmaf_rn(r1.x, dy, sx.Bdx);
+        const float G = ex2_approx(p2q[q]);
+        const float araw = __fmul_rn(r1.y, G);
+        const float alpha = okq[q] ? fminf(0.99f, araw) : 0.f;
+        const float om = __fsub_rn(1.0f, alpha);
+        T[q] = okq[q] ? __fdividef(T[q], om) : T[q];
+        const float4 dlo = s_dout[0][q * 32 + lane];
+        const float4 dhi = s_dout[1][q * 32 + lane];
+        const float2 dp[4] = {f2(dlo.x, dlo.y), f2(dlo.z, dlo.w), f2(dhi.x, dhi.y),
+                              f2(dhi.z, dhi.w)};
+        float2 F2 = __fmul2_rn(dp[0], fr[0]);
+#pragma unroll
+        for (int k = 1; k < NP; ++k) F2 = __ffma2_rn(dp[k], fr[k], F2);
+        const float F = F2.x + F2.y;
+        const float wT = alpha * T[q];
+        const float2 wT2 = f2(wT, wT);
+#pragma unroll
+        for (int k = 0; k < NP; ++k) v[3 + k] = __ffma2_rn(wT2, dp[k], v[3 + k]);
+        const float dalpha = (F - SB[q]) * T[q];
+        SB[q] = fmaf(alpha, F, om * SB[q]);
+        const bool m = okq[q] && araw < 0.99f;
+        const float dpow = m ? alpha * dalpha : 0.f;
+        const float Gm = m ? G : 0.f;
+        const float tx = dpow * dx;
+        v[0] = __ffma2_rn(f2(g0, g1), f2(dpow, dpow), v[0]);        // sum g0 dp, g1 dp
+        v[1] = __ffma2_rn(f2(tx, tx), f2(dx, dy), v[1]);            // dx^2 dp, dx dy dp
+        v[2] = __ffma2_rn(f2(dpow * dy, Gm), f2(dy, dalpha), v[2]);  // dy^2 dp, G dalpha
+      }
+      float vf[16];
+#pragma unroll
+      for (int k = 0; k < 8; ++k) {
+        vf[2 * k] = v[k].x;
+        vf[2 * k + 1] = v[k].y;
+      }
+      const float sum = warp_reduce_scatter<16>(vf);
+      // lanes 2k and 2k + 1 both hold component k; the even one owns it
+      if ((lane & 1) == 0 && (lane >> 1) < 6 + NC) gacc[slot * GR + (lane >> 1)] += sum;
+      if (lane == 0) s_touched[slot] = 1;
+    }
+    __syncwarp();
+    for (int t = lane; t < hi - lo; t += 32) {
+      if (!s_touched[t]) continue;
+      const int32_t g = ids[start + lo + t];
+      if (g < 0 || (int64_t)g >= n) {
+        set_info(info, PGB_ERR_OVERFLOW);
+        continue;
+      }
+      float4* dst = reinterpret_cast<float4*>(grad_records + (int64_t)g * GR);
+      float4* srcv = reinterpret_cast<float4*>(gacc + t * GR);
+#pragma unroll
+      for (int q = 0; q < (6 + NC + 3) / 4; ++q) {
+        atomicAdd(dst + q, srcv[q]);
+        srcv[q] = make_float4(0.f, 0.f, 0.f, 0.f);
+      }
+      s_touched[t] = 0;
+    }
+    __syncwarp();  // the stage of batch b is refilled by the next iteration's copies
   }
 }
 
@@ -1076,13 +1362,13 @@ constexpr bool kTall = NC == 3 || NC == 4 || NC == 7;
 
 inline bool tall_tiles(const ViewTable& vt) { return vt.nviews > 0 && vt.th == 32; }
 
-template <int NC, int B, int TH = 16>
+template <int NC, int B, int TH = 16, bool FLAT = false>
 static int launch_fwd_b(const float* records, const int32_t* ids, const int2* ranges, int64_t n,
                         float bg, const ViewTable& vt, int tiles, int C, float* out, float* fT,
                         int32_t* ncon, int64_t* info, cudaStream_t s, const int32_t* radius) {
   constexpr int RF = rec_floats(NC);
   const size_t smem = 2 * B * RF * sizeof(float);
-  auto kern = blend_fwd_kernel<NC, RF, B, TH>;
+  auto kern = blend_fwd_kernel<NC, RF, B, TH, FLAT>;
   if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
       cudaSuccess)
     return PGB_ERR_CUDA;
@@ -1108,6 +1394,8 @@ static int launch_fwd_nc(const float* records, const int32_t* ids, const int2* r
         case 64: return PGB_FWD(64, 32);
         case 128: return PGB_FWD(128, 32);
         case 256: return PGB_FWD(256, 32);
+        case kFwdFlat + 64: return PGB_FWD(64, 32);
+        case kFwdFlat + 128: return PGB_FWD(128, 32);
         default: return PGB_ERR_INVALID;
       }
     }
@@ -1116,12 +1404,18 @@ static int launch_fwd_nc(const float* records, const int32_t* ids, const int2* r
   switch (batch == 0 ? kFwdBatch : batch) {
     case 64: return PGB_FWD(64, 16);
     case 128: return PGB_FWD(128, 16);
+    case kFwdFlat + 64:
+      return launch_fwd_b<NC, 64, 16, true>(records, ids, ranges, n, bg, vt, tiles, C, out, fT,
+                                            ncon, info, s, radius);
+    case kFwdFlat + 128:
+      return launch_fwd_b<NC, 128, 16, true>(records, ids, ranges, n, bg, vt, tiles, C, out, fT,
+                                             ncon, info, s, radius);
     default: return PGB_ERR_INVALID;
   }
 #undef PGB_FWD
 }
 
-template <int NC, int B, int PX, int MINB, bool XRED>
+template <int NC, int B, int PX, int MINB, bool XRED, bool FLAT = false>
 static int launch_bwd2_b(const float* records, const int32_t* ids, const int2* ranges, int64_t n,
                          float bg, const ViewTable& vt, int tiles, int C, const float* fT,
                          const int32_t* ncon, const float* dout, float* grec, int64_t* info,
@@ -1129,7 +1423,7 @@ static int launch_bwd2_b(const float* records, const int32_t* ids, const int2* r
   constexpr int RF = rec_floats(NC);
   constexpr int GR = grad_floats(NC);
   const size_t smem = (2 * RF + GR) * B * sizeof(float);
-  auto kern = blend_bwd2_kernel<NC, RF, GR, B, PX, MINB, XRED>;
+  auto kern = blend_bwd2_kernel<NC, RF, GR, B, PX, MINB, XRED, FLAT>;
   if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
           cudaSuccess ||
       cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout,
@@ -1137,6 +1431,24 @@ static int launch_bwd2_b(const float* records, const int32_t* ids, const int2* r
     return PGB_ERR_CUDA;
   kern<<<tiles, 256 / PX, smem, s>>>(records, ids, ranges, n, bg, vt, C, fT, ncon, dout, grec,
                                      info);
+  return launch_status();
+}
+
+template <int NC, int B, int MINB>
+static int launch_bwd_solo(const float* records, const int32_t* ids, const int2* ranges,
+                           int64_t n, float bg, const ViewTable& vt, int tiles, int C,
+                           const float* fT, const int32_t* ncon, const float* dout, float* grec,
+                           int64_t* info, cudaStream_t s) {
+  constexpr int RF = rec_floats(NC);
+  constexpr int GR = grad_floats(NC);
+  const size_t smem = (2 * RF + GR) * B * sizeof(float);
+  auto kern = blend_bwd_solo_kernel<NC, RF, GR, B, MINB>;
+  if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+          cudaSuccess ||
+      cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout,
+                           cudaSharedmemCarveoutMaxShared) != cudaSuccess)
+    return PGB_ERR_CUDA;
+  kern<<<2 * tiles, 32, smem, s>>>(records, ids, ranges, n, bg, vt, C, fT, ncon, dout, grec, info);
   return launch_status();
 }
 
@@ -1179,9 +1491,17 @@ static int launch_bwd_nc(const float* records, const int32_t* ids, const int2* r
         case 256: return PGB_BWD_T(256, 2, 32);
         case kBwdPx4 + 32:
         case kBwdV2 + 512 + 32:
-        case kBwdV2 + 1024 + 32: return PGB_BWD_T(32, 4, 32);
+        case kBwdV2 + 1024 + 32:
+        case kBwdV2 + kBwdFlat + 32:
+        case kBwdV2 + kBwdFlat + 1024 + 32: return PGB_BWD_T(32, 4, 32);
         case kBwdPx4 + 64:
-        case kBwdV2 + 64: return PGB_BWD_T(64, 4, 32);
+        case kBwdV2 + 64:
+        case kBwdV2 + kBwdFlat + 64:
+        case kBwdV2 + kBwdFlat + 1024 + 64:
+        case kBwdSolo + 64: return PGB_BWD_T(64, 4, 32);
+        case kBwdSolo + 32:
+        case kBwdSolo + 1024 + 32:
+        case kBwdSolo + 2048 + 32: return PGB_BWD_T(32, 4, 32);
         case kBwdPx4 + 128: return PGB_BWD_T(128, 4, 32);
         default: return PGB_ERR_INVALID;
       }
@@ -1198,23 +1518,52 @@ static int launch_bwd_nc(const float* records, const int32_t* ids, const int2* r
     default: break;
   }
   if constexpr (NC <= 8) {
-#define PGB_BWD2(B, PX, MINB, XRED)                                                            \
-  launch_bwd2_b<NC, B, PX, MINB, XRED>(records, ids, ranges, n, bg, vt, tiles, C, fT, ncon, dout, \
-                                       grec, info, s)
+#define PGB_BWD2(B, PX, MINB, XRED, FLAT)                                                     \
+  launch_bwd2_b<NC, B, PX, MINB, XRED, FLAT>(records, ids, ranges, n, bg, vt, tiles, C, fT, ncon, \
+                                             dout, grec, info, s)
     switch (batch) {
-      case kBwdV2 + 64: return PGB_BWD2(64, 4, 1, false);
-      case kBwdV2 + 512 + 32: return PGB_BWD2(32, 4, 1, true);
-      case kBwdV2 + 1024 + 32: return PGB_BWD2(32, 4, 12, true);
+      case kBwdV2 + 64: return PGB_BWD2(64, 4, 1, false, false);
+      case kBwdV2 + 512 + 32: return PGB_BWD2(32, 4, 1, true, false);
+      case kBwdV2 + 1024 + 32: return PGB_BWD2(32, 4, 12, true, false);
+      case kBwdV2 + kBwdFlat + 32: return PGB_BWD2(32, 4, 1, false, true);
+      case kBwdV2 + kBwdFlat + 64: return PGB_BWD2(64, 4, 1, false, true);
+      case kBwdV2 + kBwdFlat + 1024 + 32: return PGB_BWD2(32, 4, 10, false, true);
+      case kBwdV2 + kBwdFlat + 1024 + 64: return PGB_BWD2(64, 4, 10, false, true);
       default: break;
+    }
+    if constexpr (grad_floats(NC) == 16) {
+      switch (batch) {
+        case kBwdSolo + 32:
+          return launch_bwd_solo<NC, 32, 16>(records, ids, ranges, n, bg, vt, tiles, C, fT, ncon,
+                                              dout, grec, info, s);
+        case kBwdSolo + 64:
+          return launch_bwd_solo<NC, 64, 16>(records, ids, ranges, n, bg, vt, tiles, C, fT, ncon,
+                                              dout, grec, info, s);
+        case kBwdSolo + 1024 + 32:
+          return launch_bwd_solo<NC, 32, 20>(records, ids, ranges, n, bg, vt, tiles, C, fT, ncon,
+                                              dout, grec, info, s);
+        case kBwdSolo + 2048 + 32:
+          return launch_bwd_solo<NC, 32, 24>(records, ids, ranges, n, bg, vt, tiles, C, fT, ncon,
+                                              dout, grec, info, s);
+        default: break;
+      }
     }
 #undef PGB_BWD2
   } else {
     // the second form keeps eight channels of d_out in shared memory: wider
     // features take the first form's four-pixel kernel with the same batch
     switch (batch) {
-      case kBwdV2 + 64: return PGB_BWD(64, 4);
+      case kBwdV2 + 64:
+      case kBwdV2 + kBwdFlat + 64:
+      case kBwdV2 + kBwdFlat + 1024 + 64:
+      case kBwdSolo + 64: return PGB_BWD(64, 4);
+      case kBwdSolo + 32:
+      case kBwdSolo + 1024 + 32:
+      case kBwdSolo + 2048 + 32: return PGB_BWD(32, 4);
       case kBwdV2 + 512 + 32:
-      case kBwdV2 + 1024 + 32: return PGB_BWD(32, 4);
+      case kBwdV2 + 1024 + 32:
+      case kBwdV2 + kBwdFlat + 32:
+      case kBwdV2 + kBwdFlat + 1024 + 32: return PGB_BWD(32, 4);
       default: break;
     }
   }
@@ -1602,11 +1951,15 @@ int pgb_blend_pair_census(const float* records, int channels, int64_t n, const i
 
 // Batch sizes compiled for the forward (backward = 0) or the backward (1).
 int pgb_blend_batches(int backward, int32_t* out) {
-  static const int32_t f[] = {64, 128},
+  static const int32_t f[] = {64, 128, kFwdFlat + 64, kFwdFlat + 128},
                        b[] = {64, 128, 256, kBwdPx4 + 32, kBwdPx4 + 64, kBwdPx4 + 128,
-                              kBwdV2 + 64, kBwdV2 + 512 + 32, kBwdV2 + 1024 + 32};
+                              kBwdV2 + 64, kBwdV2 + 512 + 32, kBwdV2 + 1024 + 32,
+                              kBwdV2 + kBwdFlat + 32, kBwdV2 + kBwdFlat + 64,
+                              kBwdV2 + kBwdFlat + 1024 + 32, kBwdV2 + kBwdFlat + 1024 + 64,
+                              kBwdSolo + 32, kBwdSolo + 64, kBwdSolo + 1024 + 32,
+                              kBwdSolo + 2048 + 32};
   const int32_t* src = backward ? b : f;
-  const int cnt = backward ? 9 : 2;
+  const int cnt = backward ? 17 : 4;
   if (out)
     for (int i = 0; i < cnt; ++i) out[i] = src[i];
   return cnt;
