@@ -347,6 +347,7 @@ __device__ __forceinline__ bool in_list16(const float* rec, int r, const List16&
 template <int BW, int BH, int B, bool F16 = false>
 __device__ __forceinline__ int warp_cull(const float* stage, int RF, int cnt, float x0, float y0,
                                          uint8_t* list, const List16& f16 = List16{}) {
+  static_assert(B % 32 == 0, "the warp tests its batch 32 slots at a time");
   const int lane = threadIdx.x & 31;
   const uint32_t lt = (1u << lane) - 1u;
   int n = 0;
@@ -831,6 +832,9 @@ constexpr int kBwdFlat = 2048;
 // (at most 128 registers), + 1024 + records (102 registers), + 2048 +
 // records (85 registers).
 constexpr int kBwdSolo = 16384;
+// One warp per 16 x 16 tile (blend_bwd_tile_kernel): kBwdTile + records per
+// batch.
+constexpr int kBwdTile = 32768;
 
 __device__ __forceinline__ float2 f2(float x, float y) { return make_float2(x, y); }
 
@@ -1282,6 +1286,191 @@ __global__ void __launch_bounds__(32, MINB) blend_bwd_solo_kernel(
   }
 }
 
+// Backward, one warp per 16 x 16 tile: lane l owns the eight pixels
+// (l % 8 + 8 (q & 1), l / 8 + 4 (q >> 1)), q < 8, so one per-splat warp
+// reduction serves the whole tile (256 pixels) and every pixel slot q is an
+// 8 x 4 block.  The skip tests of all eight slots come first; a slot where
+// no lane composites the splat is skipped by a warp-uniform branch, and a
+// slot where some lane does runs its replay step without per-pixel branches
+// (a lane that skips gets alpha = 0 and keeps T and SB exactly).  No CTA
+// barrier (one warp per CTA); per-splat sums in shared memory with one
+// owner lane per component, flushed with 16-byte vector atomics.
+template <int NC, int RF, int GR, int B, int MINB>
+__global__ void __launch_bounds__(32, MINB) blend_bwd_tile_kernel(
+    const float* __restrict__ records, const int32_t* __restrict__ ids,
+    const int2* __restrict__ ranges, int64_t n, float bg, const ViewTable vt, int C,
+    const float* __restrict__ final_T, const int32_t* __restrict__ n_contrib,
+    const float* __restrict__ d_out, float* __restrict__ grad_records,
+    int64_t* __restrict__ info) {
+  static_assert(GR == 16, "one owner lane per component of a 16-float gradient record");
+  static_assert(NC <= 8, "the d_out planes hold eight channels");
+  constexpr int PX = 8;
+  constexpr int NP = (NC + 1) / 2;
+  extern __shared__ __align__(128) float smem[];
+  __shared__ uint8_t s_touched[B];
+  __shared__ uint8_t s_list[B];
+  __shared__ __align__(16) float4 s_dout[2][PX * 32];  // [plane][q * 32 + lane]
+  float* gacc = smem + 2 * B * RF;                     // [B][GR]
+
+  const int tile = blockIdx.x;
+  int W, H, gx, ltile;
+  int64_t pbase;
+  tile_view(vt, tile, W, H, gx, ltile, pbase);
+  const int lane = threadIdx.x;
+  const int bx0 = (ltile % gx) * kTile, by0 = (ltile / gx) * kTile;
+
+  for (int i = lane; i < B * GR; i += 32) gacc[i] = 0.f;
+  for (int i = lane; i < B; i += 32) s_touched[i] = 0;
+
+  const int64_t plane = (int64_t)W * H;
+  const float pxa = (float)(bx0 + (lane & 7)), pxb = pxa + 8.f;
+  const float py0 = (float)(by0 + (lane >> 3));
+  float T[PX], SB[PX];
+  int nc[PX];
+  int my_nc = 0;
+#pragma unroll
+  for (int q = 0; q < PX; ++q) {
+    const int px = bx0 + (lane & 7) + 8 * (q & 1), py = by0 + (lane >> 3) + 4 * (q >> 1);
+    float dv[8];
+#pragma unroll
+    for (int c = 0; c < 8; ++c) dv[c] = 0.f;
+    T[q] = 1.f;
+    nc[q] = 0;
+    if (px < W && py < H) {
+      const int64_t pix = (int64_t)py * W + px;
+      T[q] = final_T[pbase + pix];
+      nc[q] = n_contrib[pbase + pix];
+#pragma unroll
+      for (int c = 0; c < NC; ++c)
+        if (c < C) dv[c] = d_out[C * pbase + c * plane + pix];
+    }
+    float sd = 0.f;
+#pragma unroll
+    for (int c = 0; c < NC; ++c) sd += dv[c];
+    SB[q] = bg * sd;
+    s_dout[0][q * 32 + lane] = make_float4(dv[0], dv[1], dv[2], dv[3]);
+    s_dout[1][q * 32 + lane] = make_float4(dv[4], dv[5], dv[6], dv[7]);
+    my_nc = max(my_nc, nc[q]);
+  }
+  int warp_nc = my_nc;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) warp_nc = max(warp_nc, __shfl_xor_sync(0xffffffffu, warp_nc, o));
+  const int2 rg = ranges[tile];
+  const int64_t start = rg.x;
+  const int list_len = max(0, rg.y - rg.x);
+  if (warp_nc > list_len && lane == 0) set_info(info, PGB_ERR_OVERFLOW);
+  const int max_nc = min(warp_nc, list_len);
+  const int nb = (max_nc + B - 1) / B;
+  auto lo_of = [&](int b) { return max(0, max_nc - (b + 1) * B); };
+  auto hi_of = [&](int b) { return max_nc - b * B; };
+  __syncwarp();
+
+  if (nb > 0)
+    stage_batch<RF, 32, B>(records, ids, start + lo_of(0), start + hi_of(0), n, smem, info);
+  for (int b = 0; b < nb; ++b) {
+    const int buf = b & 1;
+    const int lo = lo_of(b), hi = hi_of(b);
+    if (b + 1 < nb) {
+      stage_batch<RF, 32, B>(records, ids, start + lo_of(b + 1), start + hi_of(b + 1), n,
+                             smem + (buf ^ 1) * B * RF, info);
+      cp_async_wait<1>();
+    } else {
+      cp_async_wait<0>();
+    }
+    __syncwarp();  // every lane's copies of batch b have landed
+    const float* st = smem + buf * B * RF;
+    const int nl = warp_cull<16, 16, B>(st, RF, hi - lo, (float)bx0, (float)by0, s_list);
+    for (int t = nl - 1; t >= 0; --t) {
+      const int slot = s_list[t];
+      const int j = lo + slot;
+      const float* rec = st + slot * RF;
+      const float4 r0 = *reinterpret_cast<const float4*>(rec);      // u, v, A, B
+      const float4 r1 = *reinterpret_cast<const float4*>(rec + 4);  // C, o, tau, thr
+      const float dxh[2] = {__fsub_rn(r0.x, pxa), __fsub_rn(r0.x, pxb)};
+      const SplatX sxh[2] = {splat_x(r0.z, r0.w, dxh[0]), splat_x(r0.z, r0.w, dxh[1])};
+      float p2q[PX];
+      bool okq[PX];
+      bool contrib = false;
+#pragma unroll
+      for (int q = 0; q < PX; ++q) {
+        const float dy = __fsub_rn(r0.y, py0 + (float)(4 * (q >> 1)));
+        p2q[q] = splat_power2(sxh[q & 1], r1.x, dy);
+        okq[q] = j < nc[q] && !(p2q[q] > 0.f || p2q[q] < r1.w);  // the forward's skip test
+        contrib |= okq[q];
+      }
+      if (!__any_sync(0xffffffffu, contrib)) continue;
+      float2 v[8];
+#pragma unroll
+      for (int k = 0; k < 8; ++k) v[k] = f2(0.f, 0.f);
+      const float2* fp = reinterpret_cast<const float2*>(rec + kRecFeat);
+      float2 fr[NP];
+#pragma unroll
+      for (int k = 0; k < NP; ++k) fr[k] = fp[k];
+#pragma unroll
+      for (int q = 0; q < PX; ++q) {
+        if (!__any_sync(0xffffffffu, okq[q])) continue;  // warp-uniform
+        const float dx = dxh[q & 1];
+        const float dy = __fsub_rn(r0.y, py0 + (float)(4 * (q >> 1)));
+        const SplatX& sx = sxh[q & 1];
+        const float g0 = __fmaf_rn(r0.w, dy, sx.Adx), g1 = __fmaf_rn(r1.x, dy, sx.Bdx);
+        const float G = ex2_approx(p2q[q]);
+        const float araw = __fmul_rn(r1.y, G);
+        const float alpha = okq[q] ? fminf(0.99f, araw) : 0.f;
+        const float om = __fsub_rn(1.0f, alpha);
+        T[q] = okq[q] ? __fdividef(T[q], om) : T[q];
+        const float4 dlo = s_dout[0][q * 32 + lane];
+        const float4 dhi = s_dout[1][q * 32 + lane];
+        const float2 dp[4] = {f2(dlo.x, dlo.y), f2(dlo.z, dlo.w), f2(dhi.x, dhi.y),
+                              f2(dhi.z, dhi.w)};
+        float2 F2 = __fmul2_rn(dp[0], fr[0]);
+#pragma unroll
+        for (int k = 1; k < NP; ++k) F2 = __ffma2_rn(dp[k], fr[k], F2);
+        const float F = F2.x + F2.y;
+        const float wT = alpha * T[q];
+        const float2 wT2 = f2(wT, wT);
+#pragma unroll
+        for (int k = 0; k < NP; ++k) v[3 + k] = __ffma2_rn(wT2, dp[k], v[3 + k]);
+        const float dalpha = (F - SB[q]) * T[q];
+        SB[q] = fmaf(alpha, F, om * SB[q]);
+        const bool m = okq[q] && araw < 0.99f;
+        const float dpow = m ? alpha * dalpha : 0.f;
+        const float Gm = m ? G : 0.f;
+        const float tx = dpow * dx;
+        v[0] = __ffma2_rn(f2(g0, g1), f2(dpow, dpow), v[0]);        // sum g0 dp, g1 dp
+        v[1] = __ffma2_rn(f2(tx, tx), f2(dx, dy), v[1]);            // dx^2 dp, dx dy dp
+        v[2] = __ffma2_rn(f2(dpow * dy, Gm), f2(dy, dalpha), v[2]);  // dy^2 dp, G dalpha
+      }
+      float vf[16];
+#pragma unroll
+      for (int k = 0; k < 8; ++k) {
+        vf[2 * k] = v[k].x;
+        vf[2 * k + 1] = v[k].y;
+      }
+      const float sum = warp_reduce_scatter<16>(vf);
+      if ((lane & 1) == 0 && (lane >> 1) < 6 + NC) gacc[slot * GR + (lane >> 1)] += sum;
+      if (lane == 0) s_touched[slot] = 1;
+    }
+    __syncwarp();
+    for (int t = lane; t < hi - lo; t += 32) {
+      if (!s_touched[t]) continue;
+      const int32_t g = ids[start + lo + t];
+      if (g < 0 || (int64_t)g >= n) {
+        set_info(info, PGB_ERR_OVERFLOW);
+        continue;
+      }
+      float4* dst = reinterpret_cast<float4*>(grad_records + (int64_t)g * GR);
+      float4* srcv = reinterpret_cast<float4*>(gacc + t * GR);
+#pragma unroll
+      for (int q = 0; q < (6 + NC + 3) / 4; ++q) {
+        atomicAdd(dst + q, srcv[q]);
+        srcv[q] = make_float4(0.f, 0.f, 0.f, 0.f);
+      }
+      s_touched[t] = 0;
+    }
+    __syncwarp();  // the stage of batch b is refilled by the next iteration's copies
+  }
+}
+
 // ---------------------------------------------------------------- unpack
 template <int RF>
 __global__ void unpack_kernel(const float* __restrict__ g, int64_t n, int C,
@@ -1452,6 +1641,24 @@ static int launch_bwd_solo(const float* records, const int32_t* ids, const int2*
   return launch_status();
 }
 
+template <int NC, int B, int MINB>
+static int launch_bwd_tile(const float* records, const int32_t* ids, const int2* ranges,
+                           int64_t n, float bg, const ViewTable& vt, int tiles, int C,
+                           const float* fT, const int32_t* ncon, const float* dout, float* grec,
+                           int64_t* info, cudaStream_t s) {
+  constexpr int RF = rec_floats(NC);
+  constexpr int GR = grad_floats(NC);
+  const size_t smem = (2 * RF + GR) * B * sizeof(float);
+  auto kern = blend_bwd_tile_kernel<NC, RF, GR, B, MINB>;
+  if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+          cudaSuccess ||
+      cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout,
+                           cudaSharedmemCarveoutMaxShared) != cudaSuccess)
+    return PGB_ERR_CUDA;
+  kern<<<tiles, 32, smem, s>>>(records, ids, ranges, n, bg, vt, C, fT, ncon, dout, grec, info);
+  return launch_status();
+}
+
 template <int NC, int B, int PX, int TH = 16>
 static int launch_bwd_b(const float* records, const int32_t* ids, const int2* ranges, int64_t n,
                         float bg, const ViewTable& vt, int tiles, int C, const float* fT,
@@ -1501,7 +1708,8 @@ static int launch_bwd_nc(const float* records, const int32_t* ids, const int2* r
         case kBwdSolo + 64: return PGB_BWD_T(64, 4, 32);
         case kBwdSolo + 32:
         case kBwdSolo + 1024 + 32:
-        case kBwdSolo + 2048 + 32: return PGB_BWD_T(32, 4, 32);
+        case kBwdSolo + 2048 + 32:
+        case kBwdTile + 32: return PGB_BWD_T(32, 4, 32);
         case kBwdPx4 + 128: return PGB_BWD_T(128, 4, 32);
         default: return PGB_ERR_INVALID;
       }
@@ -1545,6 +1753,10 @@ static int launch_bwd_nc(const float* records, const int32_t* ids, const int2* r
         case kBwdSolo + 2048 + 32:
           return launch_bwd_solo<NC, 32, 24>(records, ids, ranges, n, bg, vt, tiles, C, fT, ncon,
                                               dout, grec, info, s);
+        case kBwdTile + 32:
+          return launch_bwd_tile<NC, 32, 16>(records, ids, ranges, n, bg, vt, tiles, C, fT, ncon,
+                                              dout, grec, info, s);
+
         default: break;
       }
     }
@@ -1559,7 +1771,8 @@ static int launch_bwd_nc(const float* records, const int32_t* ids, const int2* r
       case kBwdSolo + 64: return PGB_BWD(64, 4);
       case kBwdSolo + 32:
       case kBwdSolo + 1024 + 32:
-      case kBwdSolo + 2048 + 32: return PGB_BWD(32, 4);
+      case kBwdSolo + 2048 + 32:
+      case kBwdTile + 32: return PGB_BWD(32, 4);
       case kBwdV2 + 512 + 32:
       case kBwdV2 + 1024 + 32:
       case kBwdV2 + kBwdFlat + 32:
@@ -1957,9 +2170,9 @@ int pgb_blend_batches(int backward, int32_t* out) {
                               kBwdV2 + kBwdFlat + 32, kBwdV2 + kBwdFlat + 64,
                               kBwdV2 + kBwdFlat + 1024 + 32, kBwdV2 + kBwdFlat + 1024 + 64,
                               kBwdSolo + 32, kBwdSolo + 64, kBwdSolo + 1024 + 32,
-                              kBwdSolo + 2048 + 32};
+                              kBwdSolo + 2048 + 32, kBwdTile + 32};
   const int32_t* src = backward ? b : f;
-  const int cnt = backward ? 17 : 4;
+  const int cnt = backward ? 18 : 4;
   if (out)
     for (int i = 0; i < cnt; ++i) out[i] = src[i];
   return cnt;
