@@ -193,8 +193,9 @@ __device__ inline void cp_async_wait() {
 
 // Deterministic sum over rows b < nrows of v[b * stride + col] for NCOL
 // columns, run by one CTA of NCOL * TPC threads: thread j of a column sums
-// rows j, j + TPC, ... in order (in double), then a fixed shared-memory tree
-// adds the TPC partial sums.  Returns the column's total in the column's
+// rows j, j + TPC, ... in order (groups of eight rows pairwise in T, each
+// group's sum added in double), then a fixed shared-memory tree adds the
+// TPC partial sums.  Returns the column's total in the column's
 // thread j == 0 (others: unspecified).  `s` holds NCOL * TPC doubles.
 template <int NCOL, int TPC, typename T>
 __device__ inline double column_sum(const T* __restrict__ v, int nrows, int stride, double* s) {
@@ -208,8 +209,10 @@ __device__ inline double column_sum(const T* __restrict__ v, int nrows, int stri
       T x[8];
 #pragma unroll
       for (int u = 0; u < 8; ++u) x[u] = v[(size_t)(b + u * TPC) * stride + col];
-#pragma unroll
-      for (int u = 0; u < 8; ++u) acc += (double)x[u];
+      // eight rows summed pairwise in T, then one double add: FP64 is a
+      // slow pipe on this part, and the finish runs on one SM
+      const T s01 = x[0] + x[1], s23 = x[2] + x[3], s45 = x[4] + x[5], s67 = x[6] + x[7];
+      acc += (double)((s01 + s23) + (s45 + s67));
     }
     for (; b < nrows; b += TPC) acc += (double)v[(size_t)b * stride + col];
   }

@@ -314,6 +314,7 @@ class _Preprocess(torch.autograd.Function):
         ctx.save_for_backward(xyz, scales, quats, intr, extr, radius)
         ctx.cfg = (W, H, nearest, extent)
         ctx.mark_non_differentiable(radius, tiles)
+        ctx.set_materialize_grads(False)  # no zero tensors for radius / tiles
         return uv, depth, conic, radius, tiles
 
     @staticmethod
@@ -373,6 +374,7 @@ class _PreprocessViews(torch.autograd.Function):
         ctx.save_for_backward(xyz, scales, quats, intrs, extrs, radius)
         ctx.cfg = (tuple(sizes), nearest, extent)
         ctx.mark_non_differentiable(radius, tiles)
+        ctx.set_materialize_grads(False)  # no zero tensors for radius / tiles
         return uv, depth, conic, radius, tiles
 
     @staticmethod

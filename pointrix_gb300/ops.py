@@ -366,6 +366,7 @@ class _EwaProject(torch.autograd.Function):
         ctx.save_for_backward(xyz, cov3d, intr, extr, radius)
         ctx.cfg = (W, H, intr_shape)
         ctx.mark_non_differentiable(radius, tiles)
+        ctx.set_materialize_grads(False)  # no zero tensors for radius / tiles
         return conic, radius, tiles
 
     @staticmethod
@@ -662,10 +663,13 @@ class _AlphaBlending(torch.autograd.Function):
         ctx.save_for_backward(records, ids, tile_range, final_T, ncon)
         ctx.cfg = (n, C, float(bg), W, H, ndc is not None)
         ctx.mark_non_differentiable(final_T, ncon)
+        ctx.set_materialize_grads(False)  # no zero images for final_T / ncon
         return out, final_T, ncon
 
     @staticmethod
     def backward(ctx, d_out, _dT, _dn):
+        if d_out is None:
+            return (None,) * 10
         records, ids, tile_range, final_T, ncon = ctx.saved_tensors
         n, C, bg, W, H, has_ndc = ctx.cfg
         d_uv, d_conic, d_op, d_feat = _blend_backward_raw(records, ids, tile_range, final_T, ncon,
@@ -687,10 +691,13 @@ class _AlphaBlendingPieces(torch.autograd.Function):
         ctx.save_for_backward(records, ids, tile_range, final_T, ncon)
         ctx.cfg = (n, sum(widths), widths, float(bg), W, H, ndc is not None)
         ctx.mark_non_differentiable(final_T, ncon)
+        ctx.set_materialize_grads(False)  # no zero images for final_T / ncon
         return out, final_T, ncon
 
     @staticmethod
     def backward(ctx, d_out, _dT, _dn):
+        if d_out is None:
+            return (None,) * (9 + len(ctx.cfg[2]))
         records, ids, tile_range, final_T, ncon = ctx.saved_tensors
         n, C, widths, bg, W, H, has_ndc = ctx.cfg
         d_uv, d_conic, d_op, d_feat = _blend_backward_raw(records, ids, tile_range, final_T, ncon,
