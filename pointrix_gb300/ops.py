@@ -150,7 +150,11 @@ class _timed:
 # ---------------------------------------------------------------------------
 _status_lock = threading.Lock()
 _dev_status: dict[int, torch.Tensor] = {}
+# Deferred status checks: (event, pinned read-back, what) per call; a caller
+# that never drains (a loop of plain sorts) keeps the list short through the
+# drain that every _PENDING_DRAIN-th deferral runs.
 _pending: list[tuple[torch.cuda.Event, torch.Tensor, str]] = []
+_PENDING_DRAIN = 32
 
 
 def _status_word(device) -> torch.Tensor:
@@ -178,6 +182,9 @@ def _defer_check(word: torch.Tensor, what: str):
     ev.record(torch.cuda.current_stream(word.device))
     with _status_lock:
         _pending.append((ev, host, what))
+        drain = len(_pending) >= _PENDING_DRAIN
+    if drain:
+        _drain_pending(block=False)
 
 
 def _drain_pending(block: bool):
@@ -185,18 +192,20 @@ def _drain_pending(block: bool):
         items = list(_pending)
         _pending.clear()
     keep, err = [], None
-    for ev, host, what in items:
+    for i, (ev, host, what) in enumerate(items):
         if block:
             ev.synchronize()
         elif not ev.query():
-            keep.append((ev, host, what))
-            continue
-        code = int(host.max())
+            # deferred in order: the ones after it are (nearly always) still
+            # pending too -- keep them unqueried
+            keep = items[i:]
+            break
+        code = int(host.numpy().max())   # the pinned words, read in place
         if code and err is None:
             err = (code, what)
     if keep:
         with _status_lock:
-            _pending.extend(keep)
+            _pending[:0] = keep          # older than anything deferred meanwhile
     if err:
         _lib.check(err[0], err[1])
 

@@ -214,19 +214,27 @@ def _batch_b(scene: ResidentScene, reqs, st: dict, pinned=None):
 class PinnedPool:
     """Pinned host image buffers by shape, handed out for results and taken
     back when the client has released its image (page-locking new host
-    memory takes milliseconds, so a server recycles its result buffers)."""
+    memory takes milliseconds, so a server recycles its result buffers).
+    Thread-safe; the servers share one pool per process, so buffers a server
+    (or a warm-up) page-locked serve the next one."""
 
     def __init__(self):
         self.free: dict = {}
+        self._lock = threading.Lock()
 
     def take(self, shape):
-        lst = self.free.get(shape)
-        if lst:
-            return lst.pop()
+        with self._lock:
+            lst = self.free.get(tuple(shape))
+            if lst:
+                return lst.pop()
         return torch.empty(shape, dtype=torch.float32, pin_memory=True)
 
     def give(self, t):
-        self.free.setdefault(tuple(t.shape), []).append(t)
+        with self._lock:
+            self.free.setdefault(tuple(t.shape), []).append(t)
+
+
+_SHARED_PINNED = PinnedPool()
 
 
 @torch.no_grad()
@@ -255,6 +263,23 @@ def batch_k_bytes(k: int, sizes) -> int:
     return k * (16 + 4) + 2 * 3 * k // 4096 * 1024 + T * 8 + sum(W * H for W, H in sizes) * (3 * 4 + 8)
 
 
+# The servers' job streams, one list per device, shared by every server on
+# it: the caching allocator keeps freed device memory per stream, so a
+# server (or a warm-up) that used these streams leaves their pools warm for
+# the next; a fresh stream would allocate anew in the middle of its first
+# burst of requests.
+_JOB_STREAMS: dict = {}
+_JOB_STREAMS_LOCK = threading.Lock()
+
+
+def _job_streams(device: torch.device, slots: int) -> list:
+    with _JOB_STREAMS_LOCK:
+        lst = _JOB_STREAMS.setdefault(device, [])
+        while len(lst) < slots:
+            lst.append(torch.cuda.Stream(device))
+        return lst[:slots]
+
+
 class RenderServer:
     """Continuous-batching server: see the module docstring.
 
@@ -276,7 +301,7 @@ class RenderServer:
                  on_done=None, max_batch: int = 16, reserve: int = 1 << 30, backlog: int = 8):
         self.scenes = scenes
         self.device = _indexed(device)
-        self.streams = [torch.cuda.Stream(self.device) for _ in range(slots)]
+        self.streams = _job_streams(self.device, slots)
         self.free_streams = list(range(slots))
         self.budget = None if memory_budget is None else int(memory_budget)
         self.reserve = int(reserve)
@@ -288,7 +313,7 @@ class RenderServer:
         self.done: list[RenderRequest] = []
         self.batches: list[int] = []        # size of every job started
         self.backlog = max(1, int(backlog))
-        self.pinned = PinnedPool()
+        self.pinned = _SHARED_PINNED
         self.on_done = on_done
         self._closed = False
         self._thread = threading.Thread(target=self._loop, name="pgb-render-server", daemon=True)
@@ -443,7 +468,7 @@ class PlainServer:
         self.inbox: "queue.Queue[RenderRequest | None]" = queue.Queue()
         self.done: list[RenderRequest] = []
         self.on_done = on_done
-        self.pinned = PinnedPool()
+        self.pinned = _SHARED_PINNED
         self._thread = threading.Thread(target=self._loop, name="pgb-plain-server", daemon=True)
         self._error: BaseException | None = None
         self._thread.start()
