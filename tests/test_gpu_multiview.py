@@ -202,3 +202,33 @@ def test_tall_tiles_need_fewer_entries_and_every_variant_agrees():
         for a, b in zip(gr, grads[0]):
             assert float((a - b).norm() / b.norm()) < 1e-5
     ops.check_device_status()
+
+
+def test_every_variant_agrees_on_16x16_views():
+    """Batched views with 16 x 16 tiles take every blend form (the flat,
+    one-warp-per-half and one-warp-per-tile backwards included): images bit
+    for bit, gradients within 1e-5 (float sums in another order)."""
+    from pointrix_gb300 import autotune
+    cams = _cams()
+    leaves = _leaves()
+    with torch.no_grad():
+        ref, _, _ = multiview.render_views(*leaves, cams, bg=0.1, tile_height=16)
+    g = torch.Generator().manual_seed(10)
+    ups = [torch.randn(r.shape, generator=g).cuda() for r in ref]
+    grads = []
+    try:
+        for bf in multiview._blend_batches_h(0, 16):
+            for bb in multiview._blend_batches_h(1, 16):
+                autotune.set_pins(f"fwd={bf},bwd={bb}")
+                lv = [t.detach().clone().requires_grad_(True) for t in leaves]
+                out, _, _ = multiview.render_views(*lv, cams, bg=0.1, tile_height=16)
+                for a, b in zip(out, ref):
+                    assert torch.equal(a, b), (bf, bb)
+                torch.autograd.backward(out, ups)
+                grads.append(((bf, bb), [t.grad for t in lv]))
+    finally:
+        autotune.set_pins("")
+    for codes, gr in grads[1:]:
+        for a, b in zip(gr, grads[0][1]):
+            assert float((a - b).norm() / b.norm()) < 1e-5, codes
+    ops.check_device_status()
