@@ -55,7 +55,13 @@
 namespace pgb {
 
 constexpr int kSortThreads = 256;
-constexpr int kPartKeys = 6144;  // keys per onesweep partition
+constexpr int kPartKeys = 6144;  // keys per onesweep partition (tile passes)
+// The depth passes sort N keys (1M at the training workload): partitions of
+// 512 x 7 keys make 280 of them, one wave at two CTAs per SM, where 6,144-key
+// partitions (163) left half the CTA slots empty and each pass one long
+// partition's latency.
+constexpr int kDepthIT = 7;
+constexpr int kDepthPartKeys = 512 * kDepthIT;
 constexpr int kScanItems = 8;
 constexpr int kScanPart = kSortThreads * kScanItems;  // 2048
 // Chunk of the tile-entry sequence whose first owner the scan records; a
@@ -233,9 +239,9 @@ struct OsCfg<9> {
   static constexpr int NT = 512, IT = 12;
 };
 
-template <int RB>
+template <int RB, int ITK = OsCfg<RB>::IT>
 struct Os {
-  static constexpr int NT = OsCfg<RB>::NT, IT = OsCfg<RB>::IT, NW = NT / 32;
+  static constexpr int NT = OsCfg<RB>::NT, IT = ITK, NW = NT / 32;
   static constexpr int PART = NT * IT;
   static constexpr int R = 1 << RB;
   // 8-bit digits: equal digits of a warp found by OR-ing lane bits into a
@@ -244,7 +250,8 @@ struct Os {
   static constexpr bool OR_MATCH = RB == 8;
   static constexpr int HW = (OR_MATCH ? 2 : 1) * NW * R;  // histogram (+ mask) words
   static constexpr size_t SMEM = ((size_t)HW + 3 * (size_t)PART) * sizeof(uint32_t);
-  static_assert(PART == kPartKeys, "one partition size for every digit width");
+  static_assert(ITK != OsCfg<RB>::IT || PART == kPartKeys,
+                "one partition size for every digit width of the tile passes");
   static_assert(NT >= R, "one thread per digit");
 };
 
@@ -424,15 +431,16 @@ __device__ inline void gen_warp(const OwnerView<STAGED>& ov, uint32_t i0, uint32
   }
 }
 
-template <int RB, bool KEYS_OUT, bool RANGES, bool GEN>
-__global__ void __launch_bounds__(Os<RB>::NT, 2) onesweep_kernel(
+template <int RB, bool KEYS_OUT, bool RANGES, bool GEN, int ITK = OsCfg<RB>::IT>
+__global__ void __launch_bounds__(Os<RB, ITK>::NT, 2) onesweep_kernel(
     const uint32_t* __restrict__ keys_in, const uint32_t* __restrict__ vals_in,
     uint32_t* __restrict__ keys_out, uint32_t* __restrict__ vals_out, int64_t cap,
     const int64_t* __restrict__ n_dev, int shift, int live, const uint32_t* __restrict__ pass_hist,
     uint32_t* __restrict__ status, uint32_t* __restrict__ part_counter, int2* __restrict__ range,
     uint32_t T, const uint4* __restrict__ owner, const uint32_t* __restrict__ chunk_first,
     int64_t n_sorted, const PassViews px, int64_t* __restrict__ info) {
-  using P = Os<RB>;
+  using P = Os<RB, ITK>;
+  static_assert(!GEN || ITK == OsCfg<RB>::IT, "generating passes use the tile-pass partitions");
   constexpr int NT = P::NT, IT = P::IT, NW = P::NW, PART = P::PART, R = P::R;
   extern __shared__ __align__(16) uint32_t os_smem[];
   constexpr int HW = P::HW;
@@ -696,14 +704,14 @@ struct GenSource {
 
 // One pass: digit width, whether keys are written, whether ranges are made,
 // whether the keys are generated from owner records (ki / vi unused).
-template <int RB, bool KEYS_OUT, bool RANGES, bool GEN = false>
+template <int RB, bool KEYS_OUT, bool RANGES, bool GEN = false, int ITK = OsCfg<RB>::IT>
 static int launch_onesweep(int parts, cudaStream_t s, const uint32_t* ki, const uint32_t* vi,
                            uint32_t* ko, uint32_t* vo, int64_t cap, const int64_t* n_dev,
                            int shift, const uint32_t* hist, uint32_t* status, uint32_t* counter,
                            int2* range, uint32_t T, int64_t* info, const GenSource& src = {},
                            int live = RB, const PassViews& px = PassViews{}) {
-  using P = Os<RB>;
-  auto kern = onesweep_kernel<RB, KEYS_OUT, RANGES, GEN>;
+  using P = Os<RB, ITK>;
+  auto kern = onesweep_kernel<RB, KEYS_OUT, RANGES, GEN, ITK>;
   // the attribute is set on every call: the call is cheap, allowed while a
   // stream is being captured, and per device
   if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)P::SMEM) !=
@@ -988,7 +996,7 @@ struct ScratchN {
 
 inline ScratchN layout_n(int64_t n) {
   ScratchN L;
-  L.parts = (int)((n + kPartKeys - 1) / kPartKeys);
+  L.parts = (int)((n + kDepthPartKeys - 1) / kDepthPartKeys);
   L.scan_parts = (int)((n + kScanPart - 1) / kScanPart);
   size_t o = 0;
   L.counters = o; o += align256(16 * sizeof(uint32_t));
@@ -1236,21 +1244,21 @@ static int sort_begin_impl(const float* depth, const int32_t* radius, const int3
     if (p == kViewPass) {  // by view (keys: the views the previous pass wrote)
       int live = 1;
       while ((1 << live) < nviews) ++live;
-      rc = launch_onesweep<8, false, false>(L.parts, s, ki, vi, ko, vo, n, nullptr, 0,
+      rc = launch_onesweep<8, false, false, false, kDepthIT>(L.parts, s, ki, vi, ko, vo, n, nullptr, 0,
                                             hist + 256 * p, st, counters + 8, nullptr, 0, info,
                                             GenSource{}, live);
     } else if (p == kDepthPasses - 1) {
       // the last depth pass: for a batch it writes the views as the next
       // pass's keys; for one image only the order is needed
       px.key_from_val = 1;
-      rc = nviews > 0 ? launch_onesweep<8, true, false>(L.parts, s, ki, vi, ko, vo, n, nullptr,
+      rc = nviews > 0 ? launch_onesweep<8, true, false, false, kDepthIT>(L.parts, s, ki, vi, ko, vo, n, nullptr,
                                                         8 * p, hist + 256 * p, st, counters + p,
                                                         nullptr, 0, info, GenSource{}, 8, px)
-                      : launch_onesweep<8, false, false>(L.parts, s, ki, vi, ko, vo, n, nullptr,
+                      : launch_onesweep<8, false, false, false, kDepthIT>(L.parts, s, ki, vi, ko, vo, n, nullptr,
                                                          8 * p, hist + 256 * p, st, counters + p,
                                                          nullptr, 0, info);
     } else {
-      rc = launch_onesweep<8, true, false>(L.parts, s, ki, vi, ko, vo, n, nullptr, 8 * p,
+      rc = launch_onesweep<8, true, false, false, kDepthIT>(L.parts, s, ki, vi, ko, vo, n, nullptr, 8 * p,
                                            hist + 256 * p, st, counters + p, nullptr, 0, info);
     }
     if (rc != PGB_OK) return rc;
