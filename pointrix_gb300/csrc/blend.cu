@@ -1390,15 +1390,17 @@ __global__ void __launch_bounds__(32, MINB) blend_bwd_tile_kernel(
       const SplatX sxh[2] = {splat_x(r0.z, r0.w, dxh[0]), splat_x(r0.z, r0.w, dxh[1])};
       float p2q[PX];
       bool okq[PX];
-      bool contrib = false;
+      uint32_t mine = 0;  // this lane's compositing slots
 #pragma unroll
       for (int q = 0; q < PX; ++q) {
         const float dy = __fsub_rn(r0.y, py0 + (float)(4 * (q >> 1)));
         p2q[q] = splat_power2(sxh[q & 1], r1.x, dy);
         okq[q] = j < nc[q] && !(p2q[q] > 0.f || p2q[q] < r1.w);  // the forward's skip test
-        contrib |= okq[q];
+        mine |= (uint32_t)okq[q] << q;
       }
-      if (!__any_sync(0xffffffffu, contrib)) continue;
+      // the slots some lane composites: one reduction, then uniform branches
+      const uint32_t slots = __reduce_or_sync(0xffffffffu, mine);
+      if (!slots) continue;
       float2 v[8];
 #pragma unroll
       for (int k = 0; k < 8; ++k) v[k] = f2(0.f, 0.f);
@@ -1408,7 +1410,7 @@ __global__ void __launch_bounds__(32, MINB) blend_bwd_tile_kernel(
       for (int k = 0; k < NP; ++k) fr[k] = fp[k];
 #pragma unroll
       for (int q = 0; q < PX; ++q) {
-        if (!__any_sync(0xffffffffu, okq[q])) continue;  // warp-uniform
+        if (!(slots & (1u << q))) continue;  // warp-uniform
         const float dx = dxh[q & 1];
         const float dy = __fsub_rn(r0.y, py0 + (float)(4 * (q >> 1)));
         const SplatX& sx = sxh[q & 1];
