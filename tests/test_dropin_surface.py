@@ -156,3 +156,47 @@ def test_band_grouping_of_tile_rows():
     assert len(group_rows(rows, bands=3)) == 3
     assert group_rows(rows, bands=1) == [(0, 8, 37)]
     assert band_rows(100, 16 * 9, bands=3) == [(0, 3), (3, 6), (6, 9)]
+
+
+class _FakeEvent:
+    def __init__(self, done):
+        self.done = done
+        self.queried = 0
+
+    def query(self):
+        self.queried += 1
+        return self.done
+
+    def synchronize(self):
+        self.done = True
+
+
+def test_deferred_status_checks_drain_in_order_and_raise():
+    """The deferred device-status read-backs: a non-blocking drain checks
+    the completed ones in order and stops at the first still pending
+    (keeping it and everything after it unqueried, ahead of later
+    deferrals); a completed non-zero word raises; a blocking drain waits
+    for all."""
+    import numpy as np
+    import torch
+    from pointrix_gb300 import _lib, ops
+
+    def word(code):
+        return torch.from_numpy(np.array([code, 0, 0], dtype=np.int64))
+
+    saved = list(ops._pending)
+    try:
+        done1, pend, after = _FakeEvent(True), _FakeEvent(False), _FakeEvent(True)
+        ops._pending[:] = [(done1, word(0), "a"), (pend, word(0), "b"), (after, word(0), "c")]
+        ops._drain_pending(block=False)
+        assert [w for _, _, w in ops._pending] == ["b", "c"]
+        assert after.queried == 0            # not queried behind a pending one
+        ops._pending.append((_FakeEvent(True), word(0), "d"))
+        ops._drain_pending(block=True)
+        assert ops._pending == []
+        ops._pending[:] = [(_FakeEvent(True), word(0), "ok"), (_FakeEvent(True), word(6), "bad")]
+        with pytest.raises(_lib.PgbError, match="bad"):
+            ops._drain_pending(block=False)
+        assert ops._pending == []
+    finally:
+        ops._pending[:] = saved
