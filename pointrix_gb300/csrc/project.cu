@@ -655,32 +655,73 @@ __global__ void preprocess_views_fwd_kernel(
   }
 }
 
-__global__ void preprocess_views_bwd_kernel(
+// Views inside the per-Gaussian loop: a thread reads its Gaussian's
+// parameters once, adds the views' gradients in view order in registers and
+// writes each parameter gradient once (the views-outer form re-read and
+// re-wrote them per view: ~5.7 GB of traffic for 16 views of 3M Gaussians
+// against ~1.6 GB).  A view's camera-gradient sums are reduced across the
+// warp right away (reduce-scatter: lane 2c ends with component c) and added
+// by their owner lanes to the warp's own row of a shared table, so the order
+// is fixed; the block then writes, per view, the sum of its warps' rows in
+// warp order -- the partials the finish kernel adds over blocks.
+__device__ __forceinline__ float warp_reduce_scatter16(float (&v)[16]) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int off = 16, m = 8; m >= 1; off >>= 1, m >>= 1) {
+    const bool upper = (lane & off) != 0;
+#pragma unroll
+    for (int i = 0; i < m; ++i) {
+      const float send = upper ? v[i] : v[i + m];
+      const float keep = upper ? v[i + m] : v[i];
+      v[i] = keep + __shfl_xor_sync(0xffffffffu, send, off);
+    }
+  }
+  return v[0] + __shfl_xor_sync(0xffffffffu, v[0], 1);
+}
+
+__global__ void __launch_bounds__(kStreamThreads) preprocess_views_bwd_kernel(
     const float* __restrict__ xyz, const float* __restrict__ scales, const float* __restrict__ q,
     int64_t n, const float* __restrict__ intrs, const float* __restrict__ extrs,
     const ViewSizes vs, float nearest, float extent, const int32_t* __restrict__ radius,
     const float* __restrict__ d_uv, const float* __restrict__ d_depth,
     const float* __restrict__ d_conic, float* __restrict__ d_xyz, float* __restrict__ d_scales,
     float* __restrict__ d_q, float* __restrict__ partials) {
-  for (int v = 0; v < vs.nviews; ++v) {
-    const Cam cm = load_cam(intrs + 4 * v, extrs + 12 * v);
-    const int W = vs.w[v], H = vs.h[v];
-    const int64_t o = (int64_t)v * n;
-    float acc[16];
+  constexpr int NW = kStreamThreads / 32;
+  extern __shared__ float s_cam[];  // [NW][nviews][16]
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int V = vs.nviews;
+  for (int j = threadIdx.x; j < NW * V * 16; j += blockDim.x) s_cam[j] = 0.f;
+  __syncthreads();
+  float* my_cam = s_cam + warp * V * 16;
+  // whole warps iterate together (the reduction needs every lane)
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t base = (int64_t)blockIdx.x * blockDim.x + warp * 32; base < n; base += stride) {
+    const int64_t i = base + lane;
+    const bool in = i < n;
+    float x = 0.f, y = 0.f, z = 0.f;
+    if (in) {
+      x = xyz[3 * i];
+      y = xyz[3 * i + 1];
+      z = xyz[3 * i + 2];
+    }
+    float gx = 0.f, gy = 0.f, gz = 0.f;
+    float ds[3] = {0.f, 0.f, 0.f};
+    float4 dq = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int v = 0; v < V; ++v) {
+      const Cam cm = load_cam(intrs + 4 * v, extrs + 12 * v);
+      const int W = vs.w[v], H = vs.h[v];
+      const int64_t e = (int64_t)v * n + i;
+      float acc[16];
 #pragma unroll
-    for (int k = 0; k < 16; ++k) acc[k] = 0.f;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
-         i += (int64_t)gridDim.x * blockDim.x) {
-      const int64_t e = o + i;
-      const float x = xyz[3 * i], y = xyz[3 * i + 1], z = xyz[3 * i + 2];
+      for (int k = 0; k < 16; ++k) acc[k] = 0.f;
       float px, py, pz, u, uy;
       cam_point(cm, x, y, z, px, py, pz);
-      float gx = 0.f, gy = 0.f, gz = 0.f;
-      float ds[3] = {0.f, 0.f, 0.f};
-      float4 dq = make_float4(0.f, 0.f, 0.f, 0.f);
-      if (project_visible(cm, px, py, pz, W, H, nearest, extent, u, uy)) {
+      float vx = 0.f, vy = 0.f, vz = 0.f;
+      float vds[3] = {0.f, 0.f, 0.f};
+      float4 vdq = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (in && project_visible(cm, px, py, pz, W, H, nearest, extent, u, uy)) {
         project_bwd_one(cm, x, y, z, px, py, pz, reinterpret_cast<const float2*>(d_uv)[e],
-                        d_depth[e], gx, gy, gz, acc);
+                        d_depth[e], vx, vy, vz, acc);
         if (radius[e] > 0) {
           float s6[6];
           cov3d_one(scales, q, i, s6);
@@ -688,22 +729,24 @@ __global__ void preprocess_views_bwd_kernel(
           float dS[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
           ewa_bwd_one(cm, W, H, x, y, z, s6, d_conic[3 * e], d_conic[3 * e + 1],
                       d_conic[3 * e + 2], ex, ey, ez, dS, acc);
-          gx = gx + ex;
-          gy = gy + ey;
-          gz = gz + ez;
-          cov3d_grad_one(scales, q, i, dS, ds, dq);
+          vx = vx + ex;
+          vy = vy + ey;
+          vz = vz + ez;
+          cov3d_grad_one(scales, q, i, dS, vds, vdq);
         }
       }
-      if (v > 0) {  // this thread wrote Gaussian i's sums of the earlier views
-        gx = d_xyz[3 * i] + gx;
-        gy = d_xyz[3 * i + 1] + gy;
-        gz = d_xyz[3 * i + 2] + gz;
-        ds[0] = d_scales[3 * i] + ds[0];
-        ds[1] = d_scales[3 * i + 1] + ds[1];
-        ds[2] = d_scales[3 * i + 2] + ds[2];
-        const float4 p = reinterpret_cast<const float4*>(d_q)[i];
-        dq = make_float4(p.x + dq.x, p.y + dq.y, p.z + dq.z, p.w + dq.w);
-      }
+      // the sums over views, in view order (as the views-outer form added them)
+      gx = gx + vx;
+      gy = gy + vy;
+      gz = gz + vz;
+      ds[0] = ds[0] + vds[0];
+      ds[1] = ds[1] + vds[1];
+      ds[2] = ds[2] + vds[2];
+      dq = make_float4(dq.x + vdq.x, dq.y + vdq.y, dq.z + vdq.z, dq.w + vdq.w);
+      const float sum = warp_reduce_scatter16(acc);
+      if ((lane & 1) == 0) my_cam[v * 16 + (lane >> 1)] += sum;
+    }
+    if (in) {
       d_xyz[3 * i] = gx;
       d_xyz[3 * i + 1] = gy;
       d_xyz[3 * i + 2] = gz;
@@ -712,8 +755,12 @@ __global__ void preprocess_views_bwd_kernel(
       d_scales[3 * i + 2] = ds[2];
       reinterpret_cast<float4*>(d_q)[i] = dq;
     }
-    block_write_partials(acc, partials + (size_t)v * gridDim.x * 16);
-    __syncthreads();  // the partials' shared buffer is reused by the next view
+  }
+  __syncthreads();
+  for (int j = threadIdx.x; j < V * 16; j += blockDim.x) {
+    float t = 0.f;
+    for (int w = 0; w < NW; ++w) t += s_cam[w * V * 16 + j];
+    partials[((size_t)(j >> 4) * gridDim.x + blockIdx.x) * 16 + (j & 15)] = t;
   }
 }
 
@@ -920,7 +967,8 @@ int pgb_preprocess_views_backward(const float* xyz, const float* scales, const f
   cudaStream_t s = as_stream(stream);
   const int grid = stream_grid(n);
   float* partials = static_cast<float*>(scratch);
-  preprocess_views_bwd_kernel<<<grid, kStreamThreads, 0, s>>>(
+  const int smem = (kStreamThreads / 32) * nviews * 16 * (int)sizeof(float);
+  preprocess_views_bwd_kernel<<<grid, kStreamThreads, smem, s>>>(
       xyz, scales, uquats, n, intrs, extrs, vs, nearest, extent, radius, d_uv, d_depth, d_conic,
       d_xyz, d_scales, d_uquats, partials);
   cam_grad_views_finish_kernel<<<nviews, 16 * kCamTPC, 0, s>>>(partials, grid, d_intrs, d_extrs);

@@ -56,12 +56,16 @@ namespace pgb {
 
 constexpr int kSortThreads = 256;
 constexpr int kPartKeys = 6144;  // keys per onesweep partition (tile passes)
-// The depth passes sort N keys (1M at the training workload): partitions of
-// 512 x 7 keys make 280 of them, one wave at two CTAs per SM, where 6,144-key
-// partitions (163) left half the CTA slots empty and each pass one long
-// partition's latency.
+// The depth passes sort N keys.  When 6,144-key partitions would not fill
+// one wave of two CTAs per SM (N below ~1.9M; 163 partitions at the 1M
+// training workload, half the CTA slots empty and each pass one long
+// partition's latency), they use partitions of 512 x 7 keys (280 at 1M);
+// larger N keep the large partitions (fewer look-backs: at 48M keys the
+// small ones cost 14 % more).
 constexpr int kDepthIT = 7;
 constexpr int kDepthPartKeys = 512 * kDepthIT;
+inline bool small_depth_parts(int64_t n) { return n <= (int64_t)2 * kNumSMs * kPartKeys; }
+inline int depth_part_keys(int64_t n) { return small_depth_parts(n) ? kDepthPartKeys : kPartKeys; }
 constexpr int kScanItems = 8;
 constexpr int kScanPart = kSortThreads * kScanItems;  // 2048
 // Chunk of the tile-entry sequence whose first owner the scan records; a
@@ -996,7 +1000,7 @@ struct ScratchN {
 
 inline ScratchN layout_n(int64_t n) {
   ScratchN L;
-  L.parts = (int)((n + kDepthPartKeys - 1) / kDepthPartKeys);
+  L.parts = (int)((n + depth_part_keys(n) - 1) / depth_part_keys(n));
   L.scan_parts = (int)((n + kScanPart - 1) / kScanPart);
   size_t o = 0;
   L.counters = o; o += align256(16 * sizeof(uint32_t));
@@ -1204,6 +1208,47 @@ int pgb_sort_scratch_bytes(int64_t n, int64_t k, int width, int height, size_t* 
 
 }  // extern "C"
 
+// The depth passes (and the view pass of a batch) with ITK keys per thread.
+template <int ITK>
+static int depth_passes(const ScratchN& L, cudaStream_t s, uint32_t* k0, uint32_t* v0,
+                        uint32_t* k1, uint32_t* v1, int64_t n, int nviews, uint32_t* hist,
+                        uint32_t* status, uint32_t* counters, int64_t* info, PassViews px) {
+  const int passes = kDepthPasses + (nviews > 0 ? 1 : 0);
+  for (int p = 0; p < passes; ++p) {
+    const uint32_t* ki = (p & 1) ? k1 : k0;
+    const uint32_t* vi = (p & 1) ? v1 : v0;
+    uint32_t* ko = (p & 1) ? k0 : k1;
+    uint32_t* vo = (p & 1) ? v0 : v1;
+    uint32_t* st = status + (size_t)p * L.parts * 256;
+    int rc;
+    if (p == kViewPass) {  // by view (keys: the views the previous pass wrote)
+      int live = 1;
+      while ((1 << live) < nviews) ++live;
+      rc = launch_onesweep<8, false, false, false, ITK>(L.parts, s, ki, vi, ko, vo, n, nullptr, 0,
+                                                        hist + 256 * p, st, counters + 8, nullptr,
+                                                        0, info, GenSource{}, live);
+    } else if (p == kDepthPasses - 1) {
+      // the last depth pass: for a batch it writes the views as the next
+      // pass's keys; for one image only the order is needed
+      px.key_from_val = 1;
+      rc = nviews > 0
+               ? launch_onesweep<8, true, false, false, ITK>(L.parts, s, ki, vi, ko, vo, n,
+                                                             nullptr, 8 * p, hist + 256 * p, st,
+                                                             counters + p, nullptr, 0, info,
+                                                             GenSource{}, 8, px)
+               : launch_onesweep<8, false, false, false, ITK>(L.parts, s, ki, vi, ko, vo, n,
+                                                              nullptr, 8 * p, hist + 256 * p, st,
+                                                              counters + p, nullptr, 0, info);
+    } else {
+      rc = launch_onesweep<8, true, false, false, ITK>(L.parts, s, ki, vi, ko, vo, n, nullptr,
+                                                       8 * p, hist + 256 * p, st, counters + p,
+                                                       nullptr, 0, info);
+    }
+    if (rc != PGB_OK) return rc;
+  }
+  return PGB_OK;
+}
+
 // Phase one.  nviews == 0: one image, the depth order ends in v0.  A batch
 // (nviews views of n_per_view elements): the fourth depth pass writes the
 // views of its values as keys and a fifth pass sorts by view, so the order
@@ -1233,36 +1278,12 @@ static int sort_begin_impl(const float* depth, const int32_t* radius, const int3
       info);
   PassViews px{};
   if (nviews > 0) px.vdiv = fast_div((uint32_t)n_per_view);
-  const int passes = kDepthPasses + (nviews > 0 ? 1 : 0);
-  for (int p = 0; p < passes; ++p) {
-    const uint32_t* ki = (p & 1) ? k1 : k0;
-    const uint32_t* vi = (p & 1) ? v1 : v0;
-    uint32_t* ko = (p & 1) ? k0 : k1;
-    uint32_t* vo = (p & 1) ? v0 : v1;
-    uint32_t* st = status + (size_t)p * L.parts * 256;
-    int rc;
-    if (p == kViewPass) {  // by view (keys: the views the previous pass wrote)
-      int live = 1;
-      while ((1 << live) < nviews) ++live;
-      rc = launch_onesweep<8, false, false, false, kDepthIT>(L.parts, s, ki, vi, ko, vo, n, nullptr, 0,
-                                            hist + 256 * p, st, counters + 8, nullptr, 0, info,
-                                            GenSource{}, live);
-    } else if (p == kDepthPasses - 1) {
-      // the last depth pass: for a batch it writes the views as the next
-      // pass's keys; for one image only the order is needed
-      px.key_from_val = 1;
-      rc = nviews > 0 ? launch_onesweep<8, true, false, false, kDepthIT>(L.parts, s, ki, vi, ko, vo, n, nullptr,
-                                                        8 * p, hist + 256 * p, st, counters + p,
-                                                        nullptr, 0, info, GenSource{}, 8, px)
-                      : launch_onesweep<8, false, false, false, kDepthIT>(L.parts, s, ki, vi, ko, vo, n, nullptr,
-                                                         8 * p, hist + 256 * p, st, counters + p,
-                                                         nullptr, 0, info);
-    } else {
-      rc = launch_onesweep<8, true, false, false, kDepthIT>(L.parts, s, ki, vi, ko, vo, n, nullptr, 8 * p,
-                                           hist + 256 * p, st, counters + p, nullptr, 0, info);
-    }
-    if (rc != PGB_OK) return rc;
-  }
+  const int rc = small_depth_parts(n)
+                     ? depth_passes<kDepthIT>(L, s, k0, v0, k1, v1, n, nviews, hist, status,
+                                              counters, info, px)
+                     : depth_passes<OsCfg<8>::IT>(L, s, k0, v0, k1, v1, n, nviews, hist, status,
+                                                  counters, info, px);
+  if (rc != PGB_OK) return rc;
   return launch_status();
 }
 
