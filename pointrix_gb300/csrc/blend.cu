@@ -1295,29 +1295,41 @@ __global__ void __launch_bounds__(32, MINB) blend_bwd_solo_kernel(
 // (a lane that skips gets alpha = 0 and keeps T and SB exactly).  No CTA
 // barrier (one warp per CTA); per-splat sums in shared memory with one
 // owner lane per component, flushed with 16-byte vector atomics.
-template <int NC, int RF, int GR, int B, int MINB>
+template <int NC, int RF, int GR, int B, int MINB, int TH = 16>
 __global__ void __launch_bounds__(32, MINB) blend_bwd_tile_kernel(
     const float* __restrict__ records, const int32_t* __restrict__ ids,
     const int2* __restrict__ ranges, int64_t n, float bg, const ViewTable vt, int C,
     const float* __restrict__ final_T, const int32_t* __restrict__ n_contrib,
     const float* __restrict__ d_out, float* __restrict__ grad_records,
-    int64_t* __restrict__ info) {
+    int64_t* __restrict__ info, const int32_t* __restrict__ radius) {
   static_assert(GR == 16, "one owner lane per component of a 16-float gradient record");
   static_assert(NC <= 8, "the d_out planes hold eight channels");
   constexpr int PX = 8;
+  // 16 x 32 tiles (a batch of views): one warp per 16 x 16 half (CTA
+  // 2t + h), the tile's list filtered to the half's msplat list
+  constexpr bool F16 = TH != kTile;
   constexpr int NP = (NC + 1) / 2;
   extern __shared__ __align__(128) float smem[];
   __shared__ uint8_t s_touched[B];
   __shared__ uint8_t s_list[B];
   __shared__ __align__(16) float4 s_dout[2][PX * 32];  // [plane][q * 32 + lane]
+  __shared__ int s_rad[F16 ? 2 : 1][F16 ? B : 1];
   float* gacc = smem + 2 * B * RF;                     // [B][GR]
 
-  const int tile = blockIdx.x;
+  const int tile = F16 ? blockIdx.x >> 1 : blockIdx.x;
   int W, H, gx, ltile;
   int64_t pbase;
   tile_view(vt, tile, W, H, gx, ltile, pbase);
   const int lane = threadIdx.x;
-  const int bx0 = (ltile % gx) * kTile, by0 = (ltile / gx) * kTile;
+  const int bx0 = (ltile % gx) * kTile;
+  const int by0 = (ltile / gx) * TH + (F16 ? kTile * (blockIdx.x & 1) : 0);
+  List16 f16{};
+  if constexpr (F16) {
+    f16.tx = bx0 / kTile;
+    f16.ty = by0 / kTile;
+    f16.gx = grid_x(W);
+    f16.gy = grid_y(H);
+  }
 
   for (int i = lane; i < B * GR; i += 32) gacc[i] = 0.f;
   for (int i = lane; i < B; i += 32) s_touched[i] = 0;
@@ -1365,21 +1377,28 @@ __global__ void __launch_bounds__(32, MINB) blend_bwd_tile_kernel(
   auto hi_of = [&](int b) { return max_nc - b * B; };
   __syncwarp();
 
-  if (nb > 0)
+  if (nb > 0) {
     stage_batch<RF, 32, B>(records, ids, start + lo_of(0), start + hi_of(0), n, smem, info);
+    if constexpr (F16)
+      stage_radius<32, B>(ids, radius, start + lo_of(0), start + hi_of(0), n, s_rad[0]);
+  }
   for (int b = 0; b < nb; ++b) {
     const int buf = b & 1;
     const int lo = lo_of(b), hi = hi_of(b);
     if (b + 1 < nb) {
       stage_batch<RF, 32, B>(records, ids, start + lo_of(b + 1), start + hi_of(b + 1), n,
                              smem + (buf ^ 1) * B * RF, info);
+      if constexpr (F16)
+        stage_radius<32, B>(ids, radius, start + lo_of(b + 1), start + hi_of(b + 1), n,
+                            s_rad[buf ^ 1]);
       cp_async_wait<1>();
     } else {
       cp_async_wait<0>();
     }
-    __syncwarp();  // every lane's copies of batch b have landed
+    __syncwarp();  // every lane's copies of batch b (and its radii) have landed
     const float* st = smem + buf * B * RF;
-    const int nl = warp_cull<16, 16, B>(st, RF, hi - lo, (float)bx0, (float)by0, s_list);
+    if constexpr (F16) f16.rad = s_rad[buf];
+    const int nl = warp_cull<16, 16, B, F16>(st, RF, hi - lo, (float)bx0, (float)by0, s_list, f16);
     for (int t = nl - 1; t >= 0; --t) {
       const int slot = s_list[t];
       const int j = lo + slot;
@@ -1643,21 +1662,22 @@ static int launch_bwd_solo(const float* records, const int32_t* ids, const int2*
   return launch_status();
 }
 
-template <int NC, int B, int MINB>
+template <int NC, int B, int MINB, int TH = 16>
 static int launch_bwd_tile(const float* records, const int32_t* ids, const int2* ranges,
                            int64_t n, float bg, const ViewTable& vt, int tiles, int C,
                            const float* fT, const int32_t* ncon, const float* dout, float* grec,
-                           int64_t* info, cudaStream_t s) {
+                           int64_t* info, cudaStream_t s, const int32_t* radius = nullptr) {
   constexpr int RF = rec_floats(NC);
   constexpr int GR = grad_floats(NC);
   const size_t smem = (2 * RF + GR) * B * sizeof(float);
-  auto kern = blend_bwd_tile_kernel<NC, RF, GR, B, MINB>;
+  auto kern = blend_bwd_tile_kernel<NC, RF, GR, B, MINB, TH>;
   if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
           cudaSuccess ||
       cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout,
                            cudaSharedmemCarveoutMaxShared) != cudaSuccess)
     return PGB_ERR_CUDA;
-  kern<<<tiles, 32, smem, s>>>(records, ids, ranges, n, bg, vt, C, fT, ncon, dout, grec, info);
+  kern<<<tiles * (TH / kTile), 32, smem, s>>>(records, ids, ranges, n, bg, vt, C, fT, ncon, dout,
+                                               grec, info, radius);
   return launch_status();
 }
 
@@ -1710,8 +1730,12 @@ static int launch_bwd_nc(const float* records, const int32_t* ids, const int2* r
         case kBwdSolo + 64: return PGB_BWD_T(64, 4, 32);
         case kBwdSolo + 32:
         case kBwdSolo + 1024 + 32:
-        case kBwdSolo + 2048 + 32:
-        case kBwdTile + 32: return PGB_BWD_T(32, 4, 32);
+        case kBwdSolo + 2048 + 32: return PGB_BWD_T(32, 4, 32);
+        case kBwdTile + 32:
+          if constexpr (NC <= 8)
+            return launch_bwd_tile<NC, 32, 16, 32>(records, ids, ranges, n, bg, vt, tiles, C, fT,
+                                                   ncon, dout, grec, info, s, radius);
+          return PGB_BWD_T(32, 4, 32);
         case kBwdPx4 + 128: return PGB_BWD_T(128, 4, 32);
         default: return PGB_ERR_INVALID;
       }
