@@ -1604,8 +1604,15 @@ static int launch_fwd_nc(const float* records, const int32_t* ids, const int2* r
         case 64: return PGB_FWD(64, 32);
         case 128: return PGB_FWD(128, 32);
         case 256: return PGB_FWD(256, 32);
-        case kFwdFlat + 64: return PGB_FWD(64, 32);
-        case kFwdFlat + 128: return PGB_FWD(128, 32);
+        case kFwdFlat + 64:
+          return launch_fwd_b<NC, 64, 32, true>(records, ids, ranges, n, bg, vt, tiles, C, out,
+                                                fT, ncon, info, s, radius);
+        case kFwdFlat + 128:
+          return launch_fwd_b<NC, 128, 32, true>(records, ids, ranges, n, bg, vt, tiles, C, out,
+                                                 fT, ncon, info, s, radius);
+        case kFwdFlat + 256:
+          return launch_fwd_b<NC, 256, 32, true>(records, ids, ranges, n, bg, vt, tiles, C, out,
+                                                 fT, ncon, info, s, radius);
         default: return PGB_ERR_INVALID;
       }
     }
@@ -2155,11 +2162,11 @@ int pgb_alpha_blending_backward_views_h(const float* records, int64_t n_per_view
 // pgb_blend_batches for 16 x 16).
 int pgb_blend_batches_h(int backward, int tile_height, int32_t* out) {
   if (tile_height != 32) return pgb_blend_batches(backward, out);
-  static const int32_t f[] = {64, 128, 256};
+  static const int32_t f[] = {64, 128, 256, kFwdFlat + 128, kFwdFlat + 256};
   if (backward) return pgb_blend_batches(backward, out);
   if (out)
-    for (int i = 0; i < 3; ++i) out[i] = f[i];
-  return 3;
+    for (int i = 0; i < 5; ++i) out[i] = f[i];
+  return 5;
 }
 
 // Pair census of a blend (no msplat counterpart): counts[0] += list entries
