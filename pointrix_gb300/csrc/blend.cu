@@ -494,13 +494,14 @@ __global__ void __launch_bounds__(64 * (TH / 8)) blend_fwd_kernel(
               const float alpha = fminf(0.99f, __fmul_rn(r1.y, ex2_approx(p2q[q])));
               const float test_T = __fmul_rn(T[q], __fsub_rn(1.0f, alpha));
               const bool stop = okq[q] && test_T < 1e-4f;
-              const bool comp = okq[q] && !stop;
               done[q] = done[q] || stop;
-              const float wgt = comp ? alpha * T[q] : 0.f;
+              if (okq[q] && !stop) {  // short: predicated, not a divergent branch
+                const float wgt = alpha * T[q];
 #pragma unroll
-              for (int c = 0; c < NC; ++c) acc[q][c] = fmaf(fr[c], wgt, acc[q][c]);
-              T[q] = comp ? test_T : T[q];
-              last[q] = comp ? base + j : last[q];
+                for (int c = 0; c < NC; ++c) acc[q][c] = fmaf(fr[c], wgt, acc[q][c]);
+                T[q] = test_T;
+                last[q] = base + j;
+              }
             }
           }
           bool all = true;
