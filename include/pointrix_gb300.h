@@ -278,16 +278,22 @@ int pgb_alpha_blending_backward_views(const float* records, int64_t n_per_view, 
 
 /* The four blend entry points with the kernel variant chosen by the caller
  * (the run-time autotuner of pointrix_gb300.autotune).  Forward: 64 or 128
- * records per batch.  Backward: 64, 128 or 256 records per batch with two
- * pixels per thread, or 4096 + 32 / 64 / 128 for four pixels per thread
- * (64 threads per tile, 8x16 pixel boxes per warp); 8192 + 64, 8192 + 512 +
- * 32 and 8192 + 1024 + 32 select the second four-pixel form (d_out in shared
- * memory, packed f32x2 accumulation; butterfly or transposed per-splat
- * reduction; at most 85 registers for the last), which up to eight channels
- * use and wider features replace by the first form.  0 = the default (128,
- * two pixels per thread).  Every variant gives the same images, final
- * transmittance and contributor counts; the backward's gradient sums are
- * formed in a variant-dependent order (float atomics).
+ * records per batch, plus 2048 for the compositing step without per-pixel
+ * branches.  Backward: 64, 128 or 256 records per batch with two pixels per
+ * thread, or 4096 + 32 / 64 / 128 for four pixels per thread (64 threads per
+ * tile, 8x16 pixel boxes per warp); 8192 + 64, 8192 + 512 + 32 and 8192 +
+ * 1024 + 32 select the second four-pixel form (d_out in shared memory,
+ * packed f32x2 accumulation; butterfly or transposed per-splat reduction; at
+ * most 85 registers for the last), 8192 + 2048 + 32 / 64 (and + 1024, at
+ * most 102 registers) its replay without per-pixel branches; 16384 + 32 /
+ * 64 (and 16384 + 1024 + 32, 16384 + 2048 + 32 at 102 / 85 registers) one
+ * warp per 8x16 half as its own CTA; 32768 + 32 one warp per 16x16 tile,
+ * eight pixels per lane.  The later forms take up to eight channels; wider
+ * features (and, except the one-warp-per-tile form, 16 x 32 tiles) use the
+ * first form with the same batch.  0 = the default (128, two pixels per
+ * thread).  Every variant gives the same images, final transmittance and
+ * contributor counts; the backward's gradient sums are formed in a
+ * variant-dependent order (float atomics).
  * pgb_blend_batches(backward, out) lists the compiled variants (returns
  * their count, writes them to out if not NULL). */
 int pgb_alpha_blending_forward_with_batch(const float* uv, const float* conic,
@@ -334,7 +340,8 @@ int pgb_blend_batches(int backward, int32_t* out);
  * pgb_alpha_blending_forward/backward_views_h: the views' blend for those
  * lists; radius [V*N] is required for tile_height 32 (RGB, RGB + depth and
  * RGB + depth + normal channel counts).  pgb_blend_batches_h lists the
- * forward batches of 16 x tile_height tiles (32: 64, 128, 256).
+ * forward batches of 16 x tile_height tiles (32: 64, 128, 256, and 2048 +
+ * 128 / 256 without per-pixel branches).
  * tile_height is 16 or 32.
  * ------------------------------------------------------------------- */
 int pgb_tile_counts_views(const float* uv, const int32_t* radius, int64_t n_per_view,
