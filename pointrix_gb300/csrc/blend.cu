@@ -298,11 +298,15 @@ __global__ void pack_kernel(const float* __restrict__ uv, const float* __restric
 // magnitude over the box, far above the ~2e-7 that evaluation can lose).
 template <int BW, int BH>
 __device__ __forceinline__ bool splat_may_touch_box(const float* rec, float x0, float y0) {
-  const float tau = rec[6];
+  // two 16-byte loads (fewer shared-memory wavefronts than six scalar ones
+  // at the record stride)
+  const float4 h0 = *reinterpret_cast<const float4*>(rec);      // u, v, A, B
+  const float4 h1 = *reinterpret_cast<const float4*>(rec + 4);  // C, o, tau, thr
+  const float tau = h1.z;
   if (!(tau < 3.0e38f)) return true;
   // the record's conic is scaled by kConicScale
-  const float u = rec[0], v = rec[1], a = rec[2] * kInvConicScale, b = rec[3] * kInvConicScale,
-              c = rec[4] * kInvConicScale;
+  const float u = h0.x, v = h0.y, a = h0.z * kInvConicScale, b = h0.w * kInvConicScale,
+              c = h1.x * kInvConicScale;
   const float dx0 = u - (x0 + (float)(BW - 1)), dx1 = u - x0;
   const float dy0 = v - (y0 + (float)(BH - 1)), dy1 = v - y0;
   if (dx0 <= 0.f && dx1 >= 0.f && dy0 <= 0.f && dy1 >= 0.f) return tau >= 0.f;
