@@ -178,8 +178,8 @@ int pgb_sort_gaussian_finish_capacity(const float* uv, const int32_t* radius,
  * PGB_ERR_OVERFLOW with *k_out (host, may be NULL) set to the K needed.
  * Synchronous: returns when the results are complete on `stream`; a
  * device-side fault comes back as the return value.  The first call on a
- * device looks up the array's device address (with that device current);
- * make that first call before any stream capture.  Under CUDA's lazy module
+ * device looks up the array's device address (with that device current).
+ * Under CUDA's lazy module
  * loading (the default since CUDA 12.2) that first call is also when the
  * library's device code, and with it the array, is set up on the device, so
  * it can fail with PGB_ERR_CUDA when device memory is short: make one warm-up

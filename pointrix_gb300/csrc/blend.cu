@@ -184,6 +184,31 @@ __device__ inline void stage_batch(const float* __restrict__ records,
   cp_async_commit();
 }
 
+// stage_batch for one warp and 32 records: lane l stages slot l and returns
+// its splat id (-1 past the list or for an id out of range).
+template <int RF>
+__device__ inline int32_t stage_batch_id(const float* __restrict__ records,
+                                         const int32_t* __restrict__ ids, int64_t first,
+                                         int64_t last, int64_t n, float* stage, int64_t* info) {
+  const int slot = threadIdx.x & 31;
+  const int64_t e = first + slot;
+  int32_t g = -1;
+  if (e < last) {
+    g = ids[e];
+    if (g < 0 || (int64_t)g >= n) {
+      set_info(info, PGB_ERR_OVERFLOW);
+      g = -1;
+    } else {
+      const float* src = records + (int64_t)g * RF;
+      float* dst = stage + slot * RF;
+#pragma unroll
+      for (int q = 0; q < RF / 4; ++q) cp_async16(dst + 4 * q, src + 4 * q);
+    }
+  }
+  cp_async_commit();
+  return g;
+}
+
 // The radii of one batch's splats (16 x 32 tiles only), plain loads into
 // s_rad[slot]; read after the barrier that publishes the batch.
 template <int NT, int B>
@@ -1298,8 +1323,10 @@ __global__ void __launch_bounds__(32, MINB) blend_bwd_solo_kernel(
 // no lane composites the splat is skipped by a warp-uniform branch, and a
 // slot where some lane does runs its replay step without per-pixel branches
 // (a lane that skips gets alpha = 0 and keeps T and SB exactly).  No CTA
-// barrier (one warp per CTA); per-splat sums in shared memory with one
-// owner lane per component, flushed with 16-byte vector atomics.
+// barrier (one warp per CTA); each splat's reduced sums are added to its
+// gradient record at once by their owner lanes (one warp-wide atomic, no
+// shared gradient table: 12.4 KB of shared memory per CTA, so 16 CTAs per
+// SM at 121 registers).
 template <int NC, int RF, int GR, int B, int MINB, int TH = 16>
 __global__ void __launch_bounds__(32, MINB) blend_bwd_tile_kernel(
     const float* __restrict__ records, const int32_t* __restrict__ ids,
@@ -1309,17 +1336,16 @@ __global__ void __launch_bounds__(32, MINB) blend_bwd_tile_kernel(
     int64_t* __restrict__ info, const int32_t* __restrict__ radius) {
   static_assert(GR == 16, "one owner lane per component of a 16-float gradient record");
   static_assert(NC <= 8, "the d_out planes hold eight channels");
+  static_assert(B == 32, "one staged splat id per lane");
   constexpr int PX = 8;
   // 16 x 32 tiles (a batch of views): one warp per 16 x 16 half (CTA
   // 2t + h), the tile's list filtered to the half's msplat list
   constexpr bool F16 = TH != kTile;
   constexpr int NP = (NC + 1) / 2;
   extern __shared__ __align__(128) float smem[];
-  __shared__ uint8_t s_touched[B];
   __shared__ uint8_t s_list[B];
   __shared__ __align__(16) float4 s_dout[2][PX * 32];  // [plane][q * 32 + lane]
   __shared__ int s_rad[F16 ? 2 : 1][F16 ? B : 1];
-  float* gacc = smem + 2 * B * RF;                     // [B][GR]
 
   const int tile = F16 ? blockIdx.x >> 1 : blockIdx.x;
   int W, H, gx, ltile;
@@ -1336,8 +1362,6 @@ __global__ void __launch_bounds__(32, MINB) blend_bwd_tile_kernel(
     f16.gy = grid_y(H);
   }
 
-  for (int i = lane; i < B * GR; i += 32) gacc[i] = 0.f;
-  for (int i = lane; i < B; i += 32) s_touched[i] = 0;
 
   const int64_t plane = (int64_t)W * H;
   const float pxa = (float)(bx0 + (lane & 7)), pxb = pxa + 8.f;
@@ -1382,17 +1406,19 @@ __global__ void __launch_bounds__(32, MINB) blend_bwd_tile_kernel(
   auto hi_of = [&](int b) { return max_nc - b * B; };
   __syncwarp();
 
+  int32_t g_cur = -1, g_nxt = -1;  // the splat id of slot `lane` (current, next batch)
   if (nb > 0) {
-    stage_batch<RF, 32, B>(records, ids, start + lo_of(0), start + hi_of(0), n, smem, info);
+    g_nxt = stage_batch_id<RF>(records, ids, start + lo_of(0), start + hi_of(0), n, smem, info);
     if constexpr (F16)
       stage_radius<32, B>(ids, radius, start + lo_of(0), start + hi_of(0), n, s_rad[0]);
   }
   for (int b = 0; b < nb; ++b) {
     const int buf = b & 1;
     const int lo = lo_of(b), hi = hi_of(b);
+    g_cur = g_nxt;
     if (b + 1 < nb) {
-      stage_batch<RF, 32, B>(records, ids, start + lo_of(b + 1), start + hi_of(b + 1), n,
-                             smem + (buf ^ 1) * B * RF, info);
+      g_nxt = stage_batch_id<RF>(records, ids, start + lo_of(b + 1), start + hi_of(b + 1), n,
+                                 smem + (buf ^ 1) * B * RF, info);
       if constexpr (F16)
         stage_radius<32, B>(ids, radius, start + lo_of(b + 1), start + hi_of(b + 1), n,
                             s_rad[buf ^ 1]);
@@ -1473,25 +1499,11 @@ __global__ void __launch_bounds__(32, MINB) blend_bwd_tile_kernel(
         vf[2 * k + 1] = v[k].y;
       }
       const float sum = warp_reduce_scatter<16>(vf);
-      if ((lane & 1) == 0 && (lane >> 1) < 6 + NC) gacc[slot * GR + (lane >> 1)] += sum;
-      if (lane == 0) s_touched[slot] = 1;
-    }
-    __syncwarp();
-    for (int t = lane; t < hi - lo; t += 32) {
-      if (!s_touched[t]) continue;
-      const int32_t g = ids[start + lo + t];
-      if (g < 0 || (int64_t)g >= n) {
-        set_info(info, PGB_ERR_OVERFLOW);
-        continue;
-      }
-      float4* dst = reinterpret_cast<float4*>(grad_records + (int64_t)g * GR);
-      float4* srcv = reinterpret_cast<float4*>(gacc + t * GR);
-#pragma unroll
-      for (int q = 0; q < (6 + NC + 3) / 4; ++q) {
-        atomicAdd(dst + q, srcv[q]);
-        srcv[q] = make_float4(0.f, 0.f, 0.f, 0.f);
-      }
-      s_touched[t] = 0;
+      // the splat's sums go straight to its gradient record, one warp-wide
+      // reduction: the owner lanes' 6 + NC floats lie in one 64-byte record
+      const int32_t g = __shfl_sync(0xffffffffu, g_cur, slot);
+      if (g >= 0 && (lane & 1) == 0 && (lane >> 1) < 6 + NC)
+        atomicAdd(grad_records + (int64_t)g * GR + (lane >> 1), sum);
     }
     __syncwarp();  // the stage of batch b is refilled by the next iteration's copies
   }
@@ -1681,7 +1693,7 @@ static int launch_bwd_tile(const float* records, const int32_t* ids, const int2*
                            int64_t* info, cudaStream_t s, const int32_t* radius = nullptr) {
   constexpr int RF = rec_floats(NC);
   constexpr int GR = grad_floats(NC);
-  const size_t smem = (2 * RF + GR) * B * sizeof(float);
+  const size_t smem = 2 * RF * B * sizeof(float);
   auto kern = blend_bwd_tile_kernel<NC, RF, GR, B, MINB, TH>;
   if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
           cudaSuccess ||

@@ -108,7 +108,7 @@ def test_l1_l2_loss_matches_torch():
     ref = F.l1_loss(x2, t) + 0.2 * F.mse_loss(x2, t)
     ref.backward()
     loss = fused.l1_l2_loss(x, t, 0.2)
-    assert abs(float(loss) - float(ref)) <= 1e-6 * float(ref)
+    assert abs(float(loss.detach()) - float(ref)) <= 1e-6 * float(ref)
     loss.backward()
     assert float((x.grad - x2.grad).abs().max()) <= 2 ** -23 * float(x2.grad.abs().max())
     # an odd length (scalar tail) and a scaled upstream gradient
