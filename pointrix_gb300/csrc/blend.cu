@@ -451,7 +451,12 @@ __global__ void __launch_bounds__(64 * (TH / 8)) blend_fwd_kernel(
   const int nb = end > start ? (int)((end - start + B - 1) / B) : 0;
 
   const int px = bx0 + (lane & 7);
-  float pyf[kFwdPix], T[kFwdPix], acc[kFwdPix][NC];
+  // colour sums in channel pairs (one fma.rn.f32x2 per pair, each lane a
+  // correctly rounded fmaf); an odd NC's last pair carries the record's pad
+  constexpr int NP = (NC + 1) / 2;
+  static_assert(kRecFeat + 2 * NP <= RF, "channel pairs stay inside the record");
+  float pyf[kFwdPix], T[kFwdPix];
+  float2 acc[kFwdPix][NP];
   int last[kFwdPix];
   bool done[kFwdPix], inside[kFwdPix];
   const float pxf = (float)px;
@@ -464,7 +469,7 @@ __global__ void __launch_bounds__(64 * (TH / 8)) blend_fwd_kernel(
     T[q] = 1.f;
     last[q] = 0;
 #pragma unroll
-    for (int c = 0; c < NC; ++c) acc[q][c] = 0.f;
+    for (int k = 0; k < NP; ++k) acc[q][k] = make_float2(0.f, 0.f);
   }
   bool timed_out = false;
 
@@ -514,10 +519,10 @@ __global__ void __launch_bounds__(64 * (TH / 8)) blend_fwd_kernel(
             any |= okq[q];
           }
           if (any) {
-            const float* f = rec + kRecFeat;
-            float fr[NC];
+            const float2* fp = reinterpret_cast<const float2*>(rec + kRecFeat);
+            float2 fr[NP];
 #pragma unroll
-            for (int c = 0; c < NC; ++c) fr[c] = f[c];
+            for (int k = 0; k < NP; ++k) fr[k] = fp[k];
 #pragma unroll
             for (int q = 0; q < kFwdPix; ++q) {
               const float alpha = fminf(0.99f, __fmul_rn(r1.y, ex2_approx(p2q[q])));
@@ -526,8 +531,9 @@ __global__ void __launch_bounds__(64 * (TH / 8)) blend_fwd_kernel(
               done[q] = done[q] || stop;
               if (okq[q] && !stop) {  // short: predicated, not a divergent branch
                 const float wgt = alpha * T[q];
+                const float2 w2 = make_float2(wgt, wgt);
 #pragma unroll
-                for (int c = 0; c < NC; ++c) acc[q][c] = fmaf(fr[c], wgt, acc[q][c]);
+                for (int k = 0; k < NP; ++k) acc[q][k] = __ffma2_rn(fr[k], w2, acc[q][k]);
                 T[q] = test_T;
                 last[q] = base + j;
               }
@@ -554,9 +560,10 @@ __global__ void __launch_bounds__(64 * (TH / 8)) blend_fwd_kernel(
             continue;
           }
           const float wgt = alpha * T[q];
-          const float* f = rec + kRecFeat;
+          const float2 w2 = make_float2(wgt, wgt);
+          const float2* fp = reinterpret_cast<const float2*>(rec + kRecFeat);
 #pragma unroll
-          for (int c = 0; c < NC; ++c) acc[q][c] = fmaf(f[c], wgt, acc[q][c]);
+          for (int k = 0; k < NP; ++k) acc[q][k] = __ffma2_rn(fp[k], w2, acc[q][k]);
           T[q] = test_T;
           last[q] = base + j;
         }
@@ -585,8 +592,10 @@ __global__ void __launch_bounds__(64 * (TH / 8)) blend_fwd_kernel(
     const int py = by0 + (lane >> 3) + 4 * q;
     const int64_t pix = (int64_t)py * W + px;
 #pragma unroll
-    for (int c = 0; c < NC; ++c)
-      if (c < C) out[C * pbase + c * plane + pix] = acc[q][c] + T[q] * bg;
+    for (int c = 0; c < NC; ++c) {
+      const float a = (c & 1) ? acc[q][c >> 1].y : acc[q][c >> 1].x;
+      if (c < C) out[C * pbase + c * plane + pix] = a + T[q] * bg;
+    }
     final_T[pbase + pix] = T[q];
     n_contrib[pbase + pix] = last[q];
   }
