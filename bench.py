@@ -790,7 +790,9 @@ def hbm_bytes(n, K, T, W, H, params):
         "preprocess_fwd": 72 * n, "preprocess_bwd": 104 * n,
         "sort_begin": n * (12 + 8 + 4 * 16),
         "sort_finish": n * 28 + K * (8 + passes * 16 + 4) + T * 8,
-        "l1_l2_loss_fwd": 8 * 7 * pix, "l1_l2_loss_bwd": 12 * 7 * pix,
+        # the loss forward also writes the gradient for dL = 1, so its
+        # backward (dL is 1 in the step) reads one scalar and returns
+        "l1_l2_loss_fwd": 12 * 7 * pix,
         "adam_step": 28 * params,
     }
 

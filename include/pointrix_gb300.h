@@ -560,6 +560,17 @@ int pgb_l1_l2_loss_forward(const float* x, const float* target, int64_t n, float
                            double* scratch, int64_t scratch_doubles, float* loss, void* stream);
 int pgb_l1_l2_loss_backward(const float* x, const float* target, int64_t n, float w,
                             const float* d_loss, float* d_x, void* stream);
+/* The training step's form: the forward also writes d_x_unit (16-byte
+ * aligned, n floats) = the backward for dL = 1, in the pass that reads x and
+ * t for the loss; pgb_l1_l2_loss_backward_unit then takes that buffer as d_x
+ * and returns at once when d_loss[0] == 1 (no pass over x and t), otherwise
+ * rewrites it exactly as pgb_l1_l2_loss_backward does.  The values are bit
+ * for bit those of pgb_l1_l2_loss_backward either way. */
+int pgb_l1_l2_loss_forward_grad(const float* x, const float* target, int64_t n, float w,
+                                double* scratch, int64_t scratch_doubles, float* loss,
+                                float* d_x_unit, void* stream);
+int pgb_l1_l2_loss_backward_unit(const float* x, const float* target, int64_t n, float w,
+                                 const float* d_loss, float* d_x, void* stream);
 
 /* pgb_preprocess_*: project_point + compute_cov3d + ewa_project as the
  * renderer chains them (pointrix/model/renderer/msplat.py:109-130, visible =

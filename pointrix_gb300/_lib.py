@@ -101,6 +101,8 @@ SIGNATURES.update({
     "pgb_l1_l2_loss_scratch_doubles": [i64],
     "pgb_l1_l2_loss_forward": [vp, vp, i64, f32, vp, i64, vp, vp],
     "pgb_l1_l2_loss_backward": [vp, vp, i64, f32, vp, vp, vp],
+    "pgb_l1_l2_loss_forward_grad": [vp, vp, i64, f32, vp, i64, vp, vp, vp],
+    "pgb_l1_l2_loss_backward_unit": [vp, vp, i64, f32, vp, vp, vp],
     "pgb_densify_accumulate": [vp, i64, vp, f32, f32, vp, vp, vp, vp],
     "pgb_ssim_scratch_doubles": [i32, i32, i32],
     "pgb_preprocess_forward": [vp, vp, vp, i64, vp, vp, i32, i32, f32, f32, vp, vp, vp, vp, vp, vp],

@@ -8,7 +8,10 @@
 // one-block finish (deterministic); the backward is one pass that reads x,
 // t and dL from the device and writes
 //   dx = sign(x - t) * (dL / n) + ((2 / n) * (x - t)) * (w * dL),
-// the same expression torch's l1 and mse backward formulas sum.
+// the same expression torch's l1 and mse backward formulas sum.  A training
+// step's forward can also write dx for dL = 1 in its own pass (the loss is
+// the step's output, so dL is 1 unless scaled); the backward then returns
+// at once when dL is 1, and rewrites dx otherwise.
 #include <algorithm>
 
 #include "pgb_common.cuh"
@@ -36,22 +39,42 @@ __device__ inline double block_sum_double(double v, double* s_red) {
   return t;
 }
 
+__device__ inline float l1l2_grad(float x, float t, float a, float b, float inv2n) {
+  const float d = x - t;
+  const float sg = d > 0.f ? 1.f : (d < 0.f ? -1.f : 0.f);
+  return sg * a + (inv2n * d) * b;
+}
+
+__device__ inline float4 l1l2_grad4(float4 x, float4 t, float a, float b, float inv2n) {
+  return make_float4(l1l2_grad(x.x, t.x, a, b, inv2n), l1l2_grad(x.y, t.y, a, b, inv2n),
+                     l1l2_grad(x.z, t.z, a, b, inv2n), l1l2_grad(x.w, t.w, a, b, inv2n));
+}
+
 // x and t 16-byte aligned: float4 body, scalar tail handled by block 0.
+// With GRAD, the same pass also writes dx = the backward for dL = 1 (the
+// backward kernel's expression with g = 1, so bit for bit its values).
+template <bool GRAD>
 __global__ void __launch_bounds__(kLossThreads) l1l2_partial_kernel(
-    const float* __restrict__ x, const float* __restrict__ t, int64_t n,
-    double* __restrict__ partial) {
+    const float* __restrict__ x, const float* __restrict__ t, int64_t n, float w,
+    double* __restrict__ partial, float* __restrict__ dx) {
   __shared__ double s_red[kLossThreads / 32];
   // per-thread sums in float over at most a few dozen float4 (four loads in
   // flight per iteration), then double across threads and blocks
   float f1 = 0.f, f2 = 0.f;
   const int64_t n4 = n / 4;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  const float nf = (float)n;
+  const float ga = 1.f / nf, gb = w, inv2n = 2.f / nf;  // l1l2_bwd_kernel's a, b at g = 1
   int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   for (; q + stride < n4; q += 2 * stride) {
     const float4 xa = reinterpret_cast<const float4*>(x)[q];
     const float4 ta = reinterpret_cast<const float4*>(t)[q];
     const float4 xb = reinterpret_cast<const float4*>(x)[q + stride];
     const float4 tb = reinterpret_cast<const float4*>(t)[q + stride];
+    if constexpr (GRAD) {
+      reinterpret_cast<float4*>(dx)[q] = l1l2_grad4(xa, ta, ga, gb, inv2n);
+      reinterpret_cast<float4*>(dx)[q + stride] = l1l2_grad4(xb, tb, ga, gb, inv2n);
+    }
     const float d[8] = {xa.x - ta.x, xa.y - ta.y, xa.z - ta.z, xa.w - ta.w,
                         xb.x - tb.x, xb.y - tb.y, xb.z - tb.z, xb.w - tb.w};
 #pragma unroll
@@ -63,6 +86,7 @@ __global__ void __launch_bounds__(kLossThreads) l1l2_partial_kernel(
   if (q < n4) {
     const float4 xv = reinterpret_cast<const float4*>(x)[q];
     const float4 tv = reinterpret_cast<const float4*>(t)[q];
+    if constexpr (GRAD) reinterpret_cast<float4*>(dx)[q] = l1l2_grad4(xv, tv, ga, gb, inv2n);
     const float d[4] = {xv.x - tv.x, xv.y - tv.y, xv.z - tv.z, xv.w - tv.w};
 #pragma unroll
     for (int c = 0; c < 4; ++c) {
@@ -76,6 +100,7 @@ __global__ void __launch_bounds__(kLossThreads) l1l2_partial_kernel(
       const float d = x[i] - t[i];
       a1 += fabsf(d);
       a2 += d * d;
+      if constexpr (GRAD) dx[i] = l1l2_grad(x[i], t[i], ga, gb, inv2n);
     }
   const double b1 = block_sum_double(a1, s_red);
   const double b2 = block_sum_double(a2, s_red);
@@ -97,16 +122,14 @@ __global__ void __launch_bounds__(2 * kFinishTPC) l1l2_finish_kernel(
   }
 }
 
-__device__ inline float l1l2_grad(float x, float t, float a, float b, float inv2n) {
-  const float d = x - t;
-  const float sg = d > 0.f ? 1.f : (d < 0.f ? -1.f : 0.f);
-  return sg * a + (inv2n * d) * b;
-}
-
+// UNIT: dx already holds the backward for dL = 1 (l1l2_partial_kernel<true>);
+// it is left as it is when dL is 1 and rewritten otherwise.
+template <bool UNIT>
 __global__ void __launch_bounds__(kLossThreads) l1l2_bwd_kernel(
     const float* __restrict__ x, const float* __restrict__ t, int64_t n, float w,
     const float* __restrict__ d_loss, float* __restrict__ dx) {
   const float g = d_loss[0];
+  if (UNIT && g == 1.f) return;
   const float nf = (float)n;
   const float a = g / nf;        // dL / n (the mean's backward)
   const float b = w * g;         // the weighted L2 term's incoming gradient
@@ -116,9 +139,7 @@ __global__ void __launch_bounds__(kLossThreads) l1l2_bwd_kernel(
        q += (int64_t)gridDim.x * blockDim.x) {
     const float4 xv = reinterpret_cast<const float4*>(x)[q];
     const float4 tv = reinterpret_cast<const float4*>(t)[q];
-    reinterpret_cast<float4*>(dx)[q] =
-        make_float4(l1l2_grad(xv.x, tv.x, a, b, inv2n), l1l2_grad(xv.y, tv.y, a, b, inv2n),
-                    l1l2_grad(xv.z, tv.z, a, b, inv2n), l1l2_grad(xv.w, tv.w, a, b, inv2n));
+    reinterpret_cast<float4*>(dx)[q] = l1l2_grad4(xv, tv, a, b, inv2n);
   }
   if (blockIdx.x == 0)
     for (int64_t i = 4 * n4 + threadIdx.x; i < n; i += blockDim.x)
@@ -141,7 +162,20 @@ int pgb_l1_l2_loss_forward(const float* x, const float* target, int64_t n, float
   const int grid = loss_grid(n);
   if (scratch_doubles < 2 * grid || !aligned16(x) || !aligned16(target)) return PGB_ERR_INVALID;
   cudaStream_t s = as_stream(stream);
-  l1l2_partial_kernel<<<grid, kLossThreads, 0, s>>>(x, target, n, scratch);
+  l1l2_partial_kernel<false><<<grid, kLossThreads, 0, s>>>(x, target, n, w, scratch, nullptr);
+  l1l2_finish_kernel<<<1, 2 * kFinishTPC, 0, s>>>(scratch, grid, n, w, loss);
+  return launch_status();
+}
+
+int pgb_l1_l2_loss_forward_grad(const float* x, const float* target, int64_t n, float w,
+                                double* scratch, int64_t scratch_doubles, float* loss,
+                                float* d_x_unit, void* stream) {
+  if (n <= 0 || !x || !target || !loss || !scratch || !d_x_unit) return PGB_ERR_INVALID;
+  const int grid = loss_grid(n);
+  if (scratch_doubles < 2 * grid || !aligned16(x) || !aligned16(target) || !aligned16(d_x_unit))
+    return PGB_ERR_INVALID;
+  cudaStream_t s = as_stream(stream);
+  l1l2_partial_kernel<true><<<grid, kLossThreads, 0, s>>>(x, target, n, w, scratch, d_x_unit);
   l1l2_finish_kernel<<<1, 2 * kFinishTPC, 0, s>>>(scratch, grid, n, w, loss);
   return launch_status();
 }
@@ -150,8 +184,17 @@ int pgb_l1_l2_loss_backward(const float* x, const float* target, int64_t n, floa
                             const float* d_loss, float* d_x, void* stream) {
   if (n <= 0 || !x || !target || !d_loss || !d_x) return PGB_ERR_INVALID;
   if (!aligned16(x) || !aligned16(target) || !aligned16(d_x)) return PGB_ERR_INVALID;
-  l1l2_bwd_kernel<<<loss_grid(n), kLossThreads, 0, as_stream(stream)>>>(x, target, n, w, d_loss,
-                                                                         d_x);
+  l1l2_bwd_kernel<false><<<loss_grid(n), kLossThreads, 0, as_stream(stream)>>>(x, target, n, w,
+                                                                                d_loss, d_x);
+  return launch_status();
+}
+
+int pgb_l1_l2_loss_backward_unit(const float* x, const float* target, int64_t n, float w,
+                                 const float* d_loss, float* d_x, void* stream) {
+  if (n <= 0 || !x || !target || !d_loss || !d_x) return PGB_ERR_INVALID;
+  if (!aligned16(x) || !aligned16(target) || !aligned16(d_x)) return PGB_ERR_INVALID;
+  l1l2_bwd_kernel<true><<<loss_grid(n), kLossThreads, 0, as_stream(stream)>>>(x, target, n, w,
+                                                                               d_loss, d_x);
   return launch_status();
 }
 

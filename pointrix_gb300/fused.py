@@ -214,6 +214,13 @@ def sh_rgb_views(shs, position, centres, active=None):
 
 # ---------------------------------------------------------------------------
 class _L1L2(torch.autograd.Function):
+    """When x needs a gradient, the forward also writes the gradient for an
+    upstream 1 in the same pass over x and t (a training step's loss is its
+    output, so that is the gradient it gets); the first backward hands that
+    buffer over and only rewrites it if the upstream gradient is not 1 (a
+    check on the device, so the step stays capturable).  A second backward
+    through a retained graph recomputes from x and t."""
+
     @staticmethod
     def forward(ctx, x, t, w):
         n = x.numel()
@@ -221,9 +228,15 @@ class _L1L2(torch.autograd.Function):
         nd = _lib.lib().pgb_l1_l2_loss_scratch_doubles(n)
         scratch = torch.empty(nd, dtype=torch.float64, device=dev)
         loss = torch.empty((), dtype=torch.float32, device=dev)
+        ctx.dx_unit = None
         with _timed("l1_l2_loss_fwd", dev, 2):
-            call("pgb_l1_l2_loss_forward", _ptr(x), _ptr(t), n, w, _ptr(scratch), nd, _ptr(loss),
-                 _stream(dev))
+            if ctx.needs_input_grad[0]:
+                ctx.dx_unit = torch.empty_like(x)
+                call("pgb_l1_l2_loss_forward_grad", _ptr(x), _ptr(t), n, w, _ptr(scratch), nd,
+                     _ptr(loss), _ptr(ctx.dx_unit), _stream(dev))
+            else:
+                call("pgb_l1_l2_loss_forward", _ptr(x), _ptr(t), n, w, _ptr(scratch), nd,
+                     _ptr(loss), _stream(dev))
         ctx.save_for_backward(x, t)
         ctx.w = w
         return loss
@@ -232,10 +245,15 @@ class _L1L2(torch.autograd.Function):
     def backward(ctx, d_loss):
         x, t = ctx.saved_tensors
         dev = x.device
-        dx = torch.empty_like(x)
+        dx, ctx.dx_unit = ctx.dx_unit, None
         with _timed("l1_l2_loss_bwd", dev, 1):
-            call("pgb_l1_l2_loss_backward", _ptr(x), _ptr(t), x.numel(), ctx.w,
-                 _ptr(_c(d_loss.reshape(1))), _ptr(dx), _stream(dev))
+            if dx is not None:
+                call("pgb_l1_l2_loss_backward_unit", _ptr(x), _ptr(t), x.numel(), ctx.w,
+                     _ptr(_c(d_loss.reshape(1))), _ptr(dx), _stream(dev))
+            else:
+                dx = torch.empty_like(x)
+                call("pgb_l1_l2_loss_backward", _ptr(x), _ptr(t), x.numel(), ctx.w,
+                     _ptr(_c(d_loss.reshape(1))), _ptr(dx), _stream(dev))
         return dx, None, None
 
 

@@ -120,6 +120,39 @@ def test_l1_l2_loss_matches_torch():
     assert rel(y.grad, y2.grad) < 1e-6
 
 
+def test_l1_l2_loss_gradient_from_the_forward_pass():
+    """The gradient the forward writes for an upstream 1, and the backward's
+    rewrite for any other upstream gradient, equal the plain backward
+    (pgb_l1_l2_loss_backward) bit for bit; a retained graph's second
+    backward recomputes it.  Odd length: the scalar tail too."""
+    from pointrix_gb300 import _lib
+    g = torch.Generator().manual_seed(9)
+    x = torch.rand(7, 53, 81, generator=g).to(DEV)
+    t = torch.rand(7, 53, 81, generator=g).to(DEV)
+    t.view(-1)[:500] = x.view(-1)[:500]                # zero differences: sign 0
+    stream = torch.cuda.current_stream().cuda_stream
+
+    def plain(dl):
+        dx = torch.empty_like(x)
+        d = torch.tensor([dl], dtype=torch.float32, device=DEV)
+        _lib.call("pgb_l1_l2_loss_backward", x.data_ptr(), t.data_ptr(), x.numel(), 0.2,
+                  d.data_ptr(), dx.data_ptr(), stream)
+        return dx
+
+    for dl in (1.0, 2.5, -0.75):
+        xr = x.clone().requires_grad_(True)
+        loss = fused.l1_l2_loss(xr, t, 0.2)
+        (dl * loss).backward(retain_graph=True)
+        assert torch.equal(xr.grad, plain(dl)), dl
+        xr.grad = None
+        (dl * loss).backward()
+        assert torch.equal(xr.grad, plain(dl)), dl
+    # no gradient wanted: the plain forward, the same loss
+    with torch.no_grad():
+        l0 = fused.l1_l2_loss(x, t, 0.2)
+    assert float(l0) == float(fused.l1_l2_loss(x.clone().requires_grad_(True), t, 0.2).detach())
+
+
 def test_capturable_adam_matches_host_steps():
     g = torch.Generator().manual_seed(2)
     ps = [torch.randn(1000, 3, generator=g).to(DEV) for _ in range(3)]
