@@ -695,10 +695,16 @@ def serve_measure(device, rates=(50, 100, 200, 500, 1000, 2000), duration=10.0):
     from pointrix_gb300 import serve
 
     scenes = serve.serving_scenes(device=device)
-    for cls in (serve.PlainServer, serve.RenderServer):   # warm-up of both paths
+    # warm-up of both paths: a burst (the large batches of the high rates)
+    # and two seconds of paced arrivals (the one- to three-view jobs of the
+    # low rates), so no measured rate is the first to run a code path
+    for cls in (serve.PlainServer, serve.RenderServer):
         srv = cls(scenes)
         for r in serve.random_requests(64, len(scenes), seed=99):
             srv.submit(r)
+        srv.close()
+        srv = cls(scenes, on_done=_drop_image)
+        serve.drive(srv, serve.random_requests(200, len(scenes), seed=98, rate=100))
         srv.close()
     out = []
     for rate in rates:
