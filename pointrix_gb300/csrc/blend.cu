@@ -1160,11 +1160,14 @@ __global__ void __launch_bounds__(32, MINB) blend_bwd_solo_kernel(
   static_assert(NC <= 8, "the d_out planes hold eight channels");
   constexpr int PX = 4, BW = 8, RS = 4, BH = 16;
   constexpr int NP = (NC + 1) / 2;
+  // 32-record batches: each splat's sums go straight to its gradient record
+  // (the tile form's scheme); 64: a shared table flushed once per batch
+  constexpr bool DIRECT = B == 32;
   extern __shared__ __align__(128) float smem[];
-  __shared__ uint8_t s_touched[B];
+  __shared__ uint8_t s_touched[DIRECT ? 1 : B];
   __shared__ uint8_t s_list[B];
   __shared__ __align__(16) float4 s_dout[2][PX * 32];  // [plane][q * 32 + lane]
-  float* gacc = smem + 2 * B * RF;                     // [B][GR]
+  float* gacc = smem + 2 * B * RF;                     // [B][GR] (not DIRECT)
 
   const int tile = blockIdx.x >> 1;
   int W, H, gx, ltile;
@@ -1174,8 +1177,10 @@ __global__ void __launch_bounds__(32, MINB) blend_bwd_solo_kernel(
   const int bx0 = (ltile % gx) * kTile + BW * (blockIdx.x & 1);
   const int by0 = (ltile / gx) * kTile;
 
-  for (int i = lane; i < B * GR; i += 32) gacc[i] = 0.f;
-  for (int i = lane; i < B; i += 32) s_touched[i] = 0;
+  if constexpr (!DIRECT) {
+    for (int i = lane; i < B * GR; i += 32) gacc[i] = 0.f;
+    for (int i = lane; i < B; i += 32) s_touched[i] = 0;
+  }
 
   const int64_t plane = (int64_t)W * H;
   const int pxi = bx0 + (lane & (BW - 1));
@@ -1221,14 +1226,24 @@ __global__ void __launch_bounds__(32, MINB) blend_bwd_solo_kernel(
   auto hi_of = [&](int b) { return max_nc - b * B; };
   __syncwarp();
 
-  if (nb > 0)
-    stage_batch<RF, 32, B>(records, ids, start + lo_of(0), start + hi_of(0), n, smem, info);
+  int32_t g_cur = -1, g_nxt = -1;  // DIRECT: the splat id of slot `lane`
+  if (nb > 0) {
+    if constexpr (DIRECT)
+      g_nxt = stage_batch_id<RF>(records, ids, start + lo_of(0), start + hi_of(0), n, smem, info);
+    else
+      stage_batch<RF, 32, B>(records, ids, start + lo_of(0), start + hi_of(0), n, smem, info);
+  }
   for (int b = 0; b < nb; ++b) {
     const int buf = b & 1;
     const int lo = lo_of(b), hi = hi_of(b);
+    g_cur = g_nxt;
     if (b + 1 < nb) {
-      stage_batch<RF, 32, B>(records, ids, start + lo_of(b + 1), start + hi_of(b + 1), n,
-                             smem + (buf ^ 1) * B * RF, info);
+      if constexpr (DIRECT)
+        g_nxt = stage_batch_id<RF>(records, ids, start + lo_of(b + 1), start + hi_of(b + 1), n,
+                                   smem + (buf ^ 1) * B * RF, info);
+      else
+        stage_batch<RF, 32, B>(records, ids, start + lo_of(b + 1), start + hi_of(b + 1), n,
+                               smem + (buf ^ 1) * B * RF, info);
       cp_async_wait<1>();
     } else {
       cp_async_wait<0>();
@@ -1301,25 +1316,33 @@ __global__ void __launch_bounds__(32, MINB) blend_bwd_solo_kernel(
       }
       const float sum = warp_reduce_scatter<16>(vf);
       // lanes 2k and 2k + 1 both hold component k; the even one owns it
-      if ((lane & 1) == 0 && (lane >> 1) < 6 + NC) gacc[slot * GR + (lane >> 1)] += sum;
-      if (lane == 0) s_touched[slot] = 1;
+      if constexpr (DIRECT) {
+        const int32_t g = __shfl_sync(0xffffffffu, g_cur, slot);
+        if (g >= 0 && (lane & 1) == 0 && (lane >> 1) < 6 + NC)
+          atomicAdd(grad_records + (int64_t)g * GR + (lane >> 1), sum);
+      } else {
+        if ((lane & 1) == 0 && (lane >> 1) < 6 + NC) gacc[slot * GR + (lane >> 1)] += sum;
+        if (lane == 0) s_touched[slot] = 1;
+      }
     }
-    __syncwarp();
-    for (int t = lane; t < hi - lo; t += 32) {
-      if (!s_touched[t]) continue;
-      const int32_t g = ids[start + lo + t];
-      if (g < 0 || (int64_t)g >= n) {
-        set_info(info, PGB_ERR_OVERFLOW);
-        continue;
-      }
-      float4* dst = reinterpret_cast<float4*>(grad_records + (int64_t)g * GR);
-      float4* srcv = reinterpret_cast<float4*>(gacc + t * GR);
+    if constexpr (!DIRECT) {
+      __syncwarp();
+      for (int t = lane; t < hi - lo; t += 32) {
+        if (!s_touched[t]) continue;
+        const int32_t g = ids[start + lo + t];
+        if (g < 0 || (int64_t)g >= n) {
+          set_info(info, PGB_ERR_OVERFLOW);
+          continue;
+        }
+        float4* dst = reinterpret_cast<float4*>(grad_records + (int64_t)g * GR);
+        float4* srcv = reinterpret_cast<float4*>(gacc + t * GR);
 #pragma unroll
-      for (int q = 0; q < (6 + NC + 3) / 4; ++q) {
-        atomicAdd(dst + q, srcv[q]);
-        srcv[q] = make_float4(0.f, 0.f, 0.f, 0.f);
+        for (int q = 0; q < (6 + NC + 3) / 4; ++q) {
+          atomicAdd(dst + q, srcv[q]);
+          srcv[q] = make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+        s_touched[t] = 0;
       }
-      s_touched[t] = 0;
     }
     __syncwarp();  // the stage of batch b is refilled by the next iteration's copies
   }
@@ -1684,7 +1707,7 @@ static int launch_bwd_solo(const float* records, const int32_t* ids, const int2*
                            int64_t* info, cudaStream_t s) {
   constexpr int RF = rec_floats(NC);
   constexpr int GR = grad_floats(NC);
-  const size_t smem = (2 * RF + GR) * B * sizeof(float);
+  const size_t smem = (2 * RF + (B == 32 ? 0 : GR)) * B * sizeof(float);  // no table at 32
   auto kern = blend_bwd_solo_kernel<NC, RF, GR, B, MINB>;
   if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
           cudaSuccess ||
