@@ -409,6 +409,36 @@ int pgb_sort_gaussian_finish_band(const float* uv, const int32_t* radius,
                                   int row0, int row1, int64_t k, void* scratch_n, size_t bytes_n,
                                   void* scratch_k, size_t bytes_k, int64_t* info, int32_t* ids_out,
                                   int32_t* tile_range_out, void* stream);
+/* Band lists: the band path above visits all n Gaussians in every band's
+ * phase two.  These calls build, once per image, each band's list of the
+ * Gaussians with at least one entry in it, in the depth order that
+ * pgb_sort_gaussian_begin left in scratch_n (bytes_n for n), so that each
+ * band's phase two visits only its own Gaussians:
+ * pgb_band_lists_count: rows (device int32 [nbands + 1], increasing tile
+ * rows; nbands <= 256), scratch of pgb_band_lists_scratch_bytes(n, nbands)
+ * bytes; writes offsets (device int64 [nbands + 1]): band b's list is
+ * lists[offsets[b] .. offsets[b + 1]).  The caller reads offsets[nbands]
+ * (the total) back to size lists.
+ * pgb_band_lists_write: the same arguments after the count, writes lists
+ * (device int32 [offsets[nbands]], Gaussian ids).
+ * pgb_sort_gaussian_finish_band_list: phase two for band rows [row0, row1)
+ * with K = k over that band's list (list [n_list]); clears what phase two
+ * counts in (no pgb_sort_gaussian_rebegin or pgb_band_tiles needed).  ids
+ * and tile_range equal pgb_sort_gaussian_finish_band's bit for bit. */
+size_t pgb_band_lists_scratch_bytes(int64_t n, int nbands);
+int pgb_band_lists_count(const float* uv, const int32_t* radius, int64_t n, int width, int height,
+                         const int32_t* rows, int nbands, const void* scratch_n, size_t bytes_n,
+                         void* scratch, size_t scratch_bytes, int64_t* offsets, void* stream);
+int pgb_band_lists_write(const float* uv, const int32_t* radius, int64_t n, int width, int height,
+                         const int32_t* rows, int nbands, const void* scratch_n, size_t bytes_n,
+                         const void* scratch, size_t scratch_bytes, const int64_t* offsets,
+                         int32_t* lists, void* stream);
+int pgb_sort_gaussian_finish_band_list(const float* uv, const int32_t* radius, int64_t n,
+                                       int width, int height, int row0, int row1, int64_t k,
+                                       const int32_t* list, int64_t n_list, void* scratch_n,
+                                       size_t bytes_n, void* scratch_k, size_t bytes_k,
+                                       int64_t* info, int32_t* ids_out, int32_t* tile_range_out,
+                                       void* stream);
 int pgb_alpha_blending_forward_band(const float* uv, const float* conic, const float* opacity,
                                     const float* feature, int64_t n, int channels,
                                     const int32_t* ids, int64_t k, const int32_t* tile_range,

@@ -71,6 +71,11 @@ SIGNATURES = {
     "pgb_sort_gaussian_rebegin": [vp, vp, i64, vp, szt, vp, vp],
     "pgb_sort_gaussian_finish_band": [vp, vp, vp, i64, i32, i32, i32, i32, i64, vp, szt, vp, szt,
                                       vp, vp, vp, vp],
+    "pgb_band_lists_scratch_bytes": [i64, i32],
+    "pgb_band_lists_count": [vp, vp, i64, i32, i32, vp, i32, vp, szt, vp, szt, vp, vp],
+    "pgb_band_lists_write": [vp, vp, i64, i32, i32, vp, i32, vp, szt, vp, szt, vp, vp, vp],
+    "pgb_sort_gaussian_finish_band_list": [vp, vp, i64, i32, i32, i32, i32, i64, vp, i64, vp, szt,
+                                           vp, szt, vp, vp, vp, vp],
     "pgb_alpha_blending_forward_band": [vp, vp, vp, vp, i64, i32, vp, i64, vp, f32, i32, i32, i32,
                                         i32, i32, vp, vp, vp, vp, vp, vp, i32],
     "pgb_alpha_blending_backward_band": [vp, i64, i32, vp, i64, vp, f32, i32, i32, i32, i32, vp,
@@ -118,7 +123,7 @@ SIGNATURES.update({
 })
 
 _RESTYPES = {"pgb_status_string": C.c_char_p, "pgb_camera_grad_scratch_bytes": szt,
-             "pgb_camera_grad_views_scratch_bytes": szt,
+             "pgb_camera_grad_views_scratch_bytes": szt, "pgb_band_lists_scratch_bytes": szt,
              "pgb_ssim_scratch_doubles": i64}
 
 

@@ -773,10 +773,15 @@ __device__ inline void hist_run(uint32_t a, uint32_t len, int passes, int bits, 
   }
 }
 
+// With `list` (a band's Gaussian list, one image), element i is Gaussian
+// list[i] and its entry count is its band-clipped rectangle; otherwise
+// element g is Gaussian g with tiles[g] entries (checked against its
+// rectangle).
 __global__ void __launch_bounds__(kStreamThreads) rect_kernel(
     const float* __restrict__ uv, const int32_t* __restrict__ radius,
     const int32_t* __restrict__ tiles, int64_t n, ViewTable vt, int tile_passes, int digit_bits,
-    uint4* __restrict__ rect, uint32_t* __restrict__ tile_hist, int64_t* __restrict__ info) {
+    uint4* __restrict__ rect, uint32_t* __restrict__ tile_hist, int64_t* __restrict__ info,
+    const uint32_t* __restrict__ list) {
   constexpr int NW = kStreamThreads / 32;
   __shared__ int s_diff[513];
   __shared__ uint32_t s_hist[kTileHistWords];
@@ -792,10 +797,11 @@ __global__ void __launch_bounds__(kStreamThreads) rect_kernel(
   __syncthreads();
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t base = (int64_t)blockIdx.x * blockDim.x + warp * 32; base < n; base += stride) {
-    const int64_t g = base + lane;
+    const int64_t i = base + lane;
     uint4 out = make_uint4(0u, 0u, 0u, 0u);
     uint32_t runs = 0;
-    if (g < n) {
+    if (i < n) {
+      const int64_t g = list ? (int64_t)list[i] : i;
       const int r = radius[g];
       if (r > 0) {
         const float2 p = reinterpret_cast<const float2*>(uv)[g];
@@ -812,9 +818,14 @@ __global__ void __launch_bounds__(kStreamThreads) rect_kernel(
           y0 -= vt.band0;
           y1 -= vt.band0;
         }
-        const uint32_t cnt = (uint32_t)max(tiles[g], 0);
         const uint32_t w = (uint32_t)(x1 - x0);
-        if ((int64_t)w * (y1 - y0) != (int64_t)cnt) set_error(info, PGB_ERR_MISMATCH);
+        uint32_t cnt;
+        if (list) {
+          cnt = w * (uint32_t)(y1 - y0);
+        } else {
+          cnt = (uint32_t)max(tiles[g], 0);
+          if ((int64_t)w * (y1 - y0) != (int64_t)cnt) set_error(info, PGB_ERR_MISMATCH);
+        }
         // tile ids local to the element's view: a batch is sorted by local
         // tile over a view-major emission (the last pass adds the bases)
         (void)tile_base;
@@ -1169,6 +1180,162 @@ __global__ void __launch_bounds__(kStreamThreads) band_counts_kernel(
     if (s_cnt[i]) atomicAdd(&counts[i], s_cnt[i]);
 }
 
+// ---------------------------------------------------------------------------
+// Band lists: for bands of tile rows [rows[b], rows[b + 1]), the Gaussians
+// with at least one entry in band b, in the depth order of phase one, so
+// that a band's rectangle and scan passes visit only its own Gaussians.
+// Three kernels over the depth order: per-block counts per band, a scan of
+// each band's block counts (and the bands' offsets), and a stable write
+// (warp ballots per band, warps in order within the block).
+// ---------------------------------------------------------------------------
+constexpr int kListThreads = 256;
+constexpr int kListChunk = kListThreads * 16;  // depth positions per block
+constexpr int kMaxListBands = 256;
+
+inline int list_blocks(int64_t n) { return (int)((n + kListChunk - 1) / kListChunk); }
+
+// Bands [b0, b1] whose rows meet Gaussian g's tile rectangle (b1 < b0:
+// none): the bands where its band-clipped entry count is positive.
+__device__ inline void element_bands(const float* __restrict__ uv,
+                                     const int32_t* __restrict__ radius, uint32_t g, int gx,
+                                     int gy, const int* s_rows, int nbands, int& b0, int& b1) {
+  b0 = INT_MAX;
+  b1 = -1;
+  const int r = radius[g];
+  if (r <= 0) return;
+  const float2 p = reinterpret_cast<const float2*>(uv)[g];
+  int x0, x1, y0, y1;
+  tile_rect(p.x, p.y, (float)r, gx, gy, x0, x1, y0, y1);
+  if (x1 <= x0 || y1 <= y0) return;
+  int lo = 0, hi = nbands;  // the first band ending after row y0
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if (s_rows[mid + 1] > y0) hi = mid; else lo = mid + 1;
+  }
+  const int first = lo;
+  hi = nbands;  // the first band starting at or after row y1
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if (s_rows[mid] >= y1) hi = mid; else lo = mid + 1;
+  }
+  if (lo - 1 >= first) {
+    b0 = first;
+    b1 = lo - 1;
+  }
+}
+
+__global__ void __launch_bounds__(kListThreads) band_list_count_kernel(
+    const uint32_t* __restrict__ order, const float* __restrict__ uv,
+    const int32_t* __restrict__ radius, int64_t n, int gx, int gy,
+    const int32_t* __restrict__ rows, int nbands, uint32_t* __restrict__ block_counts) {
+  __shared__ int s_rows[kMaxListBands + 1];
+  __shared__ uint32_t s_cnt[kMaxListBands];
+  for (int i = threadIdx.x; i <= nbands; i += kListThreads) s_rows[i] = rows[i];
+  for (int i = threadIdx.x; i < nbands; i += kListThreads) s_cnt[i] = 0u;
+  __syncthreads();
+  const int64_t base = (int64_t)blockIdx.x * kListChunk;
+  for (int j = threadIdx.x; j < kListChunk; j += kListThreads) {
+    const int64_t e = base + j;
+    if (e >= n) break;
+    int b0, b1;
+    element_bands(uv, radius, order[e], gx, gy, s_rows, nbands, b0, b1);
+    for (int b = b0; b <= b1; ++b) atomicAdd(&s_cnt[b], 1u);
+  }
+  __syncthreads();
+  for (int b = threadIdx.x; b < nbands; b += kListThreads)
+    block_counts[(size_t)b * gridDim.x + blockIdx.x] = s_cnt[b];
+}
+
+// One CTA per band: exclusive scan of the band's block counts in place; the
+// band's total to offsets[b + 1].
+__global__ void __launch_bounds__(kListThreads) band_list_scan_kernel(
+    uint32_t* __restrict__ block_counts, int nblocks, int64_t* __restrict__ offsets) {
+  __shared__ uint32_t s_warp_tot[kListThreads / 32];
+  uint32_t* row = block_counts + (size_t)blockIdx.x * nblocks;
+  uint32_t carry = 0;
+  for (int base = 0; base < nblocks; base += kListThreads) {
+    const int i = base + threadIdx.x;
+    const uint32_t v = i < nblocks ? row[i] : 0u;
+    uint32_t total;
+    const uint32_t ex = block_excl_scan<kListThreads>(v, total, s_warp_tot);
+    if (i < nblocks) row[i] = carry + ex;
+    carry += total;
+  }
+  if (threadIdx.x == 0) offsets[blockIdx.x + 1] = (int64_t)carry;
+}
+
+// offsets[0] = 0, offsets[b + 1] = the end of band b's list.
+__global__ void band_list_offsets_kernel(int64_t* __restrict__ offsets, int nbands) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    int64_t run = 0;
+    offsets[0] = 0;
+    for (int b = 0; b < nbands; ++b) {
+      run += offsets[b + 1];
+      offsets[b + 1] = run;
+    }
+  }
+}
+
+__global__ void __launch_bounds__(kListThreads) band_list_write_kernel(
+    const uint32_t* __restrict__ order, const float* __restrict__ uv,
+    const int32_t* __restrict__ radius, int64_t n, int gx, int gy,
+    const int32_t* __restrict__ rows, int nbands, const uint32_t* __restrict__ block_base,
+    const int64_t* __restrict__ offsets, uint32_t* __restrict__ lists) {
+  constexpr int NW = kListThreads / 32;
+  constexpr int PER_WARP = kListChunk / NW;  // consecutive depth positions per warp
+  __shared__ int s_rows[kMaxListBands + 1];
+  __shared__ uint32_t s_wcnt[NW][kMaxListBands];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const uint32_t lt = lanemask_lt();
+  for (int i = threadIdx.x; i <= nbands; i += kListThreads) s_rows[i] = rows[i];
+  for (int i = threadIdx.x; i < NW * kMaxListBands; i += kListThreads) (&s_wcnt[0][0])[i] = 0u;
+  __syncthreads();
+  const int64_t wbase = (int64_t)blockIdx.x * kListChunk + warp * PER_WARP;
+  // per-warp counts per band
+  for (int it = 0; it < PER_WARP / 32; ++it) {
+    const int64_t e = wbase + it * 32 + lane;
+    int b0 = INT_MAX, b1 = -1;
+    if (e < n) element_bands(uv, radius, order[e], gx, gy, s_rows, nbands, b0, b1);
+    const int lo = __reduce_min_sync(0xffffffffu, b0), hi = __reduce_max_sync(0xffffffffu, b1);
+    for (int b = lo; b <= hi; ++b) {
+      const uint32_t m = __ballot_sync(0xffffffffu, b >= b0 && b <= b1);
+      if (lane == 0) s_wcnt[warp][b] += __popc(m);
+    }
+  }
+  __syncthreads();
+  // block-local exclusive prefix per band across the warps, in warp order
+  for (int b = threadIdx.x; b < nbands; b += kListThreads) {
+    uint32_t run = 0;
+    for (int w = 0; w < NW; ++w) {
+      const uint32_t c = s_wcnt[w][b];
+      s_wcnt[w][b] = run;
+      run += c;
+    }
+  }
+  __syncthreads();
+  // stable writes: a warp's lanes in lane order, its iterations in order
+  for (int it = 0; it < PER_WARP / 32; ++it) {
+    const int64_t e = wbase + it * 32 + lane;
+    int b0 = INT_MAX, b1 = -1;
+    uint32_t g = 0;
+    if (e < n) {
+      g = order[e];
+      element_bands(uv, radius, g, gx, gy, s_rows, nbands, b0, b1);
+    }
+    const int lo = __reduce_min_sync(0xffffffffu, b0), hi = __reduce_max_sync(0xffffffffu, b1);
+    for (int b = lo; b <= hi; ++b) {
+      const bool mine = b >= b0 && b <= b1;
+      const uint32_t m = __ballot_sync(0xffffffffu, mine);
+      if (mine)
+        lists[offsets[b] + (int64_t)block_base[(size_t)b * gridDim.x + blockIdx.x] +
+              s_wcnt[warp][b] + __popc(m & lt)] = g;
+      __syncwarp();
+      if (lane == 0) s_wcnt[warp][b] += __popc(m);
+      __syncwarp();
+    }
+  }
+}
+
 // Entries of each element of a batch of views for 16 x th tiles (the
 // tiles_touched the views' sort then takes): its view's tile rectangle,
 // 0 for radius <= 0.
@@ -1311,18 +1478,22 @@ int pgb_sort_gaussian_begin_views(const float* depth, const int32_t* radius,
 // Phase two for one image or a batch of views (vt), over T global tiles.
 // K is the host value k, or (device_k) the count the depth phase left in
 // info[0], with every K-sized buffer sized for the capacity k.
+// With `list` (n_list entries), the passes run over that band list of
+// Gaussians (in depth order) instead of all n in the depth order.
 static int sort_finish_impl(const float* uv, const int32_t* radius, const int32_t* tiles_touched,
                             int64_t n, const ViewTable& vt, uint32_t T, int64_t k, bool device_k,
                             void* scratch_n, size_t bytes_n, void* scratch_k, size_t bytes_k,
                             int64_t* info, int32_t* ids_out, int32_t* tile_range_out,
-                            void* stream) {
+                            void* stream, const uint32_t* list = nullptr, int64_t n_list = 0) {
   if (n < 0 || k < 0 || !info || !tile_range_out) return PGB_ERR_INVALID;
+  if (list && (n_list < 0 || n_list > n)) return PGB_ERR_INVALID;
   // uv is read as float2 and the ranges written as int2: 8-byte starts
   if (misaligned(uv, 8) || misaligned(tile_range_out, 8) || misaligned(info, 8))
     return PGB_ERR_INVALID;
-  if (n > 0 && (!uv || !radius || !tiles_touched)) return PGB_ERR_INVALID;
+  if (n > 0 && (!uv || !radius || (!tiles_touched && !list))) return PGB_ERR_INVALID;
   if (k >= (int64_t)kValMask) return PGB_ERR_OVERFLOW;
   const ScratchN LN = layout_n(n);
+  const int64_t n_work = list ? n_list : n;  // elements the rectangle and scan passes visit
   // a batch sorts local tile ids: the plan is that of the largest view
   uint32_t T_local = T;
   if (vt.nviews > 0) {
@@ -1338,7 +1509,7 @@ static int sort_finish_impl(const float* uv, const int32_t* radius, const int32_
     return PGB_ERR_INVALID;
   if (T == 0 || T > (1u << (8 * kMaxTilePasses))) return PGB_ERR_INVALID;
   cudaStream_t s = as_stream(stream);
-  if (k == 0 || n == 0) {
+  if (k == 0 || n_work == 0) {
     // nothing can be emitted (a device count above 0 overflows the capacity)
     if (cudaMemsetAsync(tile_range_out, 0, (size_t)T * 2 * sizeof(int32_t), s) != cudaSuccess)
       return PGB_ERR_CUDA;
@@ -1352,8 +1523,9 @@ static int sort_finish_impl(const float* uv, const int32_t* radius, const int32_
   const int64_t* k_dev = device_k ? info : nullptr;
   uint32_t* counters = at<uint32_t>(scratch_n, LN.counters);
   uint32_t* thist = at<uint32_t>(scratch_n, LN.tile_hist);
-  // the depth order (view-major for a batch: begin_views ends in v1)
-  const uint32_t* order = at<uint32_t>(scratch_n, vt.nviews > 0 ? LN.dv1 : LN.dv0);
+  // the depth order (view-major for a batch: begin_views ends in v1), or
+  // the band's list of it
+  const uint32_t* order = list ? list : at<uint32_t>(scratch_n, vt.nviews > 0 ? LN.dv1 : LN.dv0);
   uint32_t* bufk[2] = {at<uint32_t>(scratch_k, LK.tk0), at<uint32_t>(scratch_k, LK.tk1)};
   uint32_t* bufv[2] = {at<uint32_t>(scratch_k, LK.tv0), at<uint32_t>(scratch_k, LK.tv1)};
   uint32_t* status = at<uint32_t>(scratch_k, LK.status);
@@ -1361,15 +1533,16 @@ static int sort_finish_impl(const float* uv, const int32_t* radius, const int32_
   uint4* rect = at<uint4>(scratch_n, LN.rect);
   uint32_t* chunk_first = at<uint32_t>(scratch_k, LK.chunk_first);
   int2* range = reinterpret_cast<int2*>(tile_range_out);
-  rect_kernel<<<stream_grid(n), kStreamThreads, 0, s>>>(
-      uv, radius, tiles_touched, n, vt, plan.passes, plan.bits, rect, thist, info);
-  scan_rect_kernel<<<LN.scan_parts, kSortThreads, 0, s>>>(
-      order, n, rect, k, k_dev, at<uint32_t>(scratch_n, LN.scan_status), counters + 4, owner,
+  rect_kernel<<<stream_grid(n_work), kStreamThreads, 0, s>>>(
+      uv, radius, tiles_touched, n_work, vt, plan.passes, plan.bits, rect, thist, info, list);
+  const int scan_parts = (int)((n_work + kScanPart - 1) / kScanPart);
+  scan_rect_kernel<<<scan_parts, kSortThreads, 0, s>>>(
+      order, n_work, rect, k, k_dev, at<uint32_t>(scratch_n, LN.scan_status), counters + 4, owner,
       chunk_first, range, T, counters + kViewsMark, (uint32_t)vt.nviews, info);
   GenSource src;
   src.owner = owner;
   src.chunk_first = chunk_first;
-  src.n_sorted = n;
+  src.n_sorted = n_work;
   PassViews px{};
   if (vt.nviews > 0) {
     px.vdiv = fast_div((uint32_t)vt.n_per_view);
@@ -1510,6 +1683,93 @@ int pgb_band_counts(const float* uv, const int32_t* radius, int64_t n, int width
   band_counts_kernel<<<stream_grid(n), kStreamThreads, 0, s>>>(
       uv, radius, n, grid_x(width), grid_y(height), bands, nbands, counts);
   return launch_status();
+}
+
+size_t pgb_band_lists_scratch_bytes(int64_t n, int nbands) {
+  if (n < 0 || nbands < 1 || nbands > kMaxListBands) return 0;
+  return align256((size_t)nbands * (size_t)std::max(1, list_blocks(n)) * sizeof(uint32_t));
+}
+
+static int band_lists_check(const float* uv, const int32_t* radius, int64_t n, int width,
+                            int height, const int32_t* rows, int nbands, const void* scratch_n,
+                            size_t bytes_n, const void* scratch, size_t scratch_bytes,
+                            const int64_t* offsets) {
+  if (n < 0 || width <= 0 || height <= 0 || nbands < 1 || nbands > kMaxListBands || !rows ||
+      !offsets || misaligned(offsets, 8))
+    return PGB_ERR_INVALID;
+  if (n > 0 && (!uv || !radius || !scratch_n || !scratch || misaligned(uv, 8) ||
+                misaligned(scratch_n, 16)))
+    return PGB_ERR_INVALID;
+  if (n > 0 && (bytes_n < layout_n(n).total ||
+                scratch_bytes < pgb_band_lists_scratch_bytes(n, nbands)))
+    return PGB_ERR_INVALID;
+  return PGB_OK;
+}
+
+int pgb_band_lists_count(const float* uv, const int32_t* radius, int64_t n, int width, int height,
+                         const int32_t* rows, int nbands, const void* scratch_n, size_t bytes_n,
+                         void* scratch, size_t scratch_bytes, int64_t* offsets, void* stream) {
+  const int rc = band_lists_check(uv, radius, n, width, height, rows, nbands, scratch_n, bytes_n,
+                                  scratch, scratch_bytes, offsets);
+  if (rc != PGB_OK) return rc;
+  cudaStream_t s = as_stream(stream);
+  if (n == 0)
+    return cudaMemsetAsync(offsets, 0, (size_t)(nbands + 1) * sizeof(int64_t), s) == cudaSuccess
+               ? PGB_OK
+               : PGB_ERR_CUDA;
+  const int nblocks = list_blocks(n);
+  uint32_t* counts = static_cast<uint32_t*>(scratch);
+  const uint32_t* order = at<uint32_t>(const_cast<void*>(scratch_n), layout_n(n).dv0);
+  band_list_count_kernel<<<nblocks, kListThreads, 0, s>>>(order, uv, radius, n, grid_x(width),
+                                                          grid_y(height), rows, nbands, counts);
+  band_list_scan_kernel<<<nbands, kListThreads, 0, s>>>(counts, nblocks, offsets);
+  band_list_offsets_kernel<<<1, 32, 0, s>>>(offsets, nbands);
+  return launch_status();
+}
+
+int pgb_band_lists_write(const float* uv, const int32_t* radius, int64_t n, int width, int height,
+                         const int32_t* rows, int nbands, const void* scratch_n, size_t bytes_n,
+                         const void* scratch, size_t scratch_bytes, const int64_t* offsets,
+                         int32_t* lists, void* stream) {
+  const int rc = band_lists_check(uv, radius, n, width, height, rows, nbands, scratch_n, bytes_n,
+                                  scratch, scratch_bytes, offsets);
+  if (rc != PGB_OK) return rc;
+  if (n == 0) return PGB_OK;
+  if (!lists) return PGB_ERR_INVALID;
+  const uint32_t* order = at<uint32_t>(const_cast<void*>(scratch_n), layout_n(n).dv0);
+  band_list_write_kernel<<<list_blocks(n), kListThreads, 0, as_stream(stream)>>>(
+      order, uv, radius, n, grid_x(width), grid_y(height), rows, nbands,
+      static_cast<const uint32_t*>(scratch), offsets, reinterpret_cast<uint32_t*>(lists));
+  return launch_status();
+}
+
+int pgb_sort_gaussian_finish_band_list(const float* uv, const int32_t* radius, int64_t n,
+                                       int width, int height, int row0, int row1, int64_t k,
+                                       const int32_t* list, int64_t n_list, void* scratch_n,
+                                       size_t bytes_n, void* scratch_k, size_t bytes_k,
+                                       int64_t* info, int32_t* ids_out, int32_t* tile_range_out,
+                                       void* stream) {
+  ViewTable vt;
+  if (!band_view(width, height, row0, row1, vt)) return PGB_ERR_INVALID;
+  if (n < 0 || n_list < 0 || n_list > n || !info || misaligned(info, 8)) return PGB_ERR_INVALID;
+  if (n_list > 0 && !list) return PGB_ERR_INVALID;
+  const ScratchN L = layout_n(n);
+  if (!scratch_n || bytes_n < L.total || misaligned(scratch_n, 16)) return PGB_ERR_INVALID;
+  cudaStream_t s = as_stream(stream);
+  // the depth order stays; phase two's counters, tile histograms and scan
+  // status start again from zero (as pgb_sort_gaussian_rebegin)
+  if (cudaMemsetAsync(info, 0, 2 * sizeof(int64_t), s) != cudaSuccess ||
+      cudaMemsetAsync(at<char>(scratch_n, L.counters), 0, L.depth_hist - L.counters, s) !=
+          cudaSuccess ||
+      cudaMemsetAsync(at<char>(scratch_n, L.tile_hist), 0, L.depth_status - L.tile_hist, s) !=
+          cudaSuccess ||
+      cudaMemsetAsync(at<char>(scratch_n, L.scan_status), 0, L.zero_bytes - L.scan_status, s) !=
+          cudaSuccess)
+    return PGB_ERR_CUDA;
+  const uint32_t T = (uint32_t)grid_x(width) * (uint32_t)(row1 - row0);
+  return sort_finish_impl(uv, radius, nullptr, n, vt, T, k, false, scratch_n, bytes_n, scratch_k,
+                          bytes_k, info, ids_out, tile_range_out, stream,
+                          reinterpret_cast<const uint32_t*>(list), n_list);
 }
 
 int pgb_tile_counts_views(const float* uv, const int32_t* radius, int64_t n_per_view,

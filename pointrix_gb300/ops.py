@@ -750,6 +750,9 @@ def group_rows(row_k, bands=None, max_entries: int = BAND_ENTRIES):
     return out
 
 
+# bands up to which a banded sort builds per-band Gaussian lists (the
+# library's limit for pgb_band_lists_*); more bands take the whole-order path
+BAND_LIST_MAX = 256
 # the band plan [(row0, row1, entries), ...] of the latest banded call (for
 # measurements)
 last_band_plan: list = []
@@ -772,14 +775,33 @@ class _BandSort:
         row_k = torch.empty(gy, dtype=torch.int64, device=dev)
         call("pgb_band_counts", _ptr(h.uv), _ptr(h.radius), n, h.W, h.H, _ptr(rows), gy,
              _ptr(row_k), h.stream.cuda_stream)
-        row_k = row_k.tolist()                      # the one synchronisation
+        row_k = row_k.tolist()                      # the first synchronisation
         self.K = int(sum(row_k))
         self.plan = group_rows(row_k, bands, max_entries)
         kmax = max(k for _, _, k in self.plan)
         _, self.bk = _sort_scratch(n, kmax, h.W, h.H)
         self.scratch_k = torch.empty(max(self.bk, 1), dtype=torch.uint8, device=dev)
         self.ids = torch.empty(max(kmax, 1), dtype=torch.int32, device=dev)
-        self.tiles_b = torch.empty_like(h.tiles)
+        self.lists = self.list_off = self.tiles_b = None
+        nb = len(self.plan)
+        if n and nb <= BAND_LIST_MAX:
+            # every band's Gaussians in depth order, so that a band's phase
+            # two visits only its own (one pass over the depth order, and the
+            # lists' total read back: the second synchronisation)
+            rows_b = torch.tensor([r0 for r0, _, _ in self.plan] + [self.plan[-1][1]],
+                                  dtype=torch.int32).to(dev)
+            sb = int(_lib.lib().pgb_band_lists_scratch_bytes(n, nb))
+            scratch = torch.empty(max(sb, 1), dtype=torch.uint8, device=dev)
+            offsets = torch.empty(nb + 1, dtype=torch.int64, device=dev)
+            s = h.stream.cuda_stream
+            args = (_ptr(h.uv), _ptr(h.radius), n, h.W, h.H, _ptr(rows_b), nb, _ptr(h.scratch_n),
+                    h.bn, _ptr(scratch), sb, _ptr(offsets))
+            call("pgb_band_lists_count", *args, s)
+            self.list_off = offsets.tolist()
+            self.lists = torch.empty(max(self.list_off[-1], 1), dtype=torch.int32, device=dev)
+            call("pgb_band_lists_write", *args, _ptr(self.lists), s)
+        else:
+            self.tiles_b = torch.empty_like(h.tiles)
 
     def band(self, i):
         """(ids [K_b] -- a view of the shared buffer --, tile_range
@@ -789,15 +811,26 @@ class _BandSort:
         dev, n, W, H = h.dev, h.n, h.W, h.H
         gx = (W + TILE - 1) // TILE
         s = h.stream.cuda_stream
-        call("pgb_band_tiles", _ptr(h.uv), _ptr(h.radius), n, W, H, r0, r1, _ptr(self.tiles_b), s)
-        call("pgb_sort_gaussian_rebegin", _ptr(h.radius), _ptr(self.tiles_b), n,
-             _ptr(h.scratch_n), h.bn, _ptr(h.info), s)
         ids = self.ids[:k]
         rng = torch.empty(gx * (r1 - r0), 2, dtype=torch.int32, device=dev)
-        with _timed("sort_finish", dev, (3 + _tile_passes(rng.shape[0])) if (k and n) else 0):
-            call("pgb_sort_gaussian_finish_band", _ptr(h.uv), _ptr(h.radius), _ptr(self.tiles_b),
-                 n, W, H, r0, r1, k, _ptr(h.scratch_n), h.bn, _ptr(self.scratch_k), self.bk,
-                 _ptr(h.info), _ptr(ids) if k else None, _ptr(rng), s)
+        launches = (3 + _tile_passes(rng.shape[0])) if (k and n) else 0
+        if self.lists is not None:
+            a, b = self.list_off[i], self.list_off[i + 1]
+            with _timed("sort_finish", dev, launches):
+                call("pgb_sort_gaussian_finish_band_list", _ptr(h.uv), _ptr(h.radius), n, W, H,
+                     r0, r1, k, self.lists.data_ptr() + 4 * a if b > a else None, b - a,
+                     _ptr(h.scratch_n), h.bn, _ptr(self.scratch_k), self.bk, _ptr(h.info),
+                     _ptr(ids) if k else None, _ptr(rng), s)
+        else:
+            call("pgb_band_tiles", _ptr(h.uv), _ptr(h.radius), n, W, H, r0, r1,
+                 _ptr(self.tiles_b), s)
+            call("pgb_sort_gaussian_rebegin", _ptr(h.radius), _ptr(self.tiles_b), n,
+                 _ptr(h.scratch_n), h.bn, _ptr(h.info), s)
+            with _timed("sort_finish", dev, launches):
+                call("pgb_sort_gaussian_finish_band", _ptr(h.uv), _ptr(h.radius),
+                     _ptr(self.tiles_b), n, W, H, r0, r1, k, _ptr(h.scratch_n), h.bn,
+                     _ptr(self.scratch_k), self.bk, _ptr(h.info), _ptr(ids) if k else None,
+                     _ptr(rng), s)
         _defer_check(h.info[1:], "sort_gaussian (band tile passes)")
         return ids, rng
 

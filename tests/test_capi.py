@@ -106,7 +106,8 @@ _SIZE_QUERIES = {"pgb_status_string", "pgb_abi_version", "pgb_camera_grad_scratc
                  "pgb_sh_rgb_scratch_floats", "pgb_sh_rgb_views_scratch_floats",
                  "pgb_l1_l2_loss_scratch_doubles", "pgb_ssim_scratch_doubles",
                  "pgb_sort_scratch_bytes", "pgb_blend_batches",
-                 "pgb_camera_grad_views_scratch_bytes", "pgb_blend_batches_h"}
+                 "pgb_camera_grad_views_scratch_bytes", "pgb_blend_batches_h",
+                 "pgb_band_lists_scratch_bytes"}
 
 
 def test_every_compute_entry_rejects_null_buffers():

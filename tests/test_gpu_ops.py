@@ -459,14 +459,32 @@ def test_blend_pair_census_counts_the_replayed_and_composited_pairs(small):
 
 
 @pytest.mark.parametrize("bands", [1, 2, 5, 16])
-def test_band_sort_lists_are_the_whole_image_lists(small, bands):
+@pytest.mark.parametrize("band_lists", [True, False])
+def test_band_sort_lists_are_the_whole_image_lists(small, bands, band_lists, monkeypatch):
     """Each band's (band-local) tile lists are the whole image's lists of
     the same tiles, bit for bit; the bands cover every tile row once and
-    their entry counts add up to K."""
+    their entry counts add up to K.  Both phase-two paths: over each band's
+    own Gaussian list, and over the whole depth order."""
     p = small
     gx, gy = O.tile_grid(p.W, p.H)
+    if not band_lists:
+        monkeypatch.setattr(ops, "BAND_LIST_MAX", 0)
     bs = ops._BandSort(p.uv, p.depth, p.W, p.H, p.radius, p.tiles, bands)
+    assert (bs.lists is not None) == band_lists
     assert bs.K == p.ids.numel()
+    if band_lists:
+        # band b's list: the Gaussians with an entry in its rows, in depth
+        # order (depth, then id), from the float32 oracle's tile rectangles
+        rad, uvc, dep = cpu(p.radius), cpu(p.uv), cpu(p.depth).reshape(-1)
+        n = rad.numel()
+        order = torch.tensor(sorted(range(n), key=lambda g: (float(dep[g]), g)))
+        x0, x1, y0, y1 = O.tile_rect(uvc[:, 0], uvc[:, 1], rad.to(torch.float32), p.W, p.H)
+        has = (rad > 0) & (x1 > x0)
+        for i, (r0, r1, _) in enumerate(bs.plan):
+            m = has & (torch.clamp(y1, max=r1) > torch.clamp(y0, min=r0))
+            want = order[m[order]].tolist()
+            got = cpu(bs.lists)[bs.list_off[i]:bs.list_off[i + 1]].tolist()
+            assert got == want, (i, len(got), len(want))
     ids, rng = cpu(p.ids), cpu(p.rng).long()
     plan = bs.plan
     assert plan[0][0] == 0 and plan[-1][1] == gy and len(plan) <= min(bands, gy)
