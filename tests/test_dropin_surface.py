@@ -158,6 +158,21 @@ def test_band_grouping_of_tile_rows():
     assert band_rows(100, 16 * 9, bands=3) == [(0, 3), (3, 6), (6, 9)]
 
 
+def test_band_list_scratch_and_limits():
+    """The band lists' scratch query (no GPU needed): one count per band and
+    block of 4,096 depth positions, 256-byte rounded; 0 for band counts
+    outside 1..256 (the banded sort then keeps its whole-order path)."""
+    from pointrix_gb300 import _lib
+    lib = _lib.lib()
+    q = lib.pgb_band_lists_scratch_bytes
+    assert ops.BAND_LIST_MAX == 256
+    assert q(0, 1) == 256 and q(4096, 1) == 256
+    assert q(4097, 13) == 256                      # 2 blocks x 13 bands x 4 B
+    assert q(6_000_000, 13) == -(-(13 * 1465 * 4) // 256) * 256
+    assert q(100, 0) == 0 and q(100, 257) == 0 and q(-1, 4) == 0
+    assert q(10_000_000, 256) >= 256 * ((10_000_000 + 4095) // 4096) * 4
+
+
 class _FakeEvent:
     def __init__(self, done):
         self.done = done
